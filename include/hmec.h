@@ -1,0 +1,247 @@
+/*
+ * hmec.h -- C ABI of libhmec_gpu.so, the GB300 (sm_103a) implementation of the
+ * per-timestep hot path of H-MEC (hydro-mechanical earthquake cycles, 2D).
+ *
+ * The reference program (cpp/h_mec_rsf_v9.cpp) has no functions on its hot
+ * path: every section is inline in main() and its state lives in globals.
+ * This header therefore defines the boundary section by section.  Each entry
+ * point below names the reference lines it replaces; a host loop that mirrors
+ * main() calls them in the same order (see driver/hmec_run.cpp).
+ *
+ * Conventions
+ *   - Node fields are Eigen column-major double arrays: element (i, j) of a
+ *     field with `rows` rows lives at [j * rows + i].  Basic-grid fields are
+ *     Ny x Nx, staggered fields are (Ny+1) x (Nx+1), exactly as the reference
+ *     declares them (cpp/h_mec_rsf_v9.cpp:54-89).  The pointer of an Eigen
+ *     MatrixXd (`M.data()`) can be passed directly.
+ *   - Host buffers are copied; the library never keeps a host pointer.
+ *   - Every entry point returns an int status (HMEC_OK == 0, negative on
+ *     error); no C++ exception crosses the ABI.  hmec_last_error() gives the
+ *     message of the last failure on a context.
+ *   - One host thread per context.  The context owns all device memory and
+ *     one CUDA stream on the device that was current at hmec_create().
+ */
+#ifndef HMEC_H
+#define HMEC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HMEC_ABI_VERSION 1
+
+/* ------------------------------------------------------------------ status */
+enum hmec_status {
+    HMEC_OK = 0,
+    HMEC_ERR_ARG = -1,           /* bad argument (null pointer, wrong size, unknown id) */
+    HMEC_ERR_CUDA = -2,          /* a CUDA runtime call failed */
+    HMEC_ERR_BOUNDS = -3,        /* a device-side index check failed */
+    HMEC_ERR_NAN = -4,           /* a non-finite value in the solution */
+    HMEC_ERR_RSF_NOCONV = -5,    /* the fault-stress bisection hit its iteration cap */
+    HMEC_ERR_KRYLOV_NOCONV = -6, /* FGMRES did not reach its tolerance within its cap */
+    HMEC_ERR_NOMEM = -7,         /* device allocation failed */
+    HMEC_ERR_STATE = -8          /* call out of order (e.g. iteration before timestep_begin) */
+};
+
+/* ------------------------------------------------------------ solver forms */
+enum hmec_form {
+    HMEC_FORM_FP64 = 0,  /* FP64 FGMRES, FP64 multigrid preconditioner */
+    HMEC_FORM_MIXED = 1  /* FP64 FGMRES, FP32 multigrid preconditioner  */
+};
+
+/*
+ * Runtime parameters.  hmec_params_default() fills the values of
+ * cpp/constants.hpp:13-146 (the reference compiles them in); derived
+ * quantities (dx, line_fault, block limits, ...) are computed from these by
+ * the library exactly as constants.hpp computes them.
+ */
+typedef struct hmec_params {
+    /* grid, constants.hpp:23-26 */
+    int32_t Nx, Ny;
+    double xsize, ysize;
+    /* markers per basic cell in x and y, constants.hpp:81-82 (4, 4) */
+    int32_t mx, my;
+    /* RSF transition abscissae, constants.hpp:29-33 */
+    double TS_1, TS_2, TS_3, TS_4;
+    /* time stepping, constants.hpp:71-74 */
+    double dtelastic0, dtmin, inertia;
+    /* RSF, constants.hpp:93-98: [0] block, [1] fault */
+    double arsfm[2], brsfm[2], lrsfm[2], omm[2];
+    double V0;
+    double alpha;
+    /* porosity / rheology, constants.hpp:101-111 */
+    double POR0, cohes, friction, dilatation, tensile, shearmod, BETAFLUID, BETASOLID;
+    /* body force / pressures, constants.hpp:115-118 */
+    double gx, gy, PCONF, PTFDIFF;
+    /* limits, constants.hpp:122-127 */
+    double etamin, etamax, kkkmin, kkkmax, stpmax, stpmax1;
+    /* boundary conditions, constants.hpp:130-132 */
+    double bcupper, bclower, bcvyflower;
+    /* iteration / timestep control, constants.hpp:135-146 */
+    int32_t niterglobal, ynlastmax, dtstep;
+    double vratiomax, dtkoef, dtkoefup, dtkoefv, errmin, etawt, syieldmin, tyield;
+    int32_t num_timesteps;
+
+    /* ---- extensions of this library (no counterpart in constants.hpp) ---- */
+    int32_t form;             /* enum hmec_form */
+    double krylov_rtol;       /* FGMRES tolerance on the row-equilibrated residual (1e-12) */
+    int32_t krylov_restart;   /* FGMRES restart length m */
+    int32_t krylov_maxit;     /* total FGMRES iteration cap per solve */
+    int32_t mg_levels;        /* max multigrid levels (1 = Vanka smoother only) */
+    int32_t mg_pre, mg_post;  /* Vanka sweeps before / after the coarse correction */
+    int32_t mg_coarse_sweeps; /* Vanka sweeps on the coarsest level */
+    int32_t rsf_maxit;        /* cap of the fault-stress bisection (reference: none) */
+    int32_t advect_markers;   /* 1: run marker advection (reference: loop never runs) */
+    int32_t rk4_as_written;   /* 1: reproduce the shifted RK stages of the reference */
+    int32_t quirk_accumulate_sums; /* oracle only: marker sums accumulate across steps */
+    int32_t bounds_check;     /* 1: device index checks set HMEC_ERR_BOUNDS */
+} hmec_params;
+
+/* ------------------------------------------------------------- node fields */
+/* X(name, grid): grid 0 = basic (Ny x Nx), 1 = staggered (Ny+1 x Nx+1).
+ * Names are the reference's (cpp/h_mec_rsf_v9.cpp:55-112).                 */
+#define HMEC_FIELD_LIST(X) \
+    X(OM0, 0) X(OM, 0) X(OM5, 0) X(ARSF, 0) X(BRSF, 0) X(LRSF, 0) \
+    X(RHO, 0) X(ETA, 0) X(ETA0, 0) X(ETA1, 0) X(ETA5, 0) X(ETA00, 0) X(ETA50, 0) \
+    X(IETAPLB, 0) X(SXY, 0) X(SXY0, 0) X(YNY0, 0) X(YNY, 0) X(KKK, 0) X(GGG, 0) \
+    X(COHC, 0) X(COHT, 0) X(FRIC, 0) X(FRIT, 0) X(DILC, 0) X(TTT, 0) X(EIIB, 0) \
+    X(VSLIPB, 0) X(SIIB, 0) X(ESP, 0) X(EXY, 0) X(DSY, 0) X(SigmaY, 0) X(SII_fault, 0) \
+    X(pt, 1) X(vxs, 1) X(vys, 1) X(pf, 1) X(vxD, 1) X(vyD, 1) \
+    X(ETAB, 1) X(ETAB0, 1) X(ETAP, 1) X(ETAP0, 1) X(POR, 1) X(GGGP, 1) X(GGGB, 1) \
+    X(PTF0, 1) X(PT0, 1) X(PF0, 1) X(SXX, 1) X(SXX0, 1) X(SYY, 1) X(SYY0, 1) \
+    X(EXX, 1) X(EYY, 1) X(DILP, 1) \
+    X(RHOX, 1) X(RHOFX, 1) X(ETADX, 1) X(PORX, 1) X(VX0, 1) X(VXF0, 1) \
+    X(RHOY, 1) X(RHOFY, 1) X(ETADY, 1) X(PORY, 1) X(VY0, 1) X(VYF0, 1) \
+    X(EII, 1) X(EIIVP, 1) X(SII, 1) X(DIS, 1) X(pt_ave, 1) X(pf_ave, 1) \
+    X(VIS_COMP, 1) X(EL_DECOM, 1)
+
+#define HMEC_X_ENUM(name, grid) HMEC_F_##name,
+enum hmec_field { HMEC_FIELD_LIST(HMEC_X_ENUM) HMEC_F_COUNT };
+#undef HMEC_X_ENUM
+
+/* ----------------------------------------------------------- marker arrays */
+/* The 19 per-marker arrays of cpp/constants.hpp:153-173 (VecXd, length marknum). */
+#define HMEC_MARKER_LIST(X) \
+    X(xm) X(ym) X(t_marker) X(rhom) X(etasm) X(etam) X(cohescm) X(cohestm) \
+    X(frictcm) X(dilatcm) X(fricttm) X(porm) X(kkkm) X(sxxm) X(syym) X(sxym) \
+    X(gm) X(rhofm) X(etafm)
+
+#define HMEC_X_MENUM(name) HMEC_M_##name,
+enum hmec_marker_field { HMEC_MARKER_LIST(HMEC_X_MENUM) HMEC_M_COUNT };
+#undef HMEC_X_MENUM
+
+/* ----------------------------------------------------------------- scalars */
+/* Scalars of cpp/h_mec_rsf_v9.cpp:99-105 and the 9 restart values of :1862,
+ * all exchanged as double.                                                  */
+#define HMEC_SCALAR_LIST(X) \
+    X(timesum) X(dt) X(dt00) X(dtx) X(dty) X(dtlapusta) X(Vmax) X(maxvxy) \
+    X(yndtdecrease) X(timestep) X(ynlast) X(iterstep) \
+    X(maxvxsmod) X(minvxsmod) X(maxvysmod) X(minvysmod)
+
+#define HMEC_X_SENUM(name) HMEC_S_##name,
+enum hmec_scalar { HMEC_SCALAR_LIST(HMEC_X_SENUM) HMEC_S_COUNT };
+#undef HMEC_X_SENUM
+
+/* ----------------------------------------------------------------- reports */
+typedef struct hmec_iter_report {
+    int32_t iterstep;      /* index of the global iteration just run */
+    int32_t stop;          /* 1 if the exit test of :1436 passed */
+    int32_t ynpl;          /* yielding fault nodes (:1277-1298) */
+    int32_t krylov_iters;  /* FGMRES iterations of this solve */
+    double dt;             /* dt after the adaptive-step logic of :1418-1427 */
+    double DSYLSQ;         /* :1311-1314 */
+    double ptscale, pfscale;
+    double Vmax;
+    double krylov_relres;  /* final row-equilibrated relative residual */
+} hmec_iter_report;
+
+typedef struct hmec_step_report {
+    int32_t timestep;        /* the step just completed */
+    int32_t global_iters;    /* iterstep + 1, as printed at :1736 */
+    int32_t ynlast;          /* ynlast + 1, as printed at :1737 */
+    int32_t krylov_iters;    /* FGMRES iterations summed over the step */
+    int32_t status;          /* first non-OK status seen in the step */
+    double timesum, dt, Vmax;
+    double max_krylov_relres;
+} hmec_step_report;
+
+typedef struct hmec_ctx hmec_ctx;
+
+/* ---------------------------------------------------------------- metadata */
+int32_t hmec_abi_version(void);
+/* Fill *p with the values of cpp/constants.hpp and the library defaults. */
+void hmec_params_default(hmec_params* p);
+const char* hmec_field_name(int32_t field);   /* NULL for an unknown id */
+int32_t hmec_field_grid(int32_t field);        /* 0 basic, 1 staggered, -1 unknown */
+const char* hmec_marker_name(int32_t field);
+const char* hmec_scalar_name(int32_t id);
+/* Marker count of the lattice: (Nx-1)*mx * (Ny-1)*my (constants.hpp:81-85). */
+int64_t hmec_marknum(const hmec_params* p);
+
+/* --------------------------------------------------------------- lifecycle */
+/* Replaces the global declarations of cpp/h_mec_rsf_v9.cpp:54-112 and
+ * constants.hpp:153-173: allocates every node field, marker array and solver
+ * buffer on the current device.  Fields start at zero.  *status receives the
+ * error code when NULL is returned.                                         */
+hmec_ctx* hmec_create(const hmec_params* p, int32_t* status);
+void hmec_destroy(hmec_ctx* ctx);
+const char* hmec_last_error(const hmec_ctx* ctx);
+
+/* ------------------------------------------------------------ data motion */
+/* Marker arrays: fields[k] points to the array of marker field k
+ * (enum hmec_marker_field order), each of length n == hmec_marknum().
+ * Replaces the initialisation of :188-209 (and the HDF5 reads of :245-251). */
+int32_t hmec_upload_markers(hmec_ctx* ctx, const double* const* fields, int64_t n);
+int32_t hmec_download_markers(hmec_ctx* ctx, double* const* fields, int64_t n);
+/* One node field; rows/cols must match the field's grid. */
+int32_t hmec_upload_field(hmec_ctx* ctx, int32_t field, const double* colmajor, int32_t rows, int32_t cols);
+int32_t hmec_download_field(hmec_ctx* ctx, int32_t field, double* colmajor, int32_t rows, int32_t cols);
+int32_t hmec_set_scalar(hmec_ctx* ctx, int32_t id, double value);
+int32_t hmec_get_scalar(hmec_ctx* ctx, int32_t id, double* value);
+
+/* ---------------------------------------------------------------- sections */
+/* a1-a4: marker properties, counting sort by cell, deterministic node
+ * reductions and normalisation.  Replaces :376-583.                         */
+int32_t hmec_markers_to_nodes(hmec_ctx* ctx);
+/* a5: viscosity reset, dt growth, iteration counters.  Replaces :585-608.   */
+int32_t hmec_timestep_begin(hmec_ctx* ctx);
+/* a6-a15: one global (plastic) iteration -- viscosity limits, assembly,
+ * FGMRES solve, reload, stress, fault RSF, error and adaptive dt, exit test
+ * and viscosity update.  Replaces one pass of the loop body :611-1456.
+ * report may be NULL.                                                        */
+int32_t hmec_global_iteration(hmec_ctx* ctx, hmec_iter_report* report);
+/* a16-a19: dt recheck, post-step stress and invariants, state rollover.
+ * Replaces :1463-1559 and :1658-1726 (advection excluded).                  */
+int32_t hmec_timestep_end(hmec_ctx* ctx);
+/* a18, a20: node-to-marker velocity/spin gather, RK4 advection, stress
+ * rotation, periodic recycling.  Replaces the (never executed) loop
+ * :1561-1656.                                                               */
+int32_t hmec_advect_markers(hmec_ctx* ctx);
+/* a1-a20 in order: one whole timestep, loop control on the device.
+ * Replaces the body of `for (; timestep <= num_timesteps; ...)` up to the
+ * output section (:377-1726).  report may be NULL.                          */
+int32_t hmec_timestep(hmec_ctx* ctx, hmec_step_report* report);
+
+/* --------------------------------------------------------- testing hooks */
+/* Assemble the global system of the current state (after the iteration
+ * preparation of :611-677) and return it as CSR with duplicates summed, the
+ * form Eigen's setFromTriplets produces at :1046-1049.  With indptr == NULL
+ * only *nnz is returned.  rhs receives R (length N).                        */
+int32_t hmec_assemble_csr(hmec_ctx* ctx, int64_t* indptr, int32_t* indices, double* data,
+                          double* rhs, int64_t* nnz, double* ptscale, double* pfscale);
+/* Solve the system assembled by the last hmec_assemble_csr / iteration with
+ * the configured solver for the given right-hand side; x holds the initial
+ * guess on entry and the solution on return.                                 */
+int32_t hmec_solve_system(hmec_ctx* ctx, const double* rhs, double* x, int32_t* iters, double* relres);
+/* Device-kernel launches issued since hmec_create. */
+int64_t hmec_kernel_launches(const hmec_ctx* ctx);
+/* Synchronise the context stream. */
+int32_t hmec_synchronize(hmec_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HMEC_H */
