@@ -1,0 +1,622 @@
+// hmec_api.cu -- the extern "C" boundary of libhmec_gpu.so (include/hmec.h).
+//
+// Lifecycle, host<->device transfers of Eigen column-major storage, and the
+// section entry points that a host loop mirroring cpp/h_mec_rsf_v9.cpp:main
+// calls in place of the inline sections.  No exception crosses the ABI;
+// every function returns an hmec status and records a message on the
+// context.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "hmec_internal.cuh"
+
+int hmec_cuda_fail(hmec_ctx* ctx, cudaError_t e, const char* what) {
+    if (ctx) {
+        char buf[512];
+        snprintf(buf, sizeof(buf), "CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
+        ctx->err = buf;
+    }
+    return HMEC_ERR_CUDA;
+}
+
+bool hmec_prof_begin(hmec_ctx* ctx, const char* kname, double bytes) {
+    ProfState& P = ctx->prof;
+    if (P.name.empty() || strncmp(kname, P.name.c_str(), P.name.size()) != 0) return false;
+    for (int k = 0; k < 2; k++) {
+        cudaEvent_t e;
+        if (P.pool.empty()) {
+            if (cudaEventCreate(&e) != cudaSuccess) return false;
+        } else {
+            e = P.pool.back();
+            P.pool.pop_back();
+        }
+        P.pending.push_back(e);
+    }
+    cudaEventRecord(P.pending[P.pending.size() - 2], ctx->stream);
+    P.launches++;
+    P.bytes += bytes;
+    return true;
+}
+
+void hmec_prof_end(hmec_ctx* ctx) { cudaEventRecord(ctx->prof.pending.back(), ctx->stream); }
+
+static void prof_drain(hmec_ctx* ctx) {
+    ProfState& P = ctx->prof;
+    if (P.pending.empty()) return;
+    cudaStreamSynchronize(ctx->stream);
+    for (size_t k = 0; k + 1 < P.pending.size(); k += 2) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, P.pending[k], P.pending[k + 1]) == cudaSuccess) P.ms += ms;
+        P.pool.push_back(P.pending[k]);
+        P.pool.push_back(P.pending[k + 1]);
+    }
+    P.pending.clear();
+}
+
+static int fail(hmec_ctx* ctx, int code, const char* msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+// Eigen 3.3 LinSpaced(n, low, high) for |high| >= |low| (every grid here).
+static void linspaced(std::vector<double>& out, int n, double low, double high) {
+    out.resize(n);
+    const double step = (n == 1) ? 0. : (high - low) / (double)(n - 1);
+    for (int i = 0; i < n; i++) out[i] = (i == n - 1) ? high : low + (double)i * step;
+}
+
+// Map device status bits to the ABI status.
+static int status_from_bits(int bits) {
+    if (bits & HMEC_DEV_BOUNDS) return HMEC_ERR_BOUNDS;
+    if (bits & HMEC_DEV_NAN) return HMEC_ERR_NAN;
+    if (bits & HMEC_DEV_RSF_NOCONV) return HMEC_ERR_RSF_NOCONV;
+    if (bits & HMEC_DEV_KRYLOV_NOCONV) return HMEC_ERR_KRYLOV_NOCONV;
+    return HMEC_OK;
+}
+
+static int pull_scalars(hmec_ctx* ctx) {
+    HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->hs, ctx->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream));
+    HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->prof.pending.size() > 4096) prof_drain(ctx);
+    return HMEC_OK;
+}
+
+extern "C" {
+
+int32_t hmec_abi_version(void) { return HMEC_ABI_VERSION; }
+
+void hmec_params_default(hmec_params* p) {
+    if (!p) return;
+    // cpp/constants.hpp:13-146
+    memset(p, 0, sizeof(*p));
+    p->Nx = 401;
+    p->Ny = 51;
+    p->xsize = 40000.;
+    p->ysize = 10000.;
+    p->mx = 4;
+    p->my = 4;
+    p->TS_1 = 2e3;
+    p->TS_2 = 4e3;
+    p->TS_3 = 34e3;
+    p->TS_4 = 38e3;
+    p->dtelastic0 = 5e8;
+    p->dtmin = 1e-4;
+    p->inertia = 1.;
+    p->arsfm[0] = .025;
+    p->arsfm[1] = .006;
+    p->brsfm[0] = .001;
+    p->brsfm[1] = .015;
+    p->lrsfm[0] = .020;
+    p->lrsfm[1] = .0085;
+    p->omm[0] = 10;
+    p->omm[1] = -10;
+    p->V0 = 1.e-9;
+    p->alpha = 29;
+    p->POR0 = .01;
+    p->cohes = 0.;
+    p->friction = .6;
+    p->dilatation = 0.;
+    p->tensile = 1.;
+    p->shearmod = 3.e10;
+    p->BETAFLUID = 1.e-8;
+    p->BETASOLID = 2.e-11;
+    p->gx = 0.;
+    p->gy = 0.;
+    p->PCONF = 1.e7;
+    p->PTFDIFF = 3.e7;
+    p->etamin = 1e-3;
+    p->etamax = 1e50;
+    p->kkkmin = 1e-22;
+    p->kkkmax = 1e-12;
+    p->stpmax = 2e-4;
+    p->stpmax1 = 6e-5;
+    p->bcupper = -1e-9;
+    p->bclower = 1e-9;
+    p->bcvyflower = 0;
+    p->niterglobal = 10000;
+    p->ynlastmax = 499;
+    p->dtstep = 5;
+    p->vratiomax = 0.001;
+    p->dtkoef = 1.1;
+    p->dtkoefup = 1.2;
+    p->dtkoefv = 1.001;
+    p->errmin = 1e2;
+    p->etawt = 0.0;
+    p->syieldmin = 1e-3;
+    p->tyield = 1;
+    p->num_timesteps = 100000;
+    // library extensions
+    p->form = HMEC_FORM_FP64;
+    p->krylov_rtol = 1e-12;
+    p->krylov_restart = 40;
+    p->krylov_maxit = 2000;
+    p->mg_levels = 6;
+    p->mg_pre = 2;
+    p->mg_post = 2;
+    p->mg_coarse_sweeps = 30;
+    p->rsf_maxit = 10000;
+    p->advect_markers = 0;
+    p->rk4_as_written = 0;
+    p->quirk_accumulate_sums = 0;
+    p->bounds_check = 0;
+}
+
+#define HMEC_X_NAME(name, grid) #name,
+#define HMEC_X_GRID(name, grid) grid,
+static const char* const kFieldNames[] = {HMEC_FIELD_LIST(HMEC_X_NAME)};
+static const int kFieldGrid[] = {HMEC_FIELD_LIST(HMEC_X_GRID)};
+#undef HMEC_X_NAME
+#undef HMEC_X_GRID
+#define HMEC_X_NAME1(name) #name,
+static const char* const kMarkerNames[] = {HMEC_MARKER_LIST(HMEC_X_NAME1)};
+static const char* const kScalarNames[] = {HMEC_SCALAR_LIST(HMEC_X_NAME1)};
+#undef HMEC_X_NAME1
+
+const char* hmec_field_name(int32_t f) { return (f >= 0 && f < HMEC_F_COUNT) ? kFieldNames[f] : nullptr; }
+int32_t hmec_field_grid(int32_t f) { return (f >= 0 && f < HMEC_F_COUNT) ? kFieldGrid[f] : -1; }
+const char* hmec_marker_name(int32_t f) { return (f >= 0 && f < HMEC_M_COUNT) ? kMarkerNames[f] : nullptr; }
+const char* hmec_scalar_name(int32_t s) { return (s >= 0 && s < HMEC_S_COUNT) ? kScalarNames[s] : nullptr; }
+
+int64_t hmec_marknum(const hmec_params* p) {
+    if (!p) return -1;
+    return (int64_t)(p->Nx - 1) * p->mx * (int64_t)(p->Ny - 1) * p->my;
+}
+
+const char* hmec_last_error(const hmec_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int64_t hmec_kernel_launches(const hmec_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+void hmec_destroy(hmec_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->dev);
+    cudaStreamSynchronize(ctx->stream);
+    for (cudaEvent_t e : ctx->prof.pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->prof.pending) cudaEventDestroy(e);
+    solver_free(ctx);
+    p2g_free(ctx);
+    for (int k = 0; k < 8; k++) cudaFree(ctx->crd[k]);
+    for (int k = 0; k < HMEC_M_COUNT; k++) cudaFree(ctx->mk[k]);
+    for (int k = 0; k < HMEC_F_COUNT; k++) cudaFree(ctx->f[k]);
+    cudaFree(ctx->R);
+    cudaFree(ctx->S);
+    cudaFree(ctx->red);
+    cudaFree(ctx->ds);
+    cudaFreeHost(ctx->hs);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+static int create_inner(hmec_ctx* ctx) {
+    const hmec_params& p = ctx->p;
+    if (p.Nx < 5 || p.Ny < 5 || p.mx < 1 || p.my < 1 || !(p.xsize > 0) || !(p.ysize > 0))
+        return fail(ctx, HMEC_ERR_ARG, "grid parameters out of range (Nx, Ny >= 5; mx, my >= 1; sizes > 0)");
+    if (p.krylov_restart < 2 || p.krylov_restart > 200) return fail(ctx, HMEC_ERR_ARG, "krylov_restart must be in [2, 200]");
+    if (p.form != HMEC_FORM_FP64 && p.form != HMEC_FORM_MIXED) return fail(ctx, HMEC_ERR_ARG, "unknown solver form");
+    HMEC_CUDA(ctx, cudaGetDevice(&ctx->dev));
+    HMEC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    Geo& g = ctx->g;
+    g.Nx = p.Nx;
+    g.Ny = p.Ny;
+    g.Nx1 = p.Nx + 1;
+    g.Ny1 = p.Ny + 1;
+    g.N = g.Nx1 * g.Ny1 * 6;
+    g.line_fault = (int)((p.Ny - 1) / 2.);  // constants.hpp:43
+    g.dx = p.xsize / (p.Nx - 1);
+    g.dy = p.ysize / (p.Ny - 1);
+    g.dx2 = g.dx * g.dx;
+    g.dy2 = g.dy * g.dy;
+    g.dx_dy = g.dx * g.dy;
+    g.lower_block = p.ysize / 2. + g.dy;  // constants.hpp:76-77
+    g.upper_block = p.ysize / 2. - g.dy;
+    g.dy_faultw = g.dy / g.dx;            // faultwidth = dx (:66, :175)
+    ctx->marknum = hmec_marknum(&p);
+    // coordinates, constants.hpp:57-64
+    std::vector<double> c[8];
+    const double dx = g.dx, dy = g.dy;
+    linspaced(c[0], p.Nx, 0, p.xsize);
+    linspaced(c[1], p.Ny, 0, p.ysize);
+    linspaced(c[2], p.Nx + 1, 0, p.xsize + dx);
+    linspaced(c[3], p.Ny + 1, 0 - dy / 2., p.ysize + dy / 2.);
+    linspaced(c[4], p.Nx + 1, 0 - dx / 2., p.xsize + dx / 2.);
+    linspaced(c[5], p.Ny + 1, 0, p.ysize + dy);
+    linspaced(c[6], p.Nx + 1, 0 - dx / 2., p.xsize + dx / 2.);
+    linspaced(c[7], p.Ny + 1, 0 - dy / 2., p.ysize + dy / 2.);
+    for (int k = 0; k < 8; k++) {
+        HMEC_CUDA(ctx, cudaMalloc(&ctx->crd[k], sizeof(double) * c[k].size()));
+        HMEC_CUDA(ctx, cudaMemcpy(ctx->crd[k], c[k].data(), sizeof(double) * c[k].size(), cudaMemcpyHostToDevice));
+    }
+    const size_t nb = (size_t)g.Nx * g.Ny, ns = (size_t)g.Nx1 * g.Ny1;
+    for (int k = 0; k < HMEC_F_COUNT; k++) {
+        const size_t n = hmec_field_grid(k) ? ns : nb;
+        HMEC_CUDA(ctx, cudaMalloc(&ctx->f[k], sizeof(double) * n));
+        HMEC_CUDA(ctx, cudaMemset(ctx->f[k], 0, sizeof(double) * n));
+    }
+    for (int k = 0; k < HMEC_M_COUNT; k++) {
+        HMEC_CUDA(ctx, cudaMalloc(&ctx->mk[k], sizeof(double) * (size_t)ctx->marknum));
+        HMEC_CUDA(ctx, cudaMemset(ctx->mk[k], 0, sizeof(double) * (size_t)ctx->marknum));
+    }
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->R, sizeof(double) * (size_t)g.N));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->S, sizeof(double) * (size_t)g.N));
+    HMEC_CUDA(ctx, cudaMemset(ctx->S, 0, sizeof(double) * (size_t)g.N));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->red, sizeof(double) * (4096 + 3 * (size_t)g.Nx + 64)));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->ds, sizeof(DevScalars)));
+    HMEC_CUDA(ctx, cudaMallocHost(&ctx->hs, sizeof(DevScalars)));
+    DevScalars s;
+    memset(&s, 0, sizeof(s));
+    s.dt = p.dtelastic0;  // h_mec_rsf_v9.cpp:101-103
+    s.yndtdecrease = 1;
+    s.timestep = 1;
+    HMEC_CUDA(ctx, cudaMemcpy(ctx->ds, &s, sizeof(s), cudaMemcpyHostToDevice));
+    *ctx->hs = s;
+    int rc = p2g_alloc(ctx);
+    if (rc) return rc;
+    rc = solver_alloc(ctx);
+    if (rc) return rc;
+    HMEC_CUDA(ctx, cudaDeviceSynchronize());
+    return HMEC_OK;
+}
+
+hmec_ctx* hmec_create(const hmec_params* p, int32_t* status) {
+    if (!p) {
+        if (status) *status = HMEC_ERR_ARG;
+        return nullptr;
+    }
+    hmec_ctx* ctx = new (std::nothrow) hmec_ctx();
+    if (!ctx) {
+        if (status) *status = HMEC_ERR_NOMEM;
+        return nullptr;
+    }
+    ctx->p = *p;
+    ctx->launches = 0;
+    ctx->in_step = 0;
+    int rc = create_inner(ctx);
+    if (rc != HMEC_OK) {
+        fprintf(stderr, "hmec_create: %s\n", ctx->err.c_str());
+        if (status) *status = rc;
+        if (ctx->stream) hmec_destroy(ctx);
+        else delete ctx;
+        return nullptr;
+    }
+    if (status) *status = HMEC_OK;
+    return ctx;
+}
+
+int32_t hmec_upload_markers(hmec_ctx* ctx, const double* const* fields, int64_t n) {
+    if (!ctx || !fields) return fail(ctx, HMEC_ERR_ARG, "null argument");
+    if (n != ctx->marknum) return fail(ctx, HMEC_ERR_ARG, "marker count differs from (Nx-1)*mx*(Ny-1)*my");
+    for (int k = 0; k < HMEC_M_COUNT; k++)
+        if (!fields[k]) return fail(ctx, HMEC_ERR_ARG, "null marker array");
+    for (int k = 0; k < HMEC_M_COUNT; k++)
+        HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->mk[k], fields[k], sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+    HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HMEC_OK;
+}
+
+int32_t hmec_download_markers(hmec_ctx* ctx, double* const* fields, int64_t n) {
+    if (!ctx || !fields) return fail(ctx, HMEC_ERR_ARG, "null argument");
+    if (n != ctx->marknum) return fail(ctx, HMEC_ERR_ARG, "marker count differs from (Nx-1)*mx*(Ny-1)*my");
+    for (int k = 0; k < HMEC_M_COUNT; k++)
+        if (fields[k])
+            HMEC_CUDA(ctx, cudaMemcpyAsync(fields[k], ctx->mk[k], sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+    HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HMEC_OK;
+}
+
+static int field_dims_ok(hmec_ctx* ctx, int32_t f, int32_t rows, int32_t cols) {
+    if (f < 0 || f >= HMEC_F_COUNT) return 0;
+    const int g = hmec_field_grid(f);
+    return rows == ctx->g.Ny + g && cols == ctx->g.Nx + g;
+}
+
+int32_t hmec_upload_field(hmec_ctx* ctx, int32_t f, const double* a, int32_t rows, int32_t cols) {
+    if (!ctx || !a) return fail(ctx, HMEC_ERR_ARG, "null argument");
+    if (!field_dims_ok(ctx, f, rows, cols)) return fail(ctx, HMEC_ERR_ARG, "unknown field or wrong dimensions");
+    HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->f[f], a, sizeof(double) * (size_t)rows * cols, cudaMemcpyHostToDevice, ctx->stream));
+    HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HMEC_OK;
+}
+
+int32_t hmec_download_field(hmec_ctx* ctx, int32_t f, double* a, int32_t rows, int32_t cols) {
+    if (!ctx || !a) return fail(ctx, HMEC_ERR_ARG, "null argument");
+    if (!field_dims_ok(ctx, f, rows, cols)) return fail(ctx, HMEC_ERR_ARG, "unknown field or wrong dimensions");
+    HMEC_CUDA(ctx, cudaMemcpyAsync(a, ctx->f[f], sizeof(double) * (size_t)rows * cols, cudaMemcpyDeviceToHost, ctx->stream));
+    HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HMEC_OK;
+}
+
+// Scalars: the host mirror is refreshed from the device, edited, pushed back.
+int32_t hmec_set_scalar(hmec_ctx* ctx, int32_t id, double v) {
+    if (!ctx) return HMEC_ERR_ARG;
+    if (id < 0 || id >= HMEC_S_COUNT) return fail(ctx, HMEC_ERR_ARG, "unknown scalar id");
+    int rc = pull_scalars(ctx);
+    if (rc) return rc;
+    DevScalars& s = *ctx->hs;
+    switch (id) {
+        case HMEC_S_timesum: s.timesum = v; break;
+        case HMEC_S_dt: s.dt = v; break;
+        case HMEC_S_dt00: s.dt00 = v; break;
+        case HMEC_S_dtx: s.dtx = v; break;
+        case HMEC_S_dty: s.dty = v; break;
+        case HMEC_S_dtlapusta: s.dtlapusta = v; break;
+        case HMEC_S_Vmax: s.Vmax = v; break;
+        case HMEC_S_maxvxy: s.maxvxy = v; break;
+        case HMEC_S_yndtdecrease: s.yndtdecrease = (int)v; break;
+        case HMEC_S_timestep: s.timestep = (int)v; break;
+        case HMEC_S_ynlast: s.ynlast = (int)v; break;
+        case HMEC_S_iterstep: s.iterstep = (int)v; break;
+        case HMEC_S_maxvxsmod: s.maxvxsmod = v; break;
+        case HMEC_S_minvxsmod: s.minvxsmod = v; break;
+        case HMEC_S_maxvysmod: s.maxvysmod = v; break;
+        case HMEC_S_minvysmod: s.minvysmod = v; break;
+    }
+    HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->ds, ctx->hs, sizeof(DevScalars), cudaMemcpyHostToDevice, ctx->stream));
+    HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HMEC_OK;
+}
+
+int32_t hmec_get_scalar(hmec_ctx* ctx, int32_t id, double* v) {
+    if (!ctx || !v) return fail(ctx, HMEC_ERR_ARG, "null argument");
+    if (id < 0 || id >= HMEC_S_COUNT) return fail(ctx, HMEC_ERR_ARG, "unknown scalar id");
+    int rc = pull_scalars(ctx);
+    if (rc) return rc;
+    const DevScalars& s = *ctx->hs;
+    switch (id) {
+        case HMEC_S_timesum: *v = s.timesum; break;
+        case HMEC_S_dt: *v = s.dt; break;
+        case HMEC_S_dt00: *v = s.dt00; break;
+        case HMEC_S_dtx: *v = s.dtx; break;
+        case HMEC_S_dty: *v = s.dty; break;
+        case HMEC_S_dtlapusta: *v = s.dtlapusta; break;
+        case HMEC_S_Vmax: *v = s.Vmax; break;
+        case HMEC_S_maxvxy: *v = s.maxvxy; break;
+        case HMEC_S_yndtdecrease: *v = s.yndtdecrease; break;
+        case HMEC_S_timestep: *v = s.timestep; break;
+        case HMEC_S_ynlast: *v = s.ynlast; break;
+        case HMEC_S_iterstep: *v = s.iterstep; break;
+        case HMEC_S_maxvxsmod: *v = s.maxvxsmod; break;
+        case HMEC_S_minvxsmod: *v = s.minvxsmod; break;
+        case HMEC_S_maxvysmod: *v = s.maxvysmod; break;
+        case HMEC_S_minvysmod: *v = s.minvysmod; break;
+    }
+    return HMEC_OK;
+}
+
+void* hmec_stream(hmec_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int32_t hmec_profile_kernel(hmec_ctx* ctx, const char* name) {
+    if (!ctx) return HMEC_ERR_ARG;
+    prof_drain(ctx);
+    ctx->prof.name = name ? name : "";
+    ctx->prof.launches = 0;
+    ctx->prof.ms = 0;
+    ctx->prof.bytes = 0;
+    return HMEC_OK;
+}
+
+int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, double* bytes) {
+    if (!ctx) return HMEC_ERR_ARG;
+    prof_drain(ctx);
+    if (launches) *launches = ctx->prof.launches;
+    if (total_ms) *total_ms = ctx->prof.ms;
+    if (bytes) *bytes = ctx->prof.bytes;
+    return HMEC_OK;
+}
+
+int32_t hmec_synchronize(hmec_ctx* ctx) {
+    if (!ctx) return HMEC_ERR_ARG;
+    HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HMEC_OK;
+}
+
+int32_t hmec_markers_to_nodes(hmec_ctx* ctx) {
+    if (!ctx) return HMEC_ERR_ARG;
+    // a new timestep starts here: clear the device status word of the last one
+    HMEC_CUDA(ctx, cudaMemsetAsync(&ctx->ds->status, 0, sizeof(int), ctx->stream));
+    int rc = p2g_run(ctx);
+    if (rc) return rc;
+    return HMEC_OK;
+}
+
+int32_t hmec_timestep_begin(hmec_ctx* ctx) {
+    if (!ctx) return HMEC_ERR_ARG;
+    int rc = step_begin(ctx);
+    if (rc) return rc;
+    ctx->in_step = 1;
+    return HMEC_OK;
+}
+
+static int iteration(hmec_ctx* ctx, hmec_iter_report* rep, int* krylov_rc) {
+    int rc = iter_prepare(ctx);
+    if (rc) return rc;
+    rc = iter_assemble(ctx);
+    if (rc) return rc;
+    rc = solver_setup(ctx);
+    if (rc) return rc;
+    int its = 0;
+    double rel = 0;
+    *krylov_rc = solver_solve(ctx, &its, &rel);
+    if (*krylov_rc != HMEC_OK && *krylov_rc != HMEC_ERR_KRYLOV_NOCONV) return *krylov_rc;
+    rc = iter_finish(ctx);
+    if (rc) return rc;
+    rc = pull_scalars(ctx);
+    if (rc) return rc;
+    const DevScalars& s = *ctx->hs;
+    if (rep) {
+        rep->iterstep = s.stop ? s.iterstep : s.iterstep - 1;
+        rep->stop = s.stop;
+        rep->ynpl = s.ynpl;
+        rep->krylov_iters = its;
+        rep->dt = s.dt;
+        rep->DSYLSQ = s.dsylsq;
+        rep->ptscale = s.ptscale;
+        rep->pfscale = s.pfscale;
+        rep->Vmax = s.Vmax;
+        rep->krylov_relres = rel;
+    }
+    return HMEC_OK;
+}
+
+int32_t hmec_global_iteration(hmec_ctx* ctx, hmec_iter_report* rep) {
+    if (!ctx) return HMEC_ERR_ARG;
+    if (!ctx->in_step) return fail(ctx, HMEC_ERR_STATE, "hmec_global_iteration before hmec_timestep_begin");
+    int krc = HMEC_OK;
+    int rc = iteration(ctx, rep, &krc);
+    if (rc) return rc;
+    const int bits = ctx->hs->status;
+    if (bits) return fail(ctx, status_from_bits(bits), "device status raised in the global iteration");
+    if (krc) return fail(ctx, krc, "FGMRES did not reach krylov_rtol within krylov_maxit");
+    return HMEC_OK;
+}
+
+int32_t hmec_timestep_end(hmec_ctx* ctx) {
+    if (!ctx) return HMEC_ERR_ARG;
+    int rc = step_end(ctx);
+    if (rc) return rc;
+    ctx->in_step = 0;
+    rc = pull_scalars(ctx);
+    if (rc) return rc;
+    return HMEC_OK;
+}
+
+int32_t hmec_advect_markers(hmec_ctx* ctx) {
+    if (!ctx) return HMEC_ERR_ARG;
+    return advect_run(ctx);
+}
+
+int32_t hmec_timestep(hmec_ctx* ctx, hmec_step_report* rep) {
+    if (!ctx) return HMEC_ERR_ARG;
+    int rc = hmec_markers_to_nodes(ctx);
+    if (rc) return rc;
+    rc = hmec_timestep_begin(ctx);
+    if (rc) return rc;
+    int first_bad = HMEC_OK;
+    int ktot = 0;
+    double kmax = 0;
+    for (;;) {
+        hmec_iter_report ir;
+        int krc = HMEC_OK;
+        rc = iteration(ctx, &ir, &krc);
+        if (rc) return rc;
+        ktot += ir.krylov_iters;
+        kmax = std::fmax(kmax, ir.krylov_relres);
+        if (krc && !first_bad) first_bad = krc;
+        if (ctx->hs->loop_done) break;
+        if (ctx->hs->status & HMEC_DEV_NAN) {  // a non-finite solution cannot recover
+            first_bad = HMEC_ERR_NAN;
+            break;
+        }
+    }
+    const int iters = ctx->hs->iters_in_step;
+    const int ynlast = ctx->hs->ynlast;
+    const int timestep = ctx->hs->timestep;
+    rc = hmec_timestep_end(ctx);
+    if (rc) return rc;
+    if (ctx->p.advect_markers) {
+        rc = advect_run(ctx);
+        if (rc) return rc;
+        rc = pull_scalars(ctx);
+        if (rc) return rc;
+    }
+    const int bits = ctx->hs->status;
+    if (bits && !first_bad) first_bad = status_from_bits(bits);
+    if (rep) {
+        rep->timestep = timestep;
+        rep->global_iters = iters;
+        rep->ynlast = ynlast + 1;
+        rep->krylov_iters = ktot;
+        rep->status = first_bad;
+        rep->timesum = ctx->hs->timesum;
+        rep->dt = ctx->hs->dt;
+        rep->Vmax = ctx->hs->Vmax;
+        rep->max_krylov_relres = kmax;
+    }
+    if (first_bad) return fail(ctx, first_bad, "timestep finished with a non-OK status (see report)");
+    return HMEC_OK;
+}
+
+int32_t hmec_assemble_csr(hmec_ctx* ctx, int64_t* indptr, int32_t* indices, double* data, double* rhs, int64_t* nnz,
+                          double* ptscale, double* pfscale) {
+    if (!ctx || !nnz) return fail(ctx, HMEC_ERR_ARG, "null argument");
+    int rc = iter_prepare(ctx);
+    if (rc) return rc;
+    rc = iter_assemble(ctx);
+    if (rc) return rc;
+    const Level& L = ctx->sv.lv[0];
+    const size_t N = (size_t)ctx->g.N;
+    std::vector<int32_t> col(HMEC_W * N);
+    std::vector<double> val(HMEC_W * N), ds(N);
+    HMEC_CUDA(ctx, cudaMemcpyAsync(col.data(), L.col, sizeof(int32_t) * col.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    HMEC_CUDA(ctx, cudaMemcpyAsync(val.data(), L.val, sizeof(double) * val.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    HMEC_CUDA(ctx, cudaMemcpyAsync(ds.data(), L.dscale, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->stream));
+    if (rhs) HMEC_CUDA(ctx, cudaMemcpyAsync(rhs, ctx->R, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->stream));
+    rc = pull_scalars(ctx);
+    if (rc) return rc;
+    if (ptscale) *ptscale = ctx->hs->ptscale;
+    if (pfscale) *pfscale = ctx->hs->pfscale;
+    // ELL -> CSR: drop the padding slots (column == row with value 0 after the real entries)
+    int64_t k = 0;
+    for (size_t r = 0; r < N; r++) {
+        if (indptr) indptr[r] = k;
+        for (int s = 0; s < HMEC_W; s++) {
+            const size_t o = (size_t)s * N + r;
+            const bool pad = (s > 0 && col[o] == (int32_t)r && val[o] == 0.0 && col[o - N] >= (int32_t)r);
+            if (pad) continue;
+            if (indptr) {
+                indices[k] = col[o];
+                data[k] = val[o] / ds[r];  // power-of-two scale: exact
+            }
+            k++;
+        }
+    }
+    if (indptr) indptr[N] = k;
+    *nnz = k;
+    return HMEC_OK;
+}
+
+int32_t hmec_solve_system(hmec_ctx* ctx, const double* rhs, double* x, int32_t* iters, double* relres) {
+    if (!ctx || !rhs || !x) return fail(ctx, HMEC_ERR_ARG, "null argument");
+    const size_t N = (size_t)ctx->g.N;
+    Level& L = ctx->sv.lv[0];
+    std::vector<double> ds(N), bs(N);
+    HMEC_CUDA(ctx, cudaMemcpy(ds.data(), L.dscale, sizeof(double) * N, cudaMemcpyDeviceToHost));
+    for (size_t r = 0; r < N; r++) bs[r] = rhs[r] * ds[r];
+    HMEC_CUDA(ctx, cudaMemcpy(L.db, bs.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+    HMEC_CUDA(ctx, cudaMemcpy(ctx->S, x, sizeof(double) * N, cudaMemcpyHostToDevice));
+    int rc = solver_setup(ctx);
+    if (rc) return rc;
+    int its = 0;
+    double rel = 0;
+    int krc = solver_solve(ctx, &its, &rel);
+    HMEC_CUDA(ctx, cudaMemcpy(x, ctx->S, sizeof(double) * N, cudaMemcpyDeviceToHost));
+    if (iters) *iters = its;
+    if (relres) *relres = rel;
+    if (krc) return fail(ctx, krc, "FGMRES did not reach krylov_rtol within krylov_maxit");
+    return HMEC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,189 @@
+// hmec_internal.cuh -- device-side data layout and helpers shared by the
+// translation units of libhmec_gpu.so (GB300, sm_103a).
+//
+// HBM layout: every node field is its own FP64 column-major array with the
+// reference's shape (basic Ny x Nx, staggered (Ny+1) x (Nx+1)), so uploads
+// and downloads are plain copies of Eigen storage.  Kernels map the row index
+// i to threadIdx.x, which makes a warp read 32 consecutive doubles of one
+// grid column.  Scalars of the global-iteration control live in one
+// DevScalars block in device memory and are only touched by single-thread
+// control kernels, so the whole loop runs without host round trips.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/hmec.h"
+
+#define HMEC_W 11  // ELL width: the longest assembled row (x/y-Stokes) has 11 entries
+
+// Status bits raised by device code (device word -> host status).
+enum {
+    HMEC_DEV_BOUNDS = 1,
+    HMEC_DEV_NAN = 2,
+    HMEC_DEV_RSF_NOCONV = 4,
+    HMEC_DEV_KRYLOV_NOCONV = 8,
+};
+
+// Grid geometry of one level (the fine level is the model grid).
+struct Geo {
+    int Nx, Ny, Nx1, Ny1, N, line_fault;
+    double dx, dy, dx2, dy2, dx_dy, lower_block, upper_block, dy_faultw;
+};
+
+// Control scalars of one model instance (device resident).
+struct DevScalars {
+    double timesum, dt, dt00, dtx, dty, dtlapusta, Vmax, maxvxy, maxvxy0;
+    double ptscale, pfscale;
+    double dsylsq, dsylsq_prev;
+    double maxvxsmod, minvxsmod, maxvysmod, minvysmod;
+    double krylov_relres, krylov_maxrel;
+    int yndtdecrease, timestep, ynlast, iterstep;
+    int ynpl, stop, loop_done, status;
+    int krylov_iters, krylov_total, iters_in_step, pad0;
+};
+
+// Pointers to the node fields read by the assembly of one level.
+struct AsmFields {
+    const double *ETA, *GGG, *RHO, *SXY0;                            // basic
+    const double *ETAP, *GGGP, *ETAB, *POR, *GGGB, *SXX0, *SYY0;     // P
+    const double *RHOX, *RHOFX, *PORX, *ETADX, *VX0, *VXF0;          // Vx
+    const double *RHOY, *RHOFY, *PORY, *ETADY, *VY0, *VYF0;          // Vy
+    const double *PT0, *PF0, *DILP;                                  // P (rhs)
+};
+
+// One multigrid level of the preconditioner.
+struct Level {
+    Geo g;
+    int npatch;            // interior P cells: (Ny-1)*(Nx-1)
+    int nbnd;              // rows not covered by any Vanka patch
+    int32_t* col;          // ELL columns, slot-major [HMEC_W][N]
+    double* val;           // row-scaled matrix values (FP64), slot-major
+    float* val32;          // FP32 copy (mixed form)
+    double* dscale;        // row scale (power of two) applied to the matrix
+    int32_t* bnd_rows;     // rows outside every patch
+    double* pinv;          // Vanka patch inverses, [100][npatch] (FP64 form)
+    float* pinv32;         // same in FP32 (mixed form)
+    // work vectors (FP64 form uses d*, mixed form uses f*)
+    double *dx_, *db, *dr;
+    float *fx, *fb, *fr;
+    // coarse-level coefficient fields (owned for l > 0)
+    std::vector<double*> owned;
+    AsmFields af;
+};
+
+struct Solver {
+    int m;                 // restart length
+    int N;
+    double* V;             // (m+1) x N Krylov basis
+    double* Z;             // m x N preconditioned directions
+    double* w;
+    double* H;             // (m+1) x m Hessenberg (device)
+    double* cs; double* sn; double* gvec; double* yvec;
+    double* partial;       // block partial sums [(m+1) x nblk]
+    double* dots;          // (m+1) reduced dot products
+    double* bnorm;         // ||D b||
+    int* done;             // convergence flag of the current solve
+    int* kcur;             // Arnoldi steps taken in the current cycle
+    int nblk;
+    std::vector<Level> lv;
+};
+
+// Live timing of one kernel family (bench.py roofline): CUDA events around
+// each launch whose name starts with `name`, on the context stream.
+struct ProfState {
+    std::string name;
+    std::vector<cudaEvent_t> pool;
+    std::vector<cudaEvent_t> pending;  // start/stop pairs
+    int64_t launches = 0;
+    double ms = 0, bytes = 0;
+};
+
+struct hmec_ctx {
+    hmec_params p;
+    int dev;
+    cudaStream_t stream;
+    Geo g;
+    int64_t marknum;
+    double* crd[8];          // x, y, xvx, yvx, xvy, yvy, xp, yp (Eigen LinSpaced)
+    double* mk[HMEC_M_COUNT];
+    double* f[HMEC_F_COUNT];
+    // marker sort scratch
+    int32_t* mkey;           // half-cell key per marker
+    int32_t* perm;           // marker ids sorted by key
+    int32_t* hc_count;       // markers per half-cell
+    int32_t* hc_start;       // exclusive scan of hc_count (+ total)
+    int32_t* hc_fill;        // scatter cursors
+    int32_t* scan_part;      // scan block partials
+    double* mprop;           // 17 sorted per-marker properties [17][marknum]
+    int nhalf;               // number of half-cells
+    // global system
+    double* R;               // unscaled right-hand side
+    double* S;               // solution (kept as the next initial guess)
+    double* red;             // reduction partials
+    DevScalars* ds;          // device scalars
+    DevScalars* hs;          // pinned host mirror
+    Solver sv;
+    int64_t launches;
+    ProfState prof;
+    int in_step;             // between timestep_begin and timestep_end
+    std::string err;
+};
+
+// ------------------------------------------------------------------ helpers
+#define DMIN(a, b) ((b) < (a) ? (b) : (a))
+#define DMAX(a, b) ((a) < (b) ? (b) : (a))
+
+__host__ __device__ __forceinline__ int fix_trunc(double t) { return t < 0. ? (int)ceil(t) : (int)floor(t); }
+__host__ __device__ __forceinline__ int check_bounds(int k, int bound) {
+    return k < 0 ? 0 : (k > bound - 2 ? bound - 2 : k);
+}
+__host__ __device__ __forceinline__ double divplus(double x, double y) { return x / (x + y); }
+
+static inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+// Launch bookkeeping: every kernel launch of the library goes through this.
+#define HMEC_LAUNCH(ctx, kern, grid, block, smem, ...)                          \
+    do {                                                                          \
+        kern<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);            \
+        (ctx)->launches++;                                                        \
+    } while (0)
+
+int hmec_cuda_fail(hmec_ctx* ctx, cudaError_t e, const char* what);
+bool hmec_prof_begin(hmec_ctx* ctx, const char* kname, double bytes);
+void hmec_prof_end(hmec_ctx* ctx);
+
+// Launch with algorithmic byte accounting for the live roofline.
+#define HMEC_LAUNCH_B(ctx, nbytes, kern, grid, block, smem, ...)               \
+    do {                                                                          \
+        const bool _prof = hmec_prof_begin((ctx), #kern, (nbytes));               \
+        kern<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);            \
+        (ctx)->launches++;                                                        \
+        if (_prof) hmec_prof_end(ctx);                                            \
+    } while (0)
+#define HMEC_CUDA(ctx, call)                                                     \
+    do {                                                                          \
+        cudaError_t _e = (call);                                                  \
+        if (_e != cudaSuccess) return hmec_cuda_fail((ctx), _e, #call);          \
+    } while (0)
+
+// Sections (implemented in the k_*.cu units); all return an hmec status.
+int p2g_alloc(hmec_ctx* ctx);
+void p2g_free(hmec_ctx* ctx);
+int p2g_run(hmec_ctx* ctx);
+int iter_prepare(hmec_ctx* ctx);
+int iter_assemble(hmec_ctx* ctx);
+int iter_finish(hmec_ctx* ctx);
+int step_begin(hmec_ctx* ctx);
+int step_end(hmec_ctx* ctx);
+int advect_run(hmec_ctx* ctx);
+int solver_alloc(hmec_ctx* ctx);
+void solver_free(hmec_ctx* ctx);
+int solver_setup(hmec_ctx* ctx);            // build coarse levels + Vanka inverses for the current matrix
+int solver_solve(hmec_ctx* ctx, int* iters, double* relres);  // solve A S = R in place (S = guess)
+// Assembly of one level into (col, val, dscale, rhs); rhs may be null.
+void launch_assemble(hmec_ctx* ctx, const Geo& g, const AsmFields& af, int32_t* col, double* val, double* dscale,
+                     double* rhs_scaled, double* rhs_raw, const double* sc_dev);

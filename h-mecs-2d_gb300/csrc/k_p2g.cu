@@ -1,0 +1,442 @@
+// k_p2g.cu -- markers -> nodes (sections a1-a4, cpp/h_mec_rsf_v9.cpp:376-583).
+//
+// The reference scatters every marker into four 2x2 node blocks with an
+// OpenMP `+=` that races between threads (:384-528).  Here the scatter is
+// turned into a deterministic gather:
+//
+//  1. keys: each marker's basic cell (ib, jb) and pressure cell (iP, jP) are
+//     computed with the reference's integer arithmetic (fix + check_bounds,
+//     IEEE division, no contraction), so they are bit-exact.  Because
+//     iP - ib and jP - jb are always 0 or 1, the pair defines a "half cell"
+//     (hr = 2*ib + (iP-ib), hc = 2*jb + (jP-jb)), and the cell of the
+//     marker on each of the four grids (basic, P, Vx = (iP, jb),
+//     Vy = (ib, jP)) is a function of its half cell.  One counting sort by
+//     half cell therefore serves all four grids.
+//  2. counting sort: warp-aggregated integer atomics for the histogram and
+//     the scatter, a three-phase scan, then each half-cell segment is put in
+//     marker-index order, so the permutation is deterministic.
+//  3. per-marker properties (a1) and interpolation distances are computed
+//     once, in sorted order, into structure-of-arrays buffers.
+//  4. one thread per node walks the (at most four) contiguous sorted runs of
+//     the half cells that touch it, accumulates weight * property in fixed
+//     order, and normalises in the epilogue (a4).  No float atomics.
+#include "hmec_internal.cuh"
+
+namespace {
+
+constexpr int NPROP = 21;
+// sorted per-marker property rows
+enum {
+    MP_DXB, MP_DYB, MP_DXX, MP_DYY, MP_DXP, MP_DYP,  // interpolation distances
+    MP_RHO, MP_KKK, MP_TTT, MP_INVG, MP_ETA0, MP_COHT, MP_FRIT, MP_COHC, MP_FRIC, MP_DILC,
+    MP_ETAP, MP_POR, MP_ETAB0, MP_INVETAD, MP_RHOF
+};
+
+struct MarkerCells {
+    int ib, jb, iP, jP;
+};
+
+// Cell indices of :432-433 and :468-469 (the Vx/Vy cells reuse them).
+__device__ __forceinline__ MarkerCells marker_cells(double xm, double ym, const Geo& g) {
+    MarkerCells c;
+    // __ddiv_rn / __dadd_rn keep the reference's IEEE operations (no FMA)
+    c.jb = check_bounds(fix_trunc(__ddiv_rn(xm, g.dx)), g.Nx);
+    c.ib = check_bounds(fix_trunc(__ddiv_rn(ym, g.dy)), g.Ny);
+    c.jP = check_bounds(fix_trunc(__ddiv_rn(__dadd_rn(xm, g.dx / 2.), g.dx)), g.Nx);
+    c.iP = check_bounds(fix_trunc(__ddiv_rn(__dadd_rn(ym, g.dy / 2.), g.dy)), g.Ny);
+    return c;
+}
+
+__global__ void k_keys(const double* __restrict__ xm, const double* __restrict__ ym, int64_t n, Geo g,
+                       int32_t* __restrict__ key, int32_t* __restrict__ count, int* status) {
+    int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int k = -1;
+    if (m < n) {
+        MarkerCells c = marker_cells(xm[m], ym[m], g);
+        int di = c.iP - c.ib, dj = c.jP - c.jb;
+        if (di < 0 || di > 1 || dj < 0 || dj > 1) {  // cannot happen (monotone clamp); guard anyway
+            atomicOr(status, HMEC_DEV_BOUNDS);
+            di = di < 0 ? 0 : (di > 1 ? 1 : di);
+            dj = dj < 0 ? 0 : (dj > 1 ? 1 : dj);
+        }
+        int hr = 2 * c.ib + di, hc = 2 * c.jb + dj;
+        k = hc * (2 * (g.Ny - 1)) + hr;
+        key[m] = k;
+    }
+    // warp-aggregated histogram: one atomic per distinct key in the warp
+    unsigned active = __ballot_sync(0xffffffffu, k >= 0);
+    if (k >= 0) {
+        unsigned peers = __match_any_sync(active, k);
+        int leader = __ffs(peers) - 1;
+        if ((int)(threadIdx.x & 31) == leader) atomicAdd(&count[k], __popc(peers));
+    }
+}
+
+__global__ void k_scatter(const int32_t* __restrict__ key, int64_t n, int32_t* __restrict__ cursor,
+                          int32_t* __restrict__ perm) {
+    int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int k = (m < n) ? key[m] : -1;
+    unsigned active = __ballot_sync(0xffffffffu, k >= 0);
+    if (k >= 0) {
+        unsigned peers = __match_any_sync(active, k);
+        int lane = threadIdx.x & 31;
+        int leader = __ffs(peers) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&cursor[k], __popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        int rank = __popc(peers & ((1u << lane) - 1u));
+        perm[base + rank] = (int32_t)m;
+    }
+}
+
+// Segment ordering by marker id (segments are a few markers long).
+__global__ void k_segsort(const int32_t* __restrict__ start, int nseg, int32_t* __restrict__ perm) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg) return;
+    int b = start[s], e = start[s + 1];
+    for (int a = b + 1; a < e; a++) {
+        int v = perm[a];
+        int q = a;
+        while (q > b && perm[q - 1] > v) {
+            perm[q] = perm[q - 1];
+            q--;
+        }
+        perm[q] = v;
+    }
+}
+
+// Exclusive scan, three phases (block scan of 2048, scan of block totals, add).
+__global__ void k_scan1(const int32_t* __restrict__ in, int n, int32_t* __restrict__ out, int32_t* __restrict__ part) {
+    __shared__ int32_t sh[2048];
+    int base = blockIdx.x * 2048;
+    int t = threadIdx.x;
+    sh[t] = (base + t < n) ? in[base + t] : 0;
+    sh[t + 1024] = (base + t + 1024 < n) ? in[base + t + 1024] : 0;
+    __syncthreads();
+    // Blelloch up-sweep / down-sweep
+    for (int d = 1; d < 2048; d <<= 1) {
+        int idx = (t + 1) * d * 2 - 1;
+        if (idx < 2048) sh[idx] += sh[idx - d];
+        __syncthreads();
+    }
+    if (t == 0) {
+        part[blockIdx.x] = sh[2047];
+        sh[2047] = 0;
+    }
+    __syncthreads();
+    for (int d = 1024; d >= 1; d >>= 1) {
+        int idx = (t + 1) * d * 2 - 1;
+        if (idx < 2048) {
+            int32_t v = sh[idx - d];
+            sh[idx - d] = sh[idx];
+            sh[idx] += v;
+        }
+        __syncthreads();
+    }
+    if (base + t < n) out[base + t] = sh[t];
+    if (base + t + 1024 < n) out[base + t + 1024] = sh[t + 1024];
+}
+
+__global__ void k_scan2(int32_t* __restrict__ part, int nparts, int32_t* __restrict__ total_out) {
+    // single block: sequential carry over chunks of 1024
+    __shared__ int32_t sh[1024];
+    __shared__ int32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int c0 = 0; c0 < nparts; c0 += 1024) {
+        int t = threadIdx.x;
+        int32_t v = (c0 + t < nparts) ? part[c0 + t] : 0;
+        sh[t] = v;
+        __syncthreads();
+        for (int d = 1; d < 1024; d <<= 1) {  // Hillis-Steele inclusive scan
+            int32_t a = (t >= d) ? sh[t - d] : 0;
+            __syncthreads();
+            sh[t] += a;
+            __syncthreads();
+        }
+        if (c0 + t < nparts) part[c0 + t] = carry + sh[t] - v;  // exclusive
+        __syncthreads();
+        if (t == 0) carry += sh[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total_out = carry;
+}
+
+__global__ void k_scan3(int32_t* __restrict__ out, int n, const int32_t* __restrict__ part) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += part[i / 2048];
+}
+
+__device__ __forceinline__ double enforce_bounds(double v, double lo, double hi) {
+    return v < lo ? lo : (v > hi ? hi : v);
+}
+
+// a1 per marker (:389-423) in sorted order, plus interpolation distances.
+struct MkPtrs {
+    const double *xm, *ym, *t_marker, *rhom, *etasm, *etam, *cohescm, *cohestm, *frictcm, *dilatcm, *fricttm,
+        *porm, *kkkm, *gm, *rhofm, *etafm;
+};
+struct Crd {
+    const double *x, *y, *xvx, *yvx, *xvy, *yvy, *xp, *yp;
+};
+
+__global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, int64_t n, Geo g, Crd c, hmec_params p,
+                        double* __restrict__ out) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int m = perm[k];
+    const double por = mk.porm[m];
+    double kkkmm = mk.kkkm[m] * pow(por / p.POR0, 3.0);
+    kkkmm = enforce_bounds(kkkmm, p.kkkmin, p.kkkmax);
+    double cohescmm, cohestmm, frictcmm, dilatcmm, fricttmm, etasmm0, etamm0, etamm, rhomm;
+    const double tm = mk.t_marker[m];
+    if (tm != 0) {
+        cohescmm = mk.cohescm[m] * (1 - por);
+        cohestmm = mk.cohestm[m] * (1 - por);
+        frictcmm = mk.frictcm[m];
+        dilatcmm = mk.dilatcm[m];
+        fricttmm = mk.fricttm[m];
+        etasmm0 = mk.etasm[m];
+        etamm0 = mk.etasm[m] * exp(-p.alpha * por);
+        etamm = mk.etam[m];
+        rhomm = mk.rhom[m] * (1 - por) + mk.rhofm[m] * por;
+    } else {
+        cohescmm = mk.cohescm[m];
+        cohestmm = mk.cohestm[m];
+        frictcmm = mk.frictcm[m];
+        dilatcmm = 0;
+        fricttmm = mk.fricttm[m];
+        etasmm0 = mk.etasm[m];
+        etamm0 = mk.etasm[m];
+        etamm = mk.etam[m];
+        rhomm = mk.rhom[m];
+    }
+    etamm0 = enforce_bounds(etamm0, p.etamin, p.etamax);
+    etamm = enforce_bounds(etamm, p.etamin, p.etamax);
+    const double etadm = mk.etafm[m] / kkkmm;
+    const double xmm = mk.xm[m], ymm = mk.ym[m];
+    MarkerCells mc = marker_cells(xmm, ymm, g);
+    const size_t S = (size_t)n;
+    out[MP_DXB * S + k] = (xmm - c.x[mc.jb]) / g.dx;
+    out[MP_DYB * S + k] = (ymm - c.y[mc.ib]) / g.dy;
+    out[MP_DXX * S + k] = (xmm - c.xvx[mc.jb]) / g.dx;
+    out[MP_DYY * S + k] = (ymm - c.yvy[mc.ib]) / g.dy;
+    out[MP_DXP * S + k] = (xmm - c.xp[mc.jP]) / g.dx;
+    out[MP_DYP * S + k] = (ymm - c.yp[mc.iP]) / g.dy;
+    out[MP_RHO * S + k] = rhomm;
+    out[MP_KKK * S + k] = kkkmm;
+    out[MP_TTT * S + k] = tm;
+    out[MP_INVG * S + k] = 1. / mk.gm[m];
+    out[MP_ETA0 * S + k] = etamm0;
+    out[MP_COHT * S + k] = cohestmm;
+    out[MP_FRIT * S + k] = fricttmm;
+    out[MP_COHC * S + k] = cohescmm;
+    out[MP_FRIC * S + k] = frictcmm;
+    out[MP_DILC * S + k] = dilatcmm;
+    out[MP_ETAP * S + k] = etamm;
+    out[MP_POR * S + k] = por;
+    out[MP_ETAB0 * S + k] = etasmm0;
+    out[MP_INVETAD * S + k] = 1. / etadm;
+    out[MP_RHOF * S + k] = mk.rhofm[m];
+}
+
+// Which half cells touch node (i, j) of a grid: rows [r0, r0+3], cols
+// [c0, c0+3]; "row offset" tells whether the grid's cell row of a half row
+// hr is hr>>1 (basic-type rows) or (hr+1)>>1 (pressure-type rows).
+template <int NACC>
+struct Acc {
+    double s[NACC];
+};
+
+// Generic gather: ROWP = rows follow the pressure cell, COLP = columns follow
+// the pressure cell.  DXI/DYI pick the distance rows, PROPS the properties.
+template <bool ROWP, bool COLP, int NP>
+__device__ __forceinline__ void gather_node(int i, int j, const Geo& g, const int32_t* __restrict__ start,
+                                            const double* __restrict__ mp, int64_t n, int dxrow, int dyrow,
+                                            const int (&props)[NP], double& wt, double (&acc)[NP]) {
+    const int HR = 2 * (g.Ny - 1), HC = 2 * (g.Nx - 1);
+    const int r0 = ROWP ? 2 * i - 3 : 2 * i - 2;
+    const int c0 = COLP ? 2 * j - 3 : 2 * j - 2;
+    const int rlo = r0 < 0 ? 0 : r0;
+    const int rhi = (r0 + 3) > HR - 1 ? HR - 1 : r0 + 3;
+    wt = 0;
+#pragma unroll
+    for (int q = 0; q < NP; q++) acc[q] = 0;
+    if (rlo > rhi) return;
+    const size_t S = (size_t)n;
+    for (int hc = (c0 < 0 ? 0 : c0); hc <= c0 + 3 && hc < HC; hc++) {
+        const int cj = COLP ? (hc + 1) >> 1 : hc >> 1;  // grid column of this half column
+        const int b = start[hc * HR + rlo], e = start[hc * HR + rhi + 1];
+        // half-row boundary where the grid cell row changes from i-1 to i
+        const int split_hr = ROWP ? 2 * i - 1 : 2 * i;
+        const int bsplit = (split_hr <= rlo) ? b : (split_hr > rhi ? e : start[hc * HR + split_hr]);
+        for (int k = b; k < e; k++) {
+            const double dxm = mp[dxrow * S + k];
+            const double dym = mp[dyrow * S + k];
+            const double fx = (cj == j) ? (1 - dxm) : dxm;
+            const double fy = (k >= bsplit) ? (1 - dym) : dym;  // cell row == i -> top corner
+            const double w = fx * fy;
+            wt += w;
+#pragma unroll
+            for (int q = 0; q < NP; q++) acc[q] += mp[props[q] * S + k] * w;
+        }
+    }
+}
+
+__global__ void k_node_basic(Geo g, const int32_t* __restrict__ start, const double* __restrict__ mp, int64_t n,
+                             double* RHO, double* KKK, double* TTT, double* GGG, double* ETA0, double* COHT,
+                             double* FRIT, double* COHC, double* FRIC, double* DILC) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i >= g.Ny) return;
+    const int props[10] = {MP_RHO, MP_KKK, MP_TTT, MP_INVG, MP_ETA0, MP_COHT, MP_FRIT, MP_COHC, MP_FRIC, MP_DILC};
+    double wt, a[10];
+    gather_node<false, false, 10>(i, j, g, start, mp, n, MP_DXB, MP_DYB, props, wt, a);
+    if (wt > 0) {
+        size_t o = (size_t)j * g.Ny + i;
+        RHO[o] = a[0] / wt;
+        KKK[o] = a[1] / wt;
+        TTT[o] = a[2] / wt;
+        GGG[o] = 1. / (a[3] / wt);
+        ETA0[o] = a[4] / wt;
+        COHT[o] = a[5] / wt;
+        FRIT[o] = a[6] / wt;
+        COHC[o] = a[7] / wt;
+        FRIC[o] = a[8] / wt;
+        DILC[o] = a[9] / wt;
+    }
+}
+
+__global__ void k_node_p(Geo g, const int32_t* __restrict__ start, const double* __restrict__ mp, int64_t n,
+                         double* ETAP, double* POR, double* ETAB0, double* ETAP0, double* GGGP) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i >= g.Ny1) return;
+    const int props[5] = {MP_ETAP, MP_POR, MP_ETAB0, MP_ETA0, MP_INVG};
+    double wt, a[5];
+    gather_node<true, true, 5>(i, j, g, start, mp, n, MP_DXP, MP_DYP, props, wt, a);
+    if (wt > 0) {
+        size_t o = (size_t)j * g.Ny1 + i;
+        ETAP[o] = a[0] / wt;
+        const double por = a[1] / wt;
+        POR[o] = por;
+        ETAB0[o] = a[2] / wt / por;
+        ETAP0[o] = a[3] / wt;
+        GGGP[o] = 1. / (a[4] / wt);
+    }
+}
+
+// Vx nodes: rows follow the pressure cell, columns the basic cell.
+__global__ void k_node_vx(Geo g, const int32_t* __restrict__ start, const double* __restrict__ mp, int64_t n,
+                          double* RHOX, double* ETADX, double* RHOFX, double* PORX) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i >= g.Ny1 || j >= g.Nx) return;
+    const int props[4] = {MP_RHO, MP_INVETAD, MP_RHOF, MP_POR};
+    double wt, a[4];
+    gather_node<true, false, 4>(i, j, g, start, mp, n, MP_DXX, MP_DYP, props, wt, a);
+    if (wt > 0) {
+        size_t o = (size_t)j * g.Ny1 + i;
+        RHOX[o] = a[0] / wt;
+        ETADX[o] = 1. / (a[1] / wt);
+        RHOFX[o] = a[2] / wt;
+        PORX[o] = a[3] / wt;
+    }
+}
+
+// Vy nodes: rows follow the basic cell, columns the pressure cell.
+__global__ void k_node_vy(Geo g, const int32_t* __restrict__ start, const double* __restrict__ mp, int64_t n,
+                          double* RHOY, double* ETADY, double* RHOFY, double* PORY) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i >= g.Ny) return;
+    const int props[4] = {MP_RHO, MP_INVETAD, MP_RHOF, MP_POR};
+    double wt, a[4];
+    gather_node<false, true, 4>(i, j, g, start, mp, n, MP_DXP, MP_DYY, props, wt, a);
+    if (wt > 0) {
+        size_t o = (size_t)j * g.Ny1 + i;
+        RHOY[o] = a[0] / wt;
+        ETADY[o] = 1. / (a[1] / wt);
+        RHOFY[o] = a[2] / wt;
+        PORY[o] = a[3] / wt;
+    }
+}
+
+}  // namespace
+
+int p2g_alloc(hmec_ctx* ctx) {
+    const Geo& g = ctx->g;
+    ctx->nhalf = 4 * (g.Nx - 1) * (g.Ny - 1);
+    int64_t n = ctx->marknum;
+    int nparts = (ctx->nhalf + 1 + 2047) / 2048;
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->mkey, sizeof(int32_t) * (size_t)n));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->perm, sizeof(int32_t) * (size_t)n));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->hc_count, sizeof(int32_t) * ((size_t)ctx->nhalf + 1)));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->hc_start, sizeof(int32_t) * ((size_t)ctx->nhalf + 2)));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->hc_fill, sizeof(int32_t) * ((size_t)ctx->nhalf + 1)));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->scan_part, sizeof(int32_t) * ((size_t)nparts + 1)));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->mprop, sizeof(double) * (size_t)NPROP * (size_t)n));
+    return HMEC_OK;
+}
+
+void p2g_free(hmec_ctx* ctx) {
+    cudaFree(ctx->mkey);
+    cudaFree(ctx->perm);
+    cudaFree(ctx->hc_count);
+    cudaFree(ctx->hc_start);
+    cudaFree(ctx->hc_fill);
+    cudaFree(ctx->scan_part);
+    cudaFree(ctx->mprop);
+}
+
+int p2g_run(hmec_ctx* ctx) {
+    const Geo& g = ctx->g;
+    const int64_t n = ctx->marknum;
+    const int nh = ctx->nhalf;
+    int* status = &ctx->ds->status;
+    HMEC_CUDA(ctx, cudaMemsetAsync(ctx->hc_count, 0, sizeof(int32_t) * ((size_t)nh + 1), ctx->stream));
+    HMEC_LAUNCH(ctx, k_keys, nblocks(n, 256), 256, 0, ctx->mk[HMEC_M_xm], ctx->mk[HMEC_M_ym], n, g, ctx->mkey,
+                ctx->hc_count, status);
+    // exclusive scan of nh+1 counts (last entry is 0) -> hc_start[0..nh]
+    int ns = nh + 1;
+    int nparts = (ns + 2047) / 2048;
+    HMEC_LAUNCH(ctx, k_scan1, nparts, 1024, 0, ctx->hc_count, ns, ctx->hc_start, ctx->scan_part);
+    HMEC_LAUNCH(ctx, k_scan2, 1, 1024, 0, ctx->scan_part, nparts, ctx->scan_part + nparts);
+    HMEC_LAUNCH(ctx, k_scan3, nblocks(ns, 256), 256, 0, ctx->hc_start, ns, ctx->scan_part);
+    HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->hc_fill, ctx->hc_start, sizeof(int32_t) * (size_t)nh,
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+    HMEC_LAUNCH(ctx, k_scatter, nblocks(n, 256), 256, 0, ctx->mkey, n, ctx->hc_fill, ctx->perm);
+    HMEC_LAUNCH(ctx, k_segsort, nblocks(nh, 128), 128, 0, ctx->hc_start, nh, ctx->perm);
+    MkPtrs mk;
+    mk.xm = ctx->mk[HMEC_M_xm];
+    mk.ym = ctx->mk[HMEC_M_ym];
+    mk.t_marker = ctx->mk[HMEC_M_t_marker];
+    mk.rhom = ctx->mk[HMEC_M_rhom];
+    mk.etasm = ctx->mk[HMEC_M_etasm];
+    mk.etam = ctx->mk[HMEC_M_etam];
+    mk.cohescm = ctx->mk[HMEC_M_cohescm];
+    mk.cohestm = ctx->mk[HMEC_M_cohestm];
+    mk.frictcm = ctx->mk[HMEC_M_frictcm];
+    mk.dilatcm = ctx->mk[HMEC_M_dilatcm];
+    mk.fricttm = ctx->mk[HMEC_M_fricttm];
+    mk.porm = ctx->mk[HMEC_M_porm];
+    mk.kkkm = ctx->mk[HMEC_M_kkkm];
+    mk.gm = ctx->mk[HMEC_M_gm];
+    mk.rhofm = ctx->mk[HMEC_M_rhofm];
+    mk.etafm = ctx->mk[HMEC_M_etafm];
+    Crd c{ctx->crd[0], ctx->crd[1], ctx->crd[2], ctx->crd[3], ctx->crd[4], ctx->crd[5], ctx->crd[6], ctx->crd[7]};
+    HMEC_LAUNCH(ctx, k_mprop, nblocks(n, 256), 256, 0, mk, ctx->perm, n, g, c, ctx->p, ctx->mprop);
+    double* const* f = ctx->f;
+    dim3 bb(64), gb(nblocks(g.Ny, 64), g.Nx), gs(nblocks(g.Ny1, 64), g.Nx1);
+    HMEC_LAUNCH(ctx, k_node_basic, gb, bb, 0, g, ctx->hc_start, ctx->mprop, n, f[HMEC_F_RHO], f[HMEC_F_KKK],
+                f[HMEC_F_TTT], f[HMEC_F_GGG], f[HMEC_F_ETA0], f[HMEC_F_COHT], f[HMEC_F_FRIT], f[HMEC_F_COHC],
+                f[HMEC_F_FRIC], f[HMEC_F_DILC]);
+    HMEC_LAUNCH(ctx, k_node_p, gs, bb, 0, g, ctx->hc_start, ctx->mprop, n, f[HMEC_F_ETAP], f[HMEC_F_POR],
+                f[HMEC_F_ETAB0], f[HMEC_F_ETAP0], f[HMEC_F_GGGP]);
+    HMEC_LAUNCH(ctx, k_node_vx, gs, bb, 0, g, ctx->hc_start, ctx->mprop, n, f[HMEC_F_RHOX], f[HMEC_F_ETADX],
+                f[HMEC_F_RHOFX], f[HMEC_F_PORX]);
+    HMEC_LAUNCH(ctx, k_node_vy, gs, bb, 0, g, ctx->hc_start, ctx->mprop, n, f[HMEC_F_RHOY], f[HMEC_F_ETADY],
+                f[HMEC_F_RHOFY], f[HMEC_F_PORY]);
+    HMEC_CUDA(ctx, cudaGetLastError());
+    return HMEC_OK;
+}

@@ -1,0 +1,1019 @@
+// k_solver.cu -- solution of the assembled system (section a10), in place of
+// the Pardiso analyse/factorise/solve of cpp/h_mec_rsf_v9.cpp:1046-1052.
+//
+// Outer: FGMRES(m) in FP64 on the row-equilibrated system D A x = D b
+// (D a power of two per row, so the scaling is exact).  Orthogonalisation is
+// classical Gram-Schmidt applied twice (CGS2) so the m dot products of a
+// step are one batched kernel; all reductions are block partials summed in a
+// fixed order (deterministic, no atomics).  The Hessenberg/Givens update runs
+// in one device thread; kernels of a converged solve return immediately, so
+// the host only looks at the convergence flag every few steps.
+//
+// Preconditioner: one geometric-multigrid V-cycle.  Coarse operators are
+// rediscretised: the node coefficients that enter the assembly are
+// restricted from the fine grid and the same assembly kernel builds the
+// coarse matrix.  The smoother is a multiplicative Vanka smoother on
+// the staggered cell patch {Pt, Pf, 2 vx, 2 vy, 2 vxD, 2 vyD} (10 unknowns),
+// with the 10x10 patch inverses formed once per solve and applied in nine
+// colour classes (patches of one class neither share unknowns nor read
+// each other's), followed by a two-phase Jacobi pass over the boundary
+// rows that no patch covers.  The V-cycle runs in FP64 (HMEC_FORM_FP64) or
+// entirely in FP32 (HMEC_FORM_MIXED); FGMRES stays FP64 either way.
+#include "hmec_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace {
+
+constexpr int PB = 10;   // patch size
+constexpr int RED_BS = 256;
+
+__device__ __forceinline__ int kp_of(int i, int j, int Ny1) { return (j * Ny1 + i) * 6; }
+
+__device__ __forceinline__ void patch_unknowns(int i, int j, int Ny1, int (&u)[PB]) {
+    const int c = kp_of(i, j, Ny1), l = kp_of(i, j - 1, Ny1), t = kp_of(i - 1, j, Ny1);
+    u[0] = c + 0;  // Pt
+    u[1] = c + 3;  // Pf
+    u[2] = l + 1;  // vx left face
+    u[3] = c + 1;  // vx right face
+    u[4] = t + 2;  // vy top face
+    u[5] = c + 2;  // vy bottom face
+    u[6] = l + 4;  // vxD left
+    u[7] = c + 4;  // vxD right
+    u[8] = t + 5;  // vyD top
+    u[9] = c + 5;  // vyD bottom
+}
+
+// ------------------------------------------------------------ Vanka setup
+// Gauss-Jordan with partial pivoting on the 10x10 patch block of D A.
+__global__ void k_vanka_setup(Geo g, const int32_t* __restrict__ col, const double* __restrict__ val,
+                              double* pinv, float* pinv32, int* status) {
+    const int pi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int np = (g.Ny - 1) * (g.Nx - 1);
+    if (pi >= np) return;
+    const int i = 1 + pi % (g.Ny - 1), j = 1 + pi / (g.Ny - 1);
+    int u[PB];
+    patch_unknowns(i, j, g.Ny1, u);
+    double a[PB][PB], b[PB][PB];
+    for (int r = 0; r < PB; r++)
+        for (int c = 0; c < PB; c++) {
+            a[r][c] = 0;
+            b[r][c] = (r == c) ? 1.0 : 0.0;
+        }
+    for (int r = 0; r < PB; r++) {
+        for (int s = 0; s < HMEC_W; s++) {
+            const size_t o = (size_t)s * g.N + u[r];
+            const int cc = col[o];
+            const double v = val[o];
+            for (int c = 0; c < PB; c++)
+                if (u[c] == cc) a[r][c] += v;
+        }
+    }
+    bool singular = false;
+    for (int c = 0; c < PB; c++) {
+        int pr = c;
+        double best = fabs(a[c][c]);
+        for (int r = c + 1; r < PB; r++)
+            if (fabs(a[r][c]) > best) {
+                best = fabs(a[r][c]);
+                pr = r;
+            }
+        if (!(best > 0)) {
+            singular = true;
+            break;
+        }
+        if (pr != c)
+            for (int k = 0; k < PB; k++) {
+                double t = a[c][k];
+                a[c][k] = a[pr][k];
+                a[pr][k] = t;
+                t = b[c][k];
+                b[c][k] = b[pr][k];
+                b[pr][k] = t;
+            }
+        const double inv = 1.0 / a[c][c];
+        for (int k = 0; k < PB; k++) {
+            a[c][k] *= inv;
+            b[c][k] *= inv;
+        }
+        for (int r = 0; r < PB; r++) {
+            if (r == c) continue;
+            const double f = a[r][c];
+            if (f != 0)
+                for (int k = 0; k < PB; k++) {
+                    a[r][k] -= f * a[c][k];
+                    b[r][k] -= f * b[c][k];
+                }
+        }
+    }
+    if (singular) {
+        atomicOr(status, HMEC_DEV_NAN);
+        for (int r = 0; r < PB; r++)
+            for (int c = 0; c < PB; c++) b[r][c] = 0;
+    }
+    for (int r = 0; r < PB; r++)
+        for (int c = 0; c < PB; c++) {
+            const size_t o = (size_t)(r * PB + c) * np + pi;
+            if (pinv) pinv[o] = b[r][c];
+            if (pinv32) pinv32[o] = (float)b[r][c];
+        }
+}
+
+// One colour class of a multiplicative Vanka sweep on A x = b.
+template <typename T>
+__global__ void k_vanka_color(Geo g, const int32_t* __restrict__ col, const T* __restrict__ val,
+                              const T* __restrict__ pinv, const T* __restrict__ b, T* x, int ri, int rj) {
+    const int fi = ri == 0 ? 3 : ri, fj = rj == 0 ? 3 : rj;  // first i >= 1 with i % 3 == ri
+    const int ni = (g.Ny - 1 - fi) >= 0 ? (g.Ny - 1 - fi) / 3 + 1 : 0;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ni == 0) return;
+    const int a = t % ni, bb = t / ni;
+    const int i = fi + 3 * a, j = fj + 3 * bb;
+    if (i > g.Ny - 1 || j > g.Nx - 1) return;
+    const int np = (g.Ny - 1) * (g.Nx - 1);
+    const int pi = (j - 1) * (g.Ny - 1) + (i - 1);
+    int u[PB];
+    patch_unknowns(i, j, g.Ny1, u);
+    T r[PB];
+#pragma unroll
+    for (int q = 0; q < PB; q++) {
+        const int row = u[q];
+        T acc = b[row];
+#pragma unroll
+        for (int s = 0; s < HMEC_W; s++) {
+            const size_t o = (size_t)s * g.N + row;
+            acc -= val[o] * x[col[o]];
+        }
+        r[q] = acc;
+    }
+#pragma unroll
+    for (int q = 0; q < PB; q++) {
+        T d = 0;
+#pragma unroll
+        for (int c = 0; c < PB; c++) d += pinv[(size_t)(q * PB + c) * np + pi] * r[c];
+        x[u[q]] += d;
+    }
+}
+
+// Boundary rows outside every patch: two-phase Jacobi (deterministic).
+template <typename T>
+__global__ void k_bnd_delta(int N, const int32_t* __restrict__ rows, int nb, const int32_t* __restrict__ col,
+                            const T* __restrict__ val, const T* __restrict__ b, const T* __restrict__ x, T* delta) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nb) return;
+    const int row = rows[t];
+    T acc = b[row], diag = 0;
+#pragma unroll
+    for (int s = 0; s < HMEC_W; s++) {
+        const size_t o = (size_t)s * N + row;
+        const int c = col[o];
+        const T v = val[o];
+        acc -= v * x[c];
+        if (c == row) diag += v;
+    }
+    delta[t] = diag != 0 ? acc / diag : (T)0;
+}
+
+template <typename T>
+__global__ void k_bnd_apply(const int32_t* __restrict__ rows, int nb, const T* __restrict__ delta, T* x) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nb) x[rows[t]] += delta[t];
+}
+
+// r = b - A x
+template <typename T>
+__global__ void k_residual(int N, const int32_t* __restrict__ col, const T* __restrict__ val, const T* __restrict__ b,
+                           const T* __restrict__ x, T* r) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= N) return;
+    T acc = b[row];
+#pragma unroll
+    for (int s = 0; s < HMEC_W; s++) {
+        const size_t o = (size_t)s * N + row;
+        acc -= val[o] * x[col[o]];
+    }
+    r[row] = acc;
+}
+
+// ------------------------------------------------ multigrid transfers
+// Whether the row of unknown v at staggered cell (i, j) is an interior
+// equation (x/y-Stokes, continuity, Darcy) rather than a boundary or ghost
+// row; the ranges are those of the assembly branches (:698-980).
+__device__ __forceinline__ bool row_interior(const Geo& g, int i, int j, int v) {
+    switch (v) {
+        case 0: return i >= 1 && i <= g.Ny - 1 && j >= 1 && j <= g.Nx - 1;         // Pt
+        case 3: return i >= 2 && i <= g.Ny - 2 && j >= 1 && j <= g.Nx - 1;         // Pf
+        case 1: case 4: return i >= 1 && i <= g.Ny - 1 && j >= 1 && j <= g.Nx - 2; // vx, vxD
+        default: return i >= 1 && i <= g.Ny - 2 && j >= 1 && j <= g.Nx - 1;        // vy, vyD
+    }
+}
+
+// Restriction of the fine physical residual r/df to the coarse rows, scaled
+// by the coarse row scale.  Only interior equations are restricted, and only
+// from fine interior equations (weights renormalised); coarse boundary rows
+// get a zero residual, so the coarse correction obeys the homogeneous
+// boundary conditions, which the prolongation below preserves.
+template <typename T>
+__global__ void k_restrict(Geo gf, Geo gc, const T* __restrict__ rf, const double* __restrict__ dsf,
+                           const double* __restrict__ dsc, T* bc) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y;
+    if (I >= gc.Ny1) return;
+    const int kc = kp_of(I, J, gc.Ny1);
+    for (int v = 0; v < 6; v++) {
+        double s = 0, w = 0;
+        if (row_interior(gc, I, J, v)) {
+            int i0, i1, j0, j1;
+            if (v == 0 || v == 3) {  // cell centred: the 4 children
+                i0 = 2 * I - 1; i1 = 2 * I; j0 = 2 * J - 1; j1 = 2 * J;
+            } else if (v == 1 || v == 4) {  // x faces: rows of the children, columns 2J-1..2J+1
+                i0 = 2 * I - 1; i1 = 2 * I; j0 = 2 * J - 1; j1 = 2 * J + 1;
+            } else {  // y faces
+                i0 = 2 * I - 1; i1 = 2 * I + 1; j0 = 2 * J - 1; j1 = 2 * J;
+            }
+            for (int i = i0; i <= i1; i++)
+                for (int j = j0; j <= j1; j++) {
+                    if (i < 0 || i > gf.Ny || j < 0 || j > gf.Nx || !row_interior(gf, i, j, v)) continue;
+                    double ww = 1.0;
+                    if ((v == 1 || v == 4) && j != 2 * J) ww = 0.5;
+                    if ((v == 2 || v == 5) && i != 2 * I) ww = 0.5;
+                    const int k = kp_of(i, j, gf.Ny1) + v;
+                    s += ww * ((double)rf[k] / dsf[k]);
+                    w += ww;
+                }
+        }
+        bc[kc + v] = (T)(w > 0 ? (s / w) * dsc[kc + v] : 0.0);
+    }
+}
+
+// x_f += P x_c (constant in the cross direction, linear along the face normal)
+template <typename T>
+__global__ void k_prolong(Geo gf, Geo gc, const T* __restrict__ xc, T* xf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= gf.Ny1) return;
+    const int kf = kp_of(i, j, gf.Ny1);
+    auto xcv = [&](int I, int J, int v) -> T {
+        if (I < 0 || I > gc.Ny || J < 0 || J > gc.Nx) return (T)0;
+        return xc[kp_of(I, J, gc.Ny1) + v];
+    };
+    const int Ic = (i + 1) / 2, Jc = (j + 1) / 2;  // cell-type index (ghost rows map to ghost rows)
+    // P-type: interior fine cells only
+    if (i >= 1 && i <= gf.Ny - 1 && j >= 1 && j <= gf.Nx - 1) {
+        xf[kf + 0] += xcv(Ic, Jc, 0);
+        xf[kf + 3] += xcv(Ic, Jc, 3);
+    }
+    // vx-type: rows by cell index, columns: even j on a coarse face, odd j between two
+    {
+        T a1, a4;
+        if ((j & 1) == 0) {
+            a1 = xcv(Ic, j / 2, 1);
+            a4 = xcv(Ic, j / 2, 4);
+        } else {
+            a1 = (T)0.5 * (xcv(Ic, j / 2, 1) + xcv(Ic, j / 2 + 1, 1));
+            a4 = (T)0.5 * (xcv(Ic, j / 2, 4) + xcv(Ic, j / 2 + 1, 4));
+        }
+        xf[kf + 1] += a1;
+        xf[kf + 4] += a4;
+    }
+    {
+        T a2, a5;
+        if ((i & 1) == 0) {
+            a2 = xcv(i / 2, Jc, 2);
+            a5 = xcv(i / 2, Jc, 5);
+        } else {
+            a2 = (T)0.5 * (xcv(i / 2, Jc, 2) + xcv(i / 2 + 1, Jc, 2));
+            a5 = (T)0.5 * (xcv(i / 2, Jc, 5) + xcv(i / 2 + 1, Jc, 5));
+        }
+        xf[kf + 2] += a2;
+        xf[kf + 5] += a5;
+    }
+}
+
+// Coarse assembly coefficients from the fine ones.
+struct CoefIn {
+    const double *ETA, *GGG, *RHO;                          // basic
+    const double *ETAP, *GGGP, *ETAB, *POR, *GGGB;          // P
+    const double *RHOX, *RHOFX, *PORX, *ETADX;              // Vx
+    const double *RHOY, *RHOFY, *PORY, *ETADY;              // Vy
+};
+struct CoefOut {
+    double *ETA, *GGG, *RHO, *ETAP, *GGGP, *ETAB, *POR, *GGGB, *RHOX, *RHOFX, *PORX, *ETADX, *RHOY, *RHOFY, *PORY, *ETADY;
+};
+
+__global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y;
+    if (I >= gc.Ny1) return;
+    // basic nodes: 3x3 full weighting around fine (2I, 2J); G harmonically
+    if (I < gc.Ny && J < gc.Nx) {
+        double se = 0, sg = 0, sr = 0, w = 0;
+        for (int di = -1; di <= 1; di++)
+            for (int dj = -1; dj <= 1; dj++) {
+                const int i = 2 * I + di, j = 2 * J + dj;
+                if (i < 0 || i >= gf.Ny || j < 0 || j >= gf.Nx) continue;
+                const double ww = (di == 0 ? 2.0 : 1.0) * (dj == 0 ? 2.0 : 1.0);
+                const size_t o = (size_t)j * gf.Ny + i;
+                se += ww * F.ETA[o];
+                sg += ww / F.GGG[o];
+                sr += ww * F.RHO[o];
+                w += ww;
+            }
+        const size_t oc = (size_t)J * gc.Ny + I;
+        C.ETA[oc] = se / w;
+        C.GGG[oc] = w / sg;
+        C.RHO[oc] = sr / w;
+    }
+    const size_t oc = (size_t)J * gc.Ny1 + I;
+    // P nodes: average of the 4 children (interior coarse cells)
+    if (I >= 1 && I <= gc.Ny - 1 && J >= 1 && J <= gc.Nx - 1) {
+        double se = 0, sg = 0, sb = 0, sp = 0, sgb = 0;
+        for (int di = 0; di < 2; di++)
+            for (int dj = 0; dj < 2; dj++) {
+                const size_t o = (size_t)(2 * J - 1 + dj) * gf.Ny1 + (2 * I - 1 + di);
+                se += F.ETAP[o];
+                sg += 1.0 / F.GGGP[o];
+                sb += F.ETAB[o];
+                sp += F.POR[o];
+                sgb += 1.0 / F.GGGB[o];
+            }
+        C.ETAP[oc] = se / 4;
+        C.GGGP[oc] = 4 / sg;
+        C.ETAB[oc] = sb / 4;
+        C.POR[oc] = sp / 4;
+        C.GGGB[oc] = 4 / sgb;
+    } else {
+        C.ETAP[oc] = 1;
+        C.GGGP[oc] = 1;
+        C.ETAB[oc] = 1;
+        C.POR[oc] = 0.5;
+        C.GGGB[oc] = 1;
+    }
+    // Vx nodes (I, J): fine rows {2I-1, 2I}, fine columns 2J + {-1,0,1}
+    {
+        double a[4] = {0, 0, 0, 0}, w = 0;
+        const int r0 = I == 0 ? 0 : 2 * I - 1, r1 = I == 0 ? 0 : (I == gc.Ny ? gf.Ny : 2 * I);
+        for (int i = r0; i <= r1; i++)
+            for (int dj = -1; dj <= 1; dj++) {
+                const int j = 2 * J + dj;
+                if (j < 0 || j >= gf.Nx) continue;
+                const double ww = dj == 0 ? 2.0 : 1.0;
+                const size_t o = (size_t)j * gf.Ny1 + i;
+                a[0] += ww * F.RHOX[o];
+                a[1] += ww * F.RHOFX[o];
+                a[2] += ww * F.PORX[o];
+                a[3] += ww * F.ETADX[o];
+                w += ww;
+            }
+        if (w > 0) {
+            C.RHOX[oc] = a[0] / w;
+            C.RHOFX[oc] = a[1] / w;
+            C.PORX[oc] = a[2] / w;
+            C.ETADX[oc] = a[3] / w;
+        } else {
+            C.RHOX[oc] = 0;
+            C.RHOFX[oc] = 0;
+            C.PORX[oc] = 1;
+            C.ETADX[oc] = 1;
+        }
+    }
+    // Vy nodes (I, J): fine columns {2J-1, 2J}, fine rows 2I + {-1,0,1}
+    {
+        double a[4] = {0, 0, 0, 0}, w = 0;
+        const int c0 = J == 0 ? 0 : 2 * J - 1, c1 = J == 0 ? 0 : (J == gc.Nx ? gf.Nx : 2 * J);
+        for (int j = c0; j <= c1; j++)
+            for (int di = -1; di <= 1; di++) {
+                const int i = 2 * I + di;
+                if (i < 0 || i >= gf.Ny) continue;
+                const double ww = di == 0 ? 2.0 : 1.0;
+                const size_t o = (size_t)j * gf.Ny1 + i;
+                a[0] += ww * F.RHOY[o];
+                a[1] += ww * F.RHOFY[o];
+                a[2] += ww * F.PORY[o];
+                a[3] += ww * F.ETADY[o];
+                w += ww;
+            }
+        if (w > 0) {
+            C.RHOY[oc] = a[0] / w;
+            C.RHOFY[oc] = a[1] / w;
+            C.PORY[oc] = a[2] / w;
+            C.ETADY[oc] = a[3] / w;
+        } else {
+            C.RHOY[oc] = 0;
+            C.RHOFY[oc] = 0;
+            C.PORY[oc] = 1;
+            C.ETADY[oc] = 1;
+        }
+    }
+}
+
+template <typename S, typename D>
+__global__ void k_convert(size_t n, const S* __restrict__ a, D* b) {
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) b[t] = (D)a[t];
+}
+
+template <typename T>
+__global__ void k_zero(size_t n, T* a) {
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) a[t] = (T)0;
+}
+
+// ------------------------------------------------------------ FGMRES
+// partial[k * nblk + blk] = sum over the block's rows of V_k . w   (k = blockIdx.y)
+__global__ void k_dots(int N, const double* __restrict__ V, const double* __restrict__ w, double* partial, int nblk,
+                       const int* done) {
+    if (*done) return;
+    __shared__ double sh[RED_BS];
+    const int k = blockIdx.y;
+    const double* v = V + (size_t)k * N;
+    double acc = 0;
+    for (int r = blockIdx.x * RED_BS + threadIdx.x; r < N; r += nblk * RED_BS) acc += v[r] * w[r];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = RED_BS / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[(size_t)k * nblk + blockIdx.x] = sh[0];
+}
+
+// dots[k] = sum_b partial[k][b], one warp per k, fixed order.
+__global__ void k_dots_final(const double* __restrict__ partial, int nblk, int nk, double* dots, const int* done) {
+    if (*done) return;
+    const int k = blockIdx.x;
+    if (k >= nk) return;
+    double acc = 0;
+    for (int b = threadIdx.x; b < nblk; b += 32) acc += partial[(size_t)k * nblk + b];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) dots[k] = acc;
+}
+
+// w -= sum_k h_k V_k; partial sums of |w|^2 into partial[0..nblk)
+__global__ void k_orth_update(int N, const double* __restrict__ V, int nk, const double* __restrict__ h, double* w,
+                              double* partial, int nblk, const int* done) {
+    if (*done) return;
+    __shared__ double sh[RED_BS];
+    double acc2 = 0;
+    for (int r = blockIdx.x * RED_BS + threadIdx.x; r < N; r += nblk * RED_BS) {
+        double x = w[r];
+        for (int k = 0; k < nk; k++) x -= h[k] * V[(size_t)k * N + r];
+        w[r] = x;
+        acc2 += x * x;
+    }
+    sh[threadIdx.x] = acc2;
+    __syncthreads();
+    for (int s = RED_BS / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+// w = A z (scaled rows)
+__global__ void k_spmv(int N, const int32_t* __restrict__ col, const double* __restrict__ val,
+                       const double* __restrict__ z, double* w, const int* done) {
+    if (*done) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= N) return;
+    double acc = 0;
+#pragma unroll
+    for (int s = 0; s < HMEC_W; s++) {
+        const size_t o = (size_t)s * N + row;
+        acc += val[o] * z[col[o]];
+    }
+    w[row] = acc;
+}
+
+// r = b - A x, with partial sums of |r|^2 and |b|^2
+__global__ void k_true_resid(int N, const int32_t* __restrict__ col, const double* __restrict__ val,
+                             const double* __restrict__ b, const double* __restrict__ x, double* r, double* partial,
+                             int nblk) {
+    __shared__ double s1[RED_BS], s2[RED_BS];
+    double a1 = 0, a2 = 0;
+    for (int row = blockIdx.x * RED_BS + threadIdx.x; row < N; row += nblk * RED_BS) {
+        double acc = b[row];
+#pragma unroll
+        for (int s = 0; s < HMEC_W; s++) {
+            const size_t o = (size_t)s * N + row;
+            acc -= val[o] * x[col[o]];
+        }
+        r[row] = acc;
+        a1 += acc * acc;
+        a2 += b[row] * b[row];
+    }
+    s1[threadIdx.x] = a1;
+    s2[threadIdx.x] = a2;
+    __syncthreads();
+    for (int s = RED_BS / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            s1[threadIdx.x] += s1[threadIdx.x + s];
+            s2[threadIdx.x] += s2[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = s1[0];
+        partial[nblk + blockIdx.x] = s2[0];
+    }
+}
+
+// Start of a restart cycle: beta = ||r||, relres check, V0 = r / beta, g = beta e1.
+struct Gm {
+    double* H;
+    double* cs;
+    double* sn;
+    double* g;
+    double* y;
+    double* dots;
+    double* bnorm;
+    int* done;
+    int* kcur;
+    DevScalars* ds;
+};
+
+__global__ void k_cycle_begin(Gm G, const double* __restrict__ partial, int nblk, int first, double rtol, int m) {
+    double rr = 0, bb = 0;
+    for (int b = 0; b < nblk; b++) {
+        rr += partial[b];
+        bb += partial[nblk + b];
+    }
+    if (first) *G.bnorm = sqrt(bb);
+    const double bn = *G.bnorm;
+    const double beta = sqrt(rr);
+    const double rel = bn > 0 ? beta / bn : beta;
+    G.ds->krylov_relres = rel;
+    G.g[0] = beta;
+    for (int k = 1; k <= m; k++) G.g[k] = 0;
+    *G.kcur = 0;
+    *G.done = (rel <= rtol || !(beta > 0) || !isfinite(beta)) ? 1 : 0;
+    G.dots[0] = beta > 0 ? 1.0 / beta : 0.0;  // scale for V0
+}
+
+__global__ void k_scale_vec(int N, const double* __restrict__ a, const double* sc, double* b, const int* done) {
+    if (*done) return;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < N) b[r] = a[r] * sc[0];
+}
+
+// After the two CGS passes: column j of H, Givens rotation, residual estimate.
+__global__ void k_arnoldi_step(Gm G, const double* __restrict__ h1, const double* __restrict__ partial, int nblk,
+                               int j, int m, double rtol, double* hscale) {
+    if (*G.done) return;
+    double ww = 0;
+    for (int b = 0; b < nblk; b++) ww += partial[b];
+    const double hn = sqrt(ww);
+    double* Hc = G.H + (size_t)j * (m + 1);  // column j, rows 0..j+1
+    for (int k = 0; k <= j; k++) Hc[k] = h1[k] + G.dots[k];  // first + second CGS pass
+    Hc[j + 1] = hn;
+    for (int k = 0; k < j; k++) {  // previous rotations
+        const double t = G.cs[k] * Hc[k] + G.sn[k] * Hc[k + 1];
+        Hc[k + 1] = -G.sn[k] * Hc[k] + G.cs[k] * Hc[k + 1];
+        Hc[k] = t;
+    }
+    const double a = Hc[j], b = Hc[j + 1];
+    const double rho = sqrt(a * a + b * b);
+    const double c = rho > 0 ? a / rho : 1.0, s = rho > 0 ? b / rho : 0.0;
+    G.cs[j] = c;
+    G.sn[j] = s;
+    Hc[j] = rho;
+    Hc[j + 1] = 0;
+    G.g[j + 1] = -s * G.g[j];
+    G.g[j] = c * G.g[j];
+    *G.kcur = j + 1;
+    const double rel = fabs(G.g[j + 1]) / *G.bnorm;
+    G.ds->krylov_relres = rel;
+    G.ds->krylov_iters += 1;
+    hscale[0] = hn > 0 ? 1.0 / hn : 0.0;
+    if (rel <= rtol || !(hn > 0) || !isfinite(rel)) *G.done = 1;
+}
+
+// y = H^{-1} g (upper triangular, kcur columns)
+__global__ void k_lsq(Gm G, int m) {
+    const int k = *G.kcur;
+    for (int r = k - 1; r >= 0; r--) {
+        double s = G.g[r];
+        for (int c = r + 1; c < k; c++) s -= G.H[(size_t)c * (m + 1) + r] * G.y[c];
+        const double d = G.H[(size_t)r * (m + 1) + r];
+        G.y[r] = d != 0 ? s / d : 0.0;
+    }
+}
+
+__global__ void k_xupdate(int N, const double* __restrict__ Z, const double* __restrict__ y, const int* kcur, double* x) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N) return;
+    const int k = *kcur;
+    double acc = x[r];
+    for (int c = 0; c < k; c++) acc += y[c] * Z[(size_t)c * N + r];
+    x[r] = acc;
+}
+
+}  // namespace
+
+// ===================================================================== host
+
+static void make_geo(Geo& g, int Nx, int Ny, double xsize, double ysize) {
+    g.Nx = Nx;
+    g.Ny = Ny;
+    g.Nx1 = Nx + 1;
+    g.Ny1 = Ny + 1;
+    g.N = g.Nx1 * g.Ny1 * 6;
+    g.line_fault = (int)((Ny - 1) / 2.);
+    g.dx = xsize / (Nx - 1);
+    g.dy = ysize / (Ny - 1);
+    g.dx2 = g.dx * g.dx;
+    g.dy2 = g.dy * g.dy;
+    g.dx_dy = g.dx * g.dy;
+    g.lower_block = ysize / 2. + g.dy;
+    g.upper_block = ysize / 2. - g.dy;
+    g.dy_faultw = g.dy / g.dx;
+}
+
+static std::vector<int32_t> boundary_rows(const Geo& g) {
+    std::vector<int32_t> r;
+    for (int j = 0; j <= g.Nx; j++)
+        for (int i = 0; i <= g.Ny; i++) {
+            const int kp = (j * g.Ny1 + i) * 6;
+            const bool pin = (i >= 1 && i <= g.Ny - 1 && j >= 1 && j <= g.Nx - 1);
+            const bool vxin = (i >= 1 && i <= g.Ny - 1 && j <= g.Nx - 1);
+            const bool vyin = (i <= g.Ny - 1 && j >= 1 && j <= g.Nx - 1);
+            if (!pin) {
+                r.push_back(kp + 0);
+                r.push_back(kp + 3);
+            }
+            if (!vxin) {
+                r.push_back(kp + 1);
+                r.push_back(kp + 4);
+            }
+            if (!vyin) {
+                r.push_back(kp + 2);
+                r.push_back(kp + 5);
+            }
+        }
+    std::sort(r.begin(), r.end());
+    return r;
+}
+
+static int alloc_level(hmec_ctx* ctx, Level& L, bool mixed, bool coarse) {
+    const Geo& g = L.g;
+    const size_t N = (size_t)g.N;
+    L.npatch = (g.Ny - 1) * (g.Nx - 1);
+    HMEC_CUDA(ctx, cudaMalloc(&L.col, sizeof(int32_t) * HMEC_W * N));
+    HMEC_CUDA(ctx, cudaMalloc(&L.val, sizeof(double) * HMEC_W * N));
+    HMEC_CUDA(ctx, cudaMalloc(&L.dscale, sizeof(double) * N));
+    std::vector<int32_t> br = boundary_rows(g);
+    L.nbnd = (int)br.size();
+    HMEC_CUDA(ctx, cudaMalloc(&L.bnd_rows, sizeof(int32_t) * std::max<size_t>(br.size(), 1)));
+    HMEC_CUDA(ctx, cudaMemcpy(L.bnd_rows, br.data(), sizeof(int32_t) * br.size(), cudaMemcpyHostToDevice));
+    L.pinv = nullptr;
+    L.pinv32 = nullptr;
+    L.val32 = nullptr;
+    L.fx = L.fb = L.fr = nullptr;
+    L.dx_ = L.db = L.dr = nullptr;
+    HMEC_CUDA(ctx, cudaMalloc(&L.db, sizeof(double) * N));  // fine: scaled rhs; coarse: FP64 rhs
+    if (mixed) {
+        HMEC_CUDA(ctx, cudaMalloc(&L.val32, sizeof(float) * HMEC_W * N));
+        HMEC_CUDA(ctx, cudaMalloc(&L.pinv32, sizeof(float) * 100 * (size_t)L.npatch));
+        HMEC_CUDA(ctx, cudaMalloc(&L.fx, sizeof(float) * N));
+        HMEC_CUDA(ctx, cudaMalloc(&L.fb, sizeof(float) * N));
+        HMEC_CUDA(ctx, cudaMalloc(&L.fr, sizeof(float) * std::max(N, (size_t)L.nbnd)));
+    } else {
+        HMEC_CUDA(ctx, cudaMalloc(&L.pinv, sizeof(double) * 100 * (size_t)L.npatch));
+        HMEC_CUDA(ctx, cudaMalloc(&L.dx_, sizeof(double) * N));
+        HMEC_CUDA(ctx, cudaMalloc(&L.dr, sizeof(double) * std::max(N, (size_t)L.nbnd)));
+    }
+    if (coarse) {
+        const size_t nb = (size_t)g.Nx * g.Ny, ns = (size_t)g.Nx1 * g.Ny1;
+        auto mk = [&](size_t n) -> double* {
+            double* p = nullptr;
+            if (cudaMalloc(&p, sizeof(double) * n) != cudaSuccess) return nullptr;
+            cudaMemset(p, 0, sizeof(double) * n);
+            L.owned.push_back(p);
+            return p;
+        };
+        AsmFields& a = L.af;
+        memset(&a, 0, sizeof(a));
+        a.ETA = mk(nb);
+        a.GGG = mk(nb);
+        a.RHO = mk(nb);
+        a.ETAP = mk(ns);
+        a.GGGP = mk(ns);
+        a.ETAB = mk(ns);
+        a.POR = mk(ns);
+        a.GGGB = mk(ns);
+        a.RHOX = mk(ns);
+        a.RHOFX = mk(ns);
+        a.PORX = mk(ns);
+        a.ETADX = mk(ns);
+        a.RHOY = mk(ns);
+        a.RHOFY = mk(ns);
+        a.PORY = mk(ns);
+        a.ETADY = mk(ns);
+        for (double* p : L.owned)
+            if (!p) {
+                ctx->err = "cudaMalloc failed for a coarse level";
+                return HMEC_ERR_NOMEM;
+            }
+    }
+    return HMEC_OK;
+}
+
+int solver_alloc(hmec_ctx* ctx) {
+    Solver& sv = ctx->sv;
+    const hmec_params& p = ctx->p;
+    const bool mixed = p.form == HMEC_FORM_MIXED;
+    sv.m = std::max(2, p.krylov_restart);
+    sv.N = ctx->g.N;
+    sv.nblk = 152 * 2;
+    // levels: halve while both cell counts are even and the coarse grid keeps >= 4 cells per side
+    Level L0;
+    L0.g = ctx->g;
+    sv.lv.push_back(L0);
+    int nx = ctx->g.Nx, ny = ctx->g.Ny;
+    double xs = p.xsize, ys = p.ysize;
+    while ((int)sv.lv.size() < std::max(1, p.mg_levels)) {
+        const int cx = nx - 1, cy = ny - 1;
+        if ((cx % 2) || (cy % 2) || cx / 2 < 4 || cy / 2 < 4) break;
+        nx = cx / 2 + 1;
+        ny = cy / 2 + 1;
+        Level L;
+        make_geo(L.g, nx, ny, xs, ys);
+        sv.lv.push_back(L);
+    }
+    for (size_t l = 0; l < sv.lv.size(); l++) {
+        int rc = alloc_level(ctx, sv.lv[l], mixed, l > 0);
+        if (rc) return rc;
+    }
+    // fine-level assembly reads the model fields
+    AsmFields& a = sv.lv[0].af;
+    double* const* f = ctx->f;
+    a.ETA = f[HMEC_F_ETA];
+    a.GGG = f[HMEC_F_GGG];
+    a.RHO = f[HMEC_F_RHO];
+    a.SXY0 = f[HMEC_F_SXY0];
+    a.ETAP = f[HMEC_F_ETAP];
+    a.GGGP = f[HMEC_F_GGGP];
+    a.ETAB = f[HMEC_F_ETAB];
+    a.POR = f[HMEC_F_POR];
+    a.GGGB = f[HMEC_F_GGGB];
+    a.SXX0 = f[HMEC_F_SXX0];
+    a.SYY0 = f[HMEC_F_SYY0];
+    a.RHOX = f[HMEC_F_RHOX];
+    a.RHOFX = f[HMEC_F_RHOFX];
+    a.PORX = f[HMEC_F_PORX];
+    a.ETADX = f[HMEC_F_ETADX];
+    a.VX0 = f[HMEC_F_VX0];
+    a.VXF0 = f[HMEC_F_VXF0];
+    a.RHOY = f[HMEC_F_RHOY];
+    a.RHOFY = f[HMEC_F_RHOFY];
+    a.PORY = f[HMEC_F_PORY];
+    a.ETADY = f[HMEC_F_ETADY];
+    a.VY0 = f[HMEC_F_VY0];
+    a.VYF0 = f[HMEC_F_VYF0];
+    a.PT0 = f[HMEC_F_PT0];
+    a.PF0 = f[HMEC_F_PF0];
+    a.DILP = f[HMEC_F_DILP];
+    const size_t N = (size_t)sv.N, m = (size_t)sv.m;
+    HMEC_CUDA(ctx, cudaMalloc(&sv.V, sizeof(double) * (m + 1) * N));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.Z, sizeof(double) * m * N));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.w, sizeof(double) * N));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.H, sizeof(double) * (m + 1) * m));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.cs, sizeof(double) * (m + 1)));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.sn, sizeof(double) * (m + 1)));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.gvec, sizeof(double) * (m + 2)));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.yvec, sizeof(double) * (m + 1)));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.partial, sizeof(double) * (m + 2) * (size_t)sv.nblk));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.dots, sizeof(double) * (2 * m + 4)));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.bnorm, sizeof(double) * 2));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.done, sizeof(int) * 2));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.kcur, sizeof(int) * 2));
+    HMEC_CUDA(ctx, cudaMemset(sv.done, 0, sizeof(int) * 2));
+    return HMEC_OK;
+}
+
+void solver_free(hmec_ctx* ctx) {
+    Solver& sv = ctx->sv;
+    for (Level& L : sv.lv) {
+        cudaFree(L.col);
+        cudaFree(L.val);
+        cudaFree(L.val32);
+        cudaFree(L.dscale);
+        cudaFree(L.bnd_rows);
+        cudaFree(L.pinv);
+        cudaFree(L.pinv32);
+        cudaFree(L.dx_);
+        cudaFree(L.db);
+        cudaFree(L.dr);
+        cudaFree(L.fx);
+        cudaFree(L.fb);
+        cudaFree(L.fr);
+        for (double* p : L.owned) cudaFree(p);
+    }
+    sv.lv.clear();
+    cudaFree(sv.V);
+    cudaFree(sv.Z);
+    cudaFree(sv.w);
+    cudaFree(sv.H);
+    cudaFree(sv.cs);
+    cudaFree(sv.sn);
+    cudaFree(sv.gvec);
+    cudaFree(sv.yvec);
+    cudaFree(sv.partial);
+    cudaFree(sv.dots);
+    cudaFree(sv.bnorm);
+    cudaFree(sv.done);
+    cudaFree(sv.kcur);
+}
+
+static inline dim3 sgrid(const Geo& g) { return dim3(nblocks(g.Ny1, 64), g.Nx1); }
+
+int solver_setup(hmec_ctx* ctx) {
+    Solver& sv = ctx->sv;
+    const bool mixed = ctx->p.form == HMEC_FORM_MIXED;
+    int* status = &ctx->ds->status;
+    for (size_t l = 0; l < sv.lv.size(); l++) {
+        Level& L = sv.lv[l];
+        if (l > 0) {
+            Level& F = sv.lv[l - 1];
+            CoefIn ci{F.af.ETA, F.af.GGG, F.af.RHO, F.af.ETAP, F.af.GGGP, F.af.ETAB, F.af.POR, F.af.GGGB,
+                      F.af.RHOX, F.af.RHOFX, F.af.PORX, F.af.ETADX, F.af.RHOY, F.af.RHOFY, F.af.PORY, F.af.ETADY};
+            AsmFields& a = L.af;
+            CoefOut co{(double*)a.ETA, (double*)a.GGG, (double*)a.RHO, (double*)a.ETAP, (double*)a.GGGP,
+                       (double*)a.ETAB, (double*)a.POR, (double*)a.GGGB, (double*)a.RHOX, (double*)a.RHOFX,
+                       (double*)a.PORX, (double*)a.ETADX, (double*)a.RHOY, (double*)a.RHOFY, (double*)a.PORY,
+                       (double*)a.ETADY};
+            HMEC_LAUNCH(ctx, k_coarsen_coef, sgrid(L.g), 64, 0, F.g, L.g, ci, co);
+            launch_assemble(ctx, L.g, L.af, L.col, L.val, L.dscale, nullptr, nullptr, nullptr);
+        }
+        HMEC_LAUNCH(ctx, k_vanka_setup, nblocks(L.npatch, 64), 64, 0, L.g, L.col, L.val, L.pinv, L.pinv32, status);
+        if (mixed) {
+            const size_t n = (size_t)HMEC_W * L.g.N;
+            HMEC_LAUNCH(ctx, (k_convert<double, float>), nblocks(n, 256), 256, 0, n, L.val, L.val32);
+        }
+    }
+    HMEC_CUDA(ctx, cudaGetLastError());
+    return HMEC_OK;
+}
+
+// One smoothing sweep on level L (9 colour classes + boundary rows).
+template <typename T>
+static void vanka_sweep(hmec_ctx* ctx, Level& L, const T* val, const T* pinv, const T* b, T* x, T* tmp) {
+    const Geo& g = L.g;
+    for (int ri = 0; ri < 3; ri++)
+        for (int rj = 0; rj < 3; rj++) {
+            const int fi = ri == 0 ? 3 : ri, fj = rj == 0 ? 3 : rj;
+            const int ni = (g.Ny - 1 - fi) >= 0 ? (g.Ny - 1 - fi) / 3 + 1 : 0;
+            const int nj = (g.Nx - 1 - fj) >= 0 ? (g.Nx - 1 - fj) / 3 + 1 : 0;
+            if (ni * nj == 0) continue;
+            // algorithmic bytes per patch: its 10 ELL rows (values + columns), the
+            // 10x10 inverse, 10 rhs entries, 10 unknowns read and written
+            const double bpp = 10.0 * HMEC_W * (sizeof(T) + 4) + 100.0 * sizeof(T) + 30.0 * sizeof(T);
+            HMEC_LAUNCH_B(ctx, bpp * ni * nj, k_vanka_color<T>, nblocks((long long)ni * nj, 64), 64, 0, g, L.col, val,
+                          pinv, b, x, ri, rj);
+        }
+    HMEC_LAUNCH(ctx, k_bnd_delta<T>, nblocks(L.nbnd, 128), 128, 0, g.N, L.bnd_rows, L.nbnd, L.col, val, b, x, tmp);
+    HMEC_LAUNCH(ctx, k_bnd_apply<T>, nblocks(L.nbnd, 128), 128, 0, L.bnd_rows, L.nbnd, tmp, x);
+}
+
+template <typename T>
+struct LvPtr;
+template <>
+struct LvPtr<double> {
+    static double* x(Level& L) { return L.dx_; }
+    static double* b(Level& L) { return L.db; }
+    static double* r(Level& L) { return L.dr; }
+    static const double* val(Level& L) { return L.val; }
+    static const double* pinv(Level& L) { return L.pinv; }
+};
+template <>
+struct LvPtr<float> {
+    static float* x(Level& L) { return L.fx; }
+    static float* b(Level& L) { return L.fb; }
+    static float* r(Level& L) { return L.fr; }
+    static const float* val(Level& L) { return L.val32; }
+    static const float* pinv(Level& L) { return L.pinv32; }
+};
+
+// V-cycle on level l for A x = b with x = 0 on entry.
+template <typename T>
+static void vcycle(hmec_ctx* ctx, size_t l) {
+    Solver& sv = ctx->sv;
+    Level& L = sv.lv[l];
+    const hmec_params& p = ctx->p;
+    T* x = LvPtr<T>::x(L);
+    T* b = LvPtr<T>::b(L);
+    T* r = LvPtr<T>::r(L);
+    const T* val = LvPtr<T>::val(L);
+    const T* pinv = LvPtr<T>::pinv(L);
+    const size_t N = (size_t)L.g.N;
+    HMEC_LAUNCH(ctx, k_zero<T>, nblocks(N, 256), 256, 0, N, x);
+    if (l + 1 == sv.lv.size()) {
+        const int ns = (sv.lv.size() == 1) ? std::max(1, p.mg_pre + p.mg_post) : std::max(1, p.mg_coarse_sweeps);
+        for (int s = 0; s < ns; s++) vanka_sweep<T>(ctx, L, val, pinv, b, x, r);
+        return;
+    }
+    for (int s = 0; s < p.mg_pre; s++) vanka_sweep<T>(ctx, L, val, pinv, b, x, r);
+    Level& C = sv.lv[l + 1];
+    HMEC_LAUNCH(ctx, k_residual<T>, nblocks(N, 256), 256, 0, L.g.N, L.col, val, b, x, r);
+    HMEC_LAUNCH(ctx, k_restrict<T>, sgrid(C.g), 64, 0, L.g, C.g, r, L.dscale, C.dscale, LvPtr<T>::b(C));
+    vcycle<T>(ctx, l + 1);
+    HMEC_LAUNCH(ctx, k_prolong<T>, sgrid(L.g), 64, 0, L.g, C.g, LvPtr<T>::x(C), x);
+    for (int s = 0; s < p.mg_post; s++) vanka_sweep<T>(ctx, L, val, pinv, b, x, r);
+}
+
+// z = M^{-1} v on the fine level (v, z FP64 vectors of the scaled system)
+static int precondition(hmec_ctx* ctx, const double* v, double* z) {
+    Solver& sv = ctx->sv;
+    Level& L = sv.lv[0];
+    const size_t N = (size_t)L.g.N;
+    if (ctx->p.form == HMEC_FORM_MIXED) {
+        HMEC_LAUNCH(ctx, (k_convert<double, float>), nblocks(N, 256), 256, 0, N, v, L.fb);
+        vcycle<float>(ctx, 0);
+        HMEC_LAUNCH(ctx, (k_convert<float, double>), nblocks(N, 256), 256, 0, N, L.fx, z);
+    } else {
+        // the fine-level rhs buffer holds the system rhs, so the V-cycle runs on a copy
+        double* keep_b = L.db;
+        L.db = const_cast<double*>(v);
+        vcycle<double>(ctx, 0);
+        L.db = keep_b;
+        HMEC_CUDA(ctx, cudaMemcpyAsync(z, L.dx_, sizeof(double) * N, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    return HMEC_OK;
+}
+
+int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
+    Solver& sv = ctx->sv;
+    Level& L0 = sv.lv[0];
+    const int N = sv.N, m = sv.m, nblk = sv.nblk;
+    const double rtol = ctx->p.krylov_rtol;
+    const int maxit = std::max(1, ctx->p.krylov_maxit);
+    double* x = ctx->S;
+    const double* b = L0.db;
+    Gm G{sv.H, sv.cs, sv.sn, sv.gvec, sv.yvec, sv.dots, sv.bnorm, sv.done, sv.kcur, ctx->ds};
+    HMEC_CUDA(ctx, cudaMemsetAsync(&ctx->ds->krylov_iters, 0, sizeof(int), ctx->stream));
+    int total = 0;
+    bool first = true;
+    bool converged = false;
+    const int check_every = 8;
+    double* r = sv.w;
+    while (true) {
+        HMEC_LAUNCH(ctx, k_true_resid, nblk, RED_BS, 0, N, L0.col, L0.val, b, x, r, sv.partial, nblk);
+        HMEC_LAUNCH(ctx, k_cycle_begin, 1, 1, 0, G, sv.partial, nblk, first ? 1 : 0, rtol, m);
+        first = false;
+        HMEC_LAUNCH(ctx, k_scale_vec, nblocks(N, 256), 256, 0, N, r, sv.dots, sv.V, sv.done);
+        for (int j = 0; j < m && total + j < maxit; j++) {
+            double* Vj = sv.V + (size_t)j * N;
+            double* Zj = sv.Z + (size_t)j * N;
+            // preconditioner (skipped cheaply when converged: its kernels are not predicated,
+            // so check the flag before launching a whole V-cycle)
+            if (j > 0 && (j % check_every) == 0) {
+                int hd = 0;
+                HMEC_CUDA(ctx, cudaMemcpyAsync(&ctx->hs->pad0, sv.done, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+                HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+                hd = ctx->hs->pad0;
+                if (hd) break;
+            }
+            int prc = precondition(ctx, Vj, Zj);
+            if (prc) return prc;
+            HMEC_LAUNCH_B(ctx, (double)N * (HMEC_W * 12.0 + 16.0), k_spmv, nblocks(N, 256), 256, 0, N, L0.col, L0.val,
+                          Zj, sv.w, sv.done);
+            // CGS pass 1
+            HMEC_LAUNCH(ctx, k_dots, dim3(nblk, j + 1), RED_BS, 0, N, sv.V, sv.w, sv.partial, nblk, sv.done);
+            HMEC_LAUNCH(ctx, k_dots_final, j + 1, 32, 0, sv.partial, nblk, j + 1, sv.dots + m + 2, sv.done);
+            HMEC_LAUNCH(ctx, k_orth_update, nblk, RED_BS, 0, N, sv.V, j + 1, sv.dots + m + 2, sv.w, sv.partial, nblk, sv.done);
+            // CGS pass 2
+            HMEC_LAUNCH(ctx, k_dots, dim3(nblk, j + 1), RED_BS, 0, N, sv.V, sv.w, sv.partial, nblk, sv.done);
+            HMEC_LAUNCH(ctx, k_dots_final, j + 1, 32, 0, sv.partial, nblk, j + 1, sv.dots, sv.done);
+            HMEC_LAUNCH(ctx, k_orth_update, nblk, RED_BS, 0, N, sv.V, j + 1, sv.dots, sv.w, sv.partial, nblk, sv.done);
+            HMEC_LAUNCH(ctx, k_arnoldi_step, 1, 1, 0, G, sv.dots + m + 2, sv.partial, nblk, j, m, rtol, sv.dots + 2 * m + 3);
+            HMEC_LAUNCH(ctx, k_scale_vec, nblocks(N, 256), 256, 0, N, sv.w, sv.dots + 2 * m + 3, sv.V + (size_t)(j + 1) * N, sv.done);
+        }
+        HMEC_LAUNCH(ctx, k_lsq, 1, 1, 0, G, m);
+        HMEC_LAUNCH(ctx, k_xupdate, nblocks(N, 256), 256, 0, N, sv.Z, sv.yvec, sv.kcur, x);
+        HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->hs, ctx->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream));
+        HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        total = ctx->hs->krylov_iters;
+        if (ctx->hs->krylov_relres <= rtol) {
+            // confirm with the true residual
+            HMEC_LAUNCH(ctx, k_true_resid, nblk, RED_BS, 0, N, L0.col, L0.val, b, x, r, sv.partial, nblk);
+            HMEC_LAUNCH(ctx, k_cycle_begin, 1, 1, 0, G, sv.partial, nblk, 0, rtol, m);
+            HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->hs, ctx->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream));
+            HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            if (ctx->hs->krylov_relres <= rtol) {
+                converged = true;
+                break;
+            }
+        }
+        if (total >= maxit || !std::isfinite(ctx->hs->krylov_relres)) break;
+    }
+    if (iters_out) *iters_out = total;
+    if (relres_out) *relres_out = ctx->hs->krylov_relres;
+    if (!converged) {
+        HMEC_CUDA(ctx, cudaMemcpyAsync(&ctx->hs->pad0, &ctx->ds->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return HMEC_ERR_KRYLOV_NOCONV;
+    }
+    return HMEC_OK;
+}

@@ -1,0 +1,331 @@
+"""hmec -- Python host binding of libhmec_gpu.so (GB300 H-MEC hot path).
+
+A thin ctypes layer over the C ABI of include/hmec.h.  ``Model`` mirrors the
+sections of the reference's main() (cpp/h_mec_rsf_v9.cpp:376-1726) one to one:
+markers_to_nodes, timestep_begin, global_iteration, timestep_end,
+advect_markers, or the whole ``timestep``.  There is no CPU fallback: if the
+CUDA library is missing or cannot load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from . import build as _build
+from . import synth  # noqa: F401  (initial states)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_ROOT = os.path.dirname(os.path.dirname(_HERE))
+HEADER = os.path.join(_ROOT, "include", "hmec.h")
+
+HMEC_OK = 0
+STATUS = {0: "HMEC_OK", -1: "HMEC_ERR_ARG", -2: "HMEC_ERR_CUDA", -3: "HMEC_ERR_BOUNDS", -4: "HMEC_ERR_NAN",
+          -5: "HMEC_ERR_RSF_NOCONV", -6: "HMEC_ERR_KRYLOV_NOCONV", -7: "HMEC_ERR_NOMEM", -8: "HMEC_ERR_STATE"}
+FORM_FP64, FORM_MIXED = 0, 1
+
+
+class HmecError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (STATUS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Params(C.Structure):
+    """ctypes mirror of ``hmec_params``."""
+
+    _fields_ = [
+        ("Nx", C.c_int32), ("Ny", C.c_int32), ("xsize", C.c_double), ("ysize", C.c_double),
+        ("mx", C.c_int32), ("my", C.c_int32),
+        ("TS_1", C.c_double), ("TS_2", C.c_double), ("TS_3", C.c_double), ("TS_4", C.c_double),
+        ("dtelastic0", C.c_double), ("dtmin", C.c_double), ("inertia", C.c_double),
+        ("arsfm", C.c_double * 2), ("brsfm", C.c_double * 2), ("lrsfm", C.c_double * 2), ("omm", C.c_double * 2),
+        ("V0", C.c_double), ("alpha", C.c_double),
+        ("POR0", C.c_double), ("cohes", C.c_double), ("friction", C.c_double), ("dilatation", C.c_double),
+        ("tensile", C.c_double), ("shearmod", C.c_double), ("BETAFLUID", C.c_double), ("BETASOLID", C.c_double),
+        ("gx", C.c_double), ("gy", C.c_double), ("PCONF", C.c_double), ("PTFDIFF", C.c_double),
+        ("etamin", C.c_double), ("etamax", C.c_double), ("kkkmin", C.c_double), ("kkkmax", C.c_double),
+        ("stpmax", C.c_double), ("stpmax1", C.c_double),
+        ("bcupper", C.c_double), ("bclower", C.c_double), ("bcvyflower", C.c_double),
+        ("niterglobal", C.c_int32), ("ynlastmax", C.c_int32), ("dtstep", C.c_int32),
+        ("vratiomax", C.c_double), ("dtkoef", C.c_double), ("dtkoefup", C.c_double), ("dtkoefv", C.c_double),
+        ("errmin", C.c_double), ("etawt", C.c_double), ("syieldmin", C.c_double), ("tyield", C.c_double),
+        ("num_timesteps", C.c_int32),
+        ("form", C.c_int32), ("krylov_rtol", C.c_double), ("krylov_restart", C.c_int32),
+        ("krylov_maxit", C.c_int32), ("mg_levels", C.c_int32), ("mg_pre", C.c_int32), ("mg_post", C.c_int32),
+        ("mg_coarse_sweeps", C.c_int32), ("rsf_maxit", C.c_int32), ("advect_markers", C.c_int32),
+        ("rk4_as_written", C.c_int32), ("quirk_accumulate_sums", C.c_int32), ("bounds_check", C.c_int32),
+    ]
+
+
+class IterReport(C.Structure):
+    _fields_ = [("iterstep", C.c_int32), ("stop", C.c_int32), ("ynpl", C.c_int32), ("krylov_iters", C.c_int32),
+                ("dt", C.c_double), ("DSYLSQ", C.c_double), ("ptscale", C.c_double), ("pfscale", C.c_double),
+                ("Vmax", C.c_double), ("krylov_relres", C.c_double)]
+
+
+class StepReport(C.Structure):
+    _fields_ = [("timestep", C.c_int32), ("global_iters", C.c_int32), ("ynlast", C.c_int32),
+                ("krylov_iters", C.c_int32), ("status", C.c_int32), ("timesum", C.c_double), ("dt", C.c_double),
+                ("Vmax", C.c_double), ("max_krylov_relres", C.c_double)]
+
+
+def _xlist(macro: str):
+    text = open(HEADER).read()
+    start = text.index("#define %s(X)" % macro)
+    body = []
+    for line in text[start:].splitlines()[1:]:
+        body.append(line)
+        if not line.rstrip().endswith("\\"):
+            break
+    return re.findall(r"X\((\w+)", " ".join(body))
+
+
+FIELDS = _xlist("HMEC_FIELD_LIST")
+MARKERS = _xlist("HMEC_MARKER_LIST")
+SCALARS = _xlist("HMEC_SCALAR_LIST")
+
+#: every entry point include/hmec.h declares
+EXPORTS = ["hmec_abi_version", "hmec_params_default", "hmec_field_name", "hmec_field_grid", "hmec_marker_name",
+           "hmec_scalar_name", "hmec_marknum", "hmec_create", "hmec_destroy", "hmec_last_error",
+           "hmec_upload_markers", "hmec_download_markers", "hmec_upload_field", "hmec_download_field",
+           "hmec_set_scalar", "hmec_get_scalar", "hmec_markers_to_nodes", "hmec_timestep_begin",
+           "hmec_global_iteration", "hmec_timestep_end", "hmec_advect_markers", "hmec_timestep",
+           "hmec_assemble_csr", "hmec_solve_system", "hmec_kernel_launches", "hmec_synchronize", "hmec_stream",
+           "hmec_profile_kernel", "hmec_profile_read"]
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libhmec_gpu.so (building it first if needed); raises if impossible."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError("libhmec_gpu.so is not built (%s)" % path)
+        _build.build()
+    L = C.CDLL(path)
+    P = C.POINTER
+    vp = C.c_void_p
+    L.hmec_abi_version.restype = C.c_int32
+    L.hmec_params_default.argtypes = [P(Params)]
+    L.hmec_params_default.restype = None
+    L.hmec_field_name.argtypes = [C.c_int32]
+    L.hmec_field_name.restype = C.c_char_p
+    L.hmec_field_grid.argtypes = [C.c_int32]
+    L.hmec_field_grid.restype = C.c_int32
+    L.hmec_marker_name.argtypes = [C.c_int32]
+    L.hmec_marker_name.restype = C.c_char_p
+    L.hmec_scalar_name.argtypes = [C.c_int32]
+    L.hmec_scalar_name.restype = C.c_char_p
+    L.hmec_marknum.argtypes = [P(Params)]
+    L.hmec_marknum.restype = C.c_int64
+    L.hmec_create.argtypes = [P(Params), P(C.c_int32)]
+    L.hmec_create.restype = vp
+    L.hmec_destroy.argtypes = [vp]
+    L.hmec_destroy.restype = None
+    L.hmec_last_error.argtypes = [vp]
+    L.hmec_last_error.restype = C.c_char_p
+    L.hmec_upload_markers.argtypes = [vp, P(P(C.c_double)), C.c_int64]
+    L.hmec_download_markers.argtypes = [vp, P(P(C.c_double)), C.c_int64]
+    L.hmec_upload_field.argtypes = [vp, C.c_int32, P(C.c_double), C.c_int32, C.c_int32]
+    L.hmec_download_field.argtypes = [vp, C.c_int32, P(C.c_double), C.c_int32, C.c_int32]
+    L.hmec_set_scalar.argtypes = [vp, C.c_int32, C.c_double]
+    L.hmec_get_scalar.argtypes = [vp, C.c_int32, P(C.c_double)]
+    for fn in ("hmec_markers_to_nodes", "hmec_timestep_begin", "hmec_timestep_end", "hmec_advect_markers",
+               "hmec_synchronize"):
+        getattr(L, fn).argtypes = [vp]
+        getattr(L, fn).restype = C.c_int32
+    L.hmec_global_iteration.argtypes = [vp, P(IterReport)]
+    L.hmec_timestep.argtypes = [vp, P(StepReport)]
+    L.hmec_assemble_csr.argtypes = [vp, P(C.c_int64), P(C.c_int32), P(C.c_double), P(C.c_double), P(C.c_int64),
+                                    P(C.c_double), P(C.c_double)]
+    L.hmec_solve_system.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_int32), P(C.c_double)]
+    L.hmec_kernel_launches.argtypes = [vp]
+    L.hmec_kernel_launches.restype = C.c_int64
+    L.hmec_stream.argtypes = [vp]
+    L.hmec_stream.restype = vp
+    L.hmec_profile_kernel.argtypes = [vp, C.c_char_p]
+    L.hmec_profile_read.argtypes = [vp, P(C.c_int64), P(C.c_double), P(C.c_double)]
+    _lib = L
+    return L
+
+
+def default_params(**over) -> Params:
+    p = Params()
+    load().hmec_params_default(C.byref(p))
+    for k, v in over.items():
+        cur = getattr(p, k)
+        if isinstance(cur, C.Array):
+            for i, x in enumerate(v):
+                cur[i] = x
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Model:
+    """One model instance on the current CUDA device (a context of the C ABI)."""
+
+    def __init__(self, params: Params):
+        self.L = load()
+        self.params = params
+        st = C.c_int32(0)
+        self.h = self.L.hmec_create(C.byref(params), C.byref(st))
+        if not self.h:
+            raise HmecError(st.value, "hmec_create failed")
+        self.Nx, self.Ny = params.Nx, params.Ny
+        self.N = (self.Nx + 1) * (self.Ny + 1) * 6
+        self.marknum = self.L.hmec_marknum(C.byref(params))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hmec_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != HMEC_OK:
+            msg = self.L.hmec_last_error(self.h)
+            raise HmecError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    # ------------------------------------------------------------ data
+    def shape(self, name):
+        g = self.L.hmec_field_grid(FIELDS.index(name))
+        return (self.Ny + g, self.Nx + g)
+
+    def upload_markers(self, arrays: dict):
+        bufs = [np.ascontiguousarray(arrays[k], dtype=np.float64) for k in MARKERS]
+        for b in bufs:
+            if b.shape != (self.marknum,):
+                raise ValueError("marker arrays must have length %d" % self.marknum)
+        ptrs = (C.POINTER(C.c_double) * len(bufs))(*[_dptr(b) for b in bufs])
+        self._check(self.L.hmec_upload_markers(self.h, ptrs, self.marknum), "upload_markers")
+
+    def download_markers(self) -> dict:
+        bufs = [np.empty(self.marknum) for _ in MARKERS]
+        ptrs = (C.POINTER(C.c_double) * len(bufs))(*[_dptr(b) for b in bufs])
+        self._check(self.L.hmec_download_markers(self.h, ptrs, self.marknum), "download_markers")
+        return dict(zip(MARKERS, bufs))
+
+    def upload_field(self, name, arr):
+        r, c = self.shape(name)
+        a = np.asfortranarray(np.asarray(arr, dtype=np.float64).reshape(r, c))
+        buf = a.ravel(order="F")
+        self._check(self.L.hmec_upload_field(self.h, FIELDS.index(name), _dptr(buf), r, c), "upload_field")
+
+    def field(self, name) -> np.ndarray:
+        r, c = self.shape(name)
+        buf = np.empty(r * c)
+        self._check(self.L.hmec_download_field(self.h, FIELDS.index(name), _dptr(buf), r, c), "download_field")
+        return buf.reshape((r, c), order="F")
+
+    def set_scalar(self, name, v):
+        self._check(self.L.hmec_set_scalar(self.h, SCALARS.index(name), float(v)), "set_scalar")
+
+    def scalar(self, name) -> float:
+        v = C.c_double()
+        self._check(self.L.hmec_get_scalar(self.h, SCALARS.index(name), C.byref(v)), "get_scalar")
+        return v.value
+
+    def load_state(self, snap: dict):
+        for f in FIELDS:
+            if f in snap:
+                self.upload_field(f, snap[f])
+        for s in SCALARS:
+            if "scalar_" + s in snap:
+                self.set_scalar(s, snap["scalar_" + s])
+
+    def snapshot(self) -> dict:
+        out = {f: self.field(f) for f in FIELDS}
+        out.update({"scalar_" + s: self.scalar(s) for s in SCALARS})
+        return out
+
+    # -------------------------------------------------------- sections
+    def markers_to_nodes(self):
+        self._check(self.L.hmec_markers_to_nodes(self.h), "markers_to_nodes")
+
+    def timestep_begin(self):
+        self._check(self.L.hmec_timestep_begin(self.h), "timestep_begin")
+
+    def global_iteration(self) -> dict:
+        rep = IterReport()
+        self._check(self.L.hmec_global_iteration(self.h, C.byref(rep)), "global_iteration")
+        return {k: getattr(rep, k) for k, _ in IterReport._fields_}
+
+    def timestep_end(self):
+        self._check(self.L.hmec_timestep_end(self.h), "timestep_end")
+
+    def advect_markers(self):
+        self._check(self.L.hmec_advect_markers(self.h), "advect_markers")
+
+    def timestep(self, check=True) -> dict:
+        rep = StepReport()
+        rc = self.L.hmec_timestep(self.h, C.byref(rep))
+        if check:
+            self._check(rc, "timestep")
+        d = {k: getattr(rep, k) for k, _ in StepReport._fields_}
+        d["rc"] = rc
+        return d
+
+    def synchronize(self):
+        self._check(self.L.hmec_synchronize(self.h), "synchronize")
+
+    @property
+    def launches(self) -> int:
+        return self.L.hmec_kernel_launches(self.h)
+
+    @property
+    def stream_ptr(self) -> int:
+        """cudaStream_t of the context (for CUDA-event timing)."""
+        return self.L.hmec_stream(self.h) or 0
+
+    def profile_kernel(self, name):
+        self._check(self.L.hmec_profile_kernel(self.h, name.encode() if name else None), "profile_kernel")
+
+    def profile_read(self):
+        n, ms, b = C.c_int64(), C.c_double(), C.c_double()
+        self._check(self.L.hmec_profile_read(self.h, C.byref(n), C.byref(ms), C.byref(b)), "profile_read")
+        return n.value, ms.value, b.value
+
+    # ---------------------------------------------------------- hooks
+    def assemble_csr(self):
+        import scipy.sparse as sp
+
+        nnz = C.c_int64()
+        self._check(self.L.hmec_assemble_csr(self.h, None, None, None, None, C.byref(nnz), None, None), "assemble_csr")
+        n = self.N
+        indptr = np.zeros(n + 1, dtype=np.int64)
+        indices = np.zeros(nnz.value, dtype=np.int32)
+        data = np.zeros(nnz.value)
+        rhs = np.zeros(n)
+        pt, pf = C.c_double(), C.c_double()
+        self._check(self.L.hmec_assemble_csr(self.h, indptr.ctypes.data_as(C.POINTER(C.c_int64)),
+                                             indices.ctypes.data_as(C.POINTER(C.c_int32)), _dptr(data), _dptr(rhs),
+                                             C.byref(nnz), C.byref(pt), C.byref(pf)), "assemble_csr")
+        return sp.csr_matrix((data, indices, indptr), shape=(n, n)), rhs, pt.value, pf.value
+
+    def solve_system(self, rhs, x0=None):
+        b = np.ascontiguousarray(rhs, dtype=np.float64)
+        x = np.zeros(self.N) if x0 is None else np.array(x0, dtype=np.float64)
+        its, rel = C.c_int32(), C.c_double()
+        rc = self.L.hmec_solve_system(self.h, _dptr(b), _dptr(x), C.byref(its), C.byref(rel))
+        return x, its.value, rel.value, rc

@@ -235,6 +235,16 @@ int32_t hmec_assemble_csr(hmec_ctx* ctx, int64_t* indptr, int32_t* indices, doub
  * the configured solver for the given right-hand side; x holds the initial
  * guess on entry and the solution on return.                                 */
 int32_t hmec_solve_system(hmec_ctx* ctx, const double* rhs, double* x, int32_t* iters, double* relres);
+/* The CUDA stream (cudaStream_t) the context launches on, for timing with
+ * CUDA events (no counterpart in the reference). */
+void* hmec_stream(hmec_ctx* ctx);
+/* Time every launch of the kernel family whose name starts with `name`
+ * (NULL: stop) with CUDA events on the context stream, and accumulate the
+ * algorithmic bytes those launches move; read and reset with
+ * hmec_profile_kernel().  Used by the benchmark's live roofline (no
+ * counterpart in the reference).                                           */
+int32_t hmec_profile_kernel(hmec_ctx* ctx, const char* name);
+int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, double* bytes);
 /* Device-kernel launches issued since hmec_create. */
 int64_t hmec_kernel_launches(const hmec_ctx* ctx);
 /* Synchronise the context stream. */

@@ -1,0 +1,212 @@
+"""Parity of the GPU library (through its C ABI) with the CPU oracle.
+
+Tolerances: integer/index work bit-exact; node interpolation and assembly
+entries to 1e-13 (summation order differs from the reference's serial
+marker order); solves and whole timesteps 1e-10 relative in velocity,
+pressure, stress and slip rate against the oracle's direct solve, for the
+plain FP64 form and for the mixed form (its FP32 multigrid only
+preconditions an FP64 FGMRES, so the answer carries the FP64 tolerance).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import hmec
+import oracle as O
+import pairs
+from pairs import P2G_FIELDS
+
+pytestmark = pytest.mark.gpu
+
+TOL_STEP = 1e-10
+
+
+def grouped(m, o, fields_a=None):
+    return pairs.group_errors(m, o)
+
+
+@pytest.mark.parametrize("preset", ["tiny", "c0", "ref"])
+def test_p2g_parity(preset):
+    o, mk, nodes = pairs.oracle_for(preset)
+    m = pairs.model_for(preset, mk, nodes)
+    o.markers_to_nodes()
+    m.markers_to_nodes()
+    e = pairs.field_errors(m, o, P2G_FIELDS)
+    assert max(e.values()) < 1e-13, e
+
+
+def test_p2g_deterministic_and_jitter():
+    o, mk, nodes = pairs.oracle_for("c0")  # jittered markers, per-marker permeability
+    m = pairs.model_for("c0", mk, nodes)
+    m.markers_to_nodes()
+    a = {f: m.field(f) for f in P2G_FIELDS}
+    m.markers_to_nodes()
+    b = {f: m.field(f) for f in P2G_FIELDS}
+    for f in P2G_FIELDS:
+        assert np.array_equal(a[f], b[f]), f
+
+
+@pytest.mark.parametrize("preset,steps", [("tiny", 0), ("tiny", 3), ("c0", 3)])
+def test_assembly_parity(preset, steps):
+    o, mk, nodes = pairs.oracle_for(preset)
+    for _ in range(steps):
+        o.timestep()
+    m = pairs.model_for(preset, mk, nodes)
+    m.load_state(o.snapshot())
+    o.markers_to_nodes()
+    m.markers_to_nodes()
+    o.timestep_begin()
+    m.timestep_begin()
+    o.iter_prepare()
+    A, R = o.assemble()
+    Ag, Rg, pt, pf = m.assemble_csr()
+    assert Ag.nnz == A.nnz
+    assert np.array_equal(A.indptr, Ag.indptr) and np.array_equal(A.indices, Ag.indices)
+    rowmax = np.maximum(abs(A).max(axis=1).toarray().ravel(), 1e-300)
+    D = abs(Ag - A).max(axis=1).toarray().ravel()
+    assert np.max(D / rowmax) < 1e-13
+    assert np.max(np.abs(Rg - R) / np.maximum(np.abs(R), 1e-300)) < 1e-13
+    assert pf == pytest.approx(o.scales()[0], rel=1e-15) and pt == pf
+
+
+@pytest.mark.parametrize("form", [hmec.FORM_FP64, hmec.FORM_MIXED])
+@pytest.mark.parametrize("preset", ["tiny", "c0"])
+def test_solve_parity(preset, form):
+    o, mk, nodes = pairs.oracle_for(preset)
+    for _ in range(3):
+        o.timestep()
+    m = pairs.model_for(preset, mk, nodes, form=form)
+    m.load_state(o.snapshot())
+    o.markers_to_nodes()
+    m.markers_to_nodes()
+    o.timestep_begin()
+    m.timestep_begin()
+    o.iter_prepare()
+    A, R = o.assemble()
+    x = O.direct_solve(A, R)
+    Ag, Rg, _, _ = m.assemble_csr()
+    xg, its, rel, rc = m.solve_system(Rg)
+    assert rc == 0, (its, rel)
+    err = pairs.solution_errors(xg, x)
+    assert max(err.values()) < TOL_STEP, err
+
+
+@pytest.mark.parametrize("form", [hmec.FORM_FP64, hmec.FORM_MIXED])
+@pytest.mark.parametrize("preset,nsteps", [("tiny", 6), ("c0", 5)])
+def test_timestep_replay(preset, nsteps, form):
+    """Each step starts the GPU from the oracle's state and compares after one step."""
+    o, mk, nodes = pairs.oracle_for(preset)
+    m = pairs.model_for(preset, mk, nodes, form=form)
+    for _ in range(nsteps):
+        m.load_state(o.snapshot())
+        o.timestep()
+        rep = m.timestep()
+        assert rep["rc"] == 0
+        assert m.scalar("timestep") == o.scalar("timestep")
+        assert m.scalar("dt") == pytest.approx(o.scalar("dt"), rel=1e-12)
+        assert m.scalar("timesum") == pytest.approx(o.scalar("timesum"), rel=1e-12)
+        err = pairs.group_errors(m, o)
+        assert max(err.values()) < TOL_STEP, err
+
+
+def test_free_running_tiny_matches():
+    o, mk, nodes = pairs.oracle_for("tiny")
+    m = pairs.model_for("tiny", mk, nodes)
+    for s in range(8):
+        it = o.timestep()
+        rep = m.timestep()
+        assert rep["global_iters"] == it, s
+        assert m.scalar("dt") == pytest.approx(o.scalar("dt"), rel=1e-9)
+    err = pairs.group_errors(m, o)
+    assert max(err.values()) < 1e-8, err
+
+
+def test_global_iteration_sections_match_timestep():
+    o, mk, nodes = pairs.oracle_for("tiny")
+    for _ in range(2):
+        o.timestep()
+    snap = o.snapshot()
+    a = pairs.model_for("tiny", mk, nodes)
+    b = pairs.model_for("tiny", mk, nodes)
+    a.load_state(snap)
+    b.load_state(snap)
+    a.timestep()
+    b.markers_to_nodes()
+    b.timestep_begin()
+    n = 0
+    while True:
+        r = b.global_iteration()
+        n += 1
+        if r["stop"] or n > 100:
+            break
+    b.timestep_end()
+    for f in ("pt", "vxs", "SXY", "VSLIPB", "OM0", "ETA00"):
+        assert np.array_equal(a.field(f), b.field(f)), f
+    assert a.scalar("dt") == b.scalar("dt")
+
+
+@pytest.mark.parametrize("as_written", [0, 1])
+def test_advection_parity(as_written):
+    o, mk, nodes = pairs.oracle_for("tiny", advect_markers=1, rk4_as_written=as_written)
+    m = pairs.model_for("tiny", mk, nodes, advect_markers=1, rk4_as_written=as_written)
+    for _ in range(3):
+        m.load_state(o.snapshot())
+        o.timestep()
+        m.timestep()
+    got = m.download_markers()
+    for k in ("xm", "ym", "sxxm", "syym", "sxym"):
+        ref = o.marker(k)
+        den = max(np.max(np.abs(ref)), 1e-300)
+        assert np.max(np.abs(got[k] - ref)) / den < 1e-10, k
+    # markers moved (the reference's loop never runs; this is the enabled form)
+    assert np.max(np.abs(got["xm"] - mk["xm"])) > 0
+
+
+def test_status_rsf_cap_reported_not_hung():
+    o, mk, nodes = pairs.oracle_for("tiny")
+    for _ in range(3):
+        o.timestep()
+    m = pairs.model_for("tiny", mk, nodes, rsf_maxit=1)
+    m.load_state(o.snapshot())
+    rep = m.timestep(check=False)
+    assert rep["rc"] == -5  # HMEC_ERR_RSF_NOCONV
+
+
+def test_status_krylov_cap_reported():
+    o, mk, nodes = pairs.oracle_for("tiny")
+    m = pairs.model_for("tiny", mk, nodes, krylov_maxit=1, krylov_restart=2)
+    rep = m.timestep(check=False)
+    assert rep["rc"] == -6  # HMEC_ERR_KRYLOV_NOCONV
+
+
+def test_status_nan_input_reported():
+    o, mk, nodes = pairs.oracle_for("tiny")
+    bad = dict(mk)
+    bad["etasm"] = mk["etasm"].copy()
+    bad["etasm"][len(bad["etasm"]) // 2] = np.nan
+    bad["etam"] = bad["etasm"].copy()
+    m = pairs.model_for("tiny", bad, nodes, krylov_maxit=50)
+    rep = m.timestep(check=False)
+    assert rep["rc"] in (-4, -6)  # NaN detected in the solution or the solve
+
+
+def test_argument_and_state_errors():
+    o, mk, nodes = pairs.oracle_for("tiny")
+    m = pairs.model_for("tiny", mk, nodes)
+    with pytest.raises(hmec.HmecError) as e:
+        m.global_iteration()  # before timestep_begin
+    assert e.value.code == -8
+    buf = np.zeros(7)
+    rc = m.L.hmec_upload_field(m.h, 0, buf.ctypes.data_as(C.POINTER(C.c_double)), 1, 7)
+    assert rc == -1
+    rc = m.L.hmec_upload_field(m.h, 999, buf.ctypes.data_as(C.POINTER(C.c_double)), 1, 7)
+    assert rc == -1
+
+
+def test_kernels_launch_through_the_library():
+    o, mk, nodes = pairs.oracle_for("tiny")
+    m = pairs.model_for("tiny", mk, nodes)
+    n0 = m.launches
+    m.timestep()
+    assert m.launches > n0 + 20
