@@ -67,8 +67,9 @@ struct Level {
     int32_t* bnd_rows;     // rows outside every patch
     double* pinv;          // Vanka patch inverses, [100][npatch] (FP64 form)
     float* pinv32;         // same in FP32 (mixed form)
-    // work vectors (FP64 form uses d*, mixed form uses f*)
-    double *dx_, *db, *dr;
+    // work vectors (FP64 form uses d*, mixed form uses f*); db of level 0 is
+    // the scaled system rhs, pb the preconditioner input of the FP64 form
+    double *dx_, *db, *dr, *pb;
     float *fx, *fb, *fr;
     // coarse-level coefficient fields (owned for l > 0)
     std::vector<double*> owned;

@@ -12,42 +12,54 @@
 // Preconditioner: one geometric-multigrid V-cycle.  Coarse operators are
 // rediscretised: the node coefficients that enter the assembly are
 // restricted from the fine grid and the same assembly kernel builds the
-// coarse matrix.  The smoother is a multiplicative Vanka smoother on
-// the staggered cell patch {Pt, Pf, 2 vx, 2 vy, 2 vxD, 2 vyD} (10 unknowns),
-// with the 10x10 patch inverses formed once per solve and applied in nine
-// colour classes (patches of one class neither share unknowns nor read
-// each other's), followed by a two-phase Jacobi pass over the boundary
-// rows that no patch covers.  The V-cycle runs in FP64 (HMEC_FORM_FP64) or
-// entirely in FP32 (HMEC_FORM_MIXED); FGMRES stays FP64 either way.
+// coarse matrix.  The smoother is a multiplicative Vanka smoother on the
+// staggered cell patch {Pt, Pf, 2 vx, 2 vy, 2 vxD, 2 vyD} (10 unknowns), with
+// the 10x10 patch inverses formed once per solve.  Patches are applied in nine
+// colour classes (same-class patches neither share unknowns nor read each
+// other's), then a two-phase Jacobi pass covers the boundary rows no patch
+// contains.  A whole smoothing pass -- every sweep, colour and boundary phase
+// -- is ONE cooperative kernel with grid-wide barriers between phases (a
+// single block with __syncthreads on small levels), and half a warp works on
+// one patch (a lane per patch row, shuffles for the 10x10 product), so a
+// V-cycle is about three launches per level.  The V-cycle runs in FP64
+// (HMEC_FORM_FP64) or entirely in FP32 (HMEC_FORM_MIXED); FGMRES stays FP64.
+#include <cooperative_groups.h>
+
 #include "hmec_internal.cuh"
 
 #include <algorithm>
 #include <cmath>
 #include <vector>
 
+namespace cg = cooperative_groups;
+
 namespace {
 
 constexpr int PB = 10;   // patch size
 constexpr int RED_BS = 256;
+constexpr int SM_BS = 256;  // block size of the smoothing kernels
 
 __device__ __forceinline__ int kp_of(int i, int j, int Ny1) { return (j * Ny1 + i) * 6; }
 
-__device__ __forceinline__ void patch_unknowns(int i, int j, int Ny1, int (&u)[PB]) {
-    const int c = kp_of(i, j, Ny1), l = kp_of(i, j - 1, Ny1), t = kp_of(i - 1, j, Ny1);
-    u[0] = c + 0;  // Pt
-    u[1] = c + 3;  // Pf
-    u[2] = l + 1;  // vx left face
-    u[3] = c + 1;  // vx right face
-    u[4] = t + 2;  // vy top face
-    u[5] = c + 2;  // vy bottom face
-    u[6] = l + 4;  // vxD left
-    u[7] = c + 4;  // vxD right
-    u[8] = t + 5;  // vyD top
-    u[9] = c + 5;  // vyD bottom
+// Global index of unknown q of the patch of P cell (i, j).
+__device__ __forceinline__ int patch_unknown(int i, int j, int Ny1, int q) {
+    switch (q) {
+        case 0: return kp_of(i, j, Ny1) + 0;      // Pt
+        case 1: return kp_of(i, j, Ny1) + 3;      // Pf
+        case 2: return kp_of(i, j - 1, Ny1) + 1;  // vx left face
+        case 3: return kp_of(i, j, Ny1) + 1;      // vx right face
+        case 4: return kp_of(i - 1, j, Ny1) + 2;  // vy top face
+        case 5: return kp_of(i, j, Ny1) + 2;      // vy bottom face
+        case 6: return kp_of(i, j - 1, Ny1) + 4;  // vxD left
+        case 7: return kp_of(i, j, Ny1) + 4;      // vxD right
+        case 8: return kp_of(i - 1, j, Ny1) + 5;  // vyD top
+        default: return kp_of(i, j, Ny1) + 5;     // vyD bottom
+    }
 }
 
 // ------------------------------------------------------------ Vanka setup
-// Gauss-Jordan with partial pivoting on the 10x10 patch block of D A.
+// Gauss-Jordan with partial pivoting on the 10x10 patch block of D A;
+// inverses stored patch-major, pinv[p*100 + r*10 + c].
 __global__ void k_vanka_setup(Geo g, const int32_t* __restrict__ col, const double* __restrict__ val,
                               double* pinv, float* pinv32, int* status) {
     const int pi = blockIdx.x * blockDim.x + threadIdx.x;
@@ -55,7 +67,7 @@ __global__ void k_vanka_setup(Geo g, const int32_t* __restrict__ col, const doub
     if (pi >= np) return;
     const int i = 1 + pi % (g.Ny - 1), j = 1 + pi / (g.Ny - 1);
     int u[PB];
-    patch_unknowns(i, j, g.Ny1, u);
+    for (int q = 0; q < PB; q++) u[q] = patch_unknown(i, j, g.Ny1, q);
     double a[PB][PB], b[PB][PB];
     for (int r = 0; r < PB; r++)
         for (int c = 0; c < PB; c++) {
@@ -115,89 +127,154 @@ __global__ void k_vanka_setup(Geo g, const int32_t* __restrict__ col, const doub
     }
     for (int r = 0; r < PB; r++)
         for (int c = 0; c < PB; c++) {
-            const size_t o = (size_t)(r * PB + c) * np + pi;
+            const size_t o = (size_t)pi * 100 + r * PB + c;
             if (pinv) pinv[o] = b[r][c];
             if (pinv32) pinv32[o] = (float)b[r][c];
         }
 }
 
-// One colour class of a multiplicative Vanka sweep on A x = b.
+// ---------------------------------------------------- smoothing kernel
 template <typename T>
-__global__ void k_vanka_color(Geo g, const int32_t* __restrict__ col, const T* __restrict__ val,
-                              const T* __restrict__ pinv, const T* __restrict__ b, T* x, int ri, int rj) {
+struct SmoothArgs {
+    Geo g;
+    const int32_t* col;
+    const T* val;
+    const T* pinv;
+    const T* b;
+    T* x;
+    T* tmp;               // boundary deltas (>= nbnd)
+    const int32_t* bnd;
+    int nbnd;
+    Geo gc;               // coarse level of the prolongation (post-smoothing)
+    const T* xc;
+};
+
+template <bool COOP>
+__device__ __forceinline__ void phase_sync() {
+    if (COOP) cg::this_grid().sync();
+    else __syncthreads();
+}
+
+// One colour class (ri, rj) of the multiplicative Vanka sweep.  Half a warp
+// per patch: lane q < 10 forms the residual of patch row q, the 10x10
+// inverse is applied with shuffles, lane q updates unknown q.  Every lane of
+// a warp runs the same number of loop trips (the shuffles need them all).
+template <typename T>
+__device__ __forceinline__ void vanka_colour(const SmoothArgs<T>& a, int ri, int rj, int gwarp, int nwarps) {
+    const Geo& g = a.g;
     const int fi = ri == 0 ? 3 : ri, fj = rj == 0 ? 3 : rj;  // first i >= 1 with i % 3 == ri
     const int ni = (g.Ny - 1 - fi) >= 0 ? (g.Ny - 1 - fi) / 3 + 1 : 0;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ni == 0) return;
-    const int a = t % ni, bb = t / ni;
-    const int i = fi + 3 * a, j = fj + 3 * bb;
-    if (i > g.Ny - 1 || j > g.Nx - 1) return;
-    const int np = (g.Ny - 1) * (g.Nx - 1);
-    const int pi = (j - 1) * (g.Ny - 1) + (i - 1);
-    int u[PB];
-    patch_unknowns(i, j, g.Ny1, u);
-    T r[PB];
+    const int nj = (g.Nx - 1 - fj) >= 0 ? (g.Nx - 1 - fj) / 3 + 1 : 0;
+    const int npc = ni * nj;
+    const int lane = threadIdx.x & 31, q = lane & 15, half = lane >> 4;
+    for (int pair = gwarp; 2 * pair < npc; pair += nwarps) {
+        const int pidx = 2 * pair + half;
+        const bool valid = pidx < npc;
+        int i = 1, j = 1, row = 0;
+        T r = 0;
+        if (valid) {
+            i = fi + 3 * (pidx % ni);
+            j = fj + 3 * (pidx / ni);
+            if (q < PB) {
+                row = patch_unknown(i, j, g.Ny1, q);
+                T acc = a.b[row];
 #pragma unroll
-    for (int q = 0; q < PB; q++) {
-        const int row = u[q];
-        T acc = b[row];
-#pragma unroll
-        for (int s = 0; s < HMEC_W; s++) {
-            const size_t o = (size_t)s * g.N + row;
-            acc -= val[o] * x[col[o]];
+                for (int s = 0; s < HMEC_W; s++) {
+                    const size_t o = (size_t)s * g.N + row;
+                    acc -= a.val[o] * a.x[a.col[o]];
+                }
+                r = acc;
+            }
         }
-        r[q] = acc;
-    }
-#pragma unroll
-    for (int q = 0; q < PB; q++) {
+        const T* P = a.pinv + (size_t)((j - 1) * (g.Ny - 1) + (i - 1)) * 100 + q * PB;
         T d = 0;
 #pragma unroll
-        for (int c = 0; c < PB; c++) d += pinv[(size_t)(q * PB + c) * np + pi] * r[c];
-        x[u[q]] += d;
+        for (int c = 0; c < PB; c++) {
+            const T rc = __shfl_sync(0xffffffffu, r, (lane & 16) + c);
+            if (valid && q < PB) d += P[c] * rc;
+        }
+        if (valid && q < PB) a.x[row] += d;
     }
 }
 
-// Boundary rows outside every patch: two-phase Jacobi (deterministic).
 template <typename T>
-__global__ void k_bnd_delta(int N, const int32_t* __restrict__ rows, int nb, const int32_t* __restrict__ col,
-                            const T* __restrict__ val, const T* __restrict__ b, const T* __restrict__ x, T* delta) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nb) return;
-    const int row = rows[t];
-    T acc = b[row], diag = 0;
+__device__ __forceinline__ void bnd_delta(const SmoothArgs<T>& a, int tid, int nth) {
+    for (int t = tid; t < a.nbnd; t += nth) {
+        const int row = a.bnd[t];
+        T acc = a.b[row], diag = 0;
 #pragma unroll
-    for (int s = 0; s < HMEC_W; s++) {
-        const size_t o = (size_t)s * N + row;
-        const int c = col[o];
-        const T v = val[o];
-        acc -= v * x[c];
-        if (c == row) diag += v;
+        for (int s = 0; s < HMEC_W; s++) {
+            const size_t o = (size_t)s * a.g.N + row;
+            const int c = a.col[o];
+            const T v = a.val[o];
+            acc -= v * a.x[c];
+            if (c == row) diag += v;
+        }
+        a.tmp[t] = diag != 0 ? acc / diag : (T)0;
     }
-    delta[t] = diag != 0 ? acc / diag : (T)0;
 }
 
+// x_f += P x_c: cell-centred unknowns constant, face unknowns linear along
+// the face normal and constant across it (ghost rows map to ghost rows, which
+// keeps the homogeneous boundary relations of the coarse correction).
 template <typename T>
-__global__ void k_bnd_apply(const int32_t* __restrict__ rows, int nb, const T* __restrict__ delta, T* x) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < nb) x[rows[t]] += delta[t];
-}
-
-// r = b - A x
-template <typename T>
-__global__ void k_residual(int N, const int32_t* __restrict__ col, const T* __restrict__ val, const T* __restrict__ b,
-                           const T* __restrict__ x, T* r) {
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= N) return;
-    T acc = b[row];
-#pragma unroll
-    for (int s = 0; s < HMEC_W; s++) {
-        const size_t o = (size_t)s * N + row;
-        acc -= val[o] * x[col[o]];
+__device__ __forceinline__ void prolong_add(const Geo& gf, const Geo& gc, const T* __restrict__ xc, T* xf, int tid,
+                                            int nth) {
+    const int ncell = gf.Ny1 * gf.Nx1;
+    for (int t = tid; t < ncell; t += nth) {
+        const int i = t % gf.Ny1, j = t / gf.Ny1;
+        const int kf = kp_of(i, j, gf.Ny1);
+        auto xcv = [&](int I, int J, int v) -> T {
+            if (I < 0 || I > gc.Ny || J < 0 || J > gc.Nx) return (T)0;
+            return xc[kp_of(I, J, gc.Ny1) + v];
+        };
+        const int Ic = (i + 1) / 2, Jc = (j + 1) / 2;
+        if (i >= 1 && i <= gf.Ny - 1 && j >= 1 && j <= gf.Nx - 1) {
+            xf[kf + 0] += xcv(Ic, Jc, 0);
+            xf[kf + 3] += xcv(Ic, Jc, 3);
+        }
+        if ((j & 1) == 0) {
+            xf[kf + 1] += xcv(Ic, j / 2, 1);
+            xf[kf + 4] += xcv(Ic, j / 2, 4);
+        } else {
+            xf[kf + 1] += (T)0.5 * (xcv(Ic, j / 2, 1) + xcv(Ic, j / 2 + 1, 1));
+            xf[kf + 4] += (T)0.5 * (xcv(Ic, j / 2, 4) + xcv(Ic, j / 2 + 1, 4));
+        }
+        if ((i & 1) == 0) {
+            xf[kf + 2] += xcv(i / 2, Jc, 2);
+            xf[kf + 5] += xcv(i / 2, Jc, 5);
+        } else {
+            xf[kf + 2] += (T)0.5 * (xcv(i / 2, Jc, 2) + xcv(i / 2 + 1, Jc, 2));
+            xf[kf + 5] += (T)0.5 * (xcv(i / 2, Jc, 5) + xcv(i / 2 + 1, Jc, 5));
+        }
     }
-    r[row] = acc;
 }
 
-// ------------------------------------------------ multigrid transfers
+// A whole smoothing pass.  mode 0: x = 0 first; mode 1: x += P xc first.
+// COOP: launched cooperatively (grid-wide barriers); otherwise one block.
+template <typename T, bool COOP>
+__global__ void __launch_bounds__(SM_BS) k_smooth(SmoothArgs<T> a, int nsweeps, int mode) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const int gwarp = tid >> 5, nwarps = nth >> 5;
+    if (mode == 0) {
+        for (int t = tid; t < a.g.N; t += nth) a.x[t] = (T)0;
+    } else {
+        prolong_add(a.g, a.gc, a.xc, a.x, tid, nth);
+    }
+    phase_sync<COOP>();
+    for (int s = 0; s < nsweeps; s++) {
+        for (int c = 0; c < 9; c++) {
+            vanka_colour(a, c / 3, c % 3, gwarp, nwarps);
+            phase_sync<COOP>();
+        }
+        bnd_delta(a, tid, nth);
+        phase_sync<COOP>();
+        for (int t = tid; t < a.nbnd; t += nth) a.x[a.bnd[t]] += a.tmp[t];
+        phase_sync<COOP>();
+    }
+}
+
+// ------------------------------------------------ multigrid restriction
 // Whether the row of unknown v at staggered cell (i, j) is an interior
 // equation (x/y-Stokes, continuity, Darcy) rather than a boundary or ghost
 // row; the ranges are those of the assembly branches (:698-980).
@@ -210,14 +287,16 @@ __device__ __forceinline__ bool row_interior(const Geo& g, int i, int j, int v) 
     }
 }
 
-// Restriction of the fine physical residual r/df to the coarse rows, scaled
-// by the coarse row scale.  Only interior equations are restricted, and only
-// from fine interior equations (weights renormalised); coarse boundary rows
-// get a zero residual, so the coarse correction obeys the homogeneous
-// boundary conditions, which the prolongation below preserves.
+// Coarse rhs = restricted fine residual (b - A x computed on the fly for the
+// fine rows each coarse row needs), in physical units r/df, scaled by the
+// coarse row scale.  Only interior equations are restricted, and only from
+// fine interior equations (weights renormalised); coarse boundary rows get a
+// zero residual, so the coarse correction obeys the homogeneous boundary
+// conditions, which the prolongation preserves.
 template <typename T>
-__global__ void k_restrict(Geo gf, Geo gc, const T* __restrict__ rf, const double* __restrict__ dsf,
-                           const double* __restrict__ dsc, T* bc) {
+__global__ void k_restrict_resid(Geo gf, Geo gc, const int32_t* __restrict__ col, const T* __restrict__ val,
+                                 const T* __restrict__ bf, const T* __restrict__ xf, const double* __restrict__ dsf,
+                                 const double* __restrict__ dsc, T* bc) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y;
     if (I >= gc.Ny1) return;
@@ -225,14 +304,9 @@ __global__ void k_restrict(Geo gf, Geo gc, const T* __restrict__ rf, const doubl
     for (int v = 0; v < 6; v++) {
         double s = 0, w = 0;
         if (row_interior(gc, I, J, v)) {
-            int i0, i1, j0, j1;
-            if (v == 0 || v == 3) {  // cell centred: the 4 children
-                i0 = 2 * I - 1; i1 = 2 * I; j0 = 2 * J - 1; j1 = 2 * J;
-            } else if (v == 1 || v == 4) {  // x faces: rows of the children, columns 2J-1..2J+1
-                i0 = 2 * I - 1; i1 = 2 * I; j0 = 2 * J - 1; j1 = 2 * J + 1;
-            } else {  // y faces
-                i0 = 2 * I - 1; i1 = 2 * I + 1; j0 = 2 * J - 1; j1 = 2 * J;
-            }
+            int i0 = 2 * I - 1, i1 = 2 * I, j0 = 2 * J - 1, j1 = 2 * J;
+            if (v == 1 || v == 4) j1 = 2 * J + 1;  // x faces: columns 2J-1..2J+1
+            if (v == 2 || v == 5) i1 = 2 * I + 1;  // y faces: rows 2I-1..2I+1
             for (int i = i0; i <= i1; i++)
                 for (int j = j0; j <= j1; j++) {
                     if (i < 0 || i > gf.Ny || j < 0 || j > gf.Nx || !row_interior(gf, i, j, v)) continue;
@@ -240,55 +314,17 @@ __global__ void k_restrict(Geo gf, Geo gc, const T* __restrict__ rf, const doubl
                     if ((v == 1 || v == 4) && j != 2 * J) ww = 0.5;
                     if ((v == 2 || v == 5) && i != 2 * I) ww = 0.5;
                     const int k = kp_of(i, j, gf.Ny1) + v;
-                    s += ww * ((double)rf[k] / dsf[k]);
+                    T acc = bf[k];
+#pragma unroll
+                    for (int q = 0; q < HMEC_W; q++) {
+                        const size_t o = (size_t)q * gf.N + k;
+                        acc -= val[o] * xf[col[o]];
+                    }
+                    s += ww * ((double)acc / dsf[k]);
                     w += ww;
                 }
         }
         bc[kc + v] = (T)(w > 0 ? (s / w) * dsc[kc + v] : 0.0);
-    }
-}
-
-// x_f += P x_c (constant in the cross direction, linear along the face normal)
-template <typename T>
-__global__ void k_prolong(Geo gf, Geo gc, const T* __restrict__ xc, T* xf) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y;
-    if (i >= gf.Ny1) return;
-    const int kf = kp_of(i, j, gf.Ny1);
-    auto xcv = [&](int I, int J, int v) -> T {
-        if (I < 0 || I > gc.Ny || J < 0 || J > gc.Nx) return (T)0;
-        return xc[kp_of(I, J, gc.Ny1) + v];
-    };
-    const int Ic = (i + 1) / 2, Jc = (j + 1) / 2;  // cell-type index (ghost rows map to ghost rows)
-    // P-type: interior fine cells only
-    if (i >= 1 && i <= gf.Ny - 1 && j >= 1 && j <= gf.Nx - 1) {
-        xf[kf + 0] += xcv(Ic, Jc, 0);
-        xf[kf + 3] += xcv(Ic, Jc, 3);
-    }
-    // vx-type: rows by cell index, columns: even j on a coarse face, odd j between two
-    {
-        T a1, a4;
-        if ((j & 1) == 0) {
-            a1 = xcv(Ic, j / 2, 1);
-            a4 = xcv(Ic, j / 2, 4);
-        } else {
-            a1 = (T)0.5 * (xcv(Ic, j / 2, 1) + xcv(Ic, j / 2 + 1, 1));
-            a4 = (T)0.5 * (xcv(Ic, j / 2, 4) + xcv(Ic, j / 2 + 1, 4));
-        }
-        xf[kf + 1] += a1;
-        xf[kf + 4] += a4;
-    }
-    {
-        T a2, a5;
-        if ((i & 1) == 0) {
-            a2 = xcv(i / 2, Jc, 2);
-            a5 = xcv(i / 2, Jc, 5);
-        } else {
-            a2 = (T)0.5 * (xcv(i / 2, Jc, 2) + xcv(i / 2 + 1, Jc, 2));
-            a5 = (T)0.5 * (xcv(i / 2, Jc, 5) + xcv(i / 2 + 1, Jc, 5));
-        }
-        xf[kf + 2] += a2;
-        xf[kf + 5] += a5;
     }
 }
 
@@ -612,6 +648,7 @@ __global__ void k_xupdate(int N, const double* __restrict__ Z, const double* __r
 
 }  // namespace
 
+
 // ===================================================================== host
 
 static void make_geo(Geo& g, int Nx, int Ny, double xsize, double ysize) {
@@ -671,7 +708,7 @@ static int alloc_level(hmec_ctx* ctx, Level& L, bool mixed, bool coarse) {
     L.pinv32 = nullptr;
     L.val32 = nullptr;
     L.fx = L.fb = L.fr = nullptr;
-    L.dx_ = L.db = L.dr = nullptr;
+    L.dx_ = L.db = L.dr = L.pb = nullptr;
     HMEC_CUDA(ctx, cudaMalloc(&L.db, sizeof(double) * N));  // fine: scaled rhs; coarse: FP64 rhs
     if (mixed) {
         HMEC_CUDA(ctx, cudaMalloc(&L.val32, sizeof(float) * HMEC_W * N));
@@ -857,26 +894,6 @@ int solver_setup(hmec_ctx* ctx) {
     return HMEC_OK;
 }
 
-// One smoothing sweep on level L (9 colour classes + boundary rows).
-template <typename T>
-static void vanka_sweep(hmec_ctx* ctx, Level& L, const T* val, const T* pinv, const T* b, T* x, T* tmp) {
-    const Geo& g = L.g;
-    for (int ri = 0; ri < 3; ri++)
-        for (int rj = 0; rj < 3; rj++) {
-            const int fi = ri == 0 ? 3 : ri, fj = rj == 0 ? 3 : rj;
-            const int ni = (g.Ny - 1 - fi) >= 0 ? (g.Ny - 1 - fi) / 3 + 1 : 0;
-            const int nj = (g.Nx - 1 - fj) >= 0 ? (g.Nx - 1 - fj) / 3 + 1 : 0;
-            if (ni * nj == 0) continue;
-            // algorithmic bytes per patch: its 10 ELL rows (values + columns), the
-            // 10x10 inverse, 10 rhs entries, 10 unknowns read and written
-            const double bpp = 10.0 * HMEC_W * (sizeof(T) + 4) + 100.0 * sizeof(T) + 30.0 * sizeof(T);
-            HMEC_LAUNCH_B(ctx, bpp * ni * nj, k_vanka_color<T>, nblocks((long long)ni * nj, 64), 64, 0, g, L.col, val,
-                          pinv, b, x, ri, rj);
-        }
-    HMEC_LAUNCH(ctx, k_bnd_delta<T>, nblocks(L.nbnd, 128), 128, 0, g.N, L.bnd_rows, L.nbnd, L.col, val, b, x, tmp);
-    HMEC_LAUNCH(ctx, k_bnd_apply<T>, nblocks(L.nbnd, 128), 128, 0, L.bnd_rows, L.nbnd, tmp, x);
-}
-
 template <typename T>
 struct LvPtr;
 template <>
@@ -896,31 +913,78 @@ struct LvPtr<float> {
     static const float* pinv(Level& L) { return L.pinv32; }
 };
 
-// V-cycle on level l for A x = b with x = 0 on entry.
+// Levels with at most this many patches are smoothed by one block.
+constexpr int SINGLE_BLOCK_PATCHES = 1500;
+
 template <typename T>
-static void vcycle(hmec_ctx* ctx, size_t l) {
+static int max_coop_blocks(hmec_ctx* ctx) {
+    static int cached[2] = {0, 0};
+    int& c = cached[sizeof(T) == 8 ? 0 : 1];
+    if (c == 0) {
+        int per_sm = 0, nsm = 0;
+        HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth<T, true>, SM_BS, 0));
+        HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
+        c = std::max(1, per_sm * nsm);
+    }
+    return c;
+}
+
+// One smoothing pass on level l (x = 0 or x += P xc first, then nsweeps sweeps).
+template <typename T>
+static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mode) {
+    Solver& sv = ctx->sv;
+    Level& L = sv.lv[l];
+    SmoothArgs<T> a;
+    a.g = L.g;
+    a.col = L.col;
+    a.val = LvPtr<T>::val(L);
+    a.pinv = LvPtr<T>::pinv(L);
+    a.b = b;
+    a.x = x;
+    a.tmp = LvPtr<T>::r(L);
+    a.bnd = L.bnd_rows;
+    a.nbnd = L.nbnd;
+    a.gc = (mode == 1) ? sv.lv[l + 1].g : L.g;
+    a.xc = (mode == 1) ? LvPtr<T>::x(sv.lv[l + 1]) : nullptr;
+    // algorithmic bytes: per sweep every patch's 10 ELL rows, inverse, rhs and
+    // unknowns, and the boundary rows; plus the zero fill or the prolongation
+    const double st = sizeof(T);
+    const double bpp = 10.0 * HMEC_W * (st + 4) + 100.0 * st + 30.0 * st;
+    const double bnd = (double)L.nbnd * (HMEC_W * (st + 4) + 4.0 * st);
+    const double bytes = nsweeps * ((double)L.npatch * bpp + bnd) + (double)L.g.N * st * (mode ? 2.5 : 1.0);
+    if (L.npatch <= SINGLE_BLOCK_PATCHES) {
+        HMEC_LAUNCH_B(ctx, bytes, (k_smooth<T, false>), 1, SM_BS, 0, a, nsweeps, mode);
+        return HMEC_OK;
+    }
+    const long long work = std::max<long long>((long long)L.npatch * 16 / 9, L.g.N);
+    const int grid = (int)std::min<long long>(max_coop_blocks<T>(ctx), std::max<long long>(1, (work + SM_BS - 1) / SM_BS));
+    void* args[] = {&a, &nsweeps, &mode};
+    const bool prof = hmec_prof_begin(ctx, "k_smooth", bytes);
+    HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_smooth<T, true>, dim3(grid), dim3(SM_BS), args, 0, ctx->stream));
+    ctx->launches++;
+    if (prof) hmec_prof_end(ctx);
+    return HMEC_OK;
+}
+
+// V-cycle on level l for A x = b, x = 0 on entry (b, x default to the level's buffers).
+template <typename T>
+static int vcycle(hmec_ctx* ctx, size_t l, const T* b_in = nullptr, T* x_in = nullptr) {
     Solver& sv = ctx->sv;
     Level& L = sv.lv[l];
     const hmec_params& p = ctx->p;
-    T* x = LvPtr<T>::x(L);
-    T* b = LvPtr<T>::b(L);
-    T* r = LvPtr<T>::r(L);
-    const T* val = LvPtr<T>::val(L);
-    const T* pinv = LvPtr<T>::pinv(L);
-    const size_t N = (size_t)L.g.N;
-    HMEC_LAUNCH(ctx, k_zero<T>, nblocks(N, 256), 256, 0, N, x);
+    const T* b = b_in ? b_in : LvPtr<T>::b(L);
+    T* x = x_in ? x_in : LvPtr<T>::x(L);
+    int rc;
     if (l + 1 == sv.lv.size()) {
         const int ns = (sv.lv.size() == 1) ? std::max(1, p.mg_pre + p.mg_post) : std::max(1, p.mg_coarse_sweeps);
-        for (int s = 0; s < ns; s++) vanka_sweep<T>(ctx, L, val, pinv, b, x, r);
-        return;
+        return smooth<T>(ctx, l, b, x, ns, 0);
     }
-    for (int s = 0; s < p.mg_pre; s++) vanka_sweep<T>(ctx, L, val, pinv, b, x, r);
+    if ((rc = smooth<T>(ctx, l, b, x, p.mg_pre, 0))) return rc;
     Level& C = sv.lv[l + 1];
-    HMEC_LAUNCH(ctx, k_residual<T>, nblocks(N, 256), 256, 0, L.g.N, L.col, val, b, x, r);
-    HMEC_LAUNCH(ctx, k_restrict<T>, sgrid(C.g), 64, 0, L.g, C.g, r, L.dscale, C.dscale, LvPtr<T>::b(C));
-    vcycle<T>(ctx, l + 1);
-    HMEC_LAUNCH(ctx, k_prolong<T>, sgrid(L.g), 64, 0, L.g, C.g, LvPtr<T>::x(C), x);
-    for (int s = 0; s < p.mg_post; s++) vanka_sweep<T>(ctx, L, val, pinv, b, x, r);
+    HMEC_LAUNCH(ctx, k_restrict_resid<T>, sgrid(C.g), 64, 0, L.g, C.g, L.col, LvPtr<T>::val(L), b, x, L.dscale,
+                C.dscale, LvPtr<T>::b(C));
+    if ((rc = vcycle<T>(ctx, l + 1))) return rc;
+    return smooth<T>(ctx, l, b, x, p.mg_post, 1);
 }
 
 // z = M^{-1} v on the fine level (v, z FP64 vectors of the scaled system)
@@ -930,17 +994,12 @@ static int precondition(hmec_ctx* ctx, const double* v, double* z) {
     const size_t N = (size_t)L.g.N;
     if (ctx->p.form == HMEC_FORM_MIXED) {
         HMEC_LAUNCH(ctx, (k_convert<double, float>), nblocks(N, 256), 256, 0, N, v, L.fb);
-        vcycle<float>(ctx, 0);
+        int rc = vcycle<float>(ctx, 0);
+        if (rc) return rc;
         HMEC_LAUNCH(ctx, (k_convert<float, double>), nblocks(N, 256), 256, 0, N, L.fx, z);
-    } else {
-        // the fine-level rhs buffer holds the system rhs, so the V-cycle runs on a copy
-        double* keep_b = L.db;
-        L.db = const_cast<double*>(v);
-        vcycle<double>(ctx, 0);
-        L.db = keep_b;
-        HMEC_CUDA(ctx, cudaMemcpyAsync(z, L.dx_, sizeof(double) * N, cudaMemcpyDeviceToDevice, ctx->stream));
+        return HMEC_OK;
     }
-    return HMEC_OK;
+    return vcycle<double>(ctx, 0, v, z);
 }
 
 int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
