@@ -26,6 +26,7 @@ int hmec_cuda_fail(hmec_ctx* ctx, cudaError_t e, const char* what) {
 
 bool hmec_prof_begin(hmec_ctx* ctx, const char* kname, double bytes) {
     ProfState& P = ctx->prof;
+    while (*kname == '(' || *kname == ' ') kname++;  // template launches are parenthesised
     if (P.name.empty() || strncmp(kname, P.name.c_str(), P.name.size()) != 0) return false;
     for (int k = 0; k < 2; k++) {
         cudaEvent_t e;
@@ -158,7 +159,7 @@ void hmec_params_default(hmec_params* p) {
     p->mg_levels = 6;
     p->mg_pre = 2;
     p->mg_post = 2;
-    p->mg_coarse_sweeps = 30;
+    p->mg_coarse_sweeps = 8;
     p->rsf_maxit = 10000;
     p->advect_markers = 0;
     p->rk4_as_written = 0;

@@ -913,8 +913,10 @@ struct LvPtr<float> {
     static const float* pinv(Level& L) { return L.pinv32; }
 };
 
-// Levels with at most this many patches are smoothed by one block.
-constexpr int SINGLE_BLOCK_PATCHES = 1500;
+// Levels with at most this many patches are smoothed by one block (a block
+// barrier is cheaper than a grid barrier, but one block leaves the GPU idle:
+// measured slower than a small cooperative grid for every level size here).
+constexpr int SINGLE_BLOCK_PATCHES = 0;
 
 template <typename T>
 static int max_coop_blocks(hmec_ctx* ctx) {

@@ -141,7 +141,7 @@ void hmo_params_default(hmec_params* p) {
     p->mg_levels = 6;
     p->mg_pre = 2;
     p->mg_post = 2;
-    p->mg_coarse_sweeps = 30;
+    p->mg_coarse_sweeps = 8;
     p->rsf_maxit = 10000;
     p->advect_markers = 0;
     p->rk4_as_written = 0;
