@@ -165,6 +165,7 @@ void hmec_params_default(hmec_params* p) {
     p->rk4_as_written = 0;
     p->quirk_accumulate_sums = 0;
     p->bounds_check = 0;
+    p->mg_flags = 1; /* HMEC_MG_DARCY_HARMONIC */
 }
 
 #define HMEC_X_NAME(name, grid) #name,

@@ -339,7 +339,7 @@ struct CoefOut {
     double *ETA, *GGG, *RHO, *ETAP, *GGGP, *ETAB, *POR, *GGGB, *RHOX, *RHOFX, *PORX, *ETADX, *RHOY, *RHOFY, *PORY, *ETADY;
 };
 
-__global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C) {
+__global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y;
     if (I >= gc.Ny1) return;
@@ -408,6 +408,28 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C) {
             C.RHOFX[oc] = a[1] / w;
             C.PORX[oc] = a[2] / w;
             C.ETADX[oc] = a[3] / w;
+            if (flags & HMEC_MG_DARCY_HARMONIC) {
+                // x-flow: rows in parallel (mean conductance), columns in series (mean resistance)
+                double rs = 0, wr = 0;
+                for (int dj = -1; dj <= 1; dj++) {
+                    const int j = 2 * J + dj;
+                    if (j < 0 || j >= gf.Nx) continue;
+                    double cs = 0;
+                    int nc = 0;
+                    for (int i = r0; i <= r1; i++) {
+                        const double e = F.ETADX[(size_t)j * gf.Ny1 + i];
+                        if (e > 0) {
+                            cs += 1.0 / e;
+                            nc++;
+                        }
+                    }
+                    if (nc == 0) continue;
+                    const double ww = dj == 0 ? 2.0 : 1.0;
+                    rs += ww * (nc / cs);
+                    wr += ww;
+                }
+                if (wr > 0) C.ETADX[oc] = rs / wr;
+            }
         } else {
             C.RHOX[oc] = 0;
             C.RHOFX[oc] = 0;
@@ -436,6 +458,28 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C) {
             C.RHOFY[oc] = a[1] / w;
             C.PORY[oc] = a[2] / w;
             C.ETADY[oc] = a[3] / w;
+            if (flags & HMEC_MG_DARCY_HARMONIC) {
+                // y-flow: columns in parallel, rows in series
+                double rs = 0, wr = 0;
+                for (int di = -1; di <= 1; di++) {
+                    const int i = 2 * I + di;
+                    if (i < 0 || i >= gf.Ny) continue;
+                    double cs = 0;
+                    int nc = 0;
+                    for (int j = c0; j <= c1; j++) {
+                        const double e = F.ETADY[(size_t)j * gf.Ny1 + i];
+                        if (e > 0) {
+                            cs += 1.0 / e;
+                            nc++;
+                        }
+                    }
+                    if (nc == 0) continue;
+                    const double ww = di == 0 ? 2.0 : 1.0;
+                    rs += ww * (nc / cs);
+                    wr += ww;
+                }
+                if (wr > 0) C.ETADY[oc] = rs / wr;
+            }
         } else {
             C.RHOY[oc] = 0;
             C.RHOFY[oc] = 0;
@@ -881,7 +925,7 @@ int solver_setup(hmec_ctx* ctx) {
                        (double*)a.ETAB, (double*)a.POR, (double*)a.GGGB, (double*)a.RHOX, (double*)a.RHOFX,
                        (double*)a.PORX, (double*)a.ETADX, (double*)a.RHOY, (double*)a.RHOFY, (double*)a.PORY,
                        (double*)a.ETADY};
-            HMEC_LAUNCH(ctx, k_coarsen_coef, sgrid(L.g), 64, 0, F.g, L.g, ci, co);
+            HMEC_LAUNCH(ctx, k_coarsen_coef, sgrid(L.g), 64, 0, F.g, L.g, ci, co, ctx->p.mg_flags);
             launch_assemble(ctx, L.g, L.af, L.col, L.val, L.dscale, nullptr, nullptr, nullptr);
         }
         HMEC_LAUNCH(ctx, k_vanka_setup, nblocks(L.npatch, 64), 64, 0, L.g, L.col, L.val, L.pinv, L.pinv32, status);

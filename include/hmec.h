@@ -97,7 +97,16 @@ typedef struct hmec_params {
     int32_t rk4_as_written;   /* 1: reproduce the shifted RK stages of the reference */
     int32_t quirk_accumulate_sums; /* oracle only: marker sums accumulate across steps */
     int32_t bounds_check;     /* 1: device index checks set HMEC_ERR_BOUNDS */
+    int32_t mg_flags;         /* multigrid coarsening options, HMEC_MG_* bits */
 } hmec_params;
+
+/* mg_flags bits */
+enum hmec_mg_flags {
+    /* Darcy resistance eta_f/k of a coarse face: conductances averaged across
+     * the flow direction (parallel paths), resistances along it (series);
+     * otherwise plain arithmetic averages. */
+    HMEC_MG_DARCY_HARMONIC = 1
+};
 
 /* ------------------------------------------------------------- node fields */
 /* X(name, grid): grid 0 = basic (Ny x Nx), 1 = staggered (Ny+1 x Nx+1).

@@ -49,6 +49,7 @@ class HmecParams(C.Structure):
         ("krylov_maxit", C.c_int32), ("mg_levels", C.c_int32), ("mg_pre", C.c_int32), ("mg_post", C.c_int32),
         ("mg_coarse_sweeps", C.c_int32), ("rsf_maxit", C.c_int32), ("advect_markers", C.c_int32),
         ("rk4_as_written", C.c_int32), ("quirk_accumulate_sums", C.c_int32), ("bounds_check", C.c_int32),
+        ("mg_flags", C.c_int32),
     ]
 
 
