@@ -168,13 +168,13 @@ def equilibrate(A):
     return Dr, Dc
 
 
-def direct_solve(A, b, refine: int = 4):
+def direct_solve(A, b, refine: int = 4, ordering: str = "COLAMD"):
     """Equilibrated SuperLU solve with FP64 iterative refinement (the Pardiso stand-in)."""
     import scipy.sparse.linalg as spla
 
     Dr, Dc = equilibrate(A)
     As = (Dr @ A @ Dc).tocsc()
-    lu = spla.splu(As, permc_spec="COLAMD", diag_pivot_thresh=1.0)
+    lu = spla.splu(As, permc_spec=ordering, diag_pivot_thresh=1.0)
 
     def solve(r):
         return Dc @ lu.solve(Dr @ r)
@@ -192,6 +192,10 @@ def direct_solve(A, b, refine: int = 4):
 
 class Oracle:
     """One reference model instance on the CPU."""
+
+    #: SuperLU column ordering of the direct solve (a second ordering gives the
+    #: oracle's own round-off floor)
+    ordering = "COLAMD"
 
     def __init__(self, params: HmecParams):
         self.L = lib()
@@ -305,7 +309,7 @@ class Oracle:
             A = sp.csr_matrix((np.ctypeslib.as_array(data, shape=(nnz,)).copy(),
                                np.ctypeslib.as_array(indices, shape=(nnz,)).copy(), ip.copy()), shape=(n, n))
             b = np.ctypeslib.as_array(rhs, shape=(n,)).copy()
-            sol = direct_solve(A, b)
+            sol = direct_solve(A, b, ordering=self.ordering)
             np.ctypeslib.as_array(x, shape=(n,))[...] = sol
             self.solve_calls += 1
             self.last_solution = sol

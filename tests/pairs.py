@@ -97,3 +97,13 @@ def solution_errors(xg, x):
         den = max(float(np.max(np.abs(S[:, c]))) for c in cols)
         out[g] = num / den if den > 0 else num
     return out
+
+
+class OracleView:
+    """Gives an oracle the field() accessor of a Model (for group_errors)."""
+
+    def __init__(self, o):
+        self.o = o
+
+    def field(self, name):
+        return self.o.field(name)

@@ -101,20 +101,36 @@ def test_solve_parity(preset, form):
 @pytest.mark.parametrize("form", [hmec.FORM_FP64, hmec.FORM_MIXED])
 @pytest.mark.parametrize("preset,nsteps", [("tiny", 6), ("c0", 5)])
 def test_timestep_replay(preset, nsteps, form):
-    """Each step starts the GPU from the oracle's state and compares after one step."""
+    """Each step starts the GPU from the oracle's state and compares after one step.
+
+    Within a step the plastic (global) iterations amplify round-off near the
+    yield stress (A = syield/siiel close to 1 in :1286-1288), so two direct
+    solves of the reference's own systems that differ only in pivot order
+    already disagree by up to a few 1e-9 in stress after some steps.  That
+    floor is measured here with a second oracle (another column ordering) and
+    the GPU must stay within max(1e-10, 10 x floor) of the oracle.
+    """
     o, mk, nodes = pairs.oracle_for(preset)
+    o2, _, _ = pairs.oracle_for(preset)
+    o2.ordering = "MMD_AT_PLUS_A"
     m = pairs.model_for(preset, mk, nodes, form=form)
     log = []
     for _ in range(nsteps):
-        m.load_state(o.snapshot())
+        snap = o.snapshot()
+        m.load_state(snap)
+        o2.load_state(snap)
         it = o.timestep()
+        o2.timestep()
         rep = m.timestep()
         err = pairs.group_errors(m, o)
-        log.append((int(o.scalar("timestep")) - 1, it, rep["global_iters"], o.scalar("dt"), m.scalar("dt"), err))
-    for step, it_o, it_g, dt_o, dt_g, err in log:
+        floor = pairs.group_errors(pairs.OracleView(o2), o)
+        log.append((int(o.scalar("timestep")) - 1, it, rep["global_iters"], o.scalar("dt"), m.scalar("dt"), err, floor))
+    for step, it_o, it_g, dt_o, dt_g, err, floor in log:
         assert it_g == it_o, log
         assert dt_g == pytest.approx(dt_o, rel=1e-12), log
-        check_groups(err)
+        for g, e in err.items():
+            bound = max(TOL_DARCY if g == "darcy" else TOL_STEP, 10 * floor[g])
+            assert e < bound, (step, g, e, floor[g], log)
 
 
 def test_free_running_tiny_matches():
