@@ -28,7 +28,10 @@ def nvcc() -> str:
 
 
 def _flags(extra=()):
-    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "-I", SRC] + list(extra)
+    # host code: no fused multiply-add (GCC fuses by default on aarch64), so the
+    # host-side grid coordinates are the same IEEE values on every host
+    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+                   "-I", INC, "-I", SRC] + list(extra)
 
 
 def _stale(target, deps):
