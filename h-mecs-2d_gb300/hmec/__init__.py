@@ -95,7 +95,7 @@ EXPORTS = ["hmec_abi_version", "hmec_params_default", "hmec_field_name", "hmec_f
            "hmec_set_scalar", "hmec_get_scalar", "hmec_markers_to_nodes", "hmec_timestep_begin",
            "hmec_global_iteration", "hmec_timestep_end", "hmec_advect_markers", "hmec_timestep",
            "hmec_assemble_csr", "hmec_solve_system", "hmec_kernel_launches", "hmec_synchronize", "hmec_stream",
-           "hmec_profile_kernel", "hmec_profile_read"]
+           "hmec_profile_kernel", "hmec_profile_read", "hmec_markers_to_nodes_noalloc"]
 
 _lib = None
 
@@ -157,6 +157,8 @@ def load(build_if_missing: bool = True):
     L.hmec_stream.restype = vp
     L.hmec_profile_kernel.argtypes = [vp, C.c_char_p]
     L.hmec_profile_read.argtypes = [vp, P(C.c_int64), P(C.c_double), P(C.c_double)]
+    L.hmec_markers_to_nodes_noalloc.argtypes = [P(Params), P(P(C.c_double)), C.c_int64, P(P(C.c_double)), vp]
+    L.hmec_markers_to_nodes_noalloc.restype = C.c_int32
     _lib = L
     return L
 

@@ -254,6 +254,24 @@ void* hmec_stream(hmec_ctx* ctx);
  * counterpart in the reference).                                           */
 int32_t hmec_profile_kernel(hmec_ctx* ctx, const char* name);
 int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, double* bytes);
+/* Markers -> nodes without allocating device memory.  No counterpart in the
+ * reference: it serves hosts that may not call cudaMalloc (an application
+ * that owns the device allocator, code running under CUDA-graph capture, a
+ * real-time loop that must not block on the allocator).  Computes the same
+ * 23 node fields as hmec_markers_to_nodes() from arrays the caller already
+ * holds on the current device: markers[k] is the device array of marker
+ * field k (enum hmec_marker_field), fields[f] the column-major device array
+ * of node field f (entries of fields that are not outputs may be NULL).
+ * Scratch memory is one fixed array compiled into the library (about 6 MiB
+ * on every device that loads it, held until exit); hence the limits: at most
+ * HMEC_NOALLOC_MAX_MARKERS = 1048576 markers and 4*(Nx-1)*(Ny-1) <=
+ * HMEC_NOALLOC_MAX_HALF_CELLS = 262144, larger inputs return HMEC_ERR_ARG.
+ * Kernels go to `stream` (a cudaStream_t; NULL = legacy default stream).
+ * The first call on a device looks up the array's device address, so make
+ * it before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race, serialise them.                                  */
+int32_t hmec_markers_to_nodes_noalloc(const hmec_params* p, const double* const* markers, int64_t n,
+                                      double* const* fields, void* stream);
 /* Device-kernel launches issued since hmec_create. */
 int64_t hmec_kernel_launches(const hmec_ctx* ctx);
 /* Synchronise the context stream. */
