@@ -107,3 +107,19 @@ class OracleView:
 
     def field(self, name):
         return self.o.field(name)
+
+
+def bisection_resolution(o):
+    """Relative slip-rate resolution of the reference's fault-stress bisection.
+
+    The bisection of cpp/h_mec_rsf_v9.cpp:1224 stops at |dS| <= 1e-3 Pa and
+    V ~ sinh(S / (a prB)), so V is determined to about 1e-3 / (a prB).
+    """
+    p = o.params
+    i = int((p.Ny - 1) / 2.0)
+    j = np.arange(p.Nx)
+    pt, pf = o.field("pt"), o.field("pf")
+    blk = lambda f: f[i, j] + f[i + 1, j] + f[i, j + 1] + f[i + 1, j + 1]
+    prb = np.maximum((blk(pt) - blk(pf)) / 4.0, 1e3)
+    a = o.field("ARSF")[i]
+    return float(1e-3 / np.min(a * prb))

@@ -108,7 +108,10 @@ def test_timestep_replay(preset, nsteps, form):
     solves of the reference's own systems that differ only in pivot order
     already disagree by up to a few 1e-9 in stress after some steps.  That
     floor is measured here with a second oracle (another column ordering) and
-    the GPU must stay within max(1e-10, 10 x floor) of the oracle.
+    the GPU must stay within max(1e-10, 10 x floor) of the oracle.  The fault
+    slip rate (and the state variable it drives) is known only to the
+    bisection tolerance of the reference, |dS| <= 1e-3 Pa (:1224), i.e. to
+    1e-3 / (a * sigma_eff) relative; that bound applies to those two groups.
     """
     o, mk, nodes = pairs.oracle_for(preset)
     o2, _, _ = pairs.oracle_for(preset)
@@ -124,13 +127,17 @@ def test_timestep_replay(preset, nsteps, form):
         rep = m.timestep()
         err = pairs.group_errors(m, o)
         floor = pairs.group_errors(pairs.OracleView(o2), o)
-        log.append((int(o.scalar("timestep")) - 1, it, rep["global_iters"], o.scalar("dt"), m.scalar("dt"), err, floor))
-    for step, it_o, it_g, dt_o, dt_g, err, floor in log:
+        res = pairs.bisection_resolution(o)
+        log.append((int(o.scalar("timestep")) - 1, it, rep["global_iters"], o.scalar("dt"), m.scalar("dt"), err,
+                    floor, res))
+    for step, it_o, it_g, dt_o, dt_g, err, floor, res in log:
         assert it_g == it_o, log
         assert dt_g == pytest.approx(dt_o, rel=1e-12), log
         for g, e in err.items():
             bound = max(TOL_DARCY if g == "darcy" else TOL_STEP, 10 * floor[g])
-            assert e < bound, (step, g, e, floor[g], log)
+            if g in ("slip_rate", "state"):
+                bound = max(bound, 2 * res)
+            assert e < bound, (step, g, e, floor[g], res, log)
 
 
 def test_free_running_tiny_matches():
