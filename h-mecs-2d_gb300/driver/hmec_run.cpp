@@ -1,0 +1,204 @@
+// hmec_run.cpp -- host loop mirroring main() of cpp/h_mec_rsf_v9.cpp, with the
+// hot path delegated to libhmec_gpu.so through include/hmec.h.
+//
+// What stays on the host, as in the reference: the initial marker lattice and
+// node fields (:188-209, :283-338), the per-step stdout report (:1732-1737)
+// and the EVO_*.txt time series of the fault row (:1751-1805).  Everything in
+// between (:377-1726) is one hmec_timestep() call per step.
+//
+//   hmec_run [steps] [Nx Ny xsize ysize] [--mixed] [--outdir DIR]
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "hmec.h"
+
+namespace {
+
+struct Grid {
+    int rows, cols;
+    std::vector<double> a;
+    Grid(int r, int c, double v = 0) : rows(r), cols(c), a((size_t)r * c, v) {}
+    double& operator()(int i, int j) { return a[(size_t)j * rows + i]; }
+};
+
+std::vector<double> linspaced(int n, double low, double high) {  // Eigen LinSpaced
+    std::vector<double> v(n);
+    const double step = (n == 1) ? 0. : (high - low) / (double)(n - 1);
+    for (int i = 0; i < n; i++) v[i] = (i == n - 1) ? high : low + (double)i * step;
+    return v;
+}
+
+void append_row(const std::string& path, double timesum, double dt, const Grid& g, int row) {
+    FILE* f = fopen(path.c_str(), "a");
+    if (!f) return;
+    fprintf(f, "%g    %g    ", timesum, dt);
+    for (int j = 0; j < g.cols; j++) fprintf(f, "%s%g", j ? " " : "", g.a[(size_t)j * g.rows + row]);
+    fprintf(f, "\n");
+    fclose(f);
+}
+
+int check(hmec_ctx* ctx, int rc, const char* what) {
+    if (rc != HMEC_OK) fprintf(stderr, "%s failed (%d): %s\n", what, rc, hmec_last_error(ctx));
+    return rc;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    hmec_params p;
+    hmec_params_default(&p);  // cpp/constants.hpp
+    int steps = 10;
+    std::string outdir = ".";
+    std::vector<const char*> pos;
+    for (int k = 1; k < argc; k++) {
+        if (!strcmp(argv[k], "--mixed")) p.form = HMEC_FORM_MIXED;
+        else if (!strcmp(argv[k], "--outdir") && k + 1 < argc) outdir = argv[++k];
+        else pos.push_back(argv[k]);
+    }
+    if (pos.size() >= 1) steps = atoi(pos[0]);
+    if (pos.size() >= 5) {
+        p.Nx = atoi(pos[1]);
+        p.Ny = atoi(pos[2]);
+        p.xsize = atof(pos[3]);
+        p.ysize = atof(pos[4]);
+    }
+    const int Nx = p.Nx, Ny = p.Ny, Nx1 = Nx + 1, Ny1 = Ny + 1;
+    const double dx = p.xsize / (Nx - 1), dy = p.ysize / (Ny - 1);
+    const double upper_block = p.ysize / 2. - dy, lower_block = p.ysize / 2. + dy;
+    const int line_fault = (int)((Ny - 1) / 2.);
+
+    // markers, :188-209 (rand() % 1 == 0: no jitter)
+    const int64_t nxm = (int64_t)(Nx - 1) * p.mx, nym = (int64_t)(Ny - 1) * p.my;
+    const int64_t marknum = nxm * nym;
+    const double dxms = p.xsize / (double)nxm, dyms = p.ysize / (double)nym;
+    std::vector<std::vector<double>> mk(HMEC_M_COUNT, std::vector<double>((size_t)marknum, 0.0));
+    for (int64_t m = 0; m < marknum; m++) {
+        double& xm = mk[HMEC_M_xm][m];
+        double& ym = mk[HMEC_M_ym][m];
+        xm = 0 + (double)(m / nym) * dxms;
+        ym = 0 + (double)(m % nym) * dyms;
+        mk[HMEC_M_t_marker][m] = 1;
+        mk[HMEC_M_rhom][m] = 2800;
+        mk[HMEC_M_etasm][m] = 1e21;
+        mk[HMEC_M_cohescm][m] = p.cohes;
+        mk[HMEC_M_cohestm][m] = p.cohes;
+        mk[HMEC_M_frictcm][m] = .5;
+        mk[HMEC_M_dilatcm][m] = p.dilatation;
+        mk[HMEC_M_fricttm][m] = p.tensile;
+        mk[HMEC_M_kkkm][m] = 2e-16;
+        mk[HMEC_M_gm][m] = p.shearmod;
+        mk[HMEC_M_rhofm][m] = 1000;
+        mk[HMEC_M_etafm][m] = 1e-3;
+        mk[HMEC_M_porm][m] = .01 * (1 + .0 * (0 - .5));
+        mk[HMEC_M_etam][m] = mk[HMEC_M_etasm][m] * exp(-p.alpha * mk[HMEC_M_porm][m]);
+        if (ym < upper_block || ym > lower_block) {
+            mk[HMEC_M_t_marker][m] = -1;
+            mk[HMEC_M_etam][m] = 1e23;
+            mk[HMEC_M_etasm][m] = 1e23;
+            mk[HMEC_M_rhom][m] = 2800;
+            mk[HMEC_M_kkkm][m] = 2e-16;
+            mk[HMEC_M_cohescm][m] = p.cohes * 1e3;
+            mk[HMEC_M_cohestm][m] = p.cohes * 1e3;
+            mk[HMEC_M_frictcm][m] = .8;
+            mk[HMEC_M_dilatcm][m] = p.dilatation;
+            mk[HMEC_M_fricttm][m] = p.tensile;
+        }
+    }
+    // node fields of a fresh start, :283-338
+    Grid OM0(Ny, Nx, p.omm[0]), ARSF(Ny, Nx, p.arsfm[1]), BRSF(Ny, Nx, p.brsfm[1]), LRSF(Ny, Nx, p.lrsfm[0]);
+    const std::vector<double> x = linspaced(Nx, 0, p.xsize), y = linspaced(Ny, 0, p.ysize);
+    for (int i = 0; i < Ny; i++) {
+        if (!(y[i] > upper_block && y[i] < lower_block)) continue;
+        for (int j = 0; j < Nx; j++) {
+            OM0(i, j) = p.omm[1];
+            const double xj = x[j];
+            if (xj < p.TS_1) {
+                BRSF(i, j) = p.brsfm[0];
+                ARSF(i, j) = p.arsfm[0];
+            }
+            if (xj >= p.TS_1 && xj < p.TS_2) {
+                const double t = (xj - p.TS_1) / (p.TS_2 - p.TS_1);
+                BRSF(i, j) = p.brsfm[0] - (p.brsfm[0] - p.brsfm[1]) * t;
+                ARSF(i, j) = p.arsfm[0] - (p.arsfm[0] - p.arsfm[1]) * t;
+                LRSF(i, j) = p.lrsfm[0] - (p.lrsfm[0] - p.lrsfm[1]) * t;
+            }
+            if (xj >= p.TS_2 && xj <= p.TS_3) LRSF(i, j) = p.lrsfm[1];
+            if (xj > p.TS_3 && xj <= p.TS_4) {
+                const double t = (xj - p.TS_3) / (p.TS_4 - p.TS_3);
+                BRSF(i, j) = p.brsfm[1] - (p.brsfm[1] - p.brsfm[0]) * t;
+                ARSF(i, j) = p.arsfm[1] - (p.arsfm[1] - p.arsfm[0]) * t;
+                LRSF(i, j) = p.lrsfm[1] - (p.lrsfm[1] - p.lrsfm[0]) * t;
+            }
+            if (xj > p.TS_4) {
+                BRSF(i, j) = p.brsfm[0];
+                ARSF(i, j) = p.arsfm[0];
+            }
+        }
+    }
+    Grid PT0(Ny1, Nx1, p.PCONF + p.PTFDIFF), PF0(Ny1, Nx1, p.PCONF);
+
+    int32_t st = 0;
+    hmec_ctx* ctx = hmec_create(&p, &st);
+    if (!ctx) {
+        fprintf(stderr, "hmec_create failed (%d)\n", st);
+        return 1;
+    }
+    std::vector<const double*> mptr(HMEC_M_COUNT);
+    for (int k = 0; k < HMEC_M_COUNT; k++) mptr[k] = mk[k].data();
+    if (check(ctx, hmec_upload_markers(ctx, mptr.data(), marknum), "upload_markers")) return 1;
+    struct {
+        int id;
+        Grid* g;
+    } init[] = {{HMEC_F_OM0, &OM0}, {HMEC_F_OM, &OM0}, {HMEC_F_ARSF, &ARSF}, {HMEC_F_BRSF, &BRSF},
+                {HMEC_F_LRSF, &LRSF}, {HMEC_F_PT0, &PT0}, {HMEC_F_PF0, &PF0}};
+    for (auto& f : init)
+        if (check(ctx, hmec_upload_field(ctx, f.id, f.g->a.data(), f.g->rows, f.g->cols), "upload_field")) return 1;
+
+    Grid VSLIPB(Ny, Nx), ETA(Ny, Nx), OM(Ny, Nx), SigmaY(Ny, Nx), SII_fault(Ny, Nx);
+    Grid pf(Ny1, Nx1), pt(Ny1, Nx1), VIS_COMP(Ny1, Nx1), EL_DECOM(Ny1, Nx1), vxD(Ny1, Nx1), Peff(Ny1, Nx1);
+    for (int s = 0; s < steps; s++) {
+        hmec_step_report r;
+        if (check(ctx, hmec_timestep(ctx, &r), "hmec_timestep")) break;
+        // :1732-1737
+        printf("====================================\n");
+        printf("total time:        %g sec\n", r.timesum);
+        printf("time step:         %g sec\n", r.dt);
+        printf("Vslip max:         %g\n", r.Vmax);
+        printf("iter - iterations:   %d\n", r.global_iters);
+        printf("global - iterations: %d\n", r.ynlast);
+        // :1751-1805 fault-row time series
+        hmec_download_field(ctx, HMEC_F_VSLIPB, VSLIPB.a.data(), Ny, Nx);
+        hmec_download_field(ctx, HMEC_F_ETA, ETA.a.data(), Ny, Nx);
+        hmec_download_field(ctx, HMEC_F_OM, OM.a.data(), Ny, Nx);
+        hmec_download_field(ctx, HMEC_F_SigmaY, SigmaY.a.data(), Ny, Nx);
+        hmec_download_field(ctx, HMEC_F_SII_fault, SII_fault.a.data(), Ny, Nx);
+        hmec_download_field(ctx, HMEC_F_pf, pf.a.data(), Ny1, Nx1);
+        hmec_download_field(ctx, HMEC_F_pt, pt.a.data(), Ny1, Nx1);
+        hmec_download_field(ctx, HMEC_F_VIS_COMP, VIS_COMP.a.data(), Ny1, Nx1);
+        hmec_download_field(ctx, HMEC_F_EL_DECOM, EL_DECOM.a.data(), Ny1, Nx1);
+        hmec_download_field(ctx, HMEC_F_vxD, vxD.a.data(), Ny1, Nx1);
+        for (size_t k = 0; k < Peff.a.size(); k++) Peff.a[k] = pt.a[k] - pf.a[k];
+        const std::string d = outdir + "/";
+        append_row(d + "EVO_Vslip.txt", r.timesum, r.dt, VSLIPB, line_fault);
+        append_row(d + "EVO_viscosity.txt", r.timesum, r.dt, ETA, line_fault);
+        append_row(d + "EVO_press_flu.txt", r.timesum, r.dt, pf, line_fault);
+        append_row(d + "EVO_press_eff.txt", r.timesum, r.dt, Peff, line_fault);
+        append_row(d + "EVO_SigmaY.txt", r.timesum, r.dt, SigmaY, line_fault);
+        append_row(d + "EVO_Sii.txt", r.timesum, r.dt, SII_fault, line_fault);
+        append_row(d + "EVO_Theta.txt", r.timesum, r.dt, OM, line_fault);
+        append_row(d + "EVO_Visc_comp.txt", r.timesum, r.dt, VIS_COMP, line_fault);
+        append_row(d + "EVO_Elast_comp.txt", r.timesum, r.dt, EL_DECOM, line_fault);
+        append_row(d + "EVO_vxD.txt", r.timesum, r.dt, vxD, line_fault);
+        FILE* f = fopen((d + "EVO_data.txt").c_str(), "a");
+        if (f) {
+            fprintf(f, "%20g%20g%20g%20d%20d\n", r.timesum, r.dt, r.Vmax, r.ynlast, r.global_iters);
+            fclose(f);
+        }
+    }
+    hmec_destroy(ctx);
+    return 0;
+}

@@ -69,7 +69,28 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
             print(r.stdout + r.stderr)
             raise RuntimeError("link of libhmec_gpu.so failed")
         os.replace(tmp, LIB)
+    build_driver(force)
     return LIB
+
+
+DRIVER_SRC = os.path.join(os.path.dirname(PKG), "driver", "hmec_run.cpp")
+DRIVER = os.path.join(OUT_DIR, "hmec_run")
+
+
+def build_driver(force: bool = False) -> str:
+    """The C++ host loop mirroring the reference's main(), linked to the library."""
+    if not force and not _stale(DRIVER, [DRIVER_SRC, LIB, os.path.join(INC, "hmec.h")]):
+        return DRIVER
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", INC, DRIVER_SRC, "-o", DRIVER + ".tmp",
+           "-L", OUT_DIR, "-lhmec_gpu", "-Wl,-rpath," + OUT_DIR]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        print(" ".join(cmd))
+        print(r.stdout + r.stderr)
+        raise RuntimeError("build of hmec_run failed")
+    os.replace(DRIVER + ".tmp", DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":
