@@ -175,6 +175,16 @@ __device__ __forceinline__ void vanka_colour(const SmoothArgs<T>& a, int ri, int
         if (valid) {
             i = fi + 3 * (pidx % ni);
             j = fj + 3 * (pidx / ni);
+        }
+        // this lane's row of the patch inverse, loaded before the residual so
+        // its latency overlaps the residual's gathers
+        T pr[PB];
+        {
+            const T* P = a.pinv + (size_t)((j - 1) * (g.Ny - 1) + (i - 1)) * 100 + (q < PB ? q : 0) * PB;
+#pragma unroll
+            for (int c = 0; c < PB; c++) pr[c] = (valid && q < PB) ? P[c] : (T)0;
+        }
+        if (valid) {
             if (q < PB) {
                 row = patch_unknown(i, j, g.Ny1, q);
                 T acc = a.b[row];
@@ -186,12 +196,11 @@ __device__ __forceinline__ void vanka_colour(const SmoothArgs<T>& a, int ri, int
                 r = acc;
             }
         }
-        const T* P = a.pinv + (size_t)((j - 1) * (g.Ny - 1) + (i - 1)) * 100 + q * PB;
         T d = 0;
 #pragma unroll
         for (int c = 0; c < PB; c++) {
             const T rc = __shfl_sync(0xffffffffu, r, (lane & 16) + c);
-            if (valid && q < PB) d += P[c] * rc;
+            d += pr[c] * rc;
         }
         if (valid && q < PB) a.x[row] += d;
     }
@@ -1002,7 +1011,9 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
         HMEC_LAUNCH_B(ctx, bytes, (k_smooth<T, false>), 1, SM_BS, 0, a, nsweeps, mode);
         return HMEC_OK;
     }
-    const long long work = std::max<long long>((long long)L.npatch * 16 / 9, L.g.N);
+    // size the grid to one colour phase (the zero/prolongation and boundary
+    // phases are grid-stride loops); fewer blocks make the grid barrier cheaper
+    const long long work = std::max<long long>((long long)L.npatch * 16 / 9 + SM_BS, 2LL * SM_BS);
     const int grid = (int)std::min<long long>(max_coop_blocks<T>(ctx), std::max<long long>(1, (work + SM_BS - 1) / SM_BS));
     void* args[] = {&a, &nsweeps, &mode};
     const bool prof = hmec_prof_begin(ctx, "k_smooth", bytes);
