@@ -283,6 +283,44 @@ __global__ void __launch_bounds__(SM_BS) k_smooth(SmoothArgs<T> a, int nsweeps, 
     }
 }
 
+// The same pass for a small level on one 1024-thread block, with the level's
+// x, b and boundary deltas in shared memory: block barriers instead of grid
+// barriers and the x gathers of every residual served from shared memory.
+// The matrix rows and inverses still come from L2 through the read-only path.
+constexpr int SMEM_BS = 1024;
+template <typename T>
+__global__ void __launch_bounds__(SMEM_BS) k_smooth_smem(SmoothArgs<T> a, int nsweeps, int mode) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* xs = reinterpret_cast<T*>(smem_raw);
+    T* bs = xs + a.g.N;
+    T* ts = bs + a.g.N;
+    const int tid = threadIdx.x, nth = blockDim.x;
+    for (int t = tid; t < a.g.N; t += nth) {
+        bs[t] = a.b[t];
+        xs[t] = (mode == 0) ? (T)0 : a.x[t];
+    }
+    __syncthreads();
+    if (mode == 1) {
+        prolong_add(a.g, a.gc, a.xc, xs, tid, nth);
+        __syncthreads();
+    }
+    SmoothArgs<T> s = a;
+    s.x = xs;
+    s.b = bs;
+    s.tmp = ts;
+    for (int k = 0; k < nsweeps; k++) {
+        for (int c = 0; c < 9; c++) {
+            vanka_colour(s, c / 3, c % 3, tid >> 5, nth >> 5);
+            __syncthreads();
+        }
+        bnd_delta(s, tid, nth);
+        __syncthreads();
+        for (int t = tid; t < s.nbnd; t += nth) xs[s.bnd[t]] += ts[t];
+        __syncthreads();
+    }
+    for (int t = tid; t < a.g.N; t += nth) a.x[t] = xs[t];
+}
+
 // ------------------------------------------------ multigrid restriction
 // Whether the row of unknown v at staggered cell (i, j) is an interior
 // equation (x/y-Stokes, continuity, Darcy) rather than a boundary or ghost
@@ -970,6 +1008,9 @@ struct LvPtr<float> {
 // barrier is cheaper than a grid barrier, but one block leaves the GPU idle:
 // measured slower than a small cooperative grid for every level size here).
 constexpr int SINGLE_BLOCK_PATCHES = 0;
+// Levels whose x, b and boundary deltas fit in this much shared memory are
+// smoothed by k_smooth_smem (one block, everything but the matrix on chip).
+constexpr size_t SMEM_LIMIT = 200 * 1024;
 
 template <typename T>
 static int max_coop_blocks(hmec_ctx* ctx) {
@@ -1009,6 +1050,17 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
     const double bytes = nsweeps * ((double)L.npatch * bpp + bnd) + (double)L.g.N * st * (mode ? 2.5 : 1.0);
     if (L.npatch <= SINGLE_BLOCK_PATCHES) {
         HMEC_LAUNCH_B(ctx, bytes, (k_smooth<T, false>), 1, SM_BS, 0, a, nsweeps, mode);
+        return HMEC_OK;
+    }
+    const size_t smem = (2 * (size_t)L.g.N + (size_t)L.nbnd) * sizeof(T);
+    if (smem <= SMEM_LIMIT) {
+        static bool attr_set[2] = {false, false};
+        if (!attr_set[sizeof(T) == 8 ? 0 : 1]) {
+            HMEC_CUDA(ctx, cudaFuncSetAttribute(k_smooth_smem<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)SMEM_LIMIT));
+            attr_set[sizeof(T) == 8 ? 0 : 1] = true;
+        }
+        HMEC_LAUNCH_B(ctx, bytes, k_smooth_smem<T>, 1, SMEM_BS, smem, a, nsweeps, mode);
         return HMEC_OK;
     }
     // size the grid to one colour phase (the zero/prolongation and boundary
