@@ -71,6 +71,13 @@ struct Level {
     // the scaled system rhs, pb the preconditioner input of the FP64 form
     double *dx_, *db, *dr, *pb;
     float *fx, *fb, *fr;
+    // tiled smoother: tiles of tsz x tsz patches, one block each; every
+    // unknown has one owning tile (owner[N]); own_start/own_list and
+    // bnd_start/bnd_list list each tile's owned unknowns and boundary rows
+    int tsz, ntile_i, ntiles;
+    int32_t *owner, *own_start, *own_list, *tbnd_start, *tbnd_list;
+    double* dx2;
+    float* fx2;
     // coarse-level coefficient fields (owned for l > 0)
     std::vector<double*> owned;
     AsmFields af;

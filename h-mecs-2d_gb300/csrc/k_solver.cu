@@ -321,6 +321,120 @@ __global__ void __launch_bounds__(SMEM_BS) k_smooth_smem(SmoothArgs<T> a, int ns
     for (int t = tid; t < a.g.N; t += nth) a.x[t] = xs[t];
 }
 
+// ------------------------------------------------ tiled smoothing pass
+// Each block owns tiles of TILE x TILE patches.  Every unknown has exactly one
+// owning tile (its cell's patch, a shared face going to the patch on its right
+// or below, a boundary row to the adjacent patch).  During a sweep a tile reads
+// the unknowns it owns from the live buffer Q and all others from the
+// snapshot P, and writes only its own unknowns to Q; so tiles are independent
+// within a sweep (deterministic, no races) and only one grid-wide barrier per
+// sweep is needed.  Inside a tile the 9 colour classes and the boundary rows
+// run in sequence with block barriers: a multiplicative Vanka sweep per tile,
+// additive across tile borders.
+constexpr int TILE = 12;
+constexpr int TILE_BS = 256;  // 16 lanes x at most 16 patches of one colour in a tile
+
+template <typename T>
+struct TileArgs {
+    SmoothArgs<T> a;
+    T* xalt;
+    const int32_t *owner, *own_start, *own_list, *tb_start, *tb_list;
+    int ntile_i, ntiles;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(TILE_BS) k_smooth_tiled(TileArgs<T> t, int nsweeps, int mode) {
+    const SmoothArgs<T>& a = t.a;
+    const Geo& g = a.g;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    T* P = a.x;
+    T* Q = t.xalt;
+    if (mode == 0) {
+        for (int r = tid; r < g.N; r += nth) P[r] = (T)0;
+    } else {
+        prolong_add(g, a.gc, a.xc, P, tid, nth);
+    }
+    cg::this_grid().sync();
+    const int lane = threadIdx.x & 31, q = lane & 15, slot = threadIdx.x >> 4;
+    for (int s = 0; s < nsweeps; s++) {
+        for (int tile = blockIdx.x; tile < t.ntiles; tile += gridDim.x) {
+            const int ti = tile % t.ntile_i, tj = tile / t.ntile_i;
+            const int i0 = 1 + ti * TILE, j0 = 1 + tj * TILE;
+            const int i1 = min(i0 + TILE, g.Ny), j1 = min(j0 + TILE, g.Nx);  // exclusive
+            for (int k = t.own_start[tile] + threadIdx.x; k < t.own_start[tile + 1]; k += blockDim.x) {
+                const int u = t.own_list[k];
+                Q[u] = P[u];
+            }
+            __syncthreads();
+            for (int c = 0; c < 9; c++) {
+                const int ri = c / 3, rj = c % 3;
+                const int fi = i0 + ((ri - i0 % 3) + 3) % 3, fj = j0 + ((rj - j0 % 3) + 3) % 3;
+                const int ni = fi < i1 ? (i1 - 1 - fi) / 3 + 1 : 0;
+                const int nj = fj < j1 ? (j1 - 1 - fj) / 3 + 1 : 0;
+                const bool valid = slot < ni * nj;
+                int i = i0, j = j0, row = 0;
+                if (valid) {
+                    i = fi + 3 * (slot % ni);
+                    j = fj + 3 * (slot / ni);
+                }
+                T pr[PB];
+                {
+                    const T* Pi = a.pinv + (size_t)((j - 1) * (g.Ny - 1) + (i - 1)) * 100 + (q < PB ? q : 0) * PB;
+#pragma unroll
+                    for (int cc = 0; cc < PB; cc++) pr[cc] = (valid && q < PB) ? Pi[cc] : (T)0;
+                }
+                T r = 0;
+                bool mine = false;
+                if (valid && q < PB) {
+                    row = patch_unknown(i, j, g.Ny1, q);
+                    mine = t.owner[row] == tile;
+                    T acc = a.b[row];
+#pragma unroll
+                    for (int sl = 0; sl < HMEC_W; sl++) {
+                        const size_t o = (size_t)sl * g.N + row;
+                        const int cl = a.col[o];
+                        const T xv = (t.owner[cl] == tile) ? Q[cl] : P[cl];
+                        acc -= a.val[o] * xv;
+                    }
+                    r = acc;
+                }
+                T d = 0;
+#pragma unroll
+                for (int cc = 0; cc < PB; cc++) {
+                    const T rc = __shfl_sync(0xffffffffu, r, (lane & 16) + cc);
+                    d += pr[cc] * rc;
+                }
+                if (mine) Q[row] += d;
+                __syncthreads();
+            }
+            // this tile's boundary rows: one Jacobi pass
+            for (int k = t.tb_start[tile] + threadIdx.x; k < t.tb_start[tile + 1]; k += blockDim.x) {
+                const int row = t.tb_list[k];
+                T acc = a.b[row], diag = 0;
+#pragma unroll
+                for (int sl = 0; sl < HMEC_W; sl++) {
+                    const size_t o = (size_t)sl * g.N + row;
+                    const int cl = a.col[o];
+                    const T v = a.val[o];
+                    acc -= v * ((t.owner[cl] == tile) ? Q[cl] : P[cl]);
+                    if (cl == row) diag += v;
+                }
+                a.tmp[k] = diag != 0 ? acc / diag : (T)0;
+            }
+            __syncthreads();
+            for (int k = t.tb_start[tile] + threadIdx.x; k < t.tb_start[tile + 1]; k += blockDim.x)
+                Q[t.tb_list[k]] += a.tmp[k];
+            __syncthreads();
+        }
+        cg::this_grid().sync();
+        T* sw = P;
+        P = Q;
+        Q = sw;
+    }
+    if (P != a.x)
+        for (int r = tid; r < g.N; r += nth) a.x[r] = P[r];
+}
+
 // ------------------------------------------------ multigrid restriction
 // Whether the row of unknown v at staggered cell (i, j) is an interior
 // equation (x/y-Stokes, continuity, Darcy) rather than a boundary or ghost
@@ -801,16 +915,76 @@ static int alloc_level(hmec_ctx* ctx, Level& L, bool mixed, bool coarse) {
     L.fx = L.fb = L.fr = nullptr;
     L.dx_ = L.db = L.dr = L.pb = nullptr;
     HMEC_CUDA(ctx, cudaMalloc(&L.db, sizeof(double) * N));  // fine: scaled rhs; coarse: FP64 rhs
+    L.dx2 = nullptr;
+    L.fx2 = nullptr;
     if (mixed) {
         HMEC_CUDA(ctx, cudaMalloc(&L.val32, sizeof(float) * HMEC_W * N));
         HMEC_CUDA(ctx, cudaMalloc(&L.pinv32, sizeof(float) * 100 * (size_t)L.npatch));
         HMEC_CUDA(ctx, cudaMalloc(&L.fx, sizeof(float) * N));
+        HMEC_CUDA(ctx, cudaMalloc(&L.fx2, sizeof(float) * N));
         HMEC_CUDA(ctx, cudaMalloc(&L.fb, sizeof(float) * N));
         HMEC_CUDA(ctx, cudaMalloc(&L.fr, sizeof(float) * std::max(N, (size_t)L.nbnd)));
     } else {
         HMEC_CUDA(ctx, cudaMalloc(&L.pinv, sizeof(double) * 100 * (size_t)L.npatch));
         HMEC_CUDA(ctx, cudaMalloc(&L.dx_, sizeof(double) * N));
+        HMEC_CUDA(ctx, cudaMalloc(&L.dx2, sizeof(double) * N));
         HMEC_CUDA(ctx, cudaMalloc(&L.dr, sizeof(double) * std::max(N, (size_t)L.nbnd)));
+    }
+    {
+        // tile ownership of every unknown (see k_smooth_tiled)
+        L.tsz = TILE;
+        L.ntile_i = (g.Ny - 1 + TILE - 1) / TILE;
+        const int ntile_j = (g.Nx - 1 + TILE - 1) / TILE;
+        L.ntiles = L.ntile_i * ntile_j;
+        auto tile_of = [&](int pi, int pj) { return (pi - 1) / TILE + ((pj - 1) / TILE) * L.ntile_i; };
+        std::vector<int32_t> owner(N);
+        std::vector<char> isb(N, 0);
+        for (int32_t r : br) isb[r] = 1;
+        for (int j = 0; j <= g.Nx; j++)
+            for (int i = 0; i <= g.Ny; i++)
+                for (int v = 0; v < 6; v++) {
+                    const int u = (j * g.Ny1 + i) * 6 + v;
+                    int pi, pj;
+                    if (isb[u]) {  // boundary row: the adjacent patch
+                        pi = std::min(std::max(i, 1), g.Ny - 1);
+                        pj = std::min(std::max(j, 1), g.Nx - 1);
+                    } else if (v == 0 || v == 3) {
+                        pi = i;
+                        pj = j;
+                    } else if (v == 1 || v == 4) {  // x face: the patch on its right
+                        pi = i;
+                        pj = (j + 1 <= g.Nx - 1) ? j + 1 : j;
+                    } else {  // y face: the patch below
+                        pi = (i + 1 <= g.Ny - 1) ? i + 1 : i;
+                        pj = j;
+                    }
+                    owner[u] = tile_of(pi, pj);
+                }
+        std::vector<int32_t> os(L.ntiles + 1, 0), bs(L.ntiles + 1, 0);
+        for (size_t u = 0; u < N; u++) {
+            os[owner[u] + 1]++;
+            if (isb[u]) bs[owner[u] + 1]++;
+        }
+        for (int k = 0; k < L.ntiles; k++) {
+            os[k + 1] += os[k];
+            bs[k + 1] += bs[k];
+        }
+        std::vector<int32_t> ol(N), bl(std::max<size_t>(br.size(), 1)), oc(os.begin(), os.end() - 1),
+            bc(bs.begin(), bs.end() - 1);
+        for (size_t u = 0; u < N; u++) {
+            ol[oc[owner[u]]++] = (int32_t)u;
+            if (isb[u]) bl[bc[owner[u]]++] = (int32_t)u;
+        }
+        HMEC_CUDA(ctx, cudaMalloc(&L.owner, sizeof(int32_t) * N));
+        HMEC_CUDA(ctx, cudaMalloc(&L.own_start, sizeof(int32_t) * os.size()));
+        HMEC_CUDA(ctx, cudaMalloc(&L.own_list, sizeof(int32_t) * N));
+        HMEC_CUDA(ctx, cudaMalloc(&L.tbnd_start, sizeof(int32_t) * bs.size()));
+        HMEC_CUDA(ctx, cudaMalloc(&L.tbnd_list, sizeof(int32_t) * bl.size()));
+        HMEC_CUDA(ctx, cudaMemcpy(L.owner, owner.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice));
+        HMEC_CUDA(ctx, cudaMemcpy(L.own_start, os.data(), sizeof(int32_t) * os.size(), cudaMemcpyHostToDevice));
+        HMEC_CUDA(ctx, cudaMemcpy(L.own_list, ol.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice));
+        HMEC_CUDA(ctx, cudaMemcpy(L.tbnd_start, bs.data(), sizeof(int32_t) * bs.size(), cudaMemcpyHostToDevice));
+        HMEC_CUDA(ctx, cudaMemcpy(L.tbnd_list, bl.data(), sizeof(int32_t) * bl.size(), cudaMemcpyHostToDevice));
     }
     if (coarse) {
         const size_t nb = (size_t)g.Nx * g.Ny, ns = (size_t)g.Nx1 * g.Ny1;
@@ -937,6 +1111,13 @@ void solver_free(hmec_ctx* ctx) {
         cudaFree(L.fx);
         cudaFree(L.fb);
         cudaFree(L.fr);
+        cudaFree(L.dx2);
+        cudaFree(L.fx2);
+        cudaFree(L.owner);
+        cudaFree(L.own_start);
+        cudaFree(L.own_list);
+        cudaFree(L.tbnd_start);
+        cudaFree(L.tbnd_list);
         for (double* p : L.owned) cudaFree(p);
     }
     sv.lv.clear();
@@ -1025,6 +1206,30 @@ static int max_coop_blocks(hmec_ctx* ctx) {
     return c;
 }
 
+template <typename T>
+static int max_tiled_blocks(hmec_ctx* ctx) {
+    static int cached[2] = {0, 0};
+    int& c = cached[sizeof(T) == 8 ? 0 : 1];
+    if (c == 0) {
+        int per_sm = 0, nsm = 0;
+        HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth_tiled<T>, TILE_BS, 0));
+        HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
+        c = std::max(1, per_sm * nsm);
+    }
+    return c;
+}
+
+template <typename T>
+static T* x_alt(Level& L);
+template <>
+double* x_alt<double>(Level& L) {
+    return L.dx2;
+}
+template <>
+float* x_alt<float>(Level& L) {
+    return L.fx2;
+}
+
 // One smoothing pass on level l (x = 0 or x += P xc first, then nsweeps sweeps).
 template <typename T>
 static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mode) {
@@ -1050,6 +1255,29 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
     const double bytes = nsweeps * ((double)L.npatch * bpp + bnd) + (double)L.g.N * st * (mode ? 2.5 : 1.0);
     if (L.npatch <= SINGLE_BLOCK_PATCHES) {
         HMEC_LAUNCH_B(ctx, bytes, (k_smooth<T, false>), 1, SM_BS, 0, a, nsweeps, mode);
+        return HMEC_OK;
+    }
+    if (!(ctx->p.mg_flags & HMEC_MG_UNTILED)) {
+        TileArgs<T> t;
+        t.a = a;
+        t.xalt = x_alt<T>(L);
+        t.owner = L.owner;
+        t.own_start = L.own_start;
+        t.own_list = L.own_list;
+        t.tb_start = L.tbnd_start;
+        t.tb_list = L.tbnd_list;
+        t.ntile_i = L.ntile_i;
+        t.ntiles = L.ntiles;
+        // the owner tests add one int per matrix entry read and the second buffer
+        const double tb = nsweeps * ((double)L.npatch * (10.0 * HMEC_W * 4 + 10.0 * HMEC_W * st) +
+                                     (double)L.g.N * (2 * st + 8)) + bytes;
+        const int grid = std::min(L.ntiles, max_tiled_blocks<T>(ctx));
+        void* args[] = {&t, &nsweeps, &mode};
+        const bool prof = hmec_prof_begin(ctx, "k_smooth", tb);
+        HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_smooth_tiled<T>, dim3(grid), dim3(TILE_BS), args, 0,
+                                                   ctx->stream));
+        ctx->launches++;
+        if (prof) hmec_prof_end(ctx);
         return HMEC_OK;
     }
     const size_t smem = (2 * (size_t)L.g.N + (size_t)L.nbnd) * sizeof(T);

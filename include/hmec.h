@@ -105,7 +105,12 @@ enum hmec_mg_flags {
     /* Darcy resistance eta_f/k of a coarse face: conductances averaged across
      * the flow direction (parallel paths), resistances along it (series);
      * otherwise plain arithmetic averages. */
-    HMEC_MG_DARCY_HARMONIC = 1
+    HMEC_MG_DARCY_HARMONIC = 1,
+    /* Smooth each level with one grid-wide barrier per Vanka colour class
+     * (a true multiplicative sweep over the whole level) instead of the
+     * default tiled sweep (multiplicative inside 12x12-patch tiles, the
+     * neighbours' unknowns taken from the start of the sweep). */
+    HMEC_MG_UNTILED = 2
 };
 
 /* ------------------------------------------------------------- node fields */
