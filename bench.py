@@ -108,7 +108,7 @@ def make_model(form, cfg, device_index):
     import hmec
     from hmec import synth
 
-    over = dict(synth.PRESETS[cfg], form=form, krylov_rtol=1e-14, krylov_restart=40, krylov_maxit=4000)
+    over = dict(synth.PRESETS[cfg], form=form, krylov_rtol=1e-15, krylov_restart=40, krylov_maxit=4000)
     p = hmec.default_params(**over)
     m = hmec.Model(p)
     mk, nodes = synth.make_state(p, cfg)
@@ -339,7 +339,7 @@ def main():
         "ms_per_step": mx["ms"] / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64/f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "form": "mixed: FP64 FGMRES(40), FP32 Vanka multigrid preconditioner",
-                   "krylov_rtol": 1e-14, "l2": "inputs larger than L2 (1M markers x 19 FP64 arrays = 152 MB); "
+                   "krylov_rtol": 1e-15, "l2": "inputs larger than L2 (1M markers x 19 FP64 arrays = 152 MB); "
                    "256 MB buffer written between timed steps", "parallelism": "replicas" if world > 1 else "single",
                    "global_iters_per_step": mx["gi"] / K, "krylov_iters_per_step": mx["kr"] / K,
                    "global_iterations_per_s": world * mx["gi"] / (mx["ms"] / 1e3)},

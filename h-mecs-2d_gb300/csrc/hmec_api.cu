@@ -153,7 +153,7 @@ void hmec_params_default(hmec_params* p) {
     p->num_timesteps = 100000;
     // library extensions
     p->form = HMEC_FORM_FP64;
-    p->krylov_rtol = 1e-14;
+    p->krylov_rtol = 1e-15;
     p->krylov_restart = 40;
     p->krylov_maxit = 2000;
     p->mg_levels = 6;

@@ -86,7 +86,9 @@ typedef struct hmec_params {
 
     /* ---- extensions of this library (no counterpart in constants.hpp) ---- */
     int32_t form;             /* enum hmec_form */
-    double krylov_rtol;       /* FGMRES tolerance on the row-equilibrated residual (1e-14) */
+    double krylov_rtol;       /* FGMRES tolerance on the row-equilibrated residual (1e-15);
+                                 a restart cycle that gains less than 2x ends the solve,
+                                 accepted when within 100x of it (FP64 rounding floor) */
     int32_t krylov_restart;   /* FGMRES restart length m */
     int32_t krylov_maxit;     /* total FGMRES iteration cap per solve */
     int32_t mg_levels;        /* max multigrid levels (1 = Vanka smoother only) */

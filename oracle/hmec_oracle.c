@@ -135,7 +135,7 @@ void hmo_params_default(hmec_params* p) {
     p->tyield = 1;
     p->num_timesteps = 100000;
     p->form = HMEC_FORM_FP64;
-    p->krylov_rtol = 1e-14;
+    p->krylov_rtol = 1e-15;
     p->krylov_restart = 40;
     p->krylov_maxit = 2000;
     p->mg_levels = 6;

@@ -6,9 +6,9 @@ import numpy as np
 import oracle as O
 from hmec import synth
 
-# Solver settings shared by the parity tests: FGMRES to 1e-14 on the
-# row-equilibrated residual (the plain form's tolerance).
-SOLVER = dict(krylov_rtol=1e-14, krylov_restart=40, krylov_maxit=4000)
+# Solver settings shared by the parity tests: FGMRES to 1e-15 on the
+# row-equilibrated residual.
+SOLVER = dict(krylov_rtol=1e-15, krylov_restart=40, krylov_maxit=4000)
 
 # Fields compared after a section / step (velocity, pressure, stress, slip rate, state).
 STEP_FIELDS = ["pt", "vxs", "vys", "pf", "vxD", "vyD", "SXX", "SYY", "SXY", "VSLIPB", "OM", "OM0", "ETA",
