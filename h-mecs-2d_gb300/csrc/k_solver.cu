@@ -340,6 +340,7 @@ struct TileArgs {
     T* xalt;
     const int32_t *owner, *own_start, *own_list, *tb_start, *tb_list;
     int ntile_i, ntiles;
+    T* r_out;  // if set, r = b - A x is written after the last sweep
 };
 
 template <typename T>
@@ -433,6 +434,155 @@ __global__ void __launch_bounds__(TILE_BS) k_smooth_tiled(TileArgs<T> t, int nsw
     }
     if (P != a.x)
         for (int r = tid; r < g.N; r += nth) a.x[r] = P[r];
+}
+
+// Tiled pass with the tile's window of unknowns staged in shared memory.
+// Window = the cells the tile's patch rows and boundary rows can read (the
+// tile's patches extended by two cells up/left and one down/right), at most
+// (TILE+3)^2 cells.  Per sweep: load the window from P, run the 9 colour
+// classes and the boundary rows on shared memory (unknowns the tile does not
+// own stay at their P values: the same additive-across-tiles rule as
+// k_smooth_tiled, bit for bit), write the owned unknowns to Q.  A matrix
+// column maps to its window slot from its offset to the row: delta = col -
+// row = dj*6*Ny1 + (di*6 + dv) with |di*6 + dv| < 12, so dj follows from two
+// comparisons and the window offset is dj*6*WI + (delta - dj*6*Ny1).
+constexpr int WIN_MAX = (TILE + 3) * (TILE + 3) * 6;
+
+template <typename T>
+__global__ void __launch_bounds__(TILE_BS) k_smooth_win(TileArgs<T> t, int nsweeps, int mode) {
+    __shared__ T xs[WIN_MAX];
+    __shared__ unsigned char own[WIN_MAX];
+    const SmoothArgs<T>& a = t.a;
+    const Geo& g = a.g;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const int RS = 6 * g.Ny1;
+    T* P = a.x;
+    T* Q = t.xalt;
+    if (mode == 0) {
+        for (int r = tid; r < g.N; r += nth) P[r] = (T)0;
+    } else {
+        prolong_add(g, a.gc, a.xc, P, tid, nth);
+    }
+    cg::this_grid().sync();
+    const int lane = threadIdx.x & 31, q = lane & 15, slot = threadIdx.x >> 4;
+    for (int s = 0; s < nsweeps; s++) {
+        for (int tile = blockIdx.x; tile < t.ntiles; tile += gridDim.x) {
+            const int ti = tile % t.ntile_i, tj = tile / t.ntile_i;
+            const int i0 = 1 + ti * TILE, j0 = 1 + tj * TILE;
+            const int i1 = min(i0 + TILE, g.Ny), j1 = min(j0 + TILE, g.Nx);  // exclusive
+            const int wi0 = max(i0 - 2, 0), wj0 = max(j0 - 2, 0);
+            const int WI = min(i1, g.Ny) - wi0 + 1, WJ = min(j1, g.Nx) - wj0 + 1;
+            const int W = WI * WJ * 6, SJ = 6 * WI;
+            // stage the window
+            for (int lw = threadIdx.x; lw < W; lw += blockDim.x) {
+                const int lc = lw / 6, v = lw - 6 * lc;
+                const int cj = wj0 + lc / WI, ci = wi0 + lc % WI;
+                const int gw = (cj * g.Ny1 + ci) * 6 + v;
+                xs[lw] = P[gw];
+                own[lw] = (t.owner[gw] == tile) ? 1 : 0;
+            }
+            __syncthreads();
+            for (int c = 0; c < 9; c++) {
+                const int ri = c / 3, rj = c % 3;
+                const int fi = i0 + ((ri - i0 % 3) + 3) % 3, fj = j0 + ((rj - j0 % 3) + 3) % 3;
+                const int ni = fi < i1 ? (i1 - 1 - fi) / 3 + 1 : 0;
+                const int nj = fj < j1 ? (j1 - 1 - fj) / 3 + 1 : 0;
+                const bool valid = slot < ni * nj;
+                int i = i0, j = j0;
+                if (valid) {
+                    i = fi + 3 * (slot % ni);
+                    j = fj + 3 * (slot / ni);
+                }
+                T pr[PB];
+                {
+                    const T* Pi = a.pinv + (size_t)((j - 1) * (g.Ny - 1) + (i - 1)) * 100 + (q < PB ? q : 0) * PB;
+#pragma unroll
+                    for (int cc = 0; cc < PB; cc++) pr[cc] = (valid && q < PB) ? Pi[cc] : (T)0;
+                }
+                T r = 0;
+                int lrow = 0;
+                if (valid && q < PB) {
+                    const int row = patch_unknown(i, j, g.Ny1, q);
+                    // cell of unknown q: (i, j), left (i, j-1) or top (i-1, j)
+                    const int ci = (q == 4 || q == 8) ? i - 1 : i;
+                    const int cj = (q == 2 || q == 6) ? j - 1 : j;
+                    lrow = ((cj - wj0) * WI + (ci - wi0)) * 6 + (row - 6 * (row / 6));
+                    T acc = a.b[row];
+#pragma unroll
+                    for (int sl = 0; sl < HMEC_W; sl++) {
+                        const size_t o = (size_t)sl * g.N + row;
+                        const int delta = a.col[o] - row;
+                        const int dj = delta > RS / 2 ? 1 : (delta < -RS / 2 ? -1 : 0);
+                        acc -= a.val[o] * xs[lrow + dj * SJ + (delta - dj * RS)];
+                    }
+                    r = acc;
+                }
+                T d = 0;
+#pragma unroll
+                for (int cc = 0; cc < PB; cc++) {
+                    const T rc = __shfl_sync(0xffffffffu, r, (lane & 16) + cc);
+                    d += pr[cc] * rc;
+                }
+                // same-class patches never read each other's unknowns, and the
+                // shuffles above order this patch's reads before its writes
+                if (valid && q < PB && own[lrow]) xs[lrow] += d;
+                __syncthreads();
+            }
+            // this tile's boundary rows: one Jacobi pass on the window
+            const int kb = t.tb_start[tile], ke = t.tb_start[tile + 1];
+            for (int k = kb + threadIdx.x; k < ke; k += blockDim.x) {
+                const int row = t.tb_list[k];
+                const int cell = row / 6;
+                const int lr = (((cell / g.Ny1) - wj0) * WI + ((cell % g.Ny1) - wi0)) * 6 + (row - 6 * cell);
+                T acc = a.b[row], diag = 0;
+#pragma unroll
+                for (int sl = 0; sl < HMEC_W; sl++) {
+                    const size_t o = (size_t)sl * g.N + row;
+                    const int cl = a.col[o];
+                    const int delta = cl - row;
+                    const int dj = delta > RS / 2 ? 1 : (delta < -RS / 2 ? -1 : 0);
+                    const T v = a.val[o];
+                    acc -= v * xs[lr + dj * SJ + (delta - dj * RS)];
+                    if (cl == row) diag += v;
+                }
+                a.tmp[k] = diag != 0 ? acc / diag : (T)0;
+            }
+            __syncthreads();
+            for (int k = kb + threadIdx.x; k < ke; k += blockDim.x) {
+                const int row = t.tb_list[k];
+                const int cell = row / 6;
+                const int lr = (((cell / g.Ny1) - wj0) * WI + ((cell % g.Ny1) - wi0)) * 6 + (row - 6 * cell);
+                xs[lr] += a.tmp[k];
+            }
+            __syncthreads();
+            // publish the owned unknowns
+            for (int lw = threadIdx.x; lw < W; lw += blockDim.x) {
+                if (!own[lw]) continue;
+                const int lc = lw / 6, v = lw - 6 * lc;
+                const int cj = wj0 + lc / WI, ci = wi0 + lc % WI;
+                Q[(cj * g.Ny1 + ci) * 6 + v] = xs[lw];
+            }
+            __syncthreads();
+        }
+        cg::this_grid().sync();
+        T* sw = P;
+        P = Q;
+        Q = sw;
+    }
+    if (P != a.x)
+        for (int r = tid; r < g.N; r += nth) a.x[r] = P[r];
+    if (t.r_out) {  // residual for the restriction, fused to save a launch
+        cg::this_grid().sync();
+        for (int row = tid; row < g.N; row += nth) {
+            T acc = a.b[row];
+#pragma unroll
+            for (int sl = 0; sl < HMEC_W; sl++) {
+                const size_t o = (size_t)sl * g.N + row;
+                acc -= a.val[o] * a.x[a.col[o]];
+            }
+            t.r_out[row] = acc;
+        }
+    }
 }
 
 // ------------------------------------------------ multigrid restriction
@@ -648,6 +798,32 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
             C.ETADY[oc] = 1;
         }
     }
+}
+
+// The same restriction from a residual the pre-smoothing pass already wrote.
+template <typename T>
+__global__ void k_restrict_r(Geo gf, Geo gc, const T* __restrict__ rf, const double* __restrict__ dsf,
+                             const double* __restrict__ dsc, T* bc) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= gc.Ny1 * gc.Nx1 * 6) return;
+    const int v = t % 6, cell = t / 6, I = cell % gc.Ny1, J = cell / gc.Ny1;
+    double s = 0, w = 0;
+    if (row_interior(gc, I, J, v)) {
+        int i0 = 2 * I - 1, i1 = 2 * I, j0 = 2 * J - 1, j1 = 2 * J;
+        if (v == 1 || v == 4) j1 = 2 * J + 1;
+        if (v == 2 || v == 5) i1 = 2 * I + 1;
+        for (int i = i0; i <= i1; i++)
+            for (int j = j0; j <= j1; j++) {
+                if (i < 0 || i > gf.Ny || j < 0 || j > gf.Nx || !row_interior(gf, i, j, v)) continue;
+                double ww = 1.0;
+                if ((v == 1 || v == 4) && j != 2 * J) ww = 0.5;
+                if ((v == 2 || v == 5) && i != 2 * I) ww = 0.5;
+                const int k = kp_of(i, j, gf.Ny1) + v;
+                s += ww * ((double)rf[k] / dsf[k]);
+                w += ww;
+            }
+    }
+    bc[t] = (T)(w > 0 ? (s / w) * dsc[t] : 0.0);
 }
 
 template <typename S, typename D>
@@ -1212,7 +1388,7 @@ static int max_tiled_blocks(hmec_ctx* ctx) {
     int& c = cached[sizeof(T) == 8 ? 0 : 1];
     if (c == 0) {
         int per_sm = 0, nsm = 0;
-        HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth_tiled<T>, TILE_BS, 0));
+        HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth_win<T>, TILE_BS, 0));
         HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
         c = std::max(1, per_sm * nsm);
     }
@@ -1232,7 +1408,7 @@ float* x_alt<float>(Level& L) {
 
 // One smoothing pass on level l (x = 0 or x += P xc first, then nsweeps sweeps).
 template <typename T>
-static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mode) {
+static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mode, T* r_out = nullptr) {
     Solver& sv = ctx->sv;
     Level& L = sv.lv[l];
     SmoothArgs<T> a;
@@ -1268,13 +1444,14 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
         t.tb_list = L.tbnd_list;
         t.ntile_i = L.ntile_i;
         t.ntiles = L.ntiles;
+        t.r_out = r_out;
         // the owner tests add one int per matrix entry read and the second buffer
         const double tb = nsweeps * ((double)L.npatch * (10.0 * HMEC_W * 4 + 10.0 * HMEC_W * st) +
                                      (double)L.g.N * (2 * st + 8)) + bytes;
         const int grid = std::min(L.ntiles, max_tiled_blocks<T>(ctx));
         void* args[] = {&t, &nsweeps, &mode};
         const bool prof = hmec_prof_begin(ctx, "k_smooth", tb);
-        HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_smooth_tiled<T>, dim3(grid), dim3(TILE_BS), args, 0,
+        HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_smooth_win<T>, dim3(grid), dim3(TILE_BS), args, 0,
                                                    ctx->stream));
         ctx->launches++;
         if (prof) hmec_prof_end(ctx);
@@ -1316,10 +1493,18 @@ static int vcycle(hmec_ctx* ctx, size_t l, const T* b_in = nullptr, T* x_in = nu
         const int ns = (sv.lv.size() == 1) ? std::max(1, p.mg_pre + p.mg_post) : std::max(1, p.mg_coarse_sweeps);
         return smooth<T>(ctx, l, b, x, ns, 0);
     }
-    if ((rc = smooth<T>(ctx, l, b, x, p.mg_pre, 0))) return rc;
     Level& C = sv.lv[l + 1];
-    HMEC_LAUNCH(ctx, k_restrict_resid<T>, sgrid(C.g), 64, 0, L.g, C.g, L.col, LvPtr<T>::val(L), b, x, L.dscale,
-                C.dscale, LvPtr<T>::b(C));
+    if (!(p.mg_flags & HMEC_MG_UNTILED)) {
+        // the pre-smoothing pass leaves the residual in the level's r buffer
+        if ((rc = smooth<T>(ctx, l, b, x, p.mg_pre, 0, LvPtr<T>::r(L)))) return rc;
+        const long long nc = (long long)C.g.N;
+        HMEC_LAUNCH(ctx, k_restrict_r<T>, nblocks(nc, 128), 128, 0, L.g, C.g, LvPtr<T>::r(L), L.dscale, C.dscale,
+                    LvPtr<T>::b(C));
+    } else {
+        if ((rc = smooth<T>(ctx, l, b, x, p.mg_pre, 0))) return rc;
+        HMEC_LAUNCH(ctx, k_restrict_resid<T>, sgrid(C.g), 64, 0, L.g, C.g, L.col, LvPtr<T>::val(L), b, x, L.dscale,
+                    C.dscale, LvPtr<T>::b(C));
+    }
     if ((rc = vcycle<T>(ctx, l + 1))) return rc;
     return smooth<T>(ctx, l, b, x, p.mg_post, 1);
 }

@@ -182,9 +182,9 @@ def reference_state(p):
     return reference_markers(p), reference_nodes(p)
 
 
-def config_state(p, name: str, seed: int | None = None):
-    """Seeded synthetic model of benchmark configuration ``name`` on params ``p``."""
-    mat = MATERIALS[name]
+def config_state(p, name: str, seed: int | None = None, mat: dict | None = None):
+    """Seeded synthetic model of benchmark configuration ``name`` (or material ``mat``) on params ``p``."""
+    mat = MATERIALS[name] if mat is None else mat
     seed = SEEDS[name] if seed is None else seed
     rng = np.random.default_rng(seed)
     d = derived(p)
@@ -241,3 +241,34 @@ def make_state(p, preset: str, seed: int | None = None):
     if preset in MATERIALS:
         return config_state(p, preset, seed)
     return reference_state(p)
+
+
+def ensemble_members(n: int = 64, seed: int = 1003, side=(51, 301), mpc: int = 4):
+    """Parameter overrides of the instances of an ensemble (configuration 3).
+
+    Each instance: per-side node counts uniform in ``side`` (uneven grids),
+    ``mpc`` x ``mpc`` markers per cell, the configuration-0 material model on a
+    10 km x 10 km domain, and per-instance rate-and-state a in [0.008, 0.016]
+    and b in [0.012, 0.020] on the velocity-weakening patch, L in
+    [0.005, 0.05] m, and a fault permeability log-uniform in [1e-18, 1e-14] m^2.
+    Returns a list of (overrides, material) pairs for ``instance_state``.
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    base = dict(PRESETS["c0"])
+    for k in range(n):
+        nx = int(rng.integers(side[0], side[1] + 1))
+        ny = int(rng.integers(side[0], side[1] + 1))
+        a = float(rng.uniform(0.008, 0.016))
+        b = float(rng.uniform(0.012, 0.020))
+        L = float(rng.uniform(0.005, 0.05))
+        kf = float(np.exp(np.log(1e-18) + rng.random() * (np.log(1e-14) - np.log(1e-18))))
+        over = dict(base, Nx=nx, Ny=ny, mx=mpc, my=mpc, arsfm=(0.017, a), brsfm=(b, b), lrsfm=(L, L))
+        mat = dict(MATERIALS["c0"], fault_k=(kf, kf))
+        out.append((over, mat, seed * 1000 + k))
+    return out
+
+
+def instance_state(p, mat: dict, seed: int):
+    """Initial state of one ensemble instance (configuration-0 skeleton, member material)."""
+    return config_state(p, "c0", seed, mat=mat)
