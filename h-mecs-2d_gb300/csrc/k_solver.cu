@@ -223,12 +223,62 @@ __device__ __forceinline__ void bnd_delta(const SmoothArgs<T>& a, int tid, int n
     }
 }
 
-// x_f += P x_c: cell-centred unknowns constant, face unknowns linear along
-// the face normal and constant across it (ghost rows map to ghost rows, which
-// keeps the homogeneous boundary relations of the coarse correction).
+// ------------------------------------------------ 1D grid transfer maps
+// A coarse level has ceil(n/2) cells where its fine level has n, over the
+// same length, so coarse and fine points align only when n is even.  The
+// transfers are separable; in each direction there are two point families:
+//   node points j in [0, nf+1] at j*hf (nf+1: the ghost beyond the end), and
+//   cell points k in [0, nf+1] centred at (k-1/2)*hf (0, nf+1: ghosts).
+// Cell points transfer piecewise-constant (a fine cell to the coarse cell
+// containing its centre), node points by linear (hat) interpolation.  All
+// positions are compared in exact integer arithmetic (hf/hc = nc/nf).  For
+// even n these are the 2:1 operators: cells {2K-1, 2K} -> K; node 2J -> J,
+// node 2J+1 -> halves of J and J+1.
+struct Map1D {
+    int nf, nc;
+};
+
+__device__ __forceinline__ int m_cell(const Map1D& m, int k) {
+    if (k <= 0) return 0;
+    if (k >= m.nf + 1) return m.nc + 1;
+    return (int)(((long long)(2 * k - 1) * m.nc) / (2LL * m.nf)) + 1;
+}
+
+// hat weight of coarse node K at fine node j
+__device__ __forceinline__ double m_hat(const Map1D& m, int j, int K) {
+    long long d = (long long)j * m.nc - (long long)K * m.nf;
+    if (d < 0) d = -d;
+    return d >= m.nf ? 0.0 : 1.0 - (double)d / (double)m.nf;
+}
+
+// fine nodes that can have a nonzero hat weight for coarse node K
+__device__ __forceinline__ void m_hat_range(const Map1D& m, int K, int& j0, int& j1) {
+    j0 = max(0, (int)(((long long)(K - 1) * m.nf) / m.nc));
+    j1 = min(m.nf + 1, (int)(((long long)(K + 1) * m.nf + m.nc - 1) / m.nc));
+}
+
+// fine cells that can map to coarse cell K (filter with m_cell(k) == K)
+__device__ __forceinline__ void m_cell_range(const Map1D& m, int K, int& k0, int& k1) {
+    if (K <= 0) {
+        k0 = k1 = 0;
+    } else if (K >= m.nc + 1) {
+        k0 = k1 = m.nf + 1;
+    } else {
+        k0 = max(1, (int)(((long long)(K - 1) * m.nf) / m.nc));
+        k1 = min(m.nf, (int)(((long long)K * m.nf) / m.nc) + 1);
+    }
+}
+
+__device__ __forceinline__ Map1D mapx(const Geo& gf, const Geo& gc) { return Map1D{gf.Nx - 1, gc.Nx - 1}; }
+__device__ __forceinline__ Map1D mapy(const Geo& gf, const Geo& gc) { return Map1D{gf.Ny - 1, gc.Ny - 1}; }
+
+// x_f += P x_c: cell-centred unknowns piecewise constant, face unknowns linear
+// along the face normal and constant across it (ghost rows map to ghost rows,
+// which keeps the homogeneous boundary relations of the coarse correction).
 template <typename T>
 __device__ __forceinline__ void prolong_add(const Geo& gf, const Geo& gc, const T* __restrict__ xc, T* xf, int tid,
                                             int nth) {
+    const Map1D mx = mapx(gf, gc), my = mapy(gf, gc);
     const int ncell = gf.Ny1 * gf.Nx1;
     for (int t = tid; t < ncell; t += nth) {
         const int i = t % gf.Ny1, j = t / gf.Ny1;
@@ -237,24 +287,22 @@ __device__ __forceinline__ void prolong_add(const Geo& gf, const Geo& gc, const 
             if (I < 0 || I > gc.Ny || J < 0 || J > gc.Nx) return (T)0;
             return xc[kp_of(I, J, gc.Ny1) + v];
         };
-        const int Ic = (i + 1) / 2, Jc = (j + 1) / 2;
+        const int Ic = m_cell(my, i), Jc = m_cell(mx, j);
         if (i >= 1 && i <= gf.Ny - 1 && j >= 1 && j <= gf.Nx - 1) {
             xf[kf + 0] += xcv(Ic, Jc, 0);
             xf[kf + 3] += xcv(Ic, Jc, 3);
         }
-        if ((j & 1) == 0) {
-            xf[kf + 1] += xcv(Ic, j / 2, 1);
-            xf[kf + 4] += xcv(Ic, j / 2, 4);
-        } else {
-            xf[kf + 1] += (T)0.5 * (xcv(Ic, j / 2, 1) + xcv(Ic, j / 2 + 1, 1));
-            xf[kf + 4] += (T)0.5 * (xcv(Ic, j / 2, 4) + xcv(Ic, j / 2 + 1, 4));
+        {  // x faces: linear in x between coarse nodes J0, J0+1
+            const int J0 = (int)(((long long)j * mx.nc) / mx.nf);
+            const T w1 = (T)m_hat(mx, j, J0 + 1), w0 = (T)m_hat(mx, j, J0);
+            xf[kf + 1] += w0 * xcv(Ic, J0, 1) + w1 * xcv(Ic, J0 + 1, 1);
+            xf[kf + 4] += w0 * xcv(Ic, J0, 4) + w1 * xcv(Ic, J0 + 1, 4);
         }
-        if ((i & 1) == 0) {
-            xf[kf + 2] += xcv(i / 2, Jc, 2);
-            xf[kf + 5] += xcv(i / 2, Jc, 5);
-        } else {
-            xf[kf + 2] += (T)0.5 * (xcv(i / 2, Jc, 2) + xcv(i / 2 + 1, Jc, 2));
-            xf[kf + 5] += (T)0.5 * (xcv(i / 2, Jc, 5) + xcv(i / 2 + 1, Jc, 5));
+        {  // y faces: linear in y between coarse nodes I0, I0+1
+            const int I0 = (int)(((long long)i * my.nc) / my.nf);
+            const T w1 = (T)m_hat(my, i, I0 + 1), w0 = (T)m_hat(my, i, I0);
+            xf[kf + 2] += w0 * xcv(I0, Jc, 2) + w1 * xcv(I0 + 1, Jc, 2);
+            xf[kf + 5] += w0 * xcv(I0, Jc, 5) + w1 * xcv(I0 + 1, Jc, 5);
         }
     }
 }
@@ -343,106 +391,12 @@ struct TileArgs {
     T* r_out;  // if set, r = b - A x is written after the last sweep
 };
 
-template <typename T>
-__global__ void __launch_bounds__(TILE_BS) k_smooth_tiled(TileArgs<T> t, int nsweeps, int mode) {
-    const SmoothArgs<T>& a = t.a;
-    const Geo& g = a.g;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-    T* P = a.x;
-    T* Q = t.xalt;
-    if (mode == 0) {
-        for (int r = tid; r < g.N; r += nth) P[r] = (T)0;
-    } else {
-        prolong_add(g, a.gc, a.xc, P, tid, nth);
-    }
-    cg::this_grid().sync();
-    const int lane = threadIdx.x & 31, q = lane & 15, slot = threadIdx.x >> 4;
-    for (int s = 0; s < nsweeps; s++) {
-        for (int tile = blockIdx.x; tile < t.ntiles; tile += gridDim.x) {
-            const int ti = tile % t.ntile_i, tj = tile / t.ntile_i;
-            const int i0 = 1 + ti * TILE, j0 = 1 + tj * TILE;
-            const int i1 = min(i0 + TILE, g.Ny), j1 = min(j0 + TILE, g.Nx);  // exclusive
-            for (int k = t.own_start[tile] + threadIdx.x; k < t.own_start[tile + 1]; k += blockDim.x) {
-                const int u = t.own_list[k];
-                Q[u] = P[u];
-            }
-            __syncthreads();
-            for (int c = 0; c < 9; c++) {
-                const int ri = c / 3, rj = c % 3;
-                const int fi = i0 + ((ri - i0 % 3) + 3) % 3, fj = j0 + ((rj - j0 % 3) + 3) % 3;
-                const int ni = fi < i1 ? (i1 - 1 - fi) / 3 + 1 : 0;
-                const int nj = fj < j1 ? (j1 - 1 - fj) / 3 + 1 : 0;
-                const bool valid = slot < ni * nj;
-                int i = i0, j = j0, row = 0;
-                if (valid) {
-                    i = fi + 3 * (slot % ni);
-                    j = fj + 3 * (slot / ni);
-                }
-                T pr[PB];
-                {
-                    const T* Pi = a.pinv + (size_t)((j - 1) * (g.Ny - 1) + (i - 1)) * 100 + (q < PB ? q : 0) * PB;
-#pragma unroll
-                    for (int cc = 0; cc < PB; cc++) pr[cc] = (valid && q < PB) ? Pi[cc] : (T)0;
-                }
-                T r = 0;
-                bool mine = false;
-                if (valid && q < PB) {
-                    row = patch_unknown(i, j, g.Ny1, q);
-                    mine = t.owner[row] == tile;
-                    T acc = a.b[row];
-#pragma unroll
-                    for (int sl = 0; sl < HMEC_W; sl++) {
-                        const size_t o = (size_t)sl * g.N + row;
-                        const int cl = a.col[o];
-                        const T xv = (t.owner[cl] == tile) ? Q[cl] : P[cl];
-                        acc -= a.val[o] * xv;
-                    }
-                    r = acc;
-                }
-                T d = 0;
-#pragma unroll
-                for (int cc = 0; cc < PB; cc++) {
-                    const T rc = __shfl_sync(0xffffffffu, r, (lane & 16) + cc);
-                    d += pr[cc] * rc;
-                }
-                if (mine) Q[row] += d;
-                __syncthreads();
-            }
-            // this tile's boundary rows: one Jacobi pass
-            for (int k = t.tb_start[tile] + threadIdx.x; k < t.tb_start[tile + 1]; k += blockDim.x) {
-                const int row = t.tb_list[k];
-                T acc = a.b[row], diag = 0;
-#pragma unroll
-                for (int sl = 0; sl < HMEC_W; sl++) {
-                    const size_t o = (size_t)sl * g.N + row;
-                    const int cl = a.col[o];
-                    const T v = a.val[o];
-                    acc -= v * ((t.owner[cl] == tile) ? Q[cl] : P[cl]);
-                    if (cl == row) diag += v;
-                }
-                a.tmp[k] = diag != 0 ? acc / diag : (T)0;
-            }
-            __syncthreads();
-            for (int k = t.tb_start[tile] + threadIdx.x; k < t.tb_start[tile + 1]; k += blockDim.x)
-                Q[t.tb_list[k]] += a.tmp[k];
-            __syncthreads();
-        }
-        cg::this_grid().sync();
-        T* sw = P;
-        P = Q;
-        Q = sw;
-    }
-    if (P != a.x)
-        for (int r = tid; r < g.N; r += nth) a.x[r] = P[r];
-}
-
-// Tiled pass with the tile's window of unknowns staged in shared memory.
-// Window = the cells the tile's patch rows and boundary rows can read (the
-// tile's patches extended by two cells up/left and one down/right), at most
-// (TILE+3)^2 cells.  Per sweep: load the window from P, run the 9 colour
-// classes and the boundary rows on shared memory (unknowns the tile does not
-// own stay at their P values: the same additive-across-tiles rule as
-// k_smooth_tiled, bit for bit), write the owned unknowns to Q.  A matrix
+// The tile's window of unknowns is staged in shared memory.  Window = the
+// cells the tile's patch rows and boundary rows can read (the tile's patches
+// extended by two cells up/left and one down/right), at most (TILE+3)^2
+// cells.  Per sweep: load the window from P, run the 9 colour classes and the
+// boundary rows (one Jacobi pass) on shared memory (unknowns the tile does not
+// own stay at their P values), write the owned unknowns to Q.  A matrix
 // column maps to its window slot from its offset to the row: delta = col -
 // row = dj*6*Ny1 + (di*6 + dv) with |di*6 + dv| < 12, so dj follows from two
 // comparisons and the window offset is dj*6*WI + (delta - dj*6*Ny1).
@@ -598,45 +552,19 @@ __device__ __forceinline__ bool row_interior(const Geo& g, int i, int j, int v) 
     }
 }
 
-// Coarse rhs = restricted fine residual (b - A x computed on the fly for the
-// fine rows each coarse row needs), in physical units r/df, scaled by the
-// coarse row scale.  Only interior equations are restricted, and only from
-// fine interior equations (weights renormalised); coarse boundary rows get a
-// zero residual, so the coarse correction obeys the homogeneous boundary
-// conditions, which the prolongation preserves.
+// r = b - A x on one level (the untiled smoother does not produce it).
 template <typename T>
-__global__ void k_restrict_resid(Geo gf, Geo gc, const int32_t* __restrict__ col, const T* __restrict__ val,
-                                 const T* __restrict__ bf, const T* __restrict__ xf, const double* __restrict__ dsf,
-                                 const double* __restrict__ dsc, T* bc) {
-    const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    const int J = blockIdx.y;
-    if (I >= gc.Ny1) return;
-    const int kc = kp_of(I, J, gc.Ny1);
-    for (int v = 0; v < 6; v++) {
-        double s = 0, w = 0;
-        if (row_interior(gc, I, J, v)) {
-            int i0 = 2 * I - 1, i1 = 2 * I, j0 = 2 * J - 1, j1 = 2 * J;
-            if (v == 1 || v == 4) j1 = 2 * J + 1;  // x faces: columns 2J-1..2J+1
-            if (v == 2 || v == 5) i1 = 2 * I + 1;  // y faces: rows 2I-1..2I+1
-            for (int i = i0; i <= i1; i++)
-                for (int j = j0; j <= j1; j++) {
-                    if (i < 0 || i > gf.Ny || j < 0 || j > gf.Nx || !row_interior(gf, i, j, v)) continue;
-                    double ww = 1.0;
-                    if ((v == 1 || v == 4) && j != 2 * J) ww = 0.5;
-                    if ((v == 2 || v == 5) && i != 2 * I) ww = 0.5;
-                    const int k = kp_of(i, j, gf.Ny1) + v;
-                    T acc = bf[k];
+__global__ void k_resid(int N, const int32_t* __restrict__ col, const T* __restrict__ val, const T* __restrict__ b,
+                        const T* __restrict__ x, T* r) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    T acc = b[k];
 #pragma unroll
-                    for (int q = 0; q < HMEC_W; q++) {
-                        const size_t o = (size_t)q * gf.N + k;
-                        acc -= val[o] * xf[col[o]];
-                    }
-                    s += ww * ((double)acc / dsf[k]);
-                    w += ww;
-                }
-        }
-        bc[kc + v] = (T)(w > 0 ? (s / w) * dsc[kc + v] : 0.0);
+    for (int q = 0; q < HMEC_W; q++) {
+        const size_t o = (size_t)q * N + k;
+        acc -= val[o] * x[col[o]];
     }
+    r[k] = acc;
 }
 
 // Coarse assembly coefficients from the fine ones.
@@ -654,14 +582,17 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y;
     if (I >= gc.Ny1) return;
-    // basic nodes: 3x3 full weighting around fine (2I, 2J); G harmonically
+    const Map1D mx = mapx(gf, gc), my = mapy(gf, gc);
+    // basic nodes: hat (full) weighting of the fine nodes; G harmonically
     if (I < gc.Ny && J < gc.Nx) {
         double se = 0, sg = 0, sr = 0, w = 0;
-        for (int di = -1; di <= 1; di++)
-            for (int dj = -1; dj <= 1; dj++) {
-                const int i = 2 * I + di, j = 2 * J + dj;
-                if (i < 0 || i >= gf.Ny || j < 0 || j >= gf.Nx) continue;
-                const double ww = (di == 0 ? 2.0 : 1.0) * (dj == 0 ? 2.0 : 1.0);
+        int i0, i1, j0, j1;
+        m_hat_range(my, I, i0, i1);
+        m_hat_range(mx, J, j0, j1);
+        for (int i = i0; i <= min(i1, gf.Ny - 1); i++)
+            for (int j = j0; j <= min(j1, gf.Nx - 1); j++) {
+                const double ww = m_hat(my, i, I) * m_hat(mx, j, J);
+                if (ww == 0.0) continue;
                 const size_t o = (size_t)j * gf.Ny + i;
                 se += ww * F.ETA[o];
                 sg += ww / F.GGG[o];
@@ -674,23 +605,30 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
         C.RHO[oc] = sr / w;
     }
     const size_t oc = (size_t)J * gc.Ny1 + I;
-    // P nodes: average of the 4 children (interior coarse cells)
+    // P nodes: average of the fine cells whose centres lie in the coarse cell
     if (I >= 1 && I <= gc.Ny - 1 && J >= 1 && J <= gc.Nx - 1) {
-        double se = 0, sg = 0, sb = 0, sp = 0, sgb = 0;
-        for (int di = 0; di < 2; di++)
-            for (int dj = 0; dj < 2; dj++) {
-                const size_t o = (size_t)(2 * J - 1 + dj) * gf.Ny1 + (2 * I - 1 + di);
+        double se = 0, sg = 0, sb = 0, sp = 0, sgb = 0, w = 0;
+        int i0, i1, j0, j1;
+        m_cell_range(my, I, i0, i1);
+        m_cell_range(mx, J, j0, j1);
+        for (int i = i0; i <= i1; i++) {
+            if (m_cell(my, i) != I) continue;
+            for (int j = j0; j <= j1; j++) {
+                if (m_cell(mx, j) != J) continue;
+                const size_t o = (size_t)j * gf.Ny1 + i;
                 se += F.ETAP[o];
                 sg += 1.0 / F.GGGP[o];
                 sb += F.ETAB[o];
                 sp += F.POR[o];
                 sgb += 1.0 / F.GGGB[o];
+                w += 1.0;
             }
-        C.ETAP[oc] = se / 4;
-        C.GGGP[oc] = 4 / sg;
-        C.ETAB[oc] = sb / 4;
-        C.POR[oc] = sp / 4;
-        C.GGGB[oc] = 4 / sgb;
+        }
+        C.ETAP[oc] = se / w;
+        C.GGGP[oc] = w / sg;
+        C.ETAB[oc] = sb / w;
+        C.POR[oc] = sp / w;
+        C.GGGB[oc] = w / sgb;
     } else {
         C.ETAP[oc] = 1;
         C.GGGP[oc] = 1;
@@ -698,15 +636,19 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
         C.POR[oc] = 0.5;
         C.GGGB[oc] = 1;
     }
-    // Vx nodes (I, J): fine rows {2I-1, 2I}, fine columns 2J + {-1,0,1}
+    // Vx nodes (I, J): fine rows in coarse row I, fine columns hat-weighted
+    // around coarse column J (ghost columns excluded)
     {
         double a[4] = {0, 0, 0, 0}, w = 0;
-        const int r0 = I == 0 ? 0 : 2 * I - 1, r1 = I == 0 ? 0 : (I == gc.Ny ? gf.Ny : 2 * I);
-        for (int i = r0; i <= r1; i++)
-            for (int dj = -1; dj <= 1; dj++) {
-                const int j = 2 * J + dj;
-                if (j < 0 || j >= gf.Nx) continue;
-                const double ww = dj == 0 ? 2.0 : 1.0;
+        int r0, r1, q0, q1;
+        m_cell_range(my, I, r0, r1);
+        m_hat_range(mx, J, q0, q1);
+        q1 = min(q1, gf.Nx - 1);
+        for (int i = r0; i <= r1; i++) {
+            if (m_cell(my, i) != I) continue;
+            for (int j = q0; j <= q1; j++) {
+                const double ww = m_hat(mx, j, J);
+                if (ww == 0.0) continue;
                 const size_t o = (size_t)j * gf.Ny1 + i;
                 a[0] += ww * F.RHOX[o];
                 a[1] += ww * F.RHOFX[o];
@@ -714,6 +656,7 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
                 a[3] += ww * F.ETADX[o];
                 w += ww;
             }
+        }
         if (w > 0) {
             C.RHOX[oc] = a[0] / w;
             C.RHOFX[oc] = a[1] / w;
@@ -722,12 +665,13 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
             if (flags & HMEC_MG_DARCY_HARMONIC) {
                 // x-flow: rows in parallel (mean conductance), columns in series (mean resistance)
                 double rs = 0, wr = 0;
-                for (int dj = -1; dj <= 1; dj++) {
-                    const int j = 2 * J + dj;
-                    if (j < 0 || j >= gf.Nx) continue;
+                for (int j = q0; j <= q1; j++) {
+                    const double ww = m_hat(mx, j, J);
+                    if (ww == 0.0) continue;
                     double cs = 0;
                     int nc = 0;
                     for (int i = r0; i <= r1; i++) {
+                        if (m_cell(my, i) != I) continue;
                         const double e = F.ETADX[(size_t)j * gf.Ny1 + i];
                         if (e > 0) {
                             cs += 1.0 / e;
@@ -735,7 +679,6 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
                         }
                     }
                     if (nc == 0) continue;
-                    const double ww = dj == 0 ? 2.0 : 1.0;
                     rs += ww * (nc / cs);
                     wr += ww;
                 }
@@ -748,15 +691,19 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
             C.ETADX[oc] = 1;
         }
     }
-    // Vy nodes (I, J): fine columns {2J-1, 2J}, fine rows 2I + {-1,0,1}
+    // Vy nodes (I, J): fine columns in coarse column J, fine rows hat-weighted
+    // around coarse row I (ghost rows excluded)
     {
         double a[4] = {0, 0, 0, 0}, w = 0;
-        const int c0 = J == 0 ? 0 : 2 * J - 1, c1 = J == 0 ? 0 : (J == gc.Nx ? gf.Nx : 2 * J);
-        for (int j = c0; j <= c1; j++)
-            for (int di = -1; di <= 1; di++) {
-                const int i = 2 * I + di;
-                if (i < 0 || i >= gf.Ny) continue;
-                const double ww = di == 0 ? 2.0 : 1.0;
+        int c0, c1, q0, q1;
+        m_cell_range(mx, J, c0, c1);
+        m_hat_range(my, I, q0, q1);
+        q1 = min(q1, gf.Ny - 1);
+        for (int j = c0; j <= c1; j++) {
+            if (m_cell(mx, j) != J) continue;
+            for (int i = q0; i <= q1; i++) {
+                const double ww = m_hat(my, i, I);
+                if (ww == 0.0) continue;
                 const size_t o = (size_t)j * gf.Ny1 + i;
                 a[0] += ww * F.RHOY[o];
                 a[1] += ww * F.RHOFY[o];
@@ -764,6 +711,7 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
                 a[3] += ww * F.ETADY[o];
                 w += ww;
             }
+        }
         if (w > 0) {
             C.RHOY[oc] = a[0] / w;
             C.RHOFY[oc] = a[1] / w;
@@ -772,12 +720,13 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
             if (flags & HMEC_MG_DARCY_HARMONIC) {
                 // y-flow: columns in parallel, rows in series
                 double rs = 0, wr = 0;
-                for (int di = -1; di <= 1; di++) {
-                    const int i = 2 * I + di;
-                    if (i < 0 || i >= gf.Ny) continue;
+                for (int i = q0; i <= q1; i++) {
+                    const double ww = m_hat(my, i, I);
+                    if (ww == 0.0) continue;
                     double cs = 0;
                     int nc = 0;
                     for (int j = c0; j <= c1; j++) {
+                        if (m_cell(mx, j) != J) continue;
                         const double e = F.ETADY[(size_t)j * gf.Ny1 + i];
                         if (e > 0) {
                             cs += 1.0 / e;
@@ -785,7 +734,6 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
                         }
                     }
                     if (nc == 0) continue;
-                    const double ww = di == 0 ? 2.0 : 1.0;
                     rs += ww * (nc / cs);
                     wr += ww;
                 }
@@ -800,7 +748,12 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
     }
 }
 
-// The same restriction from a residual the pre-smoothing pass already wrote.
+// Coarse rhs = restricted fine residual, in physical units r/df, scaled by the
+// coarse row scale (the transpose of the prolongation, weights normalised).
+// Only interior equations are restricted, and only from fine interior
+// equations; coarse boundary rows get a zero residual, so the coarse
+// correction obeys the homogeneous boundary conditions, which the
+// prolongation preserves.
 template <typename T>
 __global__ void k_restrict_r(Geo gf, Geo gc, const T* __restrict__ rf, const double* __restrict__ dsf,
                              const double* __restrict__ dsc, T* bc) {
@@ -809,19 +762,22 @@ __global__ void k_restrict_r(Geo gf, Geo gc, const T* __restrict__ rf, const dou
     const int v = t % 6, cell = t / 6, I = cell % gc.Ny1, J = cell / gc.Ny1;
     double s = 0, w = 0;
     if (row_interior(gc, I, J, v)) {
-        int i0 = 2 * I - 1, i1 = 2 * I, j0 = 2 * J - 1, j1 = 2 * J;
-        if (v == 1 || v == 4) j1 = 2 * J + 1;
-        if (v == 2 || v == 5) i1 = 2 * I + 1;
-        for (int i = i0; i <= i1; i++)
+        const Map1D mx = mapx(gf, gc), my = mapy(gf, gc);
+        const bool xnode = v == 1 || v == 4, ynode = v == 2 || v == 5;
+        int i0, i1, j0, j1;
+        if (ynode) m_hat_range(my, I, i0, i1); else m_cell_range(my, I, i0, i1);
+        if (xnode) m_hat_range(mx, J, j0, j1); else m_cell_range(mx, J, j0, j1);
+        for (int i = i0; i <= i1; i++) {
+            const double wi = ynode ? m_hat(my, i, I) : (m_cell(my, i) == I ? 1.0 : 0.0);
+            if (wi == 0.0) continue;
             for (int j = j0; j <= j1; j++) {
-                if (i < 0 || i > gf.Ny || j < 0 || j > gf.Nx || !row_interior(gf, i, j, v)) continue;
-                double ww = 1.0;
-                if ((v == 1 || v == 4) && j != 2 * J) ww = 0.5;
-                if ((v == 2 || v == 5) && i != 2 * I) ww = 0.5;
+                const double wj = xnode ? m_hat(mx, j, J) : (m_cell(mx, j) == J ? 1.0 : 0.0);
+                if (wj == 0.0 || !row_interior(gf, i, j, v)) continue;
                 const int k = kp_of(i, j, gf.Ny1) + v;
-                s += ww * ((double)rf[k] / dsf[k]);
-                w += ww;
+                s += wi * wj * ((double)rf[k] / dsf[k]);
+                w += wi * wj;
             }
+        }
     }
     bc[t] = (T)(w > 0 ? (s / w) * dsc[t] : 0.0);
 }
@@ -1107,7 +1063,7 @@ static int alloc_level(hmec_ctx* ctx, Level& L, bool mixed, bool coarse) {
         HMEC_CUDA(ctx, cudaMalloc(&L.dr, sizeof(double) * std::max(N, (size_t)L.nbnd)));
     }
     {
-        // tile ownership of every unknown (see k_smooth_tiled)
+        // tile ownership of every unknown (the tiled smoothing pass)
         L.tsz = TILE;
         L.ntile_i = (g.Ny - 1 + TILE - 1) / TILE;
         const int ntile_j = (g.Nx - 1 + TILE - 1) / TILE;
@@ -1205,17 +1161,17 @@ int solver_alloc(hmec_ctx* ctx) {
     sv.m = std::max(2, p.krylov_restart);
     sv.N = ctx->g.N;
     sv.nblk = 152 * 2;
-    // levels: halve while both cell counts are even and the coarse grid keeps >= 4 cells per side
+    // levels: ceil-halve the cell counts while the coarse grid keeps >= 4 cells per side
     Level L0;
     L0.g = ctx->g;
     sv.lv.push_back(L0);
     int nx = ctx->g.Nx, ny = ctx->g.Ny;
     double xs = p.xsize, ys = p.ysize;
     while ((int)sv.lv.size() < std::max(1, p.mg_levels)) {
-        const int cx = nx - 1, cy = ny - 1;
-        if ((cx % 2) || (cy % 2) || cx / 2 < 4 || cy / 2 < 4) break;
-        nx = cx / 2 + 1;
-        ny = cy / 2 + 1;
+        const int cx = (nx - 1 + 1) / 2, cy = (ny - 1 + 1) / 2;
+        if (cx < 4 || cy < 4) break;
+        nx = cx + 1;
+        ny = cy + 1;
         Level L;
         make_geo(L.g, nx, ny, xs, ys);
         sv.lv.push_back(L);
@@ -1497,14 +1453,14 @@ static int vcycle(hmec_ctx* ctx, size_t l, const T* b_in = nullptr, T* x_in = nu
     if (!(p.mg_flags & HMEC_MG_UNTILED)) {
         // the pre-smoothing pass leaves the residual in the level's r buffer
         if ((rc = smooth<T>(ctx, l, b, x, p.mg_pre, 0, LvPtr<T>::r(L)))) return rc;
-        const long long nc = (long long)C.g.N;
-        HMEC_LAUNCH(ctx, k_restrict_r<T>, nblocks(nc, 128), 128, 0, L.g, C.g, LvPtr<T>::r(L), L.dscale, C.dscale,
-                    LvPtr<T>::b(C));
     } else {
         if ((rc = smooth<T>(ctx, l, b, x, p.mg_pre, 0))) return rc;
-        HMEC_LAUNCH(ctx, k_restrict_resid<T>, sgrid(C.g), 64, 0, L.g, C.g, L.col, LvPtr<T>::val(L), b, x, L.dscale,
-                    C.dscale, LvPtr<T>::b(C));
+        HMEC_LAUNCH(ctx, k_resid<T>, nblocks(L.g.N, 256), 256, 0, L.g.N, L.col, LvPtr<T>::val(L), b, x,
+                    LvPtr<T>::r(L));
     }
+    const long long nc = (long long)C.g.N;
+    HMEC_LAUNCH(ctx, k_restrict_r<T>, nblocks(nc, 128), 128, 0, L.g, C.g, LvPtr<T>::r(L), L.dscale, C.dscale,
+                LvPtr<T>::b(C));
     if ((rc = vcycle<T>(ctx, l + 1))) return rc;
     return smooth<T>(ctx, l, b, x, p.mg_post, 1);
 }
@@ -1554,9 +1510,10 @@ int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
             break;
         }
         if (!std::isfinite(rel) || total >= maxit) break;
-        if (total > 0 && rel > 0.5 * prev) {
-            // a whole restart cycle gained less than a factor 2: the FP64 rounding
-            // floor of the residual; accept it when within 100x the tolerance
+        if (total > 0 && rel > 0.5 * prev && rel <= 1e-10) {
+            // a whole restart cycle gained less than a factor 2 near the FP64
+            // rounding floor of the residual; accept it when within 100x the
+            // tolerance (far above the floor a slow cycle just continues)
             converged = rel <= 100 * rtol;
             break;
         }
