@@ -77,6 +77,7 @@ static int status_from_bits(int bits) {
     if (bits & HMEC_DEV_NAN) return HMEC_ERR_NAN;
     if (bits & HMEC_DEV_RSF_NOCONV) return HMEC_ERR_RSF_NOCONV;
     if (bits & HMEC_DEV_KRYLOV_NOCONV) return HMEC_ERR_KRYLOV_NOCONV;
+    if (bits & HMEC_DEV_TIMEOUT) return HMEC_ERR_TIMEOUT;
     return HMEC_OK;
 }
 
@@ -156,7 +157,7 @@ void hmec_params_default(hmec_params* p) {
     p->krylov_rtol = 1e-15;
     p->krylov_restart = 40;
     p->krylov_maxit = 2000;
-    p->mg_levels = 6;
+    p->mg_levels = 5;
     p->mg_pre = 2;
     p->mg_post = 2;
     p->mg_coarse_sweeps = 8;

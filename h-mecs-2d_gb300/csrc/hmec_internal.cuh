@@ -26,7 +26,17 @@ enum {
     HMEC_DEV_NAN = 2,
     HMEC_DEV_RSF_NOCONV = 4,
     HMEC_DEV_KRYLOV_NOCONV = 8,
+    HMEC_DEV_TIMEOUT = 16,
 };
+
+// One fine index of a 1D grid transfer: the coarse cell holding the fine
+// cell centre, and the coarse nodes node0, node0+1 with their hat weights at
+// the fine node.
+struct XferEnt {
+    int cell, node0;
+    double w0, w1;
+};
+#define HMEC_RW 8  // restriction entries per coarse unknown (2 cells x 4 nodes at most)
 
 // Grid geometry of one level (the fine level is the model grid).
 struct Geo {
@@ -78,6 +88,18 @@ struct Level {
     int32_t *owner, *own_start, *own_list, *tbnd_start, *tbnd_list;
     double* dx2;
     float* fx2;
+    // column of every ELL entry as an offset in a tile's shared-memory window
+    // of unknowns (slot-major like col), rebuilt with each assembly
+    int16_t* off16;
+    // prolongation from the next coarser level: per fine x index (Nx+1) and
+    // y index (Ny+1) the coarse cell and the two coarse nodes' hat weights
+    XferEnt *pmx, *pmy;
+    // restriction from the next finer level into this one: per coarse unknown
+    // HMEC_RW (fine unknown, weight) pairs, slot-major; rwg holds the
+    // geometric weights, rw / rw32 those times the row-scale ratio
+    int32_t* ridx;
+    double *rwg, *rw;
+    float* rw32;
     // coarse-level coefficient fields (owned for l > 0)
     std::vector<double*> owned;
     AsmFields af;

@@ -147,6 +147,7 @@ struct SmoothArgs {
     int nbnd;
     Geo gc;               // coarse level of the prolongation (post-smoothing)
     const T* xc;
+    const XferEnt *pmx, *pmy;  // this level's prolongation tables
 };
 
 template <bool COOP>
@@ -238,72 +239,82 @@ struct Map1D {
     int nf, nc;
 };
 
-__device__ __forceinline__ int m_cell(const Map1D& m, int k) {
+__host__ __device__ __forceinline__ int m_cell(const Map1D& m, int k) {
     if (k <= 0) return 0;
     if (k >= m.nf + 1) return m.nc + 1;
     return (int)(((long long)(2 * k - 1) * m.nc) / (2LL * m.nf)) + 1;
 }
 
 // hat weight of coarse node K at fine node j
-__device__ __forceinline__ double m_hat(const Map1D& m, int j, int K) {
+__host__ __device__ __forceinline__ double m_hat(const Map1D& m, int j, int K) {
     long long d = (long long)j * m.nc - (long long)K * m.nf;
     if (d < 0) d = -d;
     return d >= m.nf ? 0.0 : 1.0 - (double)d / (double)m.nf;
 }
 
 // fine nodes that can have a nonzero hat weight for coarse node K
-__device__ __forceinline__ void m_hat_range(const Map1D& m, int K, int& j0, int& j1) {
-    j0 = max(0, (int)(((long long)(K - 1) * m.nf) / m.nc));
-    j1 = min(m.nf + 1, (int)(((long long)(K + 1) * m.nf + m.nc - 1) / m.nc));
+__host__ __device__ __forceinline__ void m_hat_range(const Map1D& m, int K, int& j0, int& j1) {
+    const int a = (int)(((long long)(K - 1) * m.nf) / m.nc);
+    const int b = (int)(((long long)(K + 1) * m.nf + m.nc - 1) / m.nc);
+    j0 = a > 0 ? a : 0;
+    j1 = b < m.nf + 1 ? b : m.nf + 1;
 }
 
 // fine cells that can map to coarse cell K (filter with m_cell(k) == K)
-__device__ __forceinline__ void m_cell_range(const Map1D& m, int K, int& k0, int& k1) {
+__host__ __device__ __forceinline__ void m_cell_range(const Map1D& m, int K, int& k0, int& k1) {
     if (K <= 0) {
         k0 = k1 = 0;
     } else if (K >= m.nc + 1) {
         k0 = k1 = m.nf + 1;
     } else {
-        k0 = max(1, (int)(((long long)(K - 1) * m.nf) / m.nc));
-        k1 = min(m.nf, (int)(((long long)K * m.nf) / m.nc) + 1);
+        const int a = (int)(((long long)(K - 1) * m.nf) / m.nc);
+        const int b = (int)(((long long)K * m.nf) / m.nc) + 1;
+        k0 = a > 1 ? a : 1;
+        k1 = b < m.nf ? b : m.nf;
     }
 }
 
-__device__ __forceinline__ Map1D mapx(const Geo& gf, const Geo& gc) { return Map1D{gf.Nx - 1, gc.Nx - 1}; }
-__device__ __forceinline__ Map1D mapy(const Geo& gf, const Geo& gc) { return Map1D{gf.Ny - 1, gc.Ny - 1}; }
+__host__ __device__ __forceinline__ Map1D mapx(const Geo& gf, const Geo& gc) { return Map1D{gf.Nx - 1, gc.Nx - 1}; }
+__host__ __device__ __forceinline__ Map1D mapy(const Geo& gf, const Geo& gc) { return Map1D{gf.Ny - 1, gc.Ny - 1}; }
 
-// x_f += P x_c: cell-centred unknowns piecewise constant, face unknowns linear
-// along the face normal and constant across it (ghost rows map to ghost rows,
-// which keeps the homogeneous boundary relations of the coarse correction).
+// The transfer table of one direction: entry k for fine index k in [0, nf+1].
+static inline std::vector<XferEnt> xfer_table(const Map1D& m) {
+    std::vector<XferEnt> t(m.nf + 2);
+    for (int k = 0; k <= m.nf + 1; k++) {
+        const int n0 = (int)(((long long)k * m.nc) / m.nf);
+        t[k] = XferEnt{m_cell(m, k), n0, m_hat(m, k, n0), m_hat(m, k, n0 + 1)};
+    }
+    return t;
+}
+
+// The prolongation of unknown v at fine cell (i, j): cell-centred unknowns
+// piecewise constant (interior cells only), face unknowns linear along the
+// face normal and constant across it (ghost rows map to ghost rows, which
+// keeps the homogeneous boundary relations of the coarse correction).
+// mx / my: the transfer tables of the fine level (xfer_table).
 template <typename T>
-__device__ __forceinline__ void prolong_add(const Geo& gf, const Geo& gc, const T* __restrict__ xc, T* xf, int tid,
-                                            int nth) {
-    const Map1D mx = mapx(gf, gc), my = mapy(gf, gc);
-    const int ncell = gf.Ny1 * gf.Nx1;
-    for (int t = tid; t < ncell; t += nth) {
-        const int i = t % gf.Ny1, j = t / gf.Ny1;
-        const int kf = kp_of(i, j, gf.Ny1);
-        auto xcv = [&](int I, int J, int v) -> T {
-            if (I < 0 || I > gc.Ny || J < 0 || J > gc.Nx) return (T)0;
-            return xc[kp_of(I, J, gc.Ny1) + v];
-        };
-        const int Ic = m_cell(my, i), Jc = m_cell(mx, j);
-        if (i >= 1 && i <= gf.Ny - 1 && j >= 1 && j <= gf.Nx - 1) {
-            xf[kf + 0] += xcv(Ic, Jc, 0);
-            xf[kf + 3] += xcv(Ic, Jc, 3);
-        }
-        {  // x faces: linear in x between coarse nodes J0, J0+1
-            const int J0 = (int)(((long long)j * mx.nc) / mx.nf);
-            const T w1 = (T)m_hat(mx, j, J0 + 1), w0 = (T)m_hat(mx, j, J0);
-            xf[kf + 1] += w0 * xcv(Ic, J0, 1) + w1 * xcv(Ic, J0 + 1, 1);
-            xf[kf + 4] += w0 * xcv(Ic, J0, 4) + w1 * xcv(Ic, J0 + 1, 4);
-        }
-        {  // y faces: linear in y between coarse nodes I0, I0+1
-            const int I0 = (int)(((long long)i * my.nc) / my.nf);
-            const T w1 = (T)m_hat(my, i, I0 + 1), w0 = (T)m_hat(my, i, I0);
-            xf[kf + 2] += w0 * xcv(I0, Jc, 2) + w1 * xcv(I0 + 1, Jc, 2);
-            xf[kf + 5] += w0 * xcv(I0, Jc, 5) + w1 * xcv(I0 + 1, Jc, 5);
-        }
+__device__ __forceinline__ T prolong_one(const Geo& gf, const Geo& gc, const XferEnt* __restrict__ mx,
+                                         const XferEnt* __restrict__ my, const T* __restrict__ xc, int i, int j,
+                                         int v) {
+    auto xcv = [&](int I, int J) -> T {
+        if (I < 0 || I > gc.Ny || J < 0 || J > gc.Nx) return (T)0;
+        return xc[kp_of(I, J, gc.Ny1) + v];
+    };
+    const XferEnt ex = mx[j], ey = my[i];
+    if (v == 0 || v == 3)
+        return (i >= 1 && i <= gf.Ny - 1 && j >= 1 && j <= gf.Nx - 1) ? xcv(ey.cell, ex.cell) : (T)0;
+    if (v == 1 || v == 4) return (T)ex.w0 * xcv(ey.cell, ex.node0) + (T)ex.w1 * xcv(ey.cell, ex.node0 + 1);
+    return (T)ey.w0 * xcv(ey.node0, ex.cell) + (T)ey.w1 * xcv(ey.node0 + 1, ex.cell);
+}
+
+// x_f += P x_c over the whole level.
+template <typename T>
+__device__ __forceinline__ void prolong_add(const Geo& gf, const Geo& gc, const XferEnt* __restrict__ mx,
+                                            const XferEnt* __restrict__ my, const T* __restrict__ xc, T* xf,
+                                            int tid, int nth) {
+    for (int t = tid; t < gf.N; t += nth) {
+        const int v = t % 6, cell = t / 6;
+        xf[t] += prolong_one(gf, gc, mx, my, xc, cell % gf.Ny1, cell / gf.Ny1, v);
     }
 }
 
@@ -316,7 +327,7 @@ __global__ void __launch_bounds__(SM_BS) k_smooth(SmoothArgs<T> a, int nsweeps, 
     if (mode == 0) {
         for (int t = tid; t < a.g.N; t += nth) a.x[t] = (T)0;
     } else {
-        prolong_add(a.g, a.gc, a.xc, a.x, tid, nth);
+        prolong_add(a.g, a.gc, a.pmx, a.pmy, a.xc, a.x, tid, nth);
     }
     phase_sync<COOP>();
     for (int s = 0; s < nsweeps; s++) {
@@ -349,7 +360,7 @@ __global__ void __launch_bounds__(SMEM_BS) k_smooth_smem(SmoothArgs<T> a, int ns
     }
     __syncthreads();
     if (mode == 1) {
-        prolong_add(a.g, a.gc, a.xc, xs, tid, nth);
+        prolong_add(a.g, a.gc, a.pmx, a.pmy, a.xc, xs, tid, nth);
         __syncthreads();
     }
     SmoothArgs<T> s = a;
@@ -382,94 +393,381 @@ __global__ void __launch_bounds__(SMEM_BS) k_smooth_smem(SmoothArgs<T> a, int ns
 constexpr int TILE = 12;
 constexpr int TILE_BS = 256;  // 16 lanes x at most 16 patches of one colour in a tile
 
-template <typename T>
-struct TileArgs {
-    SmoothArgs<T> a;
-    T* xalt;
-    const int32_t *owner, *own_start, *own_list, *tb_start, *tb_list;
-    int ntile_i, ntiles;
-    T* r_out;  // if set, r = b - A x is written after the last sweep
-};
-
-// The tile's window of unknowns is staged in shared memory.  Window = the
-// cells the tile's patch rows and boundary rows can read (the tile's patches
-// extended by two cells up/left and one down/right), at most (TILE+3)^2
-// cells.  Per sweep: load the window from P, run the 9 colour classes and the
-// boundary rows (one Jacobi pass) on shared memory (unknowns the tile does not
-// own stay at their P values), write the owned unknowns to Q.  A matrix
-// column maps to its window slot from its offset to the row: delta = col -
-// row = dj*6*Ny1 + (di*6 + dv) with |di*6 + dv| < 12, so dj follows from two
-// comparisons and the window offset is dj*6*WI + (delta - dj*6*Ny1).
+// The window of a tile: the cells its patch rows and boundary rows can read
+// (the tile's patches extended by two cells up/left and one down/right).
 constexpr int WIN_MAX = (TILE + 3) * (TILE + 3) * 6;
 
-template <typename T>
-__global__ void __launch_bounds__(TILE_BS) k_smooth_win(TileArgs<T> t, int nsweeps, int mode) {
-    __shared__ T xs[WIN_MAX];
-    __shared__ unsigned char own[WIN_MAX];
-    const SmoothArgs<T>& a = t.a;
-    const Geo& g = a.g;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-    const int RS = 6 * g.Ny1;
-    T* P = a.x;
-    T* Q = t.xalt;
-    if (mode == 0) {
-        for (int r = tid; r < g.N; r += nth) P[r] = (T)0;
+// ------------------------------------------------ staged tiled smoothing pass
+// Everything a tile's sweep reads is held in shared memory, so the nine colour
+// phases and the boundary phase touch no global memory.  Staged once per tile
+// (once per launch when a block keeps one tile for all sweeps, which every
+// level with at most one tile per co-resident block does):
+//  - the ELL rows of the tile's patches (cells [i0-1, i1) x [j0-1, j1), all
+//    six unknowns: (TILE+1)^2 * 6 rows), their rhs, and their columns as
+//    int16 offsets in the x window, by LDGSTS (cp.async) runs of 8/16 bytes;
+//  - the 10x10 inverses of the tile's patches by TMA bulk copies
+//    (cp.async.bulk, one per patch column) completing on an mbarrier -- for
+//    FP64 they do not fit beside the rows, and one colour's inverses are
+//    streamed per colour instead, double buffered so colour c+1's load while
+//    colour c computes;
+//  - the tile's boundary rows (values, offsets, rhs, diagonal).
+// The x window is reloaded every sweep.  It has a fixed stride (TILE+3 cells
+// per window column, starting two cells before the tile), so a column's
+// window offset depends only on its offset to the row and is precomputed
+// once per assembly (k_stage_prep).  The first sweep needs no grid barrier
+// before it: its window is zero (pre-smoothing) or x plus the prolonged
+// coarse correction computed on the fly (post-smoothing).  After the last
+// sweep the residual of the fine rows each coarse row needs is formed on the
+// fly and restricted (pre-smoothing), again without another barrier: one
+// grid barrier per sweep in all.
+constexpr int WSTR = TILE + 3;                                    // window cells per window column
+constexpr int RSTR = (TILE + 1) * 6;                              // staged rows per staged column
+constexpr int ROWS_MAX = (TILE + 1) * RSTR;                       // staged rows of a tile
+constexpr int PV_MAX = ((TILE + 2) / 3) * ((TILE + 2) / 3);       // patches of one colour in a tile
+constexpr int TB_MAX = 320;                                       // boundary rows of a tile
+static_assert(WIN_MAX == WSTR * WSTR * 6, "window size");
+static_assert(PV_MAX * 16 <= TILE_BS, "a colour's patches fit the block");
+
+// Tile owning the unknown v of staggered cell (i, j): a boundary row (outside
+// every patch) goes to the adjacent patch, a cell unknown to its own patch,
+// an x face to the patch on its right, a y face to the patch below (the
+// patch on the other side at the domain edge).
+__host__ __device__ __forceinline__ int unknown_tile(const Geo& g, int ntile_i, int i, int j, int v) {
+    const bool pin = i >= 1 && i <= g.Ny - 1 && j >= 1 && j <= g.Nx - 1;
+    const bool vxin = i >= 1 && i <= g.Ny - 1 && j <= g.Nx - 1;
+    const bool vyin = i <= g.Ny - 1 && j >= 1 && j <= g.Nx - 1;
+    const bool cellv = v == 0 || v == 3, xv = v == 1 || v == 4;
+    int pi, pj;
+    if (cellv ? !pin : (xv ? !vxin : !vyin)) {
+        pi = i < 1 ? 1 : (i > g.Ny - 1 ? g.Ny - 1 : i);
+        pj = j < 1 ? 1 : (j > g.Nx - 1 ? g.Nx - 1 : j);
+    } else if (cellv) {
+        pi = i;
+        pj = j;
+    } else if (xv) {
+        pi = i;
+        pj = (j + 1 <= g.Nx - 1) ? j + 1 : j;
     } else {
-        prolong_add(g, a.gc, a.xc, P, tid, nth);
+        pi = (i + 1 <= g.Ny - 1) ? i + 1 : i;
+        pj = j;
     }
-    cg::this_grid().sync();
+    return (pi - 1) / TILE + ((pj - 1) / TILE) * ntile_i;
+}
+
+// Window offset of every ELL entry: the x window index of the column minus
+// that of the row.  |col - row - dj*RS| <= 11 for every assembled row (the
+// stencils reach one cell); a row outside that raises HMEC_DEV_BOUNDS.  The
+// mixed form also takes its FP32 matrix copy here.
+__global__ void k_stage_prep(int N, int Ny1, const int32_t* __restrict__ col, const double* __restrict__ val,
+                             int16_t* off, float* val32, int* status) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * HMEC_W) return;
+    const int row = t % N;
+    const int RS = 6 * Ny1;
+    const int delta = col[t] - row;
+    const int dj = delta > RS / 2 ? 1 : (delta < -RS / 2 ? -1 : 0);
+    const int rem = delta - dj * RS;
+    if (rem < -11 || rem > 11) {  // never read outside the window: point at the row itself
+        atomicOr(status, HMEC_DEV_BOUNDS);
+        off[t] = 0;
+    } else {
+        off[t] = (int16_t)(dj * 6 * WSTR + rem);
+    }
+    if (val32) val32[t] = (float)val[t];
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+template <int B>
+__device__ __forceinline__ void cp_async(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(smem_u32(dst)), "l"(src), "n"(B) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for a phase of a TMA barrier: on the cap the status bit is set
+// and the caller carries on (every block must still reach the grid barriers).
+constexpr int MBAR_SPIN_CAP = 1 << 22;
+__device__ __forceinline__ void mbar_wait(unsigned long long* bar, unsigned parity, int* status) {
+    for (int it = 0; it < MBAR_SPIN_CAP; it++)
+        if (mbar_try_wait(bar, parity)) return;
+    atomicOr(status, HMEC_DEV_TIMEOUT);
+}
+
+template <typename T>
+__device__ __forceinline__ void restrict_apply(int Nc, const int32_t* __restrict__ ridx, const T* __restrict__ rw,
+                                               const T* __restrict__ rf, T* bc, int tid, int nth);
+
+template <typename T>
+struct StageArgs {
+    Geo g;
+    const int32_t* col;    // ELL (boundary rows, residual)
+    const T* val;
+    const int16_t* off;    // window offsets of the ELL entries
+    const T* pinv;
+    const T* b;
+    T* x;
+    T* xalt;
+    const int32_t *tb_start, *tb_list;
+    int ntile_i, ntiles;
+    Geo gc;                // prolongation source (mode 1)
+    const T* xc;
+    const XferEnt *pmx, *pmy;
+    int nc;                // if bc is set: the residual restricted into bc
+    const int32_t* ridx;
+    const T* rw;
+    T* bc;
+    int* status;
+};
+
+// FP32: all of a tile's inverses are staged; FP64: two colour buffers.
+template <typename T>
+__host__ __device__ constexpr bool pv_whole_tile() {
+    return sizeof(T) == 4;
+}
+
+template <typename T>
+struct StageSmem {
+    alignas(16) T xs[WIN_MAX];
+    alignas(16) T val[HMEC_W * ROWS_MAX];
+    alignas(16) T b[ROWS_MAX];
+    alignas(16) T pv[(pv_whole_tile<T>() ? TILE * TILE : 2 * PV_MAX) * 100];
+    alignas(16) T bval[HMEC_W * TB_MAX];  // boundary rows
+    alignas(16) T bb[TB_MAX];
+    alignas(16) T bdiag[TB_MAX];
+    alignas(16) T bdel[TB_MAX];
+    alignas(16) int16_t off[HMEC_W * ROWS_MAX];
+    alignas(16) int16_t boff[HMEC_W * TB_MAX];
+    alignas(16) int16_t blr[TB_MAX];
+    alignas(16) unsigned char own[WIN_MAX];
+    alignas(8) unsigned long long bar[2];
+};
+
+// bc = R (b - A x): each coarse row forms the residuals of its fine rows.
+template <typename T>
+__device__ __forceinline__ void restrict_resid(int Nc, const int32_t* __restrict__ ridx, const T* __restrict__ rw,
+                                               int N, const int32_t* __restrict__ col, const T* __restrict__ val,
+                                               const T* __restrict__ b, const T* __restrict__ x, T* bc, int tid,
+                                               int nth) {
+    for (int t = tid; t < Nc; t += nth) {
+        T s = 0;
+#pragma unroll
+        for (int e = 0; e < HMEC_RW; e++) {
+            const size_t o = (size_t)e * Nc + t;
+            const T w = rw[o];
+            if (w == (T)0) continue;
+            const int k = ridx[o];
+            T r = b[k];
+#pragma unroll
+            for (int sl = 0; sl < HMEC_W; sl++) {
+                const size_t q = (size_t)sl * N + k;
+                r -= val[q] * x[col[q]];
+            }
+            s += w * r;
+        }
+        bc[t] = s;
+    }
+}
+
+// Patches of colour c = (ri, rj) in the tile [i0, i1) x [j0, j1): the first
+// row/column of the class and the counts.
+__device__ __forceinline__ void colour_grid(int c, int i0, int j0, int i1, int j1, int& fi, int& fj, int& ni,
+                                            int& nj) {
+    const int ri = c / 3, rj = c % 3;
+    fi = i0 + ((ri - i0 % 3) + 3) % 3;
+    fj = j0 + ((rj - j0 % 3) + 3) % 3;
+    ni = fi < i1 ? (i1 - 1 - fi) / 3 + 1 : 0;
+    nj = fj < j1 ? (j1 - 1 - fj) / 3 + 1 : 0;
+}
+
+// One thread: the inverses of colour c's patches into buffer bb (FP64).
+template <typename T>
+__device__ __forceinline__ void issue_pinv(const StageArgs<T>& t, StageSmem<T>& S, int c, int bb, int i0, int j0,
+                                           int i1, int j1) {
+    int fi, fj, ni, nj;
+    colour_grid(c, i0, j0, i1, j1, fi, fj, ni, nj);
+    const int npc = ni * nj;
+    constexpr unsigned PBYTES = 100 * sizeof(T);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    mbar_expect_tx(&S.bar[bb], npc * PBYTES);
+    T* buf = S.pv + bb * PV_MAX * 100;
+    for (int p = 0; p < npc; p++) {
+        const int i = fi + 3 * (p % ni), j = fj + 3 * (p / ni);
+        bulk_g2s(buf + p * 100, t.pinv + ((size_t)(j - 1) * (t.g.Ny - 1) + (i - 1)) * 100, PBYTES, &S.bar[bb]);
+    }
+}
+
+// One thread: the inverses of all the tile's patches onto bar[0] (FP32); one
+// copy per patch column, where the patches are contiguous.
+template <typename T>
+__device__ __forceinline__ void issue_pinv_tile(const StageArgs<T>& t, StageSmem<T>& S, int i0, int j0, int i1,
+                                                int j1) {
+    const unsigned cbytes = (unsigned)(i1 - i0) * 100 * sizeof(T);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    mbar_expect_tx(&S.bar[0], cbytes * (unsigned)(j1 - j0));
+    for (int j = j0; j < j1; j++)
+        bulk_g2s(S.pv + (size_t)(j - j0) * TILE * 100, t.pinv + ((size_t)(j - 1) * (t.g.Ny - 1) + (i0 - 1)) * 100,
+                 cbytes, &S.bar[0]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(TILE_BS) k_smooth_stage(StageArgs<T> t, int nsweeps, int mode) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    StageSmem<T>& S = *reinterpret_cast<StageSmem<T>*>(smem_raw);
+    const Geo& g = t.g;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    constexpr bool PVT = pv_whole_tile<T>();
+    if (threadIdx.x == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
     const int lane = threadIdx.x & 31, q = lane & 15, slot = threadIdx.x >> 4;
+    const int warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    // this lane's patch row: unknown type and the cell shift from the patch cell
+    const int qv = q < 2 ? 3 * q : (q < 6 ? 1 + (q - 2) / 2 : (q < PB ? 4 + (q - 6) / 2 : 0));
+    const int qdi = (q == 4 || q == 8) ? 1 : 0, qdj = (q == 2 || q == 6) ? 1 : 0;
+    unsigned use0 = 0, use1 = 0;
+    int staged = -1, nbt = 0;
+    const T* src = t.x;  // sweep s > 0 reads the previous sweep's result
+    T* dst = t.xalt;
     for (int s = 0; s < nsweeps; s++) {
         for (int tile = blockIdx.x; tile < t.ntiles; tile += gridDim.x) {
             const int ti = tile % t.ntile_i, tj = tile / t.ntile_i;
             const int i0 = 1 + ti * TILE, j0 = 1 + tj * TILE;
             const int i1 = min(i0 + TILE, g.Ny), j1 = min(j0 + TILE, g.Nx);  // exclusive
-            const int wi0 = max(i0 - 2, 0), wj0 = max(j0 - 2, 0);
-            const int WI = min(i1, g.Ny) - wi0 + 1, WJ = min(j1, g.Nx) - wj0 + 1;
-            const int W = WI * WJ * 6, SJ = 6 * WI;
-            // stage the window
-            for (int lw = threadIdx.x; lw < W; lw += blockDim.x) {
-                const int lc = lw / 6, v = lw - 6 * lc;
-                const int cj = wj0 + lc / WI, ci = wi0 + lc % WI;
-                const int gw = (cj * g.Ny1 + ci) * 6 + v;
-                xs[lw] = P[gw];
-                own[lw] = (t.owner[gw] == tile) ? 1 : 0;
-            }
-            __syncthreads();
-            for (int c = 0; c < 9; c++) {
-                const int ri = c / 3, rj = c % 3;
-                const int fi = i0 + ((ri - i0 % 3) + 3) % 3, fj = j0 + ((rj - j0 % 3) + 3) % 3;
-                const int ni = fi < i1 ? (i1 - 1 - fi) / 3 + 1 : 0;
-                const int nj = fj < j1 ? (j1 - 1 - fj) / 3 + 1 : 0;
-                const bool valid = slot < ni * nj;
-                int i = i0, j = j0;
-                if (valid) {
-                    i = fi + 3 * (slot % ni);
-                    j = fj + 3 * (slot / ni);
+            const int wi0 = i0 - 2, wj0 = j0 - 2;
+            const bool fresh = staged != tile;
+            if (fresh) {
+                if (PVT && threadIdx.x == 0) issue_pinv_tile(t, S, i0, j0, i1, j1);
+                // rows of the tile's patches: per staged column and slot one run
+                // of RI*6 values, copied as RI*3 chunks of two values (a warp per run)
+                const int RI = i1 - i0 + 1, RJ = j1 - j0 + 1, nch = RI * 3;
+                constexpr int CH = 2 * sizeof(T);
+                for (int run = warp; run < HMEC_W * RJ; run += nwarp) {
+                    const int sl = run / RJ, c = run - sl * RJ;
+                    const size_t g0 = (size_t)sl * g.N + ((size_t)(j0 - 1 + c) * g.Ny1 + (i0 - 1)) * 6;
+                    const int s0 = sl * ROWS_MAX + c * RSTR;
+                    for (int k = lane; k < nch; k += 32) {
+                        cp_async<CH>(&S.val[s0 + 2 * k], t.val + g0 + 2 * k);
+                        cp_async<4>(&S.off[s0 + 2 * k], t.off + g0 + 2 * k);
+                    }
                 }
-                T pr[PB];
-                {
-                    const T* Pi = a.pinv + (size_t)((j - 1) * (g.Ny - 1) + (i - 1)) * 100 + (q < PB ? q : 0) * PB;
-#pragma unroll
-                    for (int cc = 0; cc < PB; cc++) pr[cc] = (valid && q < PB) ? Pi[cc] : (T)0;
+                for (int c = warp; c < RJ; c += nwarp) {
+                    const size_t g0 = ((size_t)(j0 - 1 + c) * g.Ny1 + (i0 - 1)) * 6;
+                    for (int k = lane; k < nch; k += 32) cp_async<CH>(&S.b[c * RSTR + 2 * k], t.b + g0 + 2 * k);
                 }
-                T r = 0;
-                int lrow = 0;
-                if (valid && q < PB) {
-                    const int row = patch_unknown(i, j, g.Ny1, q);
-                    // cell of unknown q: (i, j), left (i, j-1) or top (i-1, j)
-                    const int ci = (q == 4 || q == 8) ? i - 1 : i;
-                    const int cj = (q == 2 || q == 6) ? j - 1 : j;
-                    lrow = ((cj - wj0) * WI + (ci - wi0)) * 6 + (row - 6 * (row / 6));
-                    T acc = a.b[row];
+                // the tile's boundary rows and the ownership flags of the window
+                const int kb = t.tb_start[tile];
+                nbt = min(t.tb_start[tile + 1] - kb, TB_MAX);
+                for (int k = threadIdx.x; k < nbt; k += blockDim.x) {
+                    const int row = t.tb_list[kb + k];
+                    const int cell = row / 6;
+                    S.blr[k] = (int16_t)((((cell / g.Ny1) - wj0) * WSTR + ((cell % g.Ny1) - wi0)) * 6 + (row - 6 * cell));
+                    S.bb[k] = t.b[row];
+                    T diag = 0;
 #pragma unroll
                     for (int sl = 0; sl < HMEC_W; sl++) {
                         const size_t o = (size_t)sl * g.N + row;
-                        const int delta = a.col[o] - row;
-                        const int dj = delta > RS / 2 ? 1 : (delta < -RS / 2 ? -1 : 0);
-                        acc -= a.val[o] * xs[lrow + dj * SJ + (delta - dj * RS)];
+                        const T v = t.val[o];
+                        S.bval[sl * TB_MAX + k] = v;
+                        S.boff[sl * TB_MAX + k] = t.off[o];
+                        if (t.col[o] == row) diag += v;
                     }
+                    S.bdiag[k] = diag;
+                }
+                for (int lw = threadIdx.x; lw < WIN_MAX; lw += blockDim.x) {
+                    const int lc = lw / 6, v = lw - 6 * lc;
+                    const int ci = wi0 + lc % WSTR, cj = wj0 + lc / WSTR;
+                    S.own[lw] = (ci >= 0 && ci <= g.Ny && cj >= 0 && cj <= g.Nx &&
+                                 unknown_tile(g, t.ntile_i, ci, cj, v) == tile) ? 1 : 0;
+                }
+                staged = tile;
+            }
+            if (!PVT && threadIdx.x == 0) issue_pinv(t, S, 0, 0, i0, j0, i1, j1);
+            // the x window: zero, x + P xc, or the previous sweep's values
+            constexpr int WPT = (WIN_MAX + TILE_BS - 1) / TILE_BS;
+            T xv[WPT];
+#pragma unroll
+            for (int u = 0; u < WPT; u++) {
+                const int lw = threadIdx.x + u * TILE_BS;
+                const int lc = lw / 6, v = lw - 6 * lc;
+                const int ci = wi0 + lc % WSTR, cj = wj0 + lc / WSTR;
+                xv[u] = (T)0;
+                if (lw < WIN_MAX && ci >= 0 && ci <= g.Ny && cj >= 0 && cj <= g.Nx && (s > 0 || mode == 1)) {
+                    xv[u] = src[(cj * g.Ny1 + ci) * 6 + v];
+                    if (s == 0) xv[u] += prolong_one(g, t.gc, t.pmx, t.pmy, t.xc, ci, cj, v);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < WPT; u++) {
+                const int lw = threadIdx.x + u * TILE_BS;
+                if (lw < WIN_MAX) S.xs[lw] = xv[u];
+            }
+            cp_async_wait_all();
+            __syncthreads();
+            if (PVT && fresh) {
+                mbar_wait(&S.bar[0], use0 & 1, t.status);
+                use0++;
+            }
+            for (int c = 0; c < 9; c++) {
+                const int bb = c & 1;
+                if (!PVT) {
+                    if (bb == 0) {
+                        mbar_wait(&S.bar[0], use0 & 1, t.status);
+                        use0++;
+                    } else {
+                        mbar_wait(&S.bar[1], use1 & 1, t.status);
+                        use1++;
+                    }
+                    // the other buffer's readers passed the previous colour's barrier
+                    if (c < 8 && threadIdx.x == 0) issue_pinv(t, S, c + 1, bb ^ 1, i0, j0, i1, j1);
+                }
+                int fi, fj, ni, nj;
+                colour_grid(c, i0, j0, i1, j1, fi, fj, ni, nj);
+                const bool valid = slot < ni * nj && q < PB;
+                T pr[PB];
+                T r = 0;
+                int lrow = 0;
+                if (valid) {
+                    const int i = fi + 3 * (slot % ni), j = fj + 3 * (slot / ni);
+                    const T* pi = PVT ? &S.pv[((i - i0) + (j - j0) * TILE) * 100 + q * PB]
+                                      : &S.pv[(bb * PV_MAX + slot) * 100 + q * PB];
+#pragma unroll
+                    for (int cc = 0; cc < PB; cc++) pr[cc] = pi[cc];
+                    const int ci = i - qdi, cj = j - qdj;
+                    lrow = ((cj - wj0) * WSTR + (ci - wi0)) * 6 + qv;
+                    const int rl = (cj - j0 + 1) * RSTR + (ci - i0 + 1) * 6 + qv;
+                    T acc = S.b[rl];
+#pragma unroll
+                    for (int sl = 0; sl < HMEC_W; sl++)
+                        acc -= S.val[sl * ROWS_MAX + rl] * S.xs[lrow + S.off[sl * ROWS_MAX + rl]];
                     r = acc;
+                } else {
+#pragma unroll
+                    for (int cc = 0; cc < PB; cc++) pr[cc] = (T)0;
                 }
                 T d = 0;
 #pragma unroll
@@ -479,71 +777,44 @@ __global__ void __launch_bounds__(TILE_BS) k_smooth_win(TileArgs<T> t, int nswee
                 }
                 // same-class patches never read each other's unknowns, and the
                 // shuffles above order this patch's reads before its writes
-                if (valid && q < PB && own[lrow]) xs[lrow] += d;
+                if (valid && S.own[lrow]) S.xs[lrow] += d;
                 __syncthreads();
             }
             // this tile's boundary rows: one Jacobi pass on the window
-            const int kb = t.tb_start[tile], ke = t.tb_start[tile + 1];
-            for (int k = kb + threadIdx.x; k < ke; k += blockDim.x) {
-                const int row = t.tb_list[k];
-                const int cell = row / 6;
-                const int lr = (((cell / g.Ny1) - wj0) * WI + ((cell % g.Ny1) - wi0)) * 6 + (row - 6 * cell);
-                T acc = a.b[row], diag = 0;
+            for (int k = threadIdx.x; k < nbt; k += blockDim.x) {
+                const int lr = S.blr[k];
+                T acc = S.bb[k];
 #pragma unroll
-                for (int sl = 0; sl < HMEC_W; sl++) {
-                    const size_t o = (size_t)sl * g.N + row;
-                    const int cl = a.col[o];
-                    const int delta = cl - row;
-                    const int dj = delta > RS / 2 ? 1 : (delta < -RS / 2 ? -1 : 0);
-                    const T v = a.val[o];
-                    acc -= v * xs[lr + dj * SJ + (delta - dj * RS)];
-                    if (cl == row) diag += v;
-                }
-                a.tmp[k] = diag != 0 ? acc / diag : (T)0;
+                for (int sl = 0; sl < HMEC_W; sl++) acc -= S.bval[sl * TB_MAX + k] * S.xs[lr + S.boff[sl * TB_MAX + k]];
+                S.bdel[k] = S.bdiag[k] != (T)0 ? acc / S.bdiag[k] : (T)0;
             }
             __syncthreads();
-            for (int k = kb + threadIdx.x; k < ke; k += blockDim.x) {
-                const int row = t.tb_list[k];
-                const int cell = row / 6;
-                const int lr = (((cell / g.Ny1) - wj0) * WI + ((cell % g.Ny1) - wi0)) * 6 + (row - 6 * cell);
-                xs[lr] += a.tmp[k];
-            }
+            for (int k = threadIdx.x; k < nbt; k += blockDim.x) S.xs[S.blr[k]] += S.bdel[k];
             __syncthreads();
             // publish the owned unknowns
-            for (int lw = threadIdx.x; lw < W; lw += blockDim.x) {
-                if (!own[lw]) continue;
+            for (int lw = threadIdx.x; lw < WIN_MAX; lw += blockDim.x) {
+                if (!S.own[lw]) continue;
                 const int lc = lw / 6, v = lw - 6 * lc;
-                const int cj = wj0 + lc / WI, ci = wi0 + lc % WI;
-                Q[(cj * g.Ny1 + ci) * 6 + v] = xs[lw];
+                const int ci = wi0 + lc % WSTR, cj = wj0 + lc / WSTR;
+                dst[(cj * g.Ny1 + ci) * 6 + v] = S.xs[lw];
             }
             __syncthreads();
         }
         cg::this_grid().sync();
-        T* sw = P;
-        P = Q;
-        Q = sw;
+        src = dst;
+        dst = (dst == t.xalt) ? t.x : t.xalt;
     }
-    if (P != a.x)
-        for (int r = tid; r < g.N; r += nth) a.x[r] = P[r];
-    if (t.r_out) {  // residual for the restriction, fused to save a launch
-        cg::this_grid().sync();
-        for (int row = tid; row < g.N; row += nth) {
-            T acc = a.b[row];
-#pragma unroll
-            for (int sl = 0; sl < HMEC_W; sl++) {
-                const size_t o = (size_t)sl * g.N + row;
-                acc -= a.val[o] * a.x[a.col[o]];
-            }
-            t.r_out[row] = acc;
-        }
-    }
+    // the last sweep's barrier made src complete
+    if (src != t.x)
+        for (int r = tid; r < g.N; r += nth) t.x[r] = src[r];
+    if (t.bc) restrict_resid(t.nc, t.ridx, t.rw, g.N, t.col, t.val, t.b, src, t.bc, tid, nth);
 }
 
 // ------------------------------------------------ multigrid restriction
 // Whether the row of unknown v at staggered cell (i, j) is an interior
 // equation (x/y-Stokes, continuity, Darcy) rather than a boundary or ghost
 // row; the ranges are those of the assembly branches (:698-980).
-__device__ __forceinline__ bool row_interior(const Geo& g, int i, int j, int v) {
+__host__ __device__ __forceinline__ bool row_interior(const Geo& g, int i, int j, int v) {
     switch (v) {
         case 0: return i >= 1 && i <= g.Ny - 1 && j >= 1 && j <= g.Nx - 1;         // Pt
         case 3: return i >= 2 && i <= g.Ny - 2 && j >= 1 && j <= g.Nx - 1;         // Pf
@@ -748,38 +1019,86 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
     }
 }
 
-// Coarse rhs = restricted fine residual, in physical units r/df, scaled by the
-// coarse row scale (the transpose of the prolongation, weights normalised).
-// Only interior equations are restricted, and only from fine interior
-// equations; coarse boundary rows get a zero residual, so the coarse
-// correction obeys the homogeneous boundary conditions, which the
-// prolongation preserves.
-template <typename T>
-__global__ void k_restrict_r(Geo gf, Geo gc, const T* __restrict__ rf, const double* __restrict__ dsf,
-                             const double* __restrict__ dsc, T* bc) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= gc.Ny1 * gc.Nx1 * 6) return;
-    const int v = t % 6, cell = t / 6, I = cell % gc.Ny1, J = cell / gc.Ny1;
-    double s = 0, w = 0;
-    if (row_interior(gc, I, J, v)) {
-        const Map1D mx = mapx(gf, gc), my = mapy(gf, gc);
-        const bool xnode = v == 1 || v == 4, ynode = v == 2 || v == 5;
-        int i0, i1, j0, j1;
-        if (ynode) m_hat_range(my, I, i0, i1); else m_cell_range(my, I, i0, i1);
-        if (xnode) m_hat_range(mx, J, j0, j1); else m_cell_range(mx, J, j0, j1);
-        for (int i = i0; i <= i1; i++) {
-            const double wi = ynode ? m_hat(my, i, I) : (m_cell(my, i) == I ? 1.0 : 0.0);
-            if (wi == 0.0) continue;
-            for (int j = j0; j <= j1; j++) {
-                const double wj = xnode ? m_hat(mx, j, J) : (m_cell(mx, j) == J ? 1.0 : 0.0);
-                if (wj == 0.0 || !row_interior(gf, i, j, v)) continue;
-                const int k = kp_of(i, j, gf.Ny1) + v;
-                s += wi * wj * ((double)rf[k] / dsf[k]);
-                w += wi * wj;
+// Restriction: coarse rhs = the transpose of the prolongation applied to the
+// fine residual in physical units r/df, weights normalised, scaled by the
+// coarse row scale.  Only interior equations are restricted, and only from
+// fine interior equations; coarse boundary rows get a zero residual, so the
+// coarse correction obeys the homogeneous boundary conditions, which the
+// prolongation preserves.  The geometric part is a fixed table of HMEC_RW
+// (fine unknown, weight) pairs per coarse unknown, slot-major (built once per
+// allocation); the row-scale ratio dsc/df is folded in after each assembly.
+static bool restrict_table(const Geo& gf, const Geo& gc, std::vector<int32_t>& idx, std::vector<double>& w) {
+    const size_t Nc = (size_t)gc.N;
+    idx.assign(HMEC_RW * Nc, 0);
+    w.assign(HMEC_RW * Nc, 0.0);
+    const Map1D mx = mapx(gf, gc), my = mapy(gf, gc);
+    for (int J = 0; J <= gc.Nx; J++)
+        for (int I = 0; I <= gc.Ny; I++)
+            for (int v = 0; v < 6; v++) {
+                const size_t t = ((size_t)J * gc.Ny1 + I) * 6 + v;
+                if (!row_interior(gc, I, J, v)) continue;
+                const bool xnode = v == 1 || v == 4, ynode = v == 2 || v == 5;
+                int i0, i1, j0, j1;
+                if (ynode) m_hat_range(my, I, i0, i1); else m_cell_range(my, I, i0, i1);
+                if (xnode) m_hat_range(mx, J, j0, j1); else m_cell_range(mx, J, j0, j1);
+                int n = 0;
+                int32_t ks[HMEC_RW];
+                double ws[HMEC_RW], sum = 0;
+                for (int i = i0; i <= i1; i++) {
+                    const double wi = ynode ? m_hat(my, i, I) : (m_cell(my, i) == I ? 1.0 : 0.0);
+                    if (wi == 0.0) continue;
+                    for (int j = j0; j <= j1; j++) {
+                        const double wj = xnode ? m_hat(mx, j, J) : (m_cell(mx, j) == J ? 1.0 : 0.0);
+                        if (wj == 0.0 || !row_interior(gf, i, j, v)) continue;
+                        if (n == HMEC_RW) return false;
+                        ks[n] = (int32_t)(((size_t)j * gf.Ny1 + i) * 6 + v);
+                        ws[n] = wi * wj;
+                        sum += ws[n];
+                        n++;
+                    }
+                }
+                for (int e = 0; e < HMEC_RW; e++) {
+                    idx[e * Nc + t] = n ? ks[e < n ? e : 0] : 0;
+                    w[e * Nc + t] = e < n ? ws[e] / sum : 0.0;
+                }
             }
-        }
+    return true;
+}
+
+// rw = rwg * dsc / df (after each assembly of the two levels)
+__global__ void k_restrict_scale(int Nc, const int32_t* __restrict__ ridx, const double* __restrict__ rwg,
+                                 const double* __restrict__ dsf, const double* __restrict__ dsc, double* rw,
+                                 float* rw32) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= Nc) return;
+#pragma unroll
+    for (int e = 0; e < HMEC_RW; e++) {
+        const size_t o = (size_t)e * Nc + t;
+        const double g = rwg[o];
+        const double v = g == 0.0 ? 0.0 : g * dsc[t] / dsf[ridx[o]];
+        rw[o] = v;
+        if (rw32) rw32[o] = (float)v;
     }
-    bc[t] = (T)(w > 0 ? (s / w) * dsc[t] : 0.0);
+}
+
+template <typename T>
+__device__ __forceinline__ void restrict_apply(int Nc, const int32_t* __restrict__ ridx, const T* __restrict__ rw,
+                                               const T* __restrict__ rf, T* bc, int tid, int nth) {
+    for (int t = tid; t < Nc; t += nth) {
+        T s = 0;
+#pragma unroll
+        for (int e = 0; e < HMEC_RW; e++) {
+            const size_t o = (size_t)e * Nc + t;
+            s += rw[o] * rf[ridx[o]];
+        }
+        bc[t] = s;
+    }
+}
+
+template <typename T>
+__global__ void k_restrict(int Nc, const int32_t* __restrict__ ridx, const T* __restrict__ rw,
+                           const T* __restrict__ rf, T* bc) {
+    restrict_apply(Nc, ridx, rw, rf, bc, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 template <typename S, typename D>
@@ -1034,6 +1353,12 @@ static int alloc_level(hmec_ctx* ctx, Level& L, bool mixed, bool coarse) {
     const Geo& g = L.g;
     const size_t N = (size_t)g.N;
     L.npatch = (g.Ny - 1) * (g.Nx - 1);
+    L.off16 = nullptr;
+    L.pmx = L.pmy = nullptr;
+    L.ridx = nullptr;
+    L.rwg = L.rw = nullptr;
+    L.rw32 = nullptr;
+    HMEC_CUDA(ctx, cudaMalloc(&L.off16, sizeof(int16_t) * HMEC_W * N));
     HMEC_CUDA(ctx, cudaMalloc(&L.col, sizeof(int32_t) * HMEC_W * N));
     HMEC_CUDA(ctx, cudaMalloc(&L.val, sizeof(double) * HMEC_W * N));
     HMEC_CUDA(ctx, cudaMalloc(&L.dscale, sizeof(double) * N));
@@ -1068,35 +1393,22 @@ static int alloc_level(hmec_ctx* ctx, Level& L, bool mixed, bool coarse) {
         L.ntile_i = (g.Ny - 1 + TILE - 1) / TILE;
         const int ntile_j = (g.Nx - 1 + TILE - 1) / TILE;
         L.ntiles = L.ntile_i * ntile_j;
-        auto tile_of = [&](int pi, int pj) { return (pi - 1) / TILE + ((pj - 1) / TILE) * L.ntile_i; };
         std::vector<int32_t> owner(N);
         std::vector<char> isb(N, 0);
         for (int32_t r : br) isb[r] = 1;
         for (int j = 0; j <= g.Nx; j++)
             for (int i = 0; i <= g.Ny; i++)
-                for (int v = 0; v < 6; v++) {
-                    const int u = (j * g.Ny1 + i) * 6 + v;
-                    int pi, pj;
-                    if (isb[u]) {  // boundary row: the adjacent patch
-                        pi = std::min(std::max(i, 1), g.Ny - 1);
-                        pj = std::min(std::max(j, 1), g.Nx - 1);
-                    } else if (v == 0 || v == 3) {
-                        pi = i;
-                        pj = j;
-                    } else if (v == 1 || v == 4) {  // x face: the patch on its right
-                        pi = i;
-                        pj = (j + 1 <= g.Nx - 1) ? j + 1 : j;
-                    } else {  // y face: the patch below
-                        pi = (i + 1 <= g.Ny - 1) ? i + 1 : i;
-                        pj = j;
-                    }
-                    owner[u] = tile_of(pi, pj);
-                }
+                for (int v = 0; v < 6; v++) owner[(j * g.Ny1 + i) * 6 + v] = unknown_tile(g, L.ntile_i, i, j, v);
         std::vector<int32_t> os(L.ntiles + 1, 0), bs(L.ntiles + 1, 0);
         for (size_t u = 0; u < N; u++) {
             os[owner[u] + 1]++;
             if (isb[u]) bs[owner[u] + 1]++;
         }
+        for (int k = 0; k < L.ntiles; k++)
+            if (bs[k + 1] > TB_MAX) {
+                ctx->err = "a smoothing tile has more boundary rows than its shared-memory stage holds";
+                return HMEC_ERR_ARG;
+            }
         for (int k = 0; k < L.ntiles; k++) {
             os[k + 1] += os[k];
             bs[k + 1] += bs[k];
@@ -1180,6 +1492,29 @@ int solver_alloc(hmec_ctx* ctx) {
         int rc = alloc_level(ctx, sv.lv[l], mixed, l > 0);
         if (rc) return rc;
     }
+    // grid transfer tables between consecutive levels
+    for (size_t l = 0; l + 1 < sv.lv.size(); l++) {
+        Level& F = sv.lv[l];
+        Level& C = sv.lv[l + 1];
+        const std::vector<XferEnt> tx = xfer_table(mapx(F.g, C.g)), ty = xfer_table(mapy(F.g, C.g));
+        HMEC_CUDA(ctx, cudaMalloc(&F.pmx, sizeof(XferEnt) * tx.size()));
+        HMEC_CUDA(ctx, cudaMalloc(&F.pmy, sizeof(XferEnt) * ty.size()));
+        HMEC_CUDA(ctx, cudaMemcpy(F.pmx, tx.data(), sizeof(XferEnt) * tx.size(), cudaMemcpyHostToDevice));
+        HMEC_CUDA(ctx, cudaMemcpy(F.pmy, ty.data(), sizeof(XferEnt) * ty.size(), cudaMemcpyHostToDevice));
+        std::vector<int32_t> ri;
+        std::vector<double> rg;
+        if (!restrict_table(F.g, C.g, ri, rg)) {
+            ctx->err = "restriction stencil wider than HMEC_RW entries";
+            return HMEC_ERR_ARG;
+        }
+        const size_t n = ri.size();
+        HMEC_CUDA(ctx, cudaMalloc(&C.ridx, sizeof(int32_t) * n));
+        HMEC_CUDA(ctx, cudaMalloc(&C.rwg, sizeof(double) * n));
+        HMEC_CUDA(ctx, cudaMalloc(&C.rw, sizeof(double) * n));
+        if (mixed) HMEC_CUDA(ctx, cudaMalloc(&C.rw32, sizeof(float) * n));
+        HMEC_CUDA(ctx, cudaMemcpy(C.ridx, ri.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+        HMEC_CUDA(ctx, cudaMemcpy(C.rwg, rg.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    }
     // fine-level assembly reads the model fields
     AsmFields& a = sv.lv[0].af;
     double* const* f = ctx->f;
@@ -1250,6 +1585,13 @@ void solver_free(hmec_ctx* ctx) {
         cudaFree(L.own_list);
         cudaFree(L.tbnd_start);
         cudaFree(L.tbnd_list);
+        cudaFree(L.off16);
+        cudaFree(L.pmx);
+        cudaFree(L.pmy);
+        cudaFree(L.ridx);
+        cudaFree(L.rwg);
+        cudaFree(L.rw);
+        cudaFree(L.rw32);
         for (double* p : L.owned) cudaFree(p);
     }
     sv.lv.clear();
@@ -1289,10 +1631,12 @@ int solver_setup(hmec_ctx* ctx) {
             launch_assemble(ctx, L.g, L.af, L.col, L.val, L.dscale, nullptr, nullptr, nullptr);
         }
         HMEC_LAUNCH(ctx, k_vanka_setup, nblocks(L.npatch, 64), 64, 0, L.g, L.col, L.val, L.pinv, L.pinv32, status);
-        if (mixed) {
-            const size_t n = (size_t)HMEC_W * L.g.N;
-            HMEC_LAUNCH(ctx, (k_convert<double, float>), nblocks(n, 256), 256, 0, n, L.val, L.val32);
-        }
+        const size_t n = (size_t)HMEC_W * L.g.N;
+        HMEC_LAUNCH(ctx, k_stage_prep, nblocks(n, 256), 256, 0, L.g.N, L.g.Ny1, L.col, L.val, L.off16,
+                    mixed ? L.val32 : nullptr, status);
+        if (l > 0)
+            HMEC_LAUNCH(ctx, k_restrict_scale, nblocks(L.g.N, 256), 256, 0, L.g.N, L.ridx, L.rwg,
+                        sv.lv[l - 1].dscale, L.dscale, L.rw, L.rw32);
     }
     HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;
@@ -1307,6 +1651,7 @@ struct LvPtr<double> {
     static double* r(Level& L) { return L.dr; }
     static const double* val(Level& L) { return L.val; }
     static const double* pinv(Level& L) { return L.pinv; }
+    static const double* rw(Level& L) { return L.rw; }
 };
 template <>
 struct LvPtr<float> {
@@ -1315,6 +1660,7 @@ struct LvPtr<float> {
     static float* r(Level& L) { return L.fr; }
     static const float* val(Level& L) { return L.val32; }
     static const float* pinv(Level& L) { return L.pinv32; }
+    static const float* rw(Level& L) { return L.rw32; }
 };
 
 // Levels with at most this many patches are smoothed by one block (a block
@@ -1338,13 +1684,17 @@ static int max_coop_blocks(hmec_ctx* ctx) {
     return c;
 }
 
+// Co-resident blocks of the staged pass (its shared memory opted in once).
 template <typename T>
-static int max_tiled_blocks(hmec_ctx* ctx) {
+static int max_stage_blocks(hmec_ctx* ctx) {
     static int cached[2] = {0, 0};
     int& c = cached[sizeof(T) == 8 ? 0 : 1];
     if (c == 0) {
         int per_sm = 0, nsm = 0;
-        HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth_win<T>, TILE_BS, 0));
+        HMEC_CUDA(ctx, cudaFuncSetAttribute(k_smooth_stage<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)sizeof(StageSmem<T>)));
+        HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth_stage<T>, TILE_BS,
+                                                                     sizeof(StageSmem<T>)));
         HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
         c = std::max(1, per_sm * nsm);
     }
@@ -1362,9 +1712,11 @@ float* x_alt<float>(Level& L) {
     return L.fx2;
 }
 
-// One smoothing pass on level l (x = 0 or x += P xc first, then nsweeps sweeps).
+// One smoothing pass on level l (x = 0 or x += P xc first, then nsweeps
+// sweeps).  restrict_next (tiled pass): also restrict the residual into the
+// next coarser level's rhs in the same launch.
 template <typename T>
-static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mode, T* r_out = nullptr) {
+static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mode, bool restrict_next = false) {
     Solver& sv = ctx->sv;
     Level& L = sv.lv[l];
     SmoothArgs<T> a;
@@ -1379,6 +1731,8 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
     a.nbnd = L.nbnd;
     a.gc = (mode == 1) ? sv.lv[l + 1].g : L.g;
     a.xc = (mode == 1) ? LvPtr<T>::x(sv.lv[l + 1]) : nullptr;
+    a.pmx = L.pmx;
+    a.pmy = L.pmy;
     // algorithmic bytes: per sweep every patch's 10 ELL rows, inverse, rhs and
     // unknowns, and the boundary rows; plus the zero fill or the prolongation
     const double st = sizeof(T);
@@ -1390,25 +1744,48 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
         return HMEC_OK;
     }
     if (!(ctx->p.mg_flags & HMEC_MG_UNTILED)) {
-        TileArgs<T> t;
-        t.a = a;
+        StageArgs<T> t;
+        t.g = L.g;
+        t.col = L.col;
+        t.val = LvPtr<T>::val(L);
+        t.off = L.off16;
+        t.pinv = LvPtr<T>::pinv(L);
+        t.b = b;
+        t.x = x;
         t.xalt = x_alt<T>(L);
-        t.owner = L.owner;
-        t.own_start = L.own_start;
-        t.own_list = L.own_list;
         t.tb_start = L.tbnd_start;
         t.tb_list = L.tbnd_list;
         t.ntile_i = L.ntile_i;
         t.ntiles = L.ntiles;
-        t.r_out = r_out;
-        // the owner tests add one int per matrix entry read and the second buffer
-        const double tb = nsweeps * ((double)L.npatch * (10.0 * HMEC_W * 4 + 10.0 * HMEC_W * st) +
-                                     (double)L.g.N * (2 * st + 8)) + bytes;
-        const int grid = std::min(L.ntiles, max_tiled_blocks<T>(ctx));
+        t.gc = a.gc;
+        t.xc = a.xc;
+        t.pmx = L.pmx;
+        t.pmy = L.pmy;
+        t.nc = 0;
+        t.ridx = nullptr;
+        t.rw = nullptr;
+        t.bc = nullptr;
+        t.status = &ctx->ds->status;
+        // algorithmic bytes: per sweep the level's matrix (values and int16
+        // window offsets), every inverse, the unknowns read and written and
+        // the rhs; the prolonged correction; the fused residual (one pass
+        // over the matrix, x and b) and restriction
+        const double N = L.g.N;
+        double ab = nsweeps * (N * HMEC_W * (st + 2) + (double)L.npatch * 100.0 * st + 3.0 * N * st) +
+                    (mode ? N * st * 1.5 : 0.0);
+        if (restrict_next) {
+            Level& C = sv.lv[l + 1];
+            t.nc = C.g.N;
+            t.ridx = C.ridx;
+            t.rw = LvPtr<T>::rw(C);
+            t.bc = LvPtr<T>::b(C);
+            ab += N * HMEC_W * (st + 4) + 2.0 * N * st + (double)C.g.N * (HMEC_RW * (st + 4) + st);
+        }
+        const int grid = std::min(L.ntiles, max_stage_blocks<T>(ctx));
         void* args[] = {&t, &nsweeps, &mode};
-        const bool prof = hmec_prof_begin(ctx, "k_smooth", tb);
-        HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_smooth_win<T>, dim3(grid), dim3(TILE_BS), args, 0,
-                                                   ctx->stream));
+        const bool prof = hmec_prof_begin(ctx, "k_smooth", ab);
+        HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_smooth_stage<T>, dim3(grid), dim3(TILE_BS), args,
+                                                   sizeof(StageSmem<T>), ctx->stream));
         ctx->launches++;
         if (prof) hmec_prof_end(ctx);
         return HMEC_OK;
@@ -1451,16 +1828,15 @@ static int vcycle(hmec_ctx* ctx, size_t l, const T* b_in = nullptr, T* x_in = nu
     }
     Level& C = sv.lv[l + 1];
     if (!(p.mg_flags & HMEC_MG_UNTILED)) {
-        // the pre-smoothing pass leaves the residual in the level's r buffer
-        if ((rc = smooth<T>(ctx, l, b, x, p.mg_pre, 0, LvPtr<T>::r(L)))) return rc;
+        // the pre-smoothing pass also forms the residual and restricts it
+        if ((rc = smooth<T>(ctx, l, b, x, p.mg_pre, 0, true))) return rc;
     } else {
         if ((rc = smooth<T>(ctx, l, b, x, p.mg_pre, 0))) return rc;
         HMEC_LAUNCH(ctx, k_resid<T>, nblocks(L.g.N, 256), 256, 0, L.g.N, L.col, LvPtr<T>::val(L), b, x,
                     LvPtr<T>::r(L));
+        HMEC_LAUNCH(ctx, k_restrict<T>, nblocks(C.g.N, 256), 256, 0, C.g.N, C.ridx, LvPtr<T>::rw(C),
+                    (const T*)LvPtr<T>::r(L), LvPtr<T>::b(C));
     }
-    const long long nc = (long long)C.g.N;
-    HMEC_LAUNCH(ctx, k_restrict_r<T>, nblocks(nc, 128), 128, 0, L.g, C.g, LvPtr<T>::r(L), L.dscale, C.dscale,
-                LvPtr<T>::b(C));
     if ((rc = vcycle<T>(ctx, l + 1))) return rc;
     return smooth<T>(ctx, l, b, x, p.mg_post, 1);
 }

@@ -23,7 +23,8 @@ HEADER = os.path.join(_ROOT, "include", "hmec.h")
 
 HMEC_OK = 0
 STATUS = {0: "HMEC_OK", -1: "HMEC_ERR_ARG", -2: "HMEC_ERR_CUDA", -3: "HMEC_ERR_BOUNDS", -4: "HMEC_ERR_NAN",
-          -5: "HMEC_ERR_RSF_NOCONV", -6: "HMEC_ERR_KRYLOV_NOCONV", -7: "HMEC_ERR_NOMEM", -8: "HMEC_ERR_STATE"}
+          -5: "HMEC_ERR_RSF_NOCONV", -6: "HMEC_ERR_KRYLOV_NOCONV", -7: "HMEC_ERR_NOMEM", -8: "HMEC_ERR_STATE",
+          -9: "HMEC_ERR_TIMEOUT"}
 FORM_FP64, FORM_MIXED = 0, 1
 
 

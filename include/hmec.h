@@ -42,7 +42,8 @@ enum hmec_status {
     HMEC_ERR_RSF_NOCONV = -5,    /* the fault-stress bisection hit its iteration cap */
     HMEC_ERR_KRYLOV_NOCONV = -6, /* FGMRES did not reach its tolerance within its cap */
     HMEC_ERR_NOMEM = -7,         /* device allocation failed */
-    HMEC_ERR_STATE = -8          /* call out of order (e.g. iteration before timestep_begin) */
+    HMEC_ERR_STATE = -8,         /* call out of order (e.g. iteration before timestep_begin) */
+    HMEC_ERR_TIMEOUT = -9        /* a device-side wait hit its iteration cap */
 };
 
 /* ------------------------------------------------------------ solver forms */

@@ -138,7 +138,7 @@ void hmo_params_default(hmec_params* p) {
     p->krylov_rtol = 1e-15;
     p->krylov_restart = 40;
     p->krylov_maxit = 2000;
-    p->mg_levels = 6;
+    p->mg_levels = 5;
     p->mg_pre = 2;
     p->mg_post = 2;
     p->mg_coarse_sweeps = 8;
