@@ -86,6 +86,9 @@ struct Level {
     // bnd_start/bnd_list list each tile's owned unknowns and boundary rows
     int tsz, ntile_i, ntiles;
     int32_t *owner, *own_start, *own_list, *tbnd_start, *tbnd_list;
+    int tb_cap = 16;       // most boundary rows of one tile (rounded up to 16)
+    // staged smoothing launch of this level: inverse mode, grid, shared memory
+    int st_whole = -1, st_grid = 0, st_smem = 0;
     double* dx2;
     float* fx2;
     // column of every ELL entry as an offset in a tile's shared-memory window

@@ -538,31 +538,47 @@ struct StageArgs {
     const int32_t* ridx;
     const T* rw;
     T* bc;
+    int pv_whole;          // 1: all of a tile's inverses staged at once; 0: one colour at a time
+    int tb_cap;            // boundary rows one tile's stage holds
     int* status;
 };
 
-// FP32: all of a tile's inverses are staged; FP64: two colour buffers.
-template <typename T>
-__host__ __device__ constexpr bool pv_whole_tile() {
-    return sizeof(T) == 4;
-}
+// Shared-memory layout of the staged pass, in bytes.  Its size depends on the
+// inverse mode and on the level's boundary-row capacity, and decides how many
+// blocks are co-resident: a level with more tiles than blocks restages every
+// tile every sweep, so large levels stream the inverses (about 100 KB for
+// FP32, two blocks per SM) and the others stage them whole.
+struct StageLayout {
+    int xs, val, b, off, own, bar, pv, bval, bb, bdiag, bdel, boff, blr, total;
+};
+
+__host__ __device__ __forceinline__ int align16(int x) { return (x + 15) & ~15; }
 
 template <typename T>
-struct StageSmem {
-    alignas(16) T xs[WIN_MAX];
-    alignas(16) T val[HMEC_W * ROWS_MAX];
-    alignas(16) T b[ROWS_MAX];
-    alignas(16) T pv[(pv_whole_tile<T>() ? TILE * TILE : 2 * PV_MAX) * 100];
-    alignas(16) T bval[HMEC_W * TB_MAX];  // boundary rows
-    alignas(16) T bb[TB_MAX];
-    alignas(16) T bdiag[TB_MAX];
-    alignas(16) T bdel[TB_MAX];
-    alignas(16) int16_t off[HMEC_W * ROWS_MAX];
-    alignas(16) int16_t boff[HMEC_W * TB_MAX];
-    alignas(16) int16_t blr[TB_MAX];
-    alignas(16) unsigned char own[WIN_MAX];
-    alignas(8) unsigned long long bar[2];
-};
+__host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int tb_cap) {
+    StageLayout L;
+    int o = 0;
+    auto take = [&o](int& at, int bytes) {
+        at = o;
+        o = align16(o + bytes);
+    };
+    const int st = (int)sizeof(T);
+    take(L.xs, WIN_MAX * st);
+    take(L.val, HMEC_W * ROWS_MAX * st);
+    take(L.b, ROWS_MAX * st);
+    take(L.off, HMEC_W * ROWS_MAX * 2);
+    take(L.own, WIN_MAX);
+    take(L.bar, 16);
+    take(L.pv, (pv_whole ? TILE * TILE : 2 * PV_MAX) * 100 * st);
+    take(L.bval, HMEC_W * tb_cap * st);
+    take(L.bb, tb_cap * st);
+    take(L.bdiag, tb_cap * st);
+    take(L.bdel, tb_cap * st);
+    take(L.boff, HMEC_W * tb_cap * 2);
+    take(L.blr, tb_cap * 2);
+    L.total = o;
+    return L;
+}
 
 // bc = R (b - A x): each coarse row forms the residuals of its fine rows.
 template <typename T>
@@ -601,46 +617,60 @@ __device__ __forceinline__ void colour_grid(int c, int i0, int j0, int i1, int j
     nj = fj < j1 ? (j1 - 1 - fj) / 3 + 1 : 0;
 }
 
-// One thread: the inverses of colour c's patches into buffer bb (FP64).
+// One thread: the inverses of colour c's patches into buffer bb of pv.
 template <typename T>
-__device__ __forceinline__ void issue_pinv(const StageArgs<T>& t, StageSmem<T>& S, int c, int bb, int i0, int j0,
-                                           int i1, int j1) {
+__device__ __forceinline__ void issue_pinv(const StageArgs<T>& t, T* pv, unsigned long long* bar, int c, int bb,
+                                           int i0, int j0, int i1, int j1) {
     int fi, fj, ni, nj;
     colour_grid(c, i0, j0, i1, j1, fi, fj, ni, nj);
     const int npc = ni * nj;
     constexpr unsigned PBYTES = 100 * sizeof(T);
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    mbar_expect_tx(&S.bar[bb], npc * PBYTES);
-    T* buf = S.pv + bb * PV_MAX * 100;
+    mbar_expect_tx(&bar[bb], npc * PBYTES);
+    T* buf = pv + bb * PV_MAX * 100;
     for (int p = 0; p < npc; p++) {
         const int i = fi + 3 * (p % ni), j = fj + 3 * (p / ni);
-        bulk_g2s(buf + p * 100, t.pinv + ((size_t)(j - 1) * (t.g.Ny - 1) + (i - 1)) * 100, PBYTES, &S.bar[bb]);
+        bulk_g2s(buf + p * 100, t.pinv + ((size_t)(j - 1) * (t.g.Ny - 1) + (i - 1)) * 100, PBYTES, &bar[bb]);
     }
 }
 
-// One thread: the inverses of all the tile's patches onto bar[0] (FP32); one
-// copy per patch column, where the patches are contiguous.
+// One thread: the inverses of all the tile's patches onto bar[0]; one copy
+// per patch column, where the patches are contiguous.
 template <typename T>
-__device__ __forceinline__ void issue_pinv_tile(const StageArgs<T>& t, StageSmem<T>& S, int i0, int j0, int i1,
-                                                int j1) {
+__device__ __forceinline__ void issue_pinv_tile(const StageArgs<T>& t, T* pv, unsigned long long* bar, int i0,
+                                                int j0, int i1, int j1) {
     const unsigned cbytes = (unsigned)(i1 - i0) * 100 * sizeof(T);
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    mbar_expect_tx(&S.bar[0], cbytes * (unsigned)(j1 - j0));
+    mbar_expect_tx(&bar[0], cbytes * (unsigned)(j1 - j0));
     for (int j = j0; j < j1; j++)
-        bulk_g2s(S.pv + (size_t)(j - j0) * TILE * 100, t.pinv + ((size_t)(j - 1) * (t.g.Ny - 1) + (i0 - 1)) * 100,
-                 cbytes, &S.bar[0]);
+        bulk_g2s(pv + (size_t)(j - j0) * TILE * 100, t.pinv + ((size_t)(j - 1) * (t.g.Ny - 1) + (i0 - 1)) * 100,
+                 cbytes, &bar[0]);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(TILE_BS) k_smooth_stage(StageArgs<T> t, int nsweeps, int mode) {
+__global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(StageArgs<T> t, int nsweeps, int mode) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    StageSmem<T>& S = *reinterpret_cast<StageSmem<T>*>(smem_raw);
+    const StageLayout Lo = stage_layout<T>(t.pv_whole, t.tb_cap);
+    T* xs = reinterpret_cast<T*>(smem_raw + Lo.xs);
+    T* sval = reinterpret_cast<T*>(smem_raw + Lo.val);
+    T* sb = reinterpret_cast<T*>(smem_raw + Lo.b);
+    int16_t* soff = reinterpret_cast<int16_t*>(smem_raw + Lo.off);
+    unsigned char* own = smem_raw + Lo.own;
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem_raw + Lo.bar);
+    T* pv = reinterpret_cast<T*>(smem_raw + Lo.pv);
+    T* bval = reinterpret_cast<T*>(smem_raw + Lo.bval);
+    T* bbv = reinterpret_cast<T*>(smem_raw + Lo.bb);
+    T* bdiag = reinterpret_cast<T*>(smem_raw + Lo.bdiag);
+    T* bdel = reinterpret_cast<T*>(smem_raw + Lo.bdel);
+    int16_t* boff = reinterpret_cast<int16_t*>(smem_raw + Lo.boff);
+    int16_t* blr = reinterpret_cast<int16_t*>(smem_raw + Lo.blr);
+    const int TBC = t.tb_cap;
+    const bool whole = t.pv_whole != 0;
     const Geo& g = t.g;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-    constexpr bool PVT = pv_whole_tile<T>();
     if (threadIdx.x == 0) {
-        mbar_init(&S.bar[0], 1);
-        mbar_init(&S.bar[1], 1);
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
@@ -651,6 +681,11 @@ __global__ void __launch_bounds__(TILE_BS) k_smooth_stage(StageArgs<T> t, int ns
     const int qdi = (q == 4 || q == 8) ? 1 : 0, qdj = (q == 2 || q == 6) ? 1 : 0;
     unsigned use0 = 0, use1 = 0;
     int staged = -1, nbt = 0;
+    // per colour, this lane's row: valid << 29 | patch in tile << 21 | staged
+    // row << 11 | window index (set when a tile is staged)
+    int meta[9];
+#pragma unroll
+    for (int c = 0; c < 9; c++) meta[c] = 0;
     const T* src = t.x;  // sweep s > 0 reads the previous sweep's result
     T* dst = t.xalt;
     for (int s = 0; s < nsweeps; s++) {
@@ -661,7 +696,7 @@ __global__ void __launch_bounds__(TILE_BS) k_smooth_stage(StageArgs<T> t, int ns
             const int wi0 = i0 - 2, wj0 = j0 - 2;
             const bool fresh = staged != tile;
             if (fresh) {
-                if (PVT && threadIdx.x == 0) issue_pinv_tile(t, S, i0, j0, i1, j1);
+                if (whole && threadIdx.x == 0) issue_pinv_tile(t, pv, bar, i0, j0, i1, j1);
                 // rows of the tile's patches: per staged column and slot one run
                 // of RI*6 values, copied as RI*3 chunks of two values (a warp per run)
                 const int RI = i1 - i0 + 1, RJ = j1 - j0 + 1, nch = RI * 3;
@@ -671,42 +706,56 @@ __global__ void __launch_bounds__(TILE_BS) k_smooth_stage(StageArgs<T> t, int ns
                     const size_t g0 = (size_t)sl * g.N + ((size_t)(j0 - 1 + c) * g.Ny1 + (i0 - 1)) * 6;
                     const int s0 = sl * ROWS_MAX + c * RSTR;
                     for (int k = lane; k < nch; k += 32) {
-                        cp_async<CH>(&S.val[s0 + 2 * k], t.val + g0 + 2 * k);
-                        cp_async<4>(&S.off[s0 + 2 * k], t.off + g0 + 2 * k);
+                        cp_async<CH>(&sval[s0 + 2 * k], t.val + g0 + 2 * k);
+                        cp_async<4>(&soff[s0 + 2 * k], t.off + g0 + 2 * k);
                     }
                 }
                 for (int c = warp; c < RJ; c += nwarp) {
                     const size_t g0 = ((size_t)(j0 - 1 + c) * g.Ny1 + (i0 - 1)) * 6;
-                    for (int k = lane; k < nch; k += 32) cp_async<CH>(&S.b[c * RSTR + 2 * k], t.b + g0 + 2 * k);
+                    for (int k = lane; k < nch; k += 32) cp_async<CH>(&sb[c * RSTR + 2 * k], t.b + g0 + 2 * k);
                 }
                 // the tile's boundary rows and the ownership flags of the window
                 const int kb = t.tb_start[tile];
-                nbt = min(t.tb_start[tile + 1] - kb, TB_MAX);
+                nbt = min(t.tb_start[tile + 1] - kb, TBC);
                 for (int k = threadIdx.x; k < nbt; k += blockDim.x) {
                     const int row = t.tb_list[kb + k];
                     const int cell = row / 6;
-                    S.blr[k] = (int16_t)((((cell / g.Ny1) - wj0) * WSTR + ((cell % g.Ny1) - wi0)) * 6 + (row - 6 * cell));
-                    S.bb[k] = t.b[row];
+                    blr[k] = (int16_t)((((cell / g.Ny1) - wj0) * WSTR + ((cell % g.Ny1) - wi0)) * 6 + (row - 6 * cell));
+                    bbv[k] = t.b[row];
                     T diag = 0;
 #pragma unroll
                     for (int sl = 0; sl < HMEC_W; sl++) {
                         const size_t o = (size_t)sl * g.N + row;
                         const T v = t.val[o];
-                        S.bval[sl * TB_MAX + k] = v;
-                        S.boff[sl * TB_MAX + k] = t.off[o];
+                        bval[sl * TBC + k] = v;
+                        boff[sl * TBC + k] = t.off[o];
                         if (t.col[o] == row) diag += v;
                     }
-                    S.bdiag[k] = diag;
+                    bdiag[k] = diag;
                 }
                 for (int lw = threadIdx.x; lw < WIN_MAX; lw += blockDim.x) {
                     const int lc = lw / 6, v = lw - 6 * lc;
                     const int ci = wi0 + lc % WSTR, cj = wj0 + lc / WSTR;
-                    S.own[lw] = (ci >= 0 && ci <= g.Ny && cj >= 0 && cj <= g.Nx &&
-                                 unknown_tile(g, t.ntile_i, ci, cj, v) == tile) ? 1 : 0;
+                    own[lw] = (ci >= 0 && ci <= g.Ny && cj >= 0 && cj <= g.Nx &&
+                               unknown_tile(g, t.ntile_i, ci, cj, v) == tile) ? 1 : 0;
+                }
+#pragma unroll
+                for (int c = 0; c < 9; c++) {
+                    int fi, fj, ni, nj;
+                    colour_grid(c, i0, j0, i1, j1, fi, fj, ni, nj);
+                    meta[c] = 0;
+                    if (slot < ni * nj && q < PB) {
+                        const int i = fi + 3 * (slot % ni), j = fj + 3 * (slot / ni);
+                        const int ci = i - qdi, cj = j - qdj;
+                        const int lrow = ((cj - wj0) * WSTR + (ci - wi0)) * 6 + qv;
+                        const int rl = (cj - j0 + 1) * RSTR + (ci - i0 + 1) * 6 + qv;
+                        const int lp = (i - i0) + (j - j0) * TILE;
+                        meta[c] = (1 << 29) | (lp << 21) | (rl << 11) | lrow;
+                    }
                 }
                 staged = tile;
             }
-            if (!PVT && threadIdx.x == 0) issue_pinv(t, S, 0, 0, i0, j0, i1, j1);
+            if (!whole && threadIdx.x == 0) issue_pinv(t, pv, bar, 0, 0, i0, j0, i1, j1);
             // the x window: zero, x + P xc, or the previous sweep's values
             constexpr int WPT = (WIN_MAX + TILE_BS - 1) / TILE_BS;
             T xv[WPT];
@@ -724,46 +773,40 @@ __global__ void __launch_bounds__(TILE_BS) k_smooth_stage(StageArgs<T> t, int ns
 #pragma unroll
             for (int u = 0; u < WPT; u++) {
                 const int lw = threadIdx.x + u * TILE_BS;
-                if (lw < WIN_MAX) S.xs[lw] = xv[u];
+                if (lw < WIN_MAX) xs[lw] = xv[u];
             }
             cp_async_wait_all();
             __syncthreads();
-            if (PVT && fresh) {
-                mbar_wait(&S.bar[0], use0 & 1, t.status);
+            if (whole && fresh) {
+                mbar_wait(&bar[0], use0 & 1, t.status);
                 use0++;
             }
+#pragma unroll
             for (int c = 0; c < 9; c++) {
                 const int bb = c & 1;
-                if (!PVT) {
+                if (!whole) {
                     if (bb == 0) {
-                        mbar_wait(&S.bar[0], use0 & 1, t.status);
+                        mbar_wait(&bar[0], use0 & 1, t.status);
                         use0++;
                     } else {
-                        mbar_wait(&S.bar[1], use1 & 1, t.status);
+                        mbar_wait(&bar[1], use1 & 1, t.status);
                         use1++;
                     }
                     // the other buffer's readers passed the previous colour's barrier
-                    if (c < 8 && threadIdx.x == 0) issue_pinv(t, S, c + 1, bb ^ 1, i0, j0, i1, j1);
+                    if (c < 8 && threadIdx.x == 0) issue_pinv(t, pv, bar, c + 1, bb ^ 1, i0, j0, i1, j1);
                 }
-                int fi, fj, ni, nj;
-                colour_grid(c, i0, j0, i1, j1, fi, fj, ni, nj);
-                const bool valid = slot < ni * nj && q < PB;
+                const int m = meta[c];
+                const bool valid = (m >> 29) & 1;
+                const int lrow = m & 2047, rl = (m >> 11) & 1023;
                 T pr[PB];
                 T r = 0;
-                int lrow = 0;
                 if (valid) {
-                    const int i = fi + 3 * (slot % ni), j = fj + 3 * (slot / ni);
-                    const T* pi = PVT ? &S.pv[((i - i0) + (j - j0) * TILE) * 100 + q * PB]
-                                      : &S.pv[(bb * PV_MAX + slot) * 100 + q * PB];
+                    const T* pi = whole ? pv + ((m >> 21) & 255) * 100 + q * PB : pv + (bb * PV_MAX + slot) * 100 + q * PB;
 #pragma unroll
                     for (int cc = 0; cc < PB; cc++) pr[cc] = pi[cc];
-                    const int ci = i - qdi, cj = j - qdj;
-                    lrow = ((cj - wj0) * WSTR + (ci - wi0)) * 6 + qv;
-                    const int rl = (cj - j0 + 1) * RSTR + (ci - i0 + 1) * 6 + qv;
-                    T acc = S.b[rl];
+                    T acc = sb[rl];
 #pragma unroll
-                    for (int sl = 0; sl < HMEC_W; sl++)
-                        acc -= S.val[sl * ROWS_MAX + rl] * S.xs[lrow + S.off[sl * ROWS_MAX + rl]];
+                    for (int sl = 0; sl < HMEC_W; sl++) acc -= sval[sl * ROWS_MAX + rl] * xs[lrow + soff[sl * ROWS_MAX + rl]];
                     r = acc;
                 } else {
 #pragma unroll
@@ -777,26 +820,26 @@ __global__ void __launch_bounds__(TILE_BS) k_smooth_stage(StageArgs<T> t, int ns
                 }
                 // same-class patches never read each other's unknowns, and the
                 // shuffles above order this patch's reads before its writes
-                if (valid && S.own[lrow]) S.xs[lrow] += d;
+                if (valid && own[lrow]) xs[lrow] += d;
                 __syncthreads();
             }
             // this tile's boundary rows: one Jacobi pass on the window
             for (int k = threadIdx.x; k < nbt; k += blockDim.x) {
-                const int lr = S.blr[k];
-                T acc = S.bb[k];
+                const int lr = blr[k];
+                T acc = bbv[k];
 #pragma unroll
-                for (int sl = 0; sl < HMEC_W; sl++) acc -= S.bval[sl * TB_MAX + k] * S.xs[lr + S.boff[sl * TB_MAX + k]];
-                S.bdel[k] = S.bdiag[k] != (T)0 ? acc / S.bdiag[k] : (T)0;
+                for (int sl = 0; sl < HMEC_W; sl++) acc -= bval[sl * TBC + k] * xs[lr + boff[sl * TBC + k]];
+                bdel[k] = bdiag[k] != (T)0 ? acc / bdiag[k] : (T)0;
             }
             __syncthreads();
-            for (int k = threadIdx.x; k < nbt; k += blockDim.x) S.xs[S.blr[k]] += S.bdel[k];
+            for (int k = threadIdx.x; k < nbt; k += blockDim.x) xs[blr[k]] += bdel[k];
             __syncthreads();
             // publish the owned unknowns
             for (int lw = threadIdx.x; lw < WIN_MAX; lw += blockDim.x) {
-                if (!S.own[lw]) continue;
+                if (!own[lw]) continue;
                 const int lc = lw / 6, v = lw - 6 * lc;
                 const int ci = wi0 + lc % WSTR, cj = wj0 + lc / WSTR;
-                dst[(cj * g.Ny1 + ci) * 6 + v] = S.xs[lw];
+                dst[(cj * g.Ny1 + ci) * 6 + v] = xs[lw];
             }
             __syncthreads();
         }
@@ -1404,11 +1447,13 @@ static int alloc_level(hmec_ctx* ctx, Level& L, bool mixed, bool coarse) {
             os[owner[u] + 1]++;
             if (isb[u]) bs[owner[u] + 1]++;
         }
-        for (int k = 0; k < L.ntiles; k++)
-            if (bs[k + 1] > TB_MAX) {
-                ctx->err = "a smoothing tile has more boundary rows than its shared-memory stage holds";
-                return HMEC_ERR_ARG;
-            }
+        int tbm = 0;
+        for (int k = 0; k < L.ntiles; k++) tbm = std::max(tbm, (int)bs[k + 1]);
+        if (tbm > TB_MAX) {
+            ctx->err = "a smoothing tile has more boundary rows than its shared-memory stage holds";
+            return HMEC_ERR_ARG;
+        }
+        L.tb_cap = std::max(16, (tbm + 15) / 16 * 16);
         for (int k = 0; k < L.ntiles; k++) {
             os[k + 1] += os[k];
             bs[k + 1] += bs[k];
@@ -1684,21 +1729,35 @@ static int max_coop_blocks(hmec_ctx* ctx) {
     return c;
 }
 
-// Co-resident blocks of the staged pass (its shared memory opted in once).
+// Launch configuration of the staged pass on one level: stage whole tiles of
+// inverses when every tile then still gets its own co-resident block, else
+// stream them per colour, whichever gives more blocks (so a block keeps one
+// tile for all its sweeps whenever shared memory allows).
 template <typename T>
-static int max_stage_blocks(hmec_ctx* ctx) {
-    static int cached[2] = {0, 0};
-    int& c = cached[sizeof(T) == 8 ? 0 : 1];
-    if (c == 0) {
-        int per_sm = 0, nsm = 0;
-        HMEC_CUDA(ctx, cudaFuncSetAttribute(k_smooth_stage<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)sizeof(StageSmem<T>)));
-        HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth_stage<T>, TILE_BS,
-                                                                     sizeof(StageSmem<T>)));
-        HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
-        c = std::max(1, per_sm * nsm);
+static int stage_config(hmec_ctx* ctx, Level& L) {
+    if (L.st_whole >= 0) return HMEC_OK;
+    int nsm = 0, optin = 0;
+    HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
+    HMEC_CUDA(ctx, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->dev));
+    HMEC_CUDA(ctx, cudaFuncSetAttribute(k_smooth_stage<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    int blocks[2], smem[2];
+    for (int w = 0; w < 2; w++) {
+        smem[w] = stage_layout<T>(w, L.tb_cap).total;
+        int per_sm = 0;
+        if (smem[w] <= optin)
+            HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth_stage<T>, TILE_BS,
+                                                                         (size_t)smem[w]));
+        blocks[w] = per_sm * nsm;
     }
-    return c;
+    if (blocks[0] < 1 && blocks[1] < 1) {
+        ctx->err = "the staged smoothing pass does not fit in shared memory";
+        return HMEC_ERR_ARG;
+    }
+    const int w = (blocks[1] >= L.ntiles || blocks[1] >= blocks[0]) ? 1 : 0;
+    L.st_whole = w;
+    L.st_grid = std::min(L.ntiles, blocks[w]);
+    L.st_smem = smem[w];
+    return HMEC_OK;
 }
 
 template <typename T>
@@ -1781,11 +1840,14 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
             t.bc = LvPtr<T>::b(C);
             ab += N * HMEC_W * (st + 4) + 2.0 * N * st + (double)C.g.N * (HMEC_RW * (st + 4) + st);
         }
-        const int grid = std::min(L.ntiles, max_stage_blocks<T>(ctx));
+        int rc = stage_config<T>(ctx, L);
+        if (rc) return rc;
+        t.pv_whole = L.st_whole;
+        t.tb_cap = L.tb_cap;
         void* args[] = {&t, &nsweeps, &mode};
         const bool prof = hmec_prof_begin(ctx, "k_smooth", ab);
-        HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_smooth_stage<T>, dim3(grid), dim3(TILE_BS), args,
-                                                   sizeof(StageSmem<T>), ctx->stream));
+        HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_smooth_stage<T>, dim3(L.st_grid), dim3(TILE_BS), args,
+                                                   (size_t)L.st_smem, ctx->stream));
         ctx->launches++;
         if (prof) hmec_prof_end(ctx);
         return HMEC_OK;
