@@ -58,79 +58,98 @@ __device__ __forceinline__ int patch_unknown(int i, int j, int Ny1, int q) {
 }
 
 // ------------------------------------------------------------ Vanka setup
-// Gauss-Jordan with partial pivoting on the 10x10 patch block of D A;
-// inverses stored patch-major, pinv[p*100 + r*10 + c].
-__global__ void k_vanka_setup(Geo g, const int32_t* __restrict__ col, const double* __restrict__ val,
-                              double* pinv, float* pinv32, int* status) {
-    const int pi = blockIdx.x * blockDim.x + threadIdx.x;
+// Gauss-Jordan with partial pivoting on the 10x10 patch block of D A, in the
+// smoother's precision T (FP64 form: FP64; mixed form: FP32, the inverses
+// being used in FP32 anyway -- and FP64 arithmetic runs at a small fraction
+// of the FP32 rate on this GPU); inverses stored patch-major,
+// pinv[p*100 + r*10 + c].  Half a warp per patch, lane r holding row r of
+// [A | I] in registers.  Pivoting is implicit: column c's pivot is the
+// largest |a| among the lanes not yet used as pivots, its normalised row is
+// broadcast by shuffles and eliminated from the other lanes; at the end the
+// pivot lane of column c holds row c of the inverse.
+constexpr int VS_BS = 128;
+template <typename T>
+__global__ void __launch_bounds__(VS_BS) k_vanka_setup(Geo g, const int32_t* __restrict__ col,
+                                                       const double* __restrict__ val, T* pinv, int* status) {
+    const int lane = threadIdx.x & 31, q = lane & 15;
+    const int pi = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
     const int np = (g.Ny - 1) * (g.Nx - 1);
-    if (pi >= np) return;
-    const int i = 1 + pi % (g.Ny - 1), j = 1 + pi / (g.Ny - 1);
+    const bool live = pi < np;
+    const int pc = live ? pi : np - 1;  // spare half-warps repeat a patch (uniform shuffles)
+    const int i = 1 + pc % (g.Ny - 1), j = 1 + pc / (g.Ny - 1);
     int u[PB];
-    for (int q = 0; q < PB; q++) u[q] = patch_unknown(i, j, g.Ny1, q);
-    double a[PB][PB], b[PB][PB];
-    for (int r = 0; r < PB; r++)
-        for (int c = 0; c < PB; c++) {
-            a[r][c] = 0;
-            b[r][c] = (r == c) ? 1.0 : 0.0;
-        }
-    for (int r = 0; r < PB; r++) {
-        for (int s = 0; s < HMEC_W; s++) {
-            const size_t o = (size_t)s * g.N + u[r];
-            const int cc = col[o];
-            const double v = val[o];
-            for (int c = 0; c < PB; c++)
-                if (u[c] == cc) a[r][c] += v;
-        }
-    }
-    bool singular = false;
+#pragma unroll
+    for (int c = 0; c < PB; c++) u[c] = patch_unknown(i, j, g.Ny1, c);
+    T a[PB], b[PB];
+#pragma unroll
     for (int c = 0; c < PB; c++) {
-        int pr = c;
-        double best = fabs(a[c][c]);
-        for (int r = c + 1; r < PB; r++)
-            if (fabs(a[r][c]) > best) {
-                best = fabs(a[r][c]);
-                pr = r;
-            }
-        if (!(best > 0)) {
-            singular = true;
-            break;
-        }
-        if (pr != c)
-            for (int k = 0; k < PB; k++) {
-                double t = a[c][k];
-                a[c][k] = a[pr][k];
-                a[pr][k] = t;
-                t = b[c][k];
-                b[c][k] = b[pr][k];
-                b[pr][k] = t;
-            }
-        const double inv = 1.0 / a[c][c];
-        for (int k = 0; k < PB; k++) {
-            a[c][k] *= inv;
-            b[c][k] *= inv;
-        }
-        for (int r = 0; r < PB; r++) {
-            if (r == c) continue;
-            const double f = a[r][c];
-            if (f != 0)
-                for (int k = 0; k < PB; k++) {
-                    a[r][k] -= f * a[c][k];
-                    b[r][k] -= f * b[c][k];
-                }
+        a[c] = 0;
+        b[c] = (q == c) ? (T)1 : (T)0;
+    }
+    if (q < PB) {
+        int row = u[0];
+#pragma unroll
+        for (int c = 1; c < PB; c++)
+            if (q == c) row = u[c];
+        for (int s = 0; s < HMEC_W; s++) {
+            const size_t o = (size_t)s * g.N + row;
+            const int cc = col[o];
+            const T v = (T)val[o];
+#pragma unroll
+            for (int c = 0; c < PB; c++)
+                if (u[c] == cc) a[c] += v;
         }
     }
+    bool used = q >= PB;
+    bool singular = false;
+    int my_row = 0;
+    const int base = lane & 16;
+#pragma unroll
+    for (int c = 0; c < PB; c++) {
+        T best = used ? (T)-1 : (T)fabs(a[c]);
+        int bl = q;
+#pragma unroll
+        for (int m = 8; m >= 1; m >>= 1) {
+            const T ob = __shfl_xor_sync(0xffffffffu, best, m);
+            const int ol = __shfl_xor_sync(0xffffffffu, bl, m);
+            if (ob > best || (ob == best && ol < bl)) {
+                best = ob;
+                bl = ol;
+            }
+        }
+        if (!(best > 0)) singular = true;
+        if (q == bl) {
+            const T inv = (T)1 / a[c];
+#pragma unroll
+            for (int k = c; k < PB; k++) a[k] *= inv;
+#pragma unroll
+            for (int k = 0; k < PB; k++) b[k] *= inv;
+            used = true;
+            my_row = c;
+        }
+        T pa[PB], pb[PB];
+#pragma unroll
+        for (int k = c + 1; k < PB; k++) pa[k] = __shfl_sync(0xffffffffu, a[k], base | bl);
+#pragma unroll
+        for (int k = 0; k < PB; k++) pb[k] = __shfl_sync(0xffffffffu, b[k], base | bl);
+        if (q != bl) {
+            const T f = a[c];
+#pragma unroll
+            for (int k = c + 1; k < PB; k++) a[k] -= f * pa[k];
+            a[c] = 0;
+#pragma unroll
+            for (int k = 0; k < PB; k++) b[k] -= f * pb[k];
+        }
+    }
+    if (!live || q >= PB) return;
     if (singular) {
-        atomicOr(status, HMEC_DEV_NAN);
-        for (int r = 0; r < PB; r++)
-            for (int c = 0; c < PB; c++) b[r][c] = 0;
+        if (q == 0) atomicOr(status, HMEC_DEV_NAN);
+#pragma unroll
+        for (int k = 0; k < PB; k++) b[k] = 0;
     }
-    for (int r = 0; r < PB; r++)
-        for (int c = 0; c < PB; c++) {
-            const size_t o = (size_t)pi * 100 + r * PB + c;
-            if (pinv) pinv[o] = b[r][c];
-            if (pinv32) pinv32[o] = (float)b[r][c];
-        }
+    const size_t o = (size_t)pi * 100 + my_row * PB;
+#pragma unroll
+    for (int k = 0; k < PB; k++) pinv[o + k] = b[k];
 }
 
 // ---------------------------------------------------- smoothing kernel
@@ -1269,19 +1288,27 @@ struct Gm {
     DevScalars* ds;
 };
 
+// Sum of p[0..n) by one warp in a fixed order (lane-strided partial sums, then
+// a shuffle-down tree); the result is lane 0's, broadcast to the warp.
+__device__ __forceinline__ double warp_sum_fixed(const double* __restrict__ p, int n) {
+    double a = 0;
+    for (int b = threadIdx.x; b < n; b += 32) a += p[b];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    return __shfl_sync(0xffffffffu, a, 0);
+}
+
+// One warp; lane 0 does the scalar updates.
 __global__ void k_cycle_begin(Gm G, const double* __restrict__ partial, int nblk, int first, double rtol, int m) {
-    double rr = 0, bb = 0;
-    for (int b = 0; b < nblk; b++) {
-        rr += partial[b];
-        bb += partial[nblk + b];
-    }
+    const double rr = warp_sum_fixed(partial, nblk);
+    const double bb = warp_sum_fixed(partial + nblk, nblk);
+    for (int k = 1 + threadIdx.x; k <= m; k += 32) G.g[k] = 0;
+    if (threadIdx.x != 0) return;
     if (first) *G.bnorm = sqrt(bb);
     const double bn = *G.bnorm;
     const double beta = sqrt(rr);
     const double rel = bn > 0 ? beta / bn : beta;
     G.ds->krylov_relres = rel;
     G.g[0] = beta;
-    for (int k = 1; k <= m; k++) G.g[k] = 0;
     *G.kcur = 0;
     *G.done = (rel <= rtol || !(beta > 0) || !isfinite(beta)) ? 1 : 0;
     G.dots[0] = beta > 0 ? 1.0 / beta : 0.0;  // scale for V0
@@ -1294,14 +1321,15 @@ __global__ void k_scale_vec(int N, const double* __restrict__ a, const double* s
 }
 
 // After the two CGS passes: column j of H, Givens rotation, residual estimate.
+// One warp; lane 0 applies the rotations.
 __global__ void k_arnoldi_step(Gm G, const double* __restrict__ h1, const double* __restrict__ partial, int nblk,
                                int j, int m, double rtol, double* hscale) {
     if (*G.done) return;
-    double ww = 0;
-    for (int b = 0; b < nblk; b++) ww += partial[b];
-    const double hn = sqrt(ww);
+    const double hn = sqrt(warp_sum_fixed(partial, nblk));
     double* Hc = G.H + (size_t)j * (m + 1);  // column j, rows 0..j+1
-    for (int k = 0; k <= j; k++) Hc[k] = h1[k] + G.dots[k];  // first + second CGS pass
+    for (int k = threadIdx.x; k <= j; k += 32) Hc[k] = h1[k] + G.dots[k];  // first + second CGS pass
+    __syncwarp();
+    if (threadIdx.x != 0) return;
     Hc[j + 1] = hn;
     for (int k = 0; k < j; k++) {  // previous rotations
         const double t = G.cs[k] * Hc[k] + G.sn[k] * Hc[k + 1];
@@ -1675,7 +1703,12 @@ int solver_setup(hmec_ctx* ctx) {
             HMEC_LAUNCH(ctx, k_coarsen_coef, sgrid(L.g), 64, 0, F.g, L.g, ci, co, ctx->p.mg_flags);
             launch_assemble(ctx, L.g, L.af, L.col, L.val, L.dscale, nullptr, nullptr, nullptr);
         }
-        HMEC_LAUNCH(ctx, k_vanka_setup, nblocks(L.npatch, 64), 64, 0, L.g, L.col, L.val, L.pinv, L.pinv32, status);
+        if (mixed)
+            HMEC_LAUNCH(ctx, k_vanka_setup<float>, nblocks((long long)L.npatch * 16, VS_BS), VS_BS, 0, L.g, L.col,
+                        L.val, L.pinv32, status);
+        else
+            HMEC_LAUNCH(ctx, k_vanka_setup<double>, nblocks((long long)L.npatch * 16, VS_BS), VS_BS, 0, L.g, L.col,
+                        L.val, L.pinv, status);
         const size_t n = (size_t)HMEC_W * L.g.N;
         HMEC_LAUNCH(ctx, k_stage_prep, nblocks(n, 256), 256, 0, L.g.N, L.g.Ny1, L.col, L.val, L.off16,
                     mixed ? L.val32 : nullptr, status);
@@ -1937,7 +1970,7 @@ int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
     while (true) {
         // true residual at every restart: the only convergence decision
         HMEC_LAUNCH(ctx, k_true_resid, nblk, RED_BS, 0, N, L0.col, L0.val, b, x, r, sv.partial, nblk);
-        HMEC_LAUNCH(ctx, k_cycle_begin, 1, 1, 0, G, sv.partial, nblk, first ? 1 : 0, rtol, m);
+        HMEC_LAUNCH(ctx, k_cycle_begin, 1, 32, 0, G, sv.partial, nblk, first ? 1 : 0, rtol, m);
         HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->hs, ctx->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream));
         HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         first = false;
@@ -1981,7 +2014,8 @@ int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
             HMEC_LAUNCH(ctx, k_dots, dim3(nblk, j + 1), RED_BS, 0, N, sv.V, sv.w, sv.partial, nblk, sv.done);
             HMEC_LAUNCH(ctx, k_dots_final, j + 1, 32, 0, sv.partial, nblk, j + 1, sv.dots, sv.done);
             HMEC_LAUNCH(ctx, k_orth_update, nblk, RED_BS, 0, N, sv.V, j + 1, sv.dots, sv.w, sv.partial, nblk, sv.done);
-            HMEC_LAUNCH(ctx, k_arnoldi_step, 1, 1, 0, G, sv.dots + m + 2, sv.partial, nblk, j, m, rtol, sv.dots + 2 * m + 3);
+            HMEC_LAUNCH(ctx, k_arnoldi_step, 1, 32, 0, G, sv.dots + m + 2, sv.partial, nblk, j, m, rtol,
+                        sv.dots + 2 * m + 3);
             HMEC_LAUNCH(ctx, k_scale_vec, nblocks(N, 256), 256, 0, N, sv.w, sv.dots + 2 * m + 3, sv.V + (size_t)(j + 1) * N, sv.done);
         }
         HMEC_LAUNCH(ctx, k_lsq, 1, 1, 0, G, m);
