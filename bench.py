@@ -376,7 +376,7 @@ def main():
     nprof, prof_ms, prof_bytes = mx["prof"]
     achieved = (prof_bytes / nprof) / (prof_ms / nprof / 1e3) / 1e9 if nprof and prof_ms > 0 else None
     peak = peaks.get("hbm_gbs")
-    roof = {"kernel": DOMINANT + "<float> (mixed-form Vanka smoothing pass)", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+    roof = {"kernel": "k_smooth_stage<float> (mixed-form Vanka smoothing pass)", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak else "fallback 6800",
             "launches_timed": nprof, "avg_launch_us": (1e3 * prof_ms / nprof) if nprof else None,
