@@ -10,6 +10,7 @@
 // control kernels, so the whole loop runs without host round trips.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (the encoder is reached through the runtime's driver entry point)
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -82,18 +83,32 @@ struct Level {
     double *dx_, *db, *dr, *pb;
     float *fx, *fb, *fr;
     // tiled smoother: tiles of tsz x tsz patches, one block each; every
-    // unknown has one owning tile (owner[N]); own_start/own_list and
-    // bnd_start/bnd_list list each tile's owned unknowns and boundary rows
+    // unknown has one owning tile; tbnd_start/tbnd_list list each tile's
+    // boundary rows
     int tsz, ntile_i, ntiles;
-    int32_t *owner, *own_start, *own_list, *tbnd_start, *tbnd_list;
+    int32_t *tbnd_start, *tbnd_list;
     int tb_cap = 16;       // most boundary rows of one tile (rounded up to 16)
     // staged smoothing launch of this level: inverse mode, grid, shared memory
     int st_whole = -1, st_grid = 0, st_smem = 0;
     double* dx2;
     float* fx2;
-    // column of every ELL entry as an offset in a tile's shared-memory window
-    // of unknowns (slot-major like col), rebuilt with each assembly
-    int16_t* off16;
+    // staged smoothing pass.  The smoother's copy of the matrix in a padded
+    // layout, [slot][column j][CS] with CS = 6*Ny1 rounded up to 8, so that a
+    // tile's rows form one 3-D box for a TMA tensor copy: values in the
+    // smoother's precision (vals) and every column as an int16 offset in the
+    // tile's window of unknowns (offs), rebuilt with each assembly
+    int CS = 0;
+    void* vals = nullptr;
+    int16_t* offs = nullptr;
+    // per tile: ownership flags of its window and the per-lane colour table
+    // (fixed by the geometry), and its boundary rows packed for one bulk copy
+    // (rebuilt with each assembly)
+    uint8_t* own_t = nullptr;
+    int32_t* meta_t = nullptr;
+    unsigned char* bpack = nullptr;
+    int pack_bytes = 0;
+    // TMA descriptors of vals, offs and the patch inverses
+    CUtensorMap tm_val, tm_off, tm_pinv;
     // prolongation from the next coarser level: per fine x index (Nx+1) and
     // y index (Ny+1) the coarse cell and the two coarse nodes' hat weights
     XferEnt *pmx, *pmy;

@@ -440,12 +440,14 @@ constexpr int WIN_MAX = (TILE + 3) * (TILE + 3) * 6;
 // fly and restricted (pre-smoothing), again without another barrier: one
 // grid barrier per sweep in all.
 constexpr int WSTR = TILE + 3;                                    // window cells per window column
-constexpr int RSTR = (TILE + 1) * 6;                              // staged rows per staged column
+constexpr int RSTR = ((TILE + 1) * 6 + 7) / 8 * 8;                // staged rows per staged column (padded)
 constexpr int ROWS_MAX = (TILE + 1) * RSTR;                       // staged rows of a tile
 constexpr int PV_MAX = ((TILE + 2) / 3) * ((TILE + 2) / 3);       // patches of one colour in a tile
 constexpr int TB_MAX = 320;                                       // boundary rows of a tile
+constexpr int OWN_STRIDE = (WIN_MAX + 15) / 16 * 16;              // bytes of a tile's ownership flags
 static_assert(WIN_MAX == WSTR * WSTR * 6, "window size");
 static_assert(PV_MAX * 16 <= TILE_BS, "a colour's patches fit the block");
+static_assert((TILE * 6) % 8 == 0, "a tile's first staged row is 8-element aligned in the padded layout");
 
 // Tile owning the unknown v of staggered cell (i, j): a boundary row (outside
 // every patch) goes to the adjacent patch, a cell unknown to its own patch,
@@ -473,26 +475,88 @@ __host__ __device__ __forceinline__ int unknown_tile(const Geo& g, int ntile_i, 
     return (pi - 1) / TILE + ((pj - 1) / TILE) * ntile_i;
 }
 
-// Window offset of every ELL entry: the x window index of the column minus
-// that of the row.  |col - row - dj*RS| <= 11 for every assembled row (the
-// stencils reach one cell); a row outside that raises HMEC_DEV_BOUNDS.  The
-// mixed form also takes its FP32 matrix copy here.
-__global__ void k_stage_prep(int N, int Ny1, const int32_t* __restrict__ col, const double* __restrict__ val,
-                             int16_t* off, float* val32, int* status) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= N * HMEC_W) return;
-    const int row = t % N;
-    const int RS = 6 * Ny1;
-    const int delta = col[t] - row;
+// Window offset of an ELL entry: the x window index of the column minus that
+// of the row.  |col - row - dj*RS| <= 11 for every assembled row (the stencils
+// reach one cell); a row outside that raises HMEC_DEV_BOUNDS and points at the
+// row itself, so nothing is read outside the window.
+__device__ __forceinline__ int16_t window_offset(int row, int col, int RS, int* status) {
+    const int delta = col - row;
     const int dj = delta > RS / 2 ? 1 : (delta < -RS / 2 ? -1 : 0);
     const int rem = delta - dj * RS;
-    if (rem < -11 || rem > 11) {  // never read outside the window: point at the row itself
+    if (rem < -11 || rem > 11) {
         atomicOr(status, HMEC_DEV_BOUNDS);
-        off[t] = 0;
-    } else {
-        off[t] = (int16_t)(dj * 6 * WSTR + rem);
+        return 0;
     }
+    return (int16_t)(dj * 6 * WSTR + rem);
+}
+
+// The smoother's copy of the matrix in the padded layout (see Level::vals):
+// values in its precision and window offsets; the mixed form also takes its
+// FP32 copy in the assembly's layout here (the residuals read it).
+template <typename T>
+__global__ void k_stage_prep(int N, int Ny1, int Nx1, int CS, const int32_t* __restrict__ col,
+                             const double* __restrict__ val, T* vals, int16_t* offs, float* val32, int* status) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * HMEC_W) return;
+    const int s = t / N, row = t - s * N;
+    const int RS = 6 * Ny1;
+    const int j = row / RS, r = row - j * RS;
+    const size_t o = ((size_t)s * Nx1 + j) * CS + r;
+    offs[o] = window_offset(row, col[t], RS, status);
+    vals[o] = (T)val[t];
     if (val32) val32[t] = (float)val[t];
+}
+
+// Byte size of one tile's boundary-row pack: values [W][cap], diagonal [cap]
+// (T); window offsets [W][cap], window index [cap] (int16); row [cap] (int32).
+template <typename T>
+__host__ __device__ __forceinline__ int pack_bytes(int cap) {
+    return cap * (HMEC_W * (int)sizeof(T) + (int)sizeof(T) + HMEC_W * 2 + 2 + 4);
+}
+
+// One thread per (tile, boundary slot): the tile's boundary rows packed in
+// the pack layout, zero past the tile's count (rebuilt with each assembly).
+template <typename T>
+__global__ void k_stage_bpack(Geo g, int ntile_i, int ntiles, int cap, const int32_t* __restrict__ tb_start,
+                              const int32_t* __restrict__ tb_list, const int32_t* __restrict__ col,
+                              const double* __restrict__ val, unsigned char* pack, int* status) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles * cap) return;
+    const int tile = t / cap, k = t - tile * cap;
+    unsigned char* base = pack + (size_t)tile * pack_bytes<T>(cap);
+    T* bval = reinterpret_cast<T*>(base);
+    T* bdiag = bval + HMEC_W * cap;
+    int16_t* boff = reinterpret_cast<int16_t*>(bdiag + cap);
+    int16_t* blr = boff + HMEC_W * cap;
+    int32_t* brow = reinterpret_cast<int32_t*>(blr + cap);
+    const int kb = tb_start[tile], n = tb_start[tile + 1] - kb;
+    if (k >= n) {
+#pragma unroll
+        for (int s = 0; s < HMEC_W; s++) {
+            bval[s * cap + k] = (T)0;
+            boff[s * cap + k] = 0;
+        }
+        bdiag[k] = (T)0;
+        blr[k] = 0;
+        brow[k] = 0;
+        return;
+    }
+    const int ti = tile % ntile_i, tj = tile / ntile_i;
+    const int wi0 = TILE * ti - 1, wj0 = TILE * tj - 1;  // window origin: two cells before the tile
+    const int row = tb_list[kb + k], cell = row / 6;
+    const int RS = 6 * g.Ny1;
+    blr[k] = (int16_t)((((cell / g.Ny1) - wj0) * WSTR + ((cell % g.Ny1) - wi0)) * 6 + (row - 6 * cell));
+    brow[k] = row;
+    T diag = 0;
+#pragma unroll
+    for (int s = 0; s < HMEC_W; s++) {
+        const size_t o = (size_t)s * g.N + row;
+        const T v = (T)val[o];
+        bval[s * cap + k] = v;
+        boff[s * cap + k] = window_offset(row, col[o], RS, status);
+        if (col[o] == row) diag += v;
+    }
+    bdiag[k] = diag;
 }
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -516,6 +580,17 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
+// TMA tensor copy of a 3-D box at element coordinates (c0, c1, c2); elements
+// outside the tensor arrive as zeros, and the full box counts on the barrier.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                            unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
     unsigned ok;
     asm volatile(
@@ -540,15 +615,20 @@ __device__ __forceinline__ void restrict_apply(int Nc, const int32_t* __restrict
 
 template <typename T>
 struct StageArgs {
+    CUtensorMap tm_val;    // smoother copy of the values: box (RSTR, TILE+1, W)
+    CUtensorMap tm_off;    // window offsets: same box
+    CUtensorMap tm_pinv;   // inverses (100, Ny-1, Nx-1): box (100, TILE, TILE)
     Geo g;
-    const int32_t* col;    // ELL (boundary rows, residual)
+    const int32_t* col;    // ELL in the assembly's layout (residual)
     const T* val;
-    const int16_t* off;    // window offsets of the ELL entries
-    const T* pinv;
+    const T* pinv;         // inverses (per-colour copies)
     const T* b;
     T* x;
     T* xalt;
-    const int32_t *tb_start, *tb_list;
+    const int32_t* tb_start;
+    const uint8_t* own_t;  // per tile: window ownership flags
+    const int32_t* meta_t; // per tile: per-lane colour table
+    const unsigned char* bpack;  // per tile: boundary-row pack
     int ntile_i, ntiles;
     Geo gc;                // prolongation source (mode 1)
     const T* xc;
@@ -557,7 +637,6 @@ struct StageArgs {
     const int32_t* ridx;
     const T* rw;
     T* bc;
-    int pv_whole;          // 1: all of a tile's inverses staged at once; 0: one colour at a time
     int tb_cap;            // boundary rows one tile's stage holds
     int* status;
 };
@@ -568,35 +647,41 @@ struct StageArgs {
 // tile every sweep, so large levels stream the inverses (about 100 KB for
 // FP32, two blocks per SM) and the others stage them whole.
 struct StageLayout {
-    int xs, val, b, off, own, bar, pv, bval, bb, bdiag, bdel, boff, blr, total;
+    int xs, val, off, b, pv, pack, bb, bdel, own, bar, total;
 };
 
-__host__ __device__ __forceinline__ int align16(int x) { return (x + 15) & ~15; }
+__host__ __device__ __forceinline__ int align_up(int x, int a) { return (x + a - 1) / a * a; }
 
+// TMA destinations start on 128 bytes, the rest on 16.
 template <typename T>
 __host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int tb_cap) {
     StageLayout L;
     int o = 0;
-    auto take = [&o](int& at, int bytes) {
+    auto take = [&o](int& at, int bytes, int a) {
+        o = align_up(o, a);
         at = o;
-        o = align16(o + bytes);
+        o += bytes;
     };
     const int st = (int)sizeof(T);
-    take(L.xs, WIN_MAX * st);
-    take(L.val, HMEC_W * ROWS_MAX * st);
-    take(L.b, ROWS_MAX * st);
-    take(L.off, HMEC_W * ROWS_MAX * 2);
-    take(L.own, WIN_MAX);
-    take(L.bar, 16);
-    take(L.pv, (pv_whole ? TILE * TILE : 2 * PV_MAX) * 100 * st);
-    take(L.bval, HMEC_W * tb_cap * st);
-    take(L.bb, tb_cap * st);
-    take(L.bdiag, tb_cap * st);
-    take(L.bdel, tb_cap * st);
-    take(L.boff, HMEC_W * tb_cap * 2);
-    take(L.blr, tb_cap * 2);
-    L.total = o;
+    take(L.val, HMEC_W * ROWS_MAX * st, 128);
+    take(L.off, HMEC_W * ROWS_MAX * 2, 128);
+    take(L.pv, (pv_whole ? TILE * TILE : 2 * PV_MAX) * 100 * st, 128);
+    take(L.pack, pack_bytes<T>(tb_cap), 128);
+    take(L.own, OWN_STRIDE, 128);
+    take(L.xs, WIN_MAX * st, 16);
+    take(L.b, ROWS_MAX * st, 16);
+    take(L.bb, tb_cap * st, 16);
+    take(L.bdel, tb_cap * st, 16);
+    take(L.bar, 3 * 8, 16);
+    L.total = align_up(o, 16);
     return L;
+}
+
+// Bytes one tile's stage receives on its barrier.
+template <typename T>
+__host__ __device__ __forceinline__ unsigned stage_tx_bytes(bool whole, int tb_cap) {
+    return (unsigned)(HMEC_W * (TILE + 1) * RSTR * (sizeof(T) + 2) + (whole ? TILE * TILE * 100 * sizeof(T) : 0) +
+                      pack_bytes<T>(tb_cap) + OWN_STRIDE);
 }
 
 // bc = R (b - A x): each coarse row forms the residuals of its fine rows.
@@ -627,7 +712,7 @@ __device__ __forceinline__ void restrict_resid(int Nc, const int32_t* __restrict
 
 // Patches of colour c = (ri, rj) in the tile [i0, i1) x [j0, j1): the first
 // row/column of the class and the counts.
-__device__ __forceinline__ void colour_grid(int c, int i0, int j0, int i1, int j1, int& fi, int& fj, int& ni,
+__host__ __device__ __forceinline__ void colour_grid(int c, int i0, int j0, int i1, int j1, int& fi, int& fj, int& ni,
                                             int& nj) {
     const int ri = c / 3, rj = c % 3;
     fi = i0 + ((ri - i0 % 3) + 3) % 3;
@@ -653,23 +738,30 @@ __device__ __forceinline__ void issue_pinv(const StageArgs<T>& t, T* pv, unsigne
     }
 }
 
-// One thread: the inverses of all the tile's patches onto bar[0]; one copy
-// per patch column, where the patches are contiguous.
-template <typename T>
-__device__ __forceinline__ void issue_pinv_tile(const StageArgs<T>& t, T* pv, unsigned long long* bar, int i0,
-                                                int j0, int i1, int j1) {
-    const unsigned cbytes = (unsigned)(i1 - i0) * 100 * sizeof(T);
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    mbar_expect_tx(&bar[0], cbytes * (unsigned)(j1 - j0));
-    for (int j = j0; j < j1; j++)
-        bulk_g2s(pv + (size_t)(j - j0) * TILE * 100, t.pinv + ((size_t)(j - 1) * (t.g.Ny - 1) + (i0 - 1)) * 100,
-                 cbytes, &bar[0]);
+// Per-lane colour table entry: valid << 30 | patch in tile << 22 | staged
+// row << 11 | window index, for the patch row this lane forms in colour c of
+// a tile (host-built per tile; the kernel loads it when it stages the tile).
+__host__ __device__ __forceinline__ int lane_meta(int c, int lanetid, int i0, int j0, int i1, int j1) {
+    const int q = (lanetid & 31) & 15, slot = lanetid >> 4;
+    const int qv = q < 2 ? 3 * q : (q < 6 ? 1 + (q - 2) / 2 : (q < PB ? 4 + (q - 6) / 2 : 0));
+    const int qdi = (q == 4 || q == 8) ? 1 : 0, qdj = (q == 2 || q == 6) ? 1 : 0;
+    int fi, fj, ni, nj;
+    colour_grid(c, i0, j0, i1, j1, fi, fj, ni, nj);
+    if (!(slot < ni * nj && q < PB)) return 0;
+    const int i = fi + 3 * (slot % ni), j = fj + 3 * (slot / ni);
+    const int ci = i - qdi, cj = j - qdj;
+    const int lrow = ((cj - (j0 - 2)) * WSTR + (ci - (i0 - 2))) * 6 + qv;
+    const int rl = (cj - j0 + 1) * RSTR + (ci - i0 + 1) * 6 + qv;
+    const int lp = (i - i0) + (j - j0) * TILE;
+    return (1 << 30) | (lp << 22) | (rl << 11) | lrow;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(StageArgs<T> t, int nsweeps, int mode) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const StageLayout Lo = stage_layout<T>(t.pv_whole, t.tb_cap);
+// WHOLE: the inverse mode (one instantiation each keeps the code small).
+template <typename T, bool WHOLE>
+__global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(const __grid_constant__ StageArgs<T> t, int nsweeps,
+                                                             int mode) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const StageLayout Lo = stage_layout<T>(WHOLE ? 1 : 0, t.tb_cap);
     T* xs = reinterpret_cast<T*>(smem_raw + Lo.xs);
     T* sval = reinterpret_cast<T*>(smem_raw + Lo.val);
     T* sb = reinterpret_cast<T*>(smem_raw + Lo.b);
@@ -677,32 +769,30 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(StageArgs<T> t, int
     unsigned char* own = smem_raw + Lo.own;
     unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem_raw + Lo.bar);
     T* pv = reinterpret_cast<T*>(smem_raw + Lo.pv);
-    T* bval = reinterpret_cast<T*>(smem_raw + Lo.bval);
-    T* bbv = reinterpret_cast<T*>(smem_raw + Lo.bb);
-    T* bdiag = reinterpret_cast<T*>(smem_raw + Lo.bdiag);
-    T* bdel = reinterpret_cast<T*>(smem_raw + Lo.bdel);
-    int16_t* boff = reinterpret_cast<int16_t*>(smem_raw + Lo.boff);
-    int16_t* blr = reinterpret_cast<int16_t*>(smem_raw + Lo.blr);
     const int TBC = t.tb_cap;
-    const bool whole = t.pv_whole != 0;
+    unsigned char* pack = smem_raw + Lo.pack;  // the pack layout of k_stage_bpack
+    T* bval = reinterpret_cast<T*>(pack);
+    T* bdiag = bval + HMEC_W * TBC;
+    int16_t* boff = reinterpret_cast<int16_t*>(bdiag + TBC);
+    int16_t* blr = boff + HMEC_W * TBC;
+    T* bbv = reinterpret_cast<T*>(smem_raw + Lo.bb);
+    T* bdel = reinterpret_cast<T*>(smem_raw + Lo.bdel);
+    constexpr bool whole = WHOLE;
     const Geo& g = t.g;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    // bar[0], bar[1]: per-colour inverses (streamed mode); bar[2]: a tile's stage
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
+        mbar_init(&bar[2], 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, q = lane & 15, slot = threadIdx.x >> 4;
     const int warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    // this lane's patch row: unknown type and the cell shift from the patch cell
-    const int qv = q < 2 ? 3 * q : (q < 6 ? 1 + (q - 2) / 2 : (q < PB ? 4 + (q - 6) / 2 : 0));
-    const int qdi = (q == 4 || q == 8) ? 1 : 0, qdj = (q == 2 || q == 6) ? 1 : 0;
-    unsigned use0 = 0, use1 = 0;
+    unsigned use0 = 0, use1 = 0, use2 = 0;
     int staged = -1, nbt = 0;
-    // per colour, this lane's row: valid << 29 | patch in tile << 21 | staged
-    // row << 11 | window index (set when a tile is staged)
-    int meta[9];
+    int meta[9];  // lane_meta of this thread for the staged tile
 #pragma unroll
     for (int c = 0; c < 9; c++) meta[c] = 0;
     const T* src = t.x;  // sweep s > 0 reads the previous sweep's result
@@ -715,63 +805,31 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(StageArgs<T> t, int
             const int wi0 = i0 - 2, wj0 = j0 - 2;
             const bool fresh = staged != tile;
             if (fresh) {
-                if (whole && threadIdx.x == 0) issue_pinv_tile(t, pv, bar, i0, j0, i1, j1);
-                // rows of the tile's patches: per staged column and slot one run
-                // of RI*6 values, copied as RI*3 chunks of two values (a warp per run)
+                // one thread: the tile's rows (values and offsets, one 3-D box
+                // each), its inverses, ownership flags and boundary pack
+                if (threadIdx.x == 0) {
+                    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                    mbar_expect_tx(&bar[2], stage_tx_bytes<T>(whole, TBC));
+                    tma_load_3d(sval, &t.tm_val, (i0 - 1) * 6, j0 - 1, 0, &bar[2]);
+                    tma_load_3d(soff, &t.tm_off, (i0 - 1) * 6, j0 - 1, 0, &bar[2]);
+                    if (whole) tma_load_3d(pv, &t.tm_pinv, 0, i0 - 1, j0 - 1, &bar[2]);
+                    bulk_g2s(own, t.own_t + (size_t)tile * OWN_STRIDE, OWN_STRIDE, &bar[2]);
+                    bulk_g2s(pack, t.bpack + (size_t)tile * pack_bytes<T>(TBC), pack_bytes<T>(TBC), &bar[2]);
+                }
+                // the rows' rhs: per staged column one run of RI*6 values
                 const int RI = i1 - i0 + 1, RJ = j1 - j0 + 1, nch = RI * 3;
                 constexpr int CH = 2 * sizeof(T);
-                for (int run = warp; run < HMEC_W * RJ; run += nwarp) {
-                    const int sl = run / RJ, c = run - sl * RJ;
-                    const size_t g0 = (size_t)sl * g.N + ((size_t)(j0 - 1 + c) * g.Ny1 + (i0 - 1)) * 6;
-                    const int s0 = sl * ROWS_MAX + c * RSTR;
-                    for (int k = lane; k < nch; k += 32) {
-                        cp_async<CH>(&sval[s0 + 2 * k], t.val + g0 + 2 * k);
-                        cp_async<4>(&soff[s0 + 2 * k], t.off + g0 + 2 * k);
-                    }
-                }
                 for (int c = warp; c < RJ; c += nwarp) {
                     const size_t g0 = ((size_t)(j0 - 1 + c) * g.Ny1 + (i0 - 1)) * 6;
                     for (int k = lane; k < nch; k += 32) cp_async<CH>(&sb[c * RSTR + 2 * k], t.b + g0 + 2 * k);
                 }
-                // the tile's boundary rows and the ownership flags of the window
-                const int kb = t.tb_start[tile];
-                nbt = min(t.tb_start[tile + 1] - kb, TBC);
-                for (int k = threadIdx.x; k < nbt; k += blockDim.x) {
-                    const int row = t.tb_list[kb + k];
-                    const int cell = row / 6;
-                    blr[k] = (int16_t)((((cell / g.Ny1) - wj0) * WSTR + ((cell % g.Ny1) - wi0)) * 6 + (row - 6 * cell));
-                    bbv[k] = t.b[row];
-                    T diag = 0;
 #pragma unroll
-                    for (int sl = 0; sl < HMEC_W; sl++) {
-                        const size_t o = (size_t)sl * g.N + row;
-                        const T v = t.val[o];
-                        bval[sl * TBC + k] = v;
-                        boff[sl * TBC + k] = t.off[o];
-                        if (t.col[o] == row) diag += v;
-                    }
-                    bdiag[k] = diag;
-                }
-                for (int lw = threadIdx.x; lw < WIN_MAX; lw += blockDim.x) {
-                    const int lc = lw / 6, v = lw - 6 * lc;
-                    const int ci = wi0 + lc % WSTR, cj = wj0 + lc / WSTR;
-                    own[lw] = (ci >= 0 && ci <= g.Ny && cj >= 0 && cj <= g.Nx &&
-                               unknown_tile(g, t.ntile_i, ci, cj, v) == tile) ? 1 : 0;
-                }
-#pragma unroll
-                for (int c = 0; c < 9; c++) {
-                    int fi, fj, ni, nj;
-                    colour_grid(c, i0, j0, i1, j1, fi, fj, ni, nj);
-                    meta[c] = 0;
-                    if (slot < ni * nj && q < PB) {
-                        const int i = fi + 3 * (slot % ni), j = fj + 3 * (slot / ni);
-                        const int ci = i - qdi, cj = j - qdj;
-                        const int lrow = ((cj - wj0) * WSTR + (ci - wi0)) * 6 + qv;
-                        const int rl = (cj - j0 + 1) * RSTR + (ci - i0 + 1) * 6 + qv;
-                        const int lp = (i - i0) + (j - j0) * TILE;
-                        meta[c] = (1 << 29) | (lp << 21) | (rl << 11) | lrow;
-                    }
-                }
+                for (int c = 0; c < 9; c++) meta[c] = t.meta_t[((size_t)tile * 9 + c) * TILE_BS + threadIdx.x];
+                // the boundary rows' rhs, gathered by their row numbers in the pack
+                const int32_t* brow = reinterpret_cast<const int32_t*>(
+                    t.bpack + (size_t)tile * pack_bytes<T>(TBC) + (size_t)TBC * (HMEC_W * sizeof(T) + sizeof(T) + HMEC_W * 2 + 2));
+                nbt = min(t.tb_start[tile + 1] - t.tb_start[tile], TBC);
+                for (int k = threadIdx.x; k < nbt; k += blockDim.x) bbv[k] = t.b[brow[k]];
                 staged = tile;
             }
             if (!whole && threadIdx.x == 0) issue_pinv(t, pv, bar, 0, 0, i0, j0, i1, j1);
@@ -796,9 +854,9 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(StageArgs<T> t, int
             }
             cp_async_wait_all();
             __syncthreads();
-            if (whole && fresh) {
-                mbar_wait(&bar[0], use0 & 1, t.status);
-                use0++;
+            if (fresh) {
+                mbar_wait(&bar[2], use2 & 1, t.status);
+                use2++;
             }
 #pragma unroll
             for (int c = 0; c < 9; c++) {
@@ -815,12 +873,12 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(StageArgs<T> t, int
                     if (c < 8 && threadIdx.x == 0) issue_pinv(t, pv, bar, c + 1, bb ^ 1, i0, j0, i1, j1);
                 }
                 const int m = meta[c];
-                const bool valid = (m >> 29) & 1;
-                const int lrow = m & 2047, rl = (m >> 11) & 1023;
+                const bool valid = (m >> 30) & 1;
+                const int lrow = m & 2047, rl = (m >> 11) & 2047;
                 T pr[PB];
                 T r = 0;
                 if (valid) {
-                    const T* pi = whole ? pv + ((m >> 21) & 255) * 100 + q * PB : pv + (bb * PV_MAX + slot) * 100 + q * PB;
+                    const T* pi = whole ? pv + ((m >> 22) & 255) * 100 + q * PB : pv + (bb * PV_MAX + slot) * 100 + q * PB;
 #pragma unroll
                     for (int cc = 0; cc < PB; cc++) pr[cc] = pi[cc];
                     T acc = sb[rl];
@@ -1420,16 +1478,47 @@ static std::vector<int32_t> boundary_rows(const Geo& g) {
     return r;
 }
 
+// A 3-D TMA descriptor of a dense array [d2][d1][d0] (d0 fastest) with box
+// (b0, b1, b2); elements outside the array load as zero.  The encoder is the
+// driver's cuTensorMapEncodeTiled, reached through the runtime.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static int encode_map3(hmec_ctx* ctx, CUtensorMap* map, CUtensorMapDataType dt, size_t esize, void* base,
+                       uint64_t d0, uint64_t d1, uint64_t d2, uint32_t b0, uint32_t b1, uint32_t b2) {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+            ctx->err = "cuTensorMapEncodeTiled is not available from the driver";
+            return HMEC_ERR_CUDA;
+        }
+        fn = (EncodeTiledFn)p;
+    }
+    const cuuint64_t dims[3] = {d0, d1, d2};
+    const cuuint64_t strides[2] = {d0 * esize, d0 * d1 * esize};
+    const cuuint32_t box[3] = {b0, b1, b2};
+    const cuuint32_t es[3] = {1, 1, 1};
+    const CUresult r = fn(map, dt, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        ctx->err = "cuTensorMapEncodeTiled rejected a smoother descriptor";
+        return HMEC_ERR_CUDA;
+    }
+    return HMEC_OK;
+}
+
 static int alloc_level(hmec_ctx* ctx, Level& L, bool mixed, bool coarse) {
     const Geo& g = L.g;
     const size_t N = (size_t)g.N;
     L.npatch = (g.Ny - 1) * (g.Nx - 1);
-    L.off16 = nullptr;
     L.pmx = L.pmy = nullptr;
     L.ridx = nullptr;
     L.rwg = L.rw = nullptr;
     L.rw32 = nullptr;
-    HMEC_CUDA(ctx, cudaMalloc(&L.off16, sizeof(int16_t) * HMEC_W * N));
     HMEC_CUDA(ctx, cudaMalloc(&L.col, sizeof(int32_t) * HMEC_W * N));
     HMEC_CUDA(ctx, cudaMalloc(&L.val, sizeof(double) * HMEC_W * N));
     HMEC_CUDA(ctx, cudaMalloc(&L.dscale, sizeof(double) * N));
@@ -1470,11 +1559,10 @@ static int alloc_level(hmec_ctx* ctx, Level& L, bool mixed, bool coarse) {
         for (int j = 0; j <= g.Nx; j++)
             for (int i = 0; i <= g.Ny; i++)
                 for (int v = 0; v < 6; v++) owner[(j * g.Ny1 + i) * 6 + v] = unknown_tile(g, L.ntile_i, i, j, v);
-        std::vector<int32_t> os(L.ntiles + 1, 0), bs(L.ntiles + 1, 0);
-        for (size_t u = 0; u < N; u++) {
-            os[owner[u] + 1]++;
+        // each tile's boundary rows, listed tile by tile
+        std::vector<int32_t> bs(L.ntiles + 1, 0);
+        for (size_t u = 0; u < N; u++)
             if (isb[u]) bs[owner[u] + 1]++;
-        }
         int tbm = 0;
         for (int k = 0; k < L.ntiles; k++) tbm = std::max(tbm, (int)bs[k + 1]);
         if (tbm > TB_MAX) {
@@ -1482,26 +1570,53 @@ static int alloc_level(hmec_ctx* ctx, Level& L, bool mixed, bool coarse) {
             return HMEC_ERR_ARG;
         }
         L.tb_cap = std::max(16, (tbm + 15) / 16 * 16);
-        for (int k = 0; k < L.ntiles; k++) {
-            os[k + 1] += os[k];
-            bs[k + 1] += bs[k];
-        }
-        std::vector<int32_t> ol(N), bl(std::max<size_t>(br.size(), 1)), oc(os.begin(), os.end() - 1),
-            bc(bs.begin(), bs.end() - 1);
-        for (size_t u = 0; u < N; u++) {
-            ol[oc[owner[u]]++] = (int32_t)u;
+        for (int k = 0; k < L.ntiles; k++) bs[k + 1] += bs[k];
+        std::vector<int32_t> bl(std::max<size_t>(br.size(), 1)), bc(bs.begin(), bs.end() - 1);
+        for (size_t u = 0; u < N; u++)
             if (isb[u]) bl[bc[owner[u]]++] = (int32_t)u;
-        }
-        HMEC_CUDA(ctx, cudaMalloc(&L.owner, sizeof(int32_t) * N));
-        HMEC_CUDA(ctx, cudaMalloc(&L.own_start, sizeof(int32_t) * os.size()));
-        HMEC_CUDA(ctx, cudaMalloc(&L.own_list, sizeof(int32_t) * N));
         HMEC_CUDA(ctx, cudaMalloc(&L.tbnd_start, sizeof(int32_t) * bs.size()));
         HMEC_CUDA(ctx, cudaMalloc(&L.tbnd_list, sizeof(int32_t) * bl.size()));
-        HMEC_CUDA(ctx, cudaMemcpy(L.owner, owner.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice));
-        HMEC_CUDA(ctx, cudaMemcpy(L.own_start, os.data(), sizeof(int32_t) * os.size(), cudaMemcpyHostToDevice));
-        HMEC_CUDA(ctx, cudaMemcpy(L.own_list, ol.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice));
         HMEC_CUDA(ctx, cudaMemcpy(L.tbnd_start, bs.data(), sizeof(int32_t) * bs.size(), cudaMemcpyHostToDevice));
         HMEC_CUDA(ctx, cudaMemcpy(L.tbnd_list, bl.data(), sizeof(int32_t) * bl.size(), cudaMemcpyHostToDevice));
+        // per tile: window ownership flags and the per-lane colour table
+        std::vector<uint8_t> ownt((size_t)L.ntiles * OWN_STRIDE, 0);
+        std::vector<int32_t> meta((size_t)L.ntiles * 9 * TILE_BS, 0);
+        for (int tile = 0; tile < L.ntiles; tile++) {
+            const int ti = tile % L.ntile_i, tj = tile / L.ntile_i;
+            const int i0 = 1 + ti * TILE, j0 = 1 + tj * TILE;
+            const int i1 = std::min(i0 + TILE, g.Ny), j1 = std::min(j0 + TILE, g.Nx);
+            for (int lw = 0; lw < WIN_MAX; lw++) {
+                const int lc = lw / 6, v = lw - 6 * lc;
+                const int ci = i0 - 2 + lc % WSTR, cj = j0 - 2 + lc / WSTR;
+                if (ci >= 0 && ci <= g.Ny && cj >= 0 && cj <= g.Nx)
+                    ownt[(size_t)tile * OWN_STRIDE + lw] = owner[(cj * g.Ny1 + ci) * 6 + v] == tile ? 1 : 0;
+            }
+            for (int c = 0; c < 9; c++)
+                for (int tt = 0; tt < TILE_BS; tt++)
+                    meta[((size_t)tile * 9 + c) * TILE_BS + tt] = lane_meta(c, tt, i0, j0, i1, j1);
+        }
+        HMEC_CUDA(ctx, cudaMalloc(&L.own_t, ownt.size()));
+        HMEC_CUDA(ctx, cudaMalloc(&L.meta_t, sizeof(int32_t) * meta.size()));
+        HMEC_CUDA(ctx, cudaMemcpy(L.own_t, ownt.data(), ownt.size(), cudaMemcpyHostToDevice));
+        HMEC_CUDA(ctx, cudaMemcpy(L.meta_t, meta.data(), sizeof(int32_t) * meta.size(), cudaMemcpyHostToDevice));
+        // the smoother's padded matrix copy, the boundary packs, and their TMA maps
+        const size_t st = mixed ? sizeof(float) : sizeof(double);
+        L.CS = align_up(6 * g.Ny1, 8);
+        const size_t ns = (size_t)HMEC_W * g.Nx1 * L.CS;
+        HMEC_CUDA(ctx, cudaMalloc(&L.vals, st * ns));
+        HMEC_CUDA(ctx, cudaMalloc(&L.offs, sizeof(int16_t) * ns));
+        HMEC_CUDA(ctx, cudaMemset(L.vals, 0, st * ns));
+        HMEC_CUDA(ctx, cudaMemset(L.offs, 0, sizeof(int16_t) * ns));
+        L.pack_bytes = mixed ? pack_bytes<float>(L.tb_cap) : pack_bytes<double>(L.tb_cap);
+        HMEC_CUDA(ctx, cudaMalloc(&L.bpack, (size_t)L.ntiles * L.pack_bytes));
+        const CUtensorMapDataType dt = mixed ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+        int rc = encode_map3(ctx, &L.tm_val, dt, st, L.vals, L.CS, g.Nx1, HMEC_W, RSTR, TILE + 1, HMEC_W);
+        if (!rc) rc = encode_map3(ctx, &L.tm_off, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, L.offs, L.CS, g.Nx1, HMEC_W, RSTR,
+                                  TILE + 1, HMEC_W);
+        if (!rc)
+            rc = encode_map3(ctx, &L.tm_pinv, dt, st, mixed ? (void*)L.pinv32 : (void*)L.pinv, 100, g.Ny - 1, g.Nx - 1,
+                             100, TILE, TILE);
+        if (rc) return rc;
     }
     if (coarse) {
         const size_t nb = (size_t)g.Nx * g.Ny, ns = (size_t)g.Nx1 * g.Ny1;
@@ -1653,12 +1768,13 @@ void solver_free(hmec_ctx* ctx) {
         cudaFree(L.fr);
         cudaFree(L.dx2);
         cudaFree(L.fx2);
-        cudaFree(L.owner);
-        cudaFree(L.own_start);
-        cudaFree(L.own_list);
         cudaFree(L.tbnd_start);
         cudaFree(L.tbnd_list);
-        cudaFree(L.off16);
+        cudaFree(L.vals);
+        cudaFree(L.offs);
+        cudaFree(L.own_t);
+        cudaFree(L.meta_t);
+        cudaFree(L.bpack);
         cudaFree(L.pmx);
         cudaFree(L.pmy);
         cudaFree(L.ridx);
@@ -1710,8 +1826,18 @@ int solver_setup(hmec_ctx* ctx) {
             HMEC_LAUNCH(ctx, k_vanka_setup<double>, nblocks((long long)L.npatch * 16, VS_BS), VS_BS, 0, L.g, L.col,
                         L.val, L.pinv, status);
         const size_t n = (size_t)HMEC_W * L.g.N;
-        HMEC_LAUNCH(ctx, k_stage_prep, nblocks(n, 256), 256, 0, L.g.N, L.g.Ny1, L.col, L.val, L.off16,
-                    mixed ? L.val32 : nullptr, status);
+        const size_t nb = (size_t)L.ntiles * L.tb_cap;
+        if (mixed) {
+            HMEC_LAUNCH(ctx, k_stage_prep<float>, nblocks(n, 256), 256, 0, L.g.N, L.g.Ny1, L.g.Nx1, L.CS, L.col,
+                        L.val, (float*)L.vals, L.offs, L.val32, status);
+            HMEC_LAUNCH(ctx, k_stage_bpack<float>, nblocks(nb, 128), 128, 0, L.g, L.ntile_i, L.ntiles, L.tb_cap,
+                        L.tbnd_start, L.tbnd_list, L.col, L.val, L.bpack, status);
+        } else {
+            HMEC_LAUNCH(ctx, k_stage_prep<double>, nblocks(n, 256), 256, 0, L.g.N, L.g.Ny1, L.g.Nx1, L.CS, L.col,
+                        L.val, (double*)L.vals, L.offs, nullptr, status);
+            HMEC_LAUNCH(ctx, k_stage_bpack<double>, nblocks(nb, 128), 128, 0, L.g, L.ntile_i, L.ntiles, L.tb_cap,
+                        L.tbnd_start, L.tbnd_list, L.col, L.val, L.bpack, status);
+        }
         if (l > 0)
             HMEC_LAUNCH(ctx, k_restrict_scale, nblocks(L.g.N, 256), 256, 0, L.g.N, L.ridx, L.rwg,
                         sv.lv[l - 1].dscale, L.dscale, L.rw, L.rw32);
@@ -1772,14 +1898,14 @@ static int stage_config(hmec_ctx* ctx, Level& L) {
     int nsm = 0, optin = 0;
     HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
     HMEC_CUDA(ctx, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->dev));
-    HMEC_CUDA(ctx, cudaFuncSetAttribute(k_smooth_stage<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     int blocks[2], smem[2];
     for (int w = 0; w < 2; w++) {
+        const void* kern = w ? (const void*)k_smooth_stage<T, true> : (const void*)k_smooth_stage<T, false>;
+        HMEC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
         smem[w] = stage_layout<T>(w, L.tb_cap).total;
         int per_sm = 0;
         if (smem[w] <= optin)
-            HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth_stage<T>, TILE_BS,
-                                                                         (size_t)smem[w]));
+            HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TILE_BS, (size_t)smem[w]));
         blocks[w] = per_sm * nsm;
     }
     if (blocks[0] < 1 && blocks[1] < 1) {
@@ -1837,16 +1963,20 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
     }
     if (!(ctx->p.mg_flags & HMEC_MG_UNTILED)) {
         StageArgs<T> t;
+        t.tm_val = L.tm_val;
+        t.tm_off = L.tm_off;
+        t.tm_pinv = L.tm_pinv;
         t.g = L.g;
         t.col = L.col;
         t.val = LvPtr<T>::val(L);
-        t.off = L.off16;
         t.pinv = LvPtr<T>::pinv(L);
         t.b = b;
         t.x = x;
         t.xalt = x_alt<T>(L);
         t.tb_start = L.tbnd_start;
-        t.tb_list = L.tbnd_list;
+        t.own_t = L.own_t;
+        t.meta_t = L.meta_t;
+        t.bpack = L.bpack;
         t.ntile_i = L.ntile_i;
         t.ntiles = L.ntiles;
         t.gc = a.gc;
@@ -1875,11 +2005,11 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
         }
         int rc = stage_config<T>(ctx, L);
         if (rc) return rc;
-        t.pv_whole = L.st_whole;
         t.tb_cap = L.tb_cap;
         void* args[] = {&t, &nsweeps, &mode};
         const bool prof = hmec_prof_begin(ctx, "k_smooth", ab);
-        HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_smooth_stage<T>, dim3(L.st_grid), dim3(TILE_BS), args,
+        const void* kern = L.st_whole ? (const void*)k_smooth_stage<T, true> : (const void*)k_smooth_stage<T, false>;
+        HMEC_CUDA(ctx, cudaLaunchCooperativeKernel(kern, dim3(L.st_grid), dim3(TILE_BS), args,
                                                    (size_t)L.st_smem, ctx->stream));
         ctx->launches++;
         if (prof) hmec_prof_end(ctx);
