@@ -642,10 +642,9 @@ struct StageArgs {
 };
 
 // Shared-memory layout of the staged pass, in bytes.  Its size depends on the
-// inverse mode and on the level's boundary-row capacity, and decides how many
-// blocks are co-resident: a level with more tiles than blocks restages every
-// tile every sweep, so large levels stream the inverses (about 100 KB for
-// FP32, two blocks per SM) and the others stage them whole.
+// inverse mode and on the level's boundary-row capacity (FP32 with whole-tile
+// inverses: about 143 KB, one block per SM; a level with more tiles than
+// blocks restages a tile every time a block takes it up).
 struct StageLayout {
     int xs, val, off, b, pv, pack, bb, bdel, own, bar, total;
 };
@@ -1888,10 +1887,9 @@ static int max_coop_blocks(hmec_ctx* ctx) {
     return c;
 }
 
-// Launch configuration of the staged pass on one level: stage whole tiles of
-// inverses when every tile then still gets its own co-resident block, else
-// stream them per colour, whichever gives more blocks (so a block keeps one
-// tile for all its sweeps whenever shared memory allows).
+// Launch configuration of the staged pass on one level: whole-tile inverses
+// when they fit in shared memory (FP32), else per-colour inverses (FP64); the
+// grid is the co-resident block count or the tile count, whichever is smaller.
 template <typename T>
 static int stage_config(hmec_ctx* ctx, Level& L) {
     if (L.st_whole >= 0) return HMEC_OK;
@@ -1912,7 +1910,10 @@ static int stage_config(hmec_ctx* ctx, Level& L) {
         ctx->err = "the staged smoothing pass does not fit in shared memory";
         return HMEC_ERR_ARG;
     }
-    const int w = (blocks[1] >= L.ntiles || blocks[1] >= blocks[0]) ? 1 : 0;
+    // whole-tile inverses whenever they fit: with the TMA stage a block that
+    // restages a tile each sweep is still faster than one that waits for each
+    // colour's inverses (measured on the 201x201 and 1001x401 levels)
+    const int w = blocks[1] > 0 ? 1 : 0;
     L.st_whole = w;
     L.st_grid = std::min(L.ntiles, blocks[w]);
     L.st_smem = smem[w];
