@@ -1233,71 +1233,6 @@ __global__ void k_zero(size_t n, T* a) {
 }
 
 // ------------------------------------------------------------ FGMRES
-// partial[k * nblk + blk] = sum over the block's rows of V_k . w   (k = blockIdx.y)
-__global__ void k_dots(int N, const double* __restrict__ V, const double* __restrict__ w, double* partial, int nblk,
-                       const int* done) {
-    if (*done) return;
-    __shared__ double sh[RED_BS];
-    const int k = blockIdx.y;
-    const double* v = V + (size_t)k * N;
-    double acc = 0;
-    for (int r = blockIdx.x * RED_BS + threadIdx.x; r < N; r += nblk * RED_BS) acc += v[r] * w[r];
-    sh[threadIdx.x] = acc;
-    __syncthreads();
-    for (int s = RED_BS / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) partial[(size_t)k * nblk + blockIdx.x] = sh[0];
-}
-
-// dots[k] = sum_b partial[k][b], one warp per k, fixed order.
-__global__ void k_dots_final(const double* __restrict__ partial, int nblk, int nk, double* dots, const int* done) {
-    if (*done) return;
-    const int k = blockIdx.x;
-    if (k >= nk) return;
-    double acc = 0;
-    for (int b = threadIdx.x; b < nblk; b += 32) acc += partial[(size_t)k * nblk + b];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (threadIdx.x == 0) dots[k] = acc;
-}
-
-// w -= sum_k h_k V_k; partial sums of |w|^2 into partial[0..nblk)
-__global__ void k_orth_update(int N, const double* __restrict__ V, int nk, const double* __restrict__ h, double* w,
-                              double* partial, int nblk, const int* done) {
-    if (*done) return;
-    __shared__ double sh[RED_BS];
-    double acc2 = 0;
-    for (int r = blockIdx.x * RED_BS + threadIdx.x; r < N; r += nblk * RED_BS) {
-        double x = w[r];
-        for (int k = 0; k < nk; k++) x -= h[k] * V[(size_t)k * N + r];
-        w[r] = x;
-        acc2 += x * x;
-    }
-    sh[threadIdx.x] = acc2;
-    __syncthreads();
-    for (int s = RED_BS / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
-}
-
-// w = A z (scaled rows)
-__global__ void k_spmv(int N, const int32_t* __restrict__ col, const double* __restrict__ val,
-                       const double* __restrict__ z, double* w, const int* done) {
-    if (*done) return;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= N) return;
-    double acc = 0;
-#pragma unroll
-    for (int s = 0; s < HMEC_W; s++) {
-        const size_t o = (size_t)s * N + row;
-        acc += val[o] * z[col[o]];
-    }
-    w[row] = acc;
-}
-
 // r = b - A x, with partial sums of |r|^2 and |b|^2
 __global__ void k_true_resid(int N, const int32_t* __restrict__ col, const double* __restrict__ val,
                              const double* __restrict__ b, const double* __restrict__ x, double* r, double* partial,
@@ -1379,9 +1314,9 @@ __global__ void k_scale_vec(int N, const double* __restrict__ a, const double* s
 
 // After the two CGS passes: column j of H, Givens rotation, residual estimate.
 // One warp; lane 0 applies the rotations.
-__global__ void k_arnoldi_step(Gm G, const double* __restrict__ h1, const double* __restrict__ partial, int nblk,
-                               int j, int m, double rtol, double* hscale) {
-    if (*G.done) return;
+__device__ __forceinline__ void arnoldi_update(const Gm& G, const double* __restrict__ h1,
+                                               const double* __restrict__ partial, int nblk, int j, int m, double rtol,
+                                               double* hscale) {
     const double hn = sqrt(warp_sum_fixed(partial, nblk));
     double* Hc = G.H + (size_t)j * (m + 1);  // column j, rows 0..j+1
     for (int k = threadIdx.x; k <= j; k += 32) Hc[k] = h1[k] + G.dots[k];  // first + second CGS pass
@@ -1408,6 +1343,131 @@ __global__ void k_arnoldi_step(Gm G, const double* __restrict__ h1, const double
     G.ds->krylov_iters += 1;
     hscale[0] = hn > 0 ? 1.0 / hn : 0.0;
     if (rel <= rtol || !(hn > 0) || !isfinite(rel)) *G.done = 1;
+}
+
+// One Arnoldi step of FGMRES after the preconditioner, as one cooperative
+// launch: z_j (FP64, from the preconditioner's output zsrc), w = A z_j,
+// classical Gram-Schmidt twice against V_0..V_j, the Hessenberg column with
+// its Givens rotation, and V_{j+1} = w / |w| (plus its FP32 copy, the next
+// preconditioner input of the mixed form).  Every reduction is a block
+// partial then one warp per coefficient in a fixed order (deterministic).
+template <typename TZ>
+struct ArnArgs {
+    int N, j, m, nblk;
+    const int32_t* col;
+    const double* val;
+    const TZ* zsrc;
+    double* Zj;          // z_j in FP64 (may equal zsrc)
+    double* V;           // (m+1) x N basis
+    double* w;
+    double* partial;     // (m+2) x nblk
+    Gm G;
+    double rtol;
+    float* next32;       // if set: FP32 copy of V_{j+1}
+};
+
+constexpr int ARN_BS = 256;
+
+// thread 0 of the block gets the block's sum of v (fixed order)
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < ARN_BS / 32; k++) s += sh[k];
+    __syncthreads();
+    return s;
+}
+
+// partial[k*nblk + block] = this block's part of V_k . w, k = 0..j
+__device__ __forceinline__ void dots_partial(const double* __restrict__ V, const double* __restrict__ w, int N, int j,
+                                             double* partial, int nblk, double* sh) {
+    for (int k = 0; k <= j; k++) {
+        const double* v = V + (size_t)k * N;
+        double a = 0;
+        for (int r = blockIdx.x * ARN_BS + threadIdx.x; r < N; r += nblk * ARN_BS) a += v[r] * w[r];
+        const double s = block_sum(a, sh);
+        if (threadIdx.x == 0) partial[(size_t)k * nblk + blockIdx.x] = s;
+    }
+}
+
+// block 0: h[k] = sum over blocks of partial[k][.], one warp per k
+__device__ __forceinline__ void dots_final(const double* __restrict__ partial, int nblk, int j, double* h) {
+    if (blockIdx.x != 0) return;
+    const int lane = threadIdx.x & 31;
+    for (int k = threadIdx.x >> 5; k <= j; k += ARN_BS / 32) {
+        double a = 0;
+        for (int b = lane; b < nblk; b += 32) a += partial[(size_t)k * nblk + b];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) h[k] = a;
+    }
+}
+
+// w -= sum_k h[k] V_k; with norm: partial[block] = this block's part of |w|^2
+__device__ __forceinline__ void orth_update(const double* __restrict__ V, double* w, int N, int j,
+                                            const double* __restrict__ hg, double* partial, int nblk, double* sh,
+                                            double* shh, bool norm) {
+    for (int k = threadIdx.x; k <= j; k += ARN_BS) shh[k] = hg[k];
+    __syncthreads();
+    double a2 = 0;
+    for (int r = blockIdx.x * ARN_BS + threadIdx.x; r < N; r += nblk * ARN_BS) {
+        double x = w[r];
+        for (int k = 0; k <= j; k++) x -= shh[k] * V[(size_t)k * N + r];
+        w[r] = x;
+        a2 += x * x;
+    }
+    if (norm) {
+        const double s = block_sum(a2, sh);
+        if (threadIdx.x == 0) partial[blockIdx.x] = s;
+    }
+}
+
+// dynamic shared memory: (m + 1) doubles
+template <typename TZ>
+__global__ void __launch_bounds__(ARN_BS) k_arnoldi(ArnArgs<TZ> a) {
+    __shared__ double sh[ARN_BS / 32];
+    extern __shared__ double shh[];
+    if (*a.G.done) return;  // set only by an earlier launch: uniform across the grid
+    cg::grid_group grid = cg::this_grid();
+    const int N = a.N, j = a.j, m = a.m, nblk = a.nblk;
+    double* dots = a.G.dots;
+    // z_j and w = A z_j
+    for (int r = blockIdx.x * ARN_BS + threadIdx.x; r < N; r += nblk * ARN_BS) {
+        if ((const void*)a.zsrc != (const void*)a.Zj) a.Zj[r] = (double)a.zsrc[r];
+        double acc = 0;
+#pragma unroll
+        for (int s = 0; s < HMEC_W; s++) {
+            const size_t o = (size_t)s * N + r;
+            acc += a.val[o] * (double)a.zsrc[a.col[o]];
+        }
+        a.w[r] = acc;
+    }
+    grid.sync();
+    // CGS pass 1 (coefficients at dots[m+2..]) and pass 2 (dots[0..])
+    dots_partial(a.V, a.w, N, j, a.partial, nblk, sh);
+    grid.sync();
+    dots_final(a.partial, nblk, j, dots + m + 2);
+    grid.sync();
+    orth_update(a.V, a.w, N, j, dots + m + 2, a.partial, nblk, sh, shh, false);
+    grid.sync();
+    dots_partial(a.V, a.w, N, j, a.partial, nblk, sh);
+    grid.sync();
+    dots_final(a.partial, nblk, j, dots);
+    grid.sync();
+    orth_update(a.V, a.w, N, j, dots, a.partial, nblk, sh, shh, true);
+    grid.sync();
+    if (blockIdx.x == 0 && threadIdx.x < 32)
+        arnoldi_update(a.G, dots + m + 2, a.partial, nblk, j, m, a.rtol, dots + 2 * m + 3);
+    grid.sync();
+    // V_{j+1} = w / |w| (written whether or not this step converged)
+    const double sc = dots[2 * m + 3];
+    double* Vn = a.V + (size_t)(j + 1) * N;
+    for (int r = blockIdx.x * ARN_BS + threadIdx.x; r < N; r += nblk * ARN_BS) {
+        const double v = a.w[r] * sc;
+        Vn[r] = v;
+        if (a.next32) a.next32[r] = (float)v;
+    }
 }
 
 // y = H^{-1} g (upper triangular, kcur columns)
@@ -2068,18 +2128,52 @@ static int vcycle(hmec_ctx* ctx, size_t l, const T* b_in = nullptr, T* x_in = nu
 }
 
 // z = M^{-1} v on the fine level (v, z FP64 vectors of the scaled system)
-static int precondition(hmec_ctx* ctx, const double* v, double* z) {
+// (mixed form: z is left in FP32 in the fine level's x; input_ready: its
+// FP32 input is already in the fine level's b)
+static int precondition(hmec_ctx* ctx, const double* v, double* z, bool input_ready) {
     Solver& sv = ctx->sv;
     Level& L = sv.lv[0];
     const size_t N = (size_t)L.g.N;
     if (ctx->p.form == HMEC_FORM_MIXED) {
-        HMEC_LAUNCH(ctx, (k_convert<double, float>), nblocks(N, 256), 256, 0, N, v, L.fb);
-        int rc = vcycle<float>(ctx, 0);
-        if (rc) return rc;
-        HMEC_LAUNCH(ctx, (k_convert<float, double>), nblocks(N, 256), 256, 0, N, L.fx, z);
-        return HMEC_OK;
+        if (!input_ready) HMEC_LAUNCH(ctx, (k_convert<double, float>), nblocks(N, 256), 256, 0, N, v, L.fb);
+        return vcycle<float>(ctx, 0);
     }
     return vcycle<double>(ctx, 0, v, z);
+}
+
+// One cooperative Arnoldi step (k_arnoldi) after the preconditioner.
+template <typename TZ>
+static int arnoldi(hmec_ctx* ctx, const TZ* zsrc, double* Zj, int j, const Gm& G, double rtol) {
+    Solver& sv = ctx->sv;
+    Level& L0 = sv.lv[0];
+    static int cached = 0;
+    if (!cached) {
+        int per_sm = 0, nsm = 0;
+        HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_arnoldi<TZ>, ARN_BS,
+                                                                     sizeof(double) * 129));
+        HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
+        cached = std::max(1, per_sm * nsm);
+    }
+    ArnArgs<TZ> a;
+    a.N = sv.N;
+    a.j = j;
+    a.m = sv.m;
+    a.nblk = std::min(sv.nblk, cached);
+    a.col = L0.col;
+    a.val = L0.val;
+    a.zsrc = zsrc;
+    a.Zj = Zj;
+    a.V = sv.V;
+    a.w = sv.w;
+    a.partial = sv.partial;
+    a.G = G;
+    a.rtol = rtol;
+    a.next32 = ctx->p.form == HMEC_FORM_MIXED ? L0.fb : nullptr;
+    void* args[] = {&a};
+    HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_arnoldi<TZ>, dim3(a.nblk), dim3(ARN_BS), args,
+                                               sizeof(double) * (sv.m + 1), ctx->stream));
+    ctx->launches++;
+    return HMEC_OK;
 }
 
 int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
@@ -2088,6 +2182,7 @@ int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
     const int N = sv.N, m = sv.m, nblk = sv.nblk;
     const double rtol = ctx->p.krylov_rtol;
     const int maxit = std::max(1, ctx->p.krylov_maxit);
+    const bool mixed = ctx->p.form == HMEC_FORM_MIXED;
     double* x = ctx->S;
     const double* b = L0.db;
     Gm G{sv.H, sv.cs, sv.sn, sv.gvec, sv.yvec, sv.dots, sv.bnorm, sv.done, sv.kcur, ctx->ds};
@@ -2133,21 +2228,14 @@ int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
                 hd = ctx->hs->pad0;
                 if (hd) break;
             }
-            int prc = precondition(ctx, Vj, Zj);
+            // the previous Arnoldi step already wrote the mixed form's FP32 input
+            int prc = precondition(ctx, Vj, Zj, j > 0);
             if (prc) return prc;
-            HMEC_LAUNCH_B(ctx, (double)N * (HMEC_W * 12.0 + 16.0), k_spmv, nblocks(N, 256), 256, 0, N, L0.col, L0.val,
-                          Zj, sv.w, sv.done);
-            // CGS pass 1
-            HMEC_LAUNCH(ctx, k_dots, dim3(nblk, j + 1), RED_BS, 0, N, sv.V, sv.w, sv.partial, nblk, sv.done);
-            HMEC_LAUNCH(ctx, k_dots_final, j + 1, 32, 0, sv.partial, nblk, j + 1, sv.dots + m + 2, sv.done);
-            HMEC_LAUNCH(ctx, k_orth_update, nblk, RED_BS, 0, N, sv.V, j + 1, sv.dots + m + 2, sv.w, sv.partial, nblk, sv.done);
-            // CGS pass 2
-            HMEC_LAUNCH(ctx, k_dots, dim3(nblk, j + 1), RED_BS, 0, N, sv.V, sv.w, sv.partial, nblk, sv.done);
-            HMEC_LAUNCH(ctx, k_dots_final, j + 1, 32, 0, sv.partial, nblk, j + 1, sv.dots, sv.done);
-            HMEC_LAUNCH(ctx, k_orth_update, nblk, RED_BS, 0, N, sv.V, j + 1, sv.dots, sv.w, sv.partial, nblk, sv.done);
-            HMEC_LAUNCH(ctx, k_arnoldi_step, 1, 32, 0, G, sv.dots + m + 2, sv.partial, nblk, j, m, rtol,
-                        sv.dots + 2 * m + 3);
-            HMEC_LAUNCH(ctx, k_scale_vec, nblocks(N, 256), 256, 0, N, sv.w, sv.dots + 2 * m + 3, sv.V + (size_t)(j + 1) * N, sv.done);
+            if (mixed)
+                prc = arnoldi<float>(ctx, L0.fx, Zj, j, G, rtol);
+            else
+                prc = arnoldi<double>(ctx, Zj, Zj, j, G, rtol);
+            if (prc) return prc;
         }
         HMEC_LAUNCH(ctx, k_lsq, 1, 1, 0, G, m);
         HMEC_LAUNCH(ctx, k_xupdate, nblocks(N, 256), 256, 0, N, sv.Z, sv.yvec, sv.kcur, x);
