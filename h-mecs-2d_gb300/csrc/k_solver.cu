@@ -1380,15 +1380,20 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
     return s;
 }
 
-// partial[k*nblk + block] = this block's part of V_k . w, k = 0..j
+// partial[k*nblk + block] = this block's part of V_k . w, k = 0..j: the block
+// takes a contiguous range of rows and each warp whole coefficients, so no
+// block barrier is needed (w stays in L1 across the warp's coefficients)
 __device__ __forceinline__ void dots_partial(const double* __restrict__ V, const double* __restrict__ w, int N, int j,
-                                             double* partial, int nblk, double* sh) {
-    for (int k = 0; k <= j; k++) {
+                                             double* partial, int nblk) {
+    const int chunk = ((N + nblk - 1) / nblk + 31) / 32 * 32;
+    const int r0 = blockIdx.x * chunk, r1 = min(N, r0 + chunk);
+    const int lane = threadIdx.x & 31;
+    for (int k = threadIdx.x >> 5; k <= j; k += ARN_BS / 32) {
         const double* v = V + (size_t)k * N;
         double a = 0;
-        for (int r = blockIdx.x * ARN_BS + threadIdx.x; r < N; r += nblk * ARN_BS) a += v[r] * w[r];
-        const double s = block_sum(a, sh);
-        if (threadIdx.x == 0) partial[(size_t)k * nblk + blockIdx.x] = s;
+        for (int r = r0 + lane; r < r1; r += 32) a += v[r] * w[r];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) partial[(size_t)k * nblk + blockIdx.x] = a;
     }
 }
 
@@ -1411,7 +1416,9 @@ __device__ __forceinline__ void orth_update(const double* __restrict__ V, double
     for (int k = threadIdx.x; k <= j; k += ARN_BS) shh[k] = hg[k];
     __syncthreads();
     double a2 = 0;
-    for (int r = blockIdx.x * ARN_BS + threadIdx.x; r < N; r += nblk * ARN_BS) {
+    const int chunk = ((N + nblk - 1) / nblk + 31) / 32 * 32;
+    const int r1 = min(N, (int)blockIdx.x * chunk + chunk);
+    for (int r = blockIdx.x * chunk + threadIdx.x; r < r1; r += ARN_BS) {
         double x = w[r];
         for (int k = 0; k <= j; k++) x -= shh[k] * V[(size_t)k * N + r];
         w[r] = x;
@@ -1432,8 +1439,10 @@ __global__ void __launch_bounds__(ARN_BS) k_arnoldi(ArnArgs<TZ> a) {
     cg::grid_group grid = cg::this_grid();
     const int N = a.N, j = a.j, m = a.m, nblk = a.nblk;
     double* dots = a.G.dots;
-    // z_j and w = A z_j
-    for (int r = blockIdx.x * ARN_BS + threadIdx.x; r < N; r += nblk * ARN_BS) {
+    // z_j and w = A z_j (rows in the block's contiguous range, as below)
+    const int chunk = ((N + nblk - 1) / nblk + 31) / 32 * 32;
+    const int rend = min(N, (int)blockIdx.x * chunk + chunk);
+    for (int r = blockIdx.x * chunk + threadIdx.x; r < rend; r += ARN_BS) {
         if ((const void*)a.zsrc != (const void*)a.Zj) a.Zj[r] = (double)a.zsrc[r];
         double acc = 0;
 #pragma unroll
@@ -1445,13 +1454,13 @@ __global__ void __launch_bounds__(ARN_BS) k_arnoldi(ArnArgs<TZ> a) {
     }
     grid.sync();
     // CGS pass 1 (coefficients at dots[m+2..]) and pass 2 (dots[0..])
-    dots_partial(a.V, a.w, N, j, a.partial, nblk, sh);
+    dots_partial(a.V, a.w, N, j, a.partial, nblk);
     grid.sync();
     dots_final(a.partial, nblk, j, dots + m + 2);
     grid.sync();
     orth_update(a.V, a.w, N, j, dots + m + 2, a.partial, nblk, sh, shh, false);
     grid.sync();
-    dots_partial(a.V, a.w, N, j, a.partial, nblk, sh);
+    dots_partial(a.V, a.w, N, j, a.partial, nblk);
     grid.sync();
     dots_final(a.partial, nblk, j, dots);
     grid.sync();
