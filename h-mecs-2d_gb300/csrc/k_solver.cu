@@ -639,6 +639,7 @@ struct StageArgs {
     T* bc;
     int tb_cap;            // boundary rows one tile's stage holds
     int* status;
+    const int* done;       // the solve's convergence flag: set, the pass does nothing
 };
 
 // Shared-memory layout of the staged pass, in bytes.  Its size depends on the
@@ -779,6 +780,10 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(const __grid_consta
     constexpr bool whole = WHOLE;
     const Geo& g = t.g;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    // a V-cycle launched after the solve converged (the host looks at the
+    // flag only every few iterations) does no work; no kernel of a V-cycle
+    // writes the flag, so every block sees the same value
+    if (*t.done) return;
     // bar[0], bar[1]: per-colour inverses (streamed mode); bar[2]: a tile's stage
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
@@ -2058,6 +2063,7 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
         t.rw = nullptr;
         t.bc = nullptr;
         t.status = &ctx->ds->status;
+        t.done = sv.done;
         // algorithmic bytes: per sweep the level's matrix (values and int16
         // window offsets), every inverse, the unknowns read and written and
         // the rhs; the prolonged correction; the fused residual (one pass
