@@ -1414,10 +1414,10 @@ __device__ __forceinline__ void dots_final(const double* __restrict__ partial, i
     }
 }
 
-// w -= sum_k h[k] V_k; with norm: partial[block] = this block's part of |w|^2
+// w -= sum_k h[k] V_k; normp[block] = this block's part of |w|^2
 __device__ __forceinline__ void orth_update(const double* __restrict__ V, double* w, int N, int j,
-                                            const double* __restrict__ hg, double* partial, int nblk, double* sh,
-                                            double* shh, bool norm) {
+                                            const double* __restrict__ hg, double* normp, int nblk, double* sh,
+                                            double* shh) {
     for (int k = threadIdx.x; k <= j; k += ARN_BS) shh[k] = hg[k];
     __syncthreads();
     double a2 = 0;
@@ -1429,10 +1429,8 @@ __device__ __forceinline__ void orth_update(const double* __restrict__ V, double
         w[r] = x;
         a2 += x * x;
     }
-    if (norm) {
-        const double s = block_sum(a2, sh);
-        if (threadIdx.x == 0) partial[blockIdx.x] = s;
-    }
+    const double s = block_sum(a2, sh);
+    if (threadIdx.x == 0) normp[blockIdx.x] = s;
 }
 
 // dynamic shared memory: (m + 1) doubles
@@ -1447,6 +1445,7 @@ __global__ void __launch_bounds__(ARN_BS) k_arnoldi(ArnArgs<TZ> a) {
     // z_j and w = A z_j (rows in the block's contiguous range, as below)
     const int chunk = ((N + nblk - 1) / nblk + 31) / 32 * 32;
     const int rend = min(N, (int)blockIdx.x * chunk + chunk);
+    double n0 = 0;
     for (int r = blockIdx.x * chunk + threadIdx.x; r < rend; r += ARN_BS) {
         if ((const void*)a.zsrc != (const void*)a.Zj) a.Zj[r] = (double)a.zsrc[r];
         double acc = 0;
@@ -1456,23 +1455,48 @@ __global__ void __launch_bounds__(ARN_BS) k_arnoldi(ArnArgs<TZ> a) {
             acc += a.val[o] * (double)a.zsrc[a.col[o]];
         }
         a.w[r] = acc;
+        n0 += acc * acc;
+    }
+    // rows m+1 and m of partial (unused by the dot products, k <= j < m):
+    // |A z|^2 and |w|^2 after the first pass
+    double* norm0 = a.partial + (size_t)(m + 1) * nblk;
+    double* norm1 = a.partial + (size_t)m * nblk;
+    {
+        const double s = block_sum(n0, sh);
+        if (threadIdx.x == 0) norm0[blockIdx.x] = s;
     }
     grid.sync();
-    // CGS pass 1 (coefficients at dots[m+2..]) and pass 2 (dots[0..])
+    // classical Gram-Schmidt (coefficients at dots[m+2..]) ...
     dots_partial(a.V, a.w, N, j, a.partial, nblk);
     grid.sync();
     dots_final(a.partial, nblk, j, dots + m + 2);
     grid.sync();
-    orth_update(a.V, a.w, N, j, dots + m + 2, a.partial, nblk, sh, shh, false);
+    orth_update(a.V, a.w, N, j, dots + m + 2, norm1, nblk, sh, shh);
     grid.sync();
-    dots_partial(a.V, a.w, N, j, a.partial, nblk);
-    grid.sync();
-    dots_final(a.partial, nblk, j, dots);
-    grid.sync();
-    orth_update(a.V, a.w, N, j, dots, a.partial, nblk, sh, shh, true);
-    grid.sync();
+    // ... repeated only when the first pass cancelled more than half of |w|
+    // ("twice is enough": |w1| < |w0| / sqrt 2); every block takes the same
+    // decision from the same fixed-order sums
+    __shared__ int reorth;
+    if (threadIdx.x < 32) {
+        const double s1 = warp_sum_fixed(norm1, nblk), s0 = warp_sum_fixed(norm0, nblk);
+        if (threadIdx.x == 0) reorth = !(s1 >= 0.5 * s0);
+    }
+    __syncthreads();
+    const double* normp = norm1;
+    if (reorth) {
+        dots_partial(a.V, a.w, N, j, a.partial, nblk);
+        grid.sync();
+        dots_final(a.partial, nblk, j, dots);
+        grid.sync();
+        orth_update(a.V, a.w, N, j, dots, a.partial, nblk, sh, shh);
+        grid.sync();
+        normp = a.partial;
+    } else if (blockIdx.x == 0) {
+        for (int k = threadIdx.x; k <= j; k += ARN_BS) dots[k] = 0;  // no second-pass coefficients
+        __syncthreads();
+    }
     if (blockIdx.x == 0 && threadIdx.x < 32)
-        arnoldi_update(a.G, dots + m + 2, a.partial, nblk, j, m, a.rtol, dots + 2 * m + 3);
+        arnoldi_update(a.G, dots + m + 2, normp, nblk, j, m, a.rtol, dots + 2 * m + 3);
     grid.sync();
     // V_{j+1} = w / |w| (written whether or not this step converged)
     const double sc = dots[2 * m + 3];
@@ -2185,9 +2209,16 @@ static int arnoldi(hmec_ctx* ctx, const TZ* zsrc, double* Zj, int j, const Gm& G
     a.rtol = rtol;
     a.next32 = ctx->p.form == HMEC_FORM_MIXED ? L0.fb : nullptr;
     void* args[] = {&a};
+    // algorithmic bytes: SpMV (FP64 values, int32 columns, z gathered, w and
+    // z_j written) and two CGS passes (each a dot and an update over j+1
+    // basis vectors), V_{j+1} written
+    const double N = sv.N, nb = j + 1;
+    const double bytes = N * (HMEC_W * 12.0 + sizeof(TZ) + 16.0) + 2.0 * N * 8.0 * (3.0 * nb + 2.0) + N * 12.0;
+    const bool prof = hmec_prof_begin(ctx, "k_arnoldi", bytes);
     HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_arnoldi<TZ>, dim3(a.nblk), dim3(ARN_BS), args,
                                                sizeof(double) * (sv.m + 1), ctx->stream));
     ctx->launches++;
+    if (prof) hmec_prof_end(ctx);
     return HMEC_OK;
 }
 
