@@ -180,13 +180,20 @@ struct Crd {
     const double *x, *y, *xvx, *yvx, *xvy, *yvy, *xp, *yp;
 };
 
-__global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, int64_t n, Geo g, Crd c, hmec_params p,
-                        double* __restrict__ out) {
+// FP64 runs at a small fraction of the FP32 rate on this GPU, so the
+// arithmetic is kept to what the values need: the cells come from the sort
+// key (no second set of divisions), (por/POR0)^3 is two products, the
+// distances are products with 1/dx and 1/dy, and 1/etad = k/etaf is one
+// division; each differs from the reference's expression by at most an ulp
+// or two (the marker->node fields are tested to 1e-13).
+__global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32_t* __restrict__ key, int64_t n,
+                        Geo g, Crd c, hmec_params p, double* __restrict__ out) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int m = perm[k];
     const double por = mk.porm[m];
-    double kkkmm = mk.kkkm[m] * pow(por / p.POR0, 3.0);
+    const double pr = por / p.POR0;
+    double kkkmm = mk.kkkm[m] * (pr * pr * pr);
     kkkmm = enforce_bounds(kkkmm, p.kkkmin, p.kkkmax);
     double cohescmm, cohestmm, frictcmm, dilatcmm, fricttmm, etasmm0, etamm0, etamm, rhomm;
     const double tm = mk.t_marker[m];
@@ -213,16 +220,19 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, int64_t n, 
     }
     etamm0 = enforce_bounds(etamm0, p.etamin, p.etamax);
     etamm = enforce_bounds(etamm, p.etamin, p.etamax);
-    const double etadm = mk.etafm[m] / kkkmm;
     const double xmm = mk.xm[m], ymm = mk.ym[m];
-    MarkerCells mc = marker_cells(xmm, ymm, g);
+    // half cell (hr, hc) = (2 ib + (iP - ib), 2 jb + (jP - jb)), key = hc * HR + hr
+    const int HR = 2 * (g.Ny - 1), kk = key[m];
+    const int hc = kk / HR, hr = kk - hc * HR;
+    const int ib = hr >> 1, jb = hc >> 1, iP = ib + (hr & 1), jP = jb + (hc & 1);
+    const double idx = 1.0 / g.dx, idy = 1.0 / g.dy;
     const size_t S = (size_t)n;
-    out[MP_DXB * S + k] = (xmm - c.x[mc.jb]) / g.dx;
-    out[MP_DYB * S + k] = (ymm - c.y[mc.ib]) / g.dy;
-    out[MP_DXX * S + k] = (xmm - c.xvx[mc.jb]) / g.dx;
-    out[MP_DYY * S + k] = (ymm - c.yvy[mc.ib]) / g.dy;
-    out[MP_DXP * S + k] = (xmm - c.xp[mc.jP]) / g.dx;
-    out[MP_DYP * S + k] = (ymm - c.yp[mc.iP]) / g.dy;
+    out[MP_DXB * S + k] = (xmm - c.x[jb]) * idx;
+    out[MP_DYB * S + k] = (ymm - c.y[ib]) * idy;
+    out[MP_DXX * S + k] = (xmm - c.xvx[jb]) * idx;
+    out[MP_DYY * S + k] = (ymm - c.yvy[ib]) * idy;
+    out[MP_DXP * S + k] = (xmm - c.xp[jP]) * idx;
+    out[MP_DYP * S + k] = (ymm - c.yp[iP]) * idy;
     out[MP_RHO * S + k] = rhomm;
     out[MP_KKK * S + k] = kkkmm;
     out[MP_TTT * S + k] = tm;
@@ -236,7 +246,7 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, int64_t n, 
     out[MP_ETAP * S + k] = etamm;
     out[MP_POR * S + k] = por;
     out[MP_ETAB0 * S + k] = etasmm0;
-    out[MP_INVETAD * S + k] = 1. / etadm;
+    out[MP_INVETAD * S + k] = kkkmm / mk.etafm[m];
     out[MP_RHOF * S + k] = mk.rhofm[m];
 }
 
@@ -425,7 +435,7 @@ int p2g_run(hmec_ctx* ctx) {
     mk.rhofm = ctx->mk[HMEC_M_rhofm];
     mk.etafm = ctx->mk[HMEC_M_etafm];
     Crd c{ctx->crd[0], ctx->crd[1], ctx->crd[2], ctx->crd[3], ctx->crd[4], ctx->crd[5], ctx->crd[6], ctx->crd[7]};
-    HMEC_LAUNCH(ctx, k_mprop, nblocks(n, 256), 256, 0, mk, ctx->perm, n, g, c, ctx->p, ctx->mprop);
+    HMEC_LAUNCH(ctx, k_mprop, nblocks(n, 256), 256, 0, mk, ctx->perm, ctx->mkey, n, g, c, ctx->p, ctx->mprop);
     double* const* f = ctx->f;
     dim3 bb(64), gb(nblocks(g.Ny, 64), g.Nx), gs(nblocks(g.Ny1, 64), g.Nx1);
     HMEC_LAUNCH(ctx, k_node_basic, gb, bb, 0, g, ctx->hc_start, ctx->mprop, n, f[HMEC_F_RHO], f[HMEC_F_KKK],

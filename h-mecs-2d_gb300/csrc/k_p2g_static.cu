@@ -3,8 +3,8 @@
 //
 // Some hosts may not call cudaMalloc at all: a solver embedded in another
 // application that owns the device allocator (and forbids allocations behind
-// its back), code that runs while a CUDA graph is being captured or replayed,
-// or a real-time loop that must never block on the allocator.  This file
+// its back), or a real-time loop that must never block on the allocator.
+// This file
 // gives them one entry point, hmec_markers_to_nodes_noalloc(), which computes
 // exactly what hmec_markers_to_nodes() computes (sections a1-a4 of
 // cpp/h_mec_rsf_v9.cpp:376-583: the half-cell counting sort and the

@@ -264,8 +264,8 @@ int32_t hmec_profile_kernel(hmec_ctx* ctx, const char* name);
 int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, double* bytes);
 /* Markers -> nodes without allocating device memory.  No counterpart in the
  * reference: it serves hosts that may not call cudaMalloc (an application
- * that owns the device allocator, code running under CUDA-graph capture, a
- * real-time loop that must not block on the allocator).  Computes the same
+ * that owns the device allocator, a real-time loop that must not block on
+ * the allocator).  Computes the same
  * 23 node fields as hmec_markers_to_nodes() from arrays the caller already
  * holds on the current device: markers[k] is the device array of marker
  * field k (enum hmec_marker_field), fields[f] the column-major device array
