@@ -167,6 +167,7 @@ struct hmec_ctx {
     int32_t* hc_fill;        // scatter cursors
     int32_t* scan_part;      // scan block partials
     double* mprop;           // 17 sorted per-marker properties [17][marknum]
+    double* cellsum;         // per-cell corner sums of the four grids (k_cell_sums)
     int nhalf;               // number of half-cells
     // global system
     double* R;               // unscaled right-hand side

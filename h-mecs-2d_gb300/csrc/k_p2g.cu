@@ -17,9 +17,10 @@
 //     marker-index order, so the permutation is deterministic.
 //  3. per-marker properties (a1) and interpolation distances are computed
 //     once, in sorted order, into structure-of-arrays buffers.
-//  4. one thread per node walks the (at most four) contiguous sorted runs of
-//     the half cells that touch it, accumulates weight * property in fixed
-//     order, and normalises in the epilogue (a4).  No float atomics.
+//  4. one thread per cell of each grid sums weight and weight * property per
+//     corner node over the cell's markers (two contiguous sorted runs); one
+//     thread per node adds its four cells' corner sums in a fixed order and
+//     normalises in the epilogue (a4).  No float atomics.
 #include "hmec_internal.cuh"
 
 namespace {
@@ -250,58 +251,93 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
     out[MP_RHOF * S + k] = mk.rhofm[m];
 }
 
-// Which half cells touch node (i, j) of a grid: rows [r0, r0+3], cols
-// [c0, c0+3]; "row offset" tells whether the grid's cell row of a half row
-// hr is hr>>1 (basic-type rows) or (hr+1)>>1 (pressure-type rows).
-template <int NACC>
-struct Acc {
-    double s[NACC];
+// Gathers in two passes.  Every marker of one grid's cell (ci, cj) (cells
+// indexed by their top-left node; all four grids have (Ny-1) x (Nx-1) cells
+// after the reference's clamping) adds to the cell's four corner nodes with
+// the bilinear weights (1-dx)(1-dy) to (ci, cj), (1-dx) dy to (ci+1, cj),
+// dx (1-dy) to (ci, cj+1), dx dy to (ci+1, cj+1) -- the products fx * fy of
+// :435-528.  Pass 1, one thread per cell, sums weight and weight * property
+// per corner over the cell's markers (its half cells are two contiguous runs
+// of the sorted order, markers in sorted order); pass 2, one thread per
+// node, adds the corner sums of its four cells in a fixed order.  Each
+// marker is read once per grid, not once per node.
+//
+// ROWP / COLP: the grid's cell rows / columns follow the pressure cell.
+// Corner sums: cs[(s * 4 + corner) * ncell + cj * (Ny-1) + ci], s = 0 the
+// weight, s = 1..NP the properties.
+template <int NP>
+struct Props {
+    int p[NP];
 };
 
-// Generic gather: ROWP = rows follow the pressure cell, COLP = columns follow
-// the pressure cell.  DXI/DYI pick the distance rows, PROPS the properties.
 template <bool ROWP, bool COLP, int NP>
-__device__ __forceinline__ void gather_node(int i, int j, const Geo& g, const int32_t* __restrict__ start,
-                                            const double* __restrict__ mp, int64_t n, int dxrow, int dyrow,
-                                            const int (&props)[NP], double& wt, double (&acc)[NP]) {
+__global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const double* __restrict__ mp, int64_t n,
+                            int dxrow, int dyrow, Props<NP> props, double* __restrict__ cs) {
+    const int NCI = g.Ny - 1, NCJ = g.Nx - 1;
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x, cj = blockIdx.y;
+    if (ci >= NCI) return;
     const int HR = 2 * (g.Ny - 1), HC = 2 * (g.Nx - 1);
-    const int r0 = ROWP ? 2 * i - 3 : 2 * i - 2;
-    const int c0 = COLP ? 2 * j - 3 : 2 * j - 2;
-    const int rlo = r0 < 0 ? 0 : r0;
-    const int rhi = (r0 + 3) > HR - 1 ? HR - 1 : r0 + 3;
+    const int r0 = ROWP ? 2 * ci - 1 : 2 * ci, c0 = COLP ? 2 * cj - 1 : 2 * cj;
+    const int rlo = r0 < 0 ? 0 : r0, rhi = r0 + 1 > HR - 1 ? HR - 1 : r0 + 1;
+    double W[4] = {0, 0, 0, 0}, S[NP][4];
+#pragma unroll
+    for (int q = 0; q < NP; q++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) S[q][c] = 0;
+    const size_t Sn = (size_t)n;
+    for (int hc = c0 < 0 ? 0 : c0; hc <= c0 + 1 && hc < HC; hc++) {
+        const int b = start[hc * HR + rlo], e = start[hc * HR + rhi + 1];
+        for (int k = b; k < e; k++) {
+            const double dx = mp[dxrow * Sn + k], dy = mp[dyrow * Sn + k];
+            const double w[4] = {(1 - dx) * (1 - dy), (1 - dx) * dy, dx * (1 - dy), dx * dy};
+#pragma unroll
+            for (int c = 0; c < 4; c++) W[c] += w[c];
+#pragma unroll
+            for (int q = 0; q < NP; q++) {
+                const double pq = mp[props.p[q] * Sn + k];
+#pragma unroll
+                for (int c = 0; c < 4; c++) S[q][c] += pq * w[c];
+            }
+        }
+    }
+    const size_t ncell = (size_t)NCI * NCJ, cell = (size_t)cj * NCI + ci;
+#pragma unroll
+    for (int c = 0; c < 4; c++) cs[(size_t)c * ncell + cell] = W[c];
+#pragma unroll
+    for (int q = 0; q < NP; q++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) cs[((size_t)(1 + q) * 4 + c) * ncell + cell] = S[q][c];
+}
+
+// Node (i, j): cells (i-1, j-1), (i, j-1), (i-1, j), (i, j), of which it is
+// corner 3, 2, 1, 0, in that order.
+template <int NP>
+__device__ __forceinline__ void node_sums(int i, int j, const Geo& g, const double* __restrict__ cs, double& wt,
+                                          double (&acc)[NP]) {
+    const int NCI = g.Ny - 1, NCJ = g.Nx - 1;
+    const size_t ncell = (size_t)NCI * NCJ;
     wt = 0;
 #pragma unroll
     for (int q = 0; q < NP; q++) acc[q] = 0;
-    if (rlo > rhi) return;
-    const size_t S = (size_t)n;
-    for (int hc = (c0 < 0 ? 0 : c0); hc <= c0 + 3 && hc < HC; hc++) {
-        const int cj = COLP ? (hc + 1) >> 1 : hc >> 1;  // grid column of this half column
-        const int b = start[hc * HR + rlo], e = start[hc * HR + rhi + 1];
-        // half-row boundary where the grid cell row changes from i-1 to i
-        const int split_hr = ROWP ? 2 * i - 1 : 2 * i;
-        const int bsplit = (split_hr <= rlo) ? b : (split_hr > rhi ? e : start[hc * HR + split_hr]);
-        for (int k = b; k < e; k++) {
-            const double dxm = mp[dxrow * S + k];
-            const double dym = mp[dyrow * S + k];
-            const double fx = (cj == j) ? (1 - dxm) : dxm;
-            const double fy = (k >= bsplit) ? (1 - dym) : dym;  // cell row == i -> top corner
-            const double w = fx * fy;
-            wt += w;
 #pragma unroll
-            for (int q = 0; q < NP; q++) acc[q] += mp[props[q] * S + k] * w;
-        }
+    for (int t = 0; t < 4; t++) {
+        const int ci = i - 1 + (t & 1), cj = j - 1 + (t >> 1), corner = 3 - t;
+        if (ci < 0 || ci >= NCI || cj < 0 || cj >= NCJ) continue;
+        const size_t cell = (size_t)cj * NCI + ci;
+        wt += cs[(size_t)corner * ncell + cell];
+#pragma unroll
+        for (int q = 0; q < NP; q++) acc[q] += cs[((size_t)(1 + q) * 4 + corner) * ncell + cell];
     }
 }
 
-__global__ void k_node_basic(Geo g, const int32_t* __restrict__ start, const double* __restrict__ mp, int64_t n,
-                             double* RHO, double* KKK, double* TTT, double* GGG, double* ETA0, double* COHT,
-                             double* FRIT, double* COHC, double* FRIC, double* DILC) {
+__global__ void k_node_basic(Geo g, const double* __restrict__ cs, double* RHO, double* KKK, double* TTT,
+                             double* GGG, double* ETA0, double* COHT, double* FRIT, double* COHC, double* FRIC,
+                             double* DILC) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i >= g.Ny) return;
-    const int props[10] = {MP_RHO, MP_KKK, MP_TTT, MP_INVG, MP_ETA0, MP_COHT, MP_FRIT, MP_COHC, MP_FRIC, MP_DILC};
     double wt, a[10];
-    gather_node<false, false, 10>(i, j, g, start, mp, n, MP_DXB, MP_DYB, props, wt, a);
+    node_sums<10>(i, j, g, cs, wt, a);
     if (wt > 0) {
         size_t o = (size_t)j * g.Ny + i;
         RHO[o] = a[0] / wt;
@@ -317,14 +353,13 @@ __global__ void k_node_basic(Geo g, const int32_t* __restrict__ start, const dou
     }
 }
 
-__global__ void k_node_p(Geo g, const int32_t* __restrict__ start, const double* __restrict__ mp, int64_t n,
-                         double* ETAP, double* POR, double* ETAB0, double* ETAP0, double* GGGP) {
+__global__ void k_node_p(Geo g, const double* __restrict__ cs, double* ETAP, double* POR, double* ETAB0,
+                         double* ETAP0, double* GGGP) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i >= g.Ny1) return;
-    const int props[5] = {MP_ETAP, MP_POR, MP_ETAB0, MP_ETA0, MP_INVG};
     double wt, a[5];
-    gather_node<true, true, 5>(i, j, g, start, mp, n, MP_DXP, MP_DYP, props, wt, a);
+    node_sums<5>(i, j, g, cs, wt, a);
     if (wt > 0) {
         size_t o = (size_t)j * g.Ny1 + i;
         ETAP[o] = a[0] / wt;
@@ -337,14 +372,13 @@ __global__ void k_node_p(Geo g, const int32_t* __restrict__ start, const double*
 }
 
 // Vx nodes: rows follow the pressure cell, columns the basic cell.
-__global__ void k_node_vx(Geo g, const int32_t* __restrict__ start, const double* __restrict__ mp, int64_t n,
-                          double* RHOX, double* ETADX, double* RHOFX, double* PORX) {
+__global__ void k_node_vx(Geo g, const double* __restrict__ cs, double* RHOX, double* ETADX, double* RHOFX,
+                          double* PORX) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i >= g.Ny1 || j >= g.Nx) return;
-    const int props[4] = {MP_RHO, MP_INVETAD, MP_RHOF, MP_POR};
     double wt, a[4];
-    gather_node<true, false, 4>(i, j, g, start, mp, n, MP_DXX, MP_DYP, props, wt, a);
+    node_sums<4>(i, j, g, cs, wt, a);
     if (wt > 0) {
         size_t o = (size_t)j * g.Ny1 + i;
         RHOX[o] = a[0] / wt;
@@ -355,14 +389,13 @@ __global__ void k_node_vx(Geo g, const int32_t* __restrict__ start, const double
 }
 
 // Vy nodes: rows follow the basic cell, columns the pressure cell.
-__global__ void k_node_vy(Geo g, const int32_t* __restrict__ start, const double* __restrict__ mp, int64_t n,
-                          double* RHOY, double* ETADY, double* RHOFY, double* PORY) {
+__global__ void k_node_vy(Geo g, const double* __restrict__ cs, double* RHOY, double* ETADY, double* RHOFY,
+                          double* PORY) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i >= g.Ny) return;
-    const int props[4] = {MP_RHO, MP_INVETAD, MP_RHOF, MP_POR};
     double wt, a[4];
-    gather_node<false, true, 4>(i, j, g, start, mp, n, MP_DXP, MP_DYY, props, wt, a);
+    node_sums<4>(i, j, g, cs, wt, a);
     if (wt > 0) {
         size_t o = (size_t)j * g.Ny1 + i;
         RHOY[o] = a[0] / wt;
@@ -386,6 +419,9 @@ int p2g_alloc(hmec_ctx* ctx) {
     HMEC_CUDA(ctx, cudaMalloc(&ctx->hc_fill, sizeof(int32_t) * ((size_t)ctx->nhalf + 1)));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->scan_part, sizeof(int32_t) * ((size_t)nparts + 1)));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->mprop, sizeof(double) * (size_t)NPROP * (size_t)n));
+    // corner sums: (10 + 5 + 4 + 4 properties + 4 weights) x 4 corners per cell
+    const size_t ncell = (size_t)(g.Ny - 1) * (g.Nx - 1);
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->cellsum, sizeof(double) * 27 * 4 * ncell));
     return HMEC_OK;
 }
 
@@ -397,6 +433,7 @@ void p2g_free(hmec_ctx* ctx) {
     cudaFree(ctx->hc_fill);
     cudaFree(ctx->scan_part);
     cudaFree(ctx->mprop);
+    cudaFree(ctx->cellsum);
 }
 
 int p2g_run(hmec_ctx* ctx) {
@@ -437,16 +474,31 @@ int p2g_run(hmec_ctx* ctx) {
     Crd c{ctx->crd[0], ctx->crd[1], ctx->crd[2], ctx->crd[3], ctx->crd[4], ctx->crd[5], ctx->crd[6], ctx->crd[7]};
     HMEC_LAUNCH(ctx, k_mprop, nblocks(n, 256), 256, 0, mk, ctx->perm, ctx->mkey, n, g, c, ctx->p, ctx->mprop);
     double* const* f = ctx->f;
-    dim3 bb(64), gb(nblocks(g.Ny, 64), g.Nx), gs(nblocks(g.Ny1, 64), g.Nx1);
-    HMEC_LAUNCH(ctx, k_node_basic, gb, bb, 0, g, ctx->hc_start, ctx->mprop, n, f[HMEC_F_RHO], f[HMEC_F_KKK],
-                f[HMEC_F_TTT], f[HMEC_F_GGG], f[HMEC_F_ETA0], f[HMEC_F_COHT], f[HMEC_F_FRIT], f[HMEC_F_COHC],
-                f[HMEC_F_FRIC], f[HMEC_F_DILC]);
-    HMEC_LAUNCH(ctx, k_node_p, gs, bb, 0, g, ctx->hc_start, ctx->mprop, n, f[HMEC_F_ETAP], f[HMEC_F_POR],
-                f[HMEC_F_ETAB0], f[HMEC_F_ETAP0], f[HMEC_F_GGGP]);
-    HMEC_LAUNCH(ctx, k_node_vx, gs, bb, 0, g, ctx->hc_start, ctx->mprop, n, f[HMEC_F_RHOX], f[HMEC_F_ETADX],
-                f[HMEC_F_RHOFX], f[HMEC_F_PORX]);
-    HMEC_LAUNCH(ctx, k_node_vy, gs, bb, 0, g, ctx->hc_start, ctx->mprop, n, f[HMEC_F_RHOY], f[HMEC_F_ETADY],
-                f[HMEC_F_RHOFY], f[HMEC_F_PORY]);
+    // pass 1: corner sums per cell of each grid; pass 2: node sums and the a4 epilogues
+    const size_t ncell = (size_t)(g.Ny - 1) * (g.Nx - 1);
+    double* cs_b = ctx->cellsum;
+    double* cs_p = cs_b + 11 * 4 * ncell;
+    double* cs_x = cs_p + 6 * 4 * ncell;
+    double* cs_y = cs_x + 5 * 4 * ncell;
+    const Props<10> pb{{MP_RHO, MP_KKK, MP_TTT, MP_INVG, MP_ETA0, MP_COHT, MP_FRIT, MP_COHC, MP_FRIC, MP_DILC}};
+    const Props<5> pp{{MP_ETAP, MP_POR, MP_ETAB0, MP_ETA0, MP_INVG}};
+    const Props<4> pv{{MP_RHO, MP_INVETAD, MP_RHOF, MP_POR}};
+    dim3 bb(64), gc(nblocks(g.Ny - 1, 64), g.Nx - 1);
+    HMEC_LAUNCH(ctx, (k_cell_sums<false, false, 10>), gc, bb, 0, g, ctx->hc_start, ctx->mprop, n, MP_DXB, MP_DYB, pb,
+                cs_b);
+    HMEC_LAUNCH(ctx, (k_cell_sums<true, true, 5>), gc, bb, 0, g, ctx->hc_start, ctx->mprop, n, MP_DXP, MP_DYP, pp,
+                cs_p);
+    HMEC_LAUNCH(ctx, (k_cell_sums<true, false, 4>), gc, bb, 0, g, ctx->hc_start, ctx->mprop, n, MP_DXX, MP_DYP, pv,
+                cs_x);
+    HMEC_LAUNCH(ctx, (k_cell_sums<false, true, 4>), gc, bb, 0, g, ctx->hc_start, ctx->mprop, n, MP_DXP, MP_DYY, pv,
+                cs_y);
+    dim3 gb(nblocks(g.Ny, 64), g.Nx), gs(nblocks(g.Ny1, 64), g.Nx1);
+    HMEC_LAUNCH(ctx, k_node_basic, gb, bb, 0, g, cs_b, f[HMEC_F_RHO], f[HMEC_F_KKK], f[HMEC_F_TTT], f[HMEC_F_GGG],
+                f[HMEC_F_ETA0], f[HMEC_F_COHT], f[HMEC_F_FRIT], f[HMEC_F_COHC], f[HMEC_F_FRIC], f[HMEC_F_DILC]);
+    HMEC_LAUNCH(ctx, k_node_p, gs, bb, 0, g, cs_p, f[HMEC_F_ETAP], f[HMEC_F_POR], f[HMEC_F_ETAB0], f[HMEC_F_ETAP0],
+                f[HMEC_F_GGGP]);
+    HMEC_LAUNCH(ctx, k_node_vx, gs, bb, 0, g, cs_x, f[HMEC_F_RHOX], f[HMEC_F_ETADX], f[HMEC_F_RHOFX], f[HMEC_F_PORX]);
+    HMEC_LAUNCH(ctx, k_node_vy, gs, bb, 0, g, cs_y, f[HMEC_F_RHOY], f[HMEC_F_ETADY], f[HMEC_F_RHOFY], f[HMEC_F_PORY]);
     HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;
 }
