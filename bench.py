@@ -106,6 +106,40 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# ------------------------------------------------------------- several ranks
+# One process per GPU.  A single model does not shard (replicas only); the
+# members of an ensemble shard by rank with no collective on the data path.
+# The only collectives are the barriers and the max over ranks of the timed
+# interval.
+def rank_max(x, world):
+    """Max of x over all ranks (NCCL tensors on the GPU, CPU tensors on gloo)."""
+    if world == 1:
+        return x
+    import torch
+
+    dev = "cuda" if torch.distributed.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def rank_barrier(world):
+    if world > 1:
+        import torch
+
+        torch.distributed.barrier()
+
+
+def shard(items, rank, world):
+    """This rank's share of independent work items (round robin)."""
+    return list(items)[rank::world]
+
+
+def whole_job_rate(units_per_rank, world, seconds_max):
+    """Units all ranks processed per second of the slowest rank."""
+    return units_per_rank * world / seconds_max
+
+
 # -------------------------------------------------------------------- GPU arm
 def make_model(form, cfg, device_index):
     import hmec
@@ -164,15 +198,10 @@ def run_gpu(args, rank, world, device_index):
         flush_buf.fill_(1.0)
 
     def barrier():
-        if world > 1:
-            torch.distributed.barrier()
+        rank_barrier(world)
 
     def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return rank_max(x, world)
 
     out = {}
     # ---- mixed form (value), with the live roofline of the dominant kernel
@@ -287,48 +316,56 @@ def cpu_sample(cfg, budget_s=30.0, max_steps=2):
     return dict(value=steps / el, steps=steps, seconds=el, global_iters=gi)
 
 
-def run_ensemble(args, nmembers=64):
+def run_ensemble(args, rank=0, world=1, device_index=0, nmembers=64):
     """Configuration 3: 64 uneven members advanced concurrently (mixed form)
     against the same members run one after another in the plain FP64 form.
     Many streams are in flight, so this mode times with a device-wide
-    synchronize on both sides of the timed region."""
+    synchronize on both sides of the timed region.  Under torchrun the
+    members shard by rank (64 per rank, weak scaling)."""
     import torch
 
     import hmec
     from hmec import synth
     from hmec.ensemble import Ensemble
 
-    torch.cuda.set_device(0)
-    members = synth.ensemble_members(nmembers)
+    torch.cuda.set_device(device_index)
+    # every rank advances 64 distinct members: rank r takes members r, r+world, ... of 64*world
+    members = shard(synth.ensemble_members(nmembers * world), rank, world)
     common = dict(krylov_rtol=1e-15, krylov_restart=40, krylov_maxit=4000)
     out = {}
     for form, label in ((hmec.FORM_MIXED, "mixed"), (hmec.FORM_FP64, "fp64")):
         ens = Ensemble(members, form=form, **common)
         (ens.step if form == hmec.FORM_MIXED else ens.step_sequential)(args.warmup)
         torch.cuda.synchronize()
+        rank_barrier(world)
         l0 = sum(m.launches for m in ens.models)
         t0 = time.perf_counter()
         reps = (ens.step if form == hmec.FORM_MIXED else ens.step_sequential)(args.steps)
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
-        out[label] = dict(s=el, launches=sum(m.launches for m in ens.models) - l0,
+        rank_barrier(world)
+        out[label] = dict(s=rank_max(el, world), launches=sum(m.launches for m in ens.models) - l0,
                           bad=sum(1 for rs in reps for r in rs if r["rc"] != 0),
                           gi=sum(r["global_iters"] for rs in reps for r in rs))
         ens.close()
+    if rank != 0:
+        return 0
     K = args.steps
     mx, fp = out["mixed"], out["fp64"]
-    value = nmembers * K / mx["s"]
+    value = whole_job_rate(len(members) * K, world, mx["s"])
     line = {
-        "metric": METRIC, "value": value, "unit": "member-timesteps/s", "n_gpus": 1, "steps": K,
+        "metric": METRIC, "value": value, "unit": "member-timesteps/s", "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": 1e3 * mx["s"] / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic",
-        "config": {"workload": "config 3: %d members, per-side nodes 51-301, 4x4 markers/cell, seeded a/b/L/k" % nmembers,
+        "config": {"workload": "config 3: %d members per GPU, per-side nodes 51-301, 4x4 markers/cell, "
+                               "seeded a/b/L/k" % len(members),
                    "form": "mixed, members concurrent (one context and stream each)",
                    "timing": "device-wide synchronize around the timed region (many streams)",
+                   "parallelism": "members sharded by rank" if world > 1 else "single",
                    "failed_member_steps": mx["bad"]},
         "gpu_launches": mx["launches"],
-        "fp64_sequential": {"value": nmembers * K / fp["s"], "ms_per_step": 1e3 * fp["s"] / K,
-                            "failed_member_steps": fp["bad"]},
+        "fp64_sequential": {"value": whole_job_rate(len(members) * K, world, fp["s"]),
+                            "ms_per_step": 1e3 * fp["s"] / K, "failed_member_steps": fp["bad"]},
         "speedup_batched_mixed_vs_sequential_fp64": fp["s"] / mx["s"],
     }
     print(json.dumps(line))
@@ -341,7 +378,15 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.config == "c3" and args.impl == "ours":
-        return run_ensemble(args) if rank == 0 else 0
+        import torch
+
+        if world > 1:
+            torch.cuda.set_device(local)
+            torch.distributed.init_process_group("nccl")
+        rc = run_ensemble(args, rank, world, local if world > 1 else 0)
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return rc
 
     if args.impl == "reference":
         if rank != 0:
@@ -375,7 +420,7 @@ def main():
         return 0
     mx = out["mixed"]
     K = args.steps
-    value = world * K / (mx["ms"] / 1e3)
+    value = whole_job_rate(K, world, mx["ms"] / 1e3)
     nprof, prof_ms, prof_bytes = mx["prof"]
     achieved = (prof_bytes / nprof) / (prof_ms / nprof / 1e3) / 1e9 if nprof and prof_ms > 0 else None
     peak = peaks.get("hbm_gbs")
