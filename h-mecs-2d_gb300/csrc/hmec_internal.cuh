@@ -49,6 +49,7 @@ struct Geo {
 struct DevScalars {
     double timesum, dt, dt00, dtx, dty, dtlapusta, Vmax, maxvxy, maxvxy0;
     double ptscale, pfscale;
+    double guess_ratio;  // previous pressure scale / current one, applied to the warm start
     double dsylsq, dsylsq_prev;
     double maxvxsmod, minvxsmod, maxvysmod, minvysmod;
     double krylov_relres, krylov_maxrel;

@@ -151,8 +151,25 @@ __global__ void k_scales(Geo g, DevScalars* ds, const double* part, int nb) {
     for (int b = 0; b < nb; b++) mn = DMIN(mn, part[b]);
     const double dt = ds->dt;
     double pf = (dt > 2e5) ? mn * g.dx * 1e17 / (dt * dt) : mn * g.dx;
+    // The solution vector S holds pt/ptscale and pf/pfscale of the previous
+    // solve; the ratio brings that warm start to the new scales.
+    const double old = ds->ptscale;
+    ds->guess_ratio = (old > 0.0 && isfinite(old) && isfinite(pf) && pf > 0.0) ? old / pf : 1.0;
     ds->pfscale = pf;
     ds->ptscale = pf;
+}
+
+// Warm start of the next solve in the new pressure scales (the Krylov
+// solver's initial guess only; the converged solution does not depend on it).
+__global__ void k_rescale_guess(Geo g, const DevScalars* ds, double* S) {
+    const double r = ds->guess_ratio;
+    if (r == 1.0) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= g.Ny1) return;
+    const int kp = (j * g.Ny1 + i) * 6;
+    S[kp] *= r;
+    S[kp + 3] *= r;
 }
 
 // ------------------------------------------------------------- a9 assembly
@@ -957,6 +974,7 @@ int iter_prepare(hmec_ctx* ctx) {
     const int nb = 152;
     HMEC_LAUNCH(ctx, k_min_etadx, nb, 256, 0, g, f[HMEC_F_ETADX], ctx->red);
     HMEC_LAUNCH(ctx, k_scales, 1, 1, 0, g, ctx->ds, ctx->red, nb);
+    HMEC_LAUNCH(ctx, k_rescale_guess, grid_s(g), 64, 0, g, ctx->ds, ctx->S);
     HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;
 }
