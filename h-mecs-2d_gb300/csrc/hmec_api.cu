@@ -208,6 +208,7 @@ void hmec_destroy(hmec_ctx* ctx) {
     cudaFree(ctx->R);
     cudaFree(ctx->S);
     cudaFree(ctx->red);
+    cudaFree(ctx->ticket);
     cudaFree(ctx->ds);
     cudaFreeHost(ctx->hs);
     cudaStreamDestroy(ctx->stream);
@@ -237,6 +238,7 @@ static int create_inner(hmec_ctx* ctx) {
     g.lower_block = p.ysize / 2. + g.dy;  // constants.hpp:76-77
     g.upper_block = p.ysize / 2. - g.dy;
     g.dy_faultw = g.dy / g.dx;            // faultwidth = dx (:66, :175)
+    geo_reciprocals(g);
     ctx->marknum = hmec_marknum(&p);
     // coordinates, constants.hpp:57-64
     std::vector<double> c[8];
@@ -267,6 +269,8 @@ static int create_inner(hmec_ctx* ctx) {
     HMEC_CUDA(ctx, cudaMalloc(&ctx->S, sizeof(double) * (size_t)g.N));
     HMEC_CUDA(ctx, cudaMemset(ctx->S, 0, sizeof(double) * (size_t)g.N));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->red, sizeof(double) * (4096 + 3 * (size_t)g.Nx + 64)));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->ticket, sizeof(unsigned) * 8));
+    HMEC_CUDA(ctx, cudaMemset(ctx->ticket, 0, sizeof(unsigned) * 8));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->ds, sizeof(DevScalars)));
     HMEC_CUDA(ctx, cudaMallocHost(&ctx->hs, sizeof(DevScalars)));
     DevScalars s;

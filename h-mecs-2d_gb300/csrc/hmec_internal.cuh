@@ -43,7 +43,22 @@ struct XferEnt {
 struct Geo {
     int Nx, Ny, Nx1, Ny1, N, line_fault;
     double dx, dy, dx2, dy2, dx_dy, lower_block, upper_block, dy_faultw;
+    // 1/dx, 1/dy, 1/dx^2, 1/dy^2, 1/(dx dy), 1/(2 dx), 1/(2 dy): the kernels
+    // multiply where the reference divides by these grid constants (FP64
+    // division costs ~8 FMAs); results move by at most an ulp or two
+    double idx, idy, idx2, idy2, idx_dy, i2dx, i2dy;
 };
+
+// Fills the reciprocal grid constants of g (after dx, dy, dx2, dy2, dx_dy).
+inline void geo_reciprocals(Geo& g) {
+    g.idx = 1.0 / g.dx;
+    g.idy = 1.0 / g.dy;
+    g.idx2 = 1.0 / g.dx2;
+    g.idy2 = 1.0 / g.dy2;
+    g.idx_dy = 1.0 / g.dx_dy;
+    g.i2dx = 1.0 / (2. * g.dx);
+    g.i2dy = 1.0 / (2. * g.dy);
+}
 
 // Control scalars of one model instance (device resident).
 struct DevScalars {
@@ -174,6 +189,7 @@ struct hmec_ctx {
     double* R;               // unscaled right-hand side
     double* S;               // solution (kept as the next initial guess)
     double* red;             // reduction partials
+    unsigned* ticket;        // arrival counters of the one-launch reductions (zero between launches)
     DevScalars* ds;          // device scalars
     DevScalars* hs;          // pinned host mirror
     Solver sv;
@@ -193,7 +209,54 @@ __host__ __device__ __forceinline__ int check_bounds(int k, int bound) {
 }
 __host__ __device__ __forceinline__ double divplus(double x, double y) { return x / (x + y); }
 
+// fix(fl(x / d)) or fix(fl(fl(x + d/2) / d)) -- the reference's cell index of
+// a marker coordinate, IEEE operations -- decided in FP32 wherever that is
+// provably the same answer (FP64 arithmetic is the scarce resource here).
+// x is truncated to a 24-bit mantissa through its bit pattern (relative
+// error < 2^-23), rdf = 1/d in FP32 (< 2^-23), so q = x * rdf (+ 0.5) is
+// within 3e-7 (|q| + 0.5) of the exact quotient.  If q is farther than
+// 6e-7 (|q| + 1) from every integer, the FP64 quotient cannot round across
+// one and trunc(q) is the index; otherwise (and for x outside the FP32
+// range) the FP64 operations decide.
+__device__ __forceinline__ int fix_quot(double x, double d, float rdf, bool half) {
+    const int hi = __double2hiint(x);
+    const unsigned lo = (unsigned)__double2loint(x);
+    const int e = ((hi >> 20) & 0x7FF) - 896;  // biased FP32 exponent
+    if (e > 0 && e < 255) {
+        const float xf =
+            __int_as_float((hi & (int)0x80000000) | (e << 23) | ((hi & 0xFFFFF) << 3) | (int)(lo >> 29));
+        const float q = fmaf(xf, rdf, half ? 0.5f : 0.0f);
+        const float aq = fabsf(q);
+        if (aq < 8.0e6f) {
+            const float t = truncf(q);
+            const float fr = fabsf(q - t);
+            const float m = 6.0e-7f * (aq + 1.0f);
+            if (fr > m && fr < 1.0f - m) return (int)t;
+        }
+    }
+    const double xx = half ? __dadd_rn(x, d / 2.) : x;
+    return fix_trunc(__ddiv_rn(xx, d));
+}
+__device__ __forceinline__ float rcp_f32(double d) { return __frcp_rn(__double2float_rn(d)); }
+
 static inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+// One-launch two-level reduction: every block stores its partial (thread 0),
+// then calls this; the last block to arrive gets true, sees every partial
+// (read them with __ldcg) and has already reset the counter for the next
+// launch.  Min / max / counts are order-independent, so the result equals a
+// second kernel's.
+__device__ __forceinline__ bool arrive_last(unsigned* ticket) {
+    __shared__ unsigned s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1) ? 1u : 0u;
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    if (threadIdx.x == 0) *ticket = 0;
+    return true;
+}
 
 // Launch bookkeeping: every kernel launch of the library goes through this.
 #define HMEC_LAUNCH(ctx, kern, grid, block, smem, ...)                          \

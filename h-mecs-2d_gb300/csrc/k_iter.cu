@@ -128,27 +128,42 @@ __global__ void k_prep_p(Geo g, const DevScalars* ds, hmec_params p, const doubl
 }
 
 // :671-677 -- min(ETADX(1:Ny-1, 0:Nx-1)) in block partials, finished below.
-__global__ void k_min_etadx(Geo g, const double* __restrict__ ETADX, double* part) {
-    __shared__ double sh[256];
-    double mn = INFINITY;
-    const int nrow = g.Ny - 1;
-    const long long tot = (long long)nrow * g.Nx;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
-        int i = 1 + (int)(t % nrow), j = (int)(t / nrow);
-        mn = DMIN(mn, IS(ETADX, i, j));
-    }
-    sh[threadIdx.x] = mn;
+__device__ __forceinline__ double block_min256(double* sh, double v) {
+    sh[threadIdx.x] = v;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s) sh[threadIdx.x] = DMIN(sh[threadIdx.x], sh[threadIdx.x + s]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+    const double r = sh[0];
+    __syncthreads();
+    return r;
 }
 
-__global__ void k_scales(Geo g, DevScalars* ds, const double* part, int nb) {
+__device__ void set_scales(const Geo& g, DevScalars* ds, double mn);
+
+// min(ETADX) over rows 1..Ny-1 in block partials; the last block sets the
+// pressure scales from it (block 256 threads).
+__global__ void k_min_etadx(Geo g, const double* __restrict__ ETADX, double* part, DevScalars* ds,
+                            unsigned* ticket) {
+    __shared__ double sh[256];
     double mn = INFINITY;
-    for (int b = 0; b < nb; b++) mn = DMIN(mn, part[b]);
+    const int nrow = g.Ny - 1;
+    const int tot = nrow * g.Nx;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += gridDim.x * blockDim.x) {
+        int j = t / nrow, i = 1 + (t - j * nrow);
+        mn = DMIN(mn, IS(ETADX, i, j));
+    }
+    mn = block_min256(sh, mn);
+    if (threadIdx.x == 0) part[blockIdx.x] = mn;
+    if (!arrive_last(ticket)) return;
+    mn = INFINITY;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) mn = DMIN(mn, __ldcg(part + b));
+    mn = block_min256(sh, mn);
+    if (threadIdx.x == 0) set_scales(g, ds, mn);
+}
+
+__device__ void set_scales(const Geo& g, DevScalars* ds, double mn) {
     const double dt = ds->dt;
     double pf = (dt > 2e5) ? mn * g.dx * 1e17 / (dt * dt) : mn * g.dx;
     // The solution vector S holds pt/ptscale and pf/pfscale of the previous
@@ -237,8 +252,13 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
     int j = blockIdx.y;
     if (i >= g.Ny1) return;
     const int Nx = g.Nx, Ny = g.Ny, Ny1 = g.Ny1, N = g.N;
-    const double dx = g.dx, dy = g.dy, dx2 = g.dx2, dy2 = g.dy2, dx_dy = g.dx_dy;
+    // the reference divides by the grid constants and dt; the matrix entries
+    // multiply by their reciprocals instead (an ulp or two apart, ~40 FP64
+    // divisions per cell saved), the right-hand sides, which can cancel
+    // strongly, keep the reference's divisions
+    const double idx = g.idx, idy = g.idy, idx2 = g.idx2, idy2 = g.idy2, idx_dy = g.idx_dy;
     const double dt = ds->dt, ptscale = ds->ptscale, pfscale = ds->pfscale;
+    const double idt = 1. / dt;
     const double gx = p.gx, gy = p.gy, inertia = p.inertia;
     const int NV = 6, RS = Ny1 * 6;
     const int kp = (j * Ny1 + i) * NV;
@@ -255,12 +275,13 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
         const double por = IS(F.POR, i, j);
         const double BETADRAINED = (1. / IS(F.GGGB, i, j) + p.BETASOLID) / (1 - por);
         const double KBW = 1 - p.BETASOLID / BETADRAINED;
-        rb.add(kx - RS, -1. / dx);
-        rb.add(kx, 1. / dx);
-        rb.add(ky - NV, -1. / dy);
-        rb.add(ky, 1. / dy);
-        rb.add(kp, ptscale * (1. / IS(F.ETAB, i, j) / (1 - por) + BETADRAINED / dt));
-        rb.add(kpf, -pfscale * (1. / IS(F.ETAB, i, j) / (1 - por) + BETADRAINED * KBW / dt));
+        const double ietab = 1. / IS(F.ETAB, i, j) / (1 - por);
+        rb.add(kx - RS, -idx);
+        rb.add(kx, idx);
+        rb.add(ky - NV, -idy);
+        rb.add(ky, idy);
+        rb.add(kp, ptscale * (ietab + BETADRAINED * idt));
+        rb.add(kpf, -pfscale * (ietab + BETADRAINED * KBW * idt));
         if (want_rhs) r = BETADRAINED * (IS(F.PT0, i, j) - KBW * IS(F.PF0, i, j)) / dt + IS(F.DILP, i, j);
     }
     emit_row(rb, kp, N, col, val, dscale, rhs_scaled, rhs_raw, r);
@@ -298,24 +319,24 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
         ETAXY2 *= KXY2;
         ETAXX1 *= KXX1;
         ETAXX2 *= KXX2;
-        const double dRHOdx = (IS(F.RHOX, i, j + 1) - IS(F.RHOX, i, j - 1)) / (2. * dx);
-        const double dRHOdy = (IB(F.RHO, i, j) - IB(F.RHO, i - 1, j)) / dy;
+        const double dRHOdx = (IS(F.RHOX, i, j + 1) - IS(F.RHOX, i, j - 1)) * g.i2dx;
+        const double dRHOdy = (IB(F.RHO, i, j) - IB(F.RHO, i - 1, j)) * idy;
         const double temp = gx * dt * dRHOdy / 4.;
-        rb.add(kx, -(ETAXX1 + ETAXX2) / dx2 - (ETAXY1 + ETAXY2) / dy2 - gx * dt * dRHOdx - inertia * IS(F.RHOX, i, j) / dt);
-        rb.add(kx - RS, ETAXX1 / dx2);
-        rb.add(kx + RS, ETAXX2 / dx2);
-        rb.add(kx - NV, ETAXY1 / dy2);
-        rb.add(kx + NV, ETAXY2 / dy2);
-        rb.add(ky - NV, (ETAXY1 - ETAXX1) / dx_dy - temp);
-        rb.add(ky, (ETAXX1 - ETAXY2) / dx_dy - temp);
-        rb.add(ky - NV + RS, (ETAXX2 - ETAXY1) / dx_dy - temp);
-        rb.add(ky + RS, (ETAXY2 - ETAXX2) / dx_dy - temp);
-        rb.add(kp, ptscale / dx);
-        rb.add(kp + RS, -ptscale / dx);
+        rb.add(kx, -(ETAXX1 + ETAXX2) * idx2 - (ETAXY1 + ETAXY2) * idy2 - gx * dt * dRHOdx - inertia * IS(F.RHOX, i, j) * idt);
+        rb.add(kx - RS, ETAXX1 * idx2);
+        rb.add(kx + RS, ETAXX2 * idx2);
+        rb.add(kx - NV, ETAXY1 * idy2);
+        rb.add(kx + NV, ETAXY2 * idy2);
+        rb.add(ky - NV, (ETAXY1 - ETAXX1) * idx_dy - temp);
+        rb.add(ky, (ETAXX1 - ETAXY2) * idx_dy - temp);
+        rb.add(ky - NV + RS, (ETAXX2 - ETAXY1) * idx_dy - temp);
+        rb.add(ky + RS, (ETAXY2 - ETAXX2) * idx_dy - temp);
+        rb.add(kp, ptscale * idx);
+        rb.add(kp + RS, -ptscale * idx);
         if (want_rhs) {
             const double SXY1 = IB(F.SXY0, i - 1, j) * (1 - KXY1), SXY2 = IB(F.SXY0, i, j) * (1 - KXY2);
             const double SXX1 = IS(F.SXX0, i, j) * (1 - KXX1), SXX2 = IS(F.SXX0, i, j + 1) * (1 - KXX2);
-            r = -IS(F.RHOX, i, j) * (inertia * IS(F.VX0, i, j) / dt + gx) - (SXX2 - SXX1) / dx - (SXY2 - SXY1) / dy;
+            r = -IS(F.RHOX, i, j) * (inertia * IS(F.VX0, i, j) / dt + gx) - (SXX2 - SXX1) / g.dx - (SXY2 - SXY1) / g.dy;
         }
     }
     emit_row(rb, kx, N, col, val, dscale, rhs_scaled, rhs_raw, r);
@@ -345,24 +366,24 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
         ETAXY2 *= KXY2;
         ETAYY1 *= KYY1;
         ETAYY2 *= KYY2;
-        const double dRHOdy = (IS(F.RHOY, i + 1, j) - IS(F.RHOY, i - 1, j)) / 2. / dy;
-        const double dRHOdx = (IB(F.RHO, i, j) - IB(F.RHO, i, j - 1)) / dx;
+        const double dRHOdy = (IS(F.RHOY, i + 1, j) - IS(F.RHOY, i - 1, j)) * g.i2dy;
+        const double dRHOdx = (IB(F.RHO, i, j) - IB(F.RHO, i, j - 1)) * idx;
         const double temp = gy * dt * dRHOdx / 4.;
-        rb.add(ky, -(ETAYY1 + ETAYY2) / dy2 - (ETAXY1 + ETAXY2) / dx2 - gy * dt * dRHOdy - inertia * IS(F.RHOY, i, j) / dt);
-        rb.add(ky - RS, ETAXY1 / dx2);
-        rb.add(ky + RS, ETAXY2 / dx2);
-        rb.add(ky - NV, ETAYY1 / dy2);
-        rb.add(ky + NV, ETAYY2 / dy2);
-        rb.add(kx - RS, (ETAXY1 - ETAYY1) / dx_dy - temp);
-        rb.add(kx + NV - RS, (ETAYY2 - ETAXY1) / dx_dy - temp);
-        rb.add(kx, (ETAYY1 - ETAXY2) / dx_dy - temp);
-        rb.add(kx + NV, (ETAXY2 - ETAYY2) / dx_dy - temp);
-        rb.add(kp, ptscale / dy);
-        rb.add(kp + NV, -ptscale / dy);
+        rb.add(ky, -(ETAYY1 + ETAYY2) * idy2 - (ETAXY1 + ETAXY2) * idx2 - gy * dt * dRHOdy - inertia * IS(F.RHOY, i, j) * idt);
+        rb.add(ky - RS, ETAXY1 * idx2);
+        rb.add(ky + RS, ETAXY2 * idx2);
+        rb.add(ky - NV, ETAYY1 * idy2);
+        rb.add(ky + NV, ETAYY2 * idy2);
+        rb.add(kx - RS, (ETAXY1 - ETAYY1) * idx_dy - temp);
+        rb.add(kx + NV - RS, (ETAYY2 - ETAXY1) * idx_dy - temp);
+        rb.add(kx, (ETAYY1 - ETAXY2) * idx_dy - temp);
+        rb.add(kx + NV, (ETAXY2 - ETAYY2) * idx_dy - temp);
+        rb.add(kp, ptscale * idy);
+        rb.add(kp + NV, -ptscale * idy);
         if (want_rhs) {
             const double SXY1 = IB(F.SXY0, i, j - 1) * (1 - KXY1), SXY2 = IB(F.SXY0, i, j) * (1 - KXY2);
             const double SYY1 = IS(F.SYY0, i, j) * (1 - KYY1), SYY2 = IS(F.SYY0, i + 1, j) * (1 - KYY2);
-            r = -IS(F.RHOY, i, j) * (inertia * IS(F.VY0, i, j) / dt + gy) - (SYY2 - SYY1) / dy - (SXY2 - SXY1) / dx;
+            r = -IS(F.RHOY, i, j) * (inertia * IS(F.VY0, i, j) / dt + gy) - (SYY2 - SYY1) / g.dy - (SXY2 - SXY1) / g.dx;
         }
     }
     emit_row(rb, ky, N, col, val, dscale, rhs_scaled, rhs_raw, r);
@@ -382,12 +403,13 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
         const double BETADRAINED = (1 / IS(F.GGGB, i, j) + p.BETASOLID) / (1 - por);
         const double KBW = 1 - p.BETASOLID / BETADRAINED;
         const double KSK = (BETADRAINED - p.BETASOLID) / (BETADRAINED - p.BETASOLID + por * (p.BETAFLUID - p.BETASOLID));
-        rb.add(kxf - RS, -1. / dx);
-        rb.add(kxf, 1. / dx);
-        rb.add(kyf - NV, -1. / dy);
-        rb.add(kyf, 1. / dy);
-        rb.add(kp, -ptscale * (1 / IS(F.ETAB, i, j) / (1 - por) + BETADRAINED * KBW / dt));
-        rb.add(kpf, pfscale * (1 / IS(F.ETAB, i, j) / (1 - por) + BETADRAINED * KBW / KSK / dt));
+        const double ietab = 1 / IS(F.ETAB, i, j) / (1 - por);
+        rb.add(kxf - RS, -idx);
+        rb.add(kxf, idx);
+        rb.add(kyf - NV, -idy);
+        rb.add(kyf, idy);
+        rb.add(kp, -ptscale * (ietab + BETADRAINED * KBW * idt));
+        rb.add(kpf, pfscale * (ietab + BETADRAINED * KBW / KSK * idt));
         if (want_rhs) r = -BETADRAINED * KBW * (IS(F.PT0, i, j) - 1. / KSK * IS(F.PF0, i, j)) / dt - IS(F.DILP, i, j);
     }
     emit_row(rb, kpf, N, col, val, dscale, rhs_scaled, rhs_raw, r);
@@ -407,10 +429,10 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
         if (j == 0) rb.add(kxf, 1);
         if (j == Nx - 1) rb.add(kxf, 1);
     } else {
-        rb.add(kxf, -IS(F.ETADX, i, j) - IS(F.RHOFX, i, j) / IS(F.PORX, i, j) * inertia / dt);
-        rb.add(kx, -IS(F.RHOFX, i, j) * inertia / dt);
-        rb.add(kpf, pfscale / dx);
-        rb.add(kpf + RS, -pfscale / dx);
+        rb.add(kxf, -IS(F.ETADX, i, j) - IS(F.RHOFX, i, j) / IS(F.PORX, i, j) * inertia * idt);
+        rb.add(kx, -IS(F.RHOFX, i, j) * inertia * idt);
+        rb.add(kpf, pfscale * idx);
+        rb.add(kpf + RS, -pfscale * idx);
         if (want_rhs) r = -IS(F.RHOFX, i, j) * (inertia * IS(F.VXF0, i, j) / dt + gx);
     }
     emit_row(rb, kxf, N, col, val, dscale, rhs_scaled, rhs_raw, r);
@@ -436,10 +458,10 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
             r = p.bcvyflower;
         }
     } else {
-        rb.add(kyf, -IS(F.ETADY, i, j) - IS(F.RHOFY, i, j) / IS(F.PORY, i, j) * inertia / dt);
-        rb.add(ky, -IS(F.RHOFY, i, j) * inertia / dt);
-        rb.add(kpf, pfscale / dy);
-        rb.add(kpf + NV, -pfscale / dy);
+        rb.add(kyf, -IS(F.ETADY, i, j) - IS(F.RHOFY, i, j) / IS(F.PORY, i, j) * inertia * idt);
+        rb.add(ky, -IS(F.RHOFY, i, j) * inertia * idt);
+        rb.add(kpf, pfscale * idy);
+        rb.add(kpf + NV, -pfscale * idy);
         if (want_rhs) r = -IS(F.RHOFY, i, j) * (inertia * IS(F.VYF0, i, j) / dt + gy);
     }
     emit_row(rb, kyf, N, col, val, dscale, rhs_scaled, rhs_raw, r);
@@ -465,18 +487,31 @@ __global__ void k_reload(Geo g, const DevScalars* ds, const double* __restrict__
     vyD[o] = s5;
 }
 
-__global__ void k_vmax(Geo g, const double* __restrict__ VSLIPB, DevScalars* ds) {
-    __shared__ double sh[1024];
-    double mx = -INFINITY;
-    const long long nb = (long long)g.Nx * g.Ny;
-    for (long long t = threadIdx.x; t < nb; t += blockDim.x) mx = DMAX(mx, VSLIPB[t]);
-    sh[threadIdx.x] = mx;
+__device__ __forceinline__ double block_max256(double* sh, double v) {
+    sh[threadIdx.x] = v;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s) sh[threadIdx.x] = DMAX(sh[threadIdx.x], sh[threadIdx.x + s]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) ds->Vmax = sh[0];
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// Vmax = max(VSLIPB) (:1077): block partials, the last block finishes (256 threads).
+__global__ void k_vmax(Geo g, const double* __restrict__ VSLIPB, DevScalars* ds, double* part, unsigned* ticket) {
+    __shared__ double sh[256];
+    double mx = -INFINITY;
+    const int nb = g.Nx * g.Ny;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nb; t += gridDim.x * blockDim.x) mx = DMAX(mx, VSLIPB[t]);
+    mx = block_max256(sh, mx);
+    if (threadIdx.x == 0) part[blockIdx.x] = mx;
+    if (!arrive_last(ticket)) return;
+    mx = -INFINITY;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) mx = DMAX(mx, __ldcg(part + b));
+    mx = block_max256(sh, mx);
+    if (threadIdx.x == 0) ds->Vmax = mx;
 }
 
 // ---------------------------------------------------------- a12 stress
@@ -636,14 +671,20 @@ __global__ void k_rsf(Geo g, const DevScalars* ds, hmec_params p, RsfIn in, RsfO
 // Block partials over the staggered grid: max/min of vxs, vys, the
 // fault-band maxima of |vxs|, |vys|, and min dx*stpmax/VSLIPB over the basic grid.
 constexpr int NRED = 7;
+__device__ void control_update(const Geo& g, DevScalars* ds, const hmec_params& p, const double* red, int ynpl,
+                               double ddd, double dtlapusta);
+
+// Velocity extrema and the slip-limited dt over the grid in block partials
+// (256 threads); the last block finishes them and runs the timestep control.
 __global__ void k_reduce_vel(Geo g, hmec_params p, const double* __restrict__ yvx, const double* __restrict__ yvy,
                              const double* __restrict__ vxs, const double* __restrict__ vys,
-                             const double* __restrict__ VSLIPB, double* part) {
+                             const double* __restrict__ VSLIPB, double* part, const double* __restrict__ rsfbuf,
+                             DevScalars* ds, unsigned* ticket) {
     __shared__ double sh[NRED][256];
     double a[NRED] = {-INFINITY, INFINITY, -INFINITY, INFINITY, 0.0, 0.0, 1e30};
-    const long long ns = (long long)g.Nx1 * g.Ny1;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < ns; t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % g.Ny1);
+    const int ns = g.Nx1 * g.Ny1;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ns; t += gridDim.x * blockDim.x) {
+        const int i = t - (t / g.Ny1) * g.Ny1;
         const double vx = vxs[t], vy = vys[t];
         a[0] = DMAX(a[0], vx);
         a[1] = DMIN(a[1], vx);
@@ -673,33 +714,80 @@ __global__ void k_reduce_vel(Geo g, hmec_params p, const double* __restrict__ yv
     }
     if (threadIdx.x == 0)
         for (int q = 0; q < NRED; q++) part[blockIdx.x * NRED + q] = sh[q][0];
+    if (!arrive_last(ticket)) return;
+    // last block: combine the partials, then the fault bookkeeping and the
+    // timestep control (one thread)
+    a[0] = -INFINITY, a[1] = INFINITY, a[2] = -INFINITY, a[3] = INFINITY, a[4] = 0.0, a[5] = 0.0, a[6] = 1e30;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        double v[NRED];
+        for (int q = 0; q < NRED; q++) v[q] = __ldcg(part + b * NRED + q);
+        a[0] = DMAX(a[0], v[0]);
+        a[1] = DMIN(a[1], v[1]);
+        a[2] = DMAX(a[2], v[2]);
+        a[3] = DMIN(a[3], v[3]);
+        a[4] = DMAX(a[4], v[4]);
+        a[5] = DMAX(a[5], v[5]);
+        a[6] = DMIN(a[6], v[6]);
+    }
+    int cnt = 0;
+    double dtl = 1e7;
+    for (int j = threadIdx.x; j < g.Nx; j += blockDim.x) {
+        if (rsfbuf[j] != 0) cnt++;
+        dtl = DMIN(dtl, rsfbuf[2 * g.Nx + j]);
+    }
+    __syncthreads();
+    for (int q = 0; q < NRED; q++) sh[q][threadIdx.x] = a[q];
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sh[0][threadIdx.x] = DMAX(sh[0][threadIdx.x], sh[0][threadIdx.x + s]);
+            sh[1][threadIdx.x] = DMIN(sh[1][threadIdx.x], sh[1][threadIdx.x + s]);
+            sh[2][threadIdx.x] = DMAX(sh[2][threadIdx.x], sh[2][threadIdx.x + s]);
+            sh[3][threadIdx.x] = DMIN(sh[3][threadIdx.x], sh[3][threadIdx.x + s]);
+            sh[4][threadIdx.x] = DMAX(sh[4][threadIdx.x], sh[4][threadIdx.x + s]);
+            sh[5][threadIdx.x] = DMAX(sh[5][threadIdx.x], sh[5][threadIdx.x + s]);
+            sh[6][threadIdx.x] = DMIN(sh[6][threadIdx.x], sh[6][threadIdx.x + s]);
+        }
+        __syncthreads();
+    }
+    double red[NRED];
+    for (int q = 0; q < NRED; q++) red[q] = sh[q][0];
+    __syncthreads();
+    __shared__ int s_cnt;
+    if (threadIdx.x == 0) s_cnt = 0;
+    sh[0][threadIdx.x] = dtl;
+    __syncthreads();
+    atomicAdd(&s_cnt, cnt);
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sh[0][threadIdx.x] = DMIN(sh[0][threadIdx.x], sh[0][threadIdx.x + s]);
+        __syncthreads();
+    }
+    const double dtlapusta = sh[0][0];
+    const int ynpl = s_cnt;
+    __syncthreads();
+    // ddd: sequential sum in j order, staged through shared memory in chunks
+    double* stage = &sh[0][0];
+    const int CHUNK = NRED * 256;
+    double ddd = 0;
+    for (int j0 = 0; j0 < g.Nx; j0 += CHUNK) {
+        const int n = g.Nx - j0 < CHUNK ? g.Nx - j0 : CHUNK;
+        for (int t = threadIdx.x; t < n; t += blockDim.x)
+            stage[t] = rsfbuf[j0 + t] != 0 ? rsfbuf[g.Nx + j0 + t] : 0.0;
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int t = 0; t < n; t++) ddd += stage[t];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) control_update(g, ds, p, red, ynpl, ddd, dtlapusta);
 }
 
-// :1310-1456 on one thread.
-__global__ void k_control(Geo g, DevScalars* ds, hmec_params p, const double* __restrict__ part, int nb,
-                          const double* __restrict__ rsfbuf) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double vxmax = -INFINITY, vxmin = INFINITY, vymax = -INFINITY, vymin = INFINITY, bx = 0, by = 0, dtslip = 1e30;
-    for (int b = 0; b < nb; b++) {
-        const double* a = part + b * NRED;
-        vxmax = DMAX(vxmax, a[0]);
-        vxmin = DMIN(vxmin, a[1]);
-        vymax = DMAX(vymax, a[2]);
-        vymin = DMIN(vymin, a[3]);
-        bx = DMAX(bx, a[4]);
-        by = DMAX(by, a[5]);
-        dtslip = DMIN(dtslip, a[6]);
-    }
-    // fault bookkeeping in the reference's j order
-    int ynpl = 0;
-    double ddd = 0, dtlapusta = 1e7;
-    for (int j = 0; j < g.Nx; j++) {
-        if (rsfbuf[j] != 0) {
-            ynpl++;
-            ddd += rsfbuf[g.Nx + j];
-        }
-        dtlapusta = DMIN(dtlapusta, rsfbuf[2 * g.Nx + j]);
-    }
+// :1310-1456 on one thread, from the reduced velocity extrema red[NRED] and
+// the fault bookkeeping (ynpl, ddd summed in the reference's j order,
+// dtlapusta).
+__device__ void control_update(const Geo& g, DevScalars* ds, const hmec_params& p, const double* red, int ynpl,
+                               double ddd, double dtlapusta) {
+    const double vxmax = red[0], vxmin = red[1], vymax = red[2], vymin = red[3], bx = red[4], by = red[5];
+    double dtslip = red[6];
     const int iterstep = ds->iterstep;
     int ynlast = ds->ynlast;
     double dt = ds->dt;
@@ -876,14 +964,16 @@ __global__ void k_post_p(Geo g, const DevScalars* ds, hmec_params p, PostP P) {
     IS(P.EL_DECOM, i, j) = BETADRAINED * (pta - PT0a - KBW * pfa + KBW * PF0a) / dt;
 }
 
-// a19 rollover monitors :1665-1696 (over i < Ny, j < Nx) in one block.
+// a19 rollover monitors :1665-1696 (over i < Ny, j < Nx): block partials, the
+// last block finishes (256 threads).
 __global__ void k_monitors(Geo g, DevScalars* ds, const double* __restrict__ RHOX, const double* __restrict__ RHOY,
-                           const double* __restrict__ vxs, const double* __restrict__ vys) {
-    __shared__ double sh[4][1024];
+                           const double* __restrict__ vxs, const double* __restrict__ vys, double* part,
+                           unsigned* ticket) {
+    __shared__ double sh[4][256];
     double a0 = -1e30, a1 = 1e30, a2 = -1e30, a3 = 1e30;
-    const long long nb = (long long)g.Nx * g.Ny;
-    for (long long t = threadIdx.x; t < nb; t += blockDim.x) {
-        const int i = (int)(t % g.Ny), j = (int)(t / g.Ny);
+    const int nb = g.Nx * g.Ny;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nb; t += gridDim.x * blockDim.x) {
+        const int j = t / g.Ny, i = t - j * g.Ny;
         if (IS(RHOX, i, j) > 2000 && i != 0) {
             a0 = DMAX(a0, IS(vxs, i, j));
             a1 = DMIN(a1, IS(vxs, i, j));
@@ -907,11 +997,25 @@ __global__ void k_monitors(Geo g, DevScalars* ds, const double* __restrict__ RHO
         }
         __syncthreads();
     }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 4; q++) part[blockIdx.x * 4 + q] = sh[q][0];
+    if (!arrive_last(ticket)) return;
+    a0 = -1e30, a1 = 1e30, a2 = -1e30, a3 = 1e30;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        a0 = DMAX(a0, __ldcg(part + b * 4));
+        a1 = DMIN(a1, __ldcg(part + b * 4 + 1));
+        a2 = DMAX(a2, __ldcg(part + b * 4 + 2));
+        a3 = DMIN(a3, __ldcg(part + b * 4 + 3));
+    }
+    a0 = block_max256(sh[0], a0);
+    a1 = block_min256(sh[1], a1);
+    a2 = block_max256(sh[2], a2);
+    a3 = block_min256(sh[3], a3);
     if (threadIdx.x == 0) {
-        ds->maxvxsmod = sh[0][0];
-        ds->minvxsmod = sh[1][0];
-        ds->maxvysmod = sh[2][0];
-        ds->minvysmod = sh[3][0];
+        ds->maxvxsmod = a0;
+        ds->minvxsmod = a1;
+        ds->maxvysmod = a2;
+        ds->minvysmod = a3;
     }
 }
 
@@ -972,8 +1076,7 @@ int iter_prepare(hmec_ctx* ctx) {
                 f[HMEC_F_ETAP0], f[HMEC_F_ETAB0], f[HMEC_F_POR], f[HMEC_F_GGGP], f[HMEC_F_ETAP], f[HMEC_F_ETAB],
                 f[HMEC_F_GGGB], f[HMEC_F_DILP]);
     const int nb = 152;
-    HMEC_LAUNCH(ctx, k_min_etadx, nb, 256, 0, g, f[HMEC_F_ETADX], ctx->red);
-    HMEC_LAUNCH(ctx, k_scales, 1, 1, 0, g, ctx->ds, ctx->red, nb);
+    HMEC_LAUNCH(ctx, k_min_etadx, nb, 256, 0, g, f[HMEC_F_ETADX], ctx->red, ctx->ds, ctx->ticket);
     HMEC_LAUNCH(ctx, k_rescale_guess, grid_s(g), 64, 0, g, ctx->ds, ctx->S);
     HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;
@@ -997,7 +1100,7 @@ int iter_finish(hmec_ctx* ctx) {
     int* status = &ctx->ds->status;
     HMEC_LAUNCH(ctx, k_reload, grid_s(g), 64, 0, g, ctx->ds, ctx->S, f[HMEC_F_pt], f[HMEC_F_vxs], f[HMEC_F_vys],
                 f[HMEC_F_pf], f[HMEC_F_vxD], f[HMEC_F_vyD], status);
-    HMEC_LAUNCH(ctx, k_vmax, 1, 1024, 0, g, f[HMEC_F_VSLIPB], ctx->ds);
+    HMEC_LAUNCH(ctx, k_vmax, 152, 256, 0, g, f[HMEC_F_VSLIPB], ctx->ds, ctx->red + 2048, ctx->ticket + 1);
     HMEC_LAUNCH(ctx, k_stress_basic, grid_b(g), 64, 0, g, ctx->ds, f[HMEC_F_vxs], f[HMEC_F_vys], f[HMEC_F_GGG],
                 f[HMEC_F_ETA], f[HMEC_F_SXY0], f[HMEC_F_EXY], f[HMEC_F_SXY], f[HMEC_F_ETA0], f[HMEC_F_ETA5],
                 f[HMEC_F_DSY], f[HMEC_F_YNY], f[HMEC_F_SigmaY], f[HMEC_F_SII_fault], f[HMEC_F_OM], f[HMEC_F_OM5]);
@@ -1013,8 +1116,7 @@ int iter_finish(hmec_ctx* ctx) {
     HMEC_LAUNCH(ctx, k_rsf, nblocks(g.Nx, 128), 128, 0, g, ctx->ds, ctx->p, in, out, status);
     const int nb = 152;
     HMEC_LAUNCH(ctx, k_reduce_vel, nb, 256, 0, g, ctx->p, ctx->crd[3], ctx->crd[5], f[HMEC_F_vxs], f[HMEC_F_vys],
-                f[HMEC_F_VSLIPB], ctx->red);
-    HMEC_LAUNCH(ctx, k_control, 1, 32, 0, g, ctx->ds, ctx->p, ctx->red, nb, rsfbuf);
+                f[HMEC_F_VSLIPB], ctx->red, rsfbuf, ctx->ds, ctx->ticket + 2);
     HMEC_LAUNCH(ctx, k_eta_update, grid_b(g), 64, 0, g, ctx->ds, ctx->p, f[HMEC_F_ETA], f[HMEC_F_ETA5],
                 f[HMEC_F_ETA0], f[HMEC_F_ETA50], f[HMEC_F_YNY0], f[HMEC_F_YNY], f[HMEC_F_OM], f[HMEC_F_OM5]);
     HMEC_CUDA(ctx, cudaGetLastError());
@@ -1034,7 +1136,8 @@ int step_end(hmec_ctx* ctx) {
             f[HMEC_F_SYY], f[HMEC_F_EII], f[HMEC_F_EIIVP], f[HMEC_F_SII], f[HMEC_F_DIS], f[HMEC_F_pt_ave],
             f[HMEC_F_pf_ave], f[HMEC_F_VIS_COMP], f[HMEC_F_EL_DECOM]};
     HMEC_LAUNCH(ctx, k_post_p, grid_s(g), 64, 0, g, ctx->ds, ctx->p, P);
-    HMEC_LAUNCH(ctx, k_monitors, 1, 1024, 0, g, ctx->ds, f[HMEC_F_RHOX], f[HMEC_F_RHOY], f[HMEC_F_vxs], f[HMEC_F_vys]);
+    HMEC_LAUNCH(ctx, k_monitors, 152, 256, 0, g, ctx->ds, f[HMEC_F_RHOX], f[HMEC_F_RHOY], f[HMEC_F_vxs], f[HMEC_F_vys],
+                ctx->red + 2048, ctx->ticket + 3);
     Roll R{f[HMEC_F_vxs], f[HMEC_F_vys], f[HMEC_F_vxD], f[HMEC_F_vyD], f[HMEC_F_PORX], f[HMEC_F_PORY],
            f[HMEC_F_SXX], f[HMEC_F_SYY], f[HMEC_F_SXY], f[HMEC_F_pt], f[HMEC_F_pf], f[HMEC_F_VX0], f[HMEC_F_VY0],
            f[HMEC_F_VXF0], f[HMEC_F_VYF0], f[HMEC_F_SXX0], f[HMEC_F_SYY0], f[HMEC_F_SXY0], f[HMEC_F_PTF0],

@@ -40,11 +40,12 @@ struct MarkerCells {
 // Cell indices of :432-433 and :468-469 (the Vx/Vy cells reuse them).
 __device__ __forceinline__ MarkerCells marker_cells(double xm, double ym, const Geo& g) {
     MarkerCells c;
-    // __ddiv_rn / __dadd_rn keep the reference's IEEE operations (no FMA)
-    c.jb = check_bounds(fix_trunc(__ddiv_rn(xm, g.dx)), g.Nx);
-    c.ib = check_bounds(fix_trunc(__ddiv_rn(ym, g.dy)), g.Ny);
-    c.jP = check_bounds(fix_trunc(__ddiv_rn(__dadd_rn(xm, g.dx / 2.), g.dx)), g.Nx);
-    c.iP = check_bounds(fix_trunc(__ddiv_rn(__dadd_rn(ym, g.dy / 2.), g.dy)), g.Ny);
+    // the reference's IEEE quotients, decided in FP32 away from cell edges
+    const float rdx = rcp_f32(g.dx), rdy = rcp_f32(g.dy);
+    c.jb = check_bounds(fix_quot(xm, g.dx, rdx, false), g.Nx);
+    c.ib = check_bounds(fix_quot(ym, g.dy, rdy, false), g.Ny);
+    c.jP = check_bounds(fix_quot(xm, g.dx, rdx, true), g.Nx);
+    c.iP = check_bounds(fix_quot(ym, g.dy, rdy, true), g.Ny);
     return c;
 }
 
@@ -188,12 +189,12 @@ struct Crd {
 // division; each differs from the reference's expression by at most an ulp
 // or two (the marker->node fields are tested to 1e-13).
 __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32_t* __restrict__ key, int64_t n,
-                        Geo g, Crd c, hmec_params p, double* __restrict__ out) {
+                        Geo g, Crd c, hmec_params p, double ipor0, double* __restrict__ out) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int m = perm[k];
     const double por = mk.porm[m];
-    const double pr = por / p.POR0;
+    const double pr = por * ipor0;  // por / POR0 to an ulp
     double kkkmm = mk.kkkm[m] * (pr * pr * pr);
     kkkmm = enforce_bounds(kkkmm, p.kkkmin, p.kkkmax);
     double cohescmm, cohestmm, frictcmm, dilatcmm, fricttmm, etasmm0, etamm0, etamm, rhomm;
@@ -226,7 +227,7 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
     const int HR = 2 * (g.Ny - 1), kk = key[m];
     const int hc = kk / HR, hr = kk - hc * HR;
     const int ib = hr >> 1, jb = hc >> 1, iP = ib + (hr & 1), jP = jb + (hc & 1);
-    const double idx = 1.0 / g.dx, idy = 1.0 / g.dy;
+    const double idx = g.idx, idy = g.idy;
     const size_t S = (size_t)n;
     out[MP_DXB * S + k] = (xmm - c.x[jb]) * idx;
     out[MP_DYB * S + k] = (ymm - c.y[ib]) * idy;
@@ -340,16 +341,17 @@ __global__ void k_node_basic(Geo g, const double* __restrict__ cs, double* RHO, 
     node_sums<10>(i, j, g, cs, wt, a);
     if (wt > 0) {
         size_t o = (size_t)j * g.Ny + i;
-        RHO[o] = a[0] / wt;
-        KKK[o] = a[1] / wt;
-        TTT[o] = a[2] / wt;
-        GGG[o] = 1. / (a[3] / wt);
-        ETA0[o] = a[4] / wt;
-        COHT[o] = a[5] / wt;
-        FRIT[o] = a[6] / wt;
-        COHC[o] = a[7] / wt;
-        FRIC[o] = a[8] / wt;
-        DILC[o] = a[9] / wt;
+        const double iw = 1. / wt;  // products instead of ten divisions (an ulp apart)
+        RHO[o] = a[0] * iw;
+        KKK[o] = a[1] * iw;
+        TTT[o] = a[2] * iw;
+        GGG[o] = 1. / (a[3] * iw);
+        ETA0[o] = a[4] * iw;
+        COHT[o] = a[5] * iw;
+        FRIT[o] = a[6] * iw;
+        COHC[o] = a[7] * iw;
+        FRIC[o] = a[8] * iw;
+        DILC[o] = a[9] * iw;
     }
 }
 
@@ -362,12 +364,13 @@ __global__ void k_node_p(Geo g, const double* __restrict__ cs, double* ETAP, dou
     node_sums<5>(i, j, g, cs, wt, a);
     if (wt > 0) {
         size_t o = (size_t)j * g.Ny1 + i;
-        ETAP[o] = a[0] / wt;
-        const double por = a[1] / wt;
+        const double iw = 1. / wt;
+        ETAP[o] = a[0] * iw;
+        const double por = a[1] * iw;
         POR[o] = por;
-        ETAB0[o] = a[2] / wt / por;
-        ETAP0[o] = a[3] / wt;
-        GGGP[o] = 1. / (a[4] / wt);
+        ETAB0[o] = a[2] * iw / por;
+        ETAP0[o] = a[3] * iw;
+        GGGP[o] = 1. / (a[4] * iw);
     }
 }
 
@@ -472,7 +475,8 @@ int p2g_run(hmec_ctx* ctx) {
     mk.rhofm = ctx->mk[HMEC_M_rhofm];
     mk.etafm = ctx->mk[HMEC_M_etafm];
     Crd c{ctx->crd[0], ctx->crd[1], ctx->crd[2], ctx->crd[3], ctx->crd[4], ctx->crd[5], ctx->crd[6], ctx->crd[7]};
-    HMEC_LAUNCH(ctx, k_mprop, nblocks(n, 256), 256, 0, mk, ctx->perm, ctx->mkey, n, g, c, ctx->p, ctx->mprop);
+    HMEC_LAUNCH(ctx, k_mprop, nblocks(n, 256), 256, 0, mk, ctx->perm, ctx->mkey, n, g, c, ctx->p, 1.0 / ctx->p.POR0,
+                ctx->mprop);
     double* const* f = ctx->f;
     // pass 1: corner sums per cell of each grid; pass 2: node sums and the a4 epilogues
     const size_t ncell = (size_t)(g.Ny - 1) * (g.Nx - 1);

@@ -60,10 +60,11 @@ struct Cells {
 
 __device__ __forceinline__ Cells cells_of(double xm, double ym, const Geo& g) {
     Cells c;
-    c.jb = check_bounds(fix_trunc(__ddiv_rn(xm, g.dx)), g.Nx);
-    c.ib = check_bounds(fix_trunc(__ddiv_rn(ym, g.dy)), g.Ny);
-    c.jP = check_bounds(fix_trunc(__ddiv_rn(__dadd_rn(xm, g.dx / 2.), g.dx)), g.Nx);
-    c.iP = check_bounds(fix_trunc(__ddiv_rn(__dadd_rn(ym, g.dy / 2.), g.dy)), g.Ny);
+    const float rdx = rcp_f32(g.dx), rdy = rcp_f32(g.dy);
+    c.jb = check_bounds(fix_quot(xm, g.dx, rdx, false), g.Nx);
+    c.ib = check_bounds(fix_quot(ym, g.dy, rdy, false), g.Ny);
+    c.jP = check_bounds(fix_quot(xm, g.dx, rdx, true), g.Nx);
+    c.iP = check_bounds(fix_quot(ym, g.dy, rdy, true), g.Ny);
     return c;
 }
 
@@ -369,6 +370,7 @@ extern "C" int32_t hmec_markers_to_nodes_noalloc(const hmec_params* p, const dou
     g.lower_block = p->ysize / 2. + g.dy;
     g.upper_block = p->ysize / 2. - g.dy;
     g.dy_faultw = g.dy / g.dx;
+    geo_reciprocals(g);
     Mk mk{markers[HMEC_M_xm], markers[HMEC_M_ym], markers[HMEC_M_t_marker], markers[HMEC_M_rhom],
           markers[HMEC_M_etasm], markers[HMEC_M_etam], markers[HMEC_M_cohescm], markers[HMEC_M_cohestm],
           markers[HMEC_M_frictcm], markers[HMEC_M_dilatcm], markers[HMEC_M_fricttm], markers[HMEC_M_porm],

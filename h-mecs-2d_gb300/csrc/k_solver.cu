@@ -1548,6 +1548,7 @@ static void make_geo(Geo& g, int Nx, int Ny, double xsize, double ysize) {
     g.lower_block = ysize / 2. + g.dy;
     g.upper_block = ysize / 2. - g.dy;
     g.dy_faultw = g.dy / g.dx;
+    geo_reciprocals(g);
 }
 
 static std::vector<int32_t> boundary_rows(const Geo& g) {
