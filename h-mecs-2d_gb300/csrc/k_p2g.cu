@@ -33,6 +33,60 @@ enum {
     MP_ETAP, MP_POR, MP_ETAB0, MP_INVETAD, MP_RHOF
 };
 
+// ---------------------------------------------------------------- double-float
+// The gathers' products and sums run in double-float: a value is the
+// unevaluated sum h + l of two FP32 numbers (~48 bits), with the error-free
+// transformations of Dekker and Knuth (TwoSum; the exact FP32 product error
+// from one fmaf).  On this GPU the FP32 pipe issues ~60x the FP64 rate, and
+// FP64<->FP32 conversions run at the FP64 rate, so FP64 values are split by
+// their bit patterns.  Relative error of a sum of same-sign terms ~1e-14.
+
+// x = h + l: h keeps the top 24 bits of the mantissa (truncated), l is the
+// remaining 29 bits rounded to FP32 (|x - h - l| < 2^-47 |x|).  Zeros and
+// FP64 subnormals give 0; |x| outside [2^-74, 2^127) (and inf/NaN) take the
+// FP64 conversions.
+__device__ __forceinline__ void split_df(double x, float& h, float& l) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
+    const int E = (int)((hi32 >> 20) & 0x7FF);
+    const unsigned sign = hi32 & 0x80000000u;
+    if (E >= 949 && E <= 1150) {
+        h = __uint_as_float(sign | ((unsigned)(E - 896) << 23) | ((hi32 & 0xFFFFFu) << 3) | (lo32 >> 29));
+        const float r = __fmul_rn(__uint2float_rn(lo32 & 0x1FFFFFFFu), __uint_as_float((unsigned)(E - 948) << 23));
+        l = sign ? -r : r;
+    } else if (E == 0) {
+        h = 0.f;
+        l = 0.f;
+    } else {
+        h = __double2float_rn(x);
+        l = __double2float_rn(x - (double)h);
+    }
+}
+
+// (sh, sl) += t + e, with t + e already a double-float (|e| <= ulp(t)).
+__device__ __forceinline__ void df_acc(float& sh, float& sl, float t, float e) {
+    const float s = __fadd_rn(sh, t);
+    const float bb = __fsub_rn(s, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(t, bb));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
+// (ah + al)(bh + bl) as t + e (al * bl dropped, < 2^-48 relative).
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& t, float& e) {
+    t = __fmul_rn(ah, bh);
+    e = fmaf(ah, bh, -t);
+    e = fmaf(ah, bl, e);
+    e = fmaf(al, bh, e);
+}
+
+// normalised double-float a + b (|a| >= |b|)
+__device__ __forceinline__ void df_norm(float& a, float& b) {
+    const float s = __fadd_rn(a, b);
+    b = __fsub_rn(b, __fsub_rn(s, a));
+    a = s;
+}
+
 struct MarkerCells {
     int ib, jb, iP, jP;
 };
@@ -187,9 +241,10 @@ struct Crd {
 // key (no second set of divisions), (por/POR0)^3 is two products, the
 // distances are products with 1/dx and 1/dy, and 1/etad = k/etaf is one
 // division; each differs from the reference's expression by at most an ulp
-// or two (the marker->node fields are tested to 1e-13).
+// or two (the marker->node fields are tested to 1e-13).  Each row is stored
+// as a double-float pair of FP32 rows for the gathers.
 __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32_t* __restrict__ key, int64_t n,
-                        Geo g, Crd c, hmec_params p, double ipor0, double* __restrict__ out) {
+                        Geo g, Crd c, hmec_params p, double ipor0, float* __restrict__ out) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int m = perm[k];
@@ -229,27 +284,34 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
     const int ib = hr >> 1, jb = hc >> 1, iP = ib + (hr & 1), jP = jb + (hc & 1);
     const double idx = g.idx, idy = g.idy;
     const size_t S = (size_t)n;
-    out[MP_DXB * S + k] = (xmm - c.x[jb]) * idx;
-    out[MP_DYB * S + k] = (ymm - c.y[ib]) * idy;
-    out[MP_DXX * S + k] = (xmm - c.xvx[jb]) * idx;
-    out[MP_DYY * S + k] = (ymm - c.yvy[ib]) * idy;
-    out[MP_DXP * S + k] = (xmm - c.xp[jP]) * idx;
-    out[MP_DYP * S + k] = (ymm - c.yp[iP]) * idy;
-    out[MP_RHO * S + k] = rhomm;
-    out[MP_KKK * S + k] = kkkmm;
-    out[MP_TTT * S + k] = tm;
-    out[MP_INVG * S + k] = 1. / mk.gm[m];
-    out[MP_ETA0 * S + k] = etamm0;
-    out[MP_COHT * S + k] = cohestmm;
-    out[MP_FRIT * S + k] = fricttmm;
-    out[MP_COHC * S + k] = cohescmm;
-    out[MP_FRIC * S + k] = frictcmm;
-    out[MP_DILC * S + k] = dilatcmm;
-    out[MP_ETAP * S + k] = etamm;
-    out[MP_POR * S + k] = por;
-    out[MP_ETAB0 * S + k] = etasmm0;
-    out[MP_INVETAD * S + k] = kkkmm / mk.etafm[m];
-    out[MP_RHOF * S + k] = mk.rhofm[m];
+    // row q of the output: its high parts at row 2q, low parts at row 2q + 1
+    auto put = [&](int q, double v) {
+        float h, l;
+        split_df(v, h, l);
+        out[(size_t)(2 * q) * S + k] = h;
+        out[(size_t)(2 * q + 1) * S + k] = l;
+    };
+    put(MP_DXB, (xmm - c.x[jb]) * idx);
+    put(MP_DYB, (ymm - c.y[ib]) * idy);
+    put(MP_DXX, (xmm - c.xvx[jb]) * idx);
+    put(MP_DYY, (ymm - c.yvy[ib]) * idy);
+    put(MP_DXP, (xmm - c.xp[jP]) * idx);
+    put(MP_DYP, (ymm - c.yp[iP]) * idy);
+    put(MP_RHO, rhomm);
+    put(MP_KKK, kkkmm);
+    put(MP_TTT, tm);
+    put(MP_INVG, 1. / mk.gm[m]);
+    put(MP_ETA0, etamm0);
+    put(MP_COHT, cohestmm);
+    put(MP_FRIT, fricttmm);
+    put(MP_COHC, cohescmm);
+    put(MP_FRIC, frictcmm);
+    put(MP_DILC, dilatcmm);
+    put(MP_ETAP, etamm);
+    put(MP_POR, por);
+    put(MP_ETAB0, etasmm0);
+    put(MP_INVETAD, kkkmm / mk.etafm[m]);
+    put(MP_RHOF, mk.rhofm[m]);
 }
 
 // Gathers in two passes.  Every marker of one grid's cell (ci, cj) (cells
@@ -272,7 +334,7 @@ struct Props {
 };
 
 template <bool ROWP, bool COLP, int NP>
-__global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const double* __restrict__ mp, int64_t n,
+__global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const float* __restrict__ mp, int64_t n,
                             int dxrow, int dyrow, Props<NP> props, double* __restrict__ cs) {
     const int NCI = g.Ny - 1, NCJ = g.Nx - 1;
     const int ci = blockIdx.x * blockDim.x + threadIdx.x, cj = blockIdx.y;
@@ -280,34 +342,60 @@ __global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const doub
     const int HR = 2 * (g.Ny - 1), HC = 2 * (g.Nx - 1);
     const int r0 = ROWP ? 2 * ci - 1 : 2 * ci, c0 = COLP ? 2 * cj - 1 : 2 * cj;
     const int rlo = r0 < 0 ? 0 : r0, rhi = r0 + 1 > HR - 1 ? HR - 1 : r0 + 1;
-    double W[4] = {0, 0, 0, 0}, S[NP][4];
+    // double-float accumulators: [c] weight, [q][c] weight * property
+    float Wh[4] = {0, 0, 0, 0}, Wl[4] = {0, 0, 0, 0}, Sh[NP][4], Sl[NP][4];
 #pragma unroll
     for (int q = 0; q < NP; q++)
 #pragma unroll
-        for (int c = 0; c < 4; c++) S[q][c] = 0;
+        for (int c = 0; c < 4; c++) Sh[q][c] = Sl[q][c] = 0;
     const size_t Sn = (size_t)n;
+    const float* dxh_row = mp + (size_t)(2 * dxrow) * Sn;
+    const float* dyh_row = mp + (size_t)(2 * dyrow) * Sn;
     for (int hc = c0 < 0 ? 0 : c0; hc <= c0 + 1 && hc < HC; hc++) {
         const int b = start[hc * HR + rlo], e = start[hc * HR + rhi + 1];
         for (int k = b; k < e; k++) {
-            const double dx = mp[dxrow * Sn + k], dy = mp[dyrow * Sn + k];
-            const double w[4] = {(1 - dx) * (1 - dy), (1 - dx) * dy, dx * (1 - dy), dx * dy};
+            const float dxh = dxh_row[k], dxl = dxh_row[Sn + k], dyh = dyh_row[k], dyl = dyh_row[Sn + k];
+            // 1 - dx and 1 - dy exactly as TwoSum pairs (plus the low parts)
+            float axh = __fsub_rn(1.f, dxh), ayh = __fsub_rn(1.f, dyh);
+            float axl, ayl;
+            {
+                float bb = __fsub_rn(axh, 1.f);
+                axl = __fsub_rn(__fadd_rn(__fsub_rn(1.f, __fsub_rn(axh, bb)), __fsub_rn(-dxh, bb)), dxl);
+                bb = __fsub_rn(ayh, 1.f);
+                ayl = __fsub_rn(__fadd_rn(__fsub_rn(1.f, __fsub_rn(ayh, bb)), __fsub_rn(-dyh, bb)), dyl);
+            }
+            // the bilinear weights (1-dx)(1-dy), (1-dx) dy, dx (1-dy), dx dy
+            float wh[4], wl[4];
+            df_mul(axh, axl, ayh, ayl, wh[0], wl[0]);
+            df_mul(axh, axl, dyh, dyl, wh[1], wl[1]);
+            df_mul(dxh, dxl, ayh, ayl, wh[2], wl[2]);
+            df_mul(dxh, dxl, dyh, dyl, wh[3], wl[3]);
 #pragma unroll
-            for (int c = 0; c < 4; c++) W[c] += w[c];
+            for (int c = 0; c < 4; c++) {
+                df_norm(wh[c], wl[c]);
+                df_acc(Wh[c], Wl[c], wh[c], wl[c]);
+            }
 #pragma unroll
             for (int q = 0; q < NP; q++) {
-                const double pq = mp[props.p[q] * Sn + k];
+                const float* row = mp + (size_t)(2 * props.p[q]) * Sn;
+                const float ph = row[k], pl = row[Sn + k];
 #pragma unroll
-                for (int c = 0; c < 4; c++) S[q][c] += pq * w[c];
+                for (int c = 0; c < 4; c++) {
+                    float t, er;
+                    df_mul(wh[c], wl[c], ph, pl, t, er);
+                    df_acc(Sh[q][c], Sl[q][c], t, er);
+                }
             }
         }
     }
     const size_t ncell = (size_t)NCI * NCJ, cell = (size_t)cj * NCI + ci;
 #pragma unroll
-    for (int c = 0; c < 4; c++) cs[(size_t)c * ncell + cell] = W[c];
+    for (int c = 0; c < 4; c++) cs[(size_t)c * ncell + cell] = (double)Wh[c] + (double)Wl[c];
 #pragma unroll
     for (int q = 0; q < NP; q++)
 #pragma unroll
-        for (int c = 0; c < 4; c++) cs[((size_t)(1 + q) * 4 + c) * ncell + cell] = S[q][c];
+        for (int c = 0; c < 4; c++)
+            cs[((size_t)(1 + q) * 4 + c) * ncell + cell] = (double)Sh[q][c] + (double)Sl[q][c];
 }
 
 // Node (i, j): cells (i-1, j-1), (i, j-1), (i-1, j), (i, j), of which it is
@@ -421,7 +509,7 @@ int p2g_alloc(hmec_ctx* ctx) {
     HMEC_CUDA(ctx, cudaMalloc(&ctx->hc_start, sizeof(int32_t) * ((size_t)ctx->nhalf + 2)));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->hc_fill, sizeof(int32_t) * ((size_t)ctx->nhalf + 1)));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->scan_part, sizeof(int32_t) * ((size_t)nparts + 1)));
-    HMEC_CUDA(ctx, cudaMalloc(&ctx->mprop, sizeof(double) * (size_t)NPROP * (size_t)n));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->mprop, sizeof(float) * 2 * (size_t)NPROP * (size_t)n));
     // corner sums: (10 + 5 + 4 + 4 properties + 4 weights) x 4 corners per cell
     const size_t ncell = (size_t)(g.Ny - 1) * (g.Nx - 1);
     HMEC_CUDA(ctx, cudaMalloc(&ctx->cellsum, sizeof(double) * 27 * 4 * ncell));

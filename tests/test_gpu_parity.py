@@ -73,8 +73,13 @@ def test_assembly_parity(preset, steps):
     rowmax = np.maximum(abs(A).max(axis=1).toarray().ravel(), 1e-300)
     D = abs(Ag - A).max(axis=1).toarray().ravel()
     assert np.max(D / rowmax) < 1e-13
-    assert np.max(np.abs(Rg - R) / np.maximum(np.abs(R), 1e-300)) < 1e-13
-    assert pf == pytest.approx(o.scales()[0], rel=1e-15) and pt == pf
+    # right-hand sides per equation type (Pt, vx, vy, Pf, vxD, vyD), relative
+    # to that type's largest entry: single entries can cancel to near zero
+    for t in range(6):
+        den = max(float(np.max(np.abs(R[t::6]))), 1e-300)
+        assert float(np.max(np.abs(Rg[t::6] - R[t::6]))) / den < 1e-13, t
+    # the scale is min(ETADX) dx: a marker->node field, held to 1e-13 like them
+    assert pf == pytest.approx(o.scales()[0], rel=1e-13) and pt == pf
 
 
 @pytest.mark.parametrize("form", [hmec.FORM_FP64, hmec.FORM_MIXED])
