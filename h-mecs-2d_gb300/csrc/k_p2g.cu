@@ -52,7 +52,12 @@ __device__ __forceinline__ void split_df(double x, float& h, float& l) {
     const unsigned sign = hi32 & 0x80000000u;
     if (E >= 949 && E <= 1150) {
         h = __uint_as_float(sign | ((unsigned)(E - 896) << 23) | ((hi32 & 0xFFFFFu) << 3) | (lo32 >> 29));
-        const float r = __fmul_rn(__uint2float_rn(lo32 & 0x1FFFFFFFu), __uint_as_float((unsigned)(E - 948) << 23));
+        // the 29 remaining bits R as FP32: 2^23 + v has v in its mantissa for
+        // v < 2^23, so R = 64 (R >> 6) + (R & 63) converts exactly, one rounding
+        const unsigned R = lo32 & 0x1FFFFFFFu;
+        const float rh = __fsub_rn(__uint_as_float(0x4B000000u | (R >> 6)), 8388608.f);
+        const float rl = __fsub_rn(__uint_as_float(0x4B000000u | (R & 63u)), 8388608.f);
+        const float r = __fmul_rn(fmaf(rh, 64.f, rl), __uint_as_float((unsigned)(E - 948) << 23));
         l = sign ? -r : r;
     } else if (E == 0) {
         h = 0.f;
@@ -85,6 +90,38 @@ __device__ __forceinline__ void df_norm(float& a, float& b) {
     const float s = __fadd_rn(a, b);
     b = __fsub_rn(b, __fsub_rn(s, a));
     a = s;
+}
+
+// FP32 -> FP64 through the bit pattern (exact for normal values; FP32
+// subnormals, below 1.2e-38, give 0)
+__device__ __forceinline__ double f2d_bits(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFFu;
+    if (e == 0) return 0.0;
+    if (e == 0xFFu) return (double)f;
+    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                 ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
+    return __longlong_as_double((long long)b);
+}
+
+// h + l = 1 / a: the FP32 reciprocal refined by one Newton-Raphson step
+// x + x (u + u^2), u = 1 - a x, evaluated in double-float (relative error
+// < 3e-14).
+// False when a is outside (1e-30, 1e30) in magnitude: the caller divides.
+__device__ __forceinline__ bool df_rcp(double a, float& h, float& l) {
+    float ah, al;
+    split_df(a, ah, al);
+    const float aa = fabsf(ah);
+    if (!(aa > 1e-30f && aa < 1e30f)) return false;
+    const float r = __frcp_rn(ah);
+    const float t = __fmul_rn(ah, r);  // within 2^-23 of 1: 1 - t is exact
+    const float e1 = fmaf(ah, r, -t);
+    const float u = fmaf(-al, r, __fsub_rn(__fsub_rn(1.f, t), e1));  // 1 - a r
+    const float ru = __fmul_rn(r, u);
+    h = r;
+    l = fmaf(ru, u, ru);  // r (u + u^2)
+    df_norm(h, l);
+    return true;
 }
 
 struct MarkerCells {
@@ -223,7 +260,12 @@ __global__ void k_scan3(int32_t* __restrict__ out, int n, const int32_t* __restr
     if (i < n) out[i] += part[i / 2048];
 }
 
+// v < lo ? lo : (v > hi ? hi : v).  Non-negative finite doubles order like
+// their bit patterns, so for those the compares run on the integer pipe.
 __device__ __forceinline__ double enforce_bounds(double v, double lo, double hi) {
+    const long long b = __double_as_longlong(v), bl = __double_as_longlong(lo), bh = __double_as_longlong(hi);
+    constexpr long long INF = 0x7FF0000000000000LL;
+    if (b >= 0 && b < INF && bl >= 0 && bl < INF && bh >= 0 && bh < INF) return b < bl ? lo : (b > bh ? hi : v);
     return v < lo ? lo : (v > hi ? hi : v);
 }
 
@@ -254,7 +296,7 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
     kkkmm = enforce_bounds(kkkmm, p.kkkmin, p.kkkmax);
     double cohescmm, cohestmm, frictcmm, dilatcmm, fricttmm, etasmm0, etamm0, etamm, rhomm;
     const double tm = mk.t_marker[m];
-    if (tm != 0) {
+    if ((__double_as_longlong(tm) << 1) != 0) {  // tm != 0 (either zero fails, NaN passes)
         cohescmm = mk.cohescm[m] * (1 - por);
         cohestmm = mk.cohestm[m] * (1 - por);
         frictcmm = mk.frictcm[m];
@@ -282,25 +324,45 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
     const int HR = 2 * (g.Ny - 1), kk = key[m];
     const int hc = kk / HR, hr = kk - hc * HR;
     const int ib = hr >> 1, jb = hc >> 1, iP = ib + (hr & 1), jP = jb + (hc & 1);
-    const double idx = g.idx, idy = g.idy;
     const size_t S = (size_t)n;
     // row q of the output: its high parts at row 2q, low parts at row 2q + 1
-    auto put = [&](int q, double v) {
-        float h, l;
-        split_df(v, h, l);
+    auto put_df = [&](int q, float h, float l) {
         out[(size_t)(2 * q) * S + k] = h;
         out[(size_t)(2 * q + 1) * S + k] = l;
     };
-    put(MP_DXB, (xmm - c.x[jb]) * idx);
-    put(MP_DYB, (ymm - c.y[ib]) * idy);
-    put(MP_DXX, (xmm - c.xvx[jb]) * idx);
-    put(MP_DYY, (ymm - c.yvy[ib]) * idy);
-    put(MP_DXP, (xmm - c.xp[jP]) * idx);
-    put(MP_DYP, (ymm - c.yp[iP]) * idy);
+    auto put = [&](int q, double v) {
+        float h, l;
+        split_df(v, h, l);
+        put_df(q, h, l);
+    };
+    // distances: the node offset exactly in FP64 (Sterbenz), then the
+    // product with 1/dx or 1/dy in double-float
+    float ixh, ixl, iyh, iyl;
+    split_df(g.idx, ixh, ixl);
+    split_df(g.idy, iyh, iyl);
+    auto put_dist = [&](int q, double d, float ih, float il) {
+        float dh, dl, t, e;
+        split_df(d, dh, dl);
+        df_mul(dh, dl, ih, il, t, e);
+        df_norm(t, e);
+        put_df(q, t, e);
+    };
+    put_dist(MP_DXB, xmm - c.x[jb], ixh, ixl);
+    put_dist(MP_DYB, ymm - c.y[ib], iyh, iyl);
+    put_dist(MP_DXX, xmm - c.xvx[jb], ixh, ixl);
+    put_dist(MP_DYY, ymm - c.yvy[ib], iyh, iyl);
+    put_dist(MP_DXP, xmm - c.xp[jP], ixh, ixl);
+    put_dist(MP_DYP, ymm - c.yp[iP], iyh, iyl);
     put(MP_RHO, rhomm);
     put(MP_KKK, kkkmm);
     put(MP_TTT, tm);
-    put(MP_INVG, 1. / mk.gm[m]);
+    {
+        float h, l;
+        if (df_rcp(mk.gm[m], h, l))
+            put_df(MP_INVG, h, l);
+        else
+            put(MP_INVG, 1. / mk.gm[m]);
+    }
     put(MP_ETA0, etamm0);
     put(MP_COHT, cohestmm);
     put(MP_FRIT, fricttmm);
@@ -310,7 +372,18 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
     put(MP_ETAP, etamm);
     put(MP_POR, por);
     put(MP_ETAB0, etasmm0);
-    put(MP_INVETAD, kkkmm / mk.etafm[m]);
+    {
+        // k / etaf as k * (1 / etaf) in double-float
+        float rh, rl, kh, kl, t, e;
+        if (df_rcp(mk.etafm[m], rh, rl)) {
+            split_df(kkkmm, kh, kl);
+            df_mul(kh, kl, rh, rl, t, e);
+            df_norm(t, e);
+            put_df(MP_INVETAD, t, e);
+        } else {
+            put(MP_INVETAD, kkkmm / mk.etafm[m]);
+        }
+    }
     put(MP_RHOF, mk.rhofm[m]);
 }
 
@@ -390,12 +463,12 @@ __global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const floa
     }
     const size_t ncell = (size_t)NCI * NCJ, cell = (size_t)cj * NCI + ci;
 #pragma unroll
-    for (int c = 0; c < 4; c++) cs[(size_t)c * ncell + cell] = (double)Wh[c] + (double)Wl[c];
+    for (int c = 0; c < 4; c++) cs[(size_t)c * ncell + cell] = f2d_bits(Wh[c]) + f2d_bits(Wl[c]);
 #pragma unroll
     for (int q = 0; q < NP; q++)
 #pragma unroll
         for (int c = 0; c < 4; c++)
-            cs[((size_t)(1 + q) * 4 + c) * ncell + cell] = (double)Sh[q][c] + (double)Sl[q][c];
+            cs[((size_t)(1 + q) * 4 + c) * ncell + cell] = f2d_bits(Sh[q][c]) + f2d_bits(Sl[q][c]);
 }
 
 // Node (i, j): cells (i-1, j-1), (i, j-1), (i-1, j), (i, j), of which it is
