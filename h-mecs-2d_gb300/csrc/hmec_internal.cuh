@@ -182,7 +182,7 @@ struct hmec_ctx {
     int32_t* hc_start;       // exclusive scan of hc_count (+ total)
     int32_t* hc_fill;        // scatter cursors
     int32_t* scan_part;      // scan block partials
-    float* mprop;            // sorted per-marker properties, double-float rows [2 * 21][marknum]
+    float* mprop;            // sorted per-marker gather records of the four grids (double-float)
     double* cellsum;         // per-cell corner sums of the four grids (k_cell_sums)
     int nhalf;               // number of half-cells
     // global system

@@ -26,12 +26,24 @@
 namespace {
 
 constexpr int NPROP = 21;
+// Per-marker records of each grid's gather, in sorted order: the two
+// interpolation distances then the grid's properties, each a double-float
+// (h, l) pair of FP32, padded to whole float4s.  One thread reads its
+// marker's record with 16-byte loads, so a gather touches each sector once.
+constexpr int REC_B = 24, REC_P = 16, REC_X = 12, REC_Y = 12;  // floats per record
+constexpr int REC_ALL = REC_B + REC_P + REC_X + REC_Y;         // floats per marker
 // sorted per-marker property rows
 enum {
     MP_DXB, MP_DYB, MP_DXX, MP_DYY, MP_DXP, MP_DYP,  // interpolation distances
     MP_RHO, MP_KKK, MP_TTT, MP_INVG, MP_ETA0, MP_COHT, MP_FRIT, MP_COHC, MP_FRIC, MP_DILC,
     MP_ETAP, MP_POR, MP_ETAB0, MP_INVETAD, MP_RHOF
 };
+// Record contents (dx, dy, then the properties in the order the node
+// kernels read them):
+//   basic: DXB DYB | RHO KKK TTT INVG ETA0 COHT FRIT COHC FRIC DILC
+//   P:     DXP DYP | ETAP POR ETAB0 ETA0 INVG (+ 2 floats of padding)
+//   Vx:    DXX DYP | RHO INVETAD RHOF POR
+//   Vy:    DXP DYY | RHO INVETAD RHOF POR
 
 // ---------------------------------------------------------------- double-float
 // The gathers' products and sums run in double-float: a value is the
@@ -324,11 +336,11 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
     const int HR = 2 * (g.Ny - 1), kk = key[m];
     const int hc = kk / HR, hr = kk - hc * HR;
     const int ib = hr >> 1, jb = hc >> 1, iP = ib + (hr & 1), jP = jb + (hc & 1);
-    const size_t S = (size_t)n;
-    // row q of the output: its high parts at row 2q, low parts at row 2q + 1
+    // v[2q], v[2q + 1]: property row q as a double-float
+    float v[2 * NPROP];
     auto put_df = [&](int q, float h, float l) {
-        out[(size_t)(2 * q) * S + k] = h;
-        out[(size_t)(2 * q + 1) * S + k] = l;
+        v[2 * q] = h;
+        v[2 * q + 1] = l;
     };
     auto put = [&](int q, double v) {
         float h, l;
@@ -385,6 +397,29 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
         }
     }
     put(MP_RHOF, mk.rhofm[m]);
+    // the four grids' records (layout above), 16-byte stores
+    auto f4 = [&](int a, int b) { return make_float4(v[2 * a], v[2 * a + 1], v[2 * b], v[2 * b + 1]); };
+    const size_t n_ = (size_t)n;
+    float4* rb = reinterpret_cast<float4*>(out + (size_t)k * REC_B);
+    rb[0] = f4(MP_DXB, MP_DYB);
+    rb[1] = f4(MP_RHO, MP_KKK);
+    rb[2] = f4(MP_TTT, MP_INVG);
+    rb[3] = f4(MP_ETA0, MP_COHT);
+    rb[4] = f4(MP_FRIT, MP_COHC);
+    rb[5] = f4(MP_FRIC, MP_DILC);
+    float4* rp = reinterpret_cast<float4*>(out + n_ * REC_B + (size_t)k * REC_P);
+    rp[0] = f4(MP_DXP, MP_DYP);
+    rp[1] = f4(MP_ETAP, MP_POR);
+    rp[2] = f4(MP_ETAB0, MP_ETA0);
+    rp[3] = make_float4(v[2 * MP_INVG], v[2 * MP_INVG + 1], 0.f, 0.f);
+    float4* rx = reinterpret_cast<float4*>(out + n_ * (REC_B + REC_P) + (size_t)k * REC_X);
+    rx[0] = f4(MP_DXX, MP_DYP);
+    rx[1] = f4(MP_RHO, MP_INVETAD);
+    rx[2] = f4(MP_RHOF, MP_POR);
+    float4* ry = reinterpret_cast<float4*>(out + n_ * (REC_B + REC_P + REC_X) + (size_t)k * REC_Y);
+    ry[0] = f4(MP_DXP, MP_DYY);
+    ry[1] = f4(MP_RHO, MP_INVETAD);
+    ry[2] = f4(MP_RHOF, MP_POR);
 }
 
 // Gathers in two passes.  Every marker of one grid's cell (ci, cj) (cells
@@ -401,14 +436,11 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
 // ROWP / COLP: the grid's cell rows / columns follow the pressure cell.
 // Corner sums: cs[(s * 4 + corner) * ncell + cj * (Ny-1) + ci], s = 0 the
 // weight, s = 1..NP the properties.
-template <int NP>
-struct Props {
-    int p[NP];
-};
-
-template <bool ROWP, bool COLP, int NP>
-__global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const float* __restrict__ mp, int64_t n,
-                            int dxrow, int dyrow, Props<NP> props, double* __restrict__ cs) {
+// rec: the grid's marker records (RW floats each: dx, dy, NP properties).
+template <bool ROWP, bool COLP, int NP, int RW>
+__global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const float* __restrict__ rec,
+                            double* __restrict__ cs) {
+    static_assert(RW % 4 == 0 && RW >= 4 + 2 * NP, "record layout");
     const int NCI = g.Ny - 1, NCJ = g.Nx - 1;
     const int ci = blockIdx.x * blockDim.x + threadIdx.x, cj = blockIdx.y;
     if (ci >= NCI) return;
@@ -421,13 +453,20 @@ __global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const floa
     for (int q = 0; q < NP; q++)
 #pragma unroll
         for (int c = 0; c < 4; c++) Sh[q][c] = Sl[q][c] = 0;
-    const size_t Sn = (size_t)n;
-    const float* dxh_row = mp + (size_t)(2 * dxrow) * Sn;
-    const float* dyh_row = mp + (size_t)(2 * dyrow) * Sn;
     for (int hc = c0 < 0 ? 0 : c0; hc <= c0 + 1 && hc < HC; hc++) {
         const int b = start[hc * HR + rlo], e = start[hc * HR + rhi + 1];
         for (int k = b; k < e; k++) {
-            const float dxh = dxh_row[k], dxl = dxh_row[Sn + k], dyh = dyh_row[k], dyl = dyh_row[Sn + k];
+            float r[RW];
+            const float4* r4 = reinterpret_cast<const float4*>(rec + (size_t)k * RW);
+#pragma unroll
+            for (int t = 0; t < RW / 4; t++) {
+                const float4 x = __ldg(r4 + t);
+                r[4 * t] = x.x;
+                r[4 * t + 1] = x.y;
+                r[4 * t + 2] = x.z;
+                r[4 * t + 3] = x.w;
+            }
+            const float dxh = r[0], dxl = r[1], dyh = r[2], dyl = r[3];
             // 1 - dx and 1 - dy exactly as TwoSum pairs (plus the low parts)
             float axh = __fsub_rn(1.f, dxh), ayh = __fsub_rn(1.f, dyh);
             float axl, ayl;
@@ -450,8 +489,7 @@ __global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const floa
             }
 #pragma unroll
             for (int q = 0; q < NP; q++) {
-                const float* row = mp + (size_t)(2 * props.p[q]) * Sn;
-                const float ph = row[k], pl = row[Sn + k];
+                const float ph = r[4 + 2 * q], pl = r[5 + 2 * q];
 #pragma unroll
                 for (int c = 0; c < 4; c++) {
                     float t, er;
@@ -582,7 +620,7 @@ int p2g_alloc(hmec_ctx* ctx) {
     HMEC_CUDA(ctx, cudaMalloc(&ctx->hc_start, sizeof(int32_t) * ((size_t)ctx->nhalf + 2)));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->hc_fill, sizeof(int32_t) * ((size_t)ctx->nhalf + 1)));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->scan_part, sizeof(int32_t) * ((size_t)nparts + 1)));
-    HMEC_CUDA(ctx, cudaMalloc(&ctx->mprop, sizeof(float) * 2 * (size_t)NPROP * (size_t)n));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->mprop, sizeof(float) * (size_t)REC_ALL * (size_t)n));
     // corner sums: (10 + 5 + 4 + 4 properties + 4 weights) x 4 corners per cell
     const size_t ncell = (size_t)(g.Ny - 1) * (g.Nx - 1);
     HMEC_CUDA(ctx, cudaMalloc(&ctx->cellsum, sizeof(double) * 27 * 4 * ncell));
@@ -645,18 +683,15 @@ int p2g_run(hmec_ctx* ctx) {
     double* cs_p = cs_b + 11 * 4 * ncell;
     double* cs_x = cs_p + 6 * 4 * ncell;
     double* cs_y = cs_x + 5 * 4 * ncell;
-    const Props<10> pb{{MP_RHO, MP_KKK, MP_TTT, MP_INVG, MP_ETA0, MP_COHT, MP_FRIT, MP_COHC, MP_FRIC, MP_DILC}};
-    const Props<5> pp{{MP_ETAP, MP_POR, MP_ETAB0, MP_ETA0, MP_INVG}};
-    const Props<4> pv{{MP_RHO, MP_INVETAD, MP_RHOF, MP_POR}};
+    const float* rec_b = ctx->mprop;
+    const float* rec_p = rec_b + (size_t)n * REC_B;
+    const float* rec_x = rec_p + (size_t)n * REC_P;
+    const float* rec_y = rec_x + (size_t)n * REC_X;
     dim3 bb(64), gc(nblocks(g.Ny - 1, 64), g.Nx - 1);
-    HMEC_LAUNCH(ctx, (k_cell_sums<false, false, 10>), gc, bb, 0, g, ctx->hc_start, ctx->mprop, n, MP_DXB, MP_DYB, pb,
-                cs_b);
-    HMEC_LAUNCH(ctx, (k_cell_sums<true, true, 5>), gc, bb, 0, g, ctx->hc_start, ctx->mprop, n, MP_DXP, MP_DYP, pp,
-                cs_p);
-    HMEC_LAUNCH(ctx, (k_cell_sums<true, false, 4>), gc, bb, 0, g, ctx->hc_start, ctx->mprop, n, MP_DXX, MP_DYP, pv,
-                cs_x);
-    HMEC_LAUNCH(ctx, (k_cell_sums<false, true, 4>), gc, bb, 0, g, ctx->hc_start, ctx->mprop, n, MP_DXP, MP_DYY, pv,
-                cs_y);
+    HMEC_LAUNCH(ctx, (k_cell_sums<false, false, 10, REC_B>), gc, bb, 0, g, ctx->hc_start, rec_b, cs_b);
+    HMEC_LAUNCH(ctx, (k_cell_sums<true, true, 5, REC_P>), gc, bb, 0, g, ctx->hc_start, rec_p, cs_p);
+    HMEC_LAUNCH(ctx, (k_cell_sums<true, false, 4, REC_X>), gc, bb, 0, g, ctx->hc_start, rec_x, cs_x);
+    HMEC_LAUNCH(ctx, (k_cell_sums<false, true, 4, REC_Y>), gc, bb, 0, g, ctx->hc_start, rec_y, cs_y);
     dim3 gb(nblocks(g.Ny, 64), g.Nx), gs(nblocks(g.Ny1, 64), g.Nx1);
     HMEC_LAUNCH(ctx, k_node_basic, gb, bb, 0, g, cs_b, f[HMEC_F_RHO], f[HMEC_F_KKK], f[HMEC_F_TTT], f[HMEC_F_GGG],
                 f[HMEC_F_ETA0], f[HMEC_F_COHT], f[HMEC_F_FRIT], f[HMEC_F_COHC], f[HMEC_F_FRIC], f[HMEC_F_DILC]);
