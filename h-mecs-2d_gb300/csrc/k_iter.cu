@@ -250,6 +250,9 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
                            double* dscale, double* rhs_scaled, double* rhs_raw) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
+    // blockIdx.z: which of the cell's six rows this thread assembles (Pt,
+    // vx, vy, Pf, vxD, vyD); the rows are independent
+    const int sec = blockIdx.z;
     if (i >= g.Ny1) return;
     const int Nx = g.Nx, Ny = g.Ny, Ny1 = g.Ny1, N = g.N;
     // the reference divides by the grid constants and dt; the matrix entries
@@ -266,205 +269,217 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
     const bool want_rhs = rhs_raw != nullptr;
     RowB rb;
     double r;
-    // 5c) Pt  :842-862
-    rb.n = 0;
-    r = 0;
-    if (i == 0 || j == 0 || i == Ny || j == Nx) {
-        rb.add(kp, 1);
-    } else {
-        const double por = IS(F.POR, i, j);
-        const double BETADRAINED = (1. / IS(F.GGGB, i, j) + p.BETASOLID) / (1 - por);
-        const double KBW = 1 - p.BETASOLID / BETADRAINED;
-        const double ietab = 1. / IS(F.ETAB, i, j) / (1 - por);
-        rb.add(kx - RS, -idx);
-        rb.add(kx, idx);
-        rb.add(ky - NV, -idy);
-        rb.add(ky, idy);
-        rb.add(kp, ptscale * (ietab + BETADRAINED * idt));
-        rb.add(kpf, -pfscale * (ietab + BETADRAINED * KBW * idt));
-        if (want_rhs) r = BETADRAINED * (IS(F.PT0, i, j) - KBW * IS(F.PF0, i, j)) / dt + IS(F.DILP, i, j);
-    }
-    emit_row(rb, kp, N, col, val, dscale, rhs_scaled, rhs_raw, r);
-    // 5a) vxs  :698-768
-    rb.n = 0;
-    r = 0;
-    if (i == 0 || i == Ny || j == 0 || j >= Nx - 1) {
-        if (j == Nx) rb.add(kx, 1);
-        if (i == 0 && j < Nx) {
-            rb.add(kx, 1);
-            rb.add(kx + NV, 1);
-            r = 2 * p.bcupper;
-        }
-        if (i == Ny && j < Nx) {
-            rb.add(kx, 1);
-            rb.add(kx - NV, 1);
-            r = 2 * p.bclower;
-        }
-        if (j == 0 && i > 0 && i < Ny) {
-            rb.add(kx, 1);
-            rb.add(kx + RS, -1);
-        }
-        if (j == Nx - 1 && i > 0 && i < Ny) {
-            rb.add(kx, 1);
-            rb.add(kx - RS, -1);
-        }
-    } else {
-        double ETAXY1 = IB(F.ETA, i - 1, j), ETAXY2 = IB(F.ETA, i, j);
-        double ETAXX1 = IS(F.ETAP, i, j), ETAXX2 = IS(F.ETAP, i, j + 1);
-        const double GXY1 = IB(F.GGG, i - 1, j), GXY2 = IB(F.GGG, i, j);
-        const double GXX1 = IS(F.GGGP, i, j), GXX2 = IS(F.GGGP, i, j + 1);
-        const double KXY1 = divplus(dt * GXY1, ETAXY1), KXY2 = divplus(dt * GXY2, ETAXY2);
-        const double KXX1 = divplus(dt * GXX1, ETAXX1), KXX2 = divplus(dt * GXX2, ETAXX2);
-        ETAXY1 *= KXY1;
-        ETAXY2 *= KXY2;
-        ETAXX1 *= KXX1;
-        ETAXX2 *= KXX2;
-        const double dRHOdx = (IS(F.RHOX, i, j + 1) - IS(F.RHOX, i, j - 1)) * g.i2dx;
-        const double dRHOdy = (IB(F.RHO, i, j) - IB(F.RHO, i - 1, j)) * idy;
-        const double temp = gx * dt * dRHOdy / 4.;
-        rb.add(kx, -(ETAXX1 + ETAXX2) * idx2 - (ETAXY1 + ETAXY2) * idy2 - gx * dt * dRHOdx - inertia * IS(F.RHOX, i, j) * idt);
-        rb.add(kx - RS, ETAXX1 * idx2);
-        rb.add(kx + RS, ETAXX2 * idx2);
-        rb.add(kx - NV, ETAXY1 * idy2);
-        rb.add(kx + NV, ETAXY2 * idy2);
-        rb.add(ky - NV, (ETAXY1 - ETAXX1) * idx_dy - temp);
-        rb.add(ky, (ETAXX1 - ETAXY2) * idx_dy - temp);
-        rb.add(ky - NV + RS, (ETAXX2 - ETAXY1) * idx_dy - temp);
-        rb.add(ky + RS, (ETAXY2 - ETAXX2) * idx_dy - temp);
-        rb.add(kp, ptscale * idx);
-        rb.add(kp + RS, -ptscale * idx);
-        if (want_rhs) {
-            const double SXY1 = IB(F.SXY0, i - 1, j) * (1 - KXY1), SXY2 = IB(F.SXY0, i, j) * (1 - KXY2);
-            const double SXX1 = IS(F.SXX0, i, j) * (1 - KXX1), SXX2 = IS(F.SXX0, i, j + 1) * (1 - KXX2);
-            r = -IS(F.RHOX, i, j) * (inertia * IS(F.VX0, i, j) / dt + gx) - (SXX2 - SXX1) / g.dx - (SXY2 - SXY1) / g.dy;
-        }
-    }
-    emit_row(rb, kx, N, col, val, dscale, rhs_scaled, rhs_raw, r);
-    // 5b) vys  :770-840
-    rb.n = 0;
-    r = 0;
-    if (j == 0 || j == Nx || i == 0 || i >= Ny - 1) {
-        if (i == Ny) rb.add(ky, 1);
-        if (j == 0) {
-            rb.add(ky, 1);
-            rb.add(ky + RS, 1);
-        }
-        if (j == Nx) {
-            rb.add(ky, 1);
-            rb.add(ky - RS, 1);
-        }
-        if (i == 0 && j > 0 && j < Nx) rb.add(ky, 1);
-        if (i == Ny - 1 && j > 0 && j < Nx) rb.add(ky, 1);
-    } else {
-        double ETAXY1 = IB(F.ETA, i, j - 1), ETAXY2 = IB(F.ETA, i, j);
-        double ETAYY1 = IS(F.ETAP, i, j), ETAYY2 = IS(F.ETAP, i + 1, j);
-        const double GXY1 = IB(F.GGG, i, j - 1), GXY2 = IB(F.GGG, i, j);
-        const double GYY1 = IS(F.GGGP, i, j), GYY2 = IS(F.GGGP, i + 1, j);
-        const double KXY1 = divplus(dt * GXY1, ETAXY1), KXY2 = divplus(dt * GXY2, ETAXY2);
-        const double KYY1 = divplus(dt * GYY1, ETAYY1), KYY2 = divplus(dt * GYY2, ETAYY2);
-        ETAXY1 *= KXY1;
-        ETAXY2 *= KXY2;
-        ETAYY1 *= KYY1;
-        ETAYY2 *= KYY2;
-        const double dRHOdy = (IS(F.RHOY, i + 1, j) - IS(F.RHOY, i - 1, j)) * g.i2dy;
-        const double dRHOdx = (IB(F.RHO, i, j) - IB(F.RHO, i, j - 1)) * idx;
-        const double temp = gy * dt * dRHOdx / 4.;
-        rb.add(ky, -(ETAYY1 + ETAYY2) * idy2 - (ETAXY1 + ETAXY2) * idx2 - gy * dt * dRHOdy - inertia * IS(F.RHOY, i, j) * idt);
-        rb.add(ky - RS, ETAXY1 * idx2);
-        rb.add(ky + RS, ETAXY2 * idx2);
-        rb.add(ky - NV, ETAYY1 * idy2);
-        rb.add(ky + NV, ETAYY2 * idy2);
-        rb.add(kx - RS, (ETAXY1 - ETAYY1) * idx_dy - temp);
-        rb.add(kx + NV - RS, (ETAYY2 - ETAXY1) * idx_dy - temp);
-        rb.add(kx, (ETAYY1 - ETAXY2) * idx_dy - temp);
-        rb.add(kx + NV, (ETAXY2 - ETAYY2) * idx_dy - temp);
-        rb.add(kp, ptscale * idy);
-        rb.add(kp + NV, -ptscale * idy);
-        if (want_rhs) {
-            const double SXY1 = IB(F.SXY0, i, j - 1) * (1 - KXY1), SXY2 = IB(F.SXY0, i, j) * (1 - KXY2);
-            const double SYY1 = IS(F.SYY0, i, j) * (1 - KYY1), SYY2 = IS(F.SYY0, i + 1, j) * (1 - KYY2);
-            r = -IS(F.RHOY, i, j) * (inertia * IS(F.VY0, i, j) / dt + gy) - (SYY2 - SYY1) / g.dy - (SXY2 - SXY1) / g.dx;
-        }
-    }
-    emit_row(rb, ky, N, col, val, dscale, rhs_scaled, rhs_raw, r);
-    // 5f) Pf  :951-980
-    rb.n = 0;
-    r = 0;
-    if (j == 0 || j == Nx || i <= 1 || i >= Ny - 1) {
-        if (i == 1 || i == Ny - 1) {
-            rb.add(kpf, pfscale);
-            rb.add(kp, -ptscale);
-            r = -p.PTFDIFF;
+    if (sec == 0) {
+        // 5c) Pt  :842-862
+        rb.n = 0;
+        r = 0;
+        if (i == 0 || j == 0 || i == Ny || j == Nx) {
+            rb.add(kp, 1);
         } else {
-            rb.add(kpf, 1);
+            const double por = IS(F.POR, i, j);
+            const double BETADRAINED = (1. / IS(F.GGGB, i, j) + p.BETASOLID) / (1 - por);
+            const double KBW = 1 - p.BETASOLID / BETADRAINED;
+            const double ietab = 1. / IS(F.ETAB, i, j) / (1 - por);
+            rb.add(kx - RS, -idx);
+            rb.add(kx, idx);
+            rb.add(ky - NV, -idy);
+            rb.add(ky, idy);
+            rb.add(kp, ptscale * (ietab + BETADRAINED * idt));
+            rb.add(kpf, -pfscale * (ietab + BETADRAINED * KBW * idt));
+            if (want_rhs) r = BETADRAINED * (IS(F.PT0, i, j) - KBW * IS(F.PF0, i, j)) / dt + IS(F.DILP, i, j);
         }
-    } else {
-        const double por = IS(F.POR, i, j);
-        const double BETADRAINED = (1 / IS(F.GGGB, i, j) + p.BETASOLID) / (1 - por);
-        const double KBW = 1 - p.BETASOLID / BETADRAINED;
-        const double KSK = (BETADRAINED - p.BETASOLID) / (BETADRAINED - p.BETASOLID + por * (p.BETAFLUID - p.BETASOLID));
-        const double ietab = 1 / IS(F.ETAB, i, j) / (1 - por);
-        rb.add(kxf - RS, -idx);
-        rb.add(kxf, idx);
-        rb.add(kyf - NV, -idy);
-        rb.add(kyf, idy);
-        rb.add(kp, -ptscale * (ietab + BETADRAINED * KBW * idt));
-        rb.add(kpf, pfscale * (ietab + BETADRAINED * KBW / KSK * idt));
-        if (want_rhs) r = -BETADRAINED * KBW * (IS(F.PT0, i, j) - 1. / KSK * IS(F.PF0, i, j)) / dt - IS(F.DILP, i, j);
+        emit_row(rb, kp, N, col, val, dscale, rhs_scaled, rhs_raw, r);
     }
-    emit_row(rb, kpf, N, col, val, dscale, rhs_scaled, rhs_raw, r);
-    // 5d) vxD  :864-903
-    rb.n = 0;
-    r = 0;
-    if (i == 0 || i == Ny || j == 0 || j >= Nx - 1) {
-        if (j == Nx) rb.add(kxf, 1);
-        if (i == 0 && j < Nx) {
-            rb.add(kxf, 1);
-            rb.add(kxf + NV, -1);
+    if (sec == 1) {
+        // 5a) vxs  :698-768
+        rb.n = 0;
+        r = 0;
+        if (i == 0 || i == Ny || j == 0 || j >= Nx - 1) {
+            if (j == Nx) rb.add(kx, 1);
+            if (i == 0 && j < Nx) {
+                rb.add(kx, 1);
+                rb.add(kx + NV, 1);
+                r = 2 * p.bcupper;
+            }
+            if (i == Ny && j < Nx) {
+                rb.add(kx, 1);
+                rb.add(kx - NV, 1);
+                r = 2 * p.bclower;
+            }
+            if (j == 0 && i > 0 && i < Ny) {
+                rb.add(kx, 1);
+                rb.add(kx + RS, -1);
+            }
+            if (j == Nx - 1 && i > 0 && i < Ny) {
+                rb.add(kx, 1);
+                rb.add(kx - RS, -1);
+            }
+        } else {
+            double ETAXY1 = IB(F.ETA, i - 1, j), ETAXY2 = IB(F.ETA, i, j);
+            double ETAXX1 = IS(F.ETAP, i, j), ETAXX2 = IS(F.ETAP, i, j + 1);
+            const double GXY1 = IB(F.GGG, i - 1, j), GXY2 = IB(F.GGG, i, j);
+            const double GXX1 = IS(F.GGGP, i, j), GXX2 = IS(F.GGGP, i, j + 1);
+            const double KXY1 = divplus(dt * GXY1, ETAXY1), KXY2 = divplus(dt * GXY2, ETAXY2);
+            const double KXX1 = divplus(dt * GXX1, ETAXX1), KXX2 = divplus(dt * GXX2, ETAXX2);
+            ETAXY1 *= KXY1;
+            ETAXY2 *= KXY2;
+            ETAXX1 *= KXX1;
+            ETAXX2 *= KXX2;
+            const double dRHOdx = (IS(F.RHOX, i, j + 1) - IS(F.RHOX, i, j - 1)) * g.i2dx;
+            const double dRHOdy = (IB(F.RHO, i, j) - IB(F.RHO, i - 1, j)) * idy;
+            const double temp = gx * dt * dRHOdy / 4.;
+            rb.add(kx, -(ETAXX1 + ETAXX2) * idx2 - (ETAXY1 + ETAXY2) * idy2 - gx * dt * dRHOdx - inertia * IS(F.RHOX, i, j) * idt);
+            rb.add(kx - RS, ETAXX1 * idx2);
+            rb.add(kx + RS, ETAXX2 * idx2);
+            rb.add(kx - NV, ETAXY1 * idy2);
+            rb.add(kx + NV, ETAXY2 * idy2);
+            rb.add(ky - NV, (ETAXY1 - ETAXX1) * idx_dy - temp);
+            rb.add(ky, (ETAXX1 - ETAXY2) * idx_dy - temp);
+            rb.add(ky - NV + RS, (ETAXX2 - ETAXY1) * idx_dy - temp);
+            rb.add(ky + RS, (ETAXY2 - ETAXX2) * idx_dy - temp);
+            rb.add(kp, ptscale * idx);
+            rb.add(kp + RS, -ptscale * idx);
+            if (want_rhs) {
+                const double SXY1 = IB(F.SXY0, i - 1, j) * (1 - KXY1), SXY2 = IB(F.SXY0, i, j) * (1 - KXY2);
+                const double SXX1 = IS(F.SXX0, i, j) * (1 - KXX1), SXX2 = IS(F.SXX0, i, j + 1) * (1 - KXX2);
+                r = -IS(F.RHOX, i, j) * (inertia * IS(F.VX0, i, j) / dt + gx) - (SXX2 - SXX1) / g.dx - (SXY2 - SXY1) / g.dy;
+            }
         }
-        if (i == Ny && j < Nx) {
-            rb.add(kxf, 1);
-            rb.add(kxf - NV, -1);
-        }
-        if (j == 0) rb.add(kxf, 1);
-        if (j == Nx - 1) rb.add(kxf, 1);
-    } else {
-        rb.add(kxf, -IS(F.ETADX, i, j) - IS(F.RHOFX, i, j) / IS(F.PORX, i, j) * inertia * idt);
-        rb.add(kx, -IS(F.RHOFX, i, j) * inertia * idt);
-        rb.add(kpf, pfscale * idx);
-        rb.add(kpf + RS, -pfscale * idx);
-        if (want_rhs) r = -IS(F.RHOFX, i, j) * (inertia * IS(F.VXF0, i, j) / dt + gx);
+        emit_row(rb, kx, N, col, val, dscale, rhs_scaled, rhs_raw, r);
     }
-    emit_row(rb, kxf, N, col, val, dscale, rhs_scaled, rhs_raw, r);
-    // 5e) vyD  :905-949
-    rb.n = 0;
-    r = 0;
-    if (j == 0 || j == Nx || i == 0 || i >= Ny - 1) {
-        if (i == Ny) rb.add(kyf, 1);
-        if (j == 0 && i > 0 && i < Ny - 1) {
-            rb.add(kyf, 1);
-            rb.add(kyf + RS, -1);
+    if (sec == 2) {
+        // 5b) vys  :770-840
+        rb.n = 0;
+        r = 0;
+        if (j == 0 || j == Nx || i == 0 || i >= Ny - 1) {
+            if (i == Ny) rb.add(ky, 1);
+            if (j == 0) {
+                rb.add(ky, 1);
+                rb.add(ky + RS, 1);
+            }
+            if (j == Nx) {
+                rb.add(ky, 1);
+                rb.add(ky - RS, 1);
+            }
+            if (i == 0 && j > 0 && j < Nx) rb.add(ky, 1);
+            if (i == Ny - 1 && j > 0 && j < Nx) rb.add(ky, 1);
+        } else {
+            double ETAXY1 = IB(F.ETA, i, j - 1), ETAXY2 = IB(F.ETA, i, j);
+            double ETAYY1 = IS(F.ETAP, i, j), ETAYY2 = IS(F.ETAP, i + 1, j);
+            const double GXY1 = IB(F.GGG, i, j - 1), GXY2 = IB(F.GGG, i, j);
+            const double GYY1 = IS(F.GGGP, i, j), GYY2 = IS(F.GGGP, i + 1, j);
+            const double KXY1 = divplus(dt * GXY1, ETAXY1), KXY2 = divplus(dt * GXY2, ETAXY2);
+            const double KYY1 = divplus(dt * GYY1, ETAYY1), KYY2 = divplus(dt * GYY2, ETAYY2);
+            ETAXY1 *= KXY1;
+            ETAXY2 *= KXY2;
+            ETAYY1 *= KYY1;
+            ETAYY2 *= KYY2;
+            const double dRHOdy = (IS(F.RHOY, i + 1, j) - IS(F.RHOY, i - 1, j)) * g.i2dy;
+            const double dRHOdx = (IB(F.RHO, i, j) - IB(F.RHO, i, j - 1)) * idx;
+            const double temp = gy * dt * dRHOdx / 4.;
+            rb.add(ky, -(ETAYY1 + ETAYY2) * idy2 - (ETAXY1 + ETAXY2) * idx2 - gy * dt * dRHOdy - inertia * IS(F.RHOY, i, j) * idt);
+            rb.add(ky - RS, ETAXY1 * idx2);
+            rb.add(ky + RS, ETAXY2 * idx2);
+            rb.add(ky - NV, ETAYY1 * idy2);
+            rb.add(ky + NV, ETAYY2 * idy2);
+            rb.add(kx - RS, (ETAXY1 - ETAYY1) * idx_dy - temp);
+            rb.add(kx + NV - RS, (ETAYY2 - ETAXY1) * idx_dy - temp);
+            rb.add(kx, (ETAYY1 - ETAXY2) * idx_dy - temp);
+            rb.add(kx + NV, (ETAXY2 - ETAYY2) * idx_dy - temp);
+            rb.add(kp, ptscale * idy);
+            rb.add(kp + NV, -ptscale * idy);
+            if (want_rhs) {
+                const double SXY1 = IB(F.SXY0, i, j - 1) * (1 - KXY1), SXY2 = IB(F.SXY0, i, j) * (1 - KXY2);
+                const double SYY1 = IS(F.SYY0, i, j) * (1 - KYY1), SYY2 = IS(F.SYY0, i + 1, j) * (1 - KYY2);
+                r = -IS(F.RHOY, i, j) * (inertia * IS(F.VY0, i, j) / dt + gy) - (SYY2 - SYY1) / g.dy - (SXY2 - SXY1) / g.dx;
+            }
         }
-        if (j == Nx && i > 0 && i < Ny - 1) {
-            rb.add(kyf, 1);
-            rb.add(kyf - RS, -1);
-        }
-        if (i == 0) {
-            rb.add(kyf, 1);
-            r = p.bcvyflower;
-        }
-        if (i == Ny - 1) {
-            rb.add(kyf, 1);
-            r = p.bcvyflower;
-        }
-    } else {
-        rb.add(kyf, -IS(F.ETADY, i, j) - IS(F.RHOFY, i, j) / IS(F.PORY, i, j) * inertia * idt);
-        rb.add(ky, -IS(F.RHOFY, i, j) * inertia * idt);
-        rb.add(kpf, pfscale * idy);
-        rb.add(kpf + NV, -pfscale * idy);
-        if (want_rhs) r = -IS(F.RHOFY, i, j) * (inertia * IS(F.VYF0, i, j) / dt + gy);
+        emit_row(rb, ky, N, col, val, dscale, rhs_scaled, rhs_raw, r);
     }
-    emit_row(rb, kyf, N, col, val, dscale, rhs_scaled, rhs_raw, r);
+    if (sec == 3) {
+        // 5f) Pf  :951-980
+        rb.n = 0;
+        r = 0;
+        if (j == 0 || j == Nx || i <= 1 || i >= Ny - 1) {
+            if (i == 1 || i == Ny - 1) {
+                rb.add(kpf, pfscale);
+                rb.add(kp, -ptscale);
+                r = -p.PTFDIFF;
+            } else {
+                rb.add(kpf, 1);
+            }
+        } else {
+            const double por = IS(F.POR, i, j);
+            const double BETADRAINED = (1 / IS(F.GGGB, i, j) + p.BETASOLID) / (1 - por);
+            const double KBW = 1 - p.BETASOLID / BETADRAINED;
+            const double KSK = (BETADRAINED - p.BETASOLID) / (BETADRAINED - p.BETASOLID + por * (p.BETAFLUID - p.BETASOLID));
+            const double ietab = 1 / IS(F.ETAB, i, j) / (1 - por);
+            rb.add(kxf - RS, -idx);
+            rb.add(kxf, idx);
+            rb.add(kyf - NV, -idy);
+            rb.add(kyf, idy);
+            rb.add(kp, -ptscale * (ietab + BETADRAINED * KBW * idt));
+            rb.add(kpf, pfscale * (ietab + BETADRAINED * KBW / KSK * idt));
+            if (want_rhs) r = -BETADRAINED * KBW * (IS(F.PT0, i, j) - 1. / KSK * IS(F.PF0, i, j)) / dt - IS(F.DILP, i, j);
+        }
+        emit_row(rb, kpf, N, col, val, dscale, rhs_scaled, rhs_raw, r);
+    }
+    if (sec == 4) {
+        // 5d) vxD  :864-903
+        rb.n = 0;
+        r = 0;
+        if (i == 0 || i == Ny || j == 0 || j >= Nx - 1) {
+            if (j == Nx) rb.add(kxf, 1);
+            if (i == 0 && j < Nx) {
+                rb.add(kxf, 1);
+                rb.add(kxf + NV, -1);
+            }
+            if (i == Ny && j < Nx) {
+                rb.add(kxf, 1);
+                rb.add(kxf - NV, -1);
+            }
+            if (j == 0) rb.add(kxf, 1);
+            if (j == Nx - 1) rb.add(kxf, 1);
+        } else {
+            rb.add(kxf, -IS(F.ETADX, i, j) - IS(F.RHOFX, i, j) / IS(F.PORX, i, j) * inertia * idt);
+            rb.add(kx, -IS(F.RHOFX, i, j) * inertia * idt);
+            rb.add(kpf, pfscale * idx);
+            rb.add(kpf + RS, -pfscale * idx);
+            if (want_rhs) r = -IS(F.RHOFX, i, j) * (inertia * IS(F.VXF0, i, j) / dt + gx);
+        }
+        emit_row(rb, kxf, N, col, val, dscale, rhs_scaled, rhs_raw, r);
+    }
+    if (sec == 5) {
+        // 5e) vyD  :905-949
+        rb.n = 0;
+        r = 0;
+        if (j == 0 || j == Nx || i == 0 || i >= Ny - 1) {
+            if (i == Ny) rb.add(kyf, 1);
+            if (j == 0 && i > 0 && i < Ny - 1) {
+                rb.add(kyf, 1);
+                rb.add(kyf + RS, -1);
+            }
+            if (j == Nx && i > 0 && i < Ny - 1) {
+                rb.add(kyf, 1);
+                rb.add(kyf - RS, -1);
+            }
+            if (i == 0) {
+                rb.add(kyf, 1);
+                r = p.bcvyflower;
+            }
+            if (i == Ny - 1) {
+                rb.add(kyf, 1);
+                r = p.bcvyflower;
+            }
+        } else {
+            rb.add(kyf, -IS(F.ETADY, i, j) - IS(F.RHOFY, i, j) / IS(F.PORY, i, j) * inertia * idt);
+            rb.add(ky, -IS(F.RHOFY, i, j) * inertia * idt);
+            rb.add(kpf, pfscale * idy);
+            rb.add(kpf + NV, -pfscale * idy);
+            if (want_rhs) r = -IS(F.RHOFY, i, j) * (inertia * IS(F.VYF0, i, j) / dt + gy);
+        }
+        emit_row(rb, kyf, N, col, val, dscale, rhs_scaled, rhs_raw, r);
+    }
 }
 
 // --------------------------------------------------------- a11 reload
@@ -1084,7 +1099,8 @@ int iter_prepare(hmec_ctx* ctx) {
 
 void launch_assemble(hmec_ctx* ctx, const Geo& g, const AsmFields& af, int32_t* col, double* val, double* dscale,
                      double* rhs_scaled, double* rhs_raw, const double*) {
-    HMEC_LAUNCH(ctx, k_assemble, grid_s(g), 64, 0, g, af, ctx->ds, ctx->p, col, val, dscale, rhs_scaled, rhs_raw);
+    const dim3 grid(nblocks(g.Ny1, 64), g.Nx1, 6);  // z: the six rows of a cell
+    HMEC_LAUNCH(ctx, k_assemble, grid, 64, 0, g, af, ctx->ds, ctx->p, col, val, dscale, rhs_scaled, rhs_raw);
 }
 
 int iter_assemble(hmec_ctx* ctx) {

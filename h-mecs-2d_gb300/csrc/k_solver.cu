@@ -256,19 +256,25 @@ __device__ __forceinline__ void bnd_delta(const SmoothArgs<T>& a, int tid, int n
 // node 2J+1 -> halves of J and J+1.
 struct Map1D {
     int nf, nc;
+    double inv;  // 1 / nf
 };
 
 __host__ __device__ __forceinline__ int m_cell(const Map1D& m, int k) {
     if (k <= 0) return 0;
     if (k >= m.nf + 1) return m.nc + 1;
-    return (int)(((long long)(2 * k - 1) * m.nc) / (2LL * m.nf)) + 1;
+    const long long num = (long long)(2 * k - 1) * m.nc;
+    // 32-bit division where the operands fit (64-bit division is emulated)
+    if (num < 0x7FFFFFFFLL && m.nf < 0x3FFFFFFF) return (int)((unsigned)num / (unsigned)(2 * m.nf)) + 1;
+    return (int)(num / (2LL * m.nf)) + 1;
 }
 
-// hat weight of coarse node K at fine node j
+// hat weight of coarse node K at fine node j: 1 - |j nc - K nf| / nf (the
+// quotient as a product with 1/nf; these weights only shape the
+// preconditioner)
 __host__ __device__ __forceinline__ double m_hat(const Map1D& m, int j, int K) {
     long long d = (long long)j * m.nc - (long long)K * m.nf;
     if (d < 0) d = -d;
-    return d >= m.nf ? 0.0 : 1.0 - (double)d / (double)m.nf;
+    return d >= m.nf ? 0.0 : (double)(m.nf - d) * m.inv;
 }
 
 // fine nodes that can have a nonzero hat weight for coarse node K
@@ -293,8 +299,12 @@ __host__ __device__ __forceinline__ void m_cell_range(const Map1D& m, int K, int
     }
 }
 
-__host__ __device__ __forceinline__ Map1D mapx(const Geo& gf, const Geo& gc) { return Map1D{gf.Nx - 1, gc.Nx - 1}; }
-__host__ __device__ __forceinline__ Map1D mapy(const Geo& gf, const Geo& gc) { return Map1D{gf.Ny - 1, gc.Ny - 1}; }
+__host__ __device__ __forceinline__ Map1D mapx(const Geo& gf, const Geo& gc) {
+    return Map1D{gf.Nx - 1, gc.Nx - 1, 1.0 / (gf.Nx - 1)};
+}
+__host__ __device__ __forceinline__ Map1D mapy(const Geo& gf, const Geo& gc) {
+    return Map1D{gf.Ny - 1, gc.Ny - 1, 1.0 / (gf.Ny - 1)};
+}
 
 // The transfer table of one direction: entry k for fine index k in [0, nf+1].
 static inline std::vector<XferEnt> xfer_table(const Map1D& m) {
@@ -801,6 +811,10 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(const __grid_consta
     for (int c = 0; c < 9; c++) meta[c] = 0;
     const T* src = t.x;  // sweep s > 0 reads the previous sweep's result
     T* dst = t.xalt;
+    // one tile for the whole level (the coarsest levels): the window holds
+    // every unknown, so the sweeps stay in shared memory and only the last
+    // one is published -- no grid barrier or window reload in between
+    const bool solo = t.ntiles == 1 && gridDim.x == 1;
     for (int s = 0; s < nsweeps; s++) {
         for (int tile = blockIdx.x; tile < t.ntiles; tile += gridDim.x) {
             const int ti = tile % t.ntile_i, tj = tile / t.ntile_i;
@@ -838,23 +852,26 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(const __grid_consta
             }
             if (!whole && threadIdx.x == 0) issue_pinv(t, pv, bar, 0, 0, i0, j0, i1, j1);
             // the x window: zero, x + P xc, or the previous sweep's values
-            constexpr int WPT = (WIN_MAX + TILE_BS - 1) / TILE_BS;
-            T xv[WPT];
+            // (a solo tile keeps its window from the previous sweep)
+            if (!(solo && s > 0)) {
+                constexpr int WPT = (WIN_MAX + TILE_BS - 1) / TILE_BS;
+                T xv[WPT];
 #pragma unroll
-            for (int u = 0; u < WPT; u++) {
-                const int lw = threadIdx.x + u * TILE_BS;
-                const int lc = lw / 6, v = lw - 6 * lc;
-                const int ci = wi0 + lc % WSTR, cj = wj0 + lc / WSTR;
-                xv[u] = (T)0;
-                if (lw < WIN_MAX && ci >= 0 && ci <= g.Ny && cj >= 0 && cj <= g.Nx && (s > 0 || mode == 1)) {
-                    xv[u] = src[(cj * g.Ny1 + ci) * 6 + v];
-                    if (s == 0) xv[u] += prolong_one(g, t.gc, t.pmx, t.pmy, t.xc, ci, cj, v);
+                for (int u = 0; u < WPT; u++) {
+                    const int lw = threadIdx.x + u * TILE_BS;
+                    const int lc = lw / 6, v = lw - 6 * lc;
+                    const int ci = wi0 + lc % WSTR, cj = wj0 + lc / WSTR;
+                    xv[u] = (T)0;
+                    if (lw < WIN_MAX && ci >= 0 && ci <= g.Ny && cj >= 0 && cj <= g.Nx && (s > 0 || mode == 1)) {
+                        xv[u] = src[(cj * g.Ny1 + ci) * 6 + v];
+                        if (s == 0) xv[u] += prolong_one(g, t.gc, t.pmx, t.pmy, t.xc, ci, cj, v);
+                    }
                 }
-            }
 #pragma unroll
-            for (int u = 0; u < WPT; u++) {
-                const int lw = threadIdx.x + u * TILE_BS;
-                if (lw < WIN_MAX) xs[lw] = xv[u];
+                for (int u = 0; u < WPT; u++) {
+                    const int lw = threadIdx.x + u * TILE_BS;
+                    if (lw < WIN_MAX) xs[lw] = xv[u];
+                }
             }
             cp_async_wait_all();
             __syncthreads();
@@ -916,15 +933,17 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(const __grid_consta
             for (int k = threadIdx.x; k < nbt; k += blockDim.x) xs[blr[k]] += bdel[k];
             __syncthreads();
             // publish the owned unknowns
-            for (int lw = threadIdx.x; lw < WIN_MAX; lw += blockDim.x) {
-                if (!own[lw]) continue;
-                const int lc = lw / 6, v = lw - 6 * lc;
-                const int ci = wi0 + lc % WSTR, cj = wj0 + lc / WSTR;
-                dst[(cj * g.Ny1 + ci) * 6 + v] = xs[lw];
+            if (!solo || s == nsweeps - 1) {
+                for (int lw = threadIdx.x; lw < WIN_MAX; lw += blockDim.x) {
+                    if (!own[lw]) continue;
+                    const int lc = lw / 6, v = lw - 6 * lc;
+                    const int ci = wi0 + lc % WSTR, cj = wj0 + lc / WSTR;
+                    dst[(cj * g.Ny1 + ci) * 6 + v] = xs[lw];
+                }
             }
             __syncthreads();
         }
-        cg::this_grid().sync();
+        if (!solo) cg::this_grid().sync();
         src = dst;
         dst = (dst == t.xalt) ? t.x : t.xalt;
     }
@@ -976,10 +995,13 @@ struct CoefOut {
 __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y;
+    // blockIdx.z: the section (basic, P, Vx, Vy nodes), independent of one
+    // another; one thread each keeps the serial fine-node loops short
+    const int sec = blockIdx.z;
     if (I >= gc.Ny1) return;
     const Map1D mx = mapx(gf, gc), my = mapy(gf, gc);
     // basic nodes: hat (full) weighting of the fine nodes; G harmonically
-    if (I < gc.Ny && J < gc.Nx) {
+    if (sec == 0 && I < gc.Ny && J < gc.Nx) {
         double se = 0, sg = 0, sr = 0, w = 0;
         int i0, i1, j0, j1;
         m_hat_range(my, I, i0, i1);
@@ -1001,7 +1023,8 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
     }
     const size_t oc = (size_t)J * gc.Ny1 + I;
     // P nodes: average of the fine cells whose centres lie in the coarse cell
-    if (I >= 1 && I <= gc.Ny - 1 && J >= 1 && J <= gc.Nx - 1) {
+    if (sec != 1) {
+    } else if (I >= 1 && I <= gc.Ny - 1 && J >= 1 && J <= gc.Nx - 1) {
         double se = 0, sg = 0, sb = 0, sp = 0, sgb = 0, w = 0;
         int i0, i1, j0, j1;
         m_cell_range(my, I, i0, i1);
@@ -1033,7 +1056,7 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
     }
     // Vx nodes (I, J): fine rows in coarse row I, fine columns hat-weighted
     // around coarse column J (ghost columns excluded)
-    {
+    if (sec == 2) {
         double a[4] = {0, 0, 0, 0}, w = 0;
         int r0, r1, q0, q1;
         m_cell_range(my, I, r0, r1);
@@ -1088,7 +1111,7 @@ __global__ void k_coarsen_coef(Geo gf, Geo gc, CoefIn F, CoefOut C, int flags) {
     }
     // Vy nodes (I, J): fine columns in coarse column J, fine rows hat-weighted
     // around coarse row I (ghost rows excluded)
-    {
+    if (sec == 3) {
         double a[4] = {0, 0, 0, 0}, w = 0;
         int c0, c1, q0, q1;
         m_cell_range(mx, J, c0, c1);
@@ -1897,8 +1920,6 @@ void solver_free(hmec_ctx* ctx) {
     cudaFree(sv.kcur);
 }
 
-static inline dim3 sgrid(const Geo& g) { return dim3(nblocks(g.Ny1, 64), g.Nx1); }
-
 int solver_setup(hmec_ctx* ctx) {
     Solver& sv = ctx->sv;
     const bool mixed = ctx->p.form == HMEC_FORM_MIXED;
@@ -1914,7 +1935,8 @@ int solver_setup(hmec_ctx* ctx) {
                        (double*)a.ETAB, (double*)a.POR, (double*)a.GGGB, (double*)a.RHOX, (double*)a.RHOFX,
                        (double*)a.PORX, (double*)a.ETADX, (double*)a.RHOY, (double*)a.RHOFY, (double*)a.PORY,
                        (double*)a.ETADY};
-            HMEC_LAUNCH(ctx, k_coarsen_coef, sgrid(L.g), 64, 0, F.g, L.g, ci, co, ctx->p.mg_flags);
+            const dim3 cg4(nblocks(L.g.Ny1, 64), L.g.Nx1, 4);  // z: basic, P, Vx, Vy sections
+            HMEC_LAUNCH(ctx, k_coarsen_coef, cg4, 64, 0, F.g, L.g, ci, co, ctx->p.mg_flags);
             launch_assemble(ctx, L.g, L.af, L.col, L.val, L.dscale, nullptr, nullptr, nullptr);
         }
         if (mixed)
@@ -2108,7 +2130,10 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
         if (rc) return rc;
         t.tb_cap = L.tb_cap;
         void* args[] = {&t, &nsweeps, &mode};
-        const bool prof = hmec_prof_begin(ctx, "k_smooth", ab);
+        // live timing by name prefix: "k_smooth" is every level, "k_smooth<l>" one
+        static const char* const lname[8] = {"k_smooth0", "k_smooth1", "k_smooth2", "k_smooth3",
+                                             "k_smooth4", "k_smooth5", "k_smooth6", "k_smooth7"};
+        const bool prof = hmec_prof_begin(ctx, lname[l < 8 ? l : 7], ab);
         const void* kern = L.st_whole ? (const void*)k_smooth_stage<T, true> : (const void*)k_smooth_stage<T, false>;
         HMEC_CUDA(ctx, cudaLaunchCooperativeKernel(kern, dim3(L.st_grid), dim3(TILE_BS), args,
                                                    (size_t)L.st_smem, ctx->stream));
