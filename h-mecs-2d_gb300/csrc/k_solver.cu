@@ -2288,17 +2288,34 @@ int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
         }
         prev = rel;
         HMEC_LAUNCH(ctx, k_scale_vec, nblocks(N, 256), 256, 0, N, r, sv.dots, sv.V, sv.done);
+        // The host looks at the convergence flag only now and then (a look
+        // drains the stream); steps queued after convergence return at once
+        // but still cost their launches.  So the next look is placed where the
+        // residual estimate's observed rate says the tolerance will be met:
+        // the first after a few steps, then after the predicted number of
+        // steps (1 to check_every).
+        int next_check = std::min(4, check_every);
+        double rel_last = rel;
+        int j_last = 0;
         for (int j = 0; j < m && total + j < maxit; j++) {
             double* Vj = sv.V + (size_t)j * N;
             double* Zj = sv.Z + (size_t)j * N;
-            // preconditioner (skipped cheaply when converged: its kernels are not predicated,
-            // so check the flag before launching a whole V-cycle)
-            if (j > 0 && (j % check_every) == 0) {
-                int hd = 0;
+            if (j > 0 && j == next_check) {
                 HMEC_CUDA(ctx, cudaMemcpyAsync(&ctx->hs->pad0, sv.done, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+                HMEC_CUDA(ctx, cudaMemcpyAsync(&ctx->hs->krylov_relres, &ctx->ds->krylov_relres, sizeof(double),
+                                               cudaMemcpyDeviceToHost, ctx->stream));
                 HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-                hd = ctx->hs->pad0;
-                if (hd) break;
+                if (ctx->hs->pad0) break;
+                const double est = ctx->hs->krylov_relres;
+                int step = check_every;
+                if (std::isfinite(est) && est > 0 && est < rel_last) {
+                    const double rate = std::pow(est / rel_last, 1.0 / (j - j_last));
+                    const double need = std::ceil(std::log(rtol / est) / std::log(rate));
+                    step = (int)std::max(1.0, std::min((double)check_every, need));
+                }
+                next_check = j + step;
+                rel_last = est;
+                j_last = j;
             }
             // the previous Arnoldi step already wrote the mixed form's FP32 input
             int prc = precondition(ctx, Vj, Zj, j > 0);
