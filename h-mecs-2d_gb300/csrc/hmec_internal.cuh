@@ -154,6 +154,13 @@ struct Solver {
     int* kcur;             // Arnoldi steps taken in the current cycle
     int nblk;
     std::vector<Level> lv;
+    // setup of the levels as a dependency graph: level l's assembly and its
+    // smoother data on aux[l]; coef[l]: level l's coarse coefficients are
+    // ready (main stream), asm[l]: its matrix and row scale are, done[l]: all
+    // of its setup is
+    std::vector<cudaStream_t> aux;
+    std::vector<cudaEvent_t> ev_coef, ev_asm, ev_done;
+    cudaEvent_t ev_fork = nullptr;
 };
 
 // Live timing of one kernel family (bench.py roofline): CUDA events around

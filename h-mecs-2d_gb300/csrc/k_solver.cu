@@ -1868,6 +1868,18 @@ int solver_alloc(hmec_ctx* ctx) {
     HMEC_CUDA(ctx, cudaMalloc(&sv.done, sizeof(int) * 2));
     HMEC_CUDA(ctx, cudaMalloc(&sv.kcur, sizeof(int) * 2));
     HMEC_CUDA(ctx, cudaMemset(sv.done, 0, sizeof(int) * 2));
+    const size_t nl = sv.lv.size();
+    sv.aux.assign(nl, nullptr);
+    sv.ev_coef.assign(nl, nullptr);
+    sv.ev_asm.assign(nl, nullptr);
+    sv.ev_done.assign(nl, nullptr);
+    for (size_t l = 0; l < nl; l++) {
+        HMEC_CUDA(ctx, cudaStreamCreateWithFlags(&sv.aux[l], cudaStreamNonBlocking));
+        HMEC_CUDA(ctx, cudaEventCreateWithFlags(&sv.ev_coef[l], cudaEventDisableTiming));
+        HMEC_CUDA(ctx, cudaEventCreateWithFlags(&sv.ev_asm[l], cudaEventDisableTiming));
+        HMEC_CUDA(ctx, cudaEventCreateWithFlags(&sv.ev_done[l], cudaEventDisableTiming));
+    }
+    HMEC_CUDA(ctx, cudaEventCreateWithFlags(&sv.ev_fork, cudaEventDisableTiming));
     return HMEC_OK;
 }
 
@@ -1905,6 +1917,17 @@ void solver_free(hmec_ctx* ctx) {
         for (double* p : L.owned) cudaFree(p);
     }
     sv.lv.clear();
+    for (cudaStream_t s : sv.aux)
+        if (s) cudaStreamDestroy(s);
+    for (auto* evs : {&sv.ev_coef, &sv.ev_asm, &sv.ev_done})
+        for (cudaEvent_t e : *evs)
+            if (e) cudaEventDestroy(e);
+    if (sv.ev_fork) cudaEventDestroy(sv.ev_fork);
+    sv.aux.clear();
+    sv.ev_coef.clear();
+    sv.ev_asm.clear();
+    sv.ev_done.clear();
+    sv.ev_fork = nullptr;
     cudaFree(sv.V);
     cudaFree(sv.Z);
     cudaFree(sv.w);
@@ -1920,25 +1943,46 @@ void solver_free(hmec_ctx* ctx) {
     cudaFree(sv.kcur);
 }
 
+// The library's launch helpers use ctx->stream; inside a scope they go to s.
+struct StreamScope {
+    hmec_ctx* ctx;
+    cudaStream_t saved;
+    StreamScope(hmec_ctx* c, cudaStream_t s) : ctx(c), saved(c->stream) { c->stream = s; }
+    ~StreamScope() { ctx->stream = saved; }
+};
+
+// Rebuilds every level after a fine assembly.  The work is a graph, not a
+// chain: the coarse coefficients form a chain on the main stream (level l
+// needs level l-1's), each level's assembly, inverses, smoother copy and
+// boundary pack run on its own stream once its coefficients exist, and the
+// restriction scaling of level l also waits for level l-1's row scale.  The
+// small coarse levels' kernels thus overlap instead of queueing.
 int solver_setup(hmec_ctx* ctx) {
     Solver& sv = ctx->sv;
     const bool mixed = ctx->p.form == HMEC_FORM_MIXED;
     int* status = &ctx->ds->status;
+    const cudaStream_t main = ctx->stream;
+    HMEC_CUDA(ctx, cudaEventRecord(sv.ev_fork, main));
+    for (size_t l = 1; l < sv.lv.size(); l++) {
+        Level& L = sv.lv[l];
+        Level& F = sv.lv[l - 1];
+        CoefIn ci{F.af.ETA, F.af.GGG, F.af.RHO, F.af.ETAP, F.af.GGGP, F.af.ETAB, F.af.POR, F.af.GGGB,
+                  F.af.RHOX, F.af.RHOFX, F.af.PORX, F.af.ETADX, F.af.RHOY, F.af.RHOFY, F.af.PORY, F.af.ETADY};
+        AsmFields& a = L.af;
+        CoefOut co{(double*)a.ETA, (double*)a.GGG, (double*)a.RHO, (double*)a.ETAP, (double*)a.GGGP,
+                   (double*)a.ETAB, (double*)a.POR, (double*)a.GGGB, (double*)a.RHOX, (double*)a.RHOFX,
+                   (double*)a.PORX, (double*)a.ETADX, (double*)a.RHOY, (double*)a.RHOFY, (double*)a.PORY,
+                   (double*)a.ETADY};
+        const dim3 cg4(nblocks(L.g.Ny1, 64), L.g.Nx1, 4);  // z: basic, P, Vx, Vy sections
+        HMEC_LAUNCH(ctx, k_coarsen_coef, cg4, 64, 0, F.g, L.g, ci, co, ctx->p.mg_flags);
+        HMEC_CUDA(ctx, cudaEventRecord(sv.ev_coef[l], main));
+    }
     for (size_t l = 0; l < sv.lv.size(); l++) {
         Level& L = sv.lv[l];
-        if (l > 0) {
-            Level& F = sv.lv[l - 1];
-            CoefIn ci{F.af.ETA, F.af.GGG, F.af.RHO, F.af.ETAP, F.af.GGGP, F.af.ETAB, F.af.POR, F.af.GGGB,
-                      F.af.RHOX, F.af.RHOFX, F.af.PORX, F.af.ETADX, F.af.RHOY, F.af.RHOFY, F.af.PORY, F.af.ETADY};
-            AsmFields& a = L.af;
-            CoefOut co{(double*)a.ETA, (double*)a.GGG, (double*)a.RHO, (double*)a.ETAP, (double*)a.GGGP,
-                       (double*)a.ETAB, (double*)a.POR, (double*)a.GGGB, (double*)a.RHOX, (double*)a.RHOFX,
-                       (double*)a.PORX, (double*)a.ETADX, (double*)a.RHOY, (double*)a.RHOFY, (double*)a.PORY,
-                       (double*)a.ETADY};
-            const dim3 cg4(nblocks(L.g.Ny1, 64), L.g.Nx1, 4);  // z: basic, P, Vx, Vy sections
-            HMEC_LAUNCH(ctx, k_coarsen_coef, cg4, 64, 0, F.g, L.g, ci, co, ctx->p.mg_flags);
-            launch_assemble(ctx, L.g, L.af, L.col, L.val, L.dscale, nullptr, nullptr, nullptr);
-        }
+        StreamScope scope(ctx, sv.aux[l]);
+        HMEC_CUDA(ctx, cudaStreamWaitEvent(sv.aux[l], l == 0 ? sv.ev_fork : sv.ev_coef[l], 0));
+        if (l > 0) launch_assemble(ctx, L.g, L.af, L.col, L.val, L.dscale, nullptr, nullptr, nullptr);
+        HMEC_CUDA(ctx, cudaEventRecord(sv.ev_asm[l], sv.aux[l]));
         if (mixed)
             HMEC_LAUNCH(ctx, k_vanka_setup<float>, nblocks((long long)L.npatch * 16, VS_BS), VS_BS, 0, L.g, L.col,
                         L.val, L.pinv32, status);
@@ -1958,10 +2002,14 @@ int solver_setup(hmec_ctx* ctx) {
             HMEC_LAUNCH(ctx, k_stage_bpack<double>, nblocks(nb, 128), 128, 0, L.g, L.ntile_i, L.ntiles, L.tb_cap,
                         L.tbnd_start, L.tbnd_list, L.col, L.val, L.bpack, status);
         }
-        if (l > 0)
+        if (l > 0) {
+            HMEC_CUDA(ctx, cudaStreamWaitEvent(sv.aux[l], sv.ev_asm[l - 1], 0));
             HMEC_LAUNCH(ctx, k_restrict_scale, nblocks(L.g.N, 256), 256, 0, L.g.N, L.ridx, L.rwg,
                         sv.lv[l - 1].dscale, L.dscale, L.rw, L.rw32);
+        }
+        HMEC_CUDA(ctx, cudaEventRecord(sv.ev_done[l], sv.aux[l]));
     }
+    for (size_t l = 0; l < sv.lv.size(); l++) HMEC_CUDA(ctx, cudaStreamWaitEvent(main, sv.ev_done[l], 0));
     HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;
 }
