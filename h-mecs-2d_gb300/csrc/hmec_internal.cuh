@@ -147,7 +147,7 @@ struct Solver {
     double* w;
     double* H;             // (m+1) x m Hessenberg (device)
     double* cs; double* sn; double* gvec; double* yvec;
-    double* partial;       // block partial sums [(m+1) x nblk]
+    double* partial;       // block partial sums [(2m+3) x nblk]: both CGS passes and |w|^2
     double* dots;          // (m+1) reduced dot products
     double* bnorm;         // ||D b||
     int* done;             // convergence flag of the current solve

@@ -1425,24 +1425,27 @@ __device__ __forceinline__ void dots_partial(const double* __restrict__ V, const
     }
 }
 
-// block 0: h[k] = sum over blocks of partial[k][.], one warp per k
-__device__ __forceinline__ void dots_final(const double* __restrict__ partial, int nblk, int j, double* h) {
-    if (blockIdx.x != 0) return;
+// Every block: shh[k] = sum over blocks of partial[k][.], one warp per k, in
+// a fixed order (so all blocks hold identical coefficients and no grid
+// barrier is needed to share them); block 0 also stores them in h.
+__device__ __forceinline__ void dots_local(const double* __restrict__ partial, int nblk, int j, double* shh,
+                                           double* h) {
     const int lane = threadIdx.x & 31;
     for (int k = threadIdx.x >> 5; k <= j; k += ARN_BS / 32) {
         double a = 0;
         for (int b = lane; b < nblk; b += 32) a += partial[(size_t)k * nblk + b];
         for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-        if (lane == 0) h[k] = a;
+        if (lane == 0) {
+            shh[k] = a;
+            if (blockIdx.x == 0) h[k] = a;
+        }
     }
+    __syncthreads();
 }
 
-// w -= sum_k h[k] V_k; normp[block] = this block's part of |w|^2
-__device__ __forceinline__ void orth_update(const double* __restrict__ V, double* w, int N, int j,
-                                            const double* __restrict__ hg, double* normp, int nblk, double* sh,
-                                            double* shh) {
-    for (int k = threadIdx.x; k <= j; k += ARN_BS) shh[k] = hg[k];
-    __syncthreads();
+// w -= sum_k shh[k] V_k; normp[block] = this block's part of |w|^2
+__device__ __forceinline__ void orth_update(const double* __restrict__ V, double* w, int N, int j, double* normp,
+                                            int nblk, double* sh, const double* shh) {
     double a2 = 0;
     const int chunk = ((N + nblk - 1) / nblk + 31) / 32 * 32;
     const int r1 = min(N, (int)blockIdx.x * chunk + chunk);
@@ -1451,6 +1454,10 @@ __device__ __forceinline__ void orth_update(const double* __restrict__ V, double
         for (int k = 0; k <= j; k++) x -= shh[k] * V[(size_t)k * N + r];
         w[r] = x;
         a2 += x * x;
+    }
+    if (!normp) {
+        __syncthreads();
+        return;
     }
     const double s = block_sum(a2, sh);
     if (threadIdx.x == 0) normp[blockIdx.x] = s;
@@ -1468,7 +1475,6 @@ __global__ void __launch_bounds__(ARN_BS) k_arnoldi(ArnArgs<TZ> a) {
     // z_j and w = A z_j (rows in the block's contiguous range, as below)
     const int chunk = ((N + nblk - 1) / nblk + 31) / 32 * 32;
     const int rend = min(N, (int)blockIdx.x * chunk + chunk);
-    double n0 = 0;
     for (int r = blockIdx.x * chunk + threadIdx.x; r < rend; r += ARN_BS) {
         if ((const void*)a.zsrc != (const void*)a.Zj) a.Zj[r] = (double)a.zsrc[r];
         double acc = 0;
@@ -1478,53 +1484,39 @@ __global__ void __launch_bounds__(ARN_BS) k_arnoldi(ArnArgs<TZ> a) {
             acc += a.val[o] * (double)a.zsrc[a.col[o]];
         }
         a.w[r] = acc;
-        n0 += acc * acc;
     }
-    // rows m+1 and m of partial (unused by the dot products, k <= j < m):
-    // |A z|^2 and |w|^2 after the first pass
-    double* norm0 = a.partial + (size_t)(m + 1) * nblk;
-    double* norm1 = a.partial + (size_t)m * nblk;
-    {
-        const double s = block_sum(n0, sh);
-        if (threadIdx.x == 0) norm0[blockIdx.x] = s;
-    }
-    grid.sync();
-    // classical Gram-Schmidt (coefficients at dots[m+2..]) ...
+    // from here on a block reads and writes only its own rows of w
+    __syncthreads();
+    // classical Gram-Schmidt, two passes ("twice is enough"); the second
+    // pass's partials use rows m+1.. of partial, so the first pass's rows are
+    // not overwritten while slower blocks still read them, and |w|^2 goes to
+    // row 2m+2.  Three grid barriers: each pass's partials, then |w|.
+    double* part2 = a.partial + (size_t)(m + 1) * nblk;
+    double* normp = a.partial + (size_t)(2 * m + 2) * nblk;
     dots_partial(a.V, a.w, N, j, a.partial, nblk);
     grid.sync();
-    dots_final(a.partial, nblk, j, dots + m + 2);
+    dots_local(a.partial, nblk, j, shh, dots + m + 2);
+    orth_update(a.V, a.w, N, j, nullptr, nblk, sh, shh);
+    dots_partial(a.V, a.w, N, j, part2, nblk);
     grid.sync();
-    orth_update(a.V, a.w, N, j, dots + m + 2, norm1, nblk, sh, shh);
+    dots_local(part2, nblk, j, shh, dots);
+    orth_update(a.V, a.w, N, j, normp, nblk, sh, shh);
     grid.sync();
-    // ... repeated only when the first pass cancelled more than half of |w|
-    // ("twice is enough": |w1| < |w0| / sqrt 2); every block takes the same
-    // decision from the same fixed-order sums
-    __shared__ int reorth;
-    if (threadIdx.x < 32) {
-        const double s1 = warp_sum_fixed(norm1, nblk), s0 = warp_sum_fixed(norm0, nblk);
-        if (threadIdx.x == 0) reorth = !(s1 >= 0.5 * s0);
-    }
-    __syncthreads();
-    const double* normp = norm1;
-    if (reorth) {
-        dots_partial(a.V, a.w, N, j, a.partial, nblk);
-        grid.sync();
-        dots_final(a.partial, nblk, j, dots);
-        grid.sync();
-        orth_update(a.V, a.w, N, j, dots, a.partial, nblk, sh, shh);
-        grid.sync();
-        normp = a.partial;
-    } else if (blockIdx.x == 0) {
-        for (int k = threadIdx.x; k <= j; k += ARN_BS) dots[k] = 0;  // no second-pass coefficients
-        __syncthreads();
-    }
     if (blockIdx.x == 0 && threadIdx.x < 32)
         arnoldi_update(a.G, dots + m + 2, normp, nblk, j, m, a.rtol, dots + 2 * m + 3);
-    grid.sync();
-    // V_{j+1} = w / |w| (written whether or not this step converged)
-    const double sc = dots[2 * m + 3];
+    // V_{j+1} = w / |w| (written whether or not this step converged): every
+    // block forms |w| from the same partials in the same order as
+    // arnoldi_update and scales the rows it updated itself, so no grid
+    // barrier is needed
+    __shared__ double s_sc;
+    if (threadIdx.x < 32) {
+        const double hn = sqrt(warp_sum_fixed(normp, nblk));
+        if (threadIdx.x == 0) s_sc = hn > 0 ? 1.0 / hn : 0.0;
+    }
+    __syncthreads();
+    const double sc = s_sc;
     double* Vn = a.V + (size_t)(j + 1) * N;
-    for (int r = blockIdx.x * ARN_BS + threadIdx.x; r < N; r += nblk * ARN_BS) {
+    for (int r = blockIdx.x * chunk + threadIdx.x; r < rend; r += ARN_BS) {
         const double v = a.w[r] * sc;
         Vn[r] = v;
         if (a.next32) a.next32[r] = (float)v;
@@ -1862,7 +1854,7 @@ int solver_alloc(hmec_ctx* ctx) {
     HMEC_CUDA(ctx, cudaMalloc(&sv.sn, sizeof(double) * (m + 1)));
     HMEC_CUDA(ctx, cudaMalloc(&sv.gvec, sizeof(double) * (m + 2)));
     HMEC_CUDA(ctx, cudaMalloc(&sv.yvec, sizeof(double) * (m + 1)));
-    HMEC_CUDA(ctx, cudaMalloc(&sv.partial, sizeof(double) * (m + 2) * (size_t)sv.nblk));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.partial, sizeof(double) * (2 * m + 3) * (size_t)sv.nblk));
     HMEC_CUDA(ctx, cudaMalloc(&sv.dots, sizeof(double) * (2 * m + 4)));
     HMEC_CUDA(ctx, cudaMalloc(&sv.bnorm, sizeof(double) * 2));
     HMEC_CUDA(ctx, cudaMalloc(&sv.done, sizeof(int) * 2));
