@@ -943,7 +943,10 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(const __grid_consta
             }
             __syncthreads();
         }
-        if (!solo) cg::this_grid().sync();
+        // the last sweep needs the barrier only when this launch reads the
+        // result back: the residual restriction, or a copy into x
+        const bool last_in_x = s == nsweeps - 1 && dst == t.x && !t.bc;
+        if (!solo && !last_in_x) cg::this_grid().sync();
         src = dst;
         dst = (dst == t.xalt) ? t.x : t.xalt;
     }
