@@ -161,6 +161,13 @@ struct Solver {
     std::vector<cudaStream_t> aux;
     std::vector<cudaEvent_t> ev_coef, ev_asm, ev_done;
     cudaEvent_t ev_fork = nullptr;
+    // the mixed form's V-cycle as one launch: its pass table in device
+    // memory (built once: it holds only the levels' fixed buffers), launch
+    // shape and algorithmic bytes; state 0 unbuilt, 1 in use, -1 per-level
+    // launches instead
+    void* vpass = nullptr;
+    int vpass_state = 0, vpass_n = 0, vpass_grid = 0, vpass_smem = 0, vpass_whole = 0, vpass_cap = 0;
+    double vpass_bytes = 0;
 };
 
 // Live timing of one kernel family (bench.py roofline): CUDA events around

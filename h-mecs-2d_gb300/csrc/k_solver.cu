@@ -766,18 +766,37 @@ __host__ __device__ __forceinline__ int lane_meta(int c, int lanetid, int i0, in
     return (1 << 30) | (lp << 22) | (rl << 11) | lrow;
 }
 
-// WHOLE: the inverse mode (one instantiation each keeps the code small).
+// The TMA barriers of a smoothing block and their phase counters, kept across
+// the passes of one launch.
+struct StageBars {
+    unsigned long long* bar;  // [0], [1]: per-colour inverses (streamed mode); [2]: a tile's stage
+    unsigned use0, use1, use2;
+};
+
+__device__ __forceinline__ void stage_bars_init(unsigned long long* bar) {
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init(&bar[2], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+}
+
+// One smoothing pass of one level (nsweeps sweeps, then the optional
+// restriction), run by every block of the launch.  t lives in kernel
+// parameter space or in global memory (its tensor maps are read from where
+// it lives).  Lo: the launch's shared-memory layout, sized for at least this
+// level's boundary-row capacity.  WHOLE: the inverse mode.
 template <typename T, bool WHOLE>
-__global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(const __grid_constant__ StageArgs<T> t, int nsweeps,
-                                                             int mode) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    const StageLayout Lo = stage_layout<T>(WHOLE ? 1 : 0, t.tb_cap);
+__device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, int mode, unsigned char* smem_raw,
+                                           const StageLayout& Lo, StageBars& sb_) {
     T* xs = reinterpret_cast<T*>(smem_raw + Lo.xs);
     T* sval = reinterpret_cast<T*>(smem_raw + Lo.val);
     T* sb = reinterpret_cast<T*>(smem_raw + Lo.b);
     int16_t* soff = reinterpret_cast<int16_t*>(smem_raw + Lo.off);
     unsigned char* own = smem_raw + Lo.own;
-    unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem_raw + Lo.bar);
+    unsigned long long* bar = sb_.bar;
     T* pv = reinterpret_cast<T*>(smem_raw + Lo.pv);
     const int TBC = t.tb_cap;
     unsigned char* pack = smem_raw + Lo.pack;  // the pack layout of k_stage_bpack
@@ -790,21 +809,11 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(const __grid_consta
     constexpr bool whole = WHOLE;
     const Geo& g = t.g;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-    // a V-cycle launched after the solve converged (the host looks at the
-    // flag only every few iterations) does no work; no kernel of a V-cycle
-    // writes the flag, so every block sees the same value
-    if (*t.done) return;
-    // bar[0], bar[1]: per-colour inverses (streamed mode); bar[2]: a tile's stage
-    if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        mbar_init(&bar[2], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    __syncthreads();
     const int lane = threadIdx.x & 31, q = lane & 15, slot = threadIdx.x >> 4;
     const int warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    unsigned use0 = 0, use1 = 0, use2 = 0;
+    unsigned& use0 = sb_.use0;
+    unsigned& use1 = sb_.use1;
+    unsigned& use2 = sb_.use2;
     int staged = -1, nbt = 0;
     int meta[9];  // lane_meta of this thread for the staged tile
 #pragma unroll
@@ -954,6 +963,56 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(const __grid_consta
     if (src != t.x)
         for (int r = tid; r < g.N; r += nth) t.x[r] = src[r];
     if (t.bc) restrict_resid(t.nc, t.ridx, t.rw, g.N, t.col, t.val, t.b, src, t.bc, tid, nth);
+}
+
+// One smoothing pass as its own cooperative launch.
+template <typename T, bool WHOLE>
+__global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(const __grid_constant__ StageArgs<T> t, int nsweeps,
+                                                             int mode) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    // a V-cycle launched after the solve converged (the host looks at the
+    // flag only now and then) does no work; no kernel of a V-cycle writes
+    // the flag, so every block sees the same value
+    if (*t.done) return;
+    const StageLayout Lo = stage_layout<T>(WHOLE ? 1 : 0, t.tb_cap);
+    StageBars sb{reinterpret_cast<unsigned long long*>(smem_raw + Lo.bar), 0, 0, 0};
+    stage_bars_init(sb.bar);
+    stage_pass<T, WHOLE>(t, nsweeps, mode, smem_raw, Lo, sb);
+}
+
+// A whole V-cycle's smoothing passes in one cooperative launch: pass p of
+// the table (global memory, tensor maps included) with a grid barrier
+// between passes -- the pre-smoothing passes down the levels (each
+// restricting its residual into the next level's rhs), the coarsest level's
+// sweeps, and the post-smoothing passes back up (each adding the coarser
+// correction).  cap: the largest boundary-row capacity of the levels (the
+// shared-memory layout); done: the solve's convergence flag.
+template <typename T>
+struct VPass {
+    StageArgs<T> a;
+    int nsweeps, mode;
+};
+
+template <typename T, bool WHOLE>
+__global__ void __launch_bounds__(TILE_BS, 2) k_vcycle_stage(const VPass<T>* __restrict__ pass, int npass, int cap,
+                                                             const int* done) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    if (*done) return;
+    const StageLayout Lo = stage_layout<T>(WHOLE ? 1 : 0, cap);
+    StageBars sb{reinterpret_cast<unsigned long long*>(smem_raw + Lo.bar), 0, 0, 0};
+    // the tensor maps were written to global memory by a copy: make them
+    // visible to the tensor-map proxy of the thread that issues the copies
+    if (threadIdx.x == 0)
+        for (int p = 0; p < npass; p++) {
+            const CUtensorMap* m3[3] = {&pass[p].a.tm_val, &pass[p].a.tm_off, &pass[p].a.tm_pinv};
+            for (int k = 0; k < 3; k++)
+                asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(m3[k]) : "memory");
+        }
+    stage_bars_init(sb.bar);
+    for (int p = 0; p < npass; p++) {
+        if (p > 0) cg::this_grid().sync();
+        stage_pass<T, WHOLE>(pass[p].a, pass[p].nsweeps, pass[p].mode, smem_raw, Lo, sb);
+    }
 }
 
 // ------------------------------------------------ multigrid restriction
@@ -1923,6 +1982,9 @@ void solver_free(hmec_ctx* ctx) {
     sv.ev_asm.clear();
     sv.ev_done.clear();
     sv.ev_fork = nullptr;
+    cudaFree(sv.vpass);
+    sv.vpass = nullptr;
+    sv.vpass_state = 0;
     cudaFree(sv.V);
     cudaFree(sv.Z);
     cudaFree(sv.w);
@@ -2095,6 +2157,58 @@ float* x_alt<float>(Level& L) {
     return L.fx2;
 }
 
+// The staged pass's arguments for level l (its stage_config done); *ab gets
+// the pass's algorithmic bytes: per sweep the level's matrix (values and
+// int16 window offsets), every inverse, the unknowns read and written and the
+// rhs; the prolonged correction; the fused residual (one pass over the
+// matrix, x and b) and restriction.
+template <typename T>
+static StageArgs<T> stage_args(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mode, bool restrict_next,
+                               double* ab) {
+    Solver& sv = ctx->sv;
+    Level& L = sv.lv[l];
+    StageArgs<T> t;
+    t.tm_val = L.tm_val;
+    t.tm_off = L.tm_off;
+    t.tm_pinv = L.tm_pinv;
+    t.g = L.g;
+    t.col = L.col;
+    t.val = LvPtr<T>::val(L);
+    t.pinv = LvPtr<T>::pinv(L);
+    t.b = b;
+    t.x = x;
+    t.xalt = x_alt<T>(L);
+    t.tb_start = L.tbnd_start;
+    t.own_t = L.own_t;
+    t.meta_t = L.meta_t;
+    t.bpack = L.bpack;
+    t.ntile_i = L.ntile_i;
+    t.ntiles = L.ntiles;
+    t.gc = (mode == 1) ? sv.lv[l + 1].g : L.g;
+    t.xc = (mode == 1) ? LvPtr<T>::x(sv.lv[l + 1]) : nullptr;
+    t.pmx = L.pmx;
+    t.pmy = L.pmy;
+    t.nc = 0;
+    t.ridx = nullptr;
+    t.rw = nullptr;
+    t.bc = nullptr;
+    t.tb_cap = L.tb_cap;
+    t.status = &ctx->ds->status;
+    t.done = sv.done;
+    const double st = sizeof(T), N = L.g.N;
+    *ab = nsweeps * (N * HMEC_W * (st + 2) + (double)L.npatch * 100.0 * st + 3.0 * N * st) +
+          (mode ? N * st * 1.5 : 0.0);
+    if (restrict_next) {
+        Level& C = sv.lv[l + 1];
+        t.nc = C.g.N;
+        t.ridx = C.ridx;
+        t.rw = LvPtr<T>::rw(C);
+        t.bc = LvPtr<T>::b(C);
+        *ab += N * HMEC_W * (st + 4) + 2.0 * N * st + (double)C.g.N * (HMEC_RW * (st + 4) + st);
+    }
+    return t;
+}
+
 // One smoothing pass on level l (x = 0 or x += P xc first, then nsweeps
 // sweeps).  restrict_next (tiled pass): also restrict the residual into the
 // next coarser level's rhs in the same launch.
@@ -2127,51 +2241,10 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
         return HMEC_OK;
     }
     if (!(ctx->p.mg_flags & HMEC_MG_UNTILED)) {
-        StageArgs<T> t;
-        t.tm_val = L.tm_val;
-        t.tm_off = L.tm_off;
-        t.tm_pinv = L.tm_pinv;
-        t.g = L.g;
-        t.col = L.col;
-        t.val = LvPtr<T>::val(L);
-        t.pinv = LvPtr<T>::pinv(L);
-        t.b = b;
-        t.x = x;
-        t.xalt = x_alt<T>(L);
-        t.tb_start = L.tbnd_start;
-        t.own_t = L.own_t;
-        t.meta_t = L.meta_t;
-        t.bpack = L.bpack;
-        t.ntile_i = L.ntile_i;
-        t.ntiles = L.ntiles;
-        t.gc = a.gc;
-        t.xc = a.xc;
-        t.pmx = L.pmx;
-        t.pmy = L.pmy;
-        t.nc = 0;
-        t.ridx = nullptr;
-        t.rw = nullptr;
-        t.bc = nullptr;
-        t.status = &ctx->ds->status;
-        t.done = sv.done;
-        // algorithmic bytes: per sweep the level's matrix (values and int16
-        // window offsets), every inverse, the unknowns read and written and
-        // the rhs; the prolonged correction; the fused residual (one pass
-        // over the matrix, x and b) and restriction
-        const double N = L.g.N;
-        double ab = nsweeps * (N * HMEC_W * (st + 2) + (double)L.npatch * 100.0 * st + 3.0 * N * st) +
-                    (mode ? N * st * 1.5 : 0.0);
-        if (restrict_next) {
-            Level& C = sv.lv[l + 1];
-            t.nc = C.g.N;
-            t.ridx = C.ridx;
-            t.rw = LvPtr<T>::rw(C);
-            t.bc = LvPtr<T>::b(C);
-            ab += N * HMEC_W * (st + 4) + 2.0 * N * st + (double)C.g.N * (HMEC_RW * (st + 4) + st);
-        }
         int rc = stage_config<T>(ctx, L);
         if (rc) return rc;
-        t.tb_cap = L.tb_cap;
+        double ab = 0;
+        StageArgs<T> t = stage_args<T>(ctx, l, b, x, nsweeps, mode, restrict_next, &ab);
         void* args[] = {&t, &nsweeps, &mode};
         // live timing by name prefix: "k_smooth" is every level, "k_smooth<l>" one
         static const char* const lname[8] = {"k_smooth0", "k_smooth1", "k_smooth2", "k_smooth3",
@@ -2207,9 +2280,88 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
     return HMEC_OK;
 }
 
+// The mixed form's whole V-cycle (on the fine level's own buffers) as one
+// k_vcycle_stage launch.  *used is false when it does not apply -- untiled
+// smoothing, one level, levels in different inverse modes, or a grid that
+// cannot be co-resident -- and the caller launches level by level.
+static int vcycle_fused(hmec_ctx* ctx, bool* used) {
+    Solver& sv = ctx->sv;
+    const hmec_params& p = ctx->p;
+    *used = false;
+    const size_t nl = sv.lv.size();
+    if (sv.vpass_state < 0) return HMEC_OK;
+    if (sv.vpass_state == 0) {
+        sv.vpass_state = -1;
+        if (nl < 2 || (p.mg_flags & HMEC_MG_UNTILED)) return HMEC_OK;
+        int whole = -1, grid = 0, cap = 0;
+        for (size_t l = 0; l < nl; l++) {
+            int rc = stage_config<float>(ctx, sv.lv[l]);
+            if (rc) return rc;
+            if (whole >= 0 && sv.lv[l].st_whole != whole) return HMEC_OK;
+            whole = sv.lv[l].st_whole;
+            grid = std::max(grid, sv.lv[l].st_grid);
+            cap = std::max(cap, sv.lv[l].tb_cap);
+        }
+        const int smem = stage_layout<float>(whole, cap).total;
+        const void* kern = whole ? (const void*)k_vcycle_stage<float, true> : (const void*)k_vcycle_stage<float, false>;
+        int optin = 0, nsm = 0, per_sm = 0;
+        HMEC_CUDA(ctx, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->dev));
+        HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
+        if (smem > optin) return HMEC_OK;
+        HMEC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TILE_BS, (size_t)smem));
+        if (grid < 1 || grid > per_sm * nsm) return HMEC_OK;
+        // pre-smoothing down the levels, the coarsest level, post-smoothing up
+        std::vector<VPass<float>> ps;
+        double bytes = 0, ab = 0;
+        for (size_t l = 0; l + 1 < nl; l++) {
+            Level& L = sv.lv[l];
+            ps.push_back({stage_args<float>(ctx, l, L.fb, L.fx, p.mg_pre, 0, true, &ab), p.mg_pre, 0});
+            bytes += ab;
+        }
+        {
+            Level& L = sv.lv[nl - 1];
+            const int ns = std::max(1, p.mg_coarse_sweeps);
+            ps.push_back({stage_args<float>(ctx, nl - 1, L.fb, L.fx, ns, 0, false, &ab), ns, 0});
+            bytes += ab;
+        }
+        for (size_t l = nl - 1; l-- > 0;) {
+            Level& L = sv.lv[l];
+            ps.push_back({stage_args<float>(ctx, l, L.fb, L.fx, p.mg_post, 1, false, &ab), p.mg_post, 1});
+            bytes += ab;
+        }
+        HMEC_CUDA(ctx, cudaMalloc(&sv.vpass, sizeof(VPass<float>) * ps.size()));
+        HMEC_CUDA(ctx, cudaMemcpy(sv.vpass, ps.data(), sizeof(VPass<float>) * ps.size(), cudaMemcpyHostToDevice));
+        sv.vpass_n = (int)ps.size();
+        sv.vpass_grid = grid;
+        sv.vpass_smem = smem;
+        sv.vpass_whole = whole;
+        sv.vpass_cap = cap;
+        sv.vpass_bytes = bytes;
+        sv.vpass_state = 1;
+    }
+    void* args[] = {&sv.vpass, &sv.vpass_n, &sv.vpass_cap, &sv.done};
+    const void* kern =
+        sv.vpass_whole ? (const void*)k_vcycle_stage<float, true> : (const void*)k_vcycle_stage<float, false>;
+    const bool prof = hmec_prof_begin(ctx, "k_smooth_vcycle", sv.vpass_bytes);
+    HMEC_CUDA(ctx, cudaLaunchCooperativeKernel(kern, dim3(sv.vpass_grid), dim3(TILE_BS), args, (size_t)sv.vpass_smem,
+                                               ctx->stream));
+    ctx->launches++;
+    if (prof) hmec_prof_end(ctx);
+    *used = true;
+    return HMEC_OK;
+}
+
 // V-cycle on level l for A x = b, x = 0 on entry (b, x default to the level's buffers).
 template <typename T>
 static int vcycle(hmec_ctx* ctx, size_t l, const T* b_in = nullptr, T* x_in = nullptr) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (l == 0 && !b_in && !x_in) {
+            bool used = false;
+            const int rc = vcycle_fused(ctx, &used);
+            if (rc || used) return rc;
+        }
+    }
     Solver& sv = ctx->sv;
     Level& L = sv.lv[l];
     const hmec_params& p = ctx->p;
