@@ -161,8 +161,8 @@ struct Solver {
     std::vector<cudaStream_t> aux;
     std::vector<cudaEvent_t> ev_coef, ev_asm, ev_done;
     cudaEvent_t ev_fork = nullptr;
-    // the mixed form's V-cycle as one launch: its pass table in device
-    // memory (built once: it holds only the levels' fixed buffers), launch
+    // the mixed form's V-cycle as one launch: its pass table (the kernel
+    // parameter, built once: it holds only the levels' fixed buffers), launch
     // shape and algorithmic bytes; state 0 unbuilt, 1 in use, -1 per-level
     // launches instead
     void* vpass = nullptr;

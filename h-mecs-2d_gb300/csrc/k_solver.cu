@@ -981,7 +981,7 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(const __grid_consta
 }
 
 // A whole V-cycle's smoothing passes in one cooperative launch: pass p of
-// the table (global memory, tensor maps included) with a grid barrier
+// the table (a kernel parameter, tensor maps included) with a grid barrier
 // between passes -- the pre-smoothing passes down the levels (each
 // restricting its residual into the next level's rhs), the coarsest level's
 // sweeps, and the post-smoothing passes back up (each adding the coarser
@@ -992,26 +992,24 @@ struct VPass {
     StageArgs<T> a;
     int nsweeps, mode;
 };
+constexpr int MAX_VPASS = 11;  // six levels
+template <typename T>
+struct VTable {
+    VPass<T> p[MAX_VPASS];
+    int npass, cap;
+    const int* done;
+};
 
 template <typename T, bool WHOLE>
-__global__ void __launch_bounds__(TILE_BS, 2) k_vcycle_stage(const VPass<T>* __restrict__ pass, int npass, int cap,
-                                                             const int* done) {
+__global__ void __launch_bounds__(TILE_BS, 2) k_vcycle_stage(const __grid_constant__ VTable<T> v) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    if (*done) return;
-    const StageLayout Lo = stage_layout<T>(WHOLE ? 1 : 0, cap);
+    if (*v.done) return;
+    const StageLayout Lo = stage_layout<T>(WHOLE ? 1 : 0, v.cap);
     StageBars sb{reinterpret_cast<unsigned long long*>(smem_raw + Lo.bar), 0, 0, 0};
-    // the tensor maps were written to global memory by a copy: make them
-    // visible to the tensor-map proxy of the thread that issues the copies
-    if (threadIdx.x == 0)
-        for (int p = 0; p < npass; p++) {
-            const CUtensorMap* m3[3] = {&pass[p].a.tm_val, &pass[p].a.tm_off, &pass[p].a.tm_pinv};
-            for (int k = 0; k < 3; k++)
-                asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(m3[k]) : "memory");
-        }
     stage_bars_init(sb.bar);
-    for (int p = 0; p < npass; p++) {
+    for (int p = 0; p < v.npass; p++) {
         if (p > 0) cg::this_grid().sync();
-        stage_pass<T, WHOLE>(pass[p].a, pass[p].nsweeps, pass[p].mode, smem_raw, Lo, sb);
+        stage_pass<T, WHOLE>(v.p[p].a, v.p[p].nsweeps, v.p[p].mode, smem_raw, Lo, sb);
     }
 }
 
@@ -1982,7 +1980,7 @@ void solver_free(hmec_ctx* ctx) {
     sv.ev_asm.clear();
     sv.ev_done.clear();
     sv.ev_fork = nullptr;
-    cudaFree(sv.vpass);
+    delete static_cast<VTable<float>*>(sv.vpass);
     sv.vpass = nullptr;
     sv.vpass_state = 0;
     cudaFree(sv.V);
@@ -2330,8 +2328,14 @@ static int vcycle_fused(hmec_ctx* ctx, bool* used) {
             ps.push_back({stage_args<float>(ctx, l, L.fb, L.fx, p.mg_post, 1, false, &ab), p.mg_post, 1});
             bytes += ab;
         }
-        HMEC_CUDA(ctx, cudaMalloc(&sv.vpass, sizeof(VPass<float>) * ps.size()));
-        HMEC_CUDA(ctx, cudaMemcpy(sv.vpass, ps.data(), sizeof(VPass<float>) * ps.size(), cudaMemcpyHostToDevice));
+        if ((int)ps.size() > MAX_VPASS) return HMEC_OK;
+        VTable<float>* tab = new (std::nothrow) VTable<float>();
+        if (!tab) return HMEC_OK;
+        for (size_t k = 0; k < ps.size(); k++) tab->p[k] = ps[k];
+        tab->npass = (int)ps.size();
+        tab->cap = cap;
+        tab->done = sv.done;
+        sv.vpass = tab;
         sv.vpass_n = (int)ps.size();
         sv.vpass_grid = grid;
         sv.vpass_smem = smem;
@@ -2340,7 +2344,7 @@ static int vcycle_fused(hmec_ctx* ctx, bool* used) {
         sv.vpass_bytes = bytes;
         sv.vpass_state = 1;
     }
-    void* args[] = {&sv.vpass, &sv.vpass_n, &sv.vpass_cap, &sv.done};
+    void* args[] = {sv.vpass};
     const void* kern =
         sv.vpass_whole ? (const void*)k_vcycle_stage<float, true> : (const void*)k_vcycle_stage<float, false>;
     const bool prof = hmec_prof_begin(ctx, "k_smooth_vcycle", sv.vpass_bytes);
