@@ -1980,7 +1980,10 @@ void solver_free(hmec_ctx* ctx) {
     sv.ev_asm.clear();
     sv.ev_done.clear();
     sv.ev_fork = nullptr;
-    delete static_cast<VTable<float>*>(sv.vpass);
+    if (ctx->p.form == HMEC_FORM_MIXED)
+        delete static_cast<VTable<float>*>(sv.vpass);
+    else
+        delete static_cast<VTable<double>*>(sv.vpass);
     sv.vpass = nullptr;
     sv.vpass_state = 0;
     cudaFree(sv.V);
@@ -2278,11 +2281,14 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
     return HMEC_OK;
 }
 
-// The mixed form's whole V-cycle (on the fine level's own buffers) as one
-// k_vcycle_stage launch.  *used is false when it does not apply -- untiled
-// smoothing, one level, levels in different inverse modes, or a grid that
-// cannot be co-resident -- and the caller launches level by level.
-static int vcycle_fused(hmec_ctx* ctx, bool* used) {
+// A whole V-cycle for A x = b on the fine level as one k_vcycle_stage
+// launch.  *used is false when it does not apply -- untiled smoothing, one
+// level, levels in different inverse modes, or a grid that cannot be
+// co-resident -- and the caller launches level by level.  The pass table is
+// built once; only the fine level's b and x (the FP64 form's Krylov vectors)
+// are set per call, in the parameter copy the launch takes.
+template <typename T>
+static int vcycle_fused(hmec_ctx* ctx, const T* b0, T* x0, bool* used) {
     Solver& sv = ctx->sv;
     const hmec_params& p = ctx->p;
     *used = false;
@@ -2293,15 +2299,15 @@ static int vcycle_fused(hmec_ctx* ctx, bool* used) {
         if (nl < 2 || (p.mg_flags & HMEC_MG_UNTILED)) return HMEC_OK;
         int whole = -1, grid = 0, cap = 0;
         for (size_t l = 0; l < nl; l++) {
-            int rc = stage_config<float>(ctx, sv.lv[l]);
+            int rc = stage_config<T>(ctx, sv.lv[l]);
             if (rc) return rc;
             if (whole >= 0 && sv.lv[l].st_whole != whole) return HMEC_OK;
             whole = sv.lv[l].st_whole;
             grid = std::max(grid, sv.lv[l].st_grid);
             cap = std::max(cap, sv.lv[l].tb_cap);
         }
-        const int smem = stage_layout<float>(whole, cap).total;
-        const void* kern = whole ? (const void*)k_vcycle_stage<float, true> : (const void*)k_vcycle_stage<float, false>;
+        const int smem = stage_layout<T>(whole, cap).total;
+        const void* kern = whole ? (const void*)k_vcycle_stage<T, true> : (const void*)k_vcycle_stage<T, false>;
         int optin = 0, nsm = 0, per_sm = 0;
         HMEC_CUDA(ctx, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->dev));
         HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
@@ -2310,26 +2316,26 @@ static int vcycle_fused(hmec_ctx* ctx, bool* used) {
         HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TILE_BS, (size_t)smem));
         if (grid < 1 || grid > per_sm * nsm) return HMEC_OK;
         // pre-smoothing down the levels, the coarsest level, post-smoothing up
-        std::vector<VPass<float>> ps;
+        std::vector<VPass<T>> ps;
         double bytes = 0, ab = 0;
         for (size_t l = 0; l + 1 < nl; l++) {
             Level& L = sv.lv[l];
-            ps.push_back({stage_args<float>(ctx, l, L.fb, L.fx, p.mg_pre, 0, true, &ab), p.mg_pre, 0});
+            ps.push_back({stage_args<T>(ctx, l, LvPtr<T>::b(L), LvPtr<T>::x(L), p.mg_pre, 0, true, &ab), p.mg_pre, 0});
             bytes += ab;
         }
         {
             Level& L = sv.lv[nl - 1];
             const int ns = std::max(1, p.mg_coarse_sweeps);
-            ps.push_back({stage_args<float>(ctx, nl - 1, L.fb, L.fx, ns, 0, false, &ab), ns, 0});
+            ps.push_back({stage_args<T>(ctx, nl - 1, LvPtr<T>::b(L), LvPtr<T>::x(L), ns, 0, false, &ab), ns, 0});
             bytes += ab;
         }
         for (size_t l = nl - 1; l-- > 0;) {
             Level& L = sv.lv[l];
-            ps.push_back({stage_args<float>(ctx, l, L.fb, L.fx, p.mg_post, 1, false, &ab), p.mg_post, 1});
+            ps.push_back({stage_args<T>(ctx, l, LvPtr<T>::b(L), LvPtr<T>::x(L), p.mg_post, 1, false, &ab), p.mg_post, 1});
             bytes += ab;
         }
         if ((int)ps.size() > MAX_VPASS) return HMEC_OK;
-        VTable<float>* tab = new (std::nothrow) VTable<float>();
+        VTable<T>* tab = new (std::nothrow) VTable<T>();
         if (!tab) return HMEC_OK;
         for (size_t k = 0; k < ps.size(); k++) tab->p[k] = ps[k];
         tab->npass = (int)ps.size();
@@ -2344,9 +2350,14 @@ static int vcycle_fused(hmec_ctx* ctx, bool* used) {
         sv.vpass_bytes = bytes;
         sv.vpass_state = 1;
     }
-    void* args[] = {sv.vpass};
+    VTable<T>* tab = static_cast<VTable<T>*>(sv.vpass);
+    tab->p[0].a.b = b0;  // the fine level's pre- and post-smoothing passes
+    tab->p[0].a.x = x0;
+    tab->p[sv.vpass_n - 1].a.b = b0;
+    tab->p[sv.vpass_n - 1].a.x = x0;
+    void* args[] = {tab};
     const void* kern =
-        sv.vpass_whole ? (const void*)k_vcycle_stage<float, true> : (const void*)k_vcycle_stage<float, false>;
+        sv.vpass_whole ? (const void*)k_vcycle_stage<T, true> : (const void*)k_vcycle_stage<T, false>;
     const bool prof = hmec_prof_begin(ctx, "k_smooth_vcycle", sv.vpass_bytes);
     HMEC_CUDA(ctx, cudaLaunchCooperativeKernel(kern, dim3(sv.vpass_grid), dim3(TILE_BS), args, (size_t)sv.vpass_smem,
                                                ctx->stream));
@@ -2359,12 +2370,14 @@ static int vcycle_fused(hmec_ctx* ctx, bool* used) {
 // V-cycle on level l for A x = b, x = 0 on entry (b, x default to the level's buffers).
 template <typename T>
 static int vcycle(hmec_ctx* ctx, size_t l, const T* b_in = nullptr, T* x_in = nullptr) {
-    if constexpr (std::is_same<T, float>::value) {
-        if (l == 0 && !b_in && !x_in) {
-            bool used = false;
-            const int rc = vcycle_fused(ctx, &used);
-            if (rc || used) return rc;
-        }
+    // one launch per V-cycle for the FP32 smoother; the FP64 form (streamed
+    // inverses) measured faster with a launch per pass (33.3 vs 32.7 ms per
+    // 201x201 step), so it keeps those
+    if (l == 0 && std::is_same<T, float>::value) {
+        Level& F = ctx->sv.lv[0];
+        bool used = false;
+        const int rc = vcycle_fused<T>(ctx, b_in ? b_in : LvPtr<T>::b(F), x_in ? x_in : LvPtr<T>::x(F), &used);
+        if (rc || used) return rc;
     }
     Solver& sv = ctx->sv;
     Level& L = sv.lv[l];
