@@ -2296,7 +2296,7 @@ static int vcycle_fused(hmec_ctx* ctx, const T* b0, T* x0, bool* used) {
     if (sv.vpass_state < 0) return HMEC_OK;
     if (sv.vpass_state == 0) {
         sv.vpass_state = -1;
-        if (nl < 2 || (p.mg_flags & HMEC_MG_UNTILED)) return HMEC_OK;
+        if (nl < 2 || (p.mg_flags & (HMEC_MG_UNTILED | HMEC_MG_PASS_LAUNCHES))) return HMEC_OK;
         int whole = -1, grid = 0, cap = 0;
         for (size_t l = 0; l < nl; l++) {
             int rc = stage_config<T>(ctx, sv.lv[l]);
@@ -2312,7 +2312,10 @@ static int vcycle_fused(hmec_ctx* ctx, const T* b0, T* x0, bool* used) {
         HMEC_CUDA(ctx, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->dev));
         HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
         if (smem > optin) return HMEC_OK;
-        HMEC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        // the device maximum, not this model's size: the attribute belongs to
+        // the kernel, and concurrent models (ensembles) launch it with
+        // different layouts
+        HMEC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
         HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TILE_BS, (size_t)smem));
         if (grid < 1 || grid > per_sm * nsm) return HMEC_OK;
         // pre-smoothing down the levels, the coarsest level, post-smoothing up

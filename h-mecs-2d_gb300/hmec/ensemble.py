@@ -10,15 +10,20 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 
-from . import Model, default_params, synth
+from . import MG_PASS_LAUNCHES, Model, default_params, synth
 
 
 class Ensemble:
     def __init__(self, members, **common):
-        """members: (overrides, material, seed) triples, e.g. synth.ensemble_members()."""
+        """members: (overrides, material, seed) triples, e.g. synth.ensemble_members().
+
+        The members smooth with one launch per multigrid pass (not one per
+        V-cycle), so that the small coarse passes of different members can
+        share the GPU."""
         self.models = []
         for over, mat, seed in members:
             p = default_params(**dict(over, **common))
+            p.mg_flags |= MG_PASS_LAUNCHES
             m = Model(p)
             mk, nodes = synth.instance_state(p, mat, seed)
             m.upload_markers(mk)

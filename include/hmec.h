@@ -113,7 +113,12 @@ enum hmec_mg_flags {
      * (a true multiplicative sweep over the whole level) instead of the
      * default tiled sweep (multiplicative inside 12x12-patch tiles, the
      * neighbours' unknowns taken from the start of the sweep). */
-    HMEC_MG_UNTILED = 2
+    HMEC_MG_UNTILED = 2,
+    /* One cooperative launch per smoothing pass instead of one per V-cycle.
+     * The fused V-cycle holds its fine level's grid through the small coarse
+     * levels too; models that share the GPU concurrently (ensembles) keep
+     * the per-pass launches so their coarse passes can run side by side. */
+    HMEC_MG_PASS_LAUNCHES = 4
 };
 
 /* ------------------------------------------------------------- node fields */
