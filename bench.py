@@ -291,9 +291,14 @@ def run_gpu(args, rank, world, device_index):
         m3.load_state(snap)
         m3.timestep()
         err = {}
+        got = {f: m3.field(f) for f in fp64_next}
         for f, b in fp64_next.items():
             den = float(np.max(np.abs(b))) or 1.0
-            err[f] = float(np.max(np.abs(m3.field(f) - b))) / den
+            err[f] = float(np.max(np.abs(got[f] - b))) / den
+        # the velocity field as one quantity (as the parity tests group it):
+        # vys alone is small in this simple-shear setup
+        den = max(float(np.max(np.abs(fp64_next[f]))) for f in ("vxs", "vys")) or 1.0
+        err["velocity"] = max(float(np.max(np.abs(got[f] - fp64_next[f]))) for f in ("vxs", "vys")) / den
         dt_equal = m3.scalar("dt") == dt64
         m3.close()
         out["fp64"] = dict(ms=ms2, gi=sum(r["global_iters"] for r in reps2), kr=sum(r["krylov_iters"] for r in reps2),
@@ -463,7 +468,7 @@ def main():
                              "global_iters_per_step": f["gi"] / K, "krylov_iters_per_step": f["kr"] / K,
                              "mixed_vs_fp64_max_rel_err": f["err"], "same_dt": f["dt_equal"],
                              "err_note": "one timestep from the same state in both forms, max |mixed - fp64| / "
-                                         "max |fp64| per field"}
+                                         "max |fp64| per field; 'velocity' over vxs and vys together"}
         line["speedup_mixed_vs_fp64"] = value / line["fp64_form"]["value"]
     if "e2e" in out:
         e = out["e2e"]
