@@ -607,7 +607,31 @@ __global__ void k_node_vy(Geo g, const double* __restrict__ cs, double* RHOY, do
     }
 }
 
+// The cell-index rule of marker_cells on arbitrary coordinates.
+__global__ void k_cell_index(const double* __restrict__ x, int64_t n, double d, int half, int32_t* out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = fix_quot(x[i], d, rcp_f32(d), half != 0);
+}
+
 }  // namespace
+
+extern "C" int32_t hmec_cell_index(const double* x, int64_t n, double d, int32_t half, int32_t* out) {
+    if (n < 0 || (n > 0 && (!x || !out)) || !(d > 0)) return HMEC_ERR_ARG;
+    if (n == 0) return HMEC_OK;
+    double* dx = nullptr;
+    int32_t* dout = nullptr;
+    cudaError_t e = cudaMalloc(&dx, sizeof(double) * (size_t)n);
+    if (e == cudaSuccess) e = cudaMalloc(&dout, sizeof(int32_t) * (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_cell_index<<<nblocks(n, 256), 256>>>(dx, n, d, half, dout);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(dx);
+    cudaFree(dout);
+    return e == cudaSuccess ? HMEC_OK : HMEC_ERR_CUDA;
+}
 
 int p2g_alloc(hmec_ctx* ctx) {
     const Geo& g = ctx->g;

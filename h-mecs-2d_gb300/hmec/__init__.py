@@ -98,7 +98,7 @@ EXPORTS = ["hmec_abi_version", "hmec_params_default", "hmec_field_name", "hmec_f
            "hmec_set_scalar", "hmec_get_scalar", "hmec_markers_to_nodes", "hmec_timestep_begin",
            "hmec_global_iteration", "hmec_timestep_end", "hmec_advect_markers", "hmec_timestep",
            "hmec_assemble_csr", "hmec_solve_system", "hmec_kernel_launches", "hmec_synchronize", "hmec_stream",
-           "hmec_profile_kernel", "hmec_profile_read", "hmec_markers_to_nodes_noalloc"]
+           "hmec_profile_kernel", "hmec_profile_read", "hmec_markers_to_nodes_noalloc", "hmec_cell_index"]
 
 _lib = None
 
@@ -162,6 +162,8 @@ def load(build_if_missing: bool = True):
     L.hmec_profile_read.argtypes = [vp, P(C.c_int64), P(C.c_double), P(C.c_double)]
     L.hmec_markers_to_nodes_noalloc.argtypes = [P(Params), P(P(C.c_double)), C.c_int64, P(P(C.c_double)), vp]
     L.hmec_markers_to_nodes_noalloc.restype = C.c_int32
+    L.hmec_cell_index.argtypes = [P(C.c_double), C.c_int64, C.c_double, C.c_int32, P(C.c_int32)]
+    L.hmec_cell_index.restype = C.c_int32
     _lib = L
     return L
 
@@ -177,6 +179,17 @@ def default_params(**over) -> Params:
         else:
             setattr(p, k, v)
     return p
+
+
+def cell_index(x, d: float, half: bool = False):
+    """The library's marker cell index (hmec_cell_index) of coordinates x."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty(x.shape, dtype=np.int32)
+    rc = load().hmec_cell_index(_dptr(x), x.size, float(d), 1 if half else 0,
+                                out.ctypes.data_as(C.POINTER(C.c_int32)))
+    if rc != 0:
+        raise HmecError(rc, "hmec_cell_index failed")
+    return out
 
 
 def _dptr(a):

@@ -285,6 +285,14 @@ int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, do
  * overlap on the GPU race, serialise them.                                  */
 int32_t hmec_markers_to_nodes_noalloc(const hmec_params* p, const double* const* markers, int64_t n,
                                       double* const* fields, void* stream);
+/* The library's marker cell index on n host coordinates x[k] (copied to the
+ * current device and back): out[k] = fix(fl(x/d)) (half = 0) or
+ * fix(fl(fl(x + d/2) / d)) (half != 0), IEEE operations as in
+ * cpp/h_mec_rsf_v9.cpp:432-433 and :468-469, before the clamp to the grid.
+ * The kernels decide most indices in FP32 and fall back to FP64 division
+ * near cell edges; this entry exposes that rule so it can be checked
+ * bit-exactly (no counterpart in the reference).                           */
+int32_t hmec_cell_index(const double* x, int64_t n, double d, int32_t half, int32_t* out);
 /* Device-kernel launches issued since hmec_create. */
 int64_t hmec_kernel_launches(const hmec_ctx* ctx);
 /* Synchronise the context stream. */

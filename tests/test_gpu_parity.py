@@ -43,6 +43,31 @@ def test_p2g_parity(preset):
     assert max(e.values()) < 1e-13, e
 
 
+@pytest.mark.parametrize("d", [40000.0 / 1000, 10000.0 / 200, 16000.0 / 400, 10000.0 / 50, 1.0 / 3.0, 7.77e3])
+def test_cell_index_bit_exact_near_edges(d):
+    """The kernels' cell index (FP32 away from cell edges, FP64 division near
+    them) equals fix(fl(x/d)) and fix(fl(fl(x + d/2)/d)) of IEEE FP64 on
+    coordinates at, and up to 24 ulps either side of, every node and
+    mid-cell line, plus random ones, zero and negatives."""
+    k = np.arange(-3, 1203, dtype=np.float64)
+    lines = np.concatenate([k * d, (k + 0.5) * d, (k - 0.5) * d])
+    parts = [lines, np.array([0.0, -0.0, 1e-300, -1e-300, 5e-324])]
+    up, dn = lines.copy(), lines.copy()
+    for _ in range(24):
+        up = np.nextafter(up, np.inf)
+        dn = np.nextafter(dn, -np.inf)
+        parts += [up, dn]
+    rng = np.random.default_rng(5)
+    parts.append(rng.uniform(-2.0 * d, 1200.0 * d, 200000))
+    x = np.concatenate(parts)
+    for half in (False, True):
+        q = (x + d / 2 if half else x) / d  # IEEE FP64, as the reference
+        ref = np.trunc(q).astype(np.int64)
+        got = hmec.cell_index(x, d, half).astype(np.int64)
+        bad = np.nonzero(got != ref)[0]
+        assert bad.size == 0, (half, x[bad[:5]], got[bad[:5]], ref[bad[:5]])
+
+
 def test_p2g_deterministic_and_jitter():
     o, mk, nodes = pairs.oracle_for("c0")  # jittered markers, per-marker permeability
     m = pairs.model_for("c0", mk, nodes)
