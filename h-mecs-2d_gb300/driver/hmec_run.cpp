@@ -2,11 +2,14 @@
 // hot path delegated to libhmec_gpu.so through include/hmec.h.
 //
 // What stays on the host, as in the reference: the initial marker lattice and
-// node fields (:188-209, :283-338), the per-step stdout report (:1732-1737)
-// and the EVO_*.txt time series of the fault row (:1751-1805).  Everything in
-// between (:377-1726) is one hmec_timestep() call per step.
+// node fields (:188-209, :283-338), the per-step stdout report (:1732-1737),
+// the EVO_*.txt time series of the fault row (:1751-1805) and the checkpoint
+// files every `savestep` steps with restart from one (:211-282,
+// :1807-1870; checkpoint.hpp).  Everything in between (:377-1726) is one
+// hmec_timestep() call per step.
 //
 //   hmec_run [steps] [Nx Ny xsize ysize] [--mixed] [--outdir DIR]
+//            [--savestep N] [--restart T] [--print-layout]
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -14,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "checkpoint.hpp"
 #include "hmec.h"
 
 namespace {
@@ -52,12 +56,19 @@ int main(int argc, char** argv) {
     hmec_params p;
     hmec_params_default(&p);  // cpp/constants.hpp
     int steps = 10;
+    int savestep = 500;  // constants.hpp:15
+    int restart = 0;     // the saved step to restart from (the reference reads it from file.txt, :180-186)
     std::string outdir = ".";
     std::vector<const char*> pos;
     for (int k = 1; k < argc; k++) {
         if (!strcmp(argv[k], "--mixed")) p.form = HMEC_FORM_MIXED;
         else if (!strcmp(argv[k], "--outdir") && k + 1 < argc) outdir = argv[++k];
-        else pos.push_back(argv[k]);
+        else if (!strcmp(argv[k], "--savestep") && k + 1 < argc) savestep = atoi(argv[++k]);
+        else if (!strcmp(argv[k], "--restart") && k + 1 < argc) restart = atoi(argv[++k]);
+        else if (!strcmp(argv[k], "--print-layout")) {
+            ckpt::print_layout(stdout);
+            return 0;
+        } else pos.push_back(argv[k]);
     }
     if (pos.size() >= 1) steps = atoi(pos[0]);
     if (pos.size() >= 5) {
@@ -158,11 +169,46 @@ int main(int argc, char** argv) {
     for (auto& f : init)
         if (check(ctx, hmec_upload_field(ctx, f.id, f.g->a.data(), f.g->rows, f.g->cols), "upload_field")) return 1;
 
+    const std::string d = outdir + "/";
+    ckpt::History history(p.num_timesteps);
+    if (restart > 0) {  // :211-282
+        const std::string name = d + "h_mec_" + std::to_string(restart) + ".h5.stub";
+        std::vector<ckpt::Dataset> ds;
+        if (!ckpt::read_stub(name, ds)) {
+            fprintf(stderr, "cannot read checkpoint %s\n", name.c_str());
+            return 1;
+        }
+        if (check(ctx, ckpt::restore(ctx, p, ds, restart, history), "restore")) return 1;
+        // EVO_*.txt keep the lines of the steps up to the saved one (:268-281;
+        // the reference lists "EVO_VxD.txt" but writes "EVO_vxD.txt", so its
+        // Darcy series is not trimmed on a case-sensitive file system)
+        for (const char* evo : {"EVO_Vslip.txt", "EVO_viscosity.txt", "EVO_press_flu.txt", "EVO_press_eff.txt",
+                                "EVO_SigmaY.txt", "EVO_Sii.txt", "EVO_Theta.txt", "EVO_Visc_comp.txt",
+                                "EVO_Elast_comp.txt", "EVO_vxD.txt", "EVO_data.txt"}) {
+            const std::string path = d + evo;
+            FILE* f = fopen(path.c_str(), "r");
+            if (!f) continue;
+            std::string keep;
+            int lines = 0;
+            for (int c; lines < restart && (c = fgetc(f)) != EOF;) {
+                keep.push_back((char)c);
+                if (c == '\n') lines++;
+            }
+            fclose(f);
+            f = fopen(path.c_str(), "w");
+            if (f) {
+                fwrite(keep.data(), 1, keep.size(), f);
+                fclose(f);
+            }
+        }
+    }
+
     Grid VSLIPB(Ny, Nx), ETA(Ny, Nx), OM(Ny, Nx), SigmaY(Ny, Nx), SII_fault(Ny, Nx);
     Grid pf(Ny1, Nx1), pt(Ny1, Nx1), VIS_COMP(Ny1, Nx1), EL_DECOM(Ny1, Nx1), vxD(Ny1, Nx1), Peff(Ny1, Nx1);
     for (int s = 0; s < steps; s++) {
         hmec_step_report r;
         if (check(ctx, hmec_timestep(ctx, &r), "hmec_timestep")) break;
+        history.record(ctx, r.timestep);
         // :1732-1737
         printf("====================================\n");
         printf("total time:        %g sec\n", r.timesum);
@@ -182,7 +228,6 @@ int main(int argc, char** argv) {
         hmec_download_field(ctx, HMEC_F_EL_DECOM, EL_DECOM.a.data(), Ny1, Nx1);
         hmec_download_field(ctx, HMEC_F_vxD, vxD.a.data(), Ny1, Nx1);
         for (size_t k = 0; k < Peff.a.size(); k++) Peff.a[k] = pt.a[k] - pf.a[k];
-        const std::string d = outdir + "/";
         append_row(d + "EVO_Vslip.txt", r.timesum, r.dt, VSLIPB, line_fault);
         append_row(d + "EVO_viscosity.txt", r.timesum, r.dt, ETA, line_fault);
         append_row(d + "EVO_press_flu.txt", r.timesum, r.dt, pf, line_fault);
@@ -197,6 +242,19 @@ int main(int argc, char** argv) {
         if (f) {
             fprintf(f, "%20g%20g%20g%20d%20d\n", r.timesum, r.dt, r.Vmax, r.ynlast, r.global_iters);
             fclose(f);
+        }
+        if (savestep > 0 && r.timestep % savestep == 0) {  // :1807-1870
+            FILE* ft = fopen((d + "file.txt").c_str(), "w");
+            if (ft) {
+                fprintf(ft, "%d\n", r.timestep);
+                fclose(ft);
+            }
+            std::vector<ckpt::Dataset> ds;
+            const std::string name = d + "h_mec_" + std::to_string(r.timestep) + ".h5.stub";
+            if (check(ctx, ckpt::collect(ctx, p, history, ds), "checkpoint") || !ckpt::write_stub(name, ds)) {
+                fprintf(stderr, "cannot write checkpoint %s\n", name.c_str());
+                break;
+            }
         }
     }
     hmec_destroy(ctx);

@@ -79,7 +79,8 @@ DRIVER = os.path.join(OUT_DIR, "hmec_run")
 
 def build_driver(force: bool = False) -> str:
     """The C++ host loop mirroring the reference's main(), linked to the library."""
-    if not force and not _stale(DRIVER, [DRIVER_SRC, LIB, os.path.join(INC, "hmec.h")]):
+    deps = [DRIVER_SRC, os.path.join(os.path.dirname(DRIVER_SRC), "checkpoint.hpp"), LIB, os.path.join(INC, "hmec.h")]
+    if not force and not _stale(DRIVER, deps):
         return DRIVER
     cxx = shutil.which("g++") or "g++"
     cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", INC, DRIVER_SRC, "-o", DRIVER + ".tmp",
