@@ -283,6 +283,14 @@ int hmec_cuda_fail(hmec_ctx* ctx, cudaError_t e, const char* what);
 bool hmec_prof_begin(hmec_ctx* ctx, const char* kname, double bytes);
 void hmec_prof_end(hmec_ctx* ctx);
 
+// The library's launch helpers use ctx->stream; inside a scope they go to s.
+struct StreamScope {
+    hmec_ctx* ctx;
+    cudaStream_t saved;
+    StreamScope(hmec_ctx* c, cudaStream_t s) : ctx(c), saved(c->stream) { c->stream = s; }
+    ~StreamScope() { ctx->stream = saved; }
+};
+
 // Launch with algorithmic byte accounting for the live roofline.
 #define HMEC_LAUNCH_B(ctx, nbytes, kern, grid, block, smem, ...)               \
     do {                                                                          \

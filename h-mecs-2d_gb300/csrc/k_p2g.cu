@@ -712,17 +712,47 @@ int p2g_run(hmec_ctx* ctx) {
     const float* rec_x = rec_p + (size_t)n * REC_P;
     const float* rec_y = rec_x + (size_t)n * REC_X;
     dim3 bb(64), gc(nblocks(g.Ny - 1, 64), g.Nx - 1);
-    HMEC_LAUNCH(ctx, (k_cell_sums<false, false, 10, REC_B>), gc, bb, 0, g, ctx->hc_start, rec_b, cs_b);
-    HMEC_LAUNCH(ctx, (k_cell_sums<true, true, 5, REC_P>), gc, bb, 0, g, ctx->hc_start, rec_p, cs_p);
-    HMEC_LAUNCH(ctx, (k_cell_sums<true, false, 4, REC_X>), gc, bb, 0, g, ctx->hc_start, rec_x, cs_x);
-    HMEC_LAUNCH(ctx, (k_cell_sums<false, true, 4, REC_Y>), gc, bb, 0, g, ctx->hc_start, rec_y, cs_y);
     dim3 gb(nblocks(g.Ny, 64), g.Nx), gs(nblocks(g.Ny1, 64), g.Nx1);
-    HMEC_LAUNCH(ctx, k_node_basic, gb, bb, 0, g, cs_b, f[HMEC_F_RHO], f[HMEC_F_KKK], f[HMEC_F_TTT], f[HMEC_F_GGG],
-                f[HMEC_F_ETA0], f[HMEC_F_COHT], f[HMEC_F_FRIT], f[HMEC_F_COHC], f[HMEC_F_FRIC], f[HMEC_F_DILC]);
-    HMEC_LAUNCH(ctx, k_node_p, gs, bb, 0, g, cs_p, f[HMEC_F_ETAP], f[HMEC_F_POR], f[HMEC_F_ETAB0], f[HMEC_F_ETAP0],
-                f[HMEC_F_GGGP]);
-    HMEC_LAUNCH(ctx, k_node_vx, gs, bb, 0, g, cs_x, f[HMEC_F_RHOX], f[HMEC_F_ETADX], f[HMEC_F_RHOFX], f[HMEC_F_PORX]);
-    HMEC_LAUNCH(ctx, k_node_vy, gs, bb, 0, g, cs_y, f[HMEC_F_RHOY], f[HMEC_F_ETADY], f[HMEC_F_RHOFY], f[HMEC_F_PORY]);
+    // the four grids' gathers are independent: each pair (cell sums, node
+    // sums) on its own stream when the solver's level streams exist
+    Solver& sv = ctx->sv;
+    const cudaStream_t main = ctx->stream;
+    const bool par = sv.aux.size() >= 4 && sv.ev_fork;
+    if (par) HMEC_CUDA(ctx, cudaEventRecord(sv.ev_fork, main));
+    auto on = [&](int k) {
+        if (!par) return main;
+        cudaStreamWaitEvent(sv.aux[k], sv.ev_fork, 0);
+        return sv.aux[k];
+    };
+    {
+        StreamScope scope(ctx, on(0));
+        HMEC_LAUNCH(ctx, (k_cell_sums<false, false, 10, REC_B>), gc, bb, 0, g, ctx->hc_start, rec_b, cs_b);
+        HMEC_LAUNCH(ctx, k_node_basic, gb, bb, 0, g, cs_b, f[HMEC_F_RHO], f[HMEC_F_KKK], f[HMEC_F_TTT], f[HMEC_F_GGG],
+                    f[HMEC_F_ETA0], f[HMEC_F_COHT], f[HMEC_F_FRIT], f[HMEC_F_COHC], f[HMEC_F_FRIC], f[HMEC_F_DILC]);
+    }
+    {
+        StreamScope scope(ctx, on(1));
+        HMEC_LAUNCH(ctx, (k_cell_sums<true, true, 5, REC_P>), gc, bb, 0, g, ctx->hc_start, rec_p, cs_p);
+        HMEC_LAUNCH(ctx, k_node_p, gs, bb, 0, g, cs_p, f[HMEC_F_ETAP], f[HMEC_F_POR], f[HMEC_F_ETAB0],
+                    f[HMEC_F_ETAP0], f[HMEC_F_GGGP]);
+    }
+    {
+        StreamScope scope(ctx, on(2));
+        HMEC_LAUNCH(ctx, (k_cell_sums<true, false, 4, REC_X>), gc, bb, 0, g, ctx->hc_start, rec_x, cs_x);
+        HMEC_LAUNCH(ctx, k_node_vx, gs, bb, 0, g, cs_x, f[HMEC_F_RHOX], f[HMEC_F_ETADX], f[HMEC_F_RHOFX],
+                    f[HMEC_F_PORX]);
+    }
+    {
+        StreamScope scope(ctx, on(3));
+        HMEC_LAUNCH(ctx, (k_cell_sums<false, true, 4, REC_Y>), gc, bb, 0, g, ctx->hc_start, rec_y, cs_y);
+        HMEC_LAUNCH(ctx, k_node_vy, gs, bb, 0, g, cs_y, f[HMEC_F_RHOY], f[HMEC_F_ETADY], f[HMEC_F_RHOFY],
+                    f[HMEC_F_PORY]);
+    }
+    if (par)
+        for (int k = 0; k < 4; k++) {
+            HMEC_CUDA(ctx, cudaEventRecord(sv.ev_done[k], sv.aux[k]));
+            HMEC_CUDA(ctx, cudaStreamWaitEvent(main, sv.ev_done[k], 0));
+        }
     HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;
 }

@@ -2001,14 +2001,6 @@ void solver_free(hmec_ctx* ctx) {
     cudaFree(sv.kcur);
 }
 
-// The library's launch helpers use ctx->stream; inside a scope they go to s.
-struct StreamScope {
-    hmec_ctx* ctx;
-    cudaStream_t saved;
-    StreamScope(hmec_ctx* c, cudaStream_t s) : ctx(c), saved(c->stream) { c->stream = s; }
-    ~StreamScope() { ctx->stream = saved; }
-};
-
 // Rebuilds every level after a fine assembly.  The work is a graph, not a
 // chain: the coarse coefficients form a chain on the main stream (level l
 // needs level l-1's), each level's assembly, inverses, smoother copy and
