@@ -349,7 +349,9 @@ def run_ensemble(args, rank=0, world=1, device_index=0, nmembers=64):
     common = dict(krylov_rtol=1e-15, krylov_restart=40, krylov_maxit=4000)
     out = {}
     for form, label in ((hmec.FORM_MIXED, "mixed"), (hmec.FORM_FP64, "fp64")):
-        ens = Ensemble(members, form=form, **common)
+        # the FP64 baseline runs one member at a time, each with the settings
+        # of a model run alone
+        ens = Ensemble(members, concurrent=(form == hmec.FORM_MIXED), form=form, **common)
         (ens.step if form == hmec.FORM_MIXED else ens.step_sequential)(args.warmup)
         torch.cuda.synchronize()
         rank_barrier(world)

@@ -2135,6 +2135,10 @@ static int stage_config(hmec_ctx* ctx, Level& L) {
     const int w = blocks[1] > 0 ? 1 : 0;
     L.st_whole = w;
     L.st_grid = std::min(L.ntiles, blocks[w]);
+    // models that share the GPU (ensembles) take at most a quarter of it per
+    // pass, so that four members' passes run side by side instead of each
+    // large level holding every SM in turn
+    if (ctx->p.mg_flags & HMEC_MG_PASS_LAUNCHES) L.st_grid = std::min(L.st_grid, std::max(1, nsm / 4));
     L.st_smem = smem[w];
     return HMEC_OK;
 }

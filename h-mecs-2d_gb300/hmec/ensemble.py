@@ -14,16 +14,19 @@ from . import MG_PASS_LAUNCHES, Model, default_params, synth
 
 
 class Ensemble:
-    def __init__(self, members, **common):
+    def __init__(self, members, concurrent: bool = True, **common):
         """members: (overrides, material, seed) triples, e.g. synth.ensemble_members().
 
-        The members smooth with one launch per multigrid pass (not one per
-        V-cycle), so that the small coarse passes of different members can
-        share the GPU."""
+        concurrent: the members will run side by side (step()); they then
+        smooth with one launch per multigrid pass and at most a quarter of
+        the GPU per pass (HMEC_MG_PASS_LAUNCHES), so that different members'
+        passes share the GPU.  With concurrent=False every member keeps the
+        settings of a model run alone (for step_sequential())."""
         self.models = []
         for over, mat, seed in members:
             p = default_params(**dict(over, **common))
-            p.mg_flags |= MG_PASS_LAUNCHES
+            if concurrent:
+                p.mg_flags |= MG_PASS_LAUNCHES
             m = Model(p)
             mk, nodes = synth.instance_state(p, mat, seed)
             m.upload_markers(mk)

@@ -114,10 +114,11 @@ enum hmec_mg_flags {
      * default tiled sweep (multiplicative inside 12x12-patch tiles, the
      * neighbours' unknowns taken from the start of the sweep). */
     HMEC_MG_UNTILED = 2,
-    /* One cooperative launch per smoothing pass instead of one per V-cycle.
-     * The fused V-cycle holds its fine level's grid through the small coarse
-     * levels too; models that share the GPU concurrently (ensembles) keep
-     * the per-pass launches so their coarse passes can run side by side. */
+    /* For models that share the GPU concurrently (ensembles): one
+     * cooperative launch per smoothing pass instead of one per V-cycle (the
+     * fused V-cycle holds its fine level's grid through the small coarse
+     * levels too), and at most a quarter of the SMs per pass, so that
+     * several models' passes run side by side. */
     HMEC_MG_PASS_LAUNCHES = 4
 };
 
