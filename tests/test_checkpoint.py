@@ -67,6 +67,69 @@ def test_stub_container_round_trip_in_c_order(tmp_path):
     assert np.array_equal(first, items[0][2].ravel(order="C"))
 
 
+CXX_PROBE = r"""
+#include <cstdio>
+#include "checkpoint.hpp"
+int main(int argc, char** argv) {
+    std::vector<ckpt::Dataset> ds;
+    if (argc > 2) {  // read the container argv[1], print every dataset's sum
+        if (!ckpt::read_stub(argv[1], ds)) return 2;
+        for (const auto& d : ds) {
+            double s = 0;
+            for (size_t k = 0; k < d.v.size(); k++) s += d.v[k] * (double)(k + 1);
+            std::printf("%s %s %zu %.17g\n", d.group.c_str(), d.name.c_str(), d.dims.size(), s);
+        }
+        return 0;
+    }
+    // write: a 3 x 2 matrix 0..5 (C order) and a vector of 4
+    ds.push_back({"Matrix", "SIIB", {3, 2}, {0, 1, 2, 3, 4, 5}});
+    ds.push_back({"Vector", "xm", {4}, {1.5, -2.5, 3.25, 1e-300}});
+    return ckpt::write_stub(argv[1], ds) ? 0 : 1;
+}
+"""
+
+
+def _probe(tmp_path):
+    import shutil
+
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "probe.cpp"
+    src.write_text(CXX_PROBE)
+    exe = tmp_path / "probe"
+    r = subprocess.run([cxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), "-I",
+                        os.path.join(ROOT, "h-mecs-2d_gb300", "driver"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return str(exe)
+
+
+def test_cpp_and_python_containers_agree(tmp_path):
+    exe = _probe(tmp_path)
+    # C++ writes, Python reads
+    p = str(tmp_path / "cpp.h5.stub")
+    assert subprocess.run([exe, p]).returncode == 0
+    d = ck.read(p)
+    assert list(d) == [("Matrix", "SIIB"), ("Vector", "xm")]
+    assert np.array_equal(d[("Matrix", "SIIB")], np.arange(6.0).reshape(3, 2))
+    assert np.array_equal(d[("Vector", "xm")], [1.5, -2.5, 3.25, 1e-300])
+    # Python writes, C++ reads
+    rng = np.random.default_rng(9)
+    items = [("Matrix", "OM0", rng.standard_normal((5, 4))), ("Value", "values", rng.standard_normal(9))]
+    q = str(tmp_path / "py.h5.stub")
+    ck.write_stub(q, items)
+    out = subprocess.run([exe, q, "read"], capture_output=True, text=True)
+    assert out.returncode == 0
+    lines = out.stdout.split("\n")
+    for (g, n, a), line in zip(items, lines):
+        group, name, rank, s = line.split()
+        flat = np.ascontiguousarray(a).ravel(order="C")
+        want = float(np.sum(flat * np.arange(1, flat.size + 1)))
+        assert (group, name, int(rank)) == (g, n, a.ndim)
+        assert float(s) == pytest.approx(want, rel=1e-12)
+
+
 def test_stub_rejects_other_files(tmp_path):
     p = tmp_path / "x.h5.stub"
     p.write_bytes(b"not a checkpoint")
