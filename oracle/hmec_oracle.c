@@ -1,7 +1,7 @@
 /*
  * hmec_oracle.c -- CPU restatement of the H-MEC per-timestep hot path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker; never part of the product path).
+ * TEST INFRASTRUCTURE ONLY (the oracle; never part of the product path).
  *
  * Follows cpp/h_mec_rsf_v9.cpp of lucadalzilio/H-MECs-2D section by section;
  * each function cites the lines it restates.  Conventions carried over so

@@ -1,7 +1,7 @@
 /*
  * hmec_oracle.h -- CPU restatement of the H-MEC per-timestep hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker the GPU library is compared
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the GPU library is compared
  * against (tests, __graft_entry__.smoke, and the CPU-baseline leg of
  * bench.py).  Nothing in the product links or calls it.
  *

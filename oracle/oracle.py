@@ -1,8 +1,8 @@
 """CPU oracle driver for the H-MEC hot path.
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py, always as the checker.  It is never the thing
-measured or shipped.
+CPU-baseline leg of bench.py, always as the oracle the GPU results are
+compared with.  It is never the thing measured or shipped.
 
 Wraps ``libhmec_oracle.so`` (the C restatement of cpp/h_mec_rsf_v9.cpp in
 hmec_oracle.c).  The reference solves every global iteration with MKL Pardiso
