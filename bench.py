@@ -35,7 +35,7 @@ CONFIG = "c1"
 WORKLOAD = "config 1: 201x201 nodes, 10x10 km, 5x5 markers/cell (1,000,000 markers), seeded synthetic fault model"
 DOMINANT = "k_smooth"
 # DRAM bytes (read + write) per launch of the fused V-cycle kernel (one launch
-# = one config-1 V-cycle), from the ncu capture in profiles/k_vcycle_stage_c1.md
+# = one config-1 V-cycle), from one ncu capture of the kernel (profiles/)
 SMOOTH_TRAFFIC_BYTES = 94.97e6
 
 
