@@ -224,21 +224,7 @@ static int create_inner(hmec_ctx* ctx) {
     HMEC_CUDA(ctx, cudaGetDevice(&ctx->dev));
     HMEC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     Geo& g = ctx->g;
-    g.Nx = p.Nx;
-    g.Ny = p.Ny;
-    g.Nx1 = p.Nx + 1;
-    g.Ny1 = p.Ny + 1;
-    g.N = g.Nx1 * g.Ny1 * 6;
-    g.line_fault = (int)((p.Ny - 1) / 2.);  // constants.hpp:43
-    g.dx = p.xsize / (p.Nx - 1);
-    g.dy = p.ysize / (p.Ny - 1);
-    g.dx2 = g.dx * g.dx;
-    g.dy2 = g.dy * g.dy;
-    g.dx_dy = g.dx * g.dy;
-    g.lower_block = p.ysize / 2. + g.dy;  // constants.hpp:76-77
-    g.upper_block = p.ysize / 2. - g.dy;
-    g.dy_faultw = g.dy / g.dx;            // faultwidth = dx (:66, :175)
-    geo_reciprocals(g);
+    geo_make(g, p.Nx, p.Ny, p.xsize, p.ysize);
     ctx->marknum = hmec_marknum(&p);
     // coordinates, constants.hpp:57-64
     std::vector<double> c[8];

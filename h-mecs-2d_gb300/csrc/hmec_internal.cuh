@@ -196,6 +196,7 @@ struct hmec_ctx {
     int32_t* hc_start;       // exclusive scan of hc_count (+ total)
     int32_t* hc_fill;        // scatter cursors
     int32_t* scan_part;      // scan block partials
+    int* sort_long;          // set when a half cell holds more markers than the per-segment sort takes
     float* mprop;            // sorted per-marker gather records of the four grids (double-float)
     double* cellsum;         // per-cell corner sums of the four grids (k_cell_sums)
     int nhalf;               // number of half-cells
@@ -252,6 +253,43 @@ __device__ __forceinline__ int fix_quot(double x, double d, float rdf, bool half
     return fix_trunc(__ddiv_rn(xx, d));
 }
 __device__ __forceinline__ float rcp_f32(double d) { return __frcp_rn(__double2float_rn(d)); }
+
+// A marker's basic cell (ib, jb) and pressure cell (iP, jP): the indices of
+// cpp/h_mec_rsf_v9.cpp:432-433 and :468-469 (fix + check_bounds, IEEE
+// quotients; the Vx/Vy cells reuse them), decided in FP32 away from cell edges.
+struct MarkerCells {
+    int ib, jb, iP, jP;
+};
+__device__ __forceinline__ MarkerCells marker_cells(double xm, double ym, const Geo& g) {
+    MarkerCells c;
+    const float rdx = rcp_f32(g.dx), rdy = rcp_f32(g.dy);
+    c.jb = check_bounds(fix_quot(xm, g.dx, rdx, false), g.Nx);
+    c.ib = check_bounds(fix_quot(ym, g.dy, rdy, false), g.Ny);
+    c.jP = check_bounds(fix_quot(xm, g.dx, rdx, true), g.Nx);
+    c.iP = check_bounds(fix_quot(ym, g.dy, rdy, true), g.Ny);
+    return c;
+}
+
+// The geometry of an Nx x Ny basic grid over xsize x ysize, as
+// cpp/constants.hpp derives it (dx, dy, line_fault :43, the block limits
+// :76-77, faultwidth = dx :66), plus the reciprocal constants.
+inline void geo_make(Geo& g, int Nx, int Ny, double xsize, double ysize) {
+    g.Nx = Nx;
+    g.Ny = Ny;
+    g.Nx1 = Nx + 1;
+    g.Ny1 = Ny + 1;
+    g.N = g.Nx1 * g.Ny1 * 6;
+    g.line_fault = (int)((Ny - 1) / 2.);
+    g.dx = xsize / (Nx - 1);
+    g.dy = ysize / (Ny - 1);
+    g.dx2 = g.dx * g.dx;
+    g.dy2 = g.dy * g.dy;
+    g.dx_dy = g.dx * g.dy;
+    g.lower_block = ysize / 2. + g.dy;
+    g.upper_block = ysize / 2. - g.dy;
+    g.dy_faultw = g.dy / g.dx;
+    geo_reciprocals(g);
+}
 
 static inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 

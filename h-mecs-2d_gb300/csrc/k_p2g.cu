@@ -22,6 +22,7 @@
 //     thread per node adds its four cells' corner sums in a fixed order and
 //     normalises in the epilogue (a4).  No float atomics.
 #include "hmec_internal.cuh"
+#include "hmec_sort.cuh"
 
 namespace {
 
@@ -134,142 +135,6 @@ __device__ __forceinline__ bool df_rcp(double a, float& h, float& l) {
     l = fmaf(ru, u, ru);  // r (u + u^2)
     df_norm(h, l);
     return true;
-}
-
-struct MarkerCells {
-    int ib, jb, iP, jP;
-};
-
-// Cell indices of :432-433 and :468-469 (the Vx/Vy cells reuse them).
-__device__ __forceinline__ MarkerCells marker_cells(double xm, double ym, const Geo& g) {
-    MarkerCells c;
-    // the reference's IEEE quotients, decided in FP32 away from cell edges
-    const float rdx = rcp_f32(g.dx), rdy = rcp_f32(g.dy);
-    c.jb = check_bounds(fix_quot(xm, g.dx, rdx, false), g.Nx);
-    c.ib = check_bounds(fix_quot(ym, g.dy, rdy, false), g.Ny);
-    c.jP = check_bounds(fix_quot(xm, g.dx, rdx, true), g.Nx);
-    c.iP = check_bounds(fix_quot(ym, g.dy, rdy, true), g.Ny);
-    return c;
-}
-
-__global__ void k_keys(const double* __restrict__ xm, const double* __restrict__ ym, int64_t n, Geo g,
-                       int32_t* __restrict__ key, int32_t* __restrict__ count, int* status) {
-    int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int k = -1;
-    if (m < n) {
-        MarkerCells c = marker_cells(xm[m], ym[m], g);
-        int di = c.iP - c.ib, dj = c.jP - c.jb;
-        if (di < 0 || di > 1 || dj < 0 || dj > 1) {  // cannot happen (monotone clamp); guard anyway
-            atomicOr(status, HMEC_DEV_BOUNDS);
-            di = di < 0 ? 0 : (di > 1 ? 1 : di);
-            dj = dj < 0 ? 0 : (dj > 1 ? 1 : dj);
-        }
-        int hr = 2 * c.ib + di, hc = 2 * c.jb + dj;
-        k = hc * (2 * (g.Ny - 1)) + hr;
-        key[m] = k;
-    }
-    // warp-aggregated histogram: one atomic per distinct key in the warp
-    unsigned active = __ballot_sync(0xffffffffu, k >= 0);
-    if (k >= 0) {
-        unsigned peers = __match_any_sync(active, k);
-        int leader = __ffs(peers) - 1;
-        if ((int)(threadIdx.x & 31) == leader) atomicAdd(&count[k], __popc(peers));
-    }
-}
-
-__global__ void k_scatter(const int32_t* __restrict__ key, int64_t n, int32_t* __restrict__ cursor,
-                          int32_t* __restrict__ perm) {
-    int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int k = (m < n) ? key[m] : -1;
-    unsigned active = __ballot_sync(0xffffffffu, k >= 0);
-    if (k >= 0) {
-        unsigned peers = __match_any_sync(active, k);
-        int lane = threadIdx.x & 31;
-        int leader = __ffs(peers) - 1;
-        int base = 0;
-        if (lane == leader) base = atomicAdd(&cursor[k], __popc(peers));
-        base = __shfl_sync(peers, base, leader);
-        int rank = __popc(peers & ((1u << lane) - 1u));
-        perm[base + rank] = (int32_t)m;
-    }
-}
-
-// Segment ordering by marker id (segments are a few markers long).
-__global__ void k_segsort(const int32_t* __restrict__ start, int nseg, int32_t* __restrict__ perm) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nseg) return;
-    int b = start[s], e = start[s + 1];
-    for (int a = b + 1; a < e; a++) {
-        int v = perm[a];
-        int q = a;
-        while (q > b && perm[q - 1] > v) {
-            perm[q] = perm[q - 1];
-            q--;
-        }
-        perm[q] = v;
-    }
-}
-
-// Exclusive scan, three phases (block scan of 2048, scan of block totals, add).
-__global__ void k_scan1(const int32_t* __restrict__ in, int n, int32_t* __restrict__ out, int32_t* __restrict__ part) {
-    __shared__ int32_t sh[2048];
-    int base = blockIdx.x * 2048;
-    int t = threadIdx.x;
-    sh[t] = (base + t < n) ? in[base + t] : 0;
-    sh[t + 1024] = (base + t + 1024 < n) ? in[base + t + 1024] : 0;
-    __syncthreads();
-    // Blelloch up-sweep / down-sweep
-    for (int d = 1; d < 2048; d <<= 1) {
-        int idx = (t + 1) * d * 2 - 1;
-        if (idx < 2048) sh[idx] += sh[idx - d];
-        __syncthreads();
-    }
-    if (t == 0) {
-        part[blockIdx.x] = sh[2047];
-        sh[2047] = 0;
-    }
-    __syncthreads();
-    for (int d = 1024; d >= 1; d >>= 1) {
-        int idx = (t + 1) * d * 2 - 1;
-        if (idx < 2048) {
-            int32_t v = sh[idx - d];
-            sh[idx - d] = sh[idx];
-            sh[idx] += v;
-        }
-        __syncthreads();
-    }
-    if (base + t < n) out[base + t] = sh[t];
-    if (base + t + 1024 < n) out[base + t + 1024] = sh[t + 1024];
-}
-
-__global__ void k_scan2(int32_t* __restrict__ part, int nparts, int32_t* __restrict__ total_out) {
-    // single block: sequential carry over chunks of 1024
-    __shared__ int32_t sh[1024];
-    __shared__ int32_t carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (int c0 = 0; c0 < nparts; c0 += 1024) {
-        int t = threadIdx.x;
-        int32_t v = (c0 + t < nparts) ? part[c0 + t] : 0;
-        sh[t] = v;
-        __syncthreads();
-        for (int d = 1; d < 1024; d <<= 1) {  // Hillis-Steele inclusive scan
-            int32_t a = (t >= d) ? sh[t - d] : 0;
-            __syncthreads();
-            sh[t] += a;
-            __syncthreads();
-        }
-        if (c0 + t < nparts) part[c0 + t] = carry + sh[t] - v;  // exclusive
-        __syncthreads();
-        if (t == 0) carry += sh[1023];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *total_out = carry;
-}
-
-__global__ void k_scan3(int32_t* __restrict__ out, int n, const int32_t* __restrict__ part) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] += part[i / 2048];
 }
 
 // v < lo ? lo : (v > hi ? hi : v).  Non-negative finite doubles order like
@@ -644,7 +509,15 @@ int p2g_alloc(hmec_ctx* ctx) {
     HMEC_CUDA(ctx, cudaMalloc(&ctx->hc_start, sizeof(int32_t) * ((size_t)ctx->nhalf + 2)));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->hc_fill, sizeof(int32_t) * ((size_t)ctx->nhalf + 1)));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->scan_part, sizeof(int32_t) * ((size_t)nparts + 1)));
-    HMEC_CUDA(ctx, cudaMalloc(&ctx->mprop, sizeof(float) * (size_t)REC_ALL * (size_t)n));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->sort_long, sizeof(int)));
+    // the marker records double as the radix sort's scratch (they are
+    // written only after the sort); they hold 64 ints per marker, the sort
+    // needs about 3.5
+    int rgrid = 1;
+    HMEC_CUDA(ctx, hsort::radix_grid(&rgrid));
+    const size_t rec = (size_t)REC_ALL * (size_t)n;
+    const size_t need = hsort::radix_scratch_ints(n, rgrid);
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->mprop, sizeof(float) * (rec > need ? rec : need)));
     // corner sums: (10 + 5 + 4 + 4 properties + 4 weights) x 4 corners per cell
     const size_t ncell = (size_t)(g.Ny - 1) * (g.Nx - 1);
     HMEC_CUDA(ctx, cudaMalloc(&ctx->cellsum, sizeof(double) * 27 * 4 * ncell));
@@ -658,6 +531,7 @@ void p2g_free(hmec_ctx* ctx) {
     cudaFree(ctx->hc_start);
     cudaFree(ctx->hc_fill);
     cudaFree(ctx->scan_part);
+    cudaFree(ctx->sort_long);
     cudaFree(ctx->mprop);
     cudaFree(ctx->cellsum);
 }
@@ -668,18 +542,12 @@ int p2g_run(hmec_ctx* ctx) {
     const int nh = ctx->nhalf;
     int* status = &ctx->ds->status;
     HMEC_CUDA(ctx, cudaMemsetAsync(ctx->hc_count, 0, sizeof(int32_t) * ((size_t)nh + 1), ctx->stream));
-    HMEC_LAUNCH(ctx, k_keys, nblocks(n, 256), 256, 0, ctx->mk[HMEC_M_xm], ctx->mk[HMEC_M_ym], n, g, ctx->mkey,
+    HMEC_LAUNCH(ctx, hsort::k_keys, nblocks(n, 256), 256, 0, ctx->mk[HMEC_M_xm], ctx->mk[HMEC_M_ym], n, g, ctx->mkey,
                 ctx->hc_count, status);
-    // exclusive scan of nh+1 counts (last entry is 0) -> hc_start[0..nh]
-    int ns = nh + 1;
-    int nparts = (ns + 2047) / 2048;
-    HMEC_LAUNCH(ctx, k_scan1, nparts, 1024, 0, ctx->hc_count, ns, ctx->hc_start, ctx->scan_part);
-    HMEC_LAUNCH(ctx, k_scan2, 1, 1024, 0, ctx->scan_part, nparts, ctx->scan_part + nparts);
-    HMEC_LAUNCH(ctx, k_scan3, nblocks(ns, 256), 256, 0, ctx->hc_start, ns, ctx->scan_part);
-    HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->hc_fill, ctx->hc_start, sizeof(int32_t) * (size_t)nh,
-                                   cudaMemcpyDeviceToDevice, ctx->stream));
-    HMEC_LAUNCH(ctx, k_scatter, nblocks(n, 256), 256, 0, ctx->mkey, n, ctx->hc_fill, ctx->perm);
-    HMEC_LAUNCH(ctx, k_segsort, nblocks(nh, 128), 128, 0, ctx->hc_start, nh, ctx->perm);
+    // segment starts hc_start[0..nh], the scatter, the per-segment order
+    hsort::SortBufs sb{ctx->mkey, ctx->hc_count, ctx->hc_start, ctx->hc_fill, ctx->scan_part, ctx->perm,
+                       ctx->sort_long, reinterpret_cast<int32_t*>(ctx->mprop)};
+    HMEC_CUDA(ctx, hsort::sort_by_half_cell(ctx->stream, sb, n, nh, &ctx->launches));
     MkPtrs mk;
     mk.xm = ctx->mk[HMEC_M_xm];
     mk.ym = ctx->mk[HMEC_M_ym];

@@ -4,37 +4,51 @@
 // Some hosts may not call cudaMalloc at all: a solver embedded in another
 // application that owns the device allocator (and forbids allocations behind
 // its back), or a real-time loop that must never block on the allocator.
-// This file
-// gives them one entry point, hmec_markers_to_nodes_noalloc(), which computes
-// exactly what hmec_markers_to_nodes() computes (sections a1-a4 of
-// cpp/h_mec_rsf_v9.cpp:376-583: the half-cell counting sort and the
-// deterministic node gathers) from marker and node arrays the caller already
-// holds on the device.  Its only scratch memory -- the sort permutation and
-// the per-half-cell counts and offsets -- is one file-scope __device__ array
-// of fixed size, so the library allocates nothing for it, here or anywhere.
+// This file gives them one entry point, hmec_markers_to_nodes_noalloc(),
+// which computes what hmec_markers_to_nodes() computes (sections a1-a4 of
+// cpp/h_mec_rsf_v9.cpp:376-583) from marker and node arrays the caller
+// already holds on the device.  It sorts the markers with the same
+// deterministic half-cell sort (hmec_sort.cuh) and gathers each node's sums
+// from its half cells with the reference's weights; its summation order
+// differs from the context path's (per node here, per cell corner there), so
+// the two agree to about 1e-13 relative, not bit for bit.  Its only scratch
+// memory -- marker keys, the permutation, the per-half-cell counts, offsets
+// and cursors, and the radix sort's buffers -- is one file-scope __device__
+// array of fixed size, so nothing is allocated for it, here or anywhere.
 //
 // Limits: at most HMEC_NOALLOC_MAX_MARKERS markers and
 // HMEC_NOALLOC_MAX_HALF_CELLS half cells (4 (Nx-1)(Ny-1)); the array takes
-// about 6 MiB on every device that loads the library, until the process
-// exits.  All calls share it, so two calls that overlap on the GPU (other
-// streams, other host threads) race and corrupt each other: serialise them.
+// about 25 MiB of device memory.  The driver reserves it when it loads the
+// library's device code on a device -- under lazy module loading (the
+// default) that is the first call on that device -- and keeps it until the
+// process exits.  All calls share it, so two calls that overlap on the GPU
+// (other streams, other host threads) race and corrupt each other:
+// serialise them.
 #include <cstdio>
 #include <mutex>
 
 #include "hmec_internal.cuh"
+#include "hmec_sort.cuh"
 
 #define HMEC_NOALLOC_MAX_MARKERS (1 << 20)
 #define HMEC_NOALLOC_MAX_HALF_CELLS (1 << 18)
 
 namespace {
 
-constexpr int SCAN_CHUNK = 2048;
-constexpr int MAX_PARTS = (HMEC_NOALLOC_MAX_HALF_CELLS + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK + 1;
-// layout: [perm: MAX_MARKERS][count: MAX_HALF+1][start: MAX_HALF+2][scan partials: MAX_PARTS]
-constexpr size_t OFF_COUNT = HMEC_NOALLOC_MAX_MARKERS;
-constexpr size_t OFF_START = OFF_COUNT + HMEC_NOALLOC_MAX_HALF_CELLS + 1;
-constexpr size_t OFF_PART = OFF_START + HMEC_NOALLOC_MAX_HALF_CELLS + 2;
-constexpr size_t SCRATCH_INTS = OFF_PART + MAX_PARTS;
+constexpr int64_t MAXN = HMEC_NOALLOC_MAX_MARKERS;
+constexpr int64_t MAXH = HMEC_NOALLOC_MAX_HALF_CELLS;
+constexpr int64_t MAX_PARTS = (MAXH + 1 + 2047) / 2048 + 1;
+constexpr int64_t MAX_TILES = (MAXN + hsort::RS_BS - 1) / hsort::RS_BS;  // also bounds the radix grid
+// layout (int32): key [MAXN] | perm [MAXN] | count [MAXH+1] | start [MAXH+2] |
+// fill [MAXH+1] | scan partials [MAX_PARTS] | long flag [16] | radix scratch
+constexpr size_t OFF_PERM = MAXN;
+constexpr size_t OFF_COUNT = OFF_PERM + MAXN;
+constexpr size_t OFF_START = OFF_COUNT + MAXH + 1;
+constexpr size_t OFF_FILL = OFF_START + MAXH + 2;
+constexpr size_t OFF_PART = OFF_FILL + MAXH + 1;
+constexpr size_t OFF_FLAG = OFF_PART + MAX_PARTS;
+constexpr size_t OFF_RADIX = (OFF_FLAG + 16 + 63) / 64 * 64;
+constexpr size_t SCRATCH_INTS = OFF_RADIX + 3 * MAXN + hsort::RS_BINS * MAX_TILES + MAX_TILES + 16;
 
 }  // namespace
 
@@ -53,25 +67,6 @@ struct Mk {
     const double *xm, *ym, *t_marker, *rhom, *etasm, *etam, *cohescm, *cohestm, *frictcm, *dilatcm, *fricttm,
         *porm, *kkkm, *gm, *rhofm, *etafm;
 };
-
-struct Cells {
-    int ib, jb, iP, jP;
-};
-
-__device__ __forceinline__ Cells cells_of(double xm, double ym, const Geo& g) {
-    Cells c;
-    const float rdx = rcp_f32(g.dx), rdy = rcp_f32(g.dy);
-    c.jb = check_bounds(fix_quot(xm, g.dx, rdx, false), g.Nx);
-    c.ib = check_bounds(fix_quot(ym, g.dy, rdy, false), g.Ny);
-    c.jP = check_bounds(fix_quot(xm, g.dx, rdx, true), g.Nx);
-    c.iP = check_bounds(fix_quot(ym, g.dy, rdy, true), g.Ny);
-    return c;
-}
-
-__device__ __forceinline__ int half_key(const Cells& c, const Geo& g) {
-    const int di = min(max(c.iP - c.ib, 0), 1), dj = min(max(c.jP - c.jb, 0), 1);
-    return (2 * c.jb + dj) * (2 * (g.Ny - 1)) + 2 * c.ib + di;
-}
 
 // Marker properties of :389-423.
 struct Props {
@@ -113,99 +108,17 @@ __device__ __forceinline__ Props props_of(const Mk& mk, int m, const hmec_params
     return q;
 }
 
-__global__ void k_nz_zero(int32_t* a, int n) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) a[t] = 0;
-}
-
-__global__ void k_nz_count(Mk mk, int64_t n, Geo g, int32_t* count) {
-    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int k = -1;
-    if (m < n) k = half_key(cells_of(mk.xm[m], mk.ym[m], g), g);
-    const unsigned active = __ballot_sync(0xffffffffu, k >= 0);
-    if (k >= 0) {
-        const unsigned peers = __match_any_sync(active, k);
-        if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&count[k], __popc(peers));
-    }
-}
-
-// Exclusive scan in chunks of SCAN_CHUNK, then chunk offsets (one block), then add.
-__global__ void k_nz_scan1(const int32_t* in, int n, int32_t* out, int32_t* part) {
-    __shared__ int32_t sh[SCAN_CHUNK];
-    const int base = blockIdx.x * SCAN_CHUNK, t = threadIdx.x;
-    for (int k = t; k < SCAN_CHUNK; k += blockDim.x) sh[k] = (base + k < n) ? in[base + k] : 0;
-    __syncthreads();
-    if (t == 0) {  // chunks are short; a serial scan keeps this variant simple
-        int32_t acc = 0;
-        for (int k = 0; k < SCAN_CHUNK; k++) {
-            const int32_t v = sh[k];
-            sh[k] = acc;
-            acc += v;
-        }
-        part[blockIdx.x] = acc;
-    }
-    __syncthreads();
-    for (int k = t; k < SCAN_CHUNK; k += blockDim.x)
-        if (base + k < n) out[base + k] = sh[k];
-}
-
-__global__ void k_nz_scan2(int32_t* part, int nparts) {
-    if (threadIdx.x != 0) return;
-    int32_t acc = 0;
-    for (int k = 0; k < nparts; k++) {
-        const int32_t v = part[k];
-        part[k] = acc;
-        acc += v;
-    }
-}
-
-__global__ void k_nz_scan3(int32_t* out, int n, const int32_t* part, int32_t* cursor) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) {
-        const int32_t v = out[t] + part[t / SCAN_CHUNK];
-        out[t] = v;
-        cursor[t] = v;
-    }
-}
-
-__global__ void k_nz_scatter(Mk mk, int64_t n, Geo g, int32_t* cursor, int32_t* perm) {
-    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int k = -1;
-    if (m < n) k = half_key(cells_of(mk.xm[m], mk.ym[m], g), g);
-    const unsigned active = __ballot_sync(0xffffffffu, k >= 0);
-    if (k >= 0) {
-        const unsigned peers = __match_any_sync(active, k);
-        const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
-        int base = 0;
-        if (lane == leader) base = atomicAdd(&cursor[k], __popc(peers));
-        base = __shfl_sync(peers, base, leader);
-        perm[base + __popc(peers & ((1u << lane) - 1u))] = (int32_t)m;
-    }
-}
-
-__global__ void k_nz_segsort(const int32_t* start, int nseg, int32_t* perm) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nseg) return;
-    const int b = start[s], e = start[s + 1];
-    for (int a = b + 1; a < e; a++) {
-        const int v = perm[a];
-        int q = a;
-        while (q > b && perm[q - 1] > v) {
-            perm[q] = perm[q - 1];
-            q--;
-        }
-        perm[q] = v;
-    }
-}
-
 struct Out {
     double *RHO, *KKK, *TTT, *GGG, *ETA0, *COHT, *FRIT, *COHC, *FRIC, *DILC;
     double *ETAP, *POR, *ETAB0, *ETAP0, *GGGP;
     double *RHOX, *ETADX, *RHOFX, *PORX, *RHOY, *ETADY, *RHOFY, *PORY;
 };
 
-// grid: 0 basic, 1 P, 2 Vx, 3 Vy.  One thread per node; the same half-cell
-// runs, visiting order and weights as the context path.
+// grid: 0 basic, 1 P, 2 Vx, 3 Vy.  One thread per node sums over the
+// markers of the half cells around it (in the sorted order) with the
+// reference's bilinear weights, in FP64; the context path sums per cell
+// corner in double-float and then adds four cells, so the results agree to
+// about 1e-13 relative.
 template <int GRID>
 __global__ void k_nz_gather(Mk mk, hmec_params p, Geo g, const int32_t* __restrict__ start,
                             const int32_t* __restrict__ perm, Out o) {
@@ -227,7 +140,7 @@ __global__ void k_nz_gather(Mk mk, hmec_params p, Geo g, const int32_t* __restri
             for (int k = b; k < e; k++) {
                 const int m = perm[k];
                 const double xmm = mk.xm[m], ymm = mk.ym[m];
-                const Cells c = cells_of(xmm, ymm, g);
+                const MarkerCells c = marker_cells(xmm, ymm, g);
                 double xn, yn;
                 if (GRID == 0) {
                     xn = linsp(g.Nx, 0, p.xsize, c.jb);
@@ -307,8 +220,39 @@ __global__ void k_nz_gather(Mk mk, hmec_params p, Geo g, const int32_t* __restri
     }
 }
 
+// The device address of g_p2g_scratch for the current device.  The host
+// name of the array is only a stand-in, so the address is looked up with the
+// device current, once per device and CUDA context: a context that was torn
+// down and created again (cudaDeviceReset) gets a new ID, and the address is
+// looked up again.
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+struct ScratchAddr {
+    unsigned long long ctx_id;
+    int32_t* ptr;
+};
 std::mutex g_setup_mutex;
-int32_t* g_scratch_addr[256];  // device address of g_p2g_scratch, per device ordinal
+ScratchAddr g_scratch_addr[256];
+
+bool current_ctx_id(unsigned long long* id) {
+    static PfnCtxGetCurrent get_cur = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    if (!get_cur || !get_id) {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa = cudaDriverEntryPointSymbolNotFound, qb = qa;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) != cudaSuccess ||
+            qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b)
+            return false;
+        get_cur = (PfnCtxGetCurrent)a;
+        get_id = (PfnCtxGetId)b;
+    }
+    CUcontext c = nullptr;
+    if (get_cur(&c) != CUDA_SUCCESS || !c) return false;
+    return get_id(c, id) == CUDA_SUCCESS;
+}
 
 int noalloc_fail(int code, const char* msg) {
     fprintf(stderr, "hmec_markers_to_nodes_noalloc: %s\n", msg);
@@ -340,37 +284,22 @@ extern "C" int32_t hmec_markers_to_nodes_noalloc(const hmec_params* p, const dou
         return noalloc_fail(HMEC_ERR_CUDA, "cudaGetDevice failed");
     int32_t* scratch = nullptr;
     {
-        // Set-up, once per device, with that device current: the host name of
-        // g_p2g_scratch is only a stand-in, the kernels need its device address.
         std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_scratch_addr[dev]) {
+        unsigned long long id = 0;
+        const bool have_id = current_ctx_id(&id);
+        ScratchAddr& sa = g_scratch_addr[dev];
+        if (!sa.ptr || !have_id || sa.ctx_id != id) {
             int32_t* ptr = nullptr;
             const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_p2g_scratch);
             if (e != cudaSuccess || !ptr) return noalloc_fail(HMEC_ERR_CUDA, cudaGetErrorString(e));
-            g_scratch_addr[dev] = ptr;
+            unsigned long long id2 = 0;
+            sa.ptr = ptr;
+            sa.ctx_id = current_ctx_id(&id2) ? id2 : 0;  // the lookup made the context current
         }
-        scratch = g_scratch_addr[dev];
+        scratch = sa.ptr;
     }
-    int32_t* perm = scratch;
-    int32_t* count = scratch + OFF_COUNT;
-    int32_t* start = scratch + OFF_START;
-    int32_t* part = scratch + OFF_PART;
     Geo g;
-    g.Nx = p->Nx;
-    g.Ny = p->Ny;
-    g.Nx1 = p->Nx + 1;
-    g.Ny1 = p->Ny + 1;
-    g.N = g.Nx1 * g.Ny1 * 6;
-    g.line_fault = (int)((p->Ny - 1) / 2.);
-    g.dx = p->xsize / (p->Nx - 1);
-    g.dy = p->ysize / (p->Ny - 1);
-    g.dx2 = g.dx * g.dx;
-    g.dy2 = g.dy * g.dy;
-    g.dx_dy = g.dx * g.dy;
-    g.lower_block = p->ysize / 2. + g.dy;
-    g.upper_block = p->ysize / 2. - g.dy;
-    g.dy_faultw = g.dy / g.dx;
-    geo_reciprocals(g);
+    geo_make(g, p->Nx, p->Ny, p->xsize, p->ysize);
     Mk mk{markers[HMEC_M_xm], markers[HMEC_M_ym], markers[HMEC_M_t_marker], markers[HMEC_M_rhom],
           markers[HMEC_M_etasm], markers[HMEC_M_etam], markers[HMEC_M_cohescm], markers[HMEC_M_cohestm],
           markers[HMEC_M_frictcm], markers[HMEC_M_dilatcm], markers[HMEC_M_fricttm], markers[HMEC_M_porm],
@@ -381,16 +310,16 @@ extern "C" int32_t hmec_markers_to_nodes_noalloc(const hmec_params* p, const dou
           fields[HMEC_F_RHOX], fields[HMEC_F_ETADX], fields[HMEC_F_RHOFX], fields[HMEC_F_PORX],
           fields[HMEC_F_RHOY], fields[HMEC_F_ETADY], fields[HMEC_F_RHOFY], fields[HMEC_F_PORY]};
     cudaStream_t s = (cudaStream_t)stream;
-    const int ns = (int)nh + 1;
-    const int nparts = (ns + SCAN_CHUNK - 1) / SCAN_CHUNK;
-    // the array keeps the last call's contents: the histogram must start at zero
-    k_nz_zero<<<nblocks(ns, 256), 256, 0, s>>>(count, ns);
-    k_nz_count<<<nblocks(n, 256), 256, 0, s>>>(mk, n, g, count);
-    k_nz_scan1<<<nparts, 256, 0, s>>>(count, ns, start, part);
-    k_nz_scan2<<<1, 32, 0, s>>>(part, nparts);
-    k_nz_scan3<<<nblocks(ns, 256), 256, 0, s>>>(start, ns, part, count);  // count becomes the scatter cursor
-    k_nz_scatter<<<nblocks(n, 256), 256, 0, s>>>(mk, n, g, count, perm);
-    k_nz_segsort<<<nblocks(nh, 128), 128, 0, s>>>(start, (int)nh, perm);
+    hsort::SortBufs sb{scratch, scratch + OFF_COUNT, scratch + OFF_START, scratch + OFF_FILL, scratch + OFF_PART,
+                       scratch + OFF_PERM, scratch + OFF_FLAG, scratch + OFF_RADIX};
+    const int32_t* start = sb.start;
+    const int32_t* perm = sb.perm;
+    // the array keeps the last call's contents: the histogram starts at zero
+    cudaError_t e0 = cudaMemsetAsync(sb.count, 0, sizeof(int32_t) * ((size_t)nh + 1), s);
+    if (e0 != cudaSuccess) return noalloc_fail(HMEC_ERR_CUDA, cudaGetErrorString(e0));
+    hsort::k_keys<<<nblocks(n, 256), 256, 0, s>>>(mk.xm, mk.ym, n, g, sb.key, sb.count, nullptr);
+    e0 = hsort::sort_by_half_cell(s, sb, n, (int)nh, nullptr);
+    if (e0 != cudaSuccess) return noalloc_fail(HMEC_ERR_CUDA, cudaGetErrorString(e0));
     const dim3 bb(64);
     k_nz_gather<0><<<dim3(nblocks(g.Ny, 64), g.Nx), bb, 0, s>>>(mk, *p, g, start, perm, o);
     k_nz_gather<1><<<dim3(nblocks(g.Ny1, 64), g.Nx1), bb, 0, s>>>(mk, *p, g, start, perm, o);

@@ -1608,24 +1608,6 @@ __global__ void k_xupdate(int N, const double* __restrict__ Z, const double* __r
 
 // ===================================================================== host
 
-static void make_geo(Geo& g, int Nx, int Ny, double xsize, double ysize) {
-    g.Nx = Nx;
-    g.Ny = Ny;
-    g.Nx1 = Nx + 1;
-    g.Ny1 = Ny + 1;
-    g.N = g.Nx1 * g.Ny1 * 6;
-    g.line_fault = (int)((Ny - 1) / 2.);
-    g.dx = xsize / (Nx - 1);
-    g.dy = ysize / (Ny - 1);
-    g.dx2 = g.dx * g.dx;
-    g.dy2 = g.dy * g.dy;
-    g.dx_dy = g.dx * g.dy;
-    g.lower_block = ysize / 2. + g.dy;
-    g.upper_block = ysize / 2. - g.dy;
-    g.dy_faultw = g.dy / g.dx;
-    geo_reciprocals(g);
-}
-
 static std::vector<int32_t> boundary_rows(const Geo& g) {
     std::vector<int32_t> r;
     for (int j = 0; j <= g.Nx; j++)
@@ -1846,7 +1828,7 @@ int solver_alloc(hmec_ctx* ctx) {
         nx = cx + 1;
         ny = cy + 1;
         Level L;
-        make_geo(L.g, nx, ny, xs, ys);
+        geo_make(L.g, nx, ny, xs, ys);
         sv.lv.push_back(L);
     }
     for (size_t l = 0; l < sv.lv.size(); l++) {

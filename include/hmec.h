@@ -276,14 +276,19 @@ int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, do
  * holds on the current device: markers[k] is the device array of marker
  * field k (enum hmec_marker_field), fields[f] the column-major device array
  * of node field f (entries of fields that are not outputs may be NULL).
- * Scratch memory is one fixed array compiled into the library (about 6 MiB
- * on every device that loads it, held until exit); hence the limits: at most
- * HMEC_NOALLOC_MAX_MARKERS = 1048576 markers and 4*(Nx-1)*(Ny-1) <=
- * HMEC_NOALLOC_MAX_HALF_CELLS = 262144, larger inputs return HMEC_ERR_ARG.
- * Kernels go to `stream` (a cudaStream_t; NULL = legacy default stream).
- * The first call on a device looks up the array's device address, so make
- * it before any stream capture.  All calls share the array: calls that
- * overlap on the GPU race, serialise them.                                  */
+ * Scratch memory is one fixed array compiled into the library, about 25 MiB
+ * of device memory; hence the limits: at most HMEC_NOALLOC_MAX_MARKERS =
+ * 1048576 markers and 4*(Nx-1)*(Ny-1) <= HMEC_NOALLOC_MAX_HALF_CELLS =
+ * 262144, larger inputs return HMEC_ERR_ARG.  The driver reserves the array
+ * when it loads the library's device code on a device and keeps it until the
+ * process exits; under lazy module loading (the CUDA default) that happens
+ * in the first call on the device, which can then fail if the host's own
+ * allocator has already taken the device's memory -- make one call early, or
+ * set CUDA_MODULE_LOADING=EAGER.  Kernels go to `stream` (a cudaStream_t;
+ * NULL = legacy default stream).  The first call on a device (and the first
+ * after a device reset) looks up the array's device address, so make it
+ * before any stream capture.  All calls share the array, which keeps the
+ * last call's contents: calls that overlap on the GPU race, serialise them. */
 int32_t hmec_markers_to_nodes_noalloc(const hmec_params* p, const double* const* markers, int64_t n,
                                       double* const* fields, void* stream);
 /* The library's marker cell index on n host coordinates x[k] (copied to the

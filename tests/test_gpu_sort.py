@@ -1,0 +1,71 @@
+"""The half-cell counting sort on markers that cluster.
+
+Markers normally spread a few per half cell, and each segment of the sorted
+order is put in marker-index order by one thread.  When many markers share a
+half cell (they cluster, or coordinates outside the domain are clamped into
+an edge cell by check_bounds, cpp/h_mec_rsf_v9.cpp:144-151), the long
+segments are left to the stable radix sort instead.  Both must give the
+oracle's node fields (to the 1e-13 of the marker->node parity tests, the
+summation order differing from the reference's serial marker loop) and be
+bit-identical across runs.
+"""
+import numpy as np
+import pytest
+
+import pairs
+from pairs import P2G_FIELDS
+
+pytestmark = pytest.mark.gpu
+
+
+def clustered(preset, frac=0.4, seed=11):
+    """The preset's markers with a fraction moved into one cell and some onto
+    the far corner of the domain, whose cell index fix(xsize/dx) = Nx-1 is
+    clamped into the last cell by check_bounds."""
+    o, mk, nodes = pairs.oracle_for(preset)
+    p = o.params
+    dx, dy = p.xsize / (p.Nx - 1), p.ysize / (p.Ny - 1)
+    rng = np.random.default_rng(seed)
+    n = len(mk["xm"])
+    pick = rng.permutation(n)
+    a, b = pick[: int(frac * n)], pick[int(frac * n): int((frac + 0.05) * n)]
+    mk = {k: v.copy() for k, v in mk.items()}
+    cx, cy = 3 * dx, 2 * dy
+    mk["xm"][a] = cx + rng.uniform(0.1, 0.9, a.size) * dx
+    mk["ym"][a] = cy + rng.uniform(0.1, 0.9, a.size) * dy
+    mk["xm"][b] = p.xsize
+    mk["ym"][b] = p.ysize
+    o.set_markers(mk)
+    return o, mk, nodes
+
+
+@pytest.mark.parametrize("preset", ["tiny", "ref"])
+def test_clustered_markers_match_oracle_and_repeat(preset):
+    o, mk, nodes = clustered(preset)
+    m = pairs.model_for(preset, mk, nodes)
+    o.markers_to_nodes()
+    m.markers_to_nodes()
+    first = {f: m.field(f) for f in P2G_FIELDS}
+    e = pairs.field_errors(m, o, P2G_FIELDS)
+    assert max(e.values()) < 1e-13, e
+    m.markers_to_nodes()
+    for f in P2G_FIELDS:
+        assert np.array_equal(first[f], m.field(f)), f
+
+
+def test_clustered_and_spread_markers_in_one_model():
+    """Upload spread markers, then clustered ones, then spread ones again:
+    each P2G equals a fresh model's (the long-segment flag is cleared every
+    step)."""
+    o0, mk0, nodes = pairs.oracle_for("tiny")
+    _, mk1, _ = clustered("tiny")
+    m = pairs.model_for("tiny", mk0, nodes)
+    ref0 = pairs.model_for("tiny", mk0, nodes)
+    ref1 = pairs.model_for("tiny", mk1, nodes)
+    ref0.markers_to_nodes()
+    ref1.markers_to_nodes()
+    for mk, ref in ((mk0, ref0), (mk1, ref1), (mk0, ref0)):
+        m.upload_markers(mk)
+        m.markers_to_nodes()
+        for f in P2G_FIELDS:
+            assert np.array_equal(m.field(f), ref.field(f)), f

@@ -1,12 +1,16 @@
 """The allocation-free markers -> nodes entry point.
 
 hmec_markers_to_nodes_noalloc() is for hosts that may not call cudaMalloc
-(an application that owns the device allocator, code under CUDA-graph
-capture, a real-time loop that must not block on the allocator).  It keeps
-its scratch in a fixed array compiled into the library and must produce the
-node fields of the context path, hmec_markers_to_nodes(), on the same
-markers.  This file is collected last so a failure here never hides another
-test; it passes alone in a fresh process and after the rest of the suite.
+(an application that owns the device allocator and forbids allocations
+behind its back, a real-time loop that must not block on the allocator).  It
+keeps its scratch in a fixed array compiled into the library and must
+produce the node fields of the context path, hmec_markers_to_nodes(), on the
+same markers, to the 1e-13 of the marker->node parity tests (the two sum in
+different orders).  Configuration 1 (1,000,000 markers, 160,000 half cells)
+sits just inside both of its limits; the clustered case sends long half-cell
+segments through the radix sort.  This file is collected last so a failure
+here never hides another test; it passes alone in a fresh process and after
+the rest of the suite.
 """
 import ctypes as C
 
@@ -23,11 +27,14 @@ pytestmark = pytest.mark.gpu
 MAX_MARKERS = 1 << 20
 
 
-def _setup(preset):
+def _setup(preset, mk=None):
     import torch
 
     p = hmec.default_params(**pairs.overrides(preset))
-    mk, nodes = synth.make_state(p, preset)
+    if mk is None:
+        mk, nodes = synth.make_state(p, preset)
+    else:
+        nodes = None
     # device inputs and outputs are the caller's (allocated here by torch)
     dev_mk = [torch.from_numpy(np.ascontiguousarray(mk[k])).cuda() for k in hmec.MARKERS]
     shapes = {}
@@ -42,10 +49,31 @@ def _setup(preset):
     return p, mk, nodes, dev_mk, dev_out, shapes, mk_ptrs, f_ptrs
 
 
-def test_noalloc_matches_context_path_on_two_calls():
+def _clustered(preset):
+    """The preset's markers with 40 % moved into one cell and 5 % onto the far
+    corner of the domain (clamped into the last cell)."""
+    p = hmec.default_params(**pairs.overrides(preset))
+    mk, _ = synth.make_state(p, preset)
+    dx, dy = p.xsize / (p.Nx - 1), p.ysize / (p.Ny - 1)
+    rng = np.random.default_rng(7)
+    n = len(mk["xm"])
+    pick = rng.permutation(n)
+    a, b = pick[: int(0.4 * n)], pick[int(0.4 * n): int(0.45 * n)]
+    mk = {k: v.copy() for k, v in mk.items()}
+    mk["xm"][a] = 3 * dx + rng.uniform(0.1, 0.9, a.size) * dx
+    mk["ym"][a] = 2 * dy + rng.uniform(0.1, 0.9, a.size) * dy
+    mk["xm"][b] = p.xsize
+    mk["ym"][b] = p.ysize
+    return mk
+
+
+@pytest.mark.parametrize("case", ["c0", "c1", "ref-clustered"])
+def test_noalloc_matches_context_path_on_two_calls(case):
     import torch
 
-    p, mk, nodes, dev_mk, dev_out, shapes, mk_ptrs, f_ptrs = _setup("c0")
+    preset = case.split("-")[0]
+    mk0 = _clustered(preset) if case.endswith("clustered") else None
+    p, mk, nodes, dev_mk, dev_out, shapes, mk_ptrs, f_ptrs = _setup(preset, mk0)
     m = hmec.Model(p)
     m.upload_markers(mk)
     m.markers_to_nodes()
