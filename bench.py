@@ -3,17 +3,22 @@
 
 A step is one timestep of the reference loop (markers -> nodes, global
 iterations with assembly + solve + stress + fault update + adaptive dt, end of
-step), run through the C ABI of libhmec_gpu.so on synthetic configuration 1
-(201 x 201 nodes, 5 x 5 markers per cell, 1.0 M markers).  `value` is the
-mixed form (FP32 multigrid-preconditioned FP64 FGMRES) with inputs resident in
-HBM; the plain FP64 form is measured the same way beside it; `e2e` re-runs the
+step), run through the C ABI of libhmec_gpu.so on a seeded synthetic model.
+The headline line is configuration 2 (1001 x 401 nodes, 40 x 16 km, 6 x 6
+markers per cell, 14.4 M markers), where the 5x target is stated: `value` is
+the mixed form (FP32 multigrid-preconditioned FP64 FGMRES) with inputs
+resident in HBM, `fp64_form` the plain FP64 form on the same steps, `e2e` the
 mixed form with the model state copied from pinned host buffers every step.
+The same line carries configuration 1 (201 x 201, 1.0 M markers; its
+accuracy is measured against the FP64 CPU oracle) and configuration 3 (the
+64-member ensemble) as extra blocks.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config c2|c1|c3] [--no-extra] [--no-cpu-baseline]
 
 --impl reference times the CPU restatement of the reference (the oracle: the
 reference itself needs Eigen, HDF5 and MKL Pardiso, none of which exist here)
-on the host cores, on the same workload.
+on the host cores, on a bounded sample of the same workload.
 """
 import argparse
 import json
@@ -22,7 +27,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -31,12 +35,23 @@ for _p in (os.path.join(ROOT, "h-mecs-2d_gb300"), os.path.join(ROOT, "oracle")):
         sys.path.insert(0, _p)
 
 METRIC = "timesteps/s on 1 GB300: mixed-prec batched vs plain FP64, at ≤1e-8 rel err"
-CONFIG = "c1"
-WORKLOAD = "config 1: 201x201 nodes, 10x10 km, 5x5 markers/cell (1,000,000 markers), seeded synthetic fault model"
-DOMINANT = "k_smooth"
-# DRAM bytes (read + write) per launch of the fused V-cycle kernel (one launch
-# = one config-1 V-cycle), from one ncu capture of the kernel (profiles/)
-SMOOTH_TRAFFIC_BYTES = 94.97e6
+TARGET_REL_ERR = 1e-8
+
+# Per configuration: the workload, and the DRAM bytes (read + write) of one
+# launch of the dominant kernel (one V-cycle of the mixed form) from an ncu
+# capture of that configuration (profiles/); None where none was taken.
+CONFIGS = {
+    "c1": dict(workload="config 1: 201x201 nodes, 10x10 km, 5x5 markers/cell (1,000,000 markers), "
+                        "seeded synthetic fault model",
+               vcycle_dram_bytes=94.97e6, dram_source="profiles/k_vcycle_stage_c1.md"),
+    "c2": dict(workload="config 2: 1001x401 nodes, 40x16 km, 6x6 markers/cell (14,400,000 markers), "
+                        "log-normal host viscosity (1e22 Pa s, sigma 1 decade), 1e19 Pa s fault band, "
+                        "log-uniform permeability 1e-21..1e-14 m^2",
+               vcycle_dram_bytes=None, dram_source=None),
+}
+DOMINANT = "k_smooth"  # library profiling prefix: the smoothing passes (the fused V-cycle in the mixed form)
+FIELDS_ACC = ("vxs", "vys", "pt", "pf", "VSLIPB")
+GROUPS_ACC = {"velocity": ("vxs", "vys")}
 
 
 def parse():
@@ -45,7 +60,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default=CONFIG)
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3"])
+    ap.add_argument("--no-extra", action="store_true", help="headline configuration only")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -135,20 +151,88 @@ def shard(items, rank, world):
     return list(items)[rank::world]
 
 
+def balanced_split(costs, world):
+    """Indices of the work items of each rank, balancing the summed cost:
+    longest-processing-time greedy (items by decreasing cost, each to the
+    least-loaded rank; ties to the lower index), deterministic."""
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    load = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        parts[r].append(i)
+        load[r] += costs[i]
+    return [sorted(p) for p in parts]
+
+
+def member_cost(over):
+    """Expected work of an ensemble member: its cells (the iteration counts
+    of uneven members are alike, so cells carry the difference)."""
+    return float((over["Nx"] + 1) * (over["Ny"] + 1))
+
+
 def whole_job_rate(units_per_rank, world, seconds_max):
     """Units all ranks processed per second of the slowest rank."""
     return units_per_rank * world / seconds_max
 
 
+# ------------------------------------------------------------------ helpers
+def vcycle_levels(p):
+    """Cells (staggered nodes) of each multigrid level, as the library builds them."""
+    nx, ny = p.Nx, p.Ny
+    out = [(nx + 1) * (ny + 1)]
+    while len(out) < max(1, p.mg_levels):
+        cx, cy = nx // 2, ny // 2
+        if cx < 4 or cy < 4:
+            break
+        nx, ny = cx + 1, cy + 1
+        out.append((nx + 1) * (ny + 1))
+    return out
+
+
+def vcycle_bytes_compulsory(p, value_bytes=4):
+    """Compulsory bytes of one V-cycle: per level and sweep, every cell's 42
+    coefficients and three six-value vectors (unknowns read and written,
+    rhs), (pre + post + 1 residual/restriction) sweeps on each level and
+    the coarse sweeps on the coarsest."""
+    lv = vcycle_levels(p)
+    per = 60.0 * value_bytes
+    tot = sum((p.mg_pre + p.mg_post + 1) * per * c for c in lv[:-1])
+    return tot + max(1, p.mg_coarse_sweeps) * per * lv[-1]
+
+
+def rel_errors(got, ref):
+    import numpy as np
+
+    out = {}
+    for f in ref:
+        den = float(np.max(np.abs(ref[f]))) or 1.0
+        out[f] = float(np.max(np.abs(got[f] - ref[f]))) / den
+    for g, names in GROUPS_ACC.items():
+        if all(n in ref for n in names):
+            den = max(float(np.max(np.abs(ref[n]))) for n in names) or 1.0
+            out[g] = max(float(np.max(np.abs(got[n] - ref[n]))) for n in names) / den
+    return out
+
+
+def judged(err):
+    """The errors the target is judged on: velocity as one vector field (vys
+    alone is near zero in simple shear), pt, pf and the slip rate."""
+    keys = ("velocity", "pt", "pf", "VSLIPB")
+    worst = max(err[k] for k in keys if k in err)
+    return {"judged_on": list(keys), "max": worst, "target": TARGET_REL_ERR, "met": worst <= TARGET_REL_ERR}
+
+
 # -------------------------------------------------------------------- GPU arm
-def make_model(form, cfg, device_index):
+def make_model(form, cfg, mk=None, nodes=None):
     import hmec
     from hmec import synth
 
     over = dict(synth.PRESETS[cfg], form=form, krylov_rtol=1e-15, krylov_restart=40, krylov_maxit=4000)
     p = hmec.default_params(**over)
     m = hmec.Model(p)
-    mk, nodes = synth.make_state(p, cfg)
+    if mk is None:
+        mk, nodes = synth.make_state(p, cfg)
     m.upload_markers(mk)
     for k, v in nodes.items():
         m.upload_field(k, v)
@@ -180,53 +264,63 @@ def timed_steps(m, steps, flush, per_step=None):
     return total, reps
 
 
-def run_gpu(args, rank, world, device_index):
+def roofline(prof, ms_total, p, peaks, cfg, kernel):
+    """The dominant kernel's live roofline from the library's CUDA-event timing."""
+    nprof, prof_ms, b_alg, b_moved = prof
+    peak = peaks.get("hbm_gbs")
+    src = "measured (MEASURED_PEAKS.json hbm_gbs)"
+    if not peak:
+        peak, src = 6800.0, "fallback 6800"
+    per_launch_alg = b_alg / nprof if nprof else None
+    achieved = (b_alg / nprof) / (prof_ms / nprof / 1e3) / 1e9 if nprof and prof_ms > 0 else None
+    traffic = CONFIGS.get(cfg, {}).get("vcycle_dram_bytes")
+    out = {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak if achieved else None, "peak_source": src,
+           "bytes_per_launch_compulsory": per_launch_alg,
+           "bytes_per_launch_moved": (b_moved / nprof) if nprof else None,
+           "achieved_moved_gbs": (b_moved / nprof) / (prof_ms / nprof / 1e3) / 1e9 if nprof and prof_ms > 0 else None,
+           "compulsory_bytes_model": "per cell and sweep 42 coefficients + 3 x 6 values (FP32: 240 B), "
+                                     "(pre + post + 1) sweeps per level, coarse sweeps on the coarsest "
+                                     "(V-cycle formula of %.1f MB at this grid)" % (vcycle_bytes_compulsory(p) / 1e6),
+           "traffic": traffic,
+           "traffic_note": ("DRAM read+write per launch from ncu (%s)" % CONFIGS[cfg]["dram_source"]) if traffic
+           else "not captured for this configuration",
+           "waste_ratio": (traffic / per_launch_alg) if (traffic and per_launch_alg) else None,
+           "launches_timed": nprof, "avg_launch_us": (1e3 * prof_ms / nprof) if nprof else None,
+           "share_of_step_time": prof_ms / ms_total if ms_total else None}
+    return out
+
+
+def run_gpu(args, cfg, world, device_index, peaks, with_fp64=True, with_e2e=True, with_acc=True):
     import numpy as np
     import torch
 
     import hmec
-    from hmec import synth
 
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
     flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def flush():
         flush_buf.fill_(1.0)
 
-    def barrier():
-        rank_barrier(world)
-
-    def max_over_ranks(x):
-        return rank_max(x, world)
-
     out = {}
-    # ---- mixed form (value), with the live roofline of the dominant kernel
-    m, mk, nodes, p = make_model(hmec.FORM_MIXED, args.config, device_index)
+    m, mk, nodes, p = make_model(hmec.FORM_MIXED, cfg)
     for _ in range(args.warmup):
         m.timestep()
     m.profile_kernel(DOMINANT)
-    barrier()
+    rank_barrier(world)
     torch.cuda.synchronize()
     l0 = m.launches
     with ClockSampler(device_index) as clk:
         ms, reps = timed_steps(m, args.steps, flush)
     launches = m.launches - l0
-    nprof, prof_ms, prof_bytes = m.profile_read()
+    prof = m.profile_read()
     m.profile_kernel(None)
-    ms = max_over_ranks(ms)
-    barrier()
-    gi = sum(r["global_iters"] for r in reps)
-    kr = sum(r["krylov_iters"] for r in reps)
-    out["mixed"] = dict(ms=ms, reps=reps, launches=launches, gi=gi, kr=kr, clocks=clk.summary(),
-                        prof=(nprof, prof_ms, prof_bytes))
-    mixed_state = ("vxs", "vys", "pt", "pf", "VSLIPB")  # the fields the accuracy check compares
+    ms = rank_max(ms, world)
+    rank_barrier(world)
+    out["mixed"] = dict(ms=ms, reps=reps, launches=launches, gi=sum(r["global_iters"] for r in reps),
+                        kr=sum(r["krylov_iters"] for r in reps), clocks=clk.summary(), prof=prof, p=p)
 
-    # ---- e2e: model state through pinned host buffers every step
-    if not args.no_e2e:
+    if with_e2e:
         pin = {}
         for k, v in mk.items():
             t = torch.empty(v.shape, dtype=torch.float64, pin_memory=True)
@@ -264,79 +358,112 @@ def run_gpu(args, rank, world, device_index):
                 for f, (flat, r, c) in list(host_out.items()) + list(host_state.items()):
                     m.L.hmec_download_field(m.h, hmec.FIELDS.index(f), ptr(flat), r, c)
 
-        barrier()
-        e2e_ms, e2e_reps = timed_steps(m, args.steps, flush, per_step=hook)
-        e2e_ms = max_over_ranks(e2e_ms)
-        out["e2e"] = dict(ms=e2e_ms, h2d=h2d, d2h=d2h)
+        rank_barrier(world)
+        e2e_ms, _ = timed_steps(m, args.steps, flush, per_step=hook)
+        out["e2e"] = dict(ms=rank_max(e2e_ms, world), h2d=h2d, d2h=d2h)
     m.close()
 
-    # ---- plain FP64 form, same steps
-    if not args.no_fp64:
-        m2, _, _, _ = make_model(hmec.FORM_FP64, args.config, device_index)
+    if with_fp64:
+        m2, _, _, _ = make_model(hmec.FORM_FP64, cfg, mk, nodes)
         for _ in range(args.warmup):
             m2.timestep()
-        barrier()
+        rank_barrier(world)
         ms2, reps2 = timed_steps(m2, args.steps, flush)
-        ms2 = max_over_ranks(ms2)
-        # accuracy of the mixed form: one timestep from the same state in both
-        # forms (after many steps the adaptive dt sequences of the two runs
-        # part ways on discrete decisions, and their states are then at
-        # different times)
-        snap = m2.snapshot()
-        m2.timestep()
-        fp64_next = {f: m2.field(f) for f in mixed_state}
-        dt64 = m2.scalar("dt")
+        ms2 = rank_max(ms2, world)
+        f = dict(ms=ms2, gi=sum(r["global_iters"] for r in reps2), kr=sum(r["krylov_iters"] for r in reps2))
+        if with_acc:
+            # accuracy of the mixed form against the FP64 form: one timestep
+            # from the same state in both (after many steps the two runs' dt
+            # sequences part ways on discrete decisions)
+            snap = m2.snapshot()
+            m2.timestep()
+            ref = {k: m2.field(k) for k in FIELDS_ACC}
+            dt64 = m2.scalar("dt")
+            m3, _, _, _ = make_model(hmec.FORM_MIXED, cfg, mk, nodes)
+            m3.load_state(snap)
+            m3.timestep()
+            f["err"] = rel_errors({k: m3.field(k) for k in FIELDS_ACC}, ref)
+            f["same_dt"] = m3.scalar("dt") == dt64
+            m3.close()
         m2.close()
-        m3, _, _, _ = make_model(hmec.FORM_MIXED, args.config, device_index)
-        m3.load_state(snap)
-        m3.timestep()
-        err = {}
-        got = {f: m3.field(f) for f in fp64_next}
-        for f, b in fp64_next.items():
-            den = float(np.max(np.abs(b))) or 1.0
-            err[f] = float(np.max(np.abs(got[f] - b))) / den
-        # the velocity field as one quantity (as the parity tests group it):
-        # vys alone is small in this simple-shear setup
-        den = max(float(np.max(np.abs(fp64_next[f]))) for f in ("vxs", "vys")) or 1.0
-        err["velocity"] = max(float(np.max(np.abs(got[f] - fp64_next[f]))) for f in ("vxs", "vys")) / den
-        dt_equal = m3.scalar("dt") == dt64
-        m3.close()
-        out["fp64"] = dict(ms=ms2, gi=sum(r["global_iters"] for r in reps2), kr=sum(r["krylov_iters"] for r in reps2),
-                           err=err, dt_equal=dt_equal)
-    return out, peaks
+        out["fp64"] = f
+    return out
 
 
 # ------------------------------------------------------------------ CPU arm
-def cpu_sample(cfg, budget_s=30.0, max_steps=2):
-    """Time the CPU oracle (restatement of the reference) on the first steps of cfg."""
+def oracle_steps(cfg, nsteps, budget_s):
+    """The CPU oracle (restatement of the reference) on the first steps of cfg
+    from the initial state; returns its timing and the fields of FIELDS_ACC."""
     import oracle as O
     from hmec import synth
 
-    over = dict(synth.PRESETS[cfg])
-    p = O.default_params(**over)
+    p = O.default_params(**synth.PRESETS[cfg])
     o = O.Oracle(p)
     mk, nodes = synth.make_state(p, cfg)
     o.set_markers(mk)
     for k, v in nodes.items():
         o.set_field(k, v)
     t0 = time.perf_counter()
-    steps = 0
-    gi = 0
-    while steps < max_steps:
+    steps = gi = 0
+    while steps < nsteps:
         gi += o.timestep()
         steps += 1
         if time.perf_counter() - t0 > budget_s:
             break
     el = time.perf_counter() - t0
-    return dict(value=steps / el, steps=steps, seconds=el, global_iters=gi)
+    return dict(value=steps / el, steps=steps, seconds=el, global_iters=gi,
+                fields={k: o.field(k).copy() for k in FIELDS_ACC}, mk=mk, nodes=nodes)
 
 
+def oracle_sample_no_solve(cfg, global_iters_per_step):
+    """A bounded CPU sample of one timestep of a configuration too large for a
+    direct solve per global iteration (config 2: one SuperLU solve of its
+    2.4 M unknowns takes minutes): the oracle's markers -> nodes, step begin,
+    and per global iteration the preparation and assembly, timed; the direct
+    solves and the sections after them are left out, so the rate is an upper
+    bound of the oracle's timesteps/s."""
+    import oracle as O
+    from hmec import synth
+
+    p = O.default_params(**synth.PRESETS[cfg])
+    o = O.Oracle(p)
+    mk, nodes = synth.make_state(p, cfg)
+    o.set_markers(mk)
+    for k, v in nodes.items():
+        o.set_field(k, v)
+    t0 = time.perf_counter()
+    o.markers_to_nodes()
+    o.timestep_begin()
+    t1 = time.perf_counter()
+    o.iter_prepare()
+    o.assemble()
+    t2 = time.perf_counter()
+    per_step = (t1 - t0) + global_iters_per_step * (t2 - t1)
+    return dict(value=1.0 / per_step, seconds=t2 - t0, p2g_s=t1 - t0, assemble_s=t2 - t1)
+
+
+def cpu_block(cfg, gi_per_step):
+    if cfg == "c2":
+        r = oracle_sample_no_solve(cfg, gi_per_step)
+        return {"value": r["value"], "unit": "timesteps/s", "cores": 1, "kind": "port", "upper_bound": True,
+                "sample": "config 2, first timestep: oracle markers->nodes + step begin (%.2f s) and one global "
+                          "iteration's preparation + assembly (%.2f s) x %.1f global iterations per step; the "
+                          "direct solves (SuperLU, single thread, minutes each at 2.4 M unknowns) and the "
+                          "sections after them are not run, so this is an upper bound"
+                          % (r["p2g_s"], r["assemble_s"], gi_per_step)}
+    r = oracle_steps(cfg, 3, 40.0)
+    return {"value": r["value"], "unit": "timesteps/s", "cores": 1, "kind": "port",
+            "sample": "first %d timesteps of %s from the initial state, %.1f s (oracle: C restatement + SciPy "
+                      "SuperLU direct solve, one thread)" % (r["steps"], cfg, r["seconds"])}
+
+
+# ------------------------------------------------------------------ ensembles
 def run_ensemble(args, rank=0, world=1, device_index=0, nmembers=64):
     """Configuration 3: 64 uneven members advanced concurrently (mixed form)
     against the same members run one after another in the plain FP64 form.
     Many streams are in flight, so this mode times with a device-wide
     synchronize on both sides of the timed region.  Under torchrun the
-    members shard by rank (64 per rank, weak scaling)."""
+    members shard by rank with balanced cells (64 per rank, weak scaling)."""
     import torch
 
     import hmec
@@ -344,8 +471,9 @@ def run_ensemble(args, rank=0, world=1, device_index=0, nmembers=64):
     from hmec.ensemble import Ensemble
 
     torch.cuda.set_device(device_index)
-    # every rank advances 64 distinct members: rank r takes members r, r+world, ... of 64*world
-    members = shard(synth.ensemble_members(nmembers * world), rank, world)
+    allm = synth.ensemble_members(nmembers * world)
+    parts = balanced_split([member_cost(o) for o, _, _ in allm], world)
+    members = [allm[i] for i in parts[rank]]
     common = dict(krylov_rtol=1e-15, krylov_restart=40, krylov_maxit=4000)
     out = {}
     for form, label in ((hmec.FORM_MIXED, "mixed"), (hmec.FORM_FP64, "fp64")):
@@ -353,40 +481,110 @@ def run_ensemble(args, rank=0, world=1, device_index=0, nmembers=64):
         # of a model run alone
         ens = Ensemble(members, concurrent=(form == hmec.FORM_MIXED), form=form, **common)
         (ens.step if form == hmec.FORM_MIXED else ens.step_sequential)(args.warmup)
+        if form == hmec.FORM_MIXED:
+            for m in ens.models:
+                m.profile_kernel(DOMINANT)
         torch.cuda.synchronize()
         rank_barrier(world)
         l0 = sum(m.launches for m in ens.models)
-        t0 = time.perf_counter()
-        reps = (ens.step if form == hmec.FORM_MIXED else ens.step_sequential)(args.steps)
-        torch.cuda.synchronize()
-        el = time.perf_counter() - t0
+        with ClockSampler(device_index) as clk:
+            t0 = time.perf_counter()
+            reps = (ens.step if form == hmec.FORM_MIXED else ens.step_sequential)(args.steps)
+            torch.cuda.synchronize()
+            el = time.perf_counter() - t0
         rank_barrier(world)
+        prof = None
+        if form == hmec.FORM_MIXED:
+            tot = [0, 0.0, 0.0, 0.0]
+            for m in ens.models:
+                for i, v in enumerate(m.profile_read()):
+                    tot[i] += v
+                m.profile_kernel(None)
+            prof = tuple(tot)
         out[label] = dict(s=rank_max(el, world), launches=sum(m.launches for m in ens.models) - l0,
                           bad=sum(1 for rs in reps for r in rs if r["rc"] != 0),
-                          gi=sum(r["global_iters"] for rs in reps for r in rs))
+                          gi=sum(r["global_iters"] for rs in reps for r in rs), clocks=clk.summary(), prof=prof)
         ens.close()
-    if rank != 0:
-        return 0
+    return out, members
+
+
+def ensemble_block(args, out, members, world, peaks):
     K = args.steps
     mx, fp = out["mixed"], out["fp64"]
-    value = whole_job_rate(len(members) * K, world, mx["s"])
-    line = {
-        "metric": METRIC, "value": value, "unit": "member-timesteps/s", "n_gpus": world, "steps": K,
-        "warmup": args.warmup, "ms_per_step": 1e3 * mx["s"] / K, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic",
-        "config": {"workload": "config 3: %d members per GPU, per-side nodes 51-301, 4x4 markers/cell, "
-                               "seeded a/b/L/k" % len(members),
-                   "form": "mixed, members concurrent (one context and stream each)",
-                   "timing": "device-wide synchronize around the timed region (many streams)",
-                   "parallelism": "members sharded by rank" if world > 1 else "single",
-                   "failed_member_steps": mx["bad"]},
-        "gpu_launches": mx["launches"],
+    nprof, prof_ms, b_alg, b_moved = mx["prof"]
+    peak = peaks.get("hbm_gbs") or 6800.0
+    ach = (b_alg / nprof) / (prof_ms / nprof / 1e3) / 1e9 if nprof and prof_ms > 0 else None
+    return {
+        "value": whole_job_rate(len(members) * K, world, mx["s"]), "unit": "member-timesteps/s",
+        "workload": "config 3: %d members per GPU, per-side nodes 51-301, 4x4 markers/cell, seeded a/b/L/k"
+                    % len(members),
+        "form": "mixed, members concurrent (one context and stream each, one launch per smoothing pass on at "
+                "most a quarter of the SMs)",
+        "timing": "device-wide synchronize around the timed region (many streams)",
+        "ms_per_step": 1e3 * mx["s"] / K, "steps": K, "failed_member_steps": mx["bad"],
+        "gpu_launches": mx["launches"], "clocks": mx["clocks"],
+        "roofline": {"kernel": "k_smooth_stage<float> (one smoothing pass per launch, all members)", "bound": "hbm",
+                     "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak if ach else None,
+                     "launches_timed": nprof, "avg_launch_us": 1e3 * prof_ms / nprof if nprof else None,
+                     "note": "compulsory bytes per launch over its CUDA-event duration; members' launches overlap"},
         "fp64_sequential": {"value": whole_job_rate(len(members) * K, world, fp["s"]),
                             "ms_per_step": 1e3 * fp["s"] / K, "failed_member_steps": fp["bad"]},
-        "speedup_batched_mixed_vs_sequential_fp64": fp["s"] / mx["s"],
+        "speedup_mixed_vs_fp64": fp["s"] / mx["s"],
     }
-    print(json.dumps(line))
-    return 0
+
+
+# ------------------------------------------------------------------ lines
+def model_block(args, cfg, world, res, peaks):
+    mx = res["mixed"]
+    K = args.steps
+    p = mx["p"]
+    blk = {
+        "value": whole_job_rate(K, world, mx["ms"] / 1e3), "unit": "timesteps/s", "ms_per_step": mx["ms"] / K,
+        "workload": CONFIGS[cfg]["workload"],
+        "form": "mixed: FP64 FGMRES(40), FP32 Vanka multigrid preconditioner",
+        "global_iters_per_step": mx["gi"] / K, "krylov_iters_per_step": mx["kr"] / K,
+        "global_iterations_per_s": world * mx["gi"] / (mx["ms"] / 1e3), "gpu_launches": mx["launches"],
+        "roofline": roofline(mx["prof"], mx["ms"], p, peaks, cfg,
+                             "k_vcycle_stage<float> (mixed-form V-cycle: every level's Vanka smoothing pass in "
+                             "one cooperative launch)"),
+        "clocks": mx["clocks"],
+    }
+    if "fp64" in res:
+        f = res["fp64"]
+        blk["fp64_form"] = {"value": world * K / (f["ms"] / 1e3), "ms_per_step": f["ms"] / K,
+                            "global_iters_per_step": f["gi"] / K, "krylov_iters_per_step": f["kr"] / K}
+        if "err" in f:
+            blk["mixed_vs_fp64_form_rel_err"] = dict(f["err"], same_dt=f["same_dt"], **judged(f["err"]))
+            blk["mixed_vs_fp64_form_rel_err"]["note"] = ("one timestep from the same state in both forms, "
+                                                         "max |mixed - fp64| / max |fp64| per field; 'velocity' "
+                                                         "over vxs and vys together")
+        blk["speedup_mixed_vs_fp64"] = blk["value"] / blk["fp64_form"]["value"]
+    if "e2e" in res:
+        e = res["e2e"]
+        blk["e2e"] = {"value": world * K / (e["ms"] / 1e3), "unit": "timesteps/s", "h2d_bytes_per_step": e["h2d"],
+                      "d2h_bytes_per_step": e["d2h"]}
+    return blk
+
+
+def accuracy_vs_oracle(cfg, nsteps=3):
+    """Mixed and plain FP64 forms against the FP64 CPU oracle after the first
+    nsteps timesteps from the same initial state (the oracle's direct solve
+    stands in for Pardiso); also the oracle's timing."""
+    import hmec
+
+    r = oracle_steps(cfg, nsteps, 1e9)
+    out = {"steps": r["steps"], "oracle_seconds": r["seconds"]}
+    for form, label in ((hmec.FORM_MIXED, "mixed"), (hmec.FORM_FP64, "fp64_form")):
+        m, _, _, _ = make_model(form, cfg, r["mk"], r["nodes"])
+        for _ in range(r["steps"]):
+            m.timestep()
+        err = rel_errors({k: m.field(k) for k in FIELDS_ACC}, r["fields"])
+        out[label] = dict(err, **judged(err))
+        m.close()
+    cpu = {"value": r["value"], "unit": "timesteps/s", "cores": 1, "kind": "port",
+           "sample": "first %d timesteps of %s from the initial state, %.1f s (oracle: C restatement + SciPy "
+                     "SuperLU direct solve, one thread)" % (r["steps"], cfg, r["seconds"])}
+    return out, cpu
 
 
 def main():
@@ -394,32 +592,28 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.config == "c3" and args.impl == "ours":
-        import torch
-
-        if world > 1:
-            torch.cuda.set_device(local)
-            torch.distributed.init_process_group("nccl")
-        rc = run_ensemble(args, rank, world, local if world > 1 else 0)
-        if world > 1:
-            torch.distributed.destroy_process_group()
-        return rc
 
     if args.impl == "reference":
         if rank != 0:
             return 0
-        steps = max(1, min(args.steps, 2))
-        r = cpu_sample(args.config, budget_s=90.0, max_steps=steps)
+        cfg = "c1" if args.config == "c3" else args.config
+        if cfg == "c2":
+            r = oracle_sample_no_solve(cfg, 2.0)
+            val, secs, steps = r["value"], r["seconds"], 1
+            sample = ("config 2, first timestep: markers->nodes + step begin and one global iteration's preparation "
+                      "+ assembly x 2 global iterations per step; direct solves not run (upper bound)")
+        else:
+            r = oracle_steps(cfg, max(1, min(args.steps, 2)), 90.0)
+            val, secs, steps = r["value"], r["seconds"], r["steps"]
+            sample = "first %d timesteps of %s from the initial state" % (steps, cfg)
         line = {
-            "metric": METRIC, "value": r["value"], "unit": "timesteps/s", "n_gpus": args.gpus, "steps": r["steps"],
-            "warmup": 0, "ms_per_step": 1e3 * r["seconds"] / r["steps"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "form": "CPU oracle: C restatement + SciPy SuperLU direct solve",
-                       "global_iters": r["global_iters"], "steps_requested": args.steps},
-            "cpu_baseline": {"value": r["value"], "unit": "timesteps/s", "cores": 1, "kind": "port",
-                             "sample": "first %d timesteps of %s from the initial state (%.1f s)" %
-                                       (r["steps"], args.config, r["seconds"])},
-            "e2e": {"value": r["value"], "unit": "timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "metric": METRIC, "value": val, "unit": "timesteps/s", "n_gpus": args.gpus, "steps": steps,
+            "warmup": 0, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": CONFIGS[cfg]["workload"],
+                       "form": "CPU oracle: C restatement + SciPy SuperLU direct solve", "steps_requested": args.steps},
+            "cpu_baseline": {"value": val, "unit": "timesteps/s", "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": val, "unit": "timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line))
         return 0
@@ -431,56 +625,73 @@ def main():
         torch.distributed.init_process_group("nccl")
     else:
         torch.cuda.set_device(0)
-    out, peaks = run_gpu(args, rank, world, local if world > 1 else 0)
+    dev = local if world > 1 else 0
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+
+    if args.config == "c3":
+        out, members = run_ensemble(args, rank, world, dev)
+        if rank == 0:
+            blk = ensemble_block(args, out, members, world, peaks)
+            line = {"metric": METRIC, "value": blk["value"], "unit": blk["unit"], "n_gpus": world, "steps": args.steps,
+                    "warmup": args.warmup, "ms_per_step": blk["ms_per_step"], "higher_is_better": True,
+                    "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic",
+                    "config": {"workload": blk["workload"], "form": blk["form"], "timing": blk["timing"],
+                               "parallelism": "members sharded by rank (balanced cells)" if world > 1 else "single"},
+                    "gpu_launches": blk["gpu_launches"], "roofline": blk["roofline"], "clocks": blk["clocks"],
+                    "fp64_sequential": blk["fp64_sequential"],
+                    "speedup_mixed_vs_fp64": blk["speedup_mixed_vs_fp64"]}
+            print(json.dumps(line))
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+
+    cfg = args.config
+    res = run_gpu(args, cfg, world, dev, peaks, with_fp64=not args.no_fp64, with_e2e=not args.no_e2e)
+    extra = {}
+    if not args.no_extra and world == 1:
+        other = "c1" if cfg == "c2" else "c2"
+        r2 = run_gpu(args, other, world, dev, peaks, with_e2e=False)
+        extra["config%s" % other[1]] = model_block(args, other, world, r2, peaks)
+        eo, emem = run_ensemble(args, rank, world, dev)
+        extra["config3"] = ensemble_block(args, eo, emem, world, peaks)
     if rank != 0:
         torch.distributed.destroy_process_group()
         return 0
-    mx = out["mixed"]
+    blk = model_block(args, cfg, world, res, peaks)
     K = args.steps
-    value = whole_job_rate(K, world, mx["ms"] / 1e3)
-    nprof, prof_ms, prof_bytes = mx["prof"]
-    achieved = (prof_bytes / nprof) / (prof_ms / nprof / 1e3) / 1e9 if nprof and prof_ms > 0 else None
-    peak = peaks.get("hbm_gbs")
-    roof = {"kernel": "k_vcycle_stage<float> (mixed-form V-cycle: every level's Vanka smoothing pass in one "
-                      "cooperative launch)", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": (achieved / peak) if (achieved and peak) else None, "traffic": SMOOTH_TRAFFIC_BYTES,
-            "traffic_note": "bytes per launch (one V-cycle): DRAM read+write from one ncu capture of this kernel",
-            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak else "fallback 6800",
-            "launches_timed": nprof, "avg_launch_us": (1e3 * prof_ms / nprof) if nprof else None,
-            "share_of_step_time": prof_ms / mx["ms"] if mx["ms"] else None}
-    if not peak:
-        roof["peak"] = 6800.0
-        roof["frac"] = achieved / 6800.0 if achieved else None
     line = {
-        "metric": METRIC, "value": value, "unit": "timesteps/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
-        "ms_per_step": mx["ms"] / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64/f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": "mixed: FP64 FGMRES(40), FP32 Vanka multigrid preconditioner",
-                   "krylov_rtol": 1e-15, "l2": "inputs larger than L2 (1M markers x 19 FP64 arrays = 152 MB); "
-                   "256 MB buffer written between timed steps", "parallelism": "replicas" if world > 1 else "single",
-                   "global_iters_per_step": mx["gi"] / K, "krylov_iters_per_step": mx["kr"] / K,
-                   "global_iterations_per_s": world * mx["gi"] / (mx["ms"] / 1e3)},
-        "gpu_launches": mx["launches"],
-        "roofline": roof,
-        "clocks": mx["clocks"],
+        "metric": METRIC, "value": blk["value"], "unit": "timesteps/s", "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": blk["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic",
+        "config": {"workload": blk["workload"], "form": blk["form"], "krylov_rtol": 1e-15,
+                   "l2": "inputs larger than L2 (marker arrays alone: 19 FP64 arrays x markers); 256 MB buffer "
+                         "written between timed steps", "parallelism": "replicas" if world > 1 else "single",
+                   "global_iters_per_step": blk["global_iters_per_step"],
+                   "krylov_iters_per_step": blk["krylov_iters_per_step"],
+                   "global_iterations_per_s": blk["global_iterations_per_s"]},
+        "gpu_launches": blk["gpu_launches"],
+        "roofline": blk["roofline"],
+        "clocks": blk["clocks"],
     }
-    if "fp64" in out:
-        f = out["fp64"]
-        line["fp64_form"] = {"value": world * K / (f["ms"] / 1e3), "ms_per_step": f["ms"] / K,
-                             "global_iters_per_step": f["gi"] / K, "krylov_iters_per_step": f["kr"] / K,
-                             "mixed_vs_fp64_max_rel_err": f["err"], "same_dt": f["dt_equal"],
-                             "err_note": "one timestep from the same state in both forms, max |mixed - fp64| / "
-                                         "max |fp64| per field; 'velocity' over vxs and vys together"}
-        line["speedup_mixed_vs_fp64"] = value / line["fp64_form"]["value"]
-    if "e2e" in out:
-        e = out["e2e"]
-        line["e2e"] = {"value": world * K / (e["ms"] / 1e3), "unit": "timesteps/s", "h2d_bytes_per_step": e["h2d"],
-                       "d2h_bytes_per_step": e["d2h"]}
+    for k in ("fp64_form", "mixed_vs_fp64_form_rel_err", "speedup_mixed_vs_fp64", "e2e"):
+        if k in blk:
+            line[k] = blk[k]
     if not args.no_cpu_baseline and world == 1:
-        r = cpu_sample(args.config, budget_s=25.0, max_steps=2)
-        line["cpu_baseline"] = {"value": r["value"], "unit": "timesteps/s", "cores": 1, "kind": "port",
-                                "sample": "first %d timesteps of %s from the initial state, %.1f s" %
-                                          (r["steps"], args.config, r["seconds"])}
+        if cfg == "c1":
+            acc, cpu = accuracy_vs_oracle("c1")
+            line["mixed_vs_oracle_rel_err"] = acc
+            line["cpu_baseline"] = cpu
+        else:
+            line["cpu_baseline"] = cpu_block(cfg, blk["global_iters_per_step"])
+            if "config1" in extra:
+                acc, cpu = accuracy_vs_oracle("c1")
+                extra["config1"]["mixed_vs_oracle_rel_err"] = acc
+                extra["config1"]["cpu_baseline"] = cpu
+    line.update(extra)
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

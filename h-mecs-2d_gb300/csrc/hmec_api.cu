@@ -24,7 +24,7 @@ int hmec_cuda_fail(hmec_ctx* ctx, cudaError_t e, const char* what) {
     return HMEC_ERR_CUDA;
 }
 
-bool hmec_prof_begin(hmec_ctx* ctx, const char* kname, double bytes) {
+bool hmec_prof_begin(hmec_ctx* ctx, const char* kname, double bytes, double bytes_alg) {
     ProfState& P = ctx->prof;
     while (*kname == '(' || *kname == ' ') kname++;  // template launches are parenthesised
     if (P.name.empty() || strncmp(kname, P.name.c_str(), P.name.size()) != 0) return false;
@@ -41,6 +41,7 @@ bool hmec_prof_begin(hmec_ctx* ctx, const char* kname, double bytes) {
     cudaEventRecord(P.pending[P.pending.size() - 2], ctx->stream);
     P.launches++;
     P.bytes += bytes;
+    P.bytes_alg += bytes_alg;
     return true;
 }
 
@@ -69,6 +70,19 @@ static void linspaced(std::vector<double>& out, int n, double low, double high) 
     out.resize(n);
     const double step = (n == 1) ? 0. : (high - low) / (double)(n - 1);
     for (int i = 0; i < n; i++) out[i] = (i == n - 1) ? high : low + (double)i * step;
+}
+
+// Row `row` of nf fields into consecutive slots of out (a field's row has
+// cols[k] entries; the column-major field has rows[k] rows).
+struct RowGather {
+    const double* f[64];
+    int rows[64], cols[64], off[64];
+};
+__global__ void k_gather_rows(RowGather g, int nf, int row, double* out) {
+    const int k = blockIdx.y;
+    if (k >= nf) return;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < g.cols[k]; j += gridDim.x * blockDim.x)
+        out[g.off[k] + j] = g.f[k][(size_t)j * g.rows[k] + row];
 }
 
 // Map device status bits to the ABI status.
@@ -167,6 +181,7 @@ void hmec_params_default(hmec_params* p) {
     p->quirk_accumulate_sums = 0;
     p->bounds_check = 0;
     p->mg_flags = 1; /* HMEC_MG_DARCY_HARMONIC */
+    p->graph = 1;
 }
 
 #define HMEC_X_NAME(name, grid) #name,
@@ -194,12 +209,23 @@ const char* hmec_last_error(const hmec_ctx* ctx) { return ctx ? ctx->err.c_str()
 
 int64_t hmec_kernel_launches(const hmec_ctx* ctx) { return ctx ? ctx->launches : -1; }
 
+int32_t hmec_graph_status(hmec_ctx* ctx) {
+    if (!ctx) return -1;
+    if (!ctx->p.graph) return -1;
+    if (ctx->gr.state < 0) {
+        ctx->err = ctx->gr.why.empty() ? "graph capture failed" : ctx->gr.why;
+        return -1;
+    }
+    return ctx->gr.state == 1 ? 1 : 0;
+}
+
 void hmec_destroy(hmec_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->dev);
     cudaStreamSynchronize(ctx->stream);
     for (cudaEvent_t e : ctx->prof.pool) cudaEventDestroy(e);
     for (cudaEvent_t e : ctx->prof.pending) cudaEventDestroy(e);
+    graph_free(ctx);
     solver_free(ctx);
     p2g_free(ctx);
     for (int k = 0; k < 8; k++) cudaFree(ctx->crd[k]);
@@ -210,6 +236,7 @@ void hmec_destroy(hmec_ctx* ctx) {
     cudaFree(ctx->red);
     cudaFree(ctx->ticket);
     cudaFree(ctx->ds);
+    cudaFree(ctx->rowbuf);
     cudaFreeHost(ctx->hs);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -342,6 +369,30 @@ int32_t hmec_download_field(hmec_ctx* ctx, int32_t f, double* a, int32_t rows, i
     return HMEC_OK;
 }
 
+int32_t hmec_download_rows(hmec_ctx* ctx, int32_t row, int32_t nf, const int32_t* fields, double* out) {
+    if (!ctx || !fields || !out) return fail(ctx, HMEC_ERR_ARG, "null argument");
+    if (nf < 1 || nf > 64) return fail(ctx, HMEC_ERR_ARG, "nfields must be in [1, 64]");
+    RowGather g;
+    int total = 0;
+    for (int k = 0; k < nf; k++) {
+        const int f = fields[k];
+        if (f < 0 || f >= HMEC_F_COUNT) return fail(ctx, HMEC_ERR_ARG, "unknown field");
+        const int gr = hmec_field_grid(f);
+        g.f[k] = ctx->f[f];
+        g.rows[k] = ctx->g.Ny + gr;
+        g.cols[k] = ctx->g.Nx + gr;
+        g.off[k] = total;
+        total += g.cols[k];
+        if (row < 0 || row >= g.rows[k]) return fail(ctx, HMEC_ERR_ARG, "row outside the field");
+    }
+    if (!ctx->rowbuf) HMEC_CUDA(ctx, cudaMalloc(&ctx->rowbuf, sizeof(double) * 64 * (size_t)(ctx->g.Nx + 1)));
+    HMEC_LAUNCH(ctx, k_gather_rows, dim3(nblocks(ctx->g.Nx + 1, 128), nf), 128, 0, g, nf, row, ctx->rowbuf);
+    HMEC_CUDA(ctx, cudaMemcpyAsync(out, ctx->rowbuf, sizeof(double) * (size_t)total, cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+    HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HMEC_OK;
+}
+
 // Scalars: the host mirror is refreshed from the device, edited, pushed back.
 int32_t hmec_set_scalar(hmec_ctx* ctx, int32_t id, double v) {
     if (!ctx) return HMEC_ERR_ARG;
@@ -408,15 +459,18 @@ int32_t hmec_profile_kernel(hmec_ctx* ctx, const char* name) {
     ctx->prof.launches = 0;
     ctx->prof.ms = 0;
     ctx->prof.bytes = 0;
+    ctx->prof.bytes_alg = 0;
     return HMEC_OK;
 }
 
-int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, double* bytes) {
+int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, double* bytes_compulsory,
+                          double* bytes_moved) {
     if (!ctx) return HMEC_ERR_ARG;
     prof_drain(ctx);
     if (launches) *launches = ctx->prof.launches;
     if (total_ms) *total_ms = ctx->prof.ms;
-    if (bytes) *bytes = ctx->prof.bytes;
+    if (bytes_compulsory) *bytes_compulsory = ctx->prof.bytes_alg;
+    if (bytes_moved) *bytes_moved = ctx->prof.bytes;
     return HMEC_OK;
 }
 
@@ -503,7 +557,11 @@ int32_t hmec_advect_markers(hmec_ctx* ctx) {
 
 int32_t hmec_timestep(hmec_ctx* ctx, hmec_step_report* rep) {
     if (!ctx) return HMEC_ERR_ARG;
-    int rc = hmec_markers_to_nodes(ctx);
+    bool by_graph = false;
+    int rc = graph_timestep(ctx, rep, &by_graph);
+    if (by_graph) return rc;
+    if (rc) return rc;
+    rc = hmec_markers_to_nodes(ctx);
     if (rc) return rc;
     rc = hmec_timestep_begin(ctx);
     if (rc) return rc;
@@ -548,6 +606,7 @@ int32_t hmec_timestep(hmec_ctx* ctx, hmec_step_report* rep) {
         rep->Vmax = ctx->hs->Vmax;
         rep->max_krylov_relres = kmax;
     }
+    ctx->gr.warm = 1;  // the lazy set-up is done: later steps may run as a graph
     if (first_bad) return fail(ctx, first_bad, "timestep finished with a non-OK status (see report)");
     return HMEC_OK;
 }

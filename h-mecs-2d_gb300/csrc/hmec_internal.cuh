@@ -71,6 +71,14 @@ struct DevScalars {
     int yndtdecrease, timestep, ynlast, iterstep;
     int ynpl, stop, loop_done, status;
     int krylov_iters, krylov_total, iters_in_step, pad0;
+    int krylov_cycles, pad1;  // restart cycles of the step's solves
+};
+
+// Device state of a solve whose restart and Arnoldi loops run on the device
+// (graph mode): the previous cycle's residual, the first-cycle flag, the cap.
+struct GmCtl {
+    double prev;
+    int first, maxit;
 };
 
 // Pointers to the node fields read by the assembly of one level.
@@ -152,6 +160,7 @@ struct Solver {
     double* bnorm;         // ||D b||
     int* done;             // convergence flag of the current solve
     int* kcur;             // Arnoldi steps taken in the current cycle
+    GmCtl* gctl = nullptr; // device-controlled solve state (graph mode)
     int nblk;
     std::vector<Level> lv;
     // setup of the levels as a dependency graph: level l's assembly and its
@@ -167,7 +176,7 @@ struct Solver {
     // launches instead
     void* vpass = nullptr;
     int vpass_state = 0, vpass_n = 0, vpass_grid = 0, vpass_smem = 0, vpass_whole = 0, vpass_cap = 0;
-    double vpass_bytes = 0;
+    double vpass_bytes = 0, vpass_bytes_alg = 0;
 };
 
 // Live timing of one kernel family (bench.py roofline): CUDA events around
@@ -177,7 +186,31 @@ struct ProfState {
     std::vector<cudaEvent_t> pool;
     std::vector<cudaEvent_t> pending;  // start/stop pairs
     int64_t launches = 0;
-    double ms = 0, bytes = 0;
+    // bytes: what the launches move by this implementation's own account;
+    // bytes_alg: the compulsory bytes of the work they do (the per-cell
+    // figures of the hot-path byte model: matrix coefficients, unknowns and
+    // right-hand sides, nothing this implementation adds)
+    double ms = 0, bytes = 0, bytes_alg = 0;
+};
+
+// The timestep as a CUDA graph: the global-iteration loop, the FGMRES restart
+// loop and the Arnoldi loop are conditional WHILE nodes whose conditions the
+// device sets, so one graph launch runs a whole timestep without the host.
+// n_*: kernel launches per execution of each part (the launch count of a
+// step follows from the loop trip counts the device reports).
+struct GraphCtl {
+    int gi;  // global iterations run by the graph in this step (a guard on the loop)
+    int cap;
+};
+struct GraphState {
+    int state = 0;  // 0 not built yet, 1 ready, -1 off (host-driven steps)
+    int warm = 0;   // a host-driven step ran (lazy set-up done) before the capture
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t body[3] = {nullptr, nullptr, nullptr};
+    GraphCtl* ctl = nullptr;
+    int64_t n_top = 0, n_global = 0, n_restart = 0, n_inner = 0;
+    std::string why;  // why the graph is off
 };
 
 struct hmec_ctx {
@@ -212,6 +245,8 @@ struct hmec_ctx {
     ProfState prof;
     int in_step;             // between timestep_begin and timestep_end
     std::string err;
+    GraphState gr;
+    double* rowbuf = nullptr;  // hmec_download_rows staging (64 rows of Nx+1)
 };
 
 // ------------------------------------------------------------------ helpers
@@ -253,6 +288,21 @@ __device__ __forceinline__ int fix_quot(double x, double d, float rdf, bool half
     return fix_trunc(__ddiv_rn(xx, d));
 }
 __device__ __forceinline__ float rcp_f32(double d) { return __frcp_rn(__double2float_rn(d)); }
+
+// FP32 -> FP64 through the bit pattern, on the integer pipe (conversions run
+// at the FP64 rate on this GPU): exact for normal values, infinities and NaN;
+// FP32 subnormals (below 1.2e-38) give 0.
+__device__ __forceinline__ double f2d_bits(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFFu;
+    if (e == 0) return 0.0;
+    if (e == 0xFFu) return (double)f;
+    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                 ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
+    return __longlong_as_double((long long)b);
+}
+__device__ __forceinline__ double to_f64(float f) { return f2d_bits(f); }
+__device__ __forceinline__ double to_f64(double d) { return d; }
 
 // A marker's basic cell (ib, jb) and pressure cell (iP, jP): the indices of
 // cpp/h_mec_rsf_v9.cpp:432-433 and :468-469 (fix + check_bounds, IEEE
@@ -318,7 +368,7 @@ __device__ __forceinline__ bool arrive_last(unsigned* ticket) {
     } while (0)
 
 int hmec_cuda_fail(hmec_ctx* ctx, cudaError_t e, const char* what);
-bool hmec_prof_begin(hmec_ctx* ctx, const char* kname, double bytes);
+bool hmec_prof_begin(hmec_ctx* ctx, const char* kname, double bytes, double bytes_alg);
 void hmec_prof_end(hmec_ctx* ctx);
 
 // The library's launch helpers use ctx->stream; inside a scope they go to s.
@@ -329,10 +379,11 @@ struct StreamScope {
     ~StreamScope() { ctx->stream = saved; }
 };
 
-// Launch with algorithmic byte accounting for the live roofline.
-#define HMEC_LAUNCH_B(ctx, nbytes, kern, grid, block, smem, ...)               \
+// Launch with byte accounting for the live roofline (bytes moved by this
+// implementation, compulsory bytes of the work).
+#define HMEC_LAUNCH_B(ctx, nbytes, nalg, kern, grid, block, smem, ...)         \
     do {                                                                          \
-        const bool _prof = hmec_prof_begin((ctx), #kern, (nbytes));               \
+        const bool _prof = hmec_prof_begin((ctx), #kern, (nbytes), (nalg));       \
         kern<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);            \
         (ctx)->launches++;                                                        \
         if (_prof) hmec_prof_end(ctx);                                            \
@@ -357,6 +408,21 @@ int solver_alloc(hmec_ctx* ctx);
 void solver_free(hmec_ctx* ctx);
 int solver_setup(hmec_ctx* ctx);            // build coarse levels + Vanka inverses for the current matrix
 int solver_solve(hmec_ctx* ctx, int* iters, double* relres);  // solve A S = R in place (S = guess)
+// Graph capture helpers (hmec_graph.cu): a conditional handle of the graph
+// being captured on s; a WHILE node on handle h appended to that capture,
+// whose body is captured on stream bs until graph_while_end(bs).
+int graph_handle(hmec_ctx* ctx, cudaStream_t s, cudaGraphConditionalHandle* h);
+int graph_while_begin(hmec_ctx* ctx, cudaStream_t s, cudaGraphConditionalHandle h, cudaStream_t bs);
+int graph_while_end(hmec_ctx* ctx, cudaStream_t bs);
+// The solve with its decisions on the device, captured on ctx->stream (its
+// restart loop's body on s_restart, the Arnoldi loop's on s_inner);
+// *n_restart / *n_inner: kernel launches per trip of each loop.
+int solver_capture_solve(hmec_ctx* ctx, cudaStream_t s_restart, cudaStream_t s_inner, int64_t* n_restart,
+                         int64_t* n_inner);
+// One timestep as a graph launch (built on first use); *used is false when
+// the graph is off for this context and the caller runs the host-driven step.
+int graph_timestep(hmec_ctx* ctx, hmec_step_report* rep, bool* used);
+void graph_free(hmec_ctx* ctx);
 // Assembly of one level into (col, val, dscale, rhs); rhs may be null.
 void launch_assemble(hmec_ctx* ctx, const Geo& g, const AsmFields& af, int32_t* col, double* val, double* dscale,
                      double* rhs_scaled, double* rhs_raw, const double* sc_dev);

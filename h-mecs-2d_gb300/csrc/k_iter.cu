@@ -54,6 +54,7 @@ __global__ void k_step_begin(Geo g, DevScalars* ds, hmec_params p, const double*
         ds->krylov_total = 0;
         ds->krylov_maxrel = 0;
         ds->iters_in_step = 0;
+        ds->krylov_cycles = 0;
     }
 }
 

@@ -105,18 +105,6 @@ __device__ __forceinline__ void df_norm(float& a, float& b) {
     a = s;
 }
 
-// FP32 -> FP64 through the bit pattern (exact for normal values; FP32
-// subnormals, below 1.2e-38, give 0)
-__device__ __forceinline__ double f2d_bits(float f) {
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xFFu;
-    if (e == 0) return 0.0;
-    if (e == 0xFFu) return (double)f;
-    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                 ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
-    return __longlong_as_double((long long)b);
-}
-
 // h + l = 1 / a: the FP32 reciprocal refined by one Newton-Raphson step
 // x + x (u + u^2), u = 1 - a x, evaluated in double-float (relative error
 // < 3e-14).

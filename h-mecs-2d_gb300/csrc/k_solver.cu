@@ -1394,10 +1394,18 @@ __global__ void k_cycle_begin(Gm G, const double* __restrict__ partial, int nblk
     G.dots[0] = beta > 0 ? 1.0 / beta : 0.0;  // scale for V0
 }
 
-__global__ void k_scale_vec(int N, const double* __restrict__ a, const double* sc, double* b, const int* done) {
+// b = a * sc[0]; the preconditioner's first input is copied beside it when
+// c32 (mixed form) or c64 (FP64 form, device-controlled solve) is set.
+__global__ void k_scale_vec(int N, const double* __restrict__ a, const double* sc, double* b, const int* done,
+                            float* c32, double* c64) {
     if (*done) return;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < N) b[r] = a[r] * sc[0];
+    if (r < N) {
+        const double v = a[r] * sc[0];
+        b[r] = v;
+        if (c32) c32[r] = (float)v;
+        if (c64) c64[r] = v;
+    }
 }
 
 // After the two CGS passes: column j of H, Givens rotation, residual estimate.
@@ -1452,6 +1460,11 @@ struct ArnArgs {
     Gm G;
     double rtol;
     float* next32;       // if set: FP32 copy of V_{j+1}
+    double* next64;      // if set: FP64 copy of V_{j+1} (the FP64 form's next preconditioner input)
+    // device-controlled solve (graph): j is read from jdev (the steps taken
+    // in the cycle) and z_j lands in Zbase + j N
+    const int* jdev;
+    double* Zbase;
 };
 
 constexpr int ARN_BS = 256;
@@ -1530,18 +1543,25 @@ __global__ void __launch_bounds__(ARN_BS) k_arnoldi(ArnArgs<TZ> a) {
     extern __shared__ double shh[];
     if (*a.G.done) return;  // set only by an earlier launch: uniform across the grid
     cg::grid_group grid = cg::this_grid();
-    const int N = a.N, j = a.j, m = a.m, nblk = a.nblk;
+    const int N = a.N, m = a.m, nblk = a.nblk;
+    // the step index: a kernel argument, or (device-controlled solve) the
+    // steps taken so far, read before the first grid barrier and rewritten
+    // by block 0 only after the last one
+    const int j = a.jdev ? *a.jdev : a.j;
+    double* const Zj = a.jdev ? a.Zbase + (size_t)j * N : a.Zj;
     double* dots = a.G.dots;
     // z_j and w = A z_j (rows in the block's contiguous range, as below)
     const int chunk = ((N + nblk - 1) / nblk + 31) / 32 * 32;
     const int rend = min(N, (int)blockIdx.x * chunk + chunk);
+    // (an FP32 z is widened through its bit pattern: the same FP64 values in
+    // z_j and in the product, without FP64-rate conversions)
     for (int r = blockIdx.x * chunk + threadIdx.x; r < rend; r += ARN_BS) {
-        if ((const void*)a.zsrc != (const void*)a.Zj) a.Zj[r] = (double)a.zsrc[r];
+        if ((const void*)a.zsrc != (const void*)Zj) Zj[r] = to_f64(a.zsrc[r]);
         double acc = 0;
 #pragma unroll
         for (int s = 0; s < HMEC_W; s++) {
             const size_t o = (size_t)s * N + r;
-            acc += a.val[o] * (double)a.zsrc[a.col[o]];
+            acc += a.val[o] * to_f64(a.zsrc[a.col[o]]);
         }
         a.w[r] = acc;
     }
@@ -1580,7 +1600,66 @@ __global__ void __launch_bounds__(ARN_BS) k_arnoldi(ArnArgs<TZ> a) {
         const double v = a.w[r] * sc;
         Vn[r] = v;
         if (a.next32) a.next32[r] = (float)v;
+        if (a.next64) a.next64[r] = v;
     }
+}
+
+// ------------------------------------------- device-controlled solve (graph)
+// The decisions the host takes between launches in solver_solve, taken on
+// the device so that a solve can run inside a CUDA graph: conditional WHILE
+// nodes repeat the restart cycle and the Arnoldi step, and these one-thread
+// kernels set their conditions.  Every loop is bounded: an inner trip either
+// ends the loop or advances the step count (at most m per cycle), and a
+// cycle either stops or runs at least one Arnoldi step (at most krylov_maxit
+// in the solve).
+__global__ void k_solve_init(Gm G, GmCtl* c, int maxit, cudaGraphConditionalHandle h_restart) {
+    G.ds->krylov_iters = 0;
+    c->prev = INFINITY;
+    c->first = 1;
+    c->maxit = maxit;
+    cudaGraphSetConditional(h_restart, 1u);
+}
+
+// k_cycle_begin, then the restart decision of solver_solve: converged,
+// failed (non-finite or out of iterations; HMEC_DEV_KRYLOV_NOCONV), stalled
+// near the rounding floor (accepted within 100 x rtol), or another cycle.
+__global__ void k_cycle_begin_g(Gm G, const double* __restrict__ partial, int nblk, double rtol, int m, GmCtl* c,
+                                cudaGraphConditionalHandle h_restart, cudaGraphConditionalHandle h_inner) {
+    const double rr = warp_sum_fixed(partial, nblk);
+    const double bb = warp_sum_fixed(partial + nblk, nblk);
+    for (int k = 1 + threadIdx.x; k <= m; k += 32) G.g[k] = 0;
+    if (threadIdx.x != 0) return;
+    if (c->first) *G.bnorm = sqrt(bb);
+    c->first = 0;
+    const double bn = *G.bnorm;
+    const double beta = sqrt(rr);
+    const double rel = bn > 0 ? beta / bn : beta;
+    G.ds->krylov_relres = rel;
+    G.ds->krylov_cycles += 1;
+    G.g[0] = beta;
+    *G.kcur = 0;
+    G.dots[0] = beta > 0 ? 1.0 / beta : 0.0;
+    const int total = G.ds->krylov_iters;
+    int more = 1, conv = 0;
+    if (rel <= rtol) {
+        more = 0;
+        conv = 1;
+    } else if (!isfinite(rel) || total >= c->maxit) {
+        more = 0;
+    } else if (total > 0 && rel > 0.5 * c->prev && rel <= 1e-10) {
+        more = 0;
+        conv = rel <= 100 * rtol;
+    }
+    c->prev = rel;
+    *G.done = more ? 0 : 1;
+    if (!more && !conv) atomicOr(&G.ds->status, HMEC_DEV_KRYLOV_NOCONV);
+    cudaGraphSetConditional(h_restart, more ? 1u : 0u);
+    cudaGraphSetConditional(h_inner, more ? 1u : 0u);
+}
+
+__global__ void k_inner_cond(Gm G, int m, const GmCtl* c, cudaGraphConditionalHandle h_inner) {
+    const int more = !*G.done && *G.kcur < m && G.ds->krylov_iters < c->maxit;
+    cudaGraphSetConditional(h_inner, more ? 1u : 0u);
 }
 
 // y = H^{-1} g (upper triangular, kcur columns)
@@ -1902,6 +1981,8 @@ int solver_alloc(hmec_ctx* ctx) {
     HMEC_CUDA(ctx, cudaMalloc(&sv.done, sizeof(int) * 2));
     HMEC_CUDA(ctx, cudaMalloc(&sv.kcur, sizeof(int) * 2));
     HMEC_CUDA(ctx, cudaMemset(sv.done, 0, sizeof(int) * 2));
+    HMEC_CUDA(ctx, cudaMalloc(&sv.gctl, sizeof(GmCtl)));
+    HMEC_CUDA(ctx, cudaMemset(sv.gctl, 0, sizeof(GmCtl)));
     const size_t nl = sv.lv.size();
     sv.aux.assign(nl, nullptr);
     sv.ev_coef.assign(nl, nullptr);
@@ -1981,6 +2062,7 @@ void solver_free(hmec_ctx* ctx) {
     cudaFree(sv.bnorm);
     cudaFree(sv.done);
     cudaFree(sv.kcur);
+    cudaFree(sv.gctl);
 }
 
 // Rebuilds every level after a fine assembly.  The work is a graph, not a
@@ -2141,9 +2223,19 @@ float* x_alt<float>(Level& L) {
 // int16 window offsets), every inverse, the unknowns read and written and the
 // rhs; the prolonged correction; the fused residual (one pass over the
 // matrix, x and b) and restriction.
+// Compulsory bytes of smoothing sweeps on a level of N unknowns (N/6 cells):
+// per cell and sweep the 42 coefficients of its six rows and three vectors
+// (unknowns read and written, right-hand side) of six values, in the
+// smoother's precision; the residual and restriction that end a
+// pre-smoothing pass count as one more sweep.
+template <typename T>
+static double sweep_bytes_compulsory(double N, double sweeps) {
+    return sweeps * (N / 6.0) * (42.0 + 18.0) * sizeof(T);
+}
+
 template <typename T>
 static StageArgs<T> stage_args(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mode, bool restrict_next,
-                               double* ab) {
+                               double* ab, double* ab_alg) {
     Solver& sv = ctx->sv;
     Level& L = sv.lv[l];
     StageArgs<T> t;
@@ -2177,6 +2269,7 @@ static StageArgs<T> stage_args(hmec_ctx* ctx, size_t l, const T* b, T* x, int ns
     const double st = sizeof(T), N = L.g.N;
     *ab = nsweeps * (N * HMEC_W * (st + 2) + (double)L.npatch * 100.0 * st + 3.0 * N * st) +
           (mode ? N * st * 1.5 : 0.0);
+    *ab_alg = sweep_bytes_compulsory<T>(N, nsweeps + (restrict_next ? 1 : 0));
     if (restrict_next) {
         Level& C = sv.lv[l + 1];
         t.nc = C.g.N;
@@ -2215,20 +2308,21 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
     const double bpp = 10.0 * HMEC_W * (st + 4) + 100.0 * st + 30.0 * st;
     const double bnd = (double)L.nbnd * (HMEC_W * (st + 4) + 4.0 * st);
     const double bytes = nsweeps * ((double)L.npatch * bpp + bnd) + (double)L.g.N * st * (mode ? 2.5 : 1.0);
+    const double alg = sweep_bytes_compulsory<T>(L.g.N, nsweeps);
     if (L.npatch <= SINGLE_BLOCK_PATCHES) {
-        HMEC_LAUNCH_B(ctx, bytes, (k_smooth<T, false>), 1, SM_BS, 0, a, nsweeps, mode);
+        HMEC_LAUNCH_B(ctx, bytes, alg, (k_smooth<T, false>), 1, SM_BS, 0, a, nsweeps, mode);
         return HMEC_OK;
     }
     if (!(ctx->p.mg_flags & HMEC_MG_UNTILED)) {
         int rc = stage_config<T>(ctx, L);
         if (rc) return rc;
-        double ab = 0;
-        StageArgs<T> t = stage_args<T>(ctx, l, b, x, nsweeps, mode, restrict_next, &ab);
+        double ab = 0, ab_alg = 0;
+        StageArgs<T> t = stage_args<T>(ctx, l, b, x, nsweeps, mode, restrict_next, &ab, &ab_alg);
         void* args[] = {&t, &nsweeps, &mode};
         // live timing by name prefix: "k_smooth" is every level, "k_smooth<l>" one
         static const char* const lname[8] = {"k_smooth0", "k_smooth1", "k_smooth2", "k_smooth3",
                                              "k_smooth4", "k_smooth5", "k_smooth6", "k_smooth7"};
-        const bool prof = hmec_prof_begin(ctx, lname[l < 8 ? l : 7], ab);
+        const bool prof = hmec_prof_begin(ctx, lname[l < 8 ? l : 7], ab, ab_alg);
         const void* kern = L.st_whole ? (const void*)k_smooth_stage<T, true> : (const void*)k_smooth_stage<T, false>;
         HMEC_CUDA(ctx, cudaLaunchCooperativeKernel(kern, dim3(L.st_grid), dim3(TILE_BS), args,
                                                    (size_t)L.st_smem, ctx->stream));
@@ -2244,7 +2338,7 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
                                                 (int)SMEM_LIMIT));
             attr_set[sizeof(T) == 8 ? 0 : 1] = true;
         }
-        HMEC_LAUNCH_B(ctx, bytes, k_smooth_smem<T>, 1, SMEM_BS, smem, a, nsweeps, mode);
+        HMEC_LAUNCH_B(ctx, bytes, alg, k_smooth_smem<T>, 1, SMEM_BS, smem, a, nsweeps, mode);
         return HMEC_OK;
     }
     // size the grid to one colour phase (the zero/prolongation and boundary
@@ -2252,7 +2346,7 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
     const long long work = std::max<long long>((long long)L.npatch * 16 / 9 + SM_BS, 2LL * SM_BS);
     const int grid = (int)std::min<long long>(max_coop_blocks<T>(ctx), std::max<long long>(1, (work + SM_BS - 1) / SM_BS));
     void* args[] = {&a, &nsweeps, &mode};
-    const bool prof = hmec_prof_begin(ctx, "k_smooth", bytes);
+    const bool prof = hmec_prof_begin(ctx, "k_smooth", bytes, alg);
     HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_smooth<T, true>, dim3(grid), dim3(SM_BS), args, 0, ctx->stream));
     ctx->launches++;
     if (prof) hmec_prof_end(ctx);
@@ -2298,22 +2392,27 @@ static int vcycle_fused(hmec_ctx* ctx, const T* b0, T* x0, bool* used) {
         if (grid < 1 || grid > per_sm * nsm) return HMEC_OK;
         // pre-smoothing down the levels, the coarsest level, post-smoothing up
         std::vector<VPass<T>> ps;
-        double bytes = 0, ab = 0;
+        double bytes = 0, ab = 0, alg = 0, ab_alg = 0;
         for (size_t l = 0; l + 1 < nl; l++) {
             Level& L = sv.lv[l];
-            ps.push_back({stage_args<T>(ctx, l, LvPtr<T>::b(L), LvPtr<T>::x(L), p.mg_pre, 0, true, &ab), p.mg_pre, 0});
+            ps.push_back(
+                {stage_args<T>(ctx, l, LvPtr<T>::b(L), LvPtr<T>::x(L), p.mg_pre, 0, true, &ab, &ab_alg), p.mg_pre, 0});
             bytes += ab;
+            alg += ab_alg;
         }
         {
             Level& L = sv.lv[nl - 1];
             const int ns = std::max(1, p.mg_coarse_sweeps);
-            ps.push_back({stage_args<T>(ctx, nl - 1, LvPtr<T>::b(L), LvPtr<T>::x(L), ns, 0, false, &ab), ns, 0});
+            ps.push_back({stage_args<T>(ctx, nl - 1, LvPtr<T>::b(L), LvPtr<T>::x(L), ns, 0, false, &ab, &ab_alg), ns, 0});
             bytes += ab;
+            alg += ab_alg;
         }
         for (size_t l = nl - 1; l-- > 0;) {
             Level& L = sv.lv[l];
-            ps.push_back({stage_args<T>(ctx, l, LvPtr<T>::b(L), LvPtr<T>::x(L), p.mg_post, 1, false, &ab), p.mg_post, 1});
+            ps.push_back(
+                {stage_args<T>(ctx, l, LvPtr<T>::b(L), LvPtr<T>::x(L), p.mg_post, 1, false, &ab, &ab_alg), p.mg_post, 1});
             bytes += ab;
+            alg += ab_alg;
         }
         if ((int)ps.size() > MAX_VPASS) return HMEC_OK;
         VTable<T>* tab = new (std::nothrow) VTable<T>();
@@ -2329,6 +2428,7 @@ static int vcycle_fused(hmec_ctx* ctx, const T* b0, T* x0, bool* used) {
         sv.vpass_whole = whole;
         sv.vpass_cap = cap;
         sv.vpass_bytes = bytes;
+        sv.vpass_bytes_alg = alg;
         sv.vpass_state = 1;
     }
     VTable<T>* tab = static_cast<VTable<T>*>(sv.vpass);
@@ -2339,7 +2439,7 @@ static int vcycle_fused(hmec_ctx* ctx, const T* b0, T* x0, bool* used) {
     void* args[] = {tab};
     const void* kern =
         sv.vpass_whole ? (const void*)k_vcycle_stage<T, true> : (const void*)k_vcycle_stage<T, false>;
-    const bool prof = hmec_prof_begin(ctx, "k_smooth_vcycle", sv.vpass_bytes);
+    const bool prof = hmec_prof_begin(ctx, "k_smooth_vcycle", sv.vpass_bytes, sv.vpass_bytes_alg);
     HMEC_CUDA(ctx, cudaLaunchCooperativeKernel(kern, dim3(sv.vpass_grid), dim3(TILE_BS), args, (size_t)sv.vpass_smem,
                                                ctx->stream));
     ctx->launches++;
@@ -2400,8 +2500,10 @@ static int precondition(hmec_ctx* ctx, const double* v, double* z, bool input_re
 }
 
 // One cooperative Arnoldi step (k_arnoldi) after the preconditioner.
+// devj: the step index and z_j's slot come from the device (graph mode; j
+// is then only the estimate used for the byte accounting).
 template <typename TZ>
-static int arnoldi(hmec_ctx* ctx, const TZ* zsrc, double* Zj, int j, const Gm& G, double rtol) {
+static int arnoldi(hmec_ctx* ctx, const TZ* zsrc, double* Zj, int j, const Gm& G, double rtol, bool devj = false) {
     Solver& sv = ctx->sv;
     Level& L0 = sv.lv[0];
     static int cached = 0;
@@ -2427,13 +2529,20 @@ static int arnoldi(hmec_ctx* ctx, const TZ* zsrc, double* Zj, int j, const Gm& G
     a.G = G;
     a.rtol = rtol;
     a.next32 = ctx->p.form == HMEC_FORM_MIXED ? L0.fb : nullptr;
+    a.next64 = (devj && ctx->p.form != HMEC_FORM_MIXED) ? L0.pb : nullptr;
+    a.jdev = devj ? sv.kcur : nullptr;
+    a.Zbase = sv.Z;
     void* args[] = {&a};
     // algorithmic bytes: SpMV (FP64 values, int32 columns, z gathered, w and
     // z_j written) and two CGS passes (each a dot and an update over j+1
     // basis vectors), V_{j+1} written
     const double N = sv.N, nb = j + 1;
     const double bytes = N * (HMEC_W * 12.0 + sizeof(TZ) + 16.0) + 2.0 * N * 8.0 * (3.0 * nb + 2.0) + N * 12.0;
-    const bool prof = hmec_prof_begin(ctx, "k_arnoldi", bytes);
+    // compulsory: the FP64 operator, 42 coefficients and two vectors per
+    // cell (432 B), and the orthogonalisation against j+1 basis vectors,
+    // (2j+2) vectors of six FP64 values per cell
+    const double alg = (N / 6.0) * (432.0 + (2.0 * nb) * 48.0);
+    const bool prof = hmec_prof_begin(ctx, "k_arnoldi", bytes, alg);
     HMEC_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_arnoldi<TZ>, dim3(a.nblk), dim3(ARN_BS), args,
                                                sizeof(double) * (sv.m + 1), ctx->stream));
     ctx->launches++;
@@ -2480,7 +2589,7 @@ int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
             break;
         }
         prev = rel;
-        HMEC_LAUNCH(ctx, k_scale_vec, nblocks(N, 256), 256, 0, N, r, sv.dots, sv.V, sv.done);
+        HMEC_LAUNCH(ctx, k_scale_vec, nblocks(N, 256), 256, 0, N, r, sv.dots, sv.V, sv.done, nullptr, nullptr);
         // The host looks at the convergence flag only now and then (a look
         // drains the stream); steps queued after convergence return at once
         // but still cost their launches.  So the next look is placed where the
@@ -2529,5 +2638,57 @@ int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
         HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         return HMEC_ERR_KRYLOV_NOCONV;
     }
+    return HMEC_OK;
+}
+
+// The solve of solver_solve for the graph of a timestep: the same kernels
+// and the same decisions, taken on the device.  The restart cycle and the
+// Arnoldi step are the bodies of two nested conditional WHILE nodes; the
+// preconditioner reads fixed buffers (the mixed form's FP32 input fb and
+// output fx; the FP64 form's pb and dx_, which the Arnoldi step fills and
+// copies into z_j), so nothing in the graph depends on the step index.
+int solver_capture_solve(hmec_ctx* ctx, cudaStream_t s_restart, cudaStream_t s_inner, int64_t* n_restart,
+                         int64_t* n_inner) {
+    Solver& sv = ctx->sv;
+    Level& L0 = sv.lv[0];
+    const int N = sv.N, m = sv.m, nblk = sv.nblk;
+    const double rtol = ctx->p.krylov_rtol;
+    const int maxit = std::max(1, ctx->p.krylov_maxit);
+    const bool mixed = ctx->p.form == HMEC_FORM_MIXED;
+    Gm G{sv.H, sv.cs, sv.sn, sv.gvec, sv.yvec, sv.dots, sv.bnorm, sv.done, sv.kcur, ctx->ds};
+    cudaGraphConditionalHandle hr = 0, hi = 0;
+    int rc = graph_handle(ctx, ctx->stream, &hr);
+    if (rc) return rc;
+    HMEC_LAUNCH(ctx, k_solve_init, 1, 1, 0, G, sv.gctl, maxit, hr);
+    if ((rc = graph_while_begin(ctx, ctx->stream, hr, s_restart))) return rc;
+    const int64_t l0 = ctx->launches;
+    {
+        StreamScope scope(ctx, s_restart);
+        HMEC_LAUNCH(ctx, k_true_resid, nblk, RED_BS, 0, N, L0.col, L0.val, L0.db, ctx->S, sv.w, sv.partial, nblk);
+        if ((rc = graph_handle(ctx, s_restart, &hi))) return rc;
+        HMEC_LAUNCH(ctx, k_cycle_begin_g, 1, 32, 0, G, sv.partial, nblk, rtol, m, sv.gctl, hr, hi);
+        HMEC_LAUNCH(ctx, k_scale_vec, nblocks(N, 256), 256, 0, N, sv.w, sv.dots, sv.V, sv.done, mixed ? L0.fb : nullptr,
+                    mixed ? nullptr : L0.pb);
+        if ((rc = graph_while_begin(ctx, s_restart, hi, s_inner))) return rc;
+        const int64_t l1 = ctx->launches;
+        {
+            StreamScope scope2(ctx, s_inner);
+            if (mixed) {
+                if ((rc = vcycle<float>(ctx, 0))) return rc;
+                if ((rc = arnoldi<float>(ctx, L0.fx, nullptr, m / 2, G, rtol, true))) return rc;
+            } else {
+                if ((rc = vcycle<double>(ctx, 0, L0.pb, L0.dx_))) return rc;
+                if ((rc = arnoldi<double>(ctx, L0.dx_, nullptr, m / 2, G, rtol, true))) return rc;
+            }
+            HMEC_LAUNCH(ctx, k_inner_cond, 1, 1, 0, G, m, sv.gctl, hi);
+        }
+        *n_inner = ctx->launches - l1;
+        if ((rc = graph_while_end(ctx, s_inner))) return rc;
+        HMEC_LAUNCH(ctx, k_lsq, 1, 1, 0, G, m);
+        HMEC_LAUNCH(ctx, k_xupdate, nblocks(N, 256), 256, 0, N, sv.Z, sv.yvec, sv.kcur, ctx->S);
+    }
+    *n_restart = ctx->launches - l0 - *n_inner;
+    if ((rc = graph_while_end(ctx, s_restart))) return rc;
+    HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;
 }

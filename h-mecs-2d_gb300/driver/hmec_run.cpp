@@ -36,12 +36,40 @@ std::vector<double> linspaced(int n, double low, double high) {  // Eigen LinSpa
     return v;
 }
 
-void append_row(const std::string& path, double timesum, double dt, const Grid& g, int row) {
+// A double as an ostream with the default flags and precision 6 prints it
+// (the %g conversion).
+std::string fmt_g(double v) {
+    char b[64];
+    snprintf(b, sizeof(b), "%g", v);
+    return b;
+}
+
+// A vector the way Eigen's operator<< prints a matrix with its default
+// IOFormat (the output the reference's EVO and fault files hold): every
+// coefficient right-aligned to the width of the widest one, coefficients
+// separated by one space (a row vector) or one per line (a column vector).
+std::string eigen_text(const double* v, int n, bool column) {
+    std::vector<std::string> t(n);
+    size_t w = 0;
+    for (int k = 0; k < n; k++) {
+        t[k] = fmt_g(v[k]);
+        if (t[k].size() > w) w = t[k].size();
+    }
+    std::string out;
+    for (int k = 0; k < n; k++) {
+        if (k) out += column ? "\n" : " ";
+        out.append(w - t[k].size(), ' ');
+        out += t[k];
+    }
+    return out;
+}
+
+// One line of an EVO_*.txt series (:1751-1799): time, dt, the fault row.
+void append_row(const std::string& path, double timesum, double dt, const double* row, int n) {
     FILE* f = fopen(path.c_str(), "a");
     if (!f) return;
-    fprintf(f, "%g    %g    ", timesum, dt);
-    for (int j = 0; j < g.cols; j++) fprintf(f, "%s%g", j ? " " : "", g.a[(size_t)j * g.rows + row]);
-    fprintf(f, "\n");
+    const std::string line = fmt_g(timesum) + "    " + fmt_g(dt) + "    " + eigen_text(row, n, false) + "\n";
+    fwrite(line.data(), 1, line.size(), f);
     fclose(f);
 }
 
@@ -203,8 +231,13 @@ int main(int argc, char** argv) {
         }
     }
 
-    Grid VSLIPB(Ny, Nx), ETA(Ny, Nx), OM(Ny, Nx), SigmaY(Ny, Nx), SII_fault(Ny, Nx);
-    Grid pf(Ny1, Nx1), pt(Ny1, Nx1), VIS_COMP(Ny1, Nx1), EL_DECOM(Ny1, Nx1), vxD(Ny1, Nx1), Peff(Ny1, Nx1);
+    // the fault-row series of :1751-1799, in one row gather per step
+    const int evo_ids[] = {HMEC_F_VSLIPB, HMEC_F_ETA, HMEC_F_pf, HMEC_F_pt, HMEC_F_SigmaY, HMEC_F_SII_fault,
+                           HMEC_F_OM, HMEC_F_VIS_COMP, HMEC_F_EL_DECOM, HMEC_F_vxD};
+    const int nevo = (int)(sizeof(evo_ids) / sizeof(evo_ids[0]));
+    std::vector<int> evo_off(nevo + 1, 0);
+    for (int k = 0; k < nevo; k++) evo_off[k + 1] = evo_off[k] + (hmec_field_grid(evo_ids[k]) ? Nx1 : Nx);
+    std::vector<double> rows(evo_off[nevo]), peff(Nx1);
     for (int s = 0; s < steps; s++) {
         hmec_step_report r;
         if (check(ctx, hmec_timestep(ctx, &r), "hmec_timestep")) break;
@@ -216,28 +249,39 @@ int main(int argc, char** argv) {
         printf("Vslip max:         %g\n", r.Vmax);
         printf("iter - iterations:   %d\n", r.global_iters);
         printf("global - iterations: %d\n", r.ynlast);
-        // :1751-1805 fault-row time series
-        hmec_download_field(ctx, HMEC_F_VSLIPB, VSLIPB.a.data(), Ny, Nx);
-        hmec_download_field(ctx, HMEC_F_ETA, ETA.a.data(), Ny, Nx);
-        hmec_download_field(ctx, HMEC_F_OM, OM.a.data(), Ny, Nx);
-        hmec_download_field(ctx, HMEC_F_SigmaY, SigmaY.a.data(), Ny, Nx);
-        hmec_download_field(ctx, HMEC_F_SII_fault, SII_fault.a.data(), Ny, Nx);
-        hmec_download_field(ctx, HMEC_F_pf, pf.a.data(), Ny1, Nx1);
-        hmec_download_field(ctx, HMEC_F_pt, pt.a.data(), Ny1, Nx1);
-        hmec_download_field(ctx, HMEC_F_VIS_COMP, VIS_COMP.a.data(), Ny1, Nx1);
-        hmec_download_field(ctx, HMEC_F_EL_DECOM, EL_DECOM.a.data(), Ny1, Nx1);
-        hmec_download_field(ctx, HMEC_F_vxD, vxD.a.data(), Ny1, Nx1);
-        for (size_t k = 0; k < Peff.a.size(); k++) Peff.a[k] = pt.a[k] - pf.a[k];
-        append_row(d + "EVO_Vslip.txt", r.timesum, r.dt, VSLIPB, line_fault);
-        append_row(d + "EVO_viscosity.txt", r.timesum, r.dt, ETA, line_fault);
-        append_row(d + "EVO_press_flu.txt", r.timesum, r.dt, pf, line_fault);
-        append_row(d + "EVO_press_eff.txt", r.timesum, r.dt, Peff, line_fault);
-        append_row(d + "EVO_SigmaY.txt", r.timesum, r.dt, SigmaY, line_fault);
-        append_row(d + "EVO_Sii.txt", r.timesum, r.dt, SII_fault, line_fault);
-        append_row(d + "EVO_Theta.txt", r.timesum, r.dt, OM, line_fault);
-        append_row(d + "EVO_Visc_comp.txt", r.timesum, r.dt, VIS_COMP, line_fault);
-        append_row(d + "EVO_Elast_comp.txt", r.timesum, r.dt, EL_DECOM, line_fault);
-        append_row(d + "EVO_vxD.txt", r.timesum, r.dt, vxD, line_fault);
+        if (r.timestep == 1) {  // :1739-1749
+            FILE* fx = fopen((d + "x_fault.txt").c_str(), "w");
+            if (fx) {
+                const std::string t = eigen_text(x.data(), Nx, true) + "\n";
+                fwrite(t.data(), 1, t.size(), fx);
+                fclose(fx);
+            }
+            const int rsf_ids[] = {HMEC_F_ARSF, HMEC_F_BRSF, HMEC_F_LRSF};
+            std::vector<double> rr(3 * (size_t)Nx);
+            if (!check(ctx, hmec_download_rows(ctx, line_fault, 3, rsf_ids, rr.data()), "download_rows")) {
+                FILE* fr = fopen((d + "rsf_fault.txt").c_str(), "a");
+                if (fr) {
+                    const std::string t = eigen_text(rr.data(), Nx, false) + "\n\n" +
+                                          eigen_text(rr.data() + Nx, Nx, false) + "\n\n" +
+                                          eigen_text(rr.data() + 2 * Nx, Nx, false) + "\n";
+                    fwrite(t.data(), 1, t.size(), fr);
+                    fclose(fr);
+                }
+            }
+        }
+        if (check(ctx, hmec_download_rows(ctx, line_fault, nevo, evo_ids, rows.data()), "download_rows")) break;
+        const double* row = rows.data();
+        for (int j = 0; j < Nx1; j++) peff[j] = row[evo_off[3] + j] - row[evo_off[2] + j];  // pt - pf
+        append_row(d + "EVO_Vslip.txt", r.timesum, r.dt, row + evo_off[0], Nx);
+        append_row(d + "EVO_viscosity.txt", r.timesum, r.dt, row + evo_off[1], Nx);
+        append_row(d + "EVO_press_flu.txt", r.timesum, r.dt, row + evo_off[2], Nx1);
+        append_row(d + "EVO_press_eff.txt", r.timesum, r.dt, peff.data(), Nx1);
+        append_row(d + "EVO_SigmaY.txt", r.timesum, r.dt, row + evo_off[4], Nx);
+        append_row(d + "EVO_Sii.txt", r.timesum, r.dt, row + evo_off[5], Nx);
+        append_row(d + "EVO_Theta.txt", r.timesum, r.dt, row + evo_off[6], Nx);
+        append_row(d + "EVO_Visc_comp.txt", r.timesum, r.dt, row + evo_off[7], Nx1);
+        append_row(d + "EVO_Elast_comp.txt", r.timesum, r.dt, row + evo_off[8], Nx1);
+        append_row(d + "EVO_vxD.txt", r.timesum, r.dt, row + evo_off[9], Nx1);
         FILE* f = fopen((d + "EVO_data.txt").c_str(), "a");
         if (f) {
             fprintf(f, "%20g%20g%20g%20d%20d\n", r.timesum, r.dt, r.Vmax, r.ynlast, r.global_iters);

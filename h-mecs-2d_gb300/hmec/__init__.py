@@ -60,7 +60,7 @@ class Params(C.Structure):
         ("krylov_maxit", C.c_int32), ("mg_levels", C.c_int32), ("mg_pre", C.c_int32), ("mg_post", C.c_int32),
         ("mg_coarse_sweeps", C.c_int32), ("rsf_maxit", C.c_int32), ("advect_markers", C.c_int32),
         ("rk4_as_written", C.c_int32), ("quirk_accumulate_sums", C.c_int32), ("bounds_check", C.c_int32),
-        ("mg_flags", C.c_int32),
+        ("mg_flags", C.c_int32), ("graph", C.c_int32),
     ]
 
 
@@ -95,10 +95,12 @@ SCALARS = _xlist("HMEC_SCALAR_LIST")
 EXPORTS = ["hmec_abi_version", "hmec_params_default", "hmec_field_name", "hmec_field_grid", "hmec_marker_name",
            "hmec_scalar_name", "hmec_marknum", "hmec_create", "hmec_destroy", "hmec_last_error",
            "hmec_upload_markers", "hmec_download_markers", "hmec_upload_field", "hmec_download_field",
+           "hmec_download_rows",
            "hmec_set_scalar", "hmec_get_scalar", "hmec_markers_to_nodes", "hmec_timestep_begin",
            "hmec_global_iteration", "hmec_timestep_end", "hmec_advect_markers", "hmec_timestep",
            "hmec_assemble_csr", "hmec_solve_system", "hmec_kernel_launches", "hmec_synchronize", "hmec_stream",
-           "hmec_profile_kernel", "hmec_profile_read", "hmec_markers_to_nodes_noalloc", "hmec_cell_index"]
+           "hmec_profile_kernel", "hmec_profile_read", "hmec_markers_to_nodes_noalloc", "hmec_cell_index",
+           "hmec_graph_status"]
 
 _lib = None
 
@@ -143,6 +145,7 @@ def load(build_if_missing: bool = True):
     L.hmec_download_markers.argtypes = [vp, P(P(C.c_double)), C.c_int64]
     L.hmec_upload_field.argtypes = [vp, C.c_int32, P(C.c_double), C.c_int32, C.c_int32]
     L.hmec_download_field.argtypes = [vp, C.c_int32, P(C.c_double), C.c_int32, C.c_int32]
+    L.hmec_download_rows.argtypes = [vp, C.c_int32, C.c_int32, P(C.c_int32), P(C.c_double)]
     L.hmec_set_scalar.argtypes = [vp, C.c_int32, C.c_double]
     L.hmec_get_scalar.argtypes = [vp, C.c_int32, P(C.c_double)]
     for fn in ("hmec_markers_to_nodes", "hmec_timestep_begin", "hmec_timestep_end", "hmec_advect_markers",
@@ -156,10 +159,12 @@ def load(build_if_missing: bool = True):
     L.hmec_solve_system.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_int32), P(C.c_double)]
     L.hmec_kernel_launches.argtypes = [vp]
     L.hmec_kernel_launches.restype = C.c_int64
+    L.hmec_graph_status.argtypes = [vp]
+    L.hmec_graph_status.restype = C.c_int32
     L.hmec_stream.argtypes = [vp]
     L.hmec_stream.restype = vp
     L.hmec_profile_kernel.argtypes = [vp, C.c_char_p]
-    L.hmec_profile_read.argtypes = [vp, P(C.c_int64), P(C.c_double), P(C.c_double)]
+    L.hmec_profile_read.argtypes = [vp, P(C.c_int64), P(C.c_double), P(C.c_double), P(C.c_double)]
     L.hmec_markers_to_nodes_noalloc.argtypes = [P(Params), P(P(C.c_double)), C.c_int64, P(P(C.c_double)), vp]
     L.hmec_markers_to_nodes_noalloc.restype = C.c_int32
     L.hmec_cell_index.argtypes = [P(C.c_double), C.c_int64, C.c_double, C.c_int32, P(C.c_int32)]
@@ -257,6 +262,18 @@ class Model:
         self._check(self.L.hmec_download_field(self.h, FIELDS.index(name), _dptr(buf), r, c), "download_field")
         return buf.reshape((r, c), order="F")
 
+    def rows(self, row, names) -> dict:
+        """Row `row` of each named field, in one device gather and transfer."""
+        ids = (C.c_int32 * len(names))(*[FIELDS.index(n) for n in names])
+        lens = [self.shape(n)[1] for n in names]
+        buf = np.empty(sum(lens))
+        self._check(self.L.hmec_download_rows(self.h, row, len(names), ids, _dptr(buf)), "download_rows")
+        out, o = {}, 0
+        for n, k in zip(names, lens):
+            out[n] = buf[o:o + k].copy()
+            o += k
+        return out
+
     def set_scalar(self, name, v):
         self._check(self.L.hmec_set_scalar(self.h, SCALARS.index(name), float(v)), "set_scalar")
 
@@ -313,6 +330,16 @@ class Model:
         return self.L.hmec_kernel_launches(self.h)
 
     @property
+    def graph_status(self) -> int:
+        """1: timesteps run as one CUDA graph launch; 0: not yet; -1: host-driven."""
+        return self.L.hmec_graph_status(self.h)
+
+    def graph_error(self) -> str:
+        """Why the graph is off (after graph_status returned -1)."""
+        msg = self.L.hmec_last_error(self.h)
+        return msg.decode() if msg else ""
+
+    @property
     def stream_ptr(self) -> int:
         """cudaStream_t of the context (for CUDA-event timing)."""
         return self.L.hmec_stream(self.h) or 0
@@ -321,9 +348,11 @@ class Model:
         self._check(self.L.hmec_profile_kernel(self.h, name.encode() if name else None), "profile_kernel")
 
     def profile_read(self):
-        n, ms, b = C.c_int64(), C.c_double(), C.c_double()
-        self._check(self.L.hmec_profile_read(self.h, C.byref(n), C.byref(ms), C.byref(b)), "profile_read")
-        return n.value, ms.value, b.value
+        """(launches, total ms, compulsory bytes, bytes moved) of the profiled kernel family."""
+        n, ms, b, bm = C.c_int64(), C.c_double(), C.c_double(), C.c_double()
+        self._check(self.L.hmec_profile_read(self.h, C.byref(n), C.byref(ms), C.byref(b), C.byref(bm)),
+                    "profile_read")
+        return n.value, ms.value, b.value, bm.value
 
     # ---------------------------------------------------------- hooks
     def assemble_csr(self):

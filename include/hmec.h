@@ -101,6 +101,9 @@ typedef struct hmec_params {
     int32_t quirk_accumulate_sums; /* oracle only: marker sums accumulate across steps */
     int32_t bounds_check;     /* 1: device index checks set HMEC_ERR_BOUNDS */
     int32_t mg_flags;         /* multigrid coarsening options, HMEC_MG_* bits */
+    int32_t graph;            /* 1: hmec_timestep runs a whole step as one CUDA graph launch, its
+                                 loops (global iterations, FGMRES restarts, Arnoldi steps) as
+                                 conditional nodes decided on the device; 0: host-driven launches */
 } hmec_params;
 
 /* mg_flags bits */
@@ -221,6 +224,12 @@ int32_t hmec_download_markers(hmec_ctx* ctx, double* const* fields, int64_t n);
 /* One node field; rows/cols must match the field's grid. */
 int32_t hmec_upload_field(hmec_ctx* ctx, int32_t field, const double* colmajor, int32_t rows, int32_t cols);
 int32_t hmec_download_field(hmec_ctx* ctx, int32_t field, double* colmajor, int32_t rows, int32_t cols);
+/* Row `row` of each of nfields node fields, gathered on the device and
+ * copied back in one transfer: out receives the rows one after another, each
+ * as long as its field's row (Nx basic, Nx+1 staggered).  The per-step
+ * EVO_*.txt series print such rows of the fault line (:1751-1805); this
+ * replaces downloading the whole fields.                                    */
+int32_t hmec_download_rows(hmec_ctx* ctx, int32_t row, int32_t nfields, const int32_t* fields, double* out);
 int32_t hmec_set_scalar(hmec_ctx* ctx, int32_t id, double value);
 int32_t hmec_get_scalar(hmec_ctx* ctx, int32_t id, double* value);
 
@@ -263,11 +272,15 @@ int32_t hmec_solve_system(hmec_ctx* ctx, const double* rhs, double* x, int32_t* 
 void* hmec_stream(hmec_ctx* ctx);
 /* Time every launch of the kernel family whose name starts with `name`
  * (NULL: stop) with CUDA events on the context stream, and accumulate the
- * algorithmic bytes those launches move; read and reset with
- * hmec_profile_kernel().  Used by the benchmark's live roofline (no
- * counterpart in the reference).                                           */
+ * bytes those launches move; read and reset with hmec_profile_read():
+ * *bytes_compulsory is the compulsory traffic of the work done (per cell:
+ * the 42 matrix coefficients and the vectors a sweep or a Krylov step must
+ * touch), *bytes_moved what this implementation moves by its own account
+ * (stored patch inverses, column offsets, padding included).  Used by the
+ * benchmark's live roofline (no counterpart in the reference).             */
 int32_t hmec_profile_kernel(hmec_ctx* ctx, const char* name);
-int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, double* bytes);
+int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, double* bytes_compulsory,
+                          double* bytes_moved);
 /* Markers -> nodes without allocating device memory.  No counterpart in the
  * reference: it serves hosts that may not call cudaMalloc (an application
  * that owns the device allocator, a real-time loop that must not block on
@@ -299,6 +312,11 @@ int32_t hmec_markers_to_nodes_noalloc(const hmec_params* p, const double* const*
  * near cell edges; this entry exposes that rule so it can be checked
  * bit-exactly (no counterpart in the reference).                           */
 int32_t hmec_cell_index(const double* x, int64_t n, double d, int32_t half, int32_t* out);
+/* How hmec_timestep runs on this context (no counterpart in the reference):
+ * 1 = each step is one CUDA graph launch, 0 = host-driven launches so far
+ * (the first step, or while a kernel is profiled), -1 = host-driven for good
+ * (graph = 0, or the capture failed; hmec_last_error() then gives why).     */
+int32_t hmec_graph_status(hmec_ctx* ctx);
 /* Device-kernel launches issued since hmec_create. */
 int64_t hmec_kernel_launches(const hmec_ctx* ctx);
 /* Synchronise the context stream. */

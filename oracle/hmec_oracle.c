@@ -148,6 +148,7 @@ void hmo_params_default(hmec_params* p) {
     p->quirk_accumulate_sums = 0;
     p->bounds_check = 0;
     p->mg_flags = 1; /* HMEC_MG_DARCY_HARMONIC */
+    p->graph = 1;
 }
 
 /* Eigen 3.3 LinSpaced(n, low, high) for |high| >= |low| (all grids here). */

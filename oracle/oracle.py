@@ -49,7 +49,7 @@ class HmecParams(C.Structure):
         ("krylov_maxit", C.c_int32), ("mg_levels", C.c_int32), ("mg_pre", C.c_int32), ("mg_post", C.c_int32),
         ("mg_coarse_sweeps", C.c_int32), ("rsf_maxit", C.c_int32), ("advect_markers", C.c_int32),
         ("rk4_as_written", C.c_int32), ("quirk_accumulate_sums", C.c_int32), ("bounds_check", C.c_int32),
-        ("mg_flags", C.c_int32),
+        ("mg_flags", C.c_int32), ("graph", C.c_int32),
     ]
 
 
@@ -168,13 +168,13 @@ def equilibrate(A):
     return Dr, Dc
 
 
-def direct_solve(A, b, refine: int = 4, ordering: str = "COLAMD"):
+def direct_solve(A, b, refine: int = 4, ordering: str = "COLAMD", pivot_thresh: float = 1.0):
     """Equilibrated SuperLU solve with FP64 iterative refinement (the Pardiso stand-in)."""
     import scipy.sparse.linalg as spla
 
     Dr, Dc = equilibrate(A)
     As = (Dr @ A @ Dc).tocsc()
-    lu = spla.splu(As, permc_spec=ordering, diag_pivot_thresh=1.0)
+    lu = spla.splu(As, permc_spec=ordering, diag_pivot_thresh=pivot_thresh)
 
     def solve(r):
         return Dc @ lu.solve(Dr @ r)
@@ -193,9 +193,11 @@ def direct_solve(A, b, refine: int = 4, ordering: str = "COLAMD"):
 class Oracle:
     """One reference model instance on the CPU."""
 
-    #: SuperLU column ordering of the direct solve (a second ordering gives the
-    #: oracle's own round-off floor)
+    #: SuperLU column ordering and partial-pivoting threshold of the direct
+    #: solve (a second ordering or threshold gives the oracle's own round-off
+    #: floor: the same system solved with other pivots)
     ordering = "COLAMD"
+    pivot_thresh = 1.0
 
     def __init__(self, params: HmecParams):
         self.L = lib()
@@ -309,7 +311,7 @@ class Oracle:
             A = sp.csr_matrix((np.ctypeslib.as_array(data, shape=(nnz,)).copy(),
                                np.ctypeslib.as_array(indices, shape=(nnz,)).copy(), ip.copy()), shape=(n, n))
             b = np.ctypeslib.as_array(rhs, shape=(n,)).copy()
-            sol = direct_solve(A, b, ordering=self.ordering)
+            sol = direct_solve(A, b, ordering=self.ordering, pivot_thresh=self.pivot_thresh)
             np.ctypeslib.as_array(x, shape=(n,))[...] = sol
             self.solve_calls += 1
             self.last_solution = sol

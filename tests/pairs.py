@@ -74,6 +74,21 @@ GROUPS = {
 }
 
 
+# The output-only invariants (cpp/h_mec_rsf_v9.cpp:1523-1557) and the state
+# rolled over to the next step (:1658-1726), compared like the solution.
+# EL_DECOM is a difference quotient of pressure changes over a step and
+# VXF0/VYF0 carry the Darcy velocity; they are held to the Darcy tolerance.
+GROUPS_ALL = dict(GROUPS)
+GROUPS_ALL.update({
+    "invariants": ["EII", "EIIVP", "SII", "DIS", "VIS_COMP"],
+    "rollover": ["PT0", "PF0", "PTF0", "SXX0", "SYY0", "SXY0", "VX0", "VY0"],
+    "fluid_rollover": ["VXF0", "VYF0"],
+    "el_decom": ["EL_DECOM"],
+})
+#: groups held to the Darcy tolerance instead of the solution's
+LOOSE_GROUPS = ("darcy", "fluid_rollover", "el_decom")
+
+
 def group_errors(m, o, groups=GROUPS):
     out = {}
     for g, names in groups.items():

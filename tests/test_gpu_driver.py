@@ -1,4 +1,12 @@
-"""The C++ host loop (driver/hmec_run.cpp) drives the library like main() does."""
+"""The C++ host loop (driver/hmec_run.cpp) drives the library like main() does.
+
+Its output files follow the reference's (cpp/h_mec_rsf_v9.cpp:1739-1805):
+EVO_*.txt lines of time, dt and the fault row as Eigen prints a row vector
+(each coefficient right-aligned to the widest one's %g text, one space
+apart), EVO_data.txt in setw(20) columns, x_fault.txt (the node abscissae,
+one per line) and rsf_fault.txt (the a, b, L rows) at step 1.  The printed
+values are checked against the CPU oracle run on the same model.
+"""
 import os
 import subprocess
 
@@ -6,10 +14,17 @@ import numpy as np
 import pytest
 
 import hmec
+import oracle as O
 from hmec import build as B
 from hmec import synth
 
 pytestmark = pytest.mark.gpu
+
+
+def eigen_row(v, column=False):
+    t = ["%g" % x for x in v]
+    w = max(len(s) for s in t)
+    return ("\n" if column else " ").join(s.rjust(w) for s in t)
 
 
 def test_driver_writes_reference_outputs(tmp_path):
@@ -21,18 +36,56 @@ def test_driver_writes_reference_outputs(tmp_path):
     assert out.stdout.count("total time:") == steps
     data = open(os.path.join(tmp_path, "EVO_data.txt")).read().split("\n")
     assert len([l for l in data if l.strip()]) == steps
-    vslip = [l.split() for l in open(os.path.join(tmp_path, "EVO_Vslip.txt")) if l.strip()]
-    assert len(vslip) == steps and len(vslip[-1]) == 2 + Nx
-    # the same model through the Python binding
-    p = hmec.default_params(Nx=Nx, Ny=Ny, xsize=xs, ysize=ys)
+    assert all(len(l) == 100 for l in data if l.strip())  # five setw(20) columns
+    # the same model on the oracle
+    po = O.default_params(Nx=Nx, Ny=Ny, xsize=xs, ysize=ys)
+    o = O.Oracle(po)
+    mk, nodes = synth.reference_state(po)
+    o.set_markers(mk)
+    for k, v in nodes.items():
+        o.set_field(k, v)
+    lf = int((Ny - 1) / 2.0)
+    series = {"EVO_Vslip.txt": "VSLIPB", "EVO_viscosity.txt": "ETA", "EVO_press_flu.txt": "pf",
+              "EVO_SigmaY.txt": "SigmaY", "EVO_Theta.txt": "OM", "EVO_Visc_comp.txt": "VIS_COMP"}
+    lines = {f: [l.rstrip("\n") for l in open(os.path.join(tmp_path, f)) if l.strip()] for f in series}
+    for s in range(steps):
+        o.timestep()
+        for f, name in series.items():
+            line = lines[f][s]
+            head, row = line.split("    ", 2)[:2], line.split("    ", 2)[2]
+            ref = o.field(name)[lf]
+            got = np.array([float(v) for v in row.split()])
+            assert got.shape == ref.shape, (f, s)
+            # %g keeps six significant digits
+            assert np.allclose(got, ref, rtol=2e-6, atol=1e-300), (f, s, got, ref)
+            assert float(head[0]) == pytest.approx(o.scalar("timesum"), rel=2e-6), (f, s)
+            # the Eigen layout of the printed values
+            assert row == eigen_row(got), (f, s, row)
+    # step 1 files
+    x = [float(v) for v in open(os.path.join(tmp_path, "x_fault.txt")).read().split()]
+    assert np.allclose(x, synth.linspaced(Nx, 0, xs), rtol=2e-6)
+    xt = open(os.path.join(tmp_path, "x_fault.txt")).read()
+    assert xt == eigen_row(np.array(x), column=True) + "\n"
+    rsf = open(os.path.join(tmp_path, "rsf_fault.txt")).read().split("\n\n")
+    assert len(rsf) == 3
+    for part, name in zip(rsf, ("ARSF", "BRSF", "LRSF")):
+        got = np.array([float(v) for v in part.split()])
+        assert np.allclose(got, o.field(name)[lf], rtol=2e-6), name
+
+
+def test_download_rows_equals_field_rows():
+    p = hmec.default_params(**synth.PRESETS["tiny"])
     m = hmec.Model(p)
-    mk, nodes = synth.reference_state(p)
+    mk, nodes = synth.make_state(p, "tiny")
     m.upload_markers(mk)
     for k, v in nodes.items():
         m.upload_field(k, v)
-    for _ in range(steps):
-        r = m.timestep()
-    row = m.field("VSLIPB")[int((Ny - 1) / 2.0)]
-    got = np.array([float(v) for v in vslip[-1][2:]])
-    assert np.allclose(got, row, rtol=1e-5, atol=0)
-    assert float(vslip[-1][0]) == pytest.approx(r["timesum"], rel=1e-5)
+    m.timestep()
+    names = ["VSLIPB", "pf", "ETA", "vxD", "SigmaY"]
+    for row in (0, 5, p.Ny - 1):
+        got = m.rows(row, names)
+        for n in names:
+            assert np.array_equal(got[n], m.field(n)[row]), (row, n)
+    with pytest.raises(hmec.HmecError):
+        m.rows(p.Ny + 5, names)
+    m.close()

@@ -129,8 +129,8 @@ def test_solve_parity(preset, form):
 
 
 @pytest.mark.parametrize("form", [hmec.FORM_FP64, hmec.FORM_MIXED])
-@pytest.mark.parametrize("preset,nsteps", [("tiny", 6), ("c0", 5)])
-def test_timestep_replay(preset, nsteps, form):
+@pytest.mark.parametrize("preset,nsteps,quirk", [("tiny", 6, 0), ("c0", 5, 0), ("tiny", 6, 1)])
+def test_timestep_replay(preset, nsteps, form, quirk):
     """Each step starts the GPU from the oracle's state and compares after one step.
 
     Within a step the plastic (global) iterations amplify round-off near the
@@ -142,9 +142,13 @@ def test_timestep_replay(preset, nsteps, form):
     slip rate (and the state variable it drives) is known only to the
     bisection tolerance of the reference, |dS| <= 1e-3 Pa (:1224), i.e. to
     1e-3 / (a * sigma_eff) relative; that bound applies to those two groups.
+    The output-only invariants and the rolled-over state are compared too.
+    quirk = 1: the oracle accumulates the marker sums across steps as the
+    reference does (Q1, the zeroing at :377-381 acts on copies); the GPU
+    restarts them every step, and the ratios agree to rounding.
     """
-    o, mk, nodes = pairs.oracle_for(preset)
-    o2, _, _ = pairs.oracle_for(preset)
+    o, mk, nodes = pairs.oracle_for(preset, quirk_accumulate_sums=quirk)
+    o2, _, _ = pairs.oracle_for(preset, quirk_accumulate_sums=quirk)
     o2.ordering = "MMD_AT_PLUS_A"
     m = pairs.model_for(preset, mk, nodes, form=form)
     log = []
@@ -155,8 +159,8 @@ def test_timestep_replay(preset, nsteps, form):
         it = o.timestep()
         o2.timestep()
         rep = m.timestep()
-        err = pairs.group_errors(m, o)
-        floor = pairs.group_errors(pairs.OracleView(o2), o)
+        err = pairs.group_errors(m, o, pairs.GROUPS_ALL)
+        floor = pairs.group_errors(pairs.OracleView(o2), o, pairs.GROUPS_ALL)
         res = pairs.bisection_resolution(o)
         log.append((int(o.scalar("timestep")) - 1, it, rep["global_iters"], o.scalar("dt"), m.scalar("dt"), err,
                     floor, res))
@@ -164,7 +168,7 @@ def test_timestep_replay(preset, nsteps, form):
         assert it_g == it_o, log
         assert dt_g == pytest.approx(dt_o, rel=1e-12), log
         for g, e in err.items():
-            bound = max(TOL_DARCY if g == "darcy" else TOL_STEP, 10 * floor[g])
+            bound = max(TOL_DARCY if g in pairs.LOOSE_GROUPS else TOL_STEP, 10 * floor[g])
             if g in ("slip_rate", "state"):
                 bound = max(bound, 2 * res)
             assert e < bound, (step, g, e, floor[g], res, log)

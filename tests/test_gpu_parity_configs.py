@@ -1,0 +1,190 @@
+"""Parity at the benchmarked configurations, in every regime the benchmark
+meets: configuration 1 (201 x 201) from its initial state, after the fault
+becomes active (timestep > tyield) and in a rupture phase (dt far below a
+second); two uneven members of the configuration-3 ensemble; configuration 0
+replayed at sampled steps of a 200-step adaptive run; and a rupture phase of
+configuration 0.
+
+Replay parity: the oracle and the GPU start every compared step from the
+same state (bytes), run one timestep, and are compared field group by group
+(velocity, pressures, stress, slip rate, state, the output-only invariants of
+cpp/h_mec_rsf_v9.cpp:1523-1557 and the rolled-over state of :1658-1726).
+Where the starting state comes from a GPU run (the states after the first
+steps of configuration 1 and of the ensemble members), both sides still start
+from identical bytes.  Bounds, as in the tiny/config-0 replays: 1e-10 relative
+(1e-6 for the Darcy-velocity groups); where the global iteration amplifies
+round-off near the yield stress, max(1e-10, 10 x the oracle's own floor)
+(the same system solved with other pivots); slip rate and state within the
+reference's bisection resolution |dS| <= 1e-3 Pa (:1224).  Global iteration
+counts are equal; dt agrees to 1e-12, or to 1e-8 in a rupture phase, where dt
+follows the slip rate (Lapusta step, :1266-1273).
+"""
+import numpy as np
+import pytest
+
+import hmec
+import oracle as O
+import pairs
+from hmec import synth
+
+pytestmark = pytest.mark.gpu
+
+TOL_STEP = 1e-10
+TOL_DARCY = 1e-6
+RUPTURE_TAU = 16e6  # uniform pre-stress SXY0 (Pa), above the fault's steady-state strength at V = 1e-9 m/s
+FORMS = (hmec.FORM_MIXED, hmec.FORM_FP64)
+
+
+def replay_and_check(over, mk, snap, label, dt_rel=1e-12, forms=FORMS):
+    """One timestep from `snap` on the oracle and on the GPU (each form);
+    asserts the bounds of the module docstring and returns the errors."""
+    o = O.Oracle(O.default_params(**over))
+    o.set_markers(mk)
+    o.load_state(snap)
+    it_o = o.timestep()
+    dt_o = o.scalar("dt")
+    res = pairs.bisection_resolution(o)
+    out = {}
+    floor = None
+    for form in forms:
+        m = hmec.Model(hmec.default_params(**dict(over, form=form)))
+        m.upload_markers(mk)
+        m.load_state(snap)
+        rep = m.timestep()
+        err = pairs.group_errors(m, pairs.OracleView(o), pairs.GROUPS_ALL)
+        dt_g = m.scalar("dt")
+        m.close()
+        assert rep["global_iters"] == it_o, (label, form, rep, it_o)
+        assert dt_g == pytest.approx(dt_o, rel=dt_rel), (label, form, dt_g, dt_o)
+
+        def bound(g, fl):
+            b = TOL_DARCY if g in pairs.LOOSE_GROUPS else TOL_STEP
+            if fl is not None:
+                b = max(b, 10 * fl[g])
+            if g in ("slip_rate", "state"):
+                b = max(b, 2 * res)
+            return b
+
+        bad = {g: e for g, e in err.items() if not e < bound(g, None)}
+        if bad and floor is None:
+            # the oracle's own floor: the same step with other pivots
+            o2 = O.Oracle(O.default_params(**over))
+            o2.pivot_thresh = 0.1
+            o2.set_markers(mk)
+            o2.load_state(snap)
+            o2.timestep()
+            floor = pairs.group_errors(pairs.OracleView(o2), pairs.OracleView(o), pairs.GROUPS_ALL)
+        if bad:
+            bad = {g: (e, bound(g, floor)) for g, e in err.items() if not e < bound(g, floor)}
+        assert not bad, (label, form, bad, floor, res)
+        out[form] = err
+    return dict(errors=out, iters=it_o, dt=dt_o, Vmax=o.scalar("Vmax"))
+
+
+def fp64_state_after(over, mk, nodes, steps):
+    """The state after `steps` timesteps of the GPU's plain FP64 form."""
+    m = hmec.Model(hmec.default_params(**dict(over, form=hmec.FORM_FP64)))
+    m.upload_markers(mk)
+    for k, v in nodes.items():
+        m.upload_field(k, v)
+    for _ in range(steps):
+        m.timestep()
+    snap = m.snapshot()
+    m.close()
+    return snap
+
+
+def initial_snapshot(over, mk, nodes):
+    """The state the initial fields define (all other fields zero, the
+    library's initial scalars)."""
+    m = hmec.Model(hmec.default_params(**over))
+    m.upload_markers(mk)
+    for k, v in nodes.items():
+        m.upload_field(k, v)
+    snap = m.snapshot()
+    m.close()
+    return snap
+
+
+def prestressed(snap, tau=RUPTURE_TAU):
+    s = dict(snap)
+    s["SXY0"] = np.full_like(snap["SXY0"], tau)
+    return s
+
+
+# ------------------------------------------------------------ configuration 1
+@pytest.fixture(scope="module")
+def c1_state():
+    over = pairs.overrides("c1")
+    p = hmec.default_params(**over)
+    mk, nodes = synth.make_state(p, "c1")
+    return over, mk, nodes
+
+
+def test_c1_initial_step(c1_state):
+    over, mk, nodes = c1_state
+    replay_and_check(over, mk, initial_snapshot(over, mk, nodes), "c1 step 1")
+
+
+def test_c1_step_with_active_fault_and_rupture_phase(c1_state):
+    over, mk, nodes = c1_state
+    snap = fp64_state_after(over, mk, nodes, 2)  # the next step has timestep > tyield
+    r = replay_and_check(over, mk, snap, "c1 step 3")
+    assert r["Vmax"] > 0
+    # rupture phase: the same state under a uniform pre-stress above the
+    # fault strength; the step reduces dt to follow the slip rate
+    r = replay_and_check(over, mk, prestressed(snap), "c1 rupture", dt_rel=1e-8)
+    assert r["dt"] <= 1.0 and r["Vmax"] > 1e-3 and r["iters"] > 3, r
+
+
+# ------------------------------------------------------------ configuration 3
+def _members():
+    """Two uneven ensemble members (different side lengths in x and y), the
+    smallest ones, so that the oracle stays fast."""
+    allm = synth.ensemble_members(64)
+    uneven = [m for m in allm if m[0]["Nx"] != m[0]["Ny"]]
+    uneven.sort(key=lambda m: m[0]["Nx"] * m[0]["Ny"])
+    return uneven[:2]
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_config3_member_steps(k):
+    over0, mat, seed = _members()[k]
+    over = dict(over0, **pairs.SOLVER)
+    p = hmec.default_params(**over)
+    mk, nodes = synth.instance_state(p, mat, seed)
+    label = "member %dx%d" % (over["Nx"], over["Ny"])
+    replay_and_check(over, mk, initial_snapshot(over, mk, nodes), label + " step 1")
+    replay_and_check(over, mk, fp64_state_after(over, mk, nodes, 2), label + " step 3")
+
+
+# ------------------------------------------------------------ configuration 0
+def test_c0_sampled_steps_of_a_200_step_run():
+    """The oracle runs 200 adaptive steps; at sampled steps the GPU (both
+    forms) replays that step from the oracle's state."""
+    o, mk, nodes = pairs.oracle_for("c0")
+    over = pairs.overrides("c0")
+    samples = {1, 3, 50, 100, 150, 200}
+    seen = []
+    for s in range(1, 201):
+        if s in samples:
+            snap = o.snapshot()
+            r = replay_and_check(over, mk, snap, "c0 step %d" % s)
+            seen.append((s, r["iters"], r["dt"]))
+        o.timestep()
+    assert [x[0] for x in seen] == sorted(samples)
+
+
+def test_c0_rupture_phase():
+    o, mk, nodes = pairs.oracle_for("c0")
+    over = pairs.overrides("c0")
+    for _ in range(3):
+        o.timestep()
+    snap = prestressed(o.snapshot())
+    r = replay_and_check(over, mk, snap, "c0 rupture step", dt_rel=1e-8)
+    assert r["dt"] <= 1.0 and r["Vmax"] > 1e-3, r
+    # the next step, from the oracle's rupture state (dt ~ 1e-4 s)
+    o.load_state(snap)
+    o.timestep()
+    r = replay_and_check(over, mk, o.snapshot(), "c0 rupture step 2", dt_rel=1e-8)
+    assert r["dt"] <= 1e-2, r

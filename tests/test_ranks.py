@@ -42,7 +42,18 @@ def _worker(rank, world, port, q):
         rate = bench.whole_job_rate(10, world, slowest)
         # ensemble: members shard with no overlap
         mine = bench.shard(range(2 * 7), rank, world)
-        q.put((rank, slowest, rate, mine))
+        # the uneven configuration-3 members: each rank takes its part of a
+        # cost-balanced split of 64 per rank, and the ranks' loads are
+        # compared through a collective of the test (not of the data path)
+        from hmec import synth
+
+        allm = synth.ensemble_members(64 * world)
+        costs = [bench.member_cost(o) for o, _, _ in allm]
+        part = bench.balanced_split(costs, world)[rank]
+        load = torch.tensor([sum(costs[i] for i in part)], dtype=torch.float64)
+        loads = [torch.zeros(1, dtype=torch.float64) for _ in range(world)]
+        dist.all_gather(loads, load)
+        q.put((rank, slowest, rate, mine, part, [float(x.item()) for x in loads], sum(costs)))
     finally:
         dist.destroy_process_group()
 
@@ -65,6 +76,12 @@ def test_two_gloo_ranks_max_and_shard():
     members = sorted(m for r in res for m in r[3])
     assert members == list(range(14))  # every member exactly once
     assert res[0][3] == [0, 2, 4, 6, 8, 10, 12] and res[1][3] == [1, 3, 5, 7, 9, 11, 13]
+    # balanced members: disjoint, complete, and within 1 % of an even split
+    parts = [set(r[4]) for r in res]
+    assert not (parts[0] & parts[1]) and len(parts[0] | parts[1]) == 128
+    loads, total = res[0][5], res[0][6]
+    assert res[1][5] == loads and abs(sum(loads) - total) < 1e-6 * total
+    assert max(loads) <= 1.01 * total / world, loads
 
 
 def test_single_rank_helpers_need_no_process_group():
@@ -75,3 +92,20 @@ def test_single_rank_helpers_need_no_process_group():
     bench.rank_barrier(1)
     assert bench.shard([5, 6, 7], 0, 1) == [5, 6, 7]
     assert bench.whole_job_rate(8, 1, 2.0) == 4.0
+
+
+def test_balanced_split_beats_round_robin_on_uneven_members():
+    """The cost-balanced member split of the ensemble bench against the
+    round-robin one, on the 64 uneven configuration-3 members per rank."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from hmec import synth
+
+    for world in (2, 4, 8):
+        allm = synth.ensemble_members(64 * world)
+        costs = [bench.member_cost(o) for o, _, _ in allm]
+        parts = bench.balanced_split(costs, world)
+        assert sorted(i for p in parts for i in p) == list(range(len(costs)))
+        bal = max(sum(costs[i] for i in p) for p in parts)
+        rr = max(sum(costs[i] for i in bench.shard(range(len(costs)), r, world)) for r in range(world))
+        assert bal <= 1.01 * sum(costs) / world and bal <= rr, (world, bal, rr)
