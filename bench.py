@@ -287,7 +287,9 @@ def roofline(prof, ms_total, p, peaks, cfg, kernel):
            else "not captured for this configuration",
            "waste_ratio": (traffic / per_launch_alg) if (traffic and per_launch_alg) else None,
            "launches_timed": nprof, "avg_launch_us": (1e3 * prof_ms / nprof) if nprof else None,
-           "share_of_step_time": prof_ms / ms_total if ms_total else None}
+           "share_of_step_time": prof_ms / ms_total if ms_total else None,
+           "timing_note": "CUDA events around every launch of the kernel, in a pass of host-driven steps after the "
+                          "timed (graph) steps; share = kernel time / step time of that pass"}
     return out
 
 
@@ -306,19 +308,24 @@ def run_gpu(args, cfg, world, device_index, peaks, with_fp64=True, with_e2e=True
     m, mk, nodes, p = make_model(hmec.FORM_MIXED, cfg)
     for _ in range(args.warmup):
         m.timestep()
-    m.profile_kernel(DOMINANT)
     rank_barrier(world)
     torch.cuda.synchronize()
     l0 = m.launches
     with ClockSampler(device_index) as clk:
         ms, reps = timed_steps(m, args.steps, flush)
     launches = m.launches - l0
-    prof = m.profile_read()
-    m.profile_kernel(None)
+    graph = m.graph_status
     ms = rank_max(ms, world)
     rank_barrier(world)
+    # the dominant kernel's launches timed one by one (CUDA events around each
+    # launch need host-driven steps, so this is a separate pass of as many steps)
+    m.profile_kernel(DOMINANT)
+    pms, _ = timed_steps(m, args.steps, flush)
+    prof = m.profile_read()
+    m.profile_kernel(None)
     out["mixed"] = dict(ms=ms, reps=reps, launches=launches, gi=sum(r["global_iters"] for r in reps),
-                        kr=sum(r["krylov_iters"] for r in reps), clocks=clk.summary(), prof=prof, p=p)
+                        kr=sum(r["krylov_iters"] for r in reps), clocks=clk.summary(), prof=prof, prof_ms=pms, p=p,
+                        graph=graph)
 
     if with_e2e:
         pin = {}
@@ -353,10 +360,10 @@ def run_gpu(args, cfg, world, device_index, peaks, with_fp64=True, with_e2e=True
             if phase == "upload":
                 m.upload_markers(pin)
                 for f, (flat, r, c) in host_state.items():
-                    m.L.hmec_upload_field(m.h, hmec.FIELDS.index(f), ptr(flat), r, c)
+                    m.L.hmec_upload_field(m.h, 0, hmec.FIELDS.index(f), ptr(flat), r, c)
             elif phase == "download":
                 for f, (flat, r, c) in list(host_out.items()) + list(host_state.items()):
-                    m.L.hmec_download_field(m.h, hmec.FIELDS.index(f), ptr(flat), r, c)
+                    m.L.hmec_download_field(m.h, 0, hmec.FIELDS.index(f), ptr(flat), r, c)
 
         rank_barrier(world)
         e2e_ms, _ = timed_steps(m, args.steps, flush, per_step=hook)
@@ -459,16 +466,17 @@ def cpu_block(cfg, gi_per_step):
 
 # ------------------------------------------------------------------ ensembles
 def run_ensemble(args, rank=0, world=1, device_index=0, nmembers=64):
-    """Configuration 3: 64 uneven members advanced concurrently (mixed form)
-    against the same members run one after another in the plain FP64 form.
-    Many streams are in flight, so this mode times with a device-wide
-    synchronize on both sides of the timed region.  Under torchrun the
-    members shard by rank with balanced cells (64 per rank, weak scaling)."""
+    """Configuration 3: 64 uneven members in one context, one graph launch per
+    ensemble step (mixed form), against the same members run one after
+    another in the plain FP64 form, each in a context of its own.  Many
+    streams are in flight, so this mode times with a device-wide synchronize
+    on both sides of the timed region.  Under torchrun the members shard by
+    rank with balanced cells (64 per rank, weak scaling)."""
     import torch
 
     import hmec
     from hmec import synth
-    from hmec.ensemble import Ensemble
+    from hmec.ensemble import Ensemble, Sequential
 
     torch.cuda.set_device(device_index)
     allm = synth.ensemble_members(nmembers * world)
@@ -477,33 +485,39 @@ def run_ensemble(args, rank=0, world=1, device_index=0, nmembers=64):
     common = dict(krylov_rtol=1e-15, krylov_restart=40, krylov_maxit=4000)
     out = {}
     for form, label in ((hmec.FORM_MIXED, "mixed"), (hmec.FORM_FP64, "fp64")):
-        # the FP64 baseline runs one member at a time, each with the settings
-        # of a model run alone
-        ens = Ensemble(members, concurrent=(form == hmec.FORM_MIXED), form=form, **common)
-        (ens.step if form == hmec.FORM_MIXED else ens.step_sequential)(args.warmup)
-        if form == hmec.FORM_MIXED:
-            for m in ens.models:
-                m.profile_kernel(DOMINANT)
+        # mixed: all members in one context, one graph launch per ensemble
+        # step; the FP64 baseline runs one member at a time, each in a
+        # context of its own with the settings of a model run alone
+        ens = (Ensemble if form == hmec.FORM_MIXED else Sequential)(members, form=form, **common)
+        ens.step(args.warmup)
         torch.cuda.synchronize()
         rank_barrier(world)
-        l0 = sum(m.launches for m in ens.models)
+        l0 = ens.launches
         with ClockSampler(device_index) as clk:
             t0 = time.perf_counter()
-            reps = (ens.step if form == hmec.FORM_MIXED else ens.step_sequential)(args.steps)
+            reps = ens.step(args.steps)
             torch.cuda.synchronize()
             el = time.perf_counter() - t0
         rank_barrier(world)
+        launches = ens.launches - l0
         prof = None
+        graph = None
         if form == hmec.FORM_MIXED:
+            graph = ens.graph_status
+            # one profiled step for the smoothing kernel's roofline (host-driven)
+            for m in ens.members:
+                m.profile_kernel(DOMINANT)
+            ens.step(1)
             tot = [0, 0.0, 0.0, 0.0]
-            for m in ens.models:
+            for m in ens.members:
                 for i, v in enumerate(m.profile_read()):
                     tot[i] += v
                 m.profile_kernel(None)
             prof = tuple(tot)
-        out[label] = dict(s=rank_max(el, world), launches=sum(m.launches for m in ens.models) - l0,
+        out[label] = dict(s=rank_max(el, world), launches=launches,
                           bad=sum(1 for rs in reps for r in rs if r["rc"] != 0),
-                          gi=sum(r["global_iters"] for rs in reps for r in rs), clocks=clk.summary(), prof=prof)
+                          gi=sum(r["global_iters"] for rs in reps for r in rs), clocks=clk.summary(), prof=prof,
+                          graph=graph)
         ens.close()
     return out, members
 
@@ -518,15 +532,18 @@ def ensemble_block(args, out, members, world, peaks):
         "value": whole_job_rate(len(members) * K, world, mx["s"]), "unit": "member-timesteps/s",
         "workload": "config 3: %d members per GPU, per-side nodes 51-301, 4x4 markers/cell, seeded a/b/L/k"
                     % len(members),
-        "form": "mixed, members concurrent (one context and stream each, one launch per smoothing pass on at "
-                "most a quarter of the SMs)",
+        "form": "mixed, all members in one context: one CUDA graph launch per ensemble step (each member's "
+                "global-iteration, restart and Arnoldi loops as conditional nodes, one launch per smoothing pass "
+                "on at most a quarter of the SMs)",
+        "step_as_one_graph_launch": mx["graph"] == 1,
         "timing": "device-wide synchronize around the timed region (many streams)",
         "ms_per_step": 1e3 * mx["s"] / K, "steps": K, "failed_member_steps": mx["bad"],
         "gpu_launches": mx["launches"], "clocks": mx["clocks"],
         "roofline": {"kernel": "k_smooth_stage<float> (one smoothing pass per launch, all members)", "bound": "hbm",
                      "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak if ach else None,
                      "launches_timed": nprof, "avg_launch_us": 1e3 * prof_ms / nprof if nprof else None,
-                     "note": "compulsory bytes per launch over its CUDA-event duration; members' launches overlap"},
+                     "note": "compulsory bytes per launch over its CUDA-event duration, timed in one host-driven "
+                             "step of every member after the timed steps"},
         "fp64_sequential": {"value": whole_job_rate(len(members) * K, world, fp["s"]),
                             "ms_per_step": 1e3 * fp["s"] / K, "failed_member_steps": fp["bad"]},
         "speedup_mixed_vs_fp64": fp["s"] / mx["s"],
@@ -544,7 +561,8 @@ def model_block(args, cfg, world, res, peaks):
         "form": "mixed: FP64 FGMRES(40), FP32 Vanka multigrid preconditioner",
         "global_iters_per_step": mx["gi"] / K, "krylov_iters_per_step": mx["kr"] / K,
         "global_iterations_per_s": world * mx["gi"] / (mx["ms"] / 1e3), "gpu_launches": mx["launches"],
-        "roofline": roofline(mx["prof"], mx["ms"], p, peaks, cfg,
+        "step_as_one_graph_launch": mx["graph"] == 1,
+        "roofline": roofline(mx["prof"], mx["prof_ms"], p, peaks, cfg,
                              "k_vcycle_stage<float> (mixed-form V-cycle: every level's Vanka smoothing pass in "
                              "one cooperative launch)"),
         "clocks": mx["clocks"],
@@ -567,23 +585,47 @@ def model_block(args, cfg, world, res, peaks):
 
 
 def accuracy_vs_oracle(cfg, nsteps=3):
-    """Mixed and plain FP64 forms against the FP64 CPU oracle after the first
-    nsteps timesteps from the same initial state (the oracle's direct solve
-    stands in for Pardiso); also the oracle's timing."""
+    """Mixed and plain FP64 forms against the FP64 CPU oracle (its direct
+    solve stands in for Pardiso): step `nsteps` (the fault active) replayed
+    on the GPU from the oracle's state after nsteps - 1 steps -- the per-step
+    error the target is stated on -- and, for reference, after nsteps
+    free-running steps from the same initial state.  Also the oracle's timing."""
     import hmec
+    import oracle as O
+    from hmec import synth
 
-    r = oracle_steps(cfg, nsteps, 1e9)
-    out = {"steps": r["steps"], "oracle_seconds": r["seconds"]}
+    p = O.default_params(**synth.PRESETS[cfg])
+    o = O.Oracle(p)
+    mk, nodes = synth.make_state(p, cfg)
+    o.set_markers(mk)
+    for k, v in nodes.items():
+        o.set_field(k, v)
+    t0 = time.perf_counter()
+    for _ in range(nsteps - 1):
+        o.timestep()
+    snap = o.snapshot()
+    o.timestep()
+    el = time.perf_counter() - t0
+    ref = {k: o.field(k).copy() for k in FIELDS_ACC}
+    out = {"replayed_step": nsteps, "oracle_seconds": el,
+           "note": "replay: both sides start step %d from the oracle's state; free running: %d steps from the "
+                   "initial state (round-off amplified by the plastic iterations near yield)" % (nsteps, nsteps)}
     for form, label in ((hmec.FORM_MIXED, "mixed"), (hmec.FORM_FP64, "fp64_form")):
-        m, _, _, _ = make_model(form, cfg, r["mk"], r["nodes"])
-        for _ in range(r["steps"]):
-            m.timestep()
-        err = rel_errors({k: m.field(k) for k in FIELDS_ACC}, r["fields"])
-        out[label] = dict(err, **judged(err))
+        m, _, _, _ = make_model(form, cfg, mk, nodes)
+        m.load_state(snap)
+        m.timestep()
+        err = rel_errors({k: m.field(k) for k in FIELDS_ACC}, ref)
         m.close()
-    cpu = {"value": r["value"], "unit": "timesteps/s", "cores": 1, "kind": "port",
+        m, _, _, _ = make_model(form, cfg, mk, nodes)
+        for _ in range(nsteps):
+            m.timestep()
+        free = rel_errors({k: m.field(k) for k in FIELDS_ACC}, ref)
+        m.close()
+        out[label] = dict(err, **judged(err))
+        out[label]["free_running"] = free
+    cpu = {"value": nsteps / el, "unit": "timesteps/s", "cores": 1, "kind": "port",
            "sample": "first %d timesteps of %s from the initial state, %.1f s (oracle: C restatement + SciPy "
-                     "SuperLU direct solve, one thread)" % (r["steps"], cfg, r["seconds"])}
+                     "SuperLU direct solve, one thread)" % (nsteps, cfg, el)}
     return out, cpu
 
 

@@ -15,7 +15,7 @@
 
 #include "hmec_internal.cuh"
 
-int hmec_cuda_fail(hmec_ctx* ctx, cudaError_t e, const char* what) {
+int hmec_cuda_fail(hmec_inst* ctx, cudaError_t e, const char* what) {
     if (ctx) {
         char buf[512];
         snprintf(buf, sizeof(buf), "CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
@@ -24,7 +24,7 @@ int hmec_cuda_fail(hmec_ctx* ctx, cudaError_t e, const char* what) {
     return HMEC_ERR_CUDA;
 }
 
-bool hmec_prof_begin(hmec_ctx* ctx, const char* kname, double bytes, double bytes_alg) {
+bool hmec_prof_begin(hmec_inst* ctx, const char* kname, double bytes, double bytes_alg) {
     ProfState& P = ctx->prof;
     while (*kname == '(' || *kname == ' ') kname++;  // template launches are parenthesised
     if (P.name.empty() || strncmp(kname, P.name.c_str(), P.name.size()) != 0) return false;
@@ -45,9 +45,9 @@ bool hmec_prof_begin(hmec_ctx* ctx, const char* kname, double bytes, double byte
     return true;
 }
 
-void hmec_prof_end(hmec_ctx* ctx) { cudaEventRecord(ctx->prof.pending.back(), ctx->stream); }
+void hmec_prof_end(hmec_inst* ctx) { cudaEventRecord(ctx->prof.pending.back(), ctx->stream); }
 
-static void prof_drain(hmec_ctx* ctx) {
+static void prof_drain(hmec_inst* ctx) {
     ProfState& P = ctx->prof;
     if (P.pending.empty()) return;
     cudaStreamSynchronize(ctx->stream);
@@ -60,7 +60,7 @@ static void prof_drain(hmec_ctx* ctx) {
     P.pending.clear();
 }
 
-static int fail(hmec_ctx* ctx, int code, const char* msg) {
+static int fail(hmec_inst* ctx, int code, const char* msg) {
     if (ctx) ctx->err = msg;
     return code;
 }
@@ -95,7 +95,7 @@ static int status_from_bits(int bits) {
     return HMEC_OK;
 }
 
-static int pull_scalars(hmec_ctx* ctx) {
+static int pull_scalars(hmec_inst* ctx) {
     HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->hs, ctx->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream));
     HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (ctx->prof.pending.size() > 4096) prof_drain(ctx);
@@ -205,11 +205,13 @@ int64_t hmec_marknum(const hmec_params* p) {
     return (int64_t)(p->Nx - 1) * p->mx * (int64_t)(p->Ny - 1) * p->my;
 }
 
-const char* hmec_last_error(const hmec_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+}  // extern "C"
 
-int64_t hmec_kernel_launches(const hmec_ctx* ctx) { return ctx ? ctx->launches : -1; }
+static const char* inst_last_error(const hmec_inst* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
-int32_t hmec_graph_status(hmec_ctx* ctx) {
+static int64_t inst_kernel_launches(const hmec_inst* ctx) { return ctx ? ctx->launches : -1; }
+
+static int32_t inst_graph_status(hmec_inst* ctx) {
     if (!ctx) return -1;
     if (!ctx->p.graph) return -1;
     if (ctx->gr.state < 0) {
@@ -219,7 +221,7 @@ int32_t hmec_graph_status(hmec_ctx* ctx) {
     return ctx->gr.state == 1 ? 1 : 0;
 }
 
-void hmec_destroy(hmec_ctx* ctx) {
+static void inst_destroy(hmec_inst* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->dev);
     cudaStreamSynchronize(ctx->stream);
@@ -242,12 +244,18 @@ void hmec_destroy(hmec_ctx* ctx) {
     delete ctx;
 }
 
-static int create_inner(hmec_ctx* ctx) {
-    const hmec_params& p = ctx->p;
+// Parameter checks made before any device work; the reason, or NULL.
+static const char* params_problem(const hmec_params& p) {
     if (p.Nx < 5 || p.Ny < 5 || p.mx < 1 || p.my < 1 || !(p.xsize > 0) || !(p.ysize > 0))
-        return fail(ctx, HMEC_ERR_ARG, "grid parameters out of range (Nx, Ny >= 5; mx, my >= 1; sizes > 0)");
-    if (p.krylov_restart < 2 || p.krylov_restart > 200) return fail(ctx, HMEC_ERR_ARG, "krylov_restart must be in [2, 200]");
-    if (p.form != HMEC_FORM_FP64 && p.form != HMEC_FORM_MIXED) return fail(ctx, HMEC_ERR_ARG, "unknown solver form");
+        return "grid parameters out of range (Nx, Ny >= 5; mx, my >= 1; sizes > 0)";
+    if (p.krylov_restart < 2 || p.krylov_restart > 200) return "krylov_restart must be in [2, 200]";
+    if (p.form != HMEC_FORM_FP64 && p.form != HMEC_FORM_MIXED) return "unknown solver form";
+    return nullptr;
+}
+
+static int create_inner(hmec_inst* ctx) {
+    const hmec_params& p = ctx->p;
+    if (const char* why = params_problem(p)) return fail(ctx, HMEC_ERR_ARG, why);
     HMEC_CUDA(ctx, cudaGetDevice(&ctx->dev));
     HMEC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     Geo& g = ctx->g;
@@ -301,12 +309,12 @@ static int create_inner(hmec_ctx* ctx) {
     return HMEC_OK;
 }
 
-hmec_ctx* hmec_create(const hmec_params* p, int32_t* status) {
+static hmec_inst* inst_create(const hmec_params* p, int32_t* status) {
     if (!p) {
         if (status) *status = HMEC_ERR_ARG;
         return nullptr;
     }
-    hmec_ctx* ctx = new (std::nothrow) hmec_ctx();
+    hmec_inst* ctx = new (std::nothrow) hmec_inst();
     if (!ctx) {
         if (status) *status = HMEC_ERR_NOMEM;
         return nullptr;
@@ -316,9 +324,9 @@ hmec_ctx* hmec_create(const hmec_params* p, int32_t* status) {
     ctx->in_step = 0;
     int rc = create_inner(ctx);
     if (rc != HMEC_OK) {
-        fprintf(stderr, "hmec_create: %s\n", ctx->err.c_str());
+        fprintf(stderr, "inst_create: %s\n", ctx->err.c_str());
         if (status) *status = rc;
-        if (ctx->stream) hmec_destroy(ctx);
+        if (ctx->stream) inst_destroy(ctx);
         else delete ctx;
         return nullptr;
     }
@@ -326,7 +334,7 @@ hmec_ctx* hmec_create(const hmec_params* p, int32_t* status) {
     return ctx;
 }
 
-int32_t hmec_upload_markers(hmec_ctx* ctx, const double* const* fields, int64_t n) {
+static int32_t inst_upload_markers(hmec_inst* ctx, const double* const* fields, int64_t n) {
     if (!ctx || !fields) return fail(ctx, HMEC_ERR_ARG, "null argument");
     if (n != ctx->marknum) return fail(ctx, HMEC_ERR_ARG, "marker count differs from (Nx-1)*mx*(Ny-1)*my");
     for (int k = 0; k < HMEC_M_COUNT; k++)
@@ -337,7 +345,7 @@ int32_t hmec_upload_markers(hmec_ctx* ctx, const double* const* fields, int64_t 
     return HMEC_OK;
 }
 
-int32_t hmec_download_markers(hmec_ctx* ctx, double* const* fields, int64_t n) {
+static int32_t inst_download_markers(hmec_inst* ctx, double* const* fields, int64_t n) {
     if (!ctx || !fields) return fail(ctx, HMEC_ERR_ARG, "null argument");
     if (n != ctx->marknum) return fail(ctx, HMEC_ERR_ARG, "marker count differs from (Nx-1)*mx*(Ny-1)*my");
     for (int k = 0; k < HMEC_M_COUNT; k++)
@@ -347,13 +355,13 @@ int32_t hmec_download_markers(hmec_ctx* ctx, double* const* fields, int64_t n) {
     return HMEC_OK;
 }
 
-static int field_dims_ok(hmec_ctx* ctx, int32_t f, int32_t rows, int32_t cols) {
+static int field_dims_ok(hmec_inst* ctx, int32_t f, int32_t rows, int32_t cols) {
     if (f < 0 || f >= HMEC_F_COUNT) return 0;
     const int g = hmec_field_grid(f);
     return rows == ctx->g.Ny + g && cols == ctx->g.Nx + g;
 }
 
-int32_t hmec_upload_field(hmec_ctx* ctx, int32_t f, const double* a, int32_t rows, int32_t cols) {
+static int32_t inst_upload_field(hmec_inst* ctx, int32_t f, const double* a, int32_t rows, int32_t cols) {
     if (!ctx || !a) return fail(ctx, HMEC_ERR_ARG, "null argument");
     if (!field_dims_ok(ctx, f, rows, cols)) return fail(ctx, HMEC_ERR_ARG, "unknown field or wrong dimensions");
     HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->f[f], a, sizeof(double) * (size_t)rows * cols, cudaMemcpyHostToDevice, ctx->stream));
@@ -361,7 +369,7 @@ int32_t hmec_upload_field(hmec_ctx* ctx, int32_t f, const double* a, int32_t row
     return HMEC_OK;
 }
 
-int32_t hmec_download_field(hmec_ctx* ctx, int32_t f, double* a, int32_t rows, int32_t cols) {
+static int32_t inst_download_field(hmec_inst* ctx, int32_t f, double* a, int32_t rows, int32_t cols) {
     if (!ctx || !a) return fail(ctx, HMEC_ERR_ARG, "null argument");
     if (!field_dims_ok(ctx, f, rows, cols)) return fail(ctx, HMEC_ERR_ARG, "unknown field or wrong dimensions");
     HMEC_CUDA(ctx, cudaMemcpyAsync(a, ctx->f[f], sizeof(double) * (size_t)rows * cols, cudaMemcpyDeviceToHost, ctx->stream));
@@ -369,7 +377,7 @@ int32_t hmec_download_field(hmec_ctx* ctx, int32_t f, double* a, int32_t rows, i
     return HMEC_OK;
 }
 
-int32_t hmec_download_rows(hmec_ctx* ctx, int32_t row, int32_t nf, const int32_t* fields, double* out) {
+static int32_t inst_download_rows(hmec_inst* ctx, int32_t row, int32_t nf, const int32_t* fields, double* out) {
     if (!ctx || !fields || !out) return fail(ctx, HMEC_ERR_ARG, "null argument");
     if (nf < 1 || nf > 64) return fail(ctx, HMEC_ERR_ARG, "nfields must be in [1, 64]");
     RowGather g;
@@ -394,7 +402,7 @@ int32_t hmec_download_rows(hmec_ctx* ctx, int32_t row, int32_t nf, const int32_t
 }
 
 // Scalars: the host mirror is refreshed from the device, edited, pushed back.
-int32_t hmec_set_scalar(hmec_ctx* ctx, int32_t id, double v) {
+static int32_t inst_set_scalar(hmec_inst* ctx, int32_t id, double v) {
     if (!ctx) return HMEC_ERR_ARG;
     if (id < 0 || id >= HMEC_S_COUNT) return fail(ctx, HMEC_ERR_ARG, "unknown scalar id");
     int rc = pull_scalars(ctx);
@@ -423,7 +431,7 @@ int32_t hmec_set_scalar(hmec_ctx* ctx, int32_t id, double v) {
     return HMEC_OK;
 }
 
-int32_t hmec_get_scalar(hmec_ctx* ctx, int32_t id, double* v) {
+static int32_t inst_get_scalar(hmec_inst* ctx, int32_t id, double* v) {
     if (!ctx || !v) return fail(ctx, HMEC_ERR_ARG, "null argument");
     if (id < 0 || id >= HMEC_S_COUNT) return fail(ctx, HMEC_ERR_ARG, "unknown scalar id");
     int rc = pull_scalars(ctx);
@@ -450,9 +458,9 @@ int32_t hmec_get_scalar(hmec_ctx* ctx, int32_t id, double* v) {
     return HMEC_OK;
 }
 
-void* hmec_stream(hmec_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+static void* inst_stream(hmec_inst* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
-int32_t hmec_profile_kernel(hmec_ctx* ctx, const char* name) {
+static int32_t inst_profile_kernel(hmec_inst* ctx, const char* name) {
     if (!ctx) return HMEC_ERR_ARG;
     prof_drain(ctx);
     ctx->prof.name = name ? name : "";
@@ -463,7 +471,7 @@ int32_t hmec_profile_kernel(hmec_ctx* ctx, const char* name) {
     return HMEC_OK;
 }
 
-int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, double* bytes_compulsory,
+static int32_t inst_profile_read(hmec_inst* ctx, int64_t* launches, double* total_ms, double* bytes_compulsory,
                           double* bytes_moved) {
     if (!ctx) return HMEC_ERR_ARG;
     prof_drain(ctx);
@@ -474,13 +482,13 @@ int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, do
     return HMEC_OK;
 }
 
-int32_t hmec_synchronize(hmec_ctx* ctx) {
+static int32_t inst_synchronize(hmec_inst* ctx) {
     if (!ctx) return HMEC_ERR_ARG;
     HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return HMEC_OK;
 }
 
-int32_t hmec_markers_to_nodes(hmec_ctx* ctx) {
+static int32_t inst_markers_to_nodes(hmec_inst* ctx) {
     if (!ctx) return HMEC_ERR_ARG;
     // a new timestep starts here: clear the device status word of the last one
     HMEC_CUDA(ctx, cudaMemsetAsync(&ctx->ds->status, 0, sizeof(int), ctx->stream));
@@ -489,7 +497,7 @@ int32_t hmec_markers_to_nodes(hmec_ctx* ctx) {
     return HMEC_OK;
 }
 
-int32_t hmec_timestep_begin(hmec_ctx* ctx) {
+static int32_t inst_timestep_begin(hmec_inst* ctx) {
     if (!ctx) return HMEC_ERR_ARG;
     int rc = step_begin(ctx);
     if (rc) return rc;
@@ -497,7 +505,7 @@ int32_t hmec_timestep_begin(hmec_ctx* ctx) {
     return HMEC_OK;
 }
 
-static int iteration(hmec_ctx* ctx, hmec_iter_report* rep, int* krylov_rc) {
+static int iteration(hmec_inst* ctx, hmec_iter_report* rep, int* krylov_rc) {
     int rc = iter_prepare(ctx);
     if (rc) return rc;
     rc = iter_assemble(ctx);
@@ -528,9 +536,9 @@ static int iteration(hmec_ctx* ctx, hmec_iter_report* rep, int* krylov_rc) {
     return HMEC_OK;
 }
 
-int32_t hmec_global_iteration(hmec_ctx* ctx, hmec_iter_report* rep) {
+static int32_t inst_global_iteration(hmec_inst* ctx, hmec_iter_report* rep) {
     if (!ctx) return HMEC_ERR_ARG;
-    if (!ctx->in_step) return fail(ctx, HMEC_ERR_STATE, "hmec_global_iteration before hmec_timestep_begin");
+    if (!ctx->in_step) return fail(ctx, HMEC_ERR_STATE, "inst_global_iteration before inst_timestep_begin");
     int krc = HMEC_OK;
     int rc = iteration(ctx, rep, &krc);
     if (rc) return rc;
@@ -540,7 +548,7 @@ int32_t hmec_global_iteration(hmec_ctx* ctx, hmec_iter_report* rep) {
     return HMEC_OK;
 }
 
-int32_t hmec_timestep_end(hmec_ctx* ctx) {
+static int32_t inst_timestep_end(hmec_inst* ctx) {
     if (!ctx) return HMEC_ERR_ARG;
     int rc = step_end(ctx);
     if (rc) return rc;
@@ -550,20 +558,20 @@ int32_t hmec_timestep_end(hmec_ctx* ctx) {
     return HMEC_OK;
 }
 
-int32_t hmec_advect_markers(hmec_ctx* ctx) {
+static int32_t inst_advect_markers(hmec_inst* ctx) {
     if (!ctx) return HMEC_ERR_ARG;
     return advect_run(ctx);
 }
 
-int32_t hmec_timestep(hmec_ctx* ctx, hmec_step_report* rep) {
+static int32_t inst_timestep(hmec_inst* ctx, hmec_step_report* rep) {
     if (!ctx) return HMEC_ERR_ARG;
     bool by_graph = false;
     int rc = graph_timestep(ctx, rep, &by_graph);
     if (by_graph) return rc;
     if (rc) return rc;
-    rc = hmec_markers_to_nodes(ctx);
+    rc = inst_markers_to_nodes(ctx);
     if (rc) return rc;
-    rc = hmec_timestep_begin(ctx);
+    rc = inst_timestep_begin(ctx);
     if (rc) return rc;
     int first_bad = HMEC_OK;
     int ktot = 0;
@@ -585,7 +593,7 @@ int32_t hmec_timestep(hmec_ctx* ctx, hmec_step_report* rep) {
     const int iters = ctx->hs->iters_in_step;
     const int ynlast = ctx->hs->ynlast;
     const int timestep = ctx->hs->timestep;
-    rc = hmec_timestep_end(ctx);
+    rc = inst_timestep_end(ctx);
     if (rc) return rc;
     if (ctx->p.advect_markers) {
         rc = advect_run(ctx);
@@ -611,7 +619,7 @@ int32_t hmec_timestep(hmec_ctx* ctx, hmec_step_report* rep) {
     return HMEC_OK;
 }
 
-int32_t hmec_assemble_csr(hmec_ctx* ctx, int64_t* indptr, int32_t* indices, double* data, double* rhs, int64_t* nnz,
+static int32_t inst_assemble_csr(hmec_inst* ctx, int64_t* indptr, int32_t* indices, double* data, double* rhs, int64_t* nnz,
                           double* ptscale, double* pfscale) {
     if (!ctx || !nnz) return fail(ctx, HMEC_ERR_ARG, "null argument");
     int rc = iter_prepare(ctx);
@@ -650,7 +658,7 @@ int32_t hmec_assemble_csr(hmec_ctx* ctx, int64_t* indptr, int32_t* indices, doub
     return HMEC_OK;
 }
 
-int32_t hmec_solve_system(hmec_ctx* ctx, const double* rhs, double* x, int32_t* iters, double* relres) {
+static int32_t inst_solve_system(hmec_inst* ctx, const double* rhs, double* x, int32_t* iters, double* relres) {
     if (!ctx || !rhs || !x) return fail(ctx, HMEC_ERR_ARG, "null argument");
     const size_t N = (size_t)ctx->g.N;
     Level& L = ctx->sv.lv[0];
@@ -669,6 +677,214 @@ int32_t hmec_solve_system(hmec_ctx* ctx, const double* rhs, double* x, int32_t* 
     if (relres) *relres = rel;
     if (krc) return fail(ctx, krc, "FGMRES did not reach krylov_rtol within krylov_maxit");
     return HMEC_OK;
+}
+
+
+
+// ===================================================================== ABI
+// The context holds n instances; every data and section entry point names
+// the instance it acts on.  A failure's message is kept on the instance and
+// copied to the context, where hmec_last_error() reads it.
+
+static hmec_inst* inst_of(hmec_ctx* E, int32_t i) {
+    if (!E) return nullptr;
+    if (i < 0 || i >= (int32_t)E->inst.size()) {
+        E->err = "instance index out of range";
+        return nullptr;
+    }
+    return E->inst[i];
+}
+
+static int32_t relay(hmec_ctx* E, hmec_inst* m, int32_t rc) {
+    if (rc != HMEC_OK) E->err = m->err;
+    return rc;
+}
+
+#define HMEC_INST(E, i)                                   \
+    hmec_inst* m_ = inst_of((E), (i));                    \
+    if (!m_) return HMEC_ERR_ARG
+
+extern "C" {
+
+hmec_ctx* hmec_create(const hmec_params* p, int32_t n_instances, const hmec_grid* grids, int32_t* status) {
+    if (!p || n_instances < 1) {
+        if (status) *status = HMEC_ERR_ARG;
+        return nullptr;
+    }
+    hmec_ctx* E = new (std::nothrow) hmec_ctx();
+    if (!E) {
+        if (status) *status = HMEC_ERR_NOMEM;
+        return nullptr;
+    }
+    std::vector<hmec_params> qs(n_instances, *p);
+    for (int32_t k = 0; k < n_instances; k++) {
+        hmec_params& q = qs[k];
+        if (grids) {
+            q.Nx = grids[k].Nx;
+            q.Ny = grids[k].Ny;
+            q.xsize = grids[k].xsize;
+            q.ysize = grids[k].ysize;
+            q.mx = grids[k].mx;
+            q.my = grids[k].my;
+        }
+        // members of an ensemble share the GPU: one launch per smoothing
+        // pass on a share of the SMs (HMEC_MG_PASS_LAUNCHES)
+        if (n_instances > 1) q.mg_flags |= HMEC_MG_PASS_LAUNCHES;
+        if (const char* why = params_problem(q)) {
+            fprintf(stderr, "hmec_create: instance %d: %s\n", (int)k, why);
+            delete E;
+            if (status) *status = HMEC_ERR_ARG;
+            return nullptr;
+        }
+    }
+    cudaGetDevice(&E->dev);
+    for (int32_t k = 0; k < n_instances; k++) {
+        int32_t st = HMEC_OK;
+        hmec_inst* m = inst_create(&qs[k], &st);
+        if (!m) {
+            for (hmec_inst* x : E->inst) inst_destroy(x);
+            delete E;
+            if (status) *status = st;
+            return nullptr;
+        }
+        E->inst.push_back(m);
+    }
+    if (status) *status = HMEC_OK;
+    return E;
+}
+
+void hmec_destroy(hmec_ctx* E) {
+    if (!E) return;
+    cudaSetDevice(E->dev);
+    if (E->origin) cudaStreamSynchronize(E->origin);
+    ensemble_graph_free(E);
+    for (hmec_inst* m : E->inst) inst_destroy(m);
+    delete E;
+}
+
+int32_t hmec_instances(const hmec_ctx* E) { return E ? (int32_t)E->inst.size() : 0; }
+
+const char* hmec_last_error(const hmec_ctx* E) { return E ? E->err.c_str() : "null context"; }
+
+int64_t hmec_kernel_launches(const hmec_ctx* E) {
+    if (!E) return -1;
+    int64_t t = 0;
+    for (hmec_inst* m : E->inst) t += inst_kernel_launches(m);
+    return t;
+}
+
+int32_t hmec_graph_status(hmec_ctx* E) {
+    if (!E) return -1;
+    if (E->inst.size() > 1) {
+        if (E->gstate < 0) {
+            E->err = E->why.empty() ? "ensemble graph capture failed" : E->why;
+            return -1;
+        }
+        if (!E->inst[0]->p.graph) return -1;
+        return E->gstate == 1 ? 1 : 0;
+    }
+    const int32_t r = inst_graph_status(E->inst[0]);
+    if (r < 0) E->err = E->inst[0]->err;
+    return r;
+}
+
+int32_t hmec_upload_markers(hmec_ctx* E, int32_t i, const double* const* fields, int64_t n) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_upload_markers(m_, fields, n));
+}
+int32_t hmec_download_markers(hmec_ctx* E, int32_t i, double* const* fields, int64_t n) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_download_markers(m_, fields, n));
+}
+int32_t hmec_upload_field(hmec_ctx* E, int32_t i, int32_t f, const double* a, int32_t rows, int32_t cols) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_upload_field(m_, f, a, rows, cols));
+}
+int32_t hmec_download_field(hmec_ctx* E, int32_t i, int32_t f, double* a, int32_t rows, int32_t cols) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_download_field(m_, f, a, rows, cols));
+}
+int32_t hmec_download_rows(hmec_ctx* E, int32_t i, int32_t row, int32_t nf, const int32_t* fields, double* out) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_download_rows(m_, row, nf, fields, out));
+}
+int32_t hmec_set_scalar(hmec_ctx* E, int32_t i, int32_t id, double v) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_set_scalar(m_, id, v));
+}
+int32_t hmec_get_scalar(hmec_ctx* E, int32_t i, int32_t id, double* v) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_get_scalar(m_, id, v));
+}
+void* hmec_stream(hmec_ctx* E, int32_t i) {
+    hmec_inst* m = inst_of(E, i);
+    return m ? inst_stream(m) : nullptr;
+}
+int32_t hmec_profile_kernel(hmec_ctx* E, int32_t i, const char* name) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_profile_kernel(m_, name));
+}
+int32_t hmec_profile_read(hmec_ctx* E, int32_t i, int64_t* launches, double* total_ms, double* bytes_compulsory,
+                          double* bytes_moved) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_profile_read(m_, launches, total_ms, bytes_compulsory, bytes_moved));
+}
+int32_t hmec_synchronize(hmec_ctx* E) {
+    if (!E) return HMEC_ERR_ARG;
+    if (E->origin) cudaStreamSynchronize(E->origin);
+    for (hmec_inst* m : E->inst) {
+        const int32_t rc = inst_synchronize(m);
+        if (rc) return relay(E, m, rc);
+    }
+    return HMEC_OK;
+}
+int32_t hmec_markers_to_nodes(hmec_ctx* E, int32_t i) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_markers_to_nodes(m_));
+}
+int32_t hmec_timestep_begin(hmec_ctx* E, int32_t i) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_timestep_begin(m_));
+}
+int32_t hmec_global_iteration(hmec_ctx* E, int32_t i, hmec_iter_report* rep) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_global_iteration(m_, rep));
+}
+int32_t hmec_timestep_end(hmec_ctx* E, int32_t i) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_timestep_end(m_));
+}
+int32_t hmec_advect_markers(hmec_ctx* E, int32_t i) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_advect_markers(m_));
+}
+
+int32_t hmec_timestep(hmec_ctx* E, hmec_step_report* reports) {
+    if (!E) return HMEC_ERR_ARG;
+    if (E->inst.size() == 1) return relay(E, E->inst[0], inst_timestep(E->inst[0], reports));
+    bool used = false;
+    const int32_t rc = ensemble_graph_step(E, reports, &used);
+    if (used) return rc;
+    // members one by one (the first step of each, or graphs off)
+    int32_t first_bad = HMEC_OK;
+    for (size_t k = 0; k < E->inst.size(); k++) {
+        const int32_t r = inst_timestep(E->inst[k], reports ? &reports[k] : nullptr);
+        if (r && !first_bad) {
+            first_bad = r;
+            E->err = E->inst[k]->err;
+        }
+    }
+    return first_bad;
+}
+
+int32_t hmec_assemble_csr(hmec_ctx* E, int32_t i, int64_t* indptr, int32_t* indices, double* data, double* rhs,
+                          int64_t* nnz, double* ptscale, double* pfscale) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_assemble_csr(m_, indptr, indices, data, rhs, nnz, ptscale, pfscale));
+}
+int32_t hmec_solve_system(hmec_ctx* E, int32_t i, const double* rhs, double* x, int32_t* iters, double* relres) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_solve_system(m_, rhs, x, iters, relres));
 }
 
 }  // extern "C"

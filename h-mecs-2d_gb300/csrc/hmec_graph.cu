@@ -52,7 +52,7 @@ int status_from_device_bits(int bits) {
 
 // Ends every capture still open on the context's streams (after a failure
 // in the middle of a capture) and clears the sticky capture error.
-void abandon_capture(hmec_ctx* ctx, cudaStream_t main) {
+void abandon_capture(hmec_inst* ctx, cudaStream_t main) {
     cudaStream_t ss[4] = {main, ctx->gr.body[0], ctx->gr.body[1], ctx->gr.body[2]};
     for (cudaStream_t s : ss) {
         if (!s) continue;
@@ -73,14 +73,16 @@ void abandon_capture(hmec_ctx* ctx, cudaStream_t main) {
     cudaGetLastError();
 }
 
-int build(hmec_ctx* ctx) {
+// Launches one instance's timestep into the capture its stream belongs to,
+// ending with the copy of its device scalars to the pinned host mirror;
+// records the launch counts of the parts in ctx->gr.
+int capture_step(hmec_inst* ctx) {
     GraphState& gs = ctx->gr;
     for (int k = 0; k < 3; k++)
         if (!gs.body[k]) HMEC_CUDA(ctx, cudaStreamCreateWithFlags(&gs.body[k], cudaStreamNonBlocking));
     if (!gs.ctl) HMEC_CUDA(ctx, cudaMalloc(&gs.ctl, sizeof(GraphCtl)));
     const int64_t l_start = ctx->launches;
     cudaStream_t main = ctx->stream;
-    HMEC_CUDA(ctx, cudaStreamBeginCapture(main, cudaStreamCaptureModeRelaxed));
     int rc = HMEC_OK;
     int64_t n_restart = 0, n_inner = 0, n_global = 0;
     do {
@@ -108,29 +110,40 @@ int build(hmec_ctx* ctx) {
         // a16-a19 (and a18/a20 when advection is on)
         if ((rc = step_end(ctx))) break;
         if (ctx->p.advect_markers && (rc = advect_run(ctx))) break;
+        if (cudaMemcpyAsync(ctx->hs, ctx->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, main) != cudaSuccess) {
+            rc = HMEC_ERR_CUDA;
+            break;
+        }
     } while (0);
     if (rc == HMEC_OK && cudaGetLastError() != cudaSuccess) rc = HMEC_ERR_CUDA;
+    ctx->stream = main;
+    gs.n_global = n_global;
+    gs.n_restart = n_restart;
+    gs.n_inner = n_inner;
+    gs.n_top = ctx->launches - l_start - n_global - n_restart - n_inner;
+    ctx->launches = l_start;  // the captured launches run when the graph does
+    return rc;
+}
+
+int build(hmec_inst* ctx) {
+    GraphState& gs = ctx->gr;
+    cudaStream_t main = ctx->stream;
+    HMEC_CUDA(ctx, cudaStreamBeginCapture(main, cudaStreamCaptureModeRelaxed));
+    const int rc = capture_step(ctx);
     if (rc != HMEC_OK) {
         abandon_capture(ctx, main);
-        ctx->stream = main;
-        ctx->launches = l_start;
         return rc;
     }
     cudaGraph_t g = nullptr;
     HMEC_CUDA(ctx, cudaStreamEndCapture(main, &g));
     gs.graph = g;
     HMEC_CUDA(ctx, cudaGraphInstantiate(&gs.exec, g, 0));
-    gs.n_global = n_global;
-    gs.n_restart = n_restart;
-    gs.n_inner = n_inner;
-    gs.n_top = ctx->launches - l_start - n_global - n_restart - n_inner;
-    ctx->launches = l_start;  // the captured launches run when the graph does
     return HMEC_OK;
 }
 
 }  // namespace
 
-int graph_handle(hmec_ctx* ctx, cudaStream_t s, cudaGraphConditionalHandle* h) {
+int graph_handle(hmec_inst* ctx, cudaStream_t s, cudaGraphConditionalHandle* h) {
     cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
     cudaGraph_t g = nullptr;
     HMEC_CUDA(ctx, cudaStreamGetCaptureInfo(s, &st, nullptr, &g, nullptr, nullptr, nullptr));
@@ -142,7 +155,7 @@ int graph_handle(hmec_ctx* ctx, cudaStream_t s, cudaGraphConditionalHandle* h) {
     return HMEC_OK;
 }
 
-int graph_while_begin(hmec_ctx* ctx, cudaStream_t s, cudaGraphConditionalHandle h, cudaStream_t bs) {
+int graph_while_begin(hmec_inst* ctx, cudaStream_t s, cudaGraphConditionalHandle h, cudaStream_t bs) {
     cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
     cudaGraph_t g = nullptr;
     const cudaGraphNode_t* deps = nullptr;
@@ -165,13 +178,13 @@ int graph_while_begin(hmec_ctx* ctx, cudaStream_t s, cudaGraphConditionalHandle 
     return HMEC_OK;
 }
 
-int graph_while_end(hmec_ctx* ctx, cudaStream_t bs) {
+int graph_while_end(hmec_inst* ctx, cudaStream_t bs) {
     cudaGraph_t g = nullptr;
     HMEC_CUDA(ctx, cudaStreamEndCapture(bs, &g));
     return HMEC_OK;
 }
 
-int graph_timestep(hmec_ctx* ctx, hmec_step_report* rep, bool* used) {
+int graph_timestep(hmec_inst* ctx, hmec_step_report* rep, bool* used) {
     GraphState& gs = ctx->gr;
     *used = false;
     // host-driven: graphs off, a kernel being timed launch by launch, or the
@@ -189,8 +202,14 @@ int graph_timestep(hmec_ctx* ctx, hmec_step_report* rep, bool* used) {
         gs.state = 1;
     }
     HMEC_CUDA(ctx, cudaGraphLaunch(gs.exec, ctx->stream));
-    HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->hs, ctx->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream));
     HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *used = true;
+    return graph_report(ctx, rep);
+}
+
+// The graph copied the device scalars into hs at its end.
+int graph_report(hmec_inst* ctx, hmec_step_report* rep) {
+    const GraphState& gs = ctx->gr;
     const DevScalars& s = *ctx->hs;
     ctx->launches += gs.n_top + (int64_t)s.iters_in_step * gs.n_global + (int64_t)s.krylov_cycles * gs.n_restart +
                      (int64_t)s.krylov_total * gs.n_inner;
@@ -207,7 +226,6 @@ int graph_timestep(hmec_ctx* ctx, hmec_step_report* rep, bool* used) {
         rep->Vmax = s.Vmax;
         rep->max_krylov_relres = s.krylov_maxrel;
     }
-    *used = true;
     if (st != HMEC_OK) {
         ctx->err = "timestep finished with a non-OK status (see report)";
         return st;
@@ -215,7 +233,91 @@ int graph_timestep(hmec_ctx* ctx, hmec_step_report* rep, bool* used) {
     return HMEC_OK;
 }
 
-void graph_free(hmec_ctx* ctx) {
+// ------------------------------------------------------------ ensembles
+// Every member's step captured side by side: the members' streams fork from
+// the context's origin stream and join it again, so the graph holds n
+// independent branches, each with its own three conditional loops.
+int ensemble_graph_step(hmec_ctx* E, hmec_step_report* reps, bool* used) {
+    *used = false;
+    const size_t n = E->inst.size();
+    if (E->gstate < 0 || n < 2) return HMEC_OK;
+    for (hmec_inst* m : E->inst)
+        if (!m->p.graph || !m->gr.warm || !m->prof.name.empty() || m->gr.state < 0) return HMEC_OK;
+    if (E->gstate == 0) {
+        hmec_inst* m0 = E->inst[0];
+        auto off = [&](const std::string& why) {
+            E->gstate = -1;
+            E->why = why;
+            return HMEC_OK;
+        };
+        if (!E->origin && cudaStreamCreateWithFlags(&E->origin, cudaStreamNonBlocking) != cudaSuccess)
+            return off("cannot create the ensemble stream");
+        if (!E->ev_fork && cudaEventCreateWithFlags(&E->ev_fork, cudaEventDisableTiming) != cudaSuccess)
+            return off("cannot create the ensemble events");
+        while (E->ev_join.size() < n) {
+            cudaEvent_t e = nullptr;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return off("cannot create events");
+            E->ev_join.push_back(e);
+        }
+        if (cudaStreamBeginCapture(E->origin, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+            return off("cannot capture the ensemble step");
+        int rc = cudaEventRecord(E->ev_fork, E->origin) == cudaSuccess ? HMEC_OK : HMEC_ERR_CUDA;
+        for (size_t k = 0; k < n && rc == HMEC_OK; k++) {
+            hmec_inst* m = E->inst[k];
+            if (cudaStreamWaitEvent(m->stream, E->ev_fork, 0) != cudaSuccess) rc = HMEC_ERR_CUDA;
+            if (rc == HMEC_OK) rc = capture_step(m);
+            if (rc == HMEC_OK && (cudaEventRecord(E->ev_join[k], m->stream) != cudaSuccess ||
+                                  cudaStreamWaitEvent(E->origin, E->ev_join[k], 0) != cudaSuccess))
+                rc = HMEC_ERR_CUDA;
+            if (rc != HMEC_OK && E->why.empty()) E->why = m->err;
+        }
+        cudaGraph_t g = nullptr;
+        if (rc == HMEC_OK && cudaStreamEndCapture(E->origin, &g) != cudaSuccess) rc = HMEC_ERR_CUDA;
+        if (rc == HMEC_OK && cudaGraphInstantiate(&E->exec, g, 0) != cudaSuccess) rc = HMEC_ERR_CUDA;
+        if (rc != HMEC_OK) {
+            for (hmec_inst* m : E->inst) abandon_capture(m, m->stream);
+            cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+            if (cudaStreamIsCapturing(E->origin, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+                cudaGraph_t g2 = nullptr;
+                cudaStreamEndCapture(E->origin, &g2);
+                if (g2) cudaGraphDestroy(g2);
+            }
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            (void)m0;
+            return off(E->why.empty() ? "ensemble capture failed" : E->why);
+        }
+        E->graph = g;
+        E->gstate = 1;
+    }
+    if (cudaGraphLaunch(E->exec, E->origin) != cudaSuccess || cudaStreamSynchronize(E->origin) != cudaSuccess) {
+        E->err = "ensemble graph launch failed";
+        return HMEC_ERR_CUDA;
+    }
+    *used = true;
+    int first_bad = HMEC_OK;
+    for (size_t k = 0; k < n; k++) {
+        const int rc = graph_report(E->inst[k], reps ? &reps[k] : nullptr);
+        if (rc && !first_bad) first_bad = rc;
+    }
+    if (first_bad) E->err = "a member's timestep finished with a non-OK status (see its report)";
+    return first_bad;
+}
+
+void ensemble_graph_free(hmec_ctx* E) {
+    if (E->exec) cudaGraphExecDestroy(E->exec);
+    if (E->graph) cudaGraphDestroy(E->graph);
+    if (E->ev_fork) cudaEventDestroy(E->ev_fork);
+    for (cudaEvent_t e : E->ev_join) cudaEventDestroy(e);
+    if (E->origin) cudaStreamDestroy(E->origin);
+    E->exec = nullptr;
+    E->graph = nullptr;
+    E->ev_fork = nullptr;
+    E->ev_join.clear();
+    E->origin = nullptr;
+}
+
+void graph_free(hmec_inst* ctx) {
     GraphState& gs = ctx->gr;
     if (gs.exec) cudaGraphExecDestroy(gs.exec);
     if (gs.graph) cudaGraphDestroy(gs.graph);

@@ -213,7 +213,7 @@ struct GraphState {
     std::string why;  // why the graph is off
 };
 
-struct hmec_ctx {
+struct hmec_inst {
     hmec_params p;
     int dev;
     cudaStream_t stream;
@@ -247,6 +247,24 @@ struct hmec_ctx {
     std::string err;
     GraphState gr;
     double* rowbuf = nullptr;  // hmec_download_rows staging (64 rows of Nx+1)
+};
+
+// The ABI's context: n model instances -- one for a single model, the
+// members of an ensemble otherwise -- each with its own grid, buffers and
+// stream on the device current at hmec_create.  An ensemble step is one CUDA
+// graph launch: every member's timestep (hmec_graph.cu) captured side by side
+// into one graph, each with its own loops, dt and convergence decisions.
+struct hmec_ctx {
+    std::vector<hmec_inst*> inst;
+    int dev = 0;
+    std::string err;
+    int gstate = 0;  // ensemble graph: 0 not built, 1 ready, -1 off (member graphs or host-driven steps)
+    cudaStream_t origin = nullptr;
+    cudaEvent_t ev_fork = nullptr;
+    std::vector<cudaEvent_t> ev_join;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::string why;
 };
 
 // ------------------------------------------------------------------ helpers
@@ -367,15 +385,15 @@ __device__ __forceinline__ bool arrive_last(unsigned* ticket) {
         (ctx)->launches++;                                                        \
     } while (0)
 
-int hmec_cuda_fail(hmec_ctx* ctx, cudaError_t e, const char* what);
-bool hmec_prof_begin(hmec_ctx* ctx, const char* kname, double bytes, double bytes_alg);
-void hmec_prof_end(hmec_ctx* ctx);
+int hmec_cuda_fail(hmec_inst* ctx, cudaError_t e, const char* what);
+bool hmec_prof_begin(hmec_inst* ctx, const char* kname, double bytes, double bytes_alg);
+void hmec_prof_end(hmec_inst* ctx);
 
 // The library's launch helpers use ctx->stream; inside a scope they go to s.
 struct StreamScope {
-    hmec_ctx* ctx;
+    hmec_inst* ctx;
     cudaStream_t saved;
-    StreamScope(hmec_ctx* c, cudaStream_t s) : ctx(c), saved(c->stream) { c->stream = s; }
+    StreamScope(hmec_inst* c, cudaStream_t s) : ctx(c), saved(c->stream) { c->stream = s; }
     ~StreamScope() { ctx->stream = saved; }
 };
 
@@ -395,34 +413,41 @@ struct StreamScope {
     } while (0)
 
 // Sections (implemented in the k_*.cu units); all return an hmec status.
-int p2g_alloc(hmec_ctx* ctx);
-void p2g_free(hmec_ctx* ctx);
-int p2g_run(hmec_ctx* ctx);
-int iter_prepare(hmec_ctx* ctx);
-int iter_assemble(hmec_ctx* ctx);
-int iter_finish(hmec_ctx* ctx);
-int step_begin(hmec_ctx* ctx);
-int step_end(hmec_ctx* ctx);
-int advect_run(hmec_ctx* ctx);
-int solver_alloc(hmec_ctx* ctx);
-void solver_free(hmec_ctx* ctx);
-int solver_setup(hmec_ctx* ctx);            // build coarse levels + Vanka inverses for the current matrix
-int solver_solve(hmec_ctx* ctx, int* iters, double* relres);  // solve A S = R in place (S = guess)
+int p2g_alloc(hmec_inst* ctx);
+void p2g_free(hmec_inst* ctx);
+int p2g_run(hmec_inst* ctx);
+int iter_prepare(hmec_inst* ctx);
+int iter_assemble(hmec_inst* ctx);
+int iter_finish(hmec_inst* ctx);
+int step_begin(hmec_inst* ctx);
+int step_end(hmec_inst* ctx);
+int advect_run(hmec_inst* ctx);
+int solver_alloc(hmec_inst* ctx);
+void solver_free(hmec_inst* ctx);
+int solver_setup(hmec_inst* ctx);            // build coarse levels + Vanka inverses for the current matrix
+int solver_solve(hmec_inst* ctx, int* iters, double* relres);  // solve A S = R in place (S = guess)
 // Graph capture helpers (hmec_graph.cu): a conditional handle of the graph
 // being captured on s; a WHILE node on handle h appended to that capture,
 // whose body is captured on stream bs until graph_while_end(bs).
-int graph_handle(hmec_ctx* ctx, cudaStream_t s, cudaGraphConditionalHandle* h);
-int graph_while_begin(hmec_ctx* ctx, cudaStream_t s, cudaGraphConditionalHandle h, cudaStream_t bs);
-int graph_while_end(hmec_ctx* ctx, cudaStream_t bs);
+int graph_handle(hmec_inst* ctx, cudaStream_t s, cudaGraphConditionalHandle* h);
+int graph_while_begin(hmec_inst* ctx, cudaStream_t s, cudaGraphConditionalHandle h, cudaStream_t bs);
+int graph_while_end(hmec_inst* ctx, cudaStream_t bs);
 // The solve with its decisions on the device, captured on ctx->stream (its
 // restart loop's body on s_restart, the Arnoldi loop's on s_inner);
 // *n_restart / *n_inner: kernel launches per trip of each loop.
-int solver_capture_solve(hmec_ctx* ctx, cudaStream_t s_restart, cudaStream_t s_inner, int64_t* n_restart,
+int solver_capture_solve(hmec_inst* ctx, cudaStream_t s_restart, cudaStream_t s_inner, int64_t* n_restart,
                          int64_t* n_inner);
 // One timestep as a graph launch (built on first use); *used is false when
 // the graph is off for this context and the caller runs the host-driven step.
-int graph_timestep(hmec_ctx* ctx, hmec_step_report* rep, bool* used);
-void graph_free(hmec_ctx* ctx);
+int graph_timestep(hmec_inst* ctx, hmec_step_report* rep, bool* used);
+void graph_free(hmec_inst* ctx);
+// One timestep of every member of an ensemble as one graph launch (built on
+// first use, once every member has run a host-driven step); *used false:
+// the caller steps the members one by one.
+int ensemble_graph_step(hmec_ctx* E, hmec_step_report* reps, bool* used);
+void ensemble_graph_free(hmec_ctx* E);
+// The report of a member's graph step from its device scalars (hs).
+int graph_report(hmec_inst* ctx, hmec_step_report* rep);
 // Assembly of one level into (col, val, dscale, rhs); rhs may be null.
-void launch_assemble(hmec_ctx* ctx, const Geo& g, const AsmFields& af, int32_t* col, double* val, double* dscale,
+void launch_assemble(hmec_inst* ctx, const Geo& g, const AsmFields& af, int32_t* col, double* val, double* dscale,
                      double* rhs_scaled, double* rhs_raw, const double* sc_dev);

@@ -67,7 +67,7 @@ __global__ void k_advect(Geo g, const DevScalars* ds, hmec_params p, AdvIn in, i
 
 }  // namespace
 
-int advect_run(hmec_ctx* ctx) {
+int advect_run(hmec_inst* ctx) {
     const Geo& g = ctx->g;
     double* const* f = ctx->f;
     AdvIn in{f[HMEC_F_vxs], f[HMEC_F_vys], f[HMEC_F_ESP], ctx->crd[0], ctx->crd[1], ctx->crd[2], ctx->crd[3],

@@ -1073,7 +1073,7 @@ __global__ void k_next_step(DevScalars* ds) { ds->timestep += 1; }
 static inline dim3 grid_b(const Geo& g) { return dim3(nblocks(g.Ny, 64), g.Nx); }
 static inline dim3 grid_s(const Geo& g) { return dim3(nblocks(g.Ny1, 64), g.Nx1); }
 
-int step_begin(hmec_ctx* ctx) {
+int step_begin(hmec_inst* ctx) {
     const Geo& g = ctx->g;
     double* const* f = ctx->f;
     HMEC_LAUNCH(ctx, k_step_begin, grid_b(g), 64, 0, g, ctx->ds, ctx->p, f[HMEC_F_ETA0], f[HMEC_F_ETA00],
@@ -1082,7 +1082,7 @@ int step_begin(hmec_ctx* ctx) {
     return HMEC_OK;
 }
 
-int iter_prepare(hmec_ctx* ctx) {
+int iter_prepare(hmec_inst* ctx) {
     const Geo& g = ctx->g;
     double* const* f = ctx->f;
     HMEC_LAUNCH(ctx, k_copy_bounds, grid_s(g), 64, 0, g, f[HMEC_F_pt], f[HMEC_F_pf]);
@@ -1098,20 +1098,20 @@ int iter_prepare(hmec_ctx* ctx) {
     return HMEC_OK;
 }
 
-void launch_assemble(hmec_ctx* ctx, const Geo& g, const AsmFields& af, int32_t* col, double* val, double* dscale,
+void launch_assemble(hmec_inst* ctx, const Geo& g, const AsmFields& af, int32_t* col, double* val, double* dscale,
                      double* rhs_scaled, double* rhs_raw, const double*) {
     const dim3 grid(nblocks(g.Ny1, 64), g.Nx1, 6);  // z: the six rows of a cell
     HMEC_LAUNCH(ctx, k_assemble, grid, 64, 0, g, af, ctx->ds, ctx->p, col, val, dscale, rhs_scaled, rhs_raw);
 }
 
-int iter_assemble(hmec_ctx* ctx) {
+int iter_assemble(hmec_inst* ctx) {
     Level& L = ctx->sv.lv[0];
     launch_assemble(ctx, ctx->g, L.af, L.col, L.val, L.dscale, L.db, ctx->R, nullptr);
     HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;
 }
 
-int iter_finish(hmec_ctx* ctx) {
+int iter_finish(hmec_inst* ctx) {
     const Geo& g = ctx->g;
     double* const* f = ctx->f;
     int* status = &ctx->ds->status;
@@ -1140,7 +1140,7 @@ int iter_finish(hmec_ctx* ctx) {
     return HMEC_OK;
 }
 
-int step_end(hmec_ctx* ctx) {
+int step_end(hmec_inst* ctx) {
     const Geo& g = ctx->g;
     double* const* f = ctx->f;
     HMEC_LAUNCH(ctx, k_end_scalars, 1, 1, 0, ctx->ds);

@@ -306,9 +306,22 @@ __global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const floa
     for (int q = 0; q < NP; q++)
 #pragma unroll
         for (int c = 0; c < 4; c++) Sh[q][c] = Sl[q][c] = 0;
+    // the low parts collect the high parts' rounding errors; folding them back
+    // every 8 markers keeps the sums at double-float accuracy however many
+    // markers a cell holds (markers that cluster)
+    int since_norm = 0;
     for (int hc = c0 < 0 ? 0 : c0; hc <= c0 + 1 && hc < HC; hc++) {
         const int b = start[hc * HR + rlo], e = start[hc * HR + rhi + 1];
         for (int k = b; k < e; k++) {
+            if (++since_norm == 8) {
+                since_norm = 0;
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    df_norm(Wh[c], Wl[c]);
+#pragma unroll
+                    for (int q = 0; q < NP; q++) df_norm(Sh[q][c], Sl[q][c]);
+                }
+            }
             float r[RW];
             const float4* r4 = reinterpret_cast<const float4*>(rec + (size_t)k * RW);
 #pragma unroll
@@ -486,7 +499,7 @@ extern "C" int32_t hmec_cell_index(const double* x, int64_t n, double d, int32_t
     return e == cudaSuccess ? HMEC_OK : HMEC_ERR_CUDA;
 }
 
-int p2g_alloc(hmec_ctx* ctx) {
+int p2g_alloc(hmec_inst* ctx) {
     const Geo& g = ctx->g;
     ctx->nhalf = 4 * (g.Nx - 1) * (g.Ny - 1);
     int64_t n = ctx->marknum;
@@ -512,7 +525,7 @@ int p2g_alloc(hmec_ctx* ctx) {
     return HMEC_OK;
 }
 
-void p2g_free(hmec_ctx* ctx) {
+void p2g_free(hmec_inst* ctx) {
     cudaFree(ctx->mkey);
     cudaFree(ctx->perm);
     cudaFree(ctx->hc_count);
@@ -524,7 +537,7 @@ void p2g_free(hmec_ctx* ctx) {
     cudaFree(ctx->cellsum);
 }
 
-int p2g_run(hmec_ctx* ctx) {
+int p2g_run(hmec_inst* ctx) {
     const Geo& g = ctx->g;
     const int64_t n = ctx->marknum;
     const int nh = ctx->nhalf;

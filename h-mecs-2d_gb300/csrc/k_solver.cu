@@ -1719,7 +1719,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-static int encode_map3(hmec_ctx* ctx, CUtensorMap* map, CUtensorMapDataType dt, size_t esize, void* base,
+static int encode_map3(hmec_inst* ctx, CUtensorMap* map, CUtensorMapDataType dt, size_t esize, void* base,
                        uint64_t d0, uint64_t d1, uint64_t d2, uint32_t b0, uint32_t b1, uint32_t b2) {
     static EncodeTiledFn fn = nullptr;
     if (!fn) {
@@ -1745,7 +1745,7 @@ static int encode_map3(hmec_ctx* ctx, CUtensorMap* map, CUtensorMapDataType dt, 
     return HMEC_OK;
 }
 
-static int alloc_level(hmec_ctx* ctx, Level& L, bool mixed, bool coarse) {
+static int alloc_level(hmec_inst* ctx, Level& L, bool mixed, bool coarse) {
     const Geo& g = L.g;
     const size_t N = (size_t)g.N;
     L.npatch = (g.Ny - 1) * (g.Nx - 1);
@@ -1888,7 +1888,7 @@ static int alloc_level(hmec_ctx* ctx, Level& L, bool mixed, bool coarse) {
     return HMEC_OK;
 }
 
-int solver_alloc(hmec_ctx* ctx) {
+int solver_alloc(hmec_inst* ctx) {
     Solver& sv = ctx->sv;
     const hmec_params& p = ctx->p;
     const bool mixed = p.form == HMEC_FORM_MIXED;
@@ -1998,7 +1998,7 @@ int solver_alloc(hmec_ctx* ctx) {
     return HMEC_OK;
 }
 
-void solver_free(hmec_ctx* ctx) {
+void solver_free(hmec_inst* ctx) {
     Solver& sv = ctx->sv;
     for (Level& L : sv.lv) {
         cudaFree(L.col);
@@ -2071,7 +2071,7 @@ void solver_free(hmec_ctx* ctx) {
 // boundary pack run on its own stream once its coefficients exist, and the
 // restriction scaling of level l also waits for level l-1's row scale.  The
 // small coarse levels' kernels thus overlap instead of queueing.
-int solver_setup(hmec_ctx* ctx) {
+int solver_setup(hmec_inst* ctx) {
     Solver& sv = ctx->sv;
     const bool mixed = ctx->p.form == HMEC_FORM_MIXED;
     int* status = &ctx->ds->status;
@@ -2158,7 +2158,7 @@ constexpr int SINGLE_BLOCK_PATCHES = 0;
 constexpr size_t SMEM_LIMIT = 200 * 1024;
 
 template <typename T>
-static int max_coop_blocks(hmec_ctx* ctx) {
+static int max_coop_blocks(hmec_inst* ctx) {
     static int cached[2] = {0, 0};
     int& c = cached[sizeof(T) == 8 ? 0 : 1];
     if (c == 0) {
@@ -2174,7 +2174,7 @@ static int max_coop_blocks(hmec_ctx* ctx) {
 // when they fit in shared memory (FP32), else per-colour inverses (FP64); the
 // grid is the co-resident block count or the tile count, whichever is smaller.
 template <typename T>
-static int stage_config(hmec_ctx* ctx, Level& L) {
+static int stage_config(hmec_inst* ctx, Level& L) {
     if (L.st_whole >= 0) return HMEC_OK;
     int nsm = 0, optin = 0;
     HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
@@ -2234,7 +2234,7 @@ static double sweep_bytes_compulsory(double N, double sweeps) {
 }
 
 template <typename T>
-static StageArgs<T> stage_args(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mode, bool restrict_next,
+static StageArgs<T> stage_args(hmec_inst* ctx, size_t l, const T* b, T* x, int nsweeps, int mode, bool restrict_next,
                                double* ab, double* ab_alg) {
     Solver& sv = ctx->sv;
     Level& L = sv.lv[l];
@@ -2285,7 +2285,7 @@ static StageArgs<T> stage_args(hmec_ctx* ctx, size_t l, const T* b, T* x, int ns
 // sweeps).  restrict_next (tiled pass): also restrict the residual into the
 // next coarser level's rhs in the same launch.
 template <typename T>
-static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mode, bool restrict_next = false) {
+static int smooth(hmec_inst* ctx, size_t l, const T* b, T* x, int nsweeps, int mode, bool restrict_next = false) {
     Solver& sv = ctx->sv;
     Level& L = sv.lv[l];
     SmoothArgs<T> a;
@@ -2360,7 +2360,7 @@ static int smooth(hmec_ctx* ctx, size_t l, const T* b, T* x, int nsweeps, int mo
 // built once; only the fine level's b and x (the FP64 form's Krylov vectors)
 // are set per call, in the parameter copy the launch takes.
 template <typename T>
-static int vcycle_fused(hmec_ctx* ctx, const T* b0, T* x0, bool* used) {
+static int vcycle_fused(hmec_inst* ctx, const T* b0, T* x0, bool* used) {
     Solver& sv = ctx->sv;
     const hmec_params& p = ctx->p;
     *used = false;
@@ -2450,7 +2450,7 @@ static int vcycle_fused(hmec_ctx* ctx, const T* b0, T* x0, bool* used) {
 
 // V-cycle on level l for A x = b, x = 0 on entry (b, x default to the level's buffers).
 template <typename T>
-static int vcycle(hmec_ctx* ctx, size_t l, const T* b_in = nullptr, T* x_in = nullptr) {
+static int vcycle(hmec_inst* ctx, size_t l, const T* b_in = nullptr, T* x_in = nullptr) {
     // one launch per V-cycle for the FP32 smoother; the FP64 form (streamed
     // inverses) measured faster with a launch per pass (33.3 vs 32.7 ms per
     // 201x201 step), so it keeps those
@@ -2488,7 +2488,7 @@ static int vcycle(hmec_ctx* ctx, size_t l, const T* b_in = nullptr, T* x_in = nu
 // z = M^{-1} v on the fine level (v, z FP64 vectors of the scaled system)
 // (mixed form: z is left in FP32 in the fine level's x; input_ready: its
 // FP32 input is already in the fine level's b)
-static int precondition(hmec_ctx* ctx, const double* v, double* z, bool input_ready) {
+static int precondition(hmec_inst* ctx, const double* v, double* z, bool input_ready) {
     Solver& sv = ctx->sv;
     Level& L = sv.lv[0];
     const size_t N = (size_t)L.g.N;
@@ -2503,7 +2503,7 @@ static int precondition(hmec_ctx* ctx, const double* v, double* z, bool input_re
 // devj: the step index and z_j's slot come from the device (graph mode; j
 // is then only the estimate used for the byte accounting).
 template <typename TZ>
-static int arnoldi(hmec_ctx* ctx, const TZ* zsrc, double* Zj, int j, const Gm& G, double rtol, bool devj = false) {
+static int arnoldi(hmec_inst* ctx, const TZ* zsrc, double* Zj, int j, const Gm& G, double rtol, bool devj = false) {
     Solver& sv = ctx->sv;
     Level& L0 = sv.lv[0];
     static int cached = 0;
@@ -2550,7 +2550,7 @@ static int arnoldi(hmec_ctx* ctx, const TZ* zsrc, double* Zj, int j, const Gm& G
     return HMEC_OK;
 }
 
-int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
+int solver_solve(hmec_inst* ctx, int* iters_out, double* relres_out) {
     Solver& sv = ctx->sv;
     Level& L0 = sv.lv[0];
     const int N = sv.N, m = sv.m, nblk = sv.nblk;
@@ -2647,7 +2647,7 @@ int solver_solve(hmec_ctx* ctx, int* iters_out, double* relres_out) {
 // preconditioner reads fixed buffers (the mixed form's FP32 input fb and
 // output fx; the FP64 form's pb and dx_, which the Arnoldi step fills and
 // copies into z_j), so nothing in the graph depends on the step index.
-int solver_capture_solve(hmec_ctx* ctx, cudaStream_t s_restart, cudaStream_t s_inner, int64_t* n_restart,
+int solver_capture_solve(hmec_inst* ctx, cudaStream_t s_restart, cudaStream_t s_inner, int64_t* n_restart,
                          int64_t* n_inner) {
     Solver& sv = ctx->sv;
     Level& L0 = sv.lv[0];

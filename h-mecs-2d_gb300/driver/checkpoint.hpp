@@ -69,22 +69,23 @@ struct History {
     std::vector<std::vector<double>> v;
     explicit History(int num_timesteps) : v(6, std::vector<double>((size_t)num_timesteps, 0.0)) {}
     // after step `timestep` (1-based) has run: index timestep - 1
-    void record(hmec_ctx* ctx, int timestep) {
+    void record(hmec_ctx* ctx, int timestep, int32_t inst = 0) {
         const size_t t = (size_t)(timestep - 1);
         if (t >= v[0].size()) return;
         const char* src[6] = {"timesum", "dt", "maxvxsmod", "minvxsmod", "maxvysmod", "minvysmod"};
-        for (int k = 0; k < 6; k++) hmec_get_scalar(ctx, scalar_id(src[k]), &v[k][t]);
+        for (int k = 0; k < 6; k++) hmec_get_scalar(ctx, inst, scalar_id(src[k]), &v[k][t]);
     }
 };
 
 // The checkpoint of the context's state after a step, in write order.
-inline int collect(hmec_ctx* ctx, const hmec_params& p, const History& h, std::vector<Dataset>& out) {
+inline int collect(hmec_ctx* ctx, const hmec_params& p, const History& h, std::vector<Dataset>& out,
+                   int32_t inst = 0) {
     const int Ny = p.Ny, Nx = p.Nx, Ny1 = Ny + 1, Nx1 = Nx + 1;
     std::vector<double> colmajor;
     auto matrix = [&](const char* name, int rows, int cols) {
         Dataset d{"Matrix", name, {(uint64_t)rows, (uint64_t)cols}, std::vector<double>((size_t)rows * cols)};
         colmajor.resize((size_t)rows * cols);
-        const int rc = hmec_download_field(ctx, field_id(name), colmajor.data(), rows, cols);
+        const int rc = hmec_download_field(ctx, inst, field_id(name), colmajor.data(), rows, cols);
         for (int i = 0; i < rows; i++)  // data(i, j) -> out[i][j]
             for (int j = 0; j < cols; j++) d.v[(size_t)i * cols + j] = colmajor[(size_t)j * rows + i];
         out.push_back(std::move(d));
@@ -99,10 +100,10 @@ inline int collect(hmec_ctx* ctx, const hmec_params& p, const History& h, std::v
     std::vector<std::vector<double>> mk(HMEC_M_COUNT, std::vector<double>((size_t)n));
     std::vector<double*> mp(HMEC_M_COUNT);
     for (int k = 0; k < HMEC_M_COUNT; k++) mp[k] = mk[k].data();
-    if (int rc = hmec_download_markers(ctx, mp.data(), n)) return rc;
+    if (int rc = hmec_download_markers(ctx, inst, mp.data(), n)) return rc;
     for (const char* m : MARKERS) out.push_back({"Vector", m, {(uint64_t)n}, mk[marker_id(m)]});
     Dataset vals{"Value", "values", {9}, std::vector<double>(9)};
-    for (int k = 0; k < 9; k++) hmec_get_scalar(ctx, scalar_id(VALUES[k]), &vals.v[k]);
+    for (int k = 0; k < 9; k++) hmec_get_scalar(ctx, inst, scalar_id(VALUES[k]), &vals.v[k]);
     out.push_back(std::move(vals));
     return HMEC_OK;
 }
@@ -163,7 +164,8 @@ inline const Dataset* find(const std::vector<Dataset>& ds, const char* group, co
 // Restart as :211-282: every dataset into the context (the markers' other
 // arrays keep what the context holds -- the reference rebuilds them from its
 // lattice first), the histories into h, and the step counter past `timestep`.
-inline int restore(hmec_ctx* ctx, const hmec_params& p, const std::vector<Dataset>& ds, int timestep, History& h) {
+inline int restore(hmec_ctx* ctx, const hmec_params& p, const std::vector<Dataset>& ds, int timestep, History& h,
+                   int32_t inst = 0) {
     const int Ny = p.Ny, Nx = p.Nx;
     std::vector<double> colmajor;
     auto matrix = [&](const char* name, int rows, int cols) {
@@ -173,7 +175,7 @@ inline int restore(hmec_ctx* ctx, const hmec_params& p, const std::vector<Datase
         colmajor.resize((size_t)rows * cols);
         for (int i = 0; i < rows; i++)
             for (int j = 0; j < cols; j++) colmajor[(size_t)j * rows + i] = d->v[(size_t)i * cols + j];
-        return (int)hmec_upload_field(ctx, field_id(name), colmajor.data(), rows, cols);
+        return (int)hmec_upload_field(ctx, inst, field_id(name), colmajor.data(), rows, cols);
     };
     for (const char* n : MATRIX_BASIC)
         if (int rc = matrix(n, Ny, Nx)) return rc;
@@ -183,7 +185,7 @@ inline int restore(hmec_ctx* ctx, const hmec_params& p, const std::vector<Datase
     std::vector<std::vector<double>> mk(HMEC_M_COUNT, std::vector<double>((size_t)n));
     std::vector<double*> mp(HMEC_M_COUNT);
     for (int k = 0; k < HMEC_M_COUNT; k++) mp[k] = mk[k].data();
-    if (int rc = hmec_download_markers(ctx, mp.data(), n)) return rc;
+    if (int rc = hmec_download_markers(ctx, inst, mp.data(), n)) return rc;
     for (const char* m : MARKERS) {
         const Dataset* d = find(ds, "Vector", m);
         if (!d || d->v.size() != (size_t)n) return HMEC_ERR_ARG;
@@ -191,11 +193,11 @@ inline int restore(hmec_ctx* ctx, const hmec_params& p, const std::vector<Datase
         mp[marker_id(m)] = mk[marker_id(m)].data();
     }
     std::vector<const double*> cmp(mp.begin(), mp.end());
-    if (int rc = hmec_upload_markers(ctx, cmp.data(), n)) return rc;
+    if (int rc = hmec_upload_markers(ctx, inst, cmp.data(), n)) return rc;
     const Dataset* vals = find(ds, "Value", "values");
     if (!vals || vals->v.size() != 9) return HMEC_ERR_ARG;
-    for (int k = 0; k < 9; k++) hmec_set_scalar(ctx, scalar_id(VALUES[k]), vals->v[k]);
-    hmec_set_scalar(ctx, scalar_id("timestep"), (double)(timestep + 1));
+    for (int k = 0; k < 9; k++) hmec_set_scalar(ctx, inst, scalar_id(VALUES[k]), vals->v[k]);
+    hmec_set_scalar(ctx, inst, scalar_id("timestep"), (double)(timestep + 1));
     for (int k = 0; k < 6; k++)
         if (const Dataset* d = find(ds, "Vector", HISTORY[k])) h.v[k] = d->v;
     return HMEC_OK;

@@ -181,21 +181,21 @@ int main(int argc, char** argv) {
     Grid PT0(Ny1, Nx1, p.PCONF + p.PTFDIFF), PF0(Ny1, Nx1, p.PCONF);
 
     int32_t st = 0;
-    hmec_ctx* ctx = hmec_create(&p, &st);
+    hmec_ctx* ctx = hmec_create(&p, 1, nullptr, &st);
     if (!ctx) {
         fprintf(stderr, "hmec_create failed (%d)\n", st);
         return 1;
     }
     std::vector<const double*> mptr(HMEC_M_COUNT);
     for (int k = 0; k < HMEC_M_COUNT; k++) mptr[k] = mk[k].data();
-    if (check(ctx, hmec_upload_markers(ctx, mptr.data(), marknum), "upload_markers")) return 1;
+    if (check(ctx, hmec_upload_markers(ctx, 0, mptr.data(), marknum), "upload_markers")) return 1;
     struct {
         int id;
         Grid* g;
     } init[] = {{HMEC_F_OM0, &OM0}, {HMEC_F_OM, &OM0}, {HMEC_F_ARSF, &ARSF}, {HMEC_F_BRSF, &BRSF},
                 {HMEC_F_LRSF, &LRSF}, {HMEC_F_PT0, &PT0}, {HMEC_F_PF0, &PF0}};
     for (auto& f : init)
-        if (check(ctx, hmec_upload_field(ctx, f.id, f.g->a.data(), f.g->rows, f.g->cols), "upload_field")) return 1;
+        if (check(ctx, hmec_upload_field(ctx, 0, f.id, f.g->a.data(), f.g->rows, f.g->cols), "upload_field")) return 1;
 
     const std::string d = outdir + "/";
     ckpt::History history(p.num_timesteps);
@@ -258,7 +258,7 @@ int main(int argc, char** argv) {
             }
             const int rsf_ids[] = {HMEC_F_ARSF, HMEC_F_BRSF, HMEC_F_LRSF};
             std::vector<double> rr(3 * (size_t)Nx);
-            if (!check(ctx, hmec_download_rows(ctx, line_fault, 3, rsf_ids, rr.data()), "download_rows")) {
+            if (!check(ctx, hmec_download_rows(ctx, 0, line_fault, 3, rsf_ids, rr.data()), "download_rows")) {
                 FILE* fr = fopen((d + "rsf_fault.txt").c_str(), "a");
                 if (fr) {
                     const std::string t = eigen_text(rr.data(), Nx, false) + "\n\n" +
@@ -269,7 +269,7 @@ int main(int argc, char** argv) {
                 }
             }
         }
-        if (check(ctx, hmec_download_rows(ctx, line_fault, nevo, evo_ids, rows.data()), "download_rows")) break;
+        if (check(ctx, hmec_download_rows(ctx, 0, line_fault, nevo, evo_ids, rows.data()), "download_rows")) break;
         const double* row = rows.data();
         for (int j = 0; j < Nx1; j++) peff[j] = row[evo_off[3] + j] - row[evo_off[2] + j];  // pt - pf
         append_row(d + "EVO_Vslip.txt", r.timesum, r.dt, row + evo_off[0], Nx);

@@ -70,6 +70,13 @@ class IterReport(C.Structure):
                 ("Vmax", C.c_double), ("krylov_relres", C.c_double)]
 
 
+class Grid(C.Structure):
+    """ctypes mirror of ``hmec_grid`` (an instance's grid)."""
+
+    _fields_ = [("Nx", C.c_int32), ("Ny", C.c_int32), ("xsize", C.c_double), ("ysize", C.c_double),
+                ("mx", C.c_int32), ("my", C.c_int32)]
+
+
 class StepReport(C.Structure):
     _fields_ = [("timestep", C.c_int32), ("global_iters", C.c_int32), ("ynlast", C.c_int32),
                 ("krylov_iters", C.c_int32), ("status", C.c_int32), ("timesum", C.c_double), ("dt", C.c_double),
@@ -93,7 +100,7 @@ SCALARS = _xlist("HMEC_SCALAR_LIST")
 
 #: every entry point include/hmec.h declares
 EXPORTS = ["hmec_abi_version", "hmec_params_default", "hmec_field_name", "hmec_field_grid", "hmec_marker_name",
-           "hmec_scalar_name", "hmec_marknum", "hmec_create", "hmec_destroy", "hmec_last_error",
+           "hmec_scalar_name", "hmec_marknum", "hmec_create", "hmec_destroy", "hmec_instances", "hmec_last_error",
            "hmec_upload_markers", "hmec_download_markers", "hmec_upload_field", "hmec_download_field",
            "hmec_download_rows",
            "hmec_set_scalar", "hmec_get_scalar", "hmec_markers_to_nodes", "hmec_timestep_begin",
@@ -135,40 +142,44 @@ def load(build_if_missing: bool = True):
     L.hmec_scalar_name.restype = C.c_char_p
     L.hmec_marknum.argtypes = [P(Params)]
     L.hmec_marknum.restype = C.c_int64
-    L.hmec_create.argtypes = [P(Params), P(C.c_int32)]
+    L.hmec_create.argtypes = [P(Params), C.c_int32, P(Grid), P(C.c_int32)]
     L.hmec_create.restype = vp
     L.hmec_destroy.argtypes = [vp]
     L.hmec_destroy.restype = None
+    L.hmec_instances.argtypes = [vp]
+    L.hmec_instances.restype = C.c_int32
     L.hmec_last_error.argtypes = [vp]
     L.hmec_last_error.restype = C.c_char_p
-    L.hmec_upload_markers.argtypes = [vp, P(P(C.c_double)), C.c_int64]
-    L.hmec_download_markers.argtypes = [vp, P(P(C.c_double)), C.c_int64]
-    L.hmec_upload_field.argtypes = [vp, C.c_int32, P(C.c_double), C.c_int32, C.c_int32]
-    L.hmec_download_field.argtypes = [vp, C.c_int32, P(C.c_double), C.c_int32, C.c_int32]
-    L.hmec_download_rows.argtypes = [vp, C.c_int32, C.c_int32, P(C.c_int32), P(C.c_double)]
-    L.hmec_set_scalar.argtypes = [vp, C.c_int32, C.c_double]
-    L.hmec_get_scalar.argtypes = [vp, C.c_int32, P(C.c_double)]
-    for fn in ("hmec_markers_to_nodes", "hmec_timestep_begin", "hmec_timestep_end", "hmec_advect_markers",
-               "hmec_synchronize"):
-        getattr(L, fn).argtypes = [vp]
-        getattr(L, fn).restype = C.c_int32
-    L.hmec_global_iteration.argtypes = [vp, P(IterReport)]
+    i32 = C.c_int32
+    L.hmec_upload_markers.argtypes = [vp, i32, P(P(C.c_double)), C.c_int64]
+    L.hmec_download_markers.argtypes = [vp, i32, P(P(C.c_double)), C.c_int64]
+    L.hmec_upload_field.argtypes = [vp, i32, i32, P(C.c_double), i32, i32]
+    L.hmec_download_field.argtypes = [vp, i32, i32, P(C.c_double), i32, i32]
+    L.hmec_download_rows.argtypes = [vp, i32, i32, i32, P(i32), P(C.c_double)]
+    L.hmec_set_scalar.argtypes = [vp, i32, i32, C.c_double]
+    L.hmec_get_scalar.argtypes = [vp, i32, i32, P(C.c_double)]
+    for fn in ("hmec_markers_to_nodes", "hmec_timestep_begin", "hmec_timestep_end", "hmec_advect_markers"):
+        getattr(L, fn).argtypes = [vp, i32]
+        getattr(L, fn).restype = i32
+    L.hmec_synchronize.argtypes = [vp]
+    L.hmec_synchronize.restype = i32
+    L.hmec_global_iteration.argtypes = [vp, i32, P(IterReport)]
     L.hmec_timestep.argtypes = [vp, P(StepReport)]
-    L.hmec_assemble_csr.argtypes = [vp, P(C.c_int64), P(C.c_int32), P(C.c_double), P(C.c_double), P(C.c_int64),
+    L.hmec_assemble_csr.argtypes = [vp, i32, P(C.c_int64), P(i32), P(C.c_double), P(C.c_double), P(C.c_int64),
                                     P(C.c_double), P(C.c_double)]
-    L.hmec_solve_system.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_int32), P(C.c_double)]
+    L.hmec_solve_system.argtypes = [vp, i32, P(C.c_double), P(C.c_double), P(i32), P(C.c_double)]
     L.hmec_kernel_launches.argtypes = [vp]
     L.hmec_kernel_launches.restype = C.c_int64
     L.hmec_graph_status.argtypes = [vp]
-    L.hmec_graph_status.restype = C.c_int32
-    L.hmec_stream.argtypes = [vp]
+    L.hmec_graph_status.restype = i32
+    L.hmec_stream.argtypes = [vp, i32]
     L.hmec_stream.restype = vp
-    L.hmec_profile_kernel.argtypes = [vp, C.c_char_p]
-    L.hmec_profile_read.argtypes = [vp, P(C.c_int64), P(C.c_double), P(C.c_double), P(C.c_double)]
+    L.hmec_profile_kernel.argtypes = [vp, i32, C.c_char_p]
+    L.hmec_profile_read.argtypes = [vp, i32, P(C.c_int64), P(C.c_double), P(C.c_double), P(C.c_double)]
     L.hmec_markers_to_nodes_noalloc.argtypes = [P(Params), P(P(C.c_double)), C.c_int64, P(P(C.c_double)), vp]
-    L.hmec_markers_to_nodes_noalloc.restype = C.c_int32
-    L.hmec_cell_index.argtypes = [P(C.c_double), C.c_int64, C.c_double, C.c_int32, P(C.c_int32)]
-    L.hmec_cell_index.restype = C.c_int32
+    L.hmec_markers_to_nodes_noalloc.restype = i32
+    L.hmec_cell_index.argtypes = [P(C.c_double), C.c_int64, C.c_double, i32, P(i32)]
+    L.hmec_cell_index.restype = i32
     _lib = L
     return L
 
@@ -201,30 +212,22 @@ def _dptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
-class Model:
-    """One model instance on the current CUDA device (a context of the C ABI)."""
+class Instance:
+    """Instance `inst` of a library context: one model's data and sections
+    (the instance dimension of include/hmec.h)."""
 
-    def __init__(self, params: Params):
-        self.L = load()
+    def __init__(self, owner, inst: int, params: Params):
+        self.owner = owner
+        self.L = owner.L
+        self.inst = inst
         self.params = params
-        st = C.c_int32(0)
-        self.h = self.L.hmec_create(C.byref(params), C.byref(st))
-        if not self.h:
-            raise HmecError(st.value, "hmec_create failed")
         self.Nx, self.Ny = params.Nx, params.Ny
         self.N = (self.Nx + 1) * (self.Ny + 1) * 6
         self.marknum = self.L.hmec_marknum(C.byref(params))
 
-    def close(self):
-        if getattr(self, "h", None):
-            self.L.hmec_destroy(self.h)
-            self.h = None
-
-    def __del__(self):
-        try:
-            self.close()
-        except Exception:
-            pass
+    @property
+    def h(self):
+        return self.owner.h
 
     def _check(self, rc, what):
         if rc != HMEC_OK:
@@ -242,24 +245,24 @@ class Model:
             if b.shape != (self.marknum,):
                 raise ValueError("marker arrays must have length %d" % self.marknum)
         ptrs = (C.POINTER(C.c_double) * len(bufs))(*[_dptr(b) for b in bufs])
-        self._check(self.L.hmec_upload_markers(self.h, ptrs, self.marknum), "upload_markers")
+        self._check(self.L.hmec_upload_markers(self.h, self.inst, ptrs, self.marknum), "upload_markers")
 
     def download_markers(self) -> dict:
         bufs = [np.empty(self.marknum) for _ in MARKERS]
         ptrs = (C.POINTER(C.c_double) * len(bufs))(*[_dptr(b) for b in bufs])
-        self._check(self.L.hmec_download_markers(self.h, ptrs, self.marknum), "download_markers")
+        self._check(self.L.hmec_download_markers(self.h, self.inst, ptrs, self.marknum), "download_markers")
         return dict(zip(MARKERS, bufs))
 
     def upload_field(self, name, arr):
         r, c = self.shape(name)
         a = np.asfortranarray(np.asarray(arr, dtype=np.float64).reshape(r, c))
         buf = a.ravel(order="F")
-        self._check(self.L.hmec_upload_field(self.h, FIELDS.index(name), _dptr(buf), r, c), "upload_field")
+        self._check(self.L.hmec_upload_field(self.h, self.inst, FIELDS.index(name), _dptr(buf), r, c), "upload_field")
 
     def field(self, name) -> np.ndarray:
         r, c = self.shape(name)
         buf = np.empty(r * c)
-        self._check(self.L.hmec_download_field(self.h, FIELDS.index(name), _dptr(buf), r, c), "download_field")
+        self._check(self.L.hmec_download_field(self.h, self.inst, FIELDS.index(name), _dptr(buf), r, c), "download_field")
         return buf.reshape((r, c), order="F")
 
     def rows(self, row, names) -> dict:
@@ -267,7 +270,7 @@ class Model:
         ids = (C.c_int32 * len(names))(*[FIELDS.index(n) for n in names])
         lens = [self.shape(n)[1] for n in names]
         buf = np.empty(sum(lens))
-        self._check(self.L.hmec_download_rows(self.h, row, len(names), ids, _dptr(buf)), "download_rows")
+        self._check(self.L.hmec_download_rows(self.h, self.inst, row, len(names), ids, _dptr(buf)), "download_rows")
         out, o = {}, 0
         for n, k in zip(names, lens):
             out[n] = buf[o:o + k].copy()
@@ -275,11 +278,11 @@ class Model:
         return out
 
     def set_scalar(self, name, v):
-        self._check(self.L.hmec_set_scalar(self.h, SCALARS.index(name), float(v)), "set_scalar")
+        self._check(self.L.hmec_set_scalar(self.h, self.inst, SCALARS.index(name), float(v)), "set_scalar")
 
     def scalar(self, name) -> float:
         v = C.c_double()
-        self._check(self.L.hmec_get_scalar(self.h, SCALARS.index(name), C.byref(v)), "get_scalar")
+        self._check(self.L.hmec_get_scalar(self.h, self.inst, SCALARS.index(name), C.byref(v)), "get_scalar")
         return v.value
 
     def load_state(self, snap: dict):
@@ -297,21 +300,88 @@ class Model:
 
     # -------------------------------------------------------- sections
     def markers_to_nodes(self):
-        self._check(self.L.hmec_markers_to_nodes(self.h), "markers_to_nodes")
+        self._check(self.L.hmec_markers_to_nodes(self.h, self.inst), "markers_to_nodes")
 
     def timestep_begin(self):
-        self._check(self.L.hmec_timestep_begin(self.h), "timestep_begin")
+        self._check(self.L.hmec_timestep_begin(self.h, self.inst), "timestep_begin")
 
     def global_iteration(self) -> dict:
         rep = IterReport()
-        self._check(self.L.hmec_global_iteration(self.h, C.byref(rep)), "global_iteration")
+        self._check(self.L.hmec_global_iteration(self.h, self.inst, C.byref(rep)), "global_iteration")
         return {k: getattr(rep, k) for k, _ in IterReport._fields_}
 
     def timestep_end(self):
-        self._check(self.L.hmec_timestep_end(self.h), "timestep_end")
+        self._check(self.L.hmec_timestep_end(self.h, self.inst), "timestep_end")
 
     def advect_markers(self):
-        self._check(self.L.hmec_advect_markers(self.h), "advect_markers")
+        self._check(self.L.hmec_advect_markers(self.h, self.inst), "advect_markers")
+
+    @property
+    def stream_ptr(self) -> int:
+        """cudaStream_t of the context (for CUDA-event timing)."""
+        return self.L.hmec_stream(self.h, self.inst) or 0
+
+    def profile_kernel(self, name):
+        self._check(self.L.hmec_profile_kernel(self.h, self.inst, name.encode() if name else None), "profile_kernel")
+
+    def profile_read(self):
+        """(launches, total ms, compulsory bytes, bytes moved) of the profiled kernel family."""
+        n, ms, b, bm = C.c_int64(), C.c_double(), C.c_double(), C.c_double()
+        self._check(self.L.hmec_profile_read(self.h, self.inst, C.byref(n), C.byref(ms), C.byref(b), C.byref(bm)),
+                    "profile_read")
+        return n.value, ms.value, b.value, bm.value
+
+    # ---------------------------------------------------------- hooks
+    def assemble_csr(self):
+        import scipy.sparse as sp
+
+        nnz = C.c_int64()
+        self._check(self.L.hmec_assemble_csr(self.h, self.inst, None, None, None, None, C.byref(nnz), None, None), "assemble_csr")
+        n = self.N
+        indptr = np.zeros(n + 1, dtype=np.int64)
+        indices = np.zeros(nnz.value, dtype=np.int32)
+        data = np.zeros(nnz.value)
+        rhs = np.zeros(n)
+        pt, pf = C.c_double(), C.c_double()
+        self._check(self.L.hmec_assemble_csr(self.h, self.inst, indptr.ctypes.data_as(C.POINTER(C.c_int64)),
+                                             indices.ctypes.data_as(C.POINTER(C.c_int32)), _dptr(data), _dptr(rhs),
+                                             C.byref(nnz), C.byref(pt), C.byref(pf)), "assemble_csr")
+        return sp.csr_matrix((data, indices, indptr), shape=(n, n)), rhs, pt.value, pf.value
+
+    def solve_system(self, rhs, x0=None):
+        b = np.ascontiguousarray(rhs, dtype=np.float64)
+        x = np.zeros(self.N) if x0 is None else np.array(x0, dtype=np.float64)
+        its, rel = C.c_int32(), C.c_double()
+        rc = self.L.hmec_solve_system(self.h, self.inst, _dptr(b), _dptr(x), C.byref(its), C.byref(rel))
+        return x, its.value, rel.value, rc
+
+
+class Model(Instance):
+    """One model on the current CUDA device: a library context with one
+    instance (instance 0)."""
+
+    def __init__(self, params: Params):
+        self.L = load()
+        st = C.c_int32(0)
+        self._h = self.L.hmec_create(C.byref(params), 1, None, C.byref(st))
+        if not self._h:
+            raise HmecError(st.value, "hmec_create failed")
+        Instance.__init__(self, self, 0, params)
+
+    @property
+    def h(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.L.hmec_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
     def timestep(self, check=True) -> dict:
         rep = StepReport()
@@ -339,41 +409,3 @@ class Model:
         msg = self.L.hmec_last_error(self.h)
         return msg.decode() if msg else ""
 
-    @property
-    def stream_ptr(self) -> int:
-        """cudaStream_t of the context (for CUDA-event timing)."""
-        return self.L.hmec_stream(self.h) or 0
-
-    def profile_kernel(self, name):
-        self._check(self.L.hmec_profile_kernel(self.h, name.encode() if name else None), "profile_kernel")
-
-    def profile_read(self):
-        """(launches, total ms, compulsory bytes, bytes moved) of the profiled kernel family."""
-        n, ms, b, bm = C.c_int64(), C.c_double(), C.c_double(), C.c_double()
-        self._check(self.L.hmec_profile_read(self.h, C.byref(n), C.byref(ms), C.byref(b), C.byref(bm)),
-                    "profile_read")
-        return n.value, ms.value, b.value, bm.value
-
-    # ---------------------------------------------------------- hooks
-    def assemble_csr(self):
-        import scipy.sparse as sp
-
-        nnz = C.c_int64()
-        self._check(self.L.hmec_assemble_csr(self.h, None, None, None, None, C.byref(nnz), None, None), "assemble_csr")
-        n = self.N
-        indptr = np.zeros(n + 1, dtype=np.int64)
-        indices = np.zeros(nnz.value, dtype=np.int32)
-        data = np.zeros(nnz.value)
-        rhs = np.zeros(n)
-        pt, pf = C.c_double(), C.c_double()
-        self._check(self.L.hmec_assemble_csr(self.h, indptr.ctypes.data_as(C.POINTER(C.c_int64)),
-                                             indices.ctypes.data_as(C.POINTER(C.c_int32)), _dptr(data), _dptr(rhs),
-                                             C.byref(nnz), C.byref(pt), C.byref(pf)), "assemble_csr")
-        return sp.csr_matrix((data, indices, indptr), shape=(n, n)), rhs, pt.value, pf.value
-
-    def solve_system(self, rhs, x0=None):
-        b = np.ascontiguousarray(rhs, dtype=np.float64)
-        x = np.zeros(self.N) if x0 is None else np.array(x0, dtype=np.float64)
-        its, rel = C.c_int32(), C.c_double()
-        rc = self.L.hmec_solve_system(self.h, _dptr(b), _dptr(x), C.byref(its), C.byref(rel))
-        return x, its.value, rel.value, rc

@@ -18,8 +18,12 @@
  *   - Every entry point returns an int status (HMEC_OK == 0, negative on
  *     error); no C++ exception crosses the ABI.  hmec_last_error() gives the
  *     message of the last failure on a context.
+ *   - A context holds n model instances (n = 1: one model; n > 1: the
+ *     members of an ensemble, each with its own grid).  Every data and
+ *     section entry point names the instance `inst` it acts on; an instance
+ *     holds the reference's global state of one model.
  *   - One host thread per context.  The context owns all device memory and
- *     one CUDA stream on the device that was current at hmec_create().
+ *     one CUDA stream per instance on the device current at hmec_create().
  */
 #ifndef HMEC_H
 #define HMEC_H
@@ -30,7 +34,7 @@
 extern "C" {
 #endif
 
-#define HMEC_ABI_VERSION 1
+#define HMEC_ABI_VERSION 2
 
 /* ------------------------------------------------------------------ status */
 enum hmec_status {
@@ -207,69 +211,91 @@ const char* hmec_scalar_name(int32_t id);
 int64_t hmec_marknum(const hmec_params* p);
 
 /* --------------------------------------------------------------- lifecycle */
+/* The grid of one instance: the fields of hmec_params it overrides. */
+typedef struct hmec_grid {
+    int32_t Nx, Ny;
+    double xsize, ysize;
+    int32_t mx, my;
+} hmec_grid;
+
 /* Replaces the global declarations of cpp/h_mec_rsf_v9.cpp:54-112 and
- * constants.hpp:153-173: allocates every node field, marker array and solver
- * buffer on the current device.  Fields start at zero.  *status receives the
- * error code when NULL is returned.                                         */
-hmec_ctx* hmec_create(const hmec_params* p, int32_t* status);
+ * constants.hpp:153-173, once per instance: allocates every node field,
+ * marker array and solver buffer of n_instances models on the current
+ * device.  grids[k] (NULL: p's grid for all) gives instance k its grid; the
+ * other parameters are shared (per-instance friction, permeability and the
+ * like are node fields and marker arrays, uploaded per instance).  An
+ * ensemble (n_instances > 1) advances all its members with one
+ * hmec_timestep() call, each member with its own adaptive dt, iteration
+ * counts and convergence decisions.  Fields start at zero.  *status
+ * receives the error code when NULL is returned.                            */
+hmec_ctx* hmec_create(const hmec_params* p, int32_t n_instances, const hmec_grid* grids, int32_t* status);
 void hmec_destroy(hmec_ctx* ctx);
+int32_t hmec_instances(const hmec_ctx* ctx);
 const char* hmec_last_error(const hmec_ctx* ctx);
 
 /* ------------------------------------------------------------ data motion */
-/* Marker arrays: fields[k] points to the array of marker field k
- * (enum hmec_marker_field order), each of length n == hmec_marknum().
- * Replaces the initialisation of :188-209 (and the HDF5 reads of :245-251). */
-int32_t hmec_upload_markers(hmec_ctx* ctx, const double* const* fields, int64_t n);
-int32_t hmec_download_markers(hmec_ctx* ctx, double* const* fields, int64_t n);
+/* Marker arrays of instance inst: fields[k] points to the array of marker
+ * field k (enum hmec_marker_field order), each of length n == hmec_marknum()
+ * of the instance's grid.  Replaces the initialisation of :188-209 (and the
+ * HDF5 reads of :245-251).                                                 */
+int32_t hmec_upload_markers(hmec_ctx* ctx, int32_t inst, const double* const* fields, int64_t n);
+int32_t hmec_download_markers(hmec_ctx* ctx, int32_t inst, double* const* fields, int64_t n);
 /* One node field; rows/cols must match the field's grid. */
-int32_t hmec_upload_field(hmec_ctx* ctx, int32_t field, const double* colmajor, int32_t rows, int32_t cols);
-int32_t hmec_download_field(hmec_ctx* ctx, int32_t field, double* colmajor, int32_t rows, int32_t cols);
+int32_t hmec_upload_field(hmec_ctx* ctx, int32_t inst, int32_t field, const double* colmajor, int32_t rows,
+                          int32_t cols);
+int32_t hmec_download_field(hmec_ctx* ctx, int32_t inst, int32_t field, double* colmajor, int32_t rows,
+                            int32_t cols);
 /* Row `row` of each of nfields node fields, gathered on the device and
  * copied back in one transfer: out receives the rows one after another, each
  * as long as its field's row (Nx basic, Nx+1 staggered).  The per-step
  * EVO_*.txt series print such rows of the fault line (:1751-1805); this
  * replaces downloading the whole fields.                                    */
-int32_t hmec_download_rows(hmec_ctx* ctx, int32_t row, int32_t nfields, const int32_t* fields, double* out);
-int32_t hmec_set_scalar(hmec_ctx* ctx, int32_t id, double value);
-int32_t hmec_get_scalar(hmec_ctx* ctx, int32_t id, double* value);
+int32_t hmec_download_rows(hmec_ctx* ctx, int32_t inst, int32_t row, int32_t nfields, const int32_t* fields,
+                           double* out);
+int32_t hmec_set_scalar(hmec_ctx* ctx, int32_t inst, int32_t id, double value);
+int32_t hmec_get_scalar(hmec_ctx* ctx, int32_t inst, int32_t id, double* value);
 
 /* ---------------------------------------------------------------- sections */
 /* a1-a4: marker properties, counting sort by cell, deterministic node
  * reductions and normalisation.  Replaces :376-583.                         */
-int32_t hmec_markers_to_nodes(hmec_ctx* ctx);
+int32_t hmec_markers_to_nodes(hmec_ctx* ctx, int32_t inst);
 /* a5: viscosity reset, dt growth, iteration counters.  Replaces :585-608.   */
-int32_t hmec_timestep_begin(hmec_ctx* ctx);
+int32_t hmec_timestep_begin(hmec_ctx* ctx, int32_t inst);
 /* a6-a15: one global (plastic) iteration -- viscosity limits, assembly,
  * FGMRES solve, reload, stress, fault RSF, error and adaptive dt, exit test
  * and viscosity update.  Replaces one pass of the loop body :611-1456.
  * report may be NULL.                                                        */
-int32_t hmec_global_iteration(hmec_ctx* ctx, hmec_iter_report* report);
+int32_t hmec_global_iteration(hmec_ctx* ctx, int32_t inst, hmec_iter_report* report);
 /* a16-a19: dt recheck, post-step stress and invariants, state rollover.
  * Replaces :1463-1559 and :1658-1726 (advection excluded).                  */
-int32_t hmec_timestep_end(hmec_ctx* ctx);
+int32_t hmec_timestep_end(hmec_ctx* ctx, int32_t inst);
 /* a18, a20: node-to-marker velocity/spin gather, RK4 advection, stress
  * rotation, periodic recycling.  Replaces the (never executed) loop
  * :1561-1656.                                                               */
-int32_t hmec_advect_markers(hmec_ctx* ctx);
-/* a1-a20 in order: one whole timestep, loop control on the device.
- * Replaces the body of `for (; timestep <= num_timesteps; ...)` up to the
- * output section (:377-1726).  report may be NULL.                          */
-int32_t hmec_timestep(hmec_ctx* ctx, hmec_step_report* report);
+int32_t hmec_advect_markers(hmec_ctx* ctx, int32_t inst);
+/* a1-a20 in order: one whole timestep of every instance, loop control on
+ * the device.  Replaces the body of `for (; timestep <= num_timesteps; ...)`
+ * up to the output section (:377-1726).  reports: NULL or an array of
+ * hmec_instances() reports (one per instance).  With graph = 1 every step
+ * after the first is one CUDA graph launch -- for an ensemble, one launch
+ * for all members.  Returns the first non-OK status of any instance.        */
+int32_t hmec_timestep(hmec_ctx* ctx, hmec_step_report* reports);
 
 /* --------------------------------------------------------- testing hooks */
 /* Assemble the global system of the current state (after the iteration
  * preparation of :611-677) and return it as CSR with duplicates summed, the
  * form Eigen's setFromTriplets produces at :1046-1049.  With indptr == NULL
  * only *nnz is returned.  rhs receives R (length N).                        */
-int32_t hmec_assemble_csr(hmec_ctx* ctx, int64_t* indptr, int32_t* indices, double* data,
+int32_t hmec_assemble_csr(hmec_ctx* ctx, int32_t inst, int64_t* indptr, int32_t* indices, double* data,
                           double* rhs, int64_t* nnz, double* ptscale, double* pfscale);
 /* Solve the system assembled by the last hmec_assemble_csr / iteration with
  * the configured solver for the given right-hand side; x holds the initial
  * guess on entry and the solution on return.                                 */
-int32_t hmec_solve_system(hmec_ctx* ctx, const double* rhs, double* x, int32_t* iters, double* relres);
-/* The CUDA stream (cudaStream_t) the context launches on, for timing with
+int32_t hmec_solve_system(hmec_ctx* ctx, int32_t inst, const double* rhs, double* x, int32_t* iters,
+                          double* relres);
+/* The CUDA stream (cudaStream_t) instance inst launches on, for timing with
  * CUDA events (no counterpart in the reference). */
-void* hmec_stream(hmec_ctx* ctx);
+void* hmec_stream(hmec_ctx* ctx, int32_t inst);
 /* Time every launch of the kernel family whose name starts with `name`
  * (NULL: stop) with CUDA events on the context stream, and accumulate the
  * bytes those launches move; read and reset with hmec_profile_read():
@@ -278,9 +304,9 @@ void* hmec_stream(hmec_ctx* ctx);
  * touch), *bytes_moved what this implementation moves by its own account
  * (stored patch inverses, column offsets, padding included).  Used by the
  * benchmark's live roofline (no counterpart in the reference).             */
-int32_t hmec_profile_kernel(hmec_ctx* ctx, const char* name);
-int32_t hmec_profile_read(hmec_ctx* ctx, int64_t* launches, double* total_ms, double* bytes_compulsory,
-                          double* bytes_moved);
+int32_t hmec_profile_kernel(hmec_ctx* ctx, int32_t inst, const char* name);
+int32_t hmec_profile_read(hmec_ctx* ctx, int32_t inst, int64_t* launches, double* total_ms,
+                          double* bytes_compulsory, double* bytes_moved);
 /* Markers -> nodes without allocating device memory.  No counterpart in the
  * reference: it serves hosts that may not call cudaMalloc (an application
  * that owns the device allocator, a real-time loop that must not block on
@@ -313,13 +339,15 @@ int32_t hmec_markers_to_nodes_noalloc(const hmec_params* p, const double* const*
  * bit-exactly (no counterpart in the reference).                           */
 int32_t hmec_cell_index(const double* x, int64_t n, double d, int32_t half, int32_t* out);
 /* How hmec_timestep runs on this context (no counterpart in the reference):
- * 1 = each step is one CUDA graph launch, 0 = host-driven launches so far
- * (the first step, or while a kernel is profiled), -1 = host-driven for good
- * (graph = 0, or the capture failed; hmec_last_error() then gives why).     */
+ * 1 = each step is one CUDA graph launch (for an ensemble: one launch for all
+ * members), 0 = host-driven launches so far (the first step, or while a
+ * kernel is profiled), -1 = host-driven for good (graph = 0, or the capture
+ * failed; hmec_last_error() then gives why).                                */
 int32_t hmec_graph_status(hmec_ctx* ctx);
-/* Device-kernel launches issued since hmec_create. */
+/* Device-kernel launches of all instances since hmec_create (kernels run by
+ * a graph launch included). */
 int64_t hmec_kernel_launches(const hmec_ctx* ctx);
-/* Synchronise the context stream. */
+/* Synchronise every instance's stream. */
 int32_t hmec_synchronize(hmec_ctx* ctx);
 
 #ifdef __cplusplus

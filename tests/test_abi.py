@@ -75,7 +75,17 @@ def test_create_rejects_bad_params_without_touching_a_device():
     # argument validation happens before any CUDA call
     p = hmec.default_params(Nx=2)
     st = C.c_int32(0)
-    h = hmec.load().hmec_create(C.byref(p), C.byref(st))
+    h = hmec.load().hmec_create(C.byref(p), 1, None, C.byref(st))
+    assert not h and st.value == -1
+    # an ensemble needs at least one instance
+    q = hmec.default_params()
+    st = C.c_int32(0)
+    h = hmec.load().hmec_create(C.byref(q), 0, None, C.byref(st))
+    assert not h and st.value == -1
+    # a member's grid is checked like the shared one
+    grids = (hmec.Grid * 2)(hmec.Grid(51, 51, 1e4, 1e4, 4, 4), hmec.Grid(3, 51, 1e4, 1e4, 4, 4))
+    st = C.c_int32(0)
+    h = hmec.load().hmec_create(C.byref(q), 2, grids, C.byref(st))
     assert not h and st.value == -1
 
 

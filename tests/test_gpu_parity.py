@@ -262,10 +262,12 @@ def test_argument_and_state_errors():
         m.global_iteration()  # before timestep_begin
     assert e.value.code == -8
     buf = np.zeros(7)
-    rc = m.L.hmec_upload_field(m.h, 0, buf.ctypes.data_as(C.POINTER(C.c_double)), 1, 7)
+    rc = m.L.hmec_upload_field(m.h, 0, 0, buf.ctypes.data_as(C.POINTER(C.c_double)), 1, 7)
     assert rc == -1
-    rc = m.L.hmec_upload_field(m.h, 999, buf.ctypes.data_as(C.POINTER(C.c_double)), 1, 7)
+    rc = m.L.hmec_upload_field(m.h, 0, 999, buf.ctypes.data_as(C.POINTER(C.c_double)), 1, 7)
     assert rc == -1
+    rc = m.L.hmec_upload_field(m.h, 1, 0, buf.ctypes.data_as(C.POINTER(C.c_double)), 1, 7)
+    assert rc == -1 and b"instance" in m.L.hmec_last_error(m.h)
 
 
 def test_kernels_launch_through_the_library():

@@ -16,7 +16,8 @@ from identical bytes.  Bounds, as in the tiny/config-0 replays: 1e-10 relative
 round-off near the yield stress, max(1e-10, 10 x the oracle's own floor)
 (the same system solved with other pivots); slip rate and state within the
 reference's bisection resolution |dS| <= 1e-3 Pa (:1224).  Global iteration
-counts are equal; dt agrees to 1e-12, or to 1e-8 in a rupture phase, where dt
+counts are equal; dt agrees to 1e-10 (it follows the velocity maxima of the
+adaptive-step rules, :1310-1427), or to 1e-8 in a rupture phase, where it
 follows the slip rate (Lapusta step, :1266-1273).
 """
 import numpy as np
@@ -35,7 +36,7 @@ RUPTURE_TAU = 16e6  # uniform pre-stress SXY0 (Pa), above the fault's steady-sta
 FORMS = (hmec.FORM_MIXED, hmec.FORM_FP64)
 
 
-def replay_and_check(over, mk, snap, label, dt_rel=1e-12, forms=FORMS):
+def replay_and_check(over, mk, snap, label, dt_rel=1e-10, forms=FORMS):
     """One timestep from `snap` on the oracle and on the GPU (each form);
     asserts the bounds of the module docstring and returns the errors."""
     o = O.Oracle(O.default_params(**over))

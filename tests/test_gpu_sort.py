@@ -5,9 +5,12 @@ order is put in marker-index order by one thread.  When many markers share a
 half cell (they cluster, or coordinates outside the domain are clamped into
 an edge cell by check_bounds, cpp/h_mec_rsf_v9.cpp:144-151), the long
 segments are left to the stable radix sort instead.  Both must give the
-oracle's node fields (to the 1e-13 of the marker->node parity tests, the
-summation order differing from the reference's serial marker loop) and be
-bit-identical across runs.
+oracle's node fields and be bit-identical across runs.  The tolerance is the
+1e-13 of the marker->node parity tests (the summation order differs from the
+reference's serial marker loop), widened for cells that hold very many
+markers to the accumulation error of their sums: the GPU adds in
+double-float (48-bit significands), the oracle in FP64, so the difference
+grows like the number of markers in the fullest cell times 2^-45.
 """
 import numpy as np
 import pytest
@@ -16,6 +19,15 @@ import pairs
 from pairs import P2G_FIELDS
 
 pytestmark = pytest.mark.gpu
+
+
+def tolerance(mk, p):
+    """max(1e-13, (markers in the fullest cell) x 2^-45)."""
+    dx, dy = p.xsize / (p.Nx - 1), p.ysize / (p.Ny - 1)
+    j = np.clip(np.trunc(mk["xm"] / dx).astype(np.int64), 0, p.Nx - 2)
+    i = np.clip(np.trunc(mk["ym"] / dy).astype(np.int64), 0, p.Ny - 2)
+    nmax = int(np.bincount(j * (p.Ny - 1) + i).max())
+    return max(1e-13, nmax * 2.0 ** -45)
 
 
 def clustered(preset, frac=0.4, seed=11):
@@ -47,7 +59,7 @@ def test_clustered_markers_match_oracle_and_repeat(preset):
     m.markers_to_nodes()
     first = {f: m.field(f) for f in P2G_FIELDS}
     e = pairs.field_errors(m, o, P2G_FIELDS)
-    assert max(e.values()) < 1e-13, e
+    assert max(e.values()) < tolerance(mk, o.params), (e, tolerance(mk, o.params))
     m.markers_to_nodes()
     for f in P2G_FIELDS:
         assert np.array_equal(first[f], m.field(f)), f
@@ -56,7 +68,8 @@ def test_clustered_markers_match_oracle_and_repeat(preset):
 def test_clustered_and_spread_markers_in_one_model():
     """Upload spread markers, then clustered ones, then spread ones again:
     each P2G equals a fresh model's (the long-segment flag is cleared every
-    step)."""
+    step).  Nodes without markers keep their values (:536 etc.), so the
+    outputs are cleared before each P2G, as in a fresh model."""
     o0, mk0, nodes = pairs.oracle_for("tiny")
     _, mk1, _ = clustered("tiny")
     m = pairs.model_for("tiny", mk0, nodes)
@@ -66,6 +79,8 @@ def test_clustered_and_spread_markers_in_one_model():
     ref1.markers_to_nodes()
     for mk, ref in ((mk0, ref0), (mk1, ref1), (mk0, ref0)):
         m.upload_markers(mk)
+        for f in P2G_FIELDS:
+            m.upload_field(f, np.zeros(m.shape(f)))
         m.markers_to_nodes()
         for f in P2G_FIELDS:
             assert np.array_equal(m.field(f), ref.field(f)), f
