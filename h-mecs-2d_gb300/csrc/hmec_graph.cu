@@ -63,6 +63,14 @@ void abandon_capture(hmec_inst* ctx, cudaStream_t main) {
             if (g && s == main) cudaGraphDestroy(g);
         }
     }
+    for (cudaStream_t a : ctx->gs4) {
+        if (!a) continue;
+        cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(a, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(a, &g);
+        }
+    }
     for (cudaStream_t a : ctx->sv.aux) {
         cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
         if (cudaStreamIsCapturing(a, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {

@@ -230,6 +230,8 @@ struct hmec_inst {
     int32_t* hc_fill;        // scatter cursors
     int32_t* scan_part;      // scan block partials
     int* sort_long;          // set when a half cell holds more markers than the per-segment sort takes
+    cudaStream_t gs4[4] = {nullptr, nullptr, nullptr, nullptr};  // the four grids' gathers
+    cudaEvent_t ev_g_fork = nullptr, ev_g_done[4] = {nullptr, nullptr, nullptr, nullptr};
     float* mprop;            // sorted per-marker gather records of the four grids (double-float)
     double* cellsum;         // per-cell corner sums of the four grids (k_cell_sums)
     int nhalf;               // number of half-cells

@@ -511,6 +511,11 @@ int p2g_alloc(hmec_inst* ctx) {
     HMEC_CUDA(ctx, cudaMalloc(&ctx->hc_fill, sizeof(int32_t) * ((size_t)ctx->nhalf + 1)));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->scan_part, sizeof(int32_t) * ((size_t)nparts + 1)));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->sort_long, sizeof(int)));
+    for (int k = 0; k < 4; k++) {
+        HMEC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->gs4[k], cudaStreamNonBlocking));
+        HMEC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_g_done[k], cudaEventDisableTiming));
+    }
+    HMEC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_g_fork, cudaEventDisableTiming));
     // the marker records double as the radix sort's scratch (they are
     // written only after the sort); they hold 64 ints per marker, the sort
     // needs about 3.5
@@ -533,6 +538,11 @@ void p2g_free(hmec_inst* ctx) {
     cudaFree(ctx->hc_fill);
     cudaFree(ctx->scan_part);
     cudaFree(ctx->sort_long);
+    for (int k = 0; k < 4; k++) {
+        if (ctx->gs4[k]) cudaStreamDestroy(ctx->gs4[k]);
+        if (ctx->ev_g_done[k]) cudaEventDestroy(ctx->ev_g_done[k]);
+    }
+    if (ctx->ev_g_fork) cudaEventDestroy(ctx->ev_g_fork);
     cudaFree(ctx->mprop);
     cudaFree(ctx->cellsum);
 }
@@ -583,15 +593,17 @@ int p2g_run(hmec_inst* ctx) {
     dim3 bb(64), gc(nblocks(g.Ny - 1, 64), g.Nx - 1);
     dim3 gb(nblocks(g.Ny, 64), g.Nx), gs(nblocks(g.Ny1, 64), g.Nx1);
     // the four grids' gathers are independent: each pair (cell sums, node
-    // sums) on its own stream when the solver's level streams exist
-    Solver& sv = ctx->sv;
+    // sums) on a stream of its own (streams of this section only: the
+    // solver's level streams join the capture of a global iteration's body
+    // when the timestep is captured as a graph, and a stream belongs to one
+    // capture at a time)
     const cudaStream_t main = ctx->stream;
-    const bool par = sv.aux.size() >= 4 && sv.ev_fork;
-    if (par) HMEC_CUDA(ctx, cudaEventRecord(sv.ev_fork, main));
+    HMEC_CUDA(ctx, cudaEventRecord(ctx->ev_g_fork, main));
+    cudaError_t fork_err = cudaSuccess;
     auto on = [&](int k) {
-        if (!par) return main;
-        cudaStreamWaitEvent(sv.aux[k], sv.ev_fork, 0);
-        return sv.aux[k];
+        const cudaError_t e = cudaStreamWaitEvent(ctx->gs4[k], ctx->ev_g_fork, 0);
+        if (e != cudaSuccess) fork_err = e;
+        return ctx->gs4[k];
     };
     {
         StreamScope scope(ctx, on(0));
@@ -617,11 +629,11 @@ int p2g_run(hmec_inst* ctx) {
         HMEC_LAUNCH(ctx, k_node_vy, gs, bb, 0, g, cs_y, f[HMEC_F_RHOY], f[HMEC_F_ETADY], f[HMEC_F_RHOFY],
                     f[HMEC_F_PORY]);
     }
-    if (par)
-        for (int k = 0; k < 4; k++) {
-            HMEC_CUDA(ctx, cudaEventRecord(sv.ev_done[k], sv.aux[k]));
-            HMEC_CUDA(ctx, cudaStreamWaitEvent(main, sv.ev_done[k], 0));
-        }
+    HMEC_CUDA(ctx, fork_err);
+    for (int k = 0; k < 4; k++) {
+        HMEC_CUDA(ctx, cudaEventRecord(ctx->ev_g_done[k], ctx->gs4[k]));
+        HMEC_CUDA(ctx, cudaStreamWaitEvent(main, ctx->ev_g_done[k], 0));
+    }
     HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;
 }

@@ -1780,6 +1780,8 @@ static int alloc_level(hmec_inst* ctx, Level& L, bool mixed, bool coarse) {
         HMEC_CUDA(ctx, cudaMalloc(&L.dx_, sizeof(double) * N));
         HMEC_CUDA(ctx, cudaMalloc(&L.dx2, sizeof(double) * N));
         HMEC_CUDA(ctx, cudaMalloc(&L.dr, sizeof(double) * std::max(N, (size_t)L.nbnd)));
+        // the fine level's fixed preconditioner input (device-controlled solve)
+        if (!coarse) HMEC_CUDA(ctx, cudaMalloc(&L.pb, sizeof(double) * N));
     }
     {
         // tile ownership of every unknown (the tiled smoothing pass)
@@ -2009,6 +2011,7 @@ void solver_free(hmec_inst* ctx) {
         cudaFree(L.pinv);
         cudaFree(L.pinv32);
         cudaFree(L.dx_);
+        cudaFree(L.pb);
         cudaFree(L.db);
         cudaFree(L.dr);
         cudaFree(L.fx);
@@ -2465,6 +2468,10 @@ static int vcycle(hmec_inst* ctx, size_t l, const T* b_in = nullptr, T* x_in = n
     const hmec_params& p = ctx->p;
     const T* b = b_in ? b_in : LvPtr<T>::b(L);
     T* x = x_in ? x_in : LvPtr<T>::x(L);
+    if (!b || !x) {
+        ctx->err = "vcycle: a level vector is missing";
+        return HMEC_ERR_STATE;
+    }
     int rc;
     if (l + 1 == sv.lv.size()) {
         const int ns = (sv.lv.size() == 1) ? std::max(1, p.mg_pre + p.mg_post) : std::max(1, p.mg_coarse_sweeps);
@@ -2656,6 +2663,11 @@ int solver_capture_solve(hmec_inst* ctx, cudaStream_t s_restart, cudaStream_t s_
     const int maxit = std::max(1, ctx->p.krylov_maxit);
     const bool mixed = ctx->p.form == HMEC_FORM_MIXED;
     Gm G{sv.H, sv.cs, sv.sn, sv.gvec, sv.yvec, sv.dots, sv.bnorm, sv.done, sv.kcur, ctx->ds};
+    // the fixed buffers the captured preconditioner reads and writes
+    if (mixed ? (!L0.fb || !L0.fx) : (!L0.pb || !L0.dx_)) {
+        ctx->err = "solver_capture_solve: a preconditioner buffer is missing";
+        return HMEC_ERR_STATE;
+    }
     cudaGraphConditionalHandle hr = 0, hi = 0;
     int rc = graph_handle(ctx, ctx->stream, &hr);
     if (rc) return rc;

@@ -63,10 +63,10 @@ class Ensemble:
         out = [[] for _ in range(n)]
         reps = (StepReport * n)()
         for _ in range(nsteps):
-            rc = self.L.hmec_timestep(self._h, reps)
+            self.L.hmec_timestep(self._h, reps)
             for k in range(n):
                 d = {f: getattr(reps[k], f) for f, _ in StepReport._fields_}
-                d["rc"] = d["status"] if d["status"] else (rc if rc and n == 1 else 0)
+                d["rc"] = d["status"]  # the member's own first non-OK status of the step
                 out[k].append(d)
         return out
 

@@ -56,21 +56,22 @@ def test_driver_writes_reference_outputs(tmp_path):
             ref = o.field(name)[lf]
             got = np.array([float(v) for v in row.split()])
             assert got.shape == ref.shape, (f, s)
-            # %g keeps six significant digits
-            assert np.allclose(got, ref, rtol=2e-6, atol=1e-300), (f, s, got, ref)
-            assert float(head[0]) == pytest.approx(o.scalar("timesum"), rel=2e-6), (f, s)
+            # %g keeps six significant digits: half a unit of the sixth is
+            # up to 5e-6 relative
+            assert np.allclose(got, ref, rtol=1e-5, atol=1e-300), (f, s, got, ref)
+            assert float(head[0]) == pytest.approx(o.scalar("timesum"), rel=1e-5), (f, s)
             # the Eigen layout of the printed values
             assert row == eigen_row(got), (f, s, row)
     # step 1 files
     x = [float(v) for v in open(os.path.join(tmp_path, "x_fault.txt")).read().split()]
-    assert np.allclose(x, synth.linspaced(Nx, 0, xs), rtol=2e-6)
+    assert np.allclose(x, synth.linspaced(Nx, 0, xs), rtol=1e-5)
     xt = open(os.path.join(tmp_path, "x_fault.txt")).read()
     assert xt == eigen_row(np.array(x), column=True) + "\n"
     rsf = open(os.path.join(tmp_path, "rsf_fault.txt")).read().split("\n\n")
     assert len(rsf) == 3
     for part, name in zip(rsf, ("ARSF", "BRSF", "LRSF")):
         got = np.array([float(v) for v in part.split()])
-        assert np.allclose(got, o.field(name)[lf], rtol=2e-6), name
+        assert np.allclose(got, o.field(name)[lf], rtol=1e-5), name
 
 
 def test_download_rows_equals_field_rows():
