@@ -182,6 +182,7 @@ void hmec_params_default(hmec_params* p) {
     p->bounds_check = 0;
     p->mg_flags = 1; /* HMEC_MG_DARCY_HARMONIC */
     p->graph = 1;
+    p->autotune = 1;
 }
 
 #define HMEC_X_NAME(name, grid) #name,
@@ -253,9 +254,18 @@ static const char* params_problem(const hmec_params& p) {
     return nullptr;
 }
 
+// A block size from a tuned value: a multiple of 32 in [32, 1024], or dflt.
+static int block_size(int v, int dflt) {
+    if (v <= 0) return dflt;
+    v = (v + 31) / 32 * 32;
+    return v < 32 ? 32 : (v > 1024 ? 1024 : v);
+}
+
 static int create_inner(hmec_inst* ctx) {
     const hmec_params& p = ctx->p;
     if (const char* why = params_problem(p)) return fail(ctx, HMEC_ERR_ARG, why);
+    ctx->bs_st = block_size(p.bs_stencil, 64);
+    ctx->bs_so = block_size(p.bs_sort, 256);
     HMEC_CUDA(ctx, cudaGetDevice(&ctx->dev));
     HMEC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     Geo& g = ctx->g;
@@ -730,6 +740,7 @@ hmec_ctx* hmec_create(const hmec_params* p, int32_t n_instances, const hmec_grid
         // members of an ensemble share the GPU: one launch per smoothing
         // pass on a share of the SMs (HMEC_MG_PASS_LAUNCHES)
         if (n_instances > 1) q.mg_flags |= HMEC_MG_PASS_LAUNCHES;
+        if (q.autotune) hmec_tune_apply(&q);
         if (const char* why = params_problem(q)) {
             fprintf(stderr, "hmec_create: instance %d: %s\n", (int)k, why);
             delete E;

@@ -249,6 +249,7 @@ struct hmec_inst {
     std::string err;
     GraphState gr;
     double* rowbuf = nullptr;  // hmec_download_rows staging (64 rows of Nx+1)
+    int bs_st = 64, bs_so = 256;  // threads per block: node-stencil kernels, marker kernels
 };
 
 // The ABI's context: n model instances -- one for a single model, the
@@ -443,6 +444,9 @@ int solver_capture_solve(hmec_inst* ctx, cudaStream_t s_restart, cudaStream_t s_
 // the graph is off for this context and the caller runs the host-driven step.
 int graph_timestep(hmec_inst* ctx, hmec_step_report* rep, bool* used);
 void graph_free(hmec_inst* ctx);
+// The tuning table's entry for p's grid and form applied to p (hmec_tune.cu);
+// 1 when one was applied.
+int hmec_tune_apply(hmec_params* p);
 // One timestep of every member of an ensemble as one graph launch (built on
 // first use, once every member has run a host-driven step); *used false:
 // the caller steps the members one by one.

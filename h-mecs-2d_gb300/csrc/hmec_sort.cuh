@@ -335,6 +335,7 @@ struct SortBufs {
     int32_t *key, *count, *start, *fill, *part, *perm;
     int* long_flag;
     int32_t* radix;
+    int bs = 256;  // threads per block of the scatter
 };
 
 // Co-resident blocks of k_radix_sort (cached per process; one GPU type).
@@ -360,7 +361,8 @@ inline cudaError_t sort_by_half_cell(cudaStream_t s, const SortBufs& b, int64_t 
     k_scan1<<<nparts, 1024, 0, s>>>(b.count, ns, b.start, b.part);
     k_scan2<<<1, 1024, 0, s>>>(b.part, nparts);
     k_scan3<<<nblocks(ns, 256), 256, 0, s>>>(b.start, ns, b.part, b.fill);
-    k_scatter<<<nblocks(n, 256), 256, 0, s>>>(b.key, n, b.fill, b.perm);
+    const int bs = b.bs > 0 ? b.bs : 256;
+    k_scatter<<<nblocks(n, bs), bs, 0, s>>>(b.key, n, b.fill, b.perm);
     cudaError_t e = cudaMemsetAsync(b.long_flag, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
     k_segsort<<<nblocks(nh, 128), 128, 0, s>>>(b.start, nh, b.perm, b.long_flag);

@@ -1070,13 +1070,13 @@ __global__ void k_next_step(DevScalars* ds) { ds->timestep += 1; }
 
 // =================================================================== host
 
-static inline dim3 grid_b(const Geo& g) { return dim3(nblocks(g.Ny, 64), g.Nx); }
-static inline dim3 grid_s(const Geo& g) { return dim3(nblocks(g.Ny1, 64), g.Nx1); }
+static inline dim3 grid_b(const Geo& g, int bs) { return dim3(nblocks(g.Ny, bs), g.Nx); }
+static inline dim3 grid_s(const Geo& g, int bs) { return dim3(nblocks(g.Ny1, bs), g.Nx1); }
 
 int step_begin(hmec_inst* ctx) {
     const Geo& g = ctx->g;
     double* const* f = ctx->f;
-    HMEC_LAUNCH(ctx, k_step_begin, grid_b(g), 64, 0, g, ctx->ds, ctx->p, f[HMEC_F_ETA0], f[HMEC_F_ETA00],
+    HMEC_LAUNCH(ctx, k_step_begin, grid_b(g, ctx->bs_st), ctx->bs_st, 0, g, ctx->ds, ctx->p, f[HMEC_F_ETA0], f[HMEC_F_ETA00],
                 f[HMEC_F_OM0], f[HMEC_F_ETA1], f[HMEC_F_ETA], f[HMEC_F_ETA50], f[HMEC_F_OM]);
     HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;
@@ -1085,23 +1085,23 @@ int step_begin(hmec_inst* ctx) {
 int iter_prepare(hmec_inst* ctx) {
     const Geo& g = ctx->g;
     double* const* f = ctx->f;
-    HMEC_LAUNCH(ctx, k_copy_bounds, grid_s(g), 64, 0, g, f[HMEC_F_pt], f[HMEC_F_pf]);
-    HMEC_LAUNCH(ctx, k_prep_basic, grid_b(g), 64, 0, g, ctx->ds, ctx->p, f[HMEC_F_ETA], f[HMEC_F_ETA0],
+    HMEC_LAUNCH(ctx, k_copy_bounds, grid_s(g, ctx->bs_st), ctx->bs_st, 0, g, f[HMEC_F_pt], f[HMEC_F_pf]);
+    HMEC_LAUNCH(ctx, k_prep_basic, grid_b(g, ctx->bs_st), ctx->bs_st, 0, g, ctx->ds, ctx->p, f[HMEC_F_ETA], f[HMEC_F_ETA0],
                 f[HMEC_F_SXX], f[HMEC_F_SYY], f[HMEC_F_SXY], f[HMEC_F_SIIB], f[HMEC_F_IETAPLB], f[HMEC_F_EIIB]);
-    HMEC_LAUNCH(ctx, k_prep_p, grid_s(g), 64, 0, g, ctx->ds, ctx->p, f[HMEC_F_IETAPLB], f[HMEC_F_YNY0],
+    HMEC_LAUNCH(ctx, k_prep_p, grid_s(g, ctx->bs_st), ctx->bs_st, 0, g, ctx->ds, ctx->p, f[HMEC_F_IETAPLB], f[HMEC_F_YNY0],
                 f[HMEC_F_ETAP0], f[HMEC_F_ETAB0], f[HMEC_F_POR], f[HMEC_F_GGGP], f[HMEC_F_ETAP], f[HMEC_F_ETAB],
                 f[HMEC_F_GGGB], f[HMEC_F_DILP]);
     const int nb = 152;
     HMEC_LAUNCH(ctx, k_min_etadx, nb, 256, 0, g, f[HMEC_F_ETADX], ctx->red, ctx->ds, ctx->ticket);
-    HMEC_LAUNCH(ctx, k_rescale_guess, grid_s(g), 64, 0, g, ctx->ds, ctx->S);
+    HMEC_LAUNCH(ctx, k_rescale_guess, grid_s(g, ctx->bs_st), ctx->bs_st, 0, g, ctx->ds, ctx->S);
     HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;
 }
 
 void launch_assemble(hmec_inst* ctx, const Geo& g, const AsmFields& af, int32_t* col, double* val, double* dscale,
                      double* rhs_scaled, double* rhs_raw, const double*) {
-    const dim3 grid(nblocks(g.Ny1, 64), g.Nx1, 6);  // z: the six rows of a cell
-    HMEC_LAUNCH(ctx, k_assemble, grid, 64, 0, g, af, ctx->ds, ctx->p, col, val, dscale, rhs_scaled, rhs_raw);
+    const dim3 grid(nblocks(g.Ny1, ctx->bs_st), g.Nx1, 6);  // z: the six rows of a cell
+    HMEC_LAUNCH(ctx, k_assemble, grid, ctx->bs_st, 0, g, af, ctx->ds, ctx->p, col, val, dscale, rhs_scaled, rhs_raw);
 }
 
 int iter_assemble(hmec_inst* ctx) {
@@ -1115,13 +1115,13 @@ int iter_finish(hmec_inst* ctx) {
     const Geo& g = ctx->g;
     double* const* f = ctx->f;
     int* status = &ctx->ds->status;
-    HMEC_LAUNCH(ctx, k_reload, grid_s(g), 64, 0, g, ctx->ds, ctx->S, f[HMEC_F_pt], f[HMEC_F_vxs], f[HMEC_F_vys],
+    HMEC_LAUNCH(ctx, k_reload, grid_s(g, ctx->bs_st), ctx->bs_st, 0, g, ctx->ds, ctx->S, f[HMEC_F_pt], f[HMEC_F_vxs], f[HMEC_F_vys],
                 f[HMEC_F_pf], f[HMEC_F_vxD], f[HMEC_F_vyD], status);
     HMEC_LAUNCH(ctx, k_vmax, 152, 256, 0, g, f[HMEC_F_VSLIPB], ctx->ds, ctx->red + 2048, ctx->ticket + 1);
-    HMEC_LAUNCH(ctx, k_stress_basic, grid_b(g), 64, 0, g, ctx->ds, f[HMEC_F_vxs], f[HMEC_F_vys], f[HMEC_F_GGG],
+    HMEC_LAUNCH(ctx, k_stress_basic, grid_b(g, ctx->bs_st), ctx->bs_st, 0, g, ctx->ds, f[HMEC_F_vxs], f[HMEC_F_vys], f[HMEC_F_GGG],
                 f[HMEC_F_ETA], f[HMEC_F_SXY0], f[HMEC_F_EXY], f[HMEC_F_SXY], f[HMEC_F_ETA0], f[HMEC_F_ETA5],
                 f[HMEC_F_DSY], f[HMEC_F_YNY], f[HMEC_F_SigmaY], f[HMEC_F_SII_fault], f[HMEC_F_OM], f[HMEC_F_OM5]);
-    HMEC_LAUNCH(ctx, k_stress_p, grid_s(g), 64, 0, g, ctx->ds, f[HMEC_F_vxs], f[HMEC_F_vys], f[HMEC_F_GGGP],
+    HMEC_LAUNCH(ctx, k_stress_p, grid_s(g, ctx->bs_st), ctx->bs_st, 0, g, ctx->ds, f[HMEC_F_vxs], f[HMEC_F_vys], f[HMEC_F_GGGP],
                 f[HMEC_F_ETAP], f[HMEC_F_SXX0], f[HMEC_F_SYY0], f[HMEC_F_EXX], f[HMEC_F_EYY], f[HMEC_F_SXX],
                 f[HMEC_F_SYY]);
     RsfIn in{f[HMEC_F_ARSF], f[HMEC_F_BRSF], f[HMEC_F_LRSF], f[HMEC_F_FRIC], f[HMEC_F_ETA0], f[HMEC_F_SXX],
@@ -1134,7 +1134,7 @@ int iter_finish(hmec_inst* ctx) {
     const int nb = 152;
     HMEC_LAUNCH(ctx, k_reduce_vel, nb, 256, 0, g, ctx->p, ctx->crd[3], ctx->crd[5], f[HMEC_F_vxs], f[HMEC_F_vys],
                 f[HMEC_F_VSLIPB], ctx->red, rsfbuf, ctx->ds, ctx->ticket + 2);
-    HMEC_LAUNCH(ctx, k_eta_update, grid_b(g), 64, 0, g, ctx->ds, ctx->p, f[HMEC_F_ETA], f[HMEC_F_ETA5],
+    HMEC_LAUNCH(ctx, k_eta_update, grid_b(g, ctx->bs_st), ctx->bs_st, 0, g, ctx->ds, ctx->p, f[HMEC_F_ETA], f[HMEC_F_ETA5],
                 f[HMEC_F_ETA0], f[HMEC_F_ETA50], f[HMEC_F_YNY0], f[HMEC_F_YNY], f[HMEC_F_OM], f[HMEC_F_OM5]);
     HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;
@@ -1144,7 +1144,7 @@ int step_end(hmec_inst* ctx) {
     const Geo& g = ctx->g;
     double* const* f = ctx->f;
     HMEC_LAUNCH(ctx, k_end_scalars, 1, 1, 0, ctx->ds);
-    HMEC_LAUNCH(ctx, k_post_basic, grid_b(g), 64, 0, g, ctx->ds, f[HMEC_F_vxs], f[HMEC_F_vys], f[HMEC_F_GGG],
+    HMEC_LAUNCH(ctx, k_post_basic, grid_b(g, ctx->bs_st), ctx->bs_st, 0, g, ctx->ds, f[HMEC_F_vxs], f[HMEC_F_vys], f[HMEC_F_GGG],
                 f[HMEC_F_ETA], f[HMEC_F_SXY0], f[HMEC_F_ESP], f[HMEC_F_EXY], f[HMEC_F_SXY], f[HMEC_F_ETA50],
                 f[HMEC_F_ETA00], f[HMEC_F_OM], f[HMEC_F_OM0]);
     PostP P{f[HMEC_F_vxs], f[HMEC_F_vys], f[HMEC_F_GGGP], f[HMEC_F_ETAP], f[HMEC_F_SXX0], f[HMEC_F_SYY0],
@@ -1152,14 +1152,14 @@ int step_end(hmec_inst* ctx) {
             f[HMEC_F_ETAB], f[HMEC_F_POR], f[HMEC_F_GGGB], f[HMEC_F_EXX], f[HMEC_F_EYY], f[HMEC_F_SXX],
             f[HMEC_F_SYY], f[HMEC_F_EII], f[HMEC_F_EIIVP], f[HMEC_F_SII], f[HMEC_F_DIS], f[HMEC_F_pt_ave],
             f[HMEC_F_pf_ave], f[HMEC_F_VIS_COMP], f[HMEC_F_EL_DECOM]};
-    HMEC_LAUNCH(ctx, k_post_p, grid_s(g), 64, 0, g, ctx->ds, ctx->p, P);
+    HMEC_LAUNCH(ctx, k_post_p, grid_s(g, ctx->bs_st), ctx->bs_st, 0, g, ctx->ds, ctx->p, P);
     HMEC_LAUNCH(ctx, k_monitors, 152, 256, 0, g, ctx->ds, f[HMEC_F_RHOX], f[HMEC_F_RHOY], f[HMEC_F_vxs], f[HMEC_F_vys],
                 ctx->red + 2048, ctx->ticket + 3);
     Roll R{f[HMEC_F_vxs], f[HMEC_F_vys], f[HMEC_F_vxD], f[HMEC_F_vyD], f[HMEC_F_PORX], f[HMEC_F_PORY],
            f[HMEC_F_SXX], f[HMEC_F_SYY], f[HMEC_F_SXY], f[HMEC_F_pt], f[HMEC_F_pf], f[HMEC_F_VX0], f[HMEC_F_VY0],
            f[HMEC_F_VXF0], f[HMEC_F_VYF0], f[HMEC_F_SXX0], f[HMEC_F_SYY0], f[HMEC_F_SXY0], f[HMEC_F_PTF0],
            f[HMEC_F_PT0], f[HMEC_F_PF0]};
-    HMEC_LAUNCH(ctx, k_rollover, grid_s(g), 64, 0, g, R);
+    HMEC_LAUNCH(ctx, k_rollover, grid_s(g, ctx->bs_st), ctx->bs_st, 0, g, R);
     HMEC_LAUNCH(ctx, k_next_step, 1, 1, 0, ctx->ds);
     HMEC_CUDA(ctx, cudaGetLastError());
     return HMEC_OK;

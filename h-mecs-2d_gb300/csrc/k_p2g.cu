@@ -553,11 +553,11 @@ int p2g_run(hmec_inst* ctx) {
     const int nh = ctx->nhalf;
     int* status = &ctx->ds->status;
     HMEC_CUDA(ctx, cudaMemsetAsync(ctx->hc_count, 0, sizeof(int32_t) * ((size_t)nh + 1), ctx->stream));
-    HMEC_LAUNCH(ctx, hsort::k_keys, nblocks(n, 256), 256, 0, ctx->mk[HMEC_M_xm], ctx->mk[HMEC_M_ym], n, g, ctx->mkey,
+    HMEC_LAUNCH(ctx, hsort::k_keys, nblocks(n, ctx->bs_so), ctx->bs_so, 0, ctx->mk[HMEC_M_xm], ctx->mk[HMEC_M_ym], n, g, ctx->mkey,
                 ctx->hc_count, status);
     // segment starts hc_start[0..nh], the scatter, the per-segment order
     hsort::SortBufs sb{ctx->mkey, ctx->hc_count, ctx->hc_start, ctx->hc_fill, ctx->scan_part, ctx->perm,
-                       ctx->sort_long, reinterpret_cast<int32_t*>(ctx->mprop)};
+                       ctx->sort_long, reinterpret_cast<int32_t*>(ctx->mprop), ctx->bs_so};
     HMEC_CUDA(ctx, hsort::sort_by_half_cell(ctx->stream, sb, n, nh, &ctx->launches));
     MkPtrs mk;
     mk.xm = ctx->mk[HMEC_M_xm];
@@ -577,7 +577,7 @@ int p2g_run(hmec_inst* ctx) {
     mk.rhofm = ctx->mk[HMEC_M_rhofm];
     mk.etafm = ctx->mk[HMEC_M_etafm];
     Crd c{ctx->crd[0], ctx->crd[1], ctx->crd[2], ctx->crd[3], ctx->crd[4], ctx->crd[5], ctx->crd[6], ctx->crd[7]};
-    HMEC_LAUNCH(ctx, k_mprop, nblocks(n, 256), 256, 0, mk, ctx->perm, ctx->mkey, n, g, c, ctx->p, 1.0 / ctx->p.POR0,
+    HMEC_LAUNCH(ctx, k_mprop, nblocks(n, ctx->bs_so), ctx->bs_so, 0, mk, ctx->perm, ctx->mkey, n, g, c, ctx->p, 1.0 / ctx->p.POR0,
                 ctx->mprop);
     double* const* f = ctx->f;
     // pass 1: corner sums per cell of each grid; pass 2: node sums and the a4 epilogues
@@ -590,8 +590,9 @@ int p2g_run(hmec_inst* ctx) {
     const float* rec_p = rec_b + (size_t)n * REC_B;
     const float* rec_x = rec_p + (size_t)n * REC_P;
     const float* rec_y = rec_x + (size_t)n * REC_X;
-    dim3 bb(64), gc(nblocks(g.Ny - 1, 64), g.Nx - 1);
-    dim3 gb(nblocks(g.Ny, 64), g.Nx), gs(nblocks(g.Ny1, 64), g.Nx1);
+    const int bs = ctx->bs_st;
+    dim3 bb(bs), gc(nblocks(g.Ny - 1, bs), g.Nx - 1);
+    dim3 gb(nblocks(g.Ny, bs), g.Nx), gs(nblocks(g.Ny1, bs), g.Nx1);
     // the four grids' gathers are independent: each pair (cell sums, node
     // sums) on a stream of its own (streams of this section only: the
     // solver's level streams join the capture of a global iteration's body

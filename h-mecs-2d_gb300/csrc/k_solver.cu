@@ -1896,7 +1896,12 @@ int solver_alloc(hmec_inst* ctx) {
     const bool mixed = p.form == HMEC_FORM_MIXED;
     sv.m = std::max(2, p.krylov_restart);
     sv.N = ctx->g.N;
-    sv.nblk = 152 * 2;
+    {
+        // Arnoldi blocks: the tuned count, else two per SM
+        int nsm = 0;
+        HMEC_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
+        sv.nblk = p.krylov_blocks > 0 ? std::min(p.krylov_blocks, 65536) : 2 * std::max(1, nsm);
+    }
     // levels: ceil-halve the cell counts while the coarse grid keeps >= 4 cells per side
     Level L0;
     L0.g = ctx->g;
@@ -2090,8 +2095,8 @@ int solver_setup(hmec_inst* ctx) {
                    (double*)a.ETAB, (double*)a.POR, (double*)a.GGGB, (double*)a.RHOX, (double*)a.RHOFX,
                    (double*)a.PORX, (double*)a.ETADX, (double*)a.RHOY, (double*)a.RHOFY, (double*)a.PORY,
                    (double*)a.ETADY};
-        const dim3 cg4(nblocks(L.g.Ny1, 64), L.g.Nx1, 4);  // z: basic, P, Vx, Vy sections
-        HMEC_LAUNCH(ctx, k_coarsen_coef, cg4, 64, 0, F.g, L.g, ci, co, ctx->p.mg_flags);
+        const dim3 cg4(nblocks(L.g.Ny1, ctx->bs_st), L.g.Nx1, 4);  // z: basic, P, Vx, Vy sections
+        HMEC_LAUNCH(ctx, k_coarsen_coef, cg4, ctx->bs_st, 0, F.g, L.g, ci, co, ctx->p.mg_flags);
         HMEC_CUDA(ctx, cudaEventRecord(sv.ev_coef[l], main));
     }
     for (size_t l = 0; l < sv.lv.size(); l++) {
@@ -2202,6 +2207,7 @@ static int stage_config(hmec_inst* ctx, Level& L) {
     const int w = blocks[1] > 0 ? 1 : 0;
     L.st_whole = w;
     L.st_grid = std::min(L.ntiles, blocks[w]);
+    if (ctx->p.smooth_blocks > 0) L.st_grid = std::min(L.st_grid, ctx->p.smooth_blocks);
     // models that share the GPU (ensembles) take at most a quarter of it per
     // pass, so that four members' passes run side by side instead of each
     // large level holding every SM in turn

@@ -61,6 +61,8 @@ class Params(C.Structure):
         ("mg_coarse_sweeps", C.c_int32), ("rsf_maxit", C.c_int32), ("advect_markers", C.c_int32),
         ("rk4_as_written", C.c_int32), ("quirk_accumulate_sums", C.c_int32), ("bounds_check", C.c_int32),
         ("mg_flags", C.c_int32), ("graph", C.c_int32),
+        ("bs_stencil", C.c_int32), ("bs_sort", C.c_int32), ("krylov_blocks", C.c_int32),
+        ("smooth_blocks", C.c_int32), ("autotune", C.c_int32),
     ]
 
 
@@ -107,7 +109,7 @@ EXPORTS = ["hmec_abi_version", "hmec_params_default", "hmec_field_name", "hmec_f
            "hmec_global_iteration", "hmec_timestep_end", "hmec_advect_markers", "hmec_timestep",
            "hmec_assemble_csr", "hmec_solve_system", "hmec_kernel_launches", "hmec_synchronize", "hmec_stream",
            "hmec_profile_kernel", "hmec_profile_read", "hmec_markers_to_nodes_noalloc", "hmec_cell_index",
-           "hmec_graph_status"]
+           "hmec_graph_status", "hmec_tune_params"]
 
 _lib = None
 
@@ -180,6 +182,8 @@ def load(build_if_missing: bool = True):
     L.hmec_markers_to_nodes_noalloc.restype = i32
     L.hmec_cell_index.argtypes = [P(C.c_double), C.c_int64, C.c_double, i32, P(i32)]
     L.hmec_cell_index.restype = i32
+    L.hmec_tune_params.argtypes = [P(Params)]
+    L.hmec_tune_params.restype = i32
     _lib = L
     return L
 

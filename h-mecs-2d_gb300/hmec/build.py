@@ -16,7 +16,7 @@ SRC = os.path.join(os.path.dirname(PKG), "csrc")
 INC = os.path.join(os.path.dirname(os.path.dirname(PKG)), "include")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libhmec_gpu.so")
-UNITS = ["hmec_api.cu", "hmec_graph.cu", "k_p2g.cu", "k_iter.cu", "k_solver.cu", "k_advect.cu", "k_p2g_static.cu"]
+UNITS = ["hmec_api.cu", "hmec_graph.cu", "hmec_tune.cu", "k_p2g.cu", "k_iter.cu", "k_solver.cu", "k_advect.cu", "k_p2g_static.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -108,6 +108,16 @@ typedef struct hmec_params {
     int32_t graph;            /* 1: hmec_timestep runs a whole step as one CUDA graph launch, its
                                  loops (global iterations, FGMRES restarts, Arnoldi steps) as
                                  conditional nodes decided on the device; 0: host-driven launches */
+    /* launch shapes (0: the library's default) and the tuning table */
+    int32_t bs_stencil;       /* threads per block of the node-stencil kernels (64) */
+    int32_t bs_sort;          /* threads per block of the marker key, scatter and property kernels (256) */
+    int32_t krylov_blocks;    /* blocks of the cooperative Arnoldi step (two per SM) */
+    int32_t smooth_blocks;    /* most blocks of one smoothing launch (every co-resident block) */
+    int32_t autotune;         /* 1: at hmec_create, take mg_levels, mg_pre, mg_post,
+                                 mg_coarse_sweeps and the launch shapes above from the tuning
+                                 table entry of this form nearest this grid (the table of
+                                 hmec/tune.py: $HMEC_TUNE_TABLE, else tune_table.json beside the
+                                 library's package), when there is one within 4x in cells */
 } hmec_params;
 
 /* mg_flags bits */
@@ -209,6 +219,11 @@ const char* hmec_marker_name(int32_t field);
 const char* hmec_scalar_name(int32_t id);
 /* Marker count of the lattice: (Nx-1)*mx * (Ny-1)*my (constants.hpp:81-85). */
 int64_t hmec_marknum(const hmec_params* p);
+/* What hmec_create does with p->autotune set, without creating anything:
+ * overwrite p's cycle shape and launch shapes with the tuning table's entry
+ * for p's form nearest p's grid.  1 if an entry was applied, 0 if none (no
+ * table, or none within 4x in cells).  No counterpart in the reference.     */
+int32_t hmec_tune_params(hmec_params* p);
 
 /* --------------------------------------------------------------- lifecycle */
 /* The grid of one instance: the fields of hmec_params it overrides. */

@@ -149,6 +149,7 @@ void hmo_params_default(hmec_params* p) {
     p->bounds_check = 0;
     p->mg_flags = 1; /* HMEC_MG_DARCY_HARMONIC */
     p->graph = 1;
+    p->autotune = 1;
 }
 
 /* Eigen 3.3 LinSpaced(n, low, high) for |high| >= |low| (all grids here). */

@@ -50,6 +50,8 @@ class HmecParams(C.Structure):
         ("mg_coarse_sweeps", C.c_int32), ("rsf_maxit", C.c_int32), ("advect_markers", C.c_int32),
         ("rk4_as_written", C.c_int32), ("quirk_accumulate_sums", C.c_int32), ("bounds_check", C.c_int32),
         ("mg_flags", C.c_int32), ("graph", C.c_int32),
+        ("bs_stencil", C.c_int32), ("bs_sort", C.c_int32), ("krylov_blocks", C.c_int32),
+        ("smooth_blocks", C.c_int32), ("autotune", C.c_int32),
     ]
 
 

@@ -97,3 +97,36 @@ def test_no_cpu_fallback_in_product():
             if f.endswith((".py", ".cu", ".cuh", ".cpp", ".h")):
                 text = open(os.path.join(dirpath, f)).read()
                 assert "import oracle" not in text and "hmec_oracle" not in text, f
+
+
+def test_tuning_table_entry_nearest_in_cells(tmp_path, monkeypatch):
+    """hmec_tune_params applies the table entry of the same form nearest the
+    grid in cells (what hmec_create does with autotune set)."""
+    import json
+
+    table = {"version": 1, "entries": [
+        {"Nx": 201, "Ny": 201, "form": 1, "mg_levels": 4, "mg_pre": 1, "mg_post": 1, "mg_coarse_sweeps": 6,
+         "bs_stencil": 128, "bs_sort": 512, "krylov_blocks": 456, "smooth_blocks": 152, "ms_per_step": 1.0},
+        {"Nx": 201, "Ny": 201, "form": 0, "mg_levels": 6, "mg_pre": 2, "mg_post": 2, "mg_coarse_sweeps": 4,
+         "bs_stencil": 64, "bs_sort": 256, "krylov_blocks": 304, "smooth_blocks": 0},
+        {"Nx": 1001, "Ny": 401, "form": 1, "mg_levels": 3, "mg_pre": 2, "mg_post": 2, "mg_coarse_sweeps": 8,
+         "bs_stencil": 256, "bs_sort": 128, "krylov_blocks": 608, "smooth_blocks": 0, "note": "text is skipped"}]}
+    path = tmp_path / "table.json"
+    path.write_text(json.dumps(table))
+    monkeypatch.setenv("HMEC_TUNE_TABLE", str(path))
+    lib = hmec.load()
+    p = hmec.default_params(Nx=181, Ny=221, form=hmec.FORM_MIXED)
+    assert lib.hmec_tune_params(C.byref(p)) == 1
+    assert (p.mg_levels, p.mg_pre, p.mg_post, p.mg_coarse_sweeps) == (4, 1, 1, 6)
+    assert (p.bs_stencil, p.bs_sort, p.krylov_blocks, p.smooth_blocks) == (128, 512, 456, 152)
+    p = hmec.default_params(Nx=201, Ny=201, form=hmec.FORM_FP64)
+    assert lib.hmec_tune_params(C.byref(p)) == 1 and p.mg_levels == 6
+    p = hmec.default_params(Nx=901, Ny=451, form=hmec.FORM_MIXED)
+    assert lib.hmec_tune_params(C.byref(p)) == 1 and p.mg_levels == 3 and p.bs_stencil == 256
+    # nothing within 4x in cells: unchanged
+    p = hmec.default_params(Nx=41, Ny=41, form=hmec.FORM_MIXED)
+    assert lib.hmec_tune_params(C.byref(p)) == 0 and p.mg_levels == 5
+    # no table
+    monkeypatch.setenv("HMEC_TUNE_TABLE", str(tmp_path / "missing.json"))
+    p = hmec.default_params(Nx=201, Ny=201, form=hmec.FORM_MIXED)
+    assert lib.hmec_tune_params(C.byref(p)) == 0 and p.mg_levels == 5
