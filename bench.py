@@ -14,7 +14,7 @@ accuracy is measured against the FP64 CPU oracle) and configuration 3 (the
 64-member ensemble) as extra blocks.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--config c2|c1|c3] [--no-extra] [--no-cpu-baseline]
+                    [--config c2|c1|c3|c4] [--no-extra] [--no-cpu-baseline]
 
 --impl reference times the CPU restatement of the reference (the oracle: the
 reference itself needs Eigen, HDF5 and MKL Pardiso, none of which exist here)
@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4"])
     ap.add_argument("--no-extra", action="store_true", help="headline configuration only")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
@@ -465,6 +465,84 @@ def cpu_block(cfg, gi_per_step):
 
 
 # ------------------------------------------------------------------ ensembles
+def member_oracle_error(over, mat, seed, fields_after_step1):
+    """One member's first timestep on the FP64 oracle from the member's
+    initial state, against the ensemble's result for that member."""
+    import oracle as O
+    from hmec import synth
+
+    o = O.Oracle(O.default_params(**dict(over, krylov_rtol=1e-15)))
+    mk, nodes = synth.instance_state(o.params, mat, seed)
+    o.set_markers(mk)
+    for k, v in nodes.items():
+        o.set_field(k, v)
+    gi = o.timestep()
+    err = rel_errors(fields_after_step1, {k: o.field(k) for k in FIELDS_ACC})
+    return dict(err, **judged(err), Nx=over["Nx"], Ny=over["Ny"], prestress_pa=mat.get("prestress", 0.0),
+                oracle_global_iters=gi, oracle_dt=o.scalar("dt"))
+
+
+def run_c4(args, device_index=0):
+    """Configuration 4: 256 instances (101..401 x 101..201 nodes) at seeded
+    cycle phases in one context, one graph launch per ensemble step; the
+    aggregate member-timesteps/s, the instances' dt spread, and the errors of
+    sampled instances' first step against the FP64 oracle."""
+    import numpy as np
+    import torch
+
+    import hmec
+    from hmec import synth
+    from hmec.ensemble import Ensemble
+
+    torch.cuda.set_device(device_index)
+    members = synth.ensemble_members_c4(256)
+    common = dict(krylov_rtol=1e-15, krylov_restart=40, krylov_maxit=4000, form=hmec.FORM_MIXED)
+    t0 = time.perf_counter()
+    ens = Ensemble(members, **common)
+    t_create = time.perf_counter() - t0
+    # sampled instances: the smallest of each cycle phase
+    sample = {}
+    for k, (o, mat, sd) in enumerate(members):
+        ph = mat.get("prestress", 0.0)
+        if ph not in sample or o["Nx"] * o["Ny"] < members[sample[ph]][0]["Nx"] * members[sample[ph]][0]["Ny"]:
+            sample[ph] = k
+    first = ens.step(1)
+    after1 = {k: {f: ens.members[k].field(f) for f in FIELDS_ACC} for k in sample.values()}
+    ens.step(max(0, args.warmup - 1))
+    torch.cuda.synchronize()
+    l0 = ens.launches
+    with ClockSampler(device_index) as clk:
+        t0 = time.perf_counter()
+        reps = ens.step(args.steps)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+    launches = ens.launches - l0
+    dts = np.array([ens.members[k].scalar("dt") for k in range(len(members))])
+    graph = ens.graph_status
+    gi = sum(r["global_iters"] for rs in reps for r in rs)
+    bad = sum(1 for rs in reps for r in rs if r["rc"] != 0)
+    ens.close()
+    errs = [member_oracle_error(*members[k], after1[k]) for k in sample.values()]
+    K = args.steps
+    return {"value": len(members) * K / el, "unit": "member-timesteps/s", "ms_per_step": 1e3 * el / K, "steps": K,
+            "workload": "config 4: 256 instances, nodes 101-401 x 101-201, 4x4 markers/cell (%.0f M markers, "
+                        "%.1f M cells), seeded a/b/L/k and cycle phases (%s)"
+                        % (sum((o["Nx"] - 1) * (o["Ny"] - 1) * 16 for o, _, _ in members) / 1e6,
+                           sum((o["Nx"] + 1) * (o["Ny"] + 1) for o, _, _ in members) / 1e6,
+                           ", ".join("%d%% at %g MPa pre-stress" % (100 * f, t / 1e6) for f, t in synth.C4_PHASES)),
+            "form": "mixed, all instances in one context: one CUDA graph launch per ensemble step",
+            "step_as_one_graph_launch": graph == 1, "create_seconds": t_create,
+            "global_iters_per_member_step": gi / (len(members) * K), "failed_member_steps": bad,
+            "dt_after_timed_steps": {"min": float(dts.min()), "median": float(np.median(dts)),
+                                     "max": float(dts.max())},
+            "first_step_global_iters": {"min": min(r[0]["global_iters"] for r in first),
+                                        "max": max(r[0]["global_iters"] for r in first)},
+            "gpu_launches": launches, "clocks": clk.summary(),
+            "sampled_instances_vs_oracle": errs,
+            "sampled_note": "first timestep of the smallest instance of each cycle phase, ensemble result "
+                            "against the FP64 oracle from the same initial state"}
+
+
 def run_ensemble(args, rank=0, world=1, device_index=0, nmembers=64):
     """Configuration 3: 64 uneven members in one context, one graph launch per
     ensemble step (mixed form), against the same members run one after
@@ -673,6 +751,21 @@ def main():
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
+
+    if args.config == "c4":
+        blk = run_c4(args, dev)
+        line = {"metric": METRIC, "value": blk["value"], "unit": blk["unit"], "n_gpus": 1, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": blk["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic",
+                "config": {k: blk[k] for k in ("workload", "form", "global_iters_per_member_step",
+                                                "failed_member_steps", "dt_after_timed_steps",
+                                                "first_step_global_iters", "create_seconds")},
+                "gpu_launches": blk["gpu_launches"], "clocks": blk["clocks"],
+                "step_as_one_graph_launch": blk["step_as_one_graph_launch"],
+                "sampled_instances_vs_oracle": blk["sampled_instances_vs_oracle"],
+                "sampled_note": blk["sampled_note"]}
+        print(json.dumps(line))
+        return 0
 
     if args.config == "c3":
         out, members = run_ensemble(args, rank, world, dev)

@@ -234,6 +234,12 @@ def config_state(p, name: str, seed: int | None = None, mat: dict | None = None)
     yp = linspaced(p.Ny + 1, -d["dy"] / 2.0, p.ysize + d["dy"] / 2.0)
     prow = (yp > d["upper_block"]) & (yp < d["lower_block"])
     nodes["PF0"][prow, :] = p.PCONF * (1.0 + mat["overpressure"])
+    # a cycle-phase offset: a uniform shear pre-stress (the stress the
+    # previous step leaves, SXY0) -- above the fault's steady-state strength
+    # the first step starts a rupture (dt of milliseconds), below it the
+    # instance stays interseismic
+    if mat.get("prestress", 0.0) > 0.0:
+        nodes["SXY0"] = np.full((p.Ny, p.Nx), float(mat["prestress"]))
     return mk, nodes
 
 
@@ -265,6 +271,37 @@ def ensemble_members(n: int = 64, seed: int = 1003, side=(51, 301), mpc: int = 4
         kf = float(np.exp(np.log(1e-18) + rng.random() * (np.log(1e-14) - np.log(1e-18))))
         over = dict(base, Nx=nx, Ny=ny, mx=mpc, my=mpc, arsfm=(0.017, a), brsfm=(b, b), lrsfm=(L, L))
         mat = dict(MATERIALS["c0"], fault_k=(kf, kf))
+        out.append((over, mat, seed * 1000 + k))
+    return out
+
+
+#: configuration 4: cycle phases of the instances (fraction, uniform shear
+#: pre-stress in Pa): interseismic from rest, late interseismic, and in
+#: rupture from the first step (16 MPa exceeds the fault's steady-state
+#: strength of about 15.9 MPa at 1e-9 m/s under 24.6 MPa effective pressure)
+C4_PHASES = ((0.6, 0.0), (0.2, 14e6), (0.2, 16e6))
+
+
+def ensemble_members_c4(n: int = 256, seed: int = 1004):
+    """The instances of configuration 4: per-side node counts uniform in
+    101..401 (x) and 101..201 (y), 4 x 4 markers per cell, friction and
+    fault permeability drawn as in configuration 3, and a seeded cycle phase
+    per instance (C4_PHASES) so that some instances rupture while others
+    load interseismically."""
+    rng = np.random.default_rng(seed)
+    out = []
+    base = dict(PRESETS["c0"])
+    cum = np.cumsum([f for f, _ in C4_PHASES])
+    for k in range(n):
+        nx = int(rng.integers(101, 402))
+        ny = int(rng.integers(101, 202))
+        a = float(rng.uniform(0.008, 0.016))
+        b = float(rng.uniform(0.012, 0.020))
+        L = float(rng.uniform(0.005, 0.05))
+        kf = float(np.exp(np.log(1e-18) + rng.random() * (np.log(1e-14) - np.log(1e-18))))
+        phase = C4_PHASES[int(np.searchsorted(cum, rng.random() * cum[-1], side="right"))][1]
+        over = dict(base, Nx=nx, Ny=ny, mx=4, my=4, arsfm=(0.017, a), brsfm=(b, b), lrsfm=(L, L))
+        mat = dict(MATERIALS["c0"], fault_k=(kf, kf), prestress=phase)
         out.append((over, mat, seed * 1000 + k))
     return out
 
