@@ -349,8 +349,8 @@ static int32_t inst_upload_markers(hmec_inst* ctx, const double* const* fields, 
     if (n != ctx->marknum) return fail(ctx, HMEC_ERR_ARG, "marker count differs from (Nx-1)*mx*(Ny-1)*my");
     for (int k = 0; k < HMEC_M_COUNT; k++)
         if (!fields[k]) return fail(ctx, HMEC_ERR_ARG, "null marker array");
-    for (int k = 0; k < HMEC_M_COUNT; k++)
-        HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->mk[k], fields[k], sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+    int rc = p2g_store_markers(ctx, fields);
+    if (rc) return rc;
     HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return HMEC_OK;
 }
@@ -358,9 +358,8 @@ static int32_t inst_upload_markers(hmec_inst* ctx, const double* const* fields, 
 static int32_t inst_download_markers(hmec_inst* ctx, double* const* fields, int64_t n) {
     if (!ctx || !fields) return fail(ctx, HMEC_ERR_ARG, "null argument");
     if (n != ctx->marknum) return fail(ctx, HMEC_ERR_ARG, "marker count differs from (Nx-1)*mx*(Ny-1)*my");
-    for (int k = 0; k < HMEC_M_COUNT; k++)
-        if (fields[k])
-            HMEC_CUDA(ctx, cudaMemcpyAsync(fields[k], ctx->mk[k], sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+    int rc = p2g_load_markers(ctx, fields);
+    if (rc) return rc;
     HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return HMEC_OK;
 }

@@ -230,6 +230,8 @@ struct hmec_inst {
     int32_t* hc_fill;        // scatter cursors
     int32_t* scan_part;      // scan block partials
     int* sort_long;          // set when a half cell holds more markers than the per-segment sort takes
+    int32_t* mord;           // caller index of each stored marker (markers are stored in half-cell order)
+    size_t stage_off = 0;    // floats of mprop before the marker transfers' staging
     cudaStream_t gs4[4] = {nullptr, nullptr, nullptr, nullptr};  // the four grids' gathers
     cudaEvent_t ev_g_fork = nullptr, ev_g_done[4] = {nullptr, nullptr, nullptr, nullptr};
     float* mprop;            // sorted per-marker gather records of the four grids (double-float)
@@ -419,6 +421,9 @@ struct StreamScope {
 int p2g_alloc(hmec_inst* ctx);
 void p2g_free(hmec_inst* ctx);
 int p2g_run(hmec_inst* ctx);
+// Marker arrays in and out of the library's storage order (see k_p2g.cu).
+int p2g_store_markers(hmec_inst* ctx, const double* const* fields);
+int p2g_load_markers(hmec_inst* ctx, double* const* fields);
 int iter_prepare(hmec_inst* ctx);
 int iter_assemble(hmec_inst* ctx);
 int iter_finish(hmec_inst* ctx);

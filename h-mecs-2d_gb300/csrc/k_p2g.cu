@@ -499,6 +499,28 @@ extern "C" int32_t hmec_cell_index(const double* x, int64_t n, double d, int32_t
     return e == cudaSuccess ? HMEC_OK : HMEC_ERR_CUDA;
 }
 
+// ------------------------------------------------ marker storage order
+// The library keeps the marker arrays on the device in half-cell order (the
+// order of the sort below at upload time): the per-step gathers through the
+// sort permutation then read consecutive markers instead of scattered ones.
+// mord[k] is the caller's index of stored marker k; within a half cell the
+// stored order keeps increasing caller index, so every per-step sort yields
+// the same marker sequence -- and the same sums -- as caller order would.
+__global__ void k_iota(int32_t* a, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = (int32_t)i;
+}
+__global__ void k_gather_f64(const double* __restrict__ src, const int32_t* __restrict__ idx, int64_t n,
+                             double* __restrict__ dst) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[idx[i]];
+}
+__global__ void k_scatter_f64(const double* __restrict__ src, const int32_t* __restrict__ idx, int64_t n,
+                              double* __restrict__ dst) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[idx[i]] = src[i];
+}
+
 int p2g_alloc(hmec_inst* ctx) {
     const Geo& g = ctx->g;
     ctx->nhalf = 4 * (g.Nx - 1) * (g.Ny - 1);
@@ -511,6 +533,8 @@ int p2g_alloc(hmec_inst* ctx) {
     HMEC_CUDA(ctx, cudaMalloc(&ctx->hc_fill, sizeof(int32_t) * ((size_t)ctx->nhalf + 1)));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->scan_part, sizeof(int32_t) * ((size_t)nparts + 1)));
     HMEC_CUDA(ctx, cudaMalloc(&ctx->sort_long, sizeof(int)));
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->mord, sizeof(int32_t) * (size_t)std::max<int64_t>(n, 1)));
+    HMEC_LAUNCH(ctx, k_iota, nblocks(n, 256), 256, 0, ctx->mord, n);
     for (int k = 0; k < 4; k++) {
         HMEC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->gs4[k], cudaStreamNonBlocking));
         HMEC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_g_done[k], cudaEventDisableTiming));
@@ -521,9 +545,12 @@ int p2g_alloc(hmec_inst* ctx) {
     // needs about 3.5
     int rgrid = 1;
     HMEC_CUDA(ctx, hsort::radix_grid(&rgrid));
+    // ... and the marker transfers' staging (three FP64 arrays) past the sort's part
     const size_t rec = (size_t)REC_ALL * (size_t)n;
     const size_t need = hsort::radix_scratch_ints(n, rgrid);
-    HMEC_CUDA(ctx, cudaMalloc(&ctx->mprop, sizeof(float) * (rec > need ? rec : need)));
+    ctx->stage_off = (need + 3) / 4 * 4;  // floats; 16-byte aligned
+    const size_t stage_end = ctx->stage_off + 6 * (size_t)n;
+    HMEC_CUDA(ctx, cudaMalloc(&ctx->mprop, sizeof(float) * std::max(rec, stage_end)));
     // corner sums: (10 + 5 + 4 + 4 properties + 4 weights) x 4 corners per cell
     const size_t ncell = (size_t)(g.Ny - 1) * (g.Nx - 1);
     HMEC_CUDA(ctx, cudaMalloc(&ctx->cellsum, sizeof(double) * 27 * 4 * ncell));
@@ -538,6 +565,7 @@ void p2g_free(hmec_inst* ctx) {
     cudaFree(ctx->hc_fill);
     cudaFree(ctx->scan_part);
     cudaFree(ctx->sort_long);
+    cudaFree(ctx->mord);
     for (int k = 0; k < 4; k++) {
         if (ctx->gs4[k]) cudaStreamDestroy(ctx->gs4[k]);
         if (ctx->ev_g_done[k]) cudaEventDestroy(ctx->ev_g_done[k]);
@@ -545,6 +573,57 @@ void p2g_free(hmec_inst* ctx) {
     if (ctx->ev_g_fork) cudaEventDestroy(ctx->ev_g_fork);
     cudaFree(ctx->mprop);
     cudaFree(ctx->cellsum);
+}
+
+// Staging buffers for the marker transfers: doubles of the marker-record
+// region past the part the radix sort uses as scratch.
+static double* stage_f64(hmec_inst* ctx, int k) {
+    return reinterpret_cast<double*>(ctx->mprop + ctx->stage_off) + (size_t)k * (size_t)ctx->marknum;
+}
+
+int p2g_store_markers(hmec_inst* ctx, const double* const* fields) {
+    const int64_t n = ctx->marknum;
+    const Geo& g = ctx->g;
+    double* tx = stage_f64(ctx, 0);
+    double* ty = stage_f64(ctx, 1);
+    double* tf = stage_f64(ctx, 2);
+    HMEC_CUDA(ctx, cudaMemcpyAsync(tx, fields[HMEC_M_xm], sizeof(double) * (size_t)n, cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    HMEC_CUDA(ctx, cudaMemcpyAsync(ty, fields[HMEC_M_ym], sizeof(double) * (size_t)n, cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    // the half-cell order of the caller's markers (its index breaking ties)
+    const int nh = ctx->nhalf;
+    HMEC_CUDA(ctx, cudaMemsetAsync(ctx->hc_count, 0, sizeof(int32_t) * ((size_t)nh + 1), ctx->stream));
+    HMEC_LAUNCH(ctx, hsort::k_keys, nblocks(n, ctx->bs_so), ctx->bs_so, 0, tx, ty, n, g, ctx->mkey, ctx->hc_count,
+                &ctx->ds->status);
+    hsort::SortBufs sb{ctx->mkey, ctx->hc_count, ctx->hc_start, ctx->hc_fill, ctx->scan_part, ctx->mord,
+                       ctx->sort_long, reinterpret_cast<int32_t*>(ctx->mprop), ctx->bs_so};
+    HMEC_CUDA(ctx, hsort::sort_by_half_cell(ctx->stream, sb, n, nh, &ctx->launches));
+    for (int k = 0; k < HMEC_M_COUNT; k++) {
+        const double* src = tx;
+        if (k == HMEC_M_ym) src = ty;
+        if (k != HMEC_M_xm && k != HMEC_M_ym) {
+            HMEC_CUDA(ctx, cudaMemcpyAsync(tf, fields[k], sizeof(double) * (size_t)n, cudaMemcpyHostToDevice,
+                                           ctx->stream));
+            src = tf;
+        }
+        HMEC_LAUNCH(ctx, k_gather_f64, nblocks(n, 256), 256, 0, src, ctx->mord, n, ctx->mk[k]);
+    }
+    HMEC_CUDA(ctx, cudaGetLastError());
+    return HMEC_OK;
+}
+
+int p2g_load_markers(hmec_inst* ctx, double* const* fields) {
+    const int64_t n = ctx->marknum;
+    double* tf = stage_f64(ctx, 2);
+    for (int k = 0; k < HMEC_M_COUNT; k++) {
+        if (!fields[k]) continue;
+        HMEC_LAUNCH(ctx, k_scatter_f64, nblocks(n, 256), 256, 0, ctx->mk[k], ctx->mord, n, tf);
+        HMEC_CUDA(ctx, cudaMemcpyAsync(fields[k], tf, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    }
+    HMEC_CUDA(ctx, cudaGetLastError());
+    return HMEC_OK;
 }
 
 int p2g_run(hmec_inst* ctx) {

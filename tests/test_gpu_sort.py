@@ -84,3 +84,21 @@ def test_clustered_and_spread_markers_in_one_model():
         m.markers_to_nodes()
         for f in P2G_FIELDS:
             assert np.array_equal(m.field(f), ref.field(f)), f
+
+
+def test_markers_stored_in_half_cell_order_round_trip():
+    """The library stores markers in half-cell order; downloads return the
+    caller's order, bit for bit, also after clustering and re-uploads."""
+    o, mk, nodes = pairs.oracle_for("c0")
+    _, mk1, _ = clustered("c0")
+    m = pairs.model_for("c0", mk, nodes)
+    for arrays in (mk, mk1, mk):
+        m.upload_markers(arrays)
+        got = m.download_markers()
+        for k, v in arrays.items():
+            assert np.array_equal(got[k], v), k
+    m.markers_to_nodes()
+    o.set_markers(mk)
+    o.markers_to_nodes()
+    e = pairs.field_errors(m, o, P2G_FIELDS)
+    assert max(e.values()) < 1e-13, e
