@@ -183,6 +183,7 @@ void hmec_params_default(hmec_params* p) {
     p->mg_flags = 1; /* HMEC_MG_DARCY_HARMONIC */
     p->graph = 1;
     p->autotune = 1;
+    p->invariants_every = 1;
 }
 
 #define HMEC_X_NAME(name, grid) #name,
@@ -239,6 +240,12 @@ static void inst_destroy(hmec_inst* ctx) {
     cudaFree(ctx->red);
     cudaFree(ctx->ticket);
     cudaFree(ctx->ds);
+    if (ctx->rows_stream) {
+        cudaStreamSynchronize(ctx->rows_stream);
+        cudaStreamDestroy(ctx->rows_stream);
+        cudaEventDestroy(ctx->rows_ready);
+        for (auto e : ctx->rows_done) cudaEventDestroy(e);
+    }
     cudaFree(ctx->rowbuf);
     cudaFreeHost(ctx->hs);
     cudaStreamDestroy(ctx->stream);
@@ -251,6 +258,7 @@ static const char* params_problem(const hmec_params& p) {
         return "grid parameters out of range (Nx, Ny >= 5; mx, my >= 1; sizes > 0)";
     if (p.krylov_restart < 2 || p.krylov_restart > 200) return "krylov_restart must be in [2, 200]";
     if (p.form != HMEC_FORM_FP64 && p.form != HMEC_FORM_MIXED) return "unknown solver form";
+    if (p.invariants_every < 0) return "invariants_every must be >= 0";
     return nullptr;
 }
 
@@ -386,27 +394,82 @@ static int32_t inst_download_field(hmec_inst* ctx, int32_t f, double* a, int32_t
     return HMEC_OK;
 }
 
-static int32_t inst_download_rows(hmec_inst* ctx, int32_t row, int32_t nf, const int32_t* fields, double* out) {
-    if (!ctx || !fields || !out) return fail(ctx, HMEC_ERR_ARG, "null argument");
-    if (nf < 1 || nf > 64) return fail(ctx, HMEC_ERR_ARG, "nfields must be in [1, 64]");
-    RowGather g;
+// The gather of hmec_download_rows: checks the fields and the row, fills g,
+// and returns the doubles the rows take (0 on an argument error).
+static int rows_gather(hmec_inst* ctx, int32_t row, int32_t nf, const int32_t* fields, RowGather* g) {
+    if (nf < 1 || nf > 64) return fail(ctx, HMEC_ERR_ARG, "nfields must be in [1, 64]"), 0;
     int total = 0;
     for (int k = 0; k < nf; k++) {
         const int f = fields[k];
-        if (f < 0 || f >= HMEC_F_COUNT) return fail(ctx, HMEC_ERR_ARG, "unknown field");
+        if (f < 0 || f >= HMEC_F_COUNT) return fail(ctx, HMEC_ERR_ARG, "unknown field"), 0;
         const int gr = hmec_field_grid(f);
-        g.f[k] = ctx->f[f];
-        g.rows[k] = ctx->g.Ny + gr;
-        g.cols[k] = ctx->g.Nx + gr;
-        g.off[k] = total;
-        total += g.cols[k];
-        if (row < 0 || row >= g.rows[k]) return fail(ctx, HMEC_ERR_ARG, "row outside the field");
+        g->f[k] = ctx->f[f];
+        g->rows[k] = ctx->g.Ny + gr;
+        g->cols[k] = ctx->g.Nx + gr;
+        g->off[k] = total;
+        total += g->cols[k];
+        if (row < 0 || row >= g->rows[k]) return fail(ctx, HMEC_ERR_ARG, "row outside the field"), 0;
     }
-    if (!ctx->rowbuf) HMEC_CUDA(ctx, cudaMalloc(&ctx->rowbuf, sizeof(double) * 64 * (size_t)(ctx->g.Nx + 1)));
-    HMEC_LAUNCH(ctx, k_gather_rows, dim3(nblocks(ctx->g.Nx + 1, 128), nf), 128, 0, g, nf, row, ctx->rowbuf);
-    HMEC_CUDA(ctx, cudaMemcpyAsync(out, ctx->rowbuf, sizeof(double) * (size_t)total, cudaMemcpyDeviceToHost,
-                                   ctx->stream));
+    return total;
+}
+
+static int rows_slots(hmec_inst* ctx) {
+    if (!ctx->rowbuf) HMEC_CUDA(ctx, cudaMalloc(&ctx->rowbuf, sizeof(double) * 3 * 64 * (size_t)(ctx->g.Nx + 1)));
+    return HMEC_OK;
+}
+
+static int32_t inst_download_rows(hmec_inst* ctx, int32_t row, int32_t nf, const int32_t* fields, double* out) {
+    if (!ctx || !fields || !out) return fail(ctx, HMEC_ERR_ARG, "null argument");
+    RowGather g;
+    const int total = rows_gather(ctx, row, nf, fields, &g);
+    if (!total) return HMEC_ERR_ARG;
+    if (int rc = rows_slots(ctx)) return rc;
+    // slot 2: slots 0 and 1 belong to the asynchronous copies
+    double* buf = ctx->rowbuf + (size_t)2 * 64 * (size_t)(ctx->g.Nx + 1);
+    HMEC_LAUNCH(ctx, k_gather_rows, dim3(nblocks(ctx->g.Nx + 1, 128), nf), 128, 0, g, nf, row, buf);
+    HMEC_CUDA(ctx, cudaMemcpyAsync(out, buf, sizeof(double) * (size_t)total, cudaMemcpyDeviceToHost, ctx->stream));
     HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HMEC_OK;
+}
+
+// The rows are gathered on the instance's stream into one of two device
+// slots; the host waits for the gather only (a few microseconds), so that
+// the next step may write the fields, and the copy to `out` runs on the
+// rows stream, overlapped with that step.  A slot is gathered into again only
+// after its previous copy is done (a wait queued on the instance's stream).
+static int32_t inst_download_rows_async(hmec_inst* ctx, int32_t row, int32_t nf, const int32_t* fields, double* out,
+                                        int64_t* ticket) {
+    if (!ctx || !fields || !out || !ticket) return fail(ctx, HMEC_ERR_ARG, "null argument");
+    RowGather g;
+    const int total = rows_gather(ctx, row, nf, fields, &g);
+    if (!total) return HMEC_ERR_ARG;
+    if (int rc = rows_slots(ctx)) return rc;
+    if (!ctx->rows_stream) {
+        HMEC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->rows_stream, cudaStreamNonBlocking));
+        HMEC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->rows_ready, cudaEventDisableTiming));
+        for (auto& e : ctx->rows_done) HMEC_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    const int slot = (int)(ctx->rows_last & 1);
+    double* buf = ctx->rowbuf + (size_t)slot * 64 * (size_t)(ctx->g.Nx + 1);
+    HMEC_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->rows_done[slot], 0));
+    HMEC_LAUNCH(ctx, k_gather_rows, dim3(nblocks(ctx->g.Nx + 1, 128), nf), 128, 0, g, nf, row, buf);
+    HMEC_CUDA(ctx, cudaEventRecord(ctx->rows_ready, ctx->stream));
+    HMEC_CUDA(ctx, cudaStreamWaitEvent(ctx->rows_stream, ctx->rows_ready, 0));
+    HMEC_CUDA(ctx, cudaMemcpyAsync(out, buf, sizeof(double) * (size_t)total, cudaMemcpyDeviceToHost,
+                                   ctx->rows_stream));
+    HMEC_CUDA(ctx, cudaEventRecord(ctx->rows_done[slot], ctx->rows_stream));
+    HMEC_CUDA(ctx, cudaEventSynchronize(ctx->rows_ready));
+    ctx->rows_ticket[slot] = ++ctx->rows_last;
+    *ticket = ctx->rows_last;
+    return HMEC_OK;
+}
+
+// Waits for the copy of `ticket`: its slot's last copy is that one or a
+// later one, which the stream order puts after it.
+static int32_t inst_rows_wait(hmec_inst* ctx, int64_t ticket) {
+    if (!ctx) return HMEC_ERR_ARG;
+    if (ticket < 1 || ticket > ctx->rows_last) return fail(ctx, HMEC_ERR_ARG, "unknown rows ticket");
+    HMEC_CUDA(ctx, cudaEventSynchronize(ctx->rows_done[(ticket - 1) & 1]));
     return HMEC_OK;
 }
 
@@ -817,6 +880,22 @@ int32_t hmec_download_field(hmec_ctx* E, int32_t i, int32_t f, double* a, int32_
 int32_t hmec_download_rows(hmec_ctx* E, int32_t i, int32_t row, int32_t nf, const int32_t* fields, double* out) {
     HMEC_INST(E, i);
     return relay(E, m_, inst_download_rows(m_, row, nf, fields, out));
+}
+int32_t hmec_download_rows_async(hmec_ctx* E, int32_t i, int32_t row, int32_t nf, const int32_t* fields, double* out,
+                                 int64_t* ticket) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_download_rows_async(m_, row, nf, fields, out, ticket));
+}
+int32_t hmec_rows_wait(hmec_ctx* E, int32_t i, int64_t ticket) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_rows_wait(m_, ticket));
+}
+void* hmec_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    return cudaMallocHost(&p, bytes ? bytes : 1) == cudaSuccess ? p : nullptr;
+}
+void hmec_host_free(void* p) {
+    if (p) cudaFreeHost(p);
 }
 int32_t hmec_set_scalar(hmec_ctx* E, int32_t i, int32_t id, double v) {
     HMEC_INST(E, i);

@@ -250,7 +250,14 @@ struct hmec_inst {
     int in_step;             // between timestep_begin and timestep_end
     std::string err;
     GraphState gr;
-    double* rowbuf = nullptr;  // hmec_download_rows staging (64 rows of Nx+1)
+    double* rowbuf = nullptr;  // row staging: 3 slots of 64 rows of Nx+1 (2 async, 1 sync)
+    // hmec_download_rows_async: the copies' stream, the gather's event, each
+    // slot's copy-done event and the ticket it last carried
+    cudaStream_t rows_stream = nullptr;
+    cudaEvent_t rows_ready = nullptr;
+    cudaEvent_t rows_done[2] = {nullptr, nullptr};
+    int64_t rows_ticket[2] = {0, 0};
+    int64_t rows_last = 0;
     int bs_st = 64, bs_so = 256;  // threads per block: node-stencil kernels, marker kernels
 };
 

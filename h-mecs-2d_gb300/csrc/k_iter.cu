@@ -951,6 +951,9 @@ __global__ void k_post_p(Geo g, const DevScalars* ds, hmec_params p, PostP P) {
     IS(P.EYY, i, j) = eyy;
     IS(P.SXX, i, j) = sxx;
     IS(P.SYY, i, j) = syy;
+    // the rest are output fields: with invariants_every = k > 1 the steps
+    // between multiples of k write only the fault-line row
+    if (p.invariants_every > 1 && ds->timestep % p.invariants_every != 0 && i != g.line_fault) return;
     const double s00 = IB(P.SXY, i - 1, j - 1), s01 = IB(P.SXY, i - 1, j), s10 = IB(P.SXY, i, j - 1), s11 = IB(P.SXY, i, j);
     const double e00 = IB(P.ETA, i - 1, j - 1), e01 = IB(P.ETA, i - 1, j), e10 = IB(P.ETA, i, j - 1), e11 = IB(P.ETA, i, j);
     IS(P.EII, i, j) = sqrt(exx * exx + sq4(IB(P.EXY, i - 1, j - 1), IB(P.EXY, i - 1, j), IB(P.EXY, i, j - 1), IB(P.EXY, i, j)) / 4.);

@@ -237,8 +237,51 @@ int main(int argc, char** argv) {
     const int nevo = (int)(sizeof(evo_ids) / sizeof(evo_ids[0]));
     std::vector<int> evo_off(nevo + 1, 0);
     for (int k = 0; k < nevo; k++) evo_off[k + 1] = evo_off[k] + (hmec_field_grid(evo_ids[k]) ? Nx1 : Nx);
-    std::vector<double> rows(evo_off[nevo]), peff(Nx1);
-    for (int s = 0; s < steps; s++) {
+    // The rows of a step are gathered right after it and copied to
+    // page-locked memory while the next step runs
+    // (hmec_download_rows_async); that step's EVO lines are written once the
+    // next step has returned, so the files keep the reference's line order.
+    struct Pending {
+        hmec_step_report r;
+        int64_t ticket = 0;
+        double* buf = nullptr;
+        bool live = false;
+    } pend[2];
+    std::vector<double> fallback[2];
+    for (int k = 0; k < 2; k++) {
+        pend[k].buf = (double*)hmec_host_alloc(sizeof(double) * (size_t)evo_off[nevo]);
+        if (!pend[k].buf) {
+            fallback[k].resize(evo_off[nevo]);
+            pend[k].buf = fallback[k].data();
+        }
+    }
+    std::vector<double> peff(Nx1);
+    auto write_evo = [&](Pending& q) {
+        if (!q.live) return 0;
+        q.live = false;
+        if (check(ctx, hmec_rows_wait(ctx, 0, q.ticket), "rows_wait")) return 1;
+        const hmec_step_report& r = q.r;
+        const double* row = q.buf;
+        for (int j = 0; j < Nx1; j++) peff[j] = row[evo_off[3] + j] - row[evo_off[2] + j];  // pt - pf
+        append_row(d + "EVO_Vslip.txt", r.timesum, r.dt, row + evo_off[0], Nx);
+        append_row(d + "EVO_viscosity.txt", r.timesum, r.dt, row + evo_off[1], Nx);
+        append_row(d + "EVO_press_flu.txt", r.timesum, r.dt, row + evo_off[2], Nx1);
+        append_row(d + "EVO_press_eff.txt", r.timesum, r.dt, peff.data(), Nx1);
+        append_row(d + "EVO_SigmaY.txt", r.timesum, r.dt, row + evo_off[4], Nx);
+        append_row(d + "EVO_Sii.txt", r.timesum, r.dt, row + evo_off[5], Nx);
+        append_row(d + "EVO_Theta.txt", r.timesum, r.dt, row + evo_off[6], Nx);
+        append_row(d + "EVO_Visc_comp.txt", r.timesum, r.dt, row + evo_off[7], Nx1);
+        append_row(d + "EVO_Elast_comp.txt", r.timesum, r.dt, row + evo_off[8], Nx1);
+        append_row(d + "EVO_vxD.txt", r.timesum, r.dt, row + evo_off[9], Nx1);
+        FILE* f = fopen((d + "EVO_data.txt").c_str(), "a");
+        if (f) {
+            fprintf(f, "%20g%20g%20g%20d%20d\n", r.timesum, r.dt, r.Vmax, r.ynlast, r.global_iters);
+            fclose(f);
+        }
+        return 0;
+    };
+    int failed = 0;
+    for (int s = 0; s < steps && !failed; s++) {
         hmec_step_report r;
         if (check(ctx, hmec_timestep(ctx, &r), "hmec_timestep")) break;
         history.record(ctx, r.timestep);
@@ -269,25 +312,16 @@ int main(int argc, char** argv) {
                 }
             }
         }
-        if (check(ctx, hmec_download_rows(ctx, 0, line_fault, nevo, evo_ids, rows.data()), "download_rows")) break;
-        const double* row = rows.data();
-        for (int j = 0; j < Nx1; j++) peff[j] = row[evo_off[3] + j] - row[evo_off[2] + j];  // pt - pf
-        append_row(d + "EVO_Vslip.txt", r.timesum, r.dt, row + evo_off[0], Nx);
-        append_row(d + "EVO_viscosity.txt", r.timesum, r.dt, row + evo_off[1], Nx);
-        append_row(d + "EVO_press_flu.txt", r.timesum, r.dt, row + evo_off[2], Nx1);
-        append_row(d + "EVO_press_eff.txt", r.timesum, r.dt, peff.data(), Nx1);
-        append_row(d + "EVO_SigmaY.txt", r.timesum, r.dt, row + evo_off[4], Nx);
-        append_row(d + "EVO_Sii.txt", r.timesum, r.dt, row + evo_off[5], Nx);
-        append_row(d + "EVO_Theta.txt", r.timesum, r.dt, row + evo_off[6], Nx);
-        append_row(d + "EVO_Visc_comp.txt", r.timesum, r.dt, row + evo_off[7], Nx1);
-        append_row(d + "EVO_Elast_comp.txt", r.timesum, r.dt, row + evo_off[8], Nx1);
-        append_row(d + "EVO_vxD.txt", r.timesum, r.dt, row + evo_off[9], Nx1);
-        FILE* f = fopen((d + "EVO_data.txt").c_str(), "a");
-        if (f) {
-            fprintf(f, "%20g%20g%20g%20d%20d\n", r.timesum, r.dt, r.Vmax, r.ynlast, r.global_iters);
-            fclose(f);
-        }
+        // the previous step's lines (its copy ran during this step)
+        if (write_evo(pend[(s + 1) & 1])) break;
+        Pending& q = pend[s & 1];
+        q.r = r;
+        if (check(ctx, hmec_download_rows_async(ctx, 0, line_fault, nevo, evo_ids, q.buf, &q.ticket),
+                  "download_rows_async"))
+            break;
+        q.live = true;
         if (savestep > 0 && r.timestep % savestep == 0) {  // :1807-1870
+            if (write_evo(q)) break;  // the EVO files hold every step up to the saved one
             FILE* ft = fopen((d + "file.txt").c_str(), "w");
             if (ft) {
                 fprintf(ft, "%d\n", r.timestep);
@@ -301,6 +335,9 @@ int main(int argc, char** argv) {
             }
         }
     }
+    for (auto& q : pend) failed |= write_evo(q);
+    for (int k = 0; k < 2; k++)
+        if (fallback[k].empty()) hmec_host_free(pend[k].buf);
     hmec_destroy(ctx);
-    return 0;
+    return failed ? 1 : 0;
 }

@@ -62,7 +62,7 @@ class Params(C.Structure):
         ("rk4_as_written", C.c_int32), ("quirk_accumulate_sums", C.c_int32), ("bounds_check", C.c_int32),
         ("mg_flags", C.c_int32), ("graph", C.c_int32),
         ("bs_stencil", C.c_int32), ("bs_sort", C.c_int32), ("krylov_blocks", C.c_int32),
-        ("smooth_blocks", C.c_int32), ("autotune", C.c_int32),
+        ("smooth_blocks", C.c_int32), ("autotune", C.c_int32), ("invariants_every", C.c_int32),
     ]
 
 
@@ -104,7 +104,7 @@ SCALARS = _xlist("HMEC_SCALAR_LIST")
 EXPORTS = ["hmec_abi_version", "hmec_params_default", "hmec_field_name", "hmec_field_grid", "hmec_marker_name",
            "hmec_scalar_name", "hmec_marknum", "hmec_create", "hmec_destroy", "hmec_instances", "hmec_last_error",
            "hmec_upload_markers", "hmec_download_markers", "hmec_upload_field", "hmec_download_field",
-           "hmec_download_rows",
+           "hmec_download_rows", "hmec_download_rows_async", "hmec_rows_wait", "hmec_host_alloc", "hmec_host_free",
            "hmec_set_scalar", "hmec_get_scalar", "hmec_markers_to_nodes", "hmec_timestep_begin",
            "hmec_global_iteration", "hmec_timestep_end", "hmec_advect_markers", "hmec_timestep",
            "hmec_assemble_csr", "hmec_solve_system", "hmec_kernel_launches", "hmec_synchronize", "hmec_stream",
@@ -158,6 +158,12 @@ def load(build_if_missing: bool = True):
     L.hmec_upload_field.argtypes = [vp, i32, i32, P(C.c_double), i32, i32]
     L.hmec_download_field.argtypes = [vp, i32, i32, P(C.c_double), i32, i32]
     L.hmec_download_rows.argtypes = [vp, i32, i32, i32, P(i32), P(C.c_double)]
+    L.hmec_download_rows_async.argtypes = [vp, i32, i32, i32, P(i32), P(C.c_double), P(C.c_int64)]
+    L.hmec_rows_wait.argtypes = [vp, i32, C.c_int64]
+    L.hmec_host_alloc.argtypes = [C.c_size_t]
+    L.hmec_host_alloc.restype = vp
+    L.hmec_host_free.argtypes = [vp]
+    L.hmec_host_free.restype = None
     L.hmec_set_scalar.argtypes = [vp, i32, i32, C.c_double]
     L.hmec_get_scalar.argtypes = [vp, i32, i32, P(C.c_double)]
     for fn in ("hmec_markers_to_nodes", "hmec_timestep_begin", "hmec_timestep_end", "hmec_advect_markers"):
@@ -210,6 +216,24 @@ def cell_index(x, d: float, half: bool = False):
     if rc != 0:
         raise HmecError(rc, "hmec_cell_index failed")
     return out
+
+
+class HostArray:
+    """A float64 array in page-locked host memory (hmec_host_alloc), freed
+    with close(); `a` is the numpy view."""
+
+    def __init__(self, n: int):
+        self.L = load()
+        self.ptr = self.L.hmec_host_alloc(8 * max(1, int(n)))
+        if not self.ptr:
+            raise HmecError(-7, "hmec_host_alloc failed")
+        self.a = np.ctypeslib.as_array((C.c_double * max(1, int(n))).from_address(self.ptr))[:n]
+
+    def close(self):
+        if self.ptr:
+            self.a = None
+            self.L.hmec_host_free(self.ptr)
+            self.ptr = None
 
 
 def _dptr(a):
@@ -280,6 +304,21 @@ class Instance:
             out[n] = buf[o:o + k].copy()
             o += k
         return out
+
+    def rows_async(self, row, names, out) -> int:
+        """Starts the gather and copy of hmec_download_rows_async into `out`
+        (a float64 array of the rows' total length, best page-locked: see
+        host_array); returns the ticket to pass to rows_wait."""
+        ids = (C.c_int32 * len(names))(*[FIELDS.index(n) for n in names])
+        if out.dtype != np.float64 or not out.flags.c_contiguous or out.size < sum(self.shape(n)[1] for n in names):
+            raise ValueError("out must be a contiguous float64 array of the rows' total length")
+        t = C.c_int64(0)
+        self._check(self.L.hmec_download_rows_async(self.h, self.inst, row, len(names), ids, _dptr(out), C.byref(t)),
+                    "download_rows_async")
+        return t.value
+
+    def rows_wait(self, ticket):
+        self._check(self.L.hmec_rows_wait(self.h, self.inst, ticket), "rows_wait")
 
     def set_scalar(self, name, v):
         self._check(self.L.hmec_set_scalar(self.h, self.inst, SCALARS.index(name), float(v)), "set_scalar")

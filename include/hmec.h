@@ -28,6 +28,7 @@
 #ifndef HMEC_H
 #define HMEC_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -118,6 +119,11 @@ typedef struct hmec_params {
                                  table entry of this form nearest this grid (the table of
                                  hmec/tune.py: $HMEC_TUNE_TABLE, else tune_table.json beside the
                                  library's package), when there is one within 4x in cells */
+    int32_t invariants_every; /* k > 1: the output-only fields of a17 (EII, EIIVP, SII, DIS,
+                                 pt_ave, pf_ave, VIS_COMP, EL_DECOM) over the whole grid only on
+                                 steps whose number is a multiple of k, on the other steps only
+                                 their fault-line row (what the per-step EVO_*.txt series print);
+                                 0 or 1: every step, as the reference (1) */
 } hmec_params;
 
 /* mg_flags bits */
@@ -267,6 +273,21 @@ int32_t hmec_download_field(hmec_ctx* ctx, int32_t inst, int32_t field, double* 
  * replaces downloading the whole fields.                                    */
 int32_t hmec_download_rows(hmec_ctx* ctx, int32_t inst, int32_t row, int32_t nfields, const int32_t* fields,
                            double* out);
+/* hmec_download_rows without waiting for the copy: the rows are gathered
+ * after the work queued so far (the host waits for that gather only) and
+ * copied to `out` on a stream of their own, overlapped with the next
+ * hmec_timestep.  *ticket names the copy; `out` must stay valid and unread
+ * until hmec_rows_wait(ticket) returns.  With page-locked `out`
+ * (hmec_host_alloc) the copy is asynchronous; with pageable memory this call
+ * returns after the copy.  Two copies per instance can be in flight; a third
+ * gather waits (on the device) for the oldest.  The reference writes the
+ * fault rows synchronously every step (:1751-1805).                          */
+int32_t hmec_download_rows_async(hmec_ctx* ctx, int32_t inst, int32_t row, int32_t nfields,
+                                 const int32_t* fields, double* out, int64_t* ticket);
+int32_t hmec_rows_wait(hmec_ctx* ctx, int32_t inst, int64_t ticket);
+/* Page-locked host memory for hmec_download_rows_async (NULL on failure). */
+void* hmec_host_alloc(size_t bytes);
+void hmec_host_free(void* ptr);
 int32_t hmec_set_scalar(hmec_ctx* ctx, int32_t inst, int32_t id, double value);
 int32_t hmec_get_scalar(hmec_ctx* ctx, int32_t inst, int32_t id, double* value);
 

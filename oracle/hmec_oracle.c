@@ -150,6 +150,7 @@ void hmo_params_default(hmec_params* p) {
     p->mg_flags = 1; /* HMEC_MG_DARCY_HARMONIC */
     p->graph = 1;
     p->autotune = 1;
+    p->invariants_every = 1;
 }
 
 /* Eigen 3.3 LinSpaced(n, low, high) for |high| >= |low| (all grids here). */

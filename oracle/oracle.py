@@ -51,7 +51,7 @@ class HmecParams(C.Structure):
         ("rk4_as_written", C.c_int32), ("quirk_accumulate_sums", C.c_int32), ("bounds_check", C.c_int32),
         ("mg_flags", C.c_int32), ("graph", C.c_int32),
         ("bs_stencil", C.c_int32), ("bs_sort", C.c_int32), ("krylov_blocks", C.c_int32),
-        ("smooth_blocks", C.c_int32), ("autotune", C.c_int32),
+        ("smooth_blocks", C.c_int32), ("autotune", C.c_int32), ("invariants_every", C.c_int32),
     ]
 
 

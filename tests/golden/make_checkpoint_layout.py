@@ -4,9 +4,9 @@ Writes checkpoint_layout.json beside this script: the dataset names of the
 save block of cpp/h_mec_rsf_v9.cpp (the string arrays matrix_names,
 matrix_names_plus, vector_names, vector_names_marker, and the order of the
 nine values streamed into `temp`), in write order, plus the group names and
-the file-name stem.  Run it where the reference tree is available:
+the file-name stem.  The reference's source tree is a required argument:
 
-    python tests/golden/make_checkpoint_layout.py /root/reference
+    python tests/golden/make_checkpoint_layout.py <reference source tree>
 """
 import json
 import os
@@ -38,7 +38,9 @@ def layout(ref_root: str) -> dict:
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_checkpoint_layout.py <reference source tree>")
+    ref = sys.argv[1]
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "checkpoint_layout.json")
     with open(out, "w") as f:
         json.dump(layout(ref), f, indent=1)

@@ -90,3 +90,73 @@ def test_download_rows_equals_field_rows():
     with pytest.raises(hmec.HmecError):
         m.rows(p.Ny + 5, names)
     m.close()
+
+
+def _tiny_model(**extra):
+    p = hmec.default_params(**dict(synth.PRESETS["tiny"], **extra))
+    m = hmec.Model(p)
+    mk, nodes = synth.make_state(p, "tiny")
+    m.upload_markers(mk)
+    for k, v in nodes.items():
+        m.upload_field(k, v)
+    return m, p
+
+
+def test_download_rows_async_overlaps_the_next_step():
+    """The copy of a step's rows started before the next step returns that
+    step's rows (bit for bit), into page-locked and into pageable memory."""
+    m, p = _tiny_model()
+    names = ["VSLIPB", "pf", "ETA", "vxD", "SigmaY", "VIS_COMP"]
+    lf = int((p.Ny - 1) / 2.0)
+    n = sum(m.shape(k)[1] for k in names)
+    pinned = [hmec.HostArray(n), hmec.HostArray(n)]
+    try:
+        want, tickets = [], []
+        for s in range(4):
+            m.timestep()
+            want.append(m.rows(lf, names))
+            buf = pinned[s & 1].a if s != 2 else np.empty(n)  # step 3's copy goes to pageable memory
+            tickets.append((m.rows_async(lf, names, buf), buf, s))
+            if s >= 1:
+                t, b, k = tickets[s - 1]
+                m.rows_wait(t)
+                got = np.concatenate([want[k][x] for x in names])
+                assert np.array_equal(b, got), k
+        t, b, k = tickets[-1]
+        m.rows_wait(t)
+        assert np.array_equal(b, np.concatenate([want[k][x] for x in names]))
+        with pytest.raises(hmec.HmecError):
+            m.rows_wait(tickets[-1][0] + 1)
+        with pytest.raises(hmec.HmecError):
+            m.rows_async(p.Ny + 5, names, pinned[0].a)
+    finally:
+        m.close()
+        for h in pinned:
+            h.close()
+
+
+def test_invariants_every_skips_output_fields_between_output_steps():
+    """invariants_every = 3: steps 1 and 2 write the output-only invariants on
+    the fault line only, step 3 everywhere; every state field (and the fault
+    row the EVO series print) equals the every-step run bit for bit."""
+    inv = ["EII", "EIIVP", "SII", "DIS", "pt_ave", "pf_ave", "VIS_COMP", "EL_DECOM"]
+    a, p = _tiny_model(invariants_every=1)
+    b, _ = _tiny_model(invariants_every=3)
+    lf = int((p.Ny - 1) / 2.0)
+    try:
+        for s in (1, 2, 3):
+            a.timestep()
+            b.timestep()
+            for f in ["vxs", "vys", "pt", "pf", "SXX", "SYY", "SXY", "SXX0", "SYY0", "EXX", "EYY", "OM", "ETA"]:
+                assert np.array_equal(a.field(f), b.field(f)), (s, f)
+            for f in inv:
+                fa, fb = a.field(f), b.field(f)
+                assert np.array_equal(fa[lf], fb[lf]), (s, f)
+                if s == 3:
+                    assert np.array_equal(fa, fb), (s, f)
+                else:
+                    rest = np.delete(np.arange(fa.shape[0]), [0, lf])
+                    assert not np.array_equal(fa[rest], fb[rest]), (s, f)
+    finally:
+        a.close()
+        b.close()
