@@ -19,6 +19,14 @@ reference's bisection resolution |dS| <= 1e-3 Pa (:1224).  Global iteration
 counts are equal; dt agrees to 1e-10 (it follows the velocity maxima of the
 adaptive-step rules, :1310-1427), or to 1e-8 in a rupture phase, where it
 follows the slip rate (Lapusta step, :1266-1273).
+
+The floor is the largest change of the oracle's own result when it solves
+the same step with other pivots (three partial-pivoting thresholds).  Near
+the yield stress the plastic iterations amplify a solve's last-bit
+differences by up to 1e7: on a 65 x 54 member at step 3 the three oracle
+solves spread by 0.4e-9 to 2.3e-9 in velocity, and the GPU's FP64 form gives
+9.3e-9 at the 1e-15 Krylov tolerance and 0.5e-9 at 1e-16 -- the spread does
+not shrink with the tolerance, it is the problem's sensitivity.
 """
 import numpy as np
 import pytest
@@ -34,6 +42,9 @@ TOL_STEP = 1e-10
 TOL_DARCY = 1e-6
 RUPTURE_TAU = 16e6  # uniform pre-stress SXY0 (Pa), above the fault's steady-state strength at V = 1e-9 m/s
 FORMS = (hmec.FORM_MIXED, hmec.FORM_FP64)
+# partial-pivoting thresholds of the oracle's sparse LU (SuperLU's
+# diag_pivot_thresh; the oracle's default is 1.0) whose results span its floor
+PIVOT_THRESHOLDS = (0.1, 0.5, 0.01)
 
 
 def replay_and_check(over, mk, snap, label, dt_rel=1e-10, forms=FORMS):
@@ -68,13 +79,17 @@ def replay_and_check(over, mk, snap, label, dt_rel=1e-10, forms=FORMS):
 
         bad = {g: e for g, e in err.items() if not e < bound(g, None)}
         if bad and floor is None:
-            # the oracle's own floor: the same step with other pivots
-            o2 = O.Oracle(O.default_params(**over))
-            o2.pivot_thresh = 0.1
-            o2.set_markers(mk)
-            o2.load_state(snap)
-            o2.timestep()
-            floor = pairs.group_errors(pairs.OracleView(o2), pairs.OracleView(o), pairs.GROUPS_ALL)
+            # the oracle's own floor: the largest change of its result when
+            # the same step is solved with other pivots
+            floor = {}
+            for thresh in PIVOT_THRESHOLDS:
+                o2 = O.Oracle(O.default_params(**over))
+                o2.pivot_thresh = thresh
+                o2.set_markers(mk)
+                o2.load_state(snap)
+                o2.timestep()
+                e2 = pairs.group_errors(pairs.OracleView(o2), pairs.OracleView(o), pairs.GROUPS_ALL)
+                floor = {g: max(floor.get(g, 0.0), e2[g]) for g in e2}
         if bad:
             bad = {g: (e, bound(g, floor)) for g, e in err.items() if not e < bound(g, floor)}
         assert not bad, (label, form, bad, floor, res)
