@@ -259,6 +259,7 @@ static const char* params_problem(const hmec_params& p) {
     if (p.krylov_restart < 2 || p.krylov_restart > 200) return "krylov_restart must be in [2, 200]";
     if (p.form != HMEC_FORM_FP64 && p.form != HMEC_FORM_MIXED) return "unknown solver form";
     if (p.invariants_every < 0) return "invariants_every must be >= 0";
+    if (p.smooth_inverses < 0 || p.smooth_inverses > 2) return "smooth_inverses must be 0, 1 or 2";
     return nullptr;
 }
 

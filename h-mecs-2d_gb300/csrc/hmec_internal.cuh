@@ -124,6 +124,11 @@ struct Level {
     int CS = 0;
     void* vals = nullptr;
     int16_t* offs = nullptr;
+    // the standard offsets of an interior cell's six rows [6][W], and per
+    // tile whether all its rows have them (set once: the pattern is fixed)
+    int16_t* std_off = nullptr;
+    uint8_t* std_t = nullptr;
+    bool offs_ready = false;
     // per tile: ownership flags of its window and the per-lane colour table
     // (fixed by the geometry), and its boundary rows packed for one bulk copy
     // (rebuilt with each assembly)
@@ -131,8 +136,8 @@ struct Level {
     int32_t* meta_t = nullptr;
     unsigned char* bpack = nullptr;
     int pack_bytes = 0;
-    // TMA descriptors of vals, offs and the patch inverses
-    CUtensorMap tm_val, tm_off, tm_pinv;
+    // TMA descriptors of vals and the patch inverses
+    CUtensorMap tm_val, tm_pinv;
     // prolongation from the next coarser level: per fine x index (Nx+1) and
     // y index (Ny+1) the coarse cell and the two coarse nodes' hat weights
     XferEnt *pmx, *pmy;

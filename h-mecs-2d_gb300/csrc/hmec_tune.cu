@@ -8,7 +8,7 @@
 //   {"version": 1, "entries": [{"Nx": 201, "Ny": 201, "form": 1,
 //     "mg_levels": 5, "mg_pre": 2, "mg_post": 2, "mg_coarse_sweeps": 8,
 //     "bs_stencil": 64, "bs_sort": 256, "krylov_blocks": 304,
-//     "smooth_blocks": 0, "ms_per_step": 12.1}, ...]}
+//     "smooth_blocks": 0, "smooth_inverses": 0, "ms_per_step": 12.1}, ...]}
 // With hmec_params.autotune set, hmec_create takes the entry of the same form
 // whose grid is nearest in cells (within 4x) and applies its fields.  The
 // table is $HMEC_TUNE_TABLE, else tune_table.json in the package directory
@@ -181,6 +181,7 @@ int hmec_tune_apply(hmec_params* p) {
     get("bs_sort", &p->bs_sort, 0, 1024);
     get("krylov_blocks", &p->krylov_blocks, 0, 1 << 16);
     get("smooth_blocks", &p->smooth_blocks, 0, 1 << 16);
+    get("smooth_inverses", &p->smooth_inverses, 0, 2);
     return 1;
 }
 

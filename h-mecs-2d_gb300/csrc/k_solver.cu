@@ -503,6 +503,7 @@ __device__ __forceinline__ int16_t window_offset(int row, int col, int RS, int* 
 // The smoother's copy of the matrix in the padded layout (see Level::vals):
 // values in its precision and window offsets; the mixed form also takes its
 // FP32 copy in the assembly's layout here (the residuals read it).
+// offs is set only on the first assembly: the pattern never changes.
 template <typename T>
 __global__ void k_stage_prep(int N, int Ny1, int Nx1, int CS, const int32_t* __restrict__ col,
                              const double* __restrict__ val, T* vals, int16_t* offs, float* val32, int* status) {
@@ -512,9 +513,47 @@ __global__ void k_stage_prep(int N, int Ny1, int Nx1, int CS, const int32_t* __r
     const int RS = 6 * Ny1;
     const int j = row / RS, r = row - j * RS;
     const size_t o = ((size_t)s * Nx1 + j) * CS + r;
-    offs[o] = window_offset(row, col[t], RS, status);
+    if (offs) offs[o] = window_offset(row, col[t], RS, status);
     vals[o] = (T)val[t];
     if (val32) val32[t] = (float)val[t];
+}
+
+// The standard window offsets of a level: the 11 offsets of each of the six
+// rows of its centre cell (one thread per row type and slot).  Every row of
+// an interior cell has them, since the assembly writes a row's entries
+// sorted by column and the stencil reaches the same neighbours everywhere
+// inside; which tiles hold only such rows is decided by k_tile_std.
+__global__ void k_std_pattern(Geo g, int CS, const int16_t* __restrict__ offs, int16_t* std_off) {
+    const int t = threadIdx.x;
+    if (t >= 6 * HMEC_W) return;
+    const int v = t / HMEC_W, sl = t - v * HMEC_W;
+    const int ci = g.Ny1 / 2, cj = g.Nx1 / 2;
+    std_off[t] = offs[((size_t)sl * g.Nx1 + cj) * CS + ci * 6 + v];
+}
+
+// Per tile (one block each): 1 when every row its patches can touch (cells
+// [i0-1, i1) x [j0-1, j1), all six unknowns) has the standard offsets, so
+// that the smoothing pass takes them from registers; 0 sends the tile's rows
+// to the offsets in global memory.
+__global__ void k_tile_std(Geo g, int ntile_i, int CS, const int16_t* __restrict__ offs,
+                           const int16_t* __restrict__ std_off, uint8_t* std_t) {
+    __shared__ int16_t so[6 * HMEC_W];
+    if (threadIdx.x < 6 * HMEC_W) so[threadIdx.x] = std_off[threadIdx.x];
+    __syncthreads();
+    const int tile = blockIdx.x;
+    const int ti = tile % ntile_i, tj = tile / ntile_i;
+    const int i0 = 1 + ti * TILE, j0 = 1 + tj * TILE;
+    const int i1 = min(i0 + TILE, g.Ny), j1 = min(j0 + TILE, g.Nx);
+    const int RI = (i1 - i0 + 1) * 6, n = RI * (j1 - j0 + 1);
+    int bad = 0;
+    for (int k = threadIdx.x; k < n * HMEC_W; k += blockDim.x) {
+        const int sl = k / n, rr = k - sl * n;
+        const int jj = rr / RI, ii = rr - jj * RI;
+        const int16_t o = offs[((size_t)sl * g.Nx1 + (j0 - 1 + jj)) * CS + (i0 - 1) * 6 + ii];
+        bad |= o != so[(ii % 6) * HMEC_W + sl];
+    }
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) std_t[tile] = bad ? 0 : 1;
 }
 
 // Byte size of one tile's boundary-row pack: values [W][cap], diagonal [cap]
@@ -626,9 +665,12 @@ __device__ __forceinline__ void restrict_apply(int Nc, const int32_t* __restrict
 template <typename T>
 struct StageArgs {
     CUtensorMap tm_val;    // smoother copy of the values: box (RSTR, TILE+1, W)
-    CUtensorMap tm_off;    // window offsets: same box
     CUtensorMap tm_pinv;   // inverses (100, Ny-1, Nx-1): box (100, TILE, TILE)
     Geo g;
+    const int16_t* offs;   // window offsets in the padded layout (tiles without the standard pattern)
+    const int16_t* std_off;  // the level's standard offsets [6][W]
+    const uint8_t* std_t;  // per tile: 1 when its rows all have the standard offsets
+    int cs;                // the padded layout's column stride
     const int32_t* col;    // ELL in the assembly's layout (residual)
     const T* val;
     const T* pinv;         // inverses (per-colour copies)
@@ -657,7 +699,7 @@ struct StageArgs {
 // inverses: about 143 KB, one block per SM; a level with more tiles than
 // blocks restages a tile every time a block takes it up).
 struct StageLayout {
-    int xs, val, off, b, pv, pack, bb, bdel, own, bar, total;
+    int xs, val, b, pv, pack, bb, bdel, own, bar, total;
 };
 
 __host__ __device__ __forceinline__ int align_up(int x, int a) { return (x + a - 1) / a * a; }
@@ -674,7 +716,6 @@ __host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int t
     };
     const int st = (int)sizeof(T);
     take(L.val, HMEC_W * ROWS_MAX * st, 128);
-    take(L.off, HMEC_W * ROWS_MAX * 2, 128);
     take(L.pv, (pv_whole ? TILE * TILE : 2 * PV_MAX) * 100 * st, 128);
     take(L.pack, pack_bytes<T>(tb_cap), 128);
     take(L.own, OWN_STRIDE, 128);
@@ -687,11 +728,12 @@ __host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int t
     return L;
 }
 
-// Bytes one tile's stage receives on its barrier.
+// Bytes one tile's stage receives on its barrier (the boundary pack only for
+// a tile that has boundary rows).
 template <typename T>
-__host__ __device__ __forceinline__ unsigned stage_tx_bytes(bool whole, int tb_cap) {
-    return (unsigned)(HMEC_W * (TILE + 1) * RSTR * (sizeof(T) + 2) + (whole ? TILE * TILE * 100 * sizeof(T) : 0) +
-                      pack_bytes<T>(tb_cap) + OWN_STRIDE);
+__host__ __device__ __forceinline__ unsigned stage_tx_bytes(bool whole, int tb_cap, bool pack) {
+    return (unsigned)(HMEC_W * (TILE + 1) * RSTR * sizeof(T) + (whole ? TILE * TILE * 100 * sizeof(T) : 0) +
+                      (pack ? pack_bytes<T>(tb_cap) : 0) + OWN_STRIDE);
 }
 
 // bc = R (b - A x): each coarse row forms the residuals of its fine rows.
@@ -794,7 +836,6 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
     T* xs = reinterpret_cast<T*>(smem_raw + Lo.xs);
     T* sval = reinterpret_cast<T*>(smem_raw + Lo.val);
     T* sb = reinterpret_cast<T*>(smem_raw + Lo.b);
-    int16_t* soff = reinterpret_cast<int16_t*>(smem_raw + Lo.off);
     unsigned char* own = smem_raw + Lo.own;
     unsigned long long* bar = sb_.bar;
     T* pv = reinterpret_cast<T*>(smem_raw + Lo.pv);
@@ -814,10 +855,24 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
     unsigned& use0 = sb_.use0;
     unsigned& use1 = sb_.use1;
     unsigned& use2 = sb_.use2;
-    int staged = -1, nbt = 0;
+    int staged = -1, nbt = 0, tstd = 0;
     int meta[9];  // lane_meta of this thread for the staged tile
 #pragma unroll
     for (int c = 0; c < 9; c++) meta[c] = 0;
+    // the standard window offsets of this lane's patch row (its unknown type
+    // is fixed by the lane), two int16 per register
+    constexpr int NSO = (HMEC_W + 1) / 2;
+    unsigned sop[NSO];
+    {
+        const int qv = q < 2 ? 3 * q : (q < 6 ? 1 + (q - 2) / 2 : (q < PB ? 4 + (q - 6) / 2 : 0));
+#pragma unroll
+        for (int k = 0; k < NSO; k++) {
+            const unsigned lo = (uint16_t)t.std_off[qv * HMEC_W + 2 * k];
+            const unsigned hi = 2 * k + 1 < HMEC_W ? (uint16_t)t.std_off[qv * HMEC_W + 2 * k + 1] : 0u;
+            sop[k] = lo | (hi << 16);
+        }
+    }
+    const size_t goff_slot = (size_t)g.Nx1 * t.cs;  // slot stride of the padded layout
     const T* src = t.x;  // sweep s > 0 reads the previous sweep's result
     T* dst = t.xalt;
     // one tile for the whole level (the coarsest levels): the window holds
@@ -832,16 +887,19 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
             const int wi0 = i0 - 2, wj0 = j0 - 2;
             const bool fresh = staged != tile;
             if (fresh) {
-                // one thread: the tile's rows (values and offsets, one 3-D box
-                // each), its inverses, ownership flags and boundary pack
+                nbt = min(t.tb_start[tile + 1] - t.tb_start[tile], TBC);
+                tstd = t.std_t[tile];
+                // one thread: the tile's rows (values, one 3-D box), its
+                // inverses, ownership flags and, when it has boundary rows,
+                // its boundary pack
                 if (threadIdx.x == 0) {
                     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                    mbar_expect_tx(&bar[2], stage_tx_bytes<T>(whole, TBC));
+                    mbar_expect_tx(&bar[2], stage_tx_bytes<T>(whole, TBC, nbt > 0));
                     tma_load_3d(sval, &t.tm_val, (i0 - 1) * 6, j0 - 1, 0, &bar[2]);
-                    tma_load_3d(soff, &t.tm_off, (i0 - 1) * 6, j0 - 1, 0, &bar[2]);
                     if (whole) tma_load_3d(pv, &t.tm_pinv, 0, i0 - 1, j0 - 1, &bar[2]);
                     bulk_g2s(own, t.own_t + (size_t)tile * OWN_STRIDE, OWN_STRIDE, &bar[2]);
-                    bulk_g2s(pack, t.bpack + (size_t)tile * pack_bytes<T>(TBC), pack_bytes<T>(TBC), &bar[2]);
+                    if (nbt > 0)
+                        bulk_g2s(pack, t.bpack + (size_t)tile * pack_bytes<T>(TBC), pack_bytes<T>(TBC), &bar[2]);
                 }
                 // the rows' rhs: per staged column one run of RI*6 values
                 const int RI = i1 - i0 + 1, RJ = j1 - j0 + 1, nch = RI * 3;
@@ -855,7 +913,6 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                 // the boundary rows' rhs, gathered by their row numbers in the pack
                 const int32_t* brow = reinterpret_cast<const int32_t*>(
                     t.bpack + (size_t)tile * pack_bytes<T>(TBC) + (size_t)TBC * (HMEC_W * sizeof(T) + sizeof(T) + HMEC_W * 2 + 2));
-                nbt = min(t.tb_start[tile + 1] - t.tb_start[tile], TBC);
                 for (int k = threadIdx.x; k < nbt; k += blockDim.x) bbv[k] = t.b[brow[k]];
                 staged = tile;
             }
@@ -912,8 +969,20 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
 #pragma unroll
                     for (int cc = 0; cc < PB; cc++) pr[cc] = pi[cc];
                     T acc = sb[rl];
+                    if (tstd) {
 #pragma unroll
-                    for (int sl = 0; sl < HMEC_W; sl++) acc -= sval[sl * ROWS_MAX + rl] * xs[lrow + soff[sl * ROWS_MAX + rl]];
+                        for (int sl = 0; sl < HMEC_W; sl++) {
+                            const int o = (int16_t)(uint16_t)(sop[sl >> 1] >> ((sl & 1) * 16));
+                            acc -= sval[sl * ROWS_MAX + rl] * xs[lrow + o];
+                        }
+                    } else {
+                        // staged row rl is element (i0-1)*6 + ii of column j0-1+jj
+                        const int jj = rl / RSTR, ii = rl - jj * RSTR;
+                        const int16_t* go = t.offs + (size_t)(j0 - 1 + jj) * t.cs + (i0 - 1) * 6 + ii;
+#pragma unroll
+                        for (int sl = 0; sl < HMEC_W; sl++)
+                            acc -= sval[sl * ROWS_MAX + rl] * xs[lrow + __ldg(go + sl * goff_slot)];
+                    }
                     r = acc;
                 } else {
 #pragma unroll
@@ -1843,12 +1912,14 @@ static int alloc_level(hmec_inst* ctx, Level& L, bool mixed, bool coarse) {
         HMEC_CUDA(ctx, cudaMalloc(&L.offs, sizeof(int16_t) * ns));
         HMEC_CUDA(ctx, cudaMemset(L.vals, 0, st * ns));
         HMEC_CUDA(ctx, cudaMemset(L.offs, 0, sizeof(int16_t) * ns));
+        HMEC_CUDA(ctx, cudaMalloc(&L.std_off, sizeof(int16_t) * 6 * HMEC_W));
+        HMEC_CUDA(ctx, cudaMalloc(&L.std_t, (size_t)L.ntiles));
+        HMEC_CUDA(ctx, cudaMemset(L.std_off, 0, sizeof(int16_t) * 6 * HMEC_W));
+        HMEC_CUDA(ctx, cudaMemset(L.std_t, 0, (size_t)L.ntiles));
         L.pack_bytes = mixed ? pack_bytes<float>(L.tb_cap) : pack_bytes<double>(L.tb_cap);
         HMEC_CUDA(ctx, cudaMalloc(&L.bpack, (size_t)L.ntiles * L.pack_bytes));
         const CUtensorMapDataType dt = mixed ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
         int rc = encode_map3(ctx, &L.tm_val, dt, st, L.vals, L.CS, g.Nx1, HMEC_W, RSTR, TILE + 1, HMEC_W);
-        if (!rc) rc = encode_map3(ctx, &L.tm_off, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, L.offs, L.CS, g.Nx1, HMEC_W, RSTR,
-                                  TILE + 1, HMEC_W);
         if (!rc)
             rc = encode_map3(ctx, &L.tm_pinv, dt, st, mixed ? (void*)L.pinv32 : (void*)L.pinv, 100, g.Ny - 1, g.Nx - 1,
                              100, TILE, TILE);
@@ -2028,6 +2099,8 @@ void solver_free(hmec_inst* ctx) {
         cudaFree(L.tbnd_list);
         cudaFree(L.vals);
         cudaFree(L.offs);
+        cudaFree(L.std_off);
+        cudaFree(L.std_t);
         cudaFree(L.own_t);
         cudaFree(L.meta_t);
         cudaFree(L.bpack);
@@ -2113,16 +2186,27 @@ int solver_setup(hmec_inst* ctx) {
                         L.val, L.pinv, status);
         const size_t n = (size_t)HMEC_W * L.g.N;
         const size_t nb = (size_t)L.ntiles * L.tb_cap;
+        // the window offsets follow the pattern, which never changes: formed
+        // on the first assembly (a setup captured into a graph forms them on
+        // every replay)
+        int16_t* offs = L.offs_ready ? nullptr : L.offs;
         if (mixed) {
             HMEC_LAUNCH(ctx, k_stage_prep<float>, nblocks(n, 256), 256, 0, L.g.N, L.g.Ny1, L.g.Nx1, L.CS, L.col,
-                        L.val, (float*)L.vals, L.offs, L.val32, status);
+                        L.val, (float*)L.vals, offs, L.val32, status);
             HMEC_LAUNCH(ctx, k_stage_bpack<float>, nblocks(nb, 128), 128, 0, L.g, L.ntile_i, L.ntiles, L.tb_cap,
                         L.tbnd_start, L.tbnd_list, L.col, L.val, L.bpack, status);
         } else {
             HMEC_LAUNCH(ctx, k_stage_prep<double>, nblocks(n, 256), 256, 0, L.g.N, L.g.Ny1, L.g.Nx1, L.CS, L.col,
-                        L.val, (double*)L.vals, L.offs, nullptr, status);
+                        L.val, (double*)L.vals, offs, nullptr, status);
             HMEC_LAUNCH(ctx, k_stage_bpack<double>, nblocks(nb, 128), 128, 0, L.g, L.ntile_i, L.ntiles, L.tb_cap,
                         L.tbnd_start, L.tbnd_list, L.col, L.val, L.bpack, status);
+        }
+        if (offs) {
+            HMEC_LAUNCH(ctx, k_std_pattern, 1, 6 * HMEC_W, 0, L.g, L.CS, L.offs, L.std_off);
+            HMEC_LAUNCH(ctx, k_tile_std, L.ntiles, 256, 0, L.g, L.ntile_i, L.CS, L.offs, L.std_off, L.std_t);
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            HMEC_CUDA(ctx, cudaStreamIsCapturing(sv.aux[l], &cs));
+            if (cs == cudaStreamCaptureStatusNone) L.offs_ready = true;
         }
         if (l > 0) {
             HMEC_CUDA(ctx, cudaStreamWaitEvent(sv.aux[l], sv.ev_asm[l - 1], 0));
@@ -2201,10 +2285,17 @@ static int stage_config(hmec_inst* ctx, Level& L) {
         ctx->err = "the staged smoothing pass does not fit in shared memory";
         return HMEC_ERR_ARG;
     }
-    // whole-tile inverses whenever they fit: with the TMA stage a block that
-    // restages a tile each sweep is still faster than one that waits for each
-    // colour's inverses (measured on the 201x201 and 1001x401 levels)
-    const int w = blocks[1] > 0 ? 1 : 0;
+    // whole-tile inverses when they fit, unless the finest level has more
+    // tiles than that mode keeps resident and the per-colour mode keeps more
+    // blocks resident (FP32: two per SM against one): then blocks restage
+    // tiles anyway, and a second block per SM computes while the other one
+    // waits for its stage.  Every level takes the same mode (one fused
+    // V-cycle launch serves them all).
+    int w = blocks[1] > 0 ? 1 : 0;
+    const int want = ctx->p.smooth_inverses;
+    if (want == 1 && blocks[1] > 0) w = 1;
+    else if (want == 2 && blocks[0] > 0) w = 0;
+    else if (want == 0 && w == 1 && blocks[0] > blocks[1] && ctx->sv.lv[0].ntiles > blocks[1]) w = 0;
     L.st_whole = w;
     L.st_grid = std::min(L.ntiles, blocks[w]);
     if (ctx->p.smooth_blocks > 0) L.st_grid = std::min(L.st_grid, ctx->p.smooth_blocks);
@@ -2249,9 +2340,12 @@ static StageArgs<T> stage_args(hmec_inst* ctx, size_t l, const T* b, T* x, int n
     Level& L = sv.lv[l];
     StageArgs<T> t;
     t.tm_val = L.tm_val;
-    t.tm_off = L.tm_off;
     t.tm_pinv = L.tm_pinv;
     t.g = L.g;
+    t.offs = L.offs;
+    t.std_off = L.std_off;
+    t.std_t = L.std_t;
+    t.cs = L.CS;
     t.col = L.col;
     t.val = LvPtr<T>::val(L);
     t.pinv = LvPtr<T>::pinv(L);
@@ -2276,7 +2370,7 @@ static StageArgs<T> stage_args(hmec_inst* ctx, size_t l, const T* b, T* x, int n
     t.status = &ctx->ds->status;
     t.done = sv.done;
     const double st = sizeof(T), N = L.g.N;
-    *ab = nsweeps * (N * HMEC_W * (st + 2) + (double)L.npatch * 100.0 * st + 3.0 * N * st) +
+    *ab = nsweeps * (N * HMEC_W * st + (double)L.npatch * 100.0 * st + 3.0 * N * st) +
           (mode ? N * st * 1.5 : 0.0);
     *ab_alg = sweep_bytes_compulsory<T>(N, nsweeps + (restrict_next ? 1 : 0));
     if (restrict_next) {

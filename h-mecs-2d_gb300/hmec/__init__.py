@@ -63,6 +63,7 @@ class Params(C.Structure):
         ("mg_flags", C.c_int32), ("graph", C.c_int32),
         ("bs_stencil", C.c_int32), ("bs_sort", C.c_int32), ("krylov_blocks", C.c_int32),
         ("smooth_blocks", C.c_int32), ("autotune", C.c_int32), ("invariants_every", C.c_int32),
+        ("smooth_inverses", C.c_int32),
     ]
 
 
