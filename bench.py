@@ -73,16 +73,17 @@ def parse():
 
 
 def profile_window(args):
-    """The model of --config (c0-c2) in --form: warm-up steps, then the
-    profiled steps bracketed by cudaProfilerStart/Stop (graph mode, as the
-    timed steps)."""
+    """The model of --config (c1, c2) in --form: warm-up steps, then the
+    profiled steps bracketed by cudaProfilerStart/Stop.  The steps run
+    host-driven: ncu does not profile the kernel nodes of a graph with
+    conditional nodes, and the host-driven step launches the same kernels."""
     import torch
 
     import hmec
 
     torch.cuda.set_device(0)
     form = hmec.FORM_MIXED if args.form == "mixed" else hmec.FORM_FP64
-    m, _, _, p = make_model(form, args.config)
+    m, _, _, p = make_model(form, args.config, graph=0)
     for _ in range(args.warmup):
         m.timestep()
     torch.cuda.synchronize()
@@ -252,11 +253,11 @@ def judged(err):
 
 
 # -------------------------------------------------------------------- GPU arm
-def make_model(form, cfg, mk=None, nodes=None):
+def make_model(form, cfg, mk=None, nodes=None, **extra):
     import hmec
     from hmec import synth
 
-    over = dict(synth.PRESETS[cfg], form=form, krylov_rtol=1e-15, krylov_restart=40, krylov_maxit=4000)
+    over = dict(synth.PRESETS[cfg], form=form, krylov_rtol=1e-15, krylov_restart=40, krylov_maxit=4000, **extra)
     p = hmec.default_params(**over)
     m = hmec.Model(p)
     if mk is None:
