@@ -457,7 +457,7 @@ constexpr int TB_MAX = 320;                                       // boundary ro
 constexpr int OWN_STRIDE = (WIN_MAX + 15) / 16 * 16;              // bytes of a tile's ownership flags
 static_assert(WIN_MAX == WSTR * WSTR * 6, "window size");
 static_assert(PV_MAX * 16 <= TILE_BS, "a colour's patches fit the block");
-static_assert((TILE * 6) % 8 == 0, "a tile's first staged row is 8-element aligned in the padded layout");
+static_assert((TILE * 6 * 4) % 16 == 0, "a tile's first staged row starts on 16 bytes in the padded layout");
 
 // Tile owning the unknown v of staggered cell (i, j): a boundary row (outside
 // every patch) goes to the adjacent patch, a cell unknown to its own patch,
@@ -2285,17 +2285,11 @@ static int stage_config(hmec_inst* ctx, Level& L) {
         ctx->err = "the staged smoothing pass does not fit in shared memory";
         return HMEC_ERR_ARG;
     }
-    // whole-tile inverses when they fit, unless the finest level has more
-    // tiles than that mode keeps resident and the per-colour mode keeps more
-    // blocks resident (FP32: two per SM against one): then blocks restage
-    // tiles anyway, and a second block per SM computes while the other one
-    // waits for its stage.  Every level takes the same mode (one fused
-    // V-cycle launch serves them all).
+    // whole-tile inverses whenever they fit: a block that waits for each
+    // colour's inverses is slower even with twice the blocks resident (FP32,
+    // 1001x401: 31.0 against 18.9 ms per step; 201x201: 21.4 against 12.4)
     int w = blocks[1] > 0 ? 1 : 0;
-    const int want = ctx->p.smooth_inverses;
-    if (want == 1 && blocks[1] > 0) w = 1;
-    else if (want == 2 && blocks[0] > 0) w = 0;
-    else if (want == 0 && w == 1 && blocks[0] > blocks[1] && ctx->sv.lv[0].ntiles > blocks[1]) w = 0;
+    if (ctx->p.smooth_inverses == 2 && blocks[0] > 0) w = 0;
     L.st_whole = w;
     L.st_grid = std::min(L.ntiles, blocks[w]);
     if (ctx->p.smooth_blocks > 0) L.st_grid = std::min(L.st_grid, ctx->p.smooth_blocks);

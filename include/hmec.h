@@ -125,10 +125,9 @@ typedef struct hmec_params {
                                  their fault-line row (what the per-step EVO_*.txt series print);
                                  0 or 1: every step, as the reference (1) */
     int32_t smooth_inverses;  /* the staged smoothing pass's Vanka inverses: 1 a whole tile's
-                                 staged with its rows (FP32: one block per SM), 2 one colour's
-                                 at a time, double buffered (FP32: two blocks per SM), 0 the
-                                 library's choice (2 when the finest level has more tiles than
-                                 mode 1 keeps resident, else 1; FP64 always 2) */
+                                 staged with its rows, 2 one colour's at a time, double
+                                 buffered (more blocks per SM), 0 the library's choice (1 when
+                                 it fits in shared memory: FP32; else 2: FP64) */
 } hmec_params;
 
 /* mg_flags bits */
