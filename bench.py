@@ -69,6 +69,9 @@ def parse():
                     help="for ncu --profile-from-start off: --warmup steps of --config's model in --form, then "
                          "--steps steps between cudaProfilerStart and cudaProfilerStop; no JSON line")
     ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"], help="the form --profile-window runs")
+    ap.add_argument("--markers-per-side", type=int, default=0,
+                    help="--profile-window only: markers per cell side instead of the configuration's (a smaller "
+                         "capture for the solver's kernels, which do not depend on the marker count)")
     return ap.parse_args()
 
 
@@ -83,7 +86,8 @@ def profile_window(args):
 
     torch.cuda.set_device(0)
     form = hmec.FORM_MIXED if args.form == "mixed" else hmec.FORM_FP64
-    m, _, _, p = make_model(form, args.config, graph=0)
+    extra = dict(mx=args.markers_per_side, my=args.markers_per_side) if args.markers_per_side > 0 else {}
+    m, _, _, p = make_model(form, args.config, graph=0, **extra)
     for _ in range(args.warmup):
         m.timestep()
     torch.cuda.synchronize()
