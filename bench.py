@@ -88,11 +88,13 @@ def profile_window(args):
     form = hmec.FORM_MIXED if args.form == "mixed" else hmec.FORM_FP64
     extra = dict(mx=args.markers_per_side, my=args.markers_per_side) if args.markers_per_side > 0 else {}
     m, _, _, p = make_model(form, args.config, graph=0, **extra)
+    # statuses are not checked: a capture with fewer markers per cell is a
+    # different model, which may not converge; the kernels are the same
     for _ in range(args.warmup):
-        m.timestep()
+        m.timestep(check=False)
     torch.cuda.synchronize()
     torch.cuda.profiler.start()
-    reps = [m.timestep() for _ in range(args.steps)]
+    reps = [m.timestep(check=False) for _ in range(args.steps)]
     torch.cuda.synchronize()
     torch.cuda.profiler.stop()
     print("profiled %d steps of %s (%s): global iterations %s, Krylov iterations %s"
