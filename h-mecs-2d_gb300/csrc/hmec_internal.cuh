@@ -129,10 +129,9 @@ struct Level {
     int16_t* std_off = nullptr;
     uint8_t* std_t = nullptr;
     bool offs_ready = false;
-    // per tile: ownership flags of its window and the per-lane colour table
-    // (fixed by the geometry), and its boundary rows packed for one bulk copy
-    // (rebuilt with each assembly)
-    uint8_t* own_t = nullptr;
+    // per tile: the per-lane colour table with the ownership of each lane's
+    // unknown (fixed by the geometry), and its boundary rows packed (rebuilt
+    // with each assembly; the smoothing pass reads them from global memory)
     int32_t* meta_t = nullptr;
     unsigned char* bpack = nullptr;
     int pack_bytes = 0;

@@ -454,7 +454,6 @@ constexpr int RSTR = ((TILE + 1) * 6 + 7) / 8 * 8;                // staged rows
 constexpr int ROWS_MAX = (TILE + 1) * RSTR;                       // staged rows of a tile
 constexpr int PV_MAX = ((TILE + 2) / 3) * ((TILE + 2) / 3);       // patches of one colour in a tile
 constexpr int TB_MAX = 320;                                       // boundary rows of a tile
-constexpr int OWN_STRIDE = (WIN_MAX + 15) / 16 * 16;              // bytes of a tile's ownership flags
 static_assert(WIN_MAX == WSTR * WSTR * 6, "window size");
 static_assert(PV_MAX * 16 <= TILE_BS, "a colour's patches fit the block");
 static_assert((TILE * 6 * 4) % 16 == 0, "a tile's first staged row starts on 16 bytes in the padded layout");
@@ -678,7 +677,6 @@ struct StageArgs {
     T* x;
     T* xalt;
     const int32_t* tb_start;
-    const uint8_t* own_t;  // per tile: window ownership flags
     const int32_t* meta_t; // per tile: per-lane colour table
     const unsigned char* bpack;  // per tile: boundary-row pack
     int ntile_i, ntiles;
@@ -699,7 +697,7 @@ struct StageArgs {
 // inverses: about 143 KB, one block per SM; a level with more tiles than
 // blocks restages a tile every time a block takes it up).
 struct StageLayout {
-    int xs, val, b, pv, pack, bb, bdel, own, bar, total;
+    int xs, val, b, pv, bb, bdel, bar, total;
 };
 
 __host__ __device__ __forceinline__ int align_up(int x, int a) { return (x + a - 1) / a * a; }
@@ -717,8 +715,6 @@ __host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int t
     const int st = (int)sizeof(T);
     take(L.val, HMEC_W * ROWS_MAX * st, 128);
     take(L.pv, (pv_whole ? TILE * TILE : 2 * PV_MAX) * 100 * st, 128);
-    take(L.pack, pack_bytes<T>(tb_cap), 128);
-    take(L.own, OWN_STRIDE, 128);
     take(L.xs, WIN_MAX * st, 16);
     take(L.b, ROWS_MAX * st, 16);
     take(L.bb, tb_cap * st, 16);
@@ -728,12 +724,10 @@ __host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int t
     return L;
 }
 
-// Bytes one tile's stage receives on its barrier (the boundary pack only for
-// a tile that has boundary rows).
+// Bytes one tile's stage receives on its barrier.
 template <typename T>
-__host__ __device__ __forceinline__ unsigned stage_tx_bytes(bool whole, int tb_cap, bool pack) {
-    return (unsigned)(HMEC_W * (TILE + 1) * RSTR * sizeof(T) + (whole ? TILE * TILE * 100 * sizeof(T) : 0) +
-                      (pack ? pack_bytes<T>(tb_cap) : 0) + OWN_STRIDE);
+__host__ __device__ __forceinline__ unsigned stage_tx_bytes(bool whole) {
+    return (unsigned)(HMEC_W * (TILE + 1) * RSTR * sizeof(T) + (whole ? TILE * TILE * 100 * sizeof(T) : 0));
 }
 
 // bc = R (b - A x): each coarse row forms the residuals of its fine rows.
@@ -836,15 +830,10 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
     T* xs = reinterpret_cast<T*>(smem_raw + Lo.xs);
     T* sval = reinterpret_cast<T*>(smem_raw + Lo.val);
     T* sb = reinterpret_cast<T*>(smem_raw + Lo.b);
-    unsigned char* own = smem_raw + Lo.own;
+
     unsigned long long* bar = sb_.bar;
     T* pv = reinterpret_cast<T*>(smem_raw + Lo.pv);
     const int TBC = t.tb_cap;
-    unsigned char* pack = smem_raw + Lo.pack;  // the pack layout of k_stage_bpack
-    T* bval = reinterpret_cast<T*>(pack);
-    T* bdiag = bval + HMEC_W * TBC;
-    int16_t* boff = reinterpret_cast<int16_t*>(bdiag + TBC);
-    int16_t* blr = boff + HMEC_W * TBC;
     T* bbv = reinterpret_cast<T*>(smem_raw + Lo.bb);
     T* bdel = reinterpret_cast<T*>(smem_raw + Lo.bdel);
     constexpr bool whole = WHOLE;
@@ -889,17 +878,14 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
             if (fresh) {
                 nbt = min(t.tb_start[tile + 1] - t.tb_start[tile], TBC);
                 tstd = t.std_t[tile];
-                // one thread: the tile's rows (values, one 3-D box), its
-                // inverses, ownership flags and, when it has boundary rows,
-                // its boundary pack
+                // one thread: the tile's rows (values, one 3-D box) and its
+                // inverses (the edge tiles' boundary rows are read from
+                // their pack in global memory)
                 if (threadIdx.x == 0) {
                     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                    mbar_expect_tx(&bar[2], stage_tx_bytes<T>(whole, TBC, nbt > 0));
+                    mbar_expect_tx(&bar[2], stage_tx_bytes<T>(whole));
                     tma_load_3d(sval, &t.tm_val, (i0 - 1) * 6, j0 - 1, 0, &bar[2]);
                     if (whole) tma_load_3d(pv, &t.tm_pinv, 0, i0 - 1, j0 - 1, &bar[2]);
-                    bulk_g2s(own, t.own_t + (size_t)tile * OWN_STRIDE, OWN_STRIDE, &bar[2]);
-                    if (nbt > 0)
-                        bulk_g2s(pack, t.bpack + (size_t)tile * pack_bytes<T>(TBC), pack_bytes<T>(TBC), &bar[2]);
                 }
                 // the rows' rhs: per staged column one run of RI*6 values
                 const int RI = i1 - i0 + 1, RJ = j1 - j0 + 1, nch = RI * 3;
@@ -961,6 +947,7 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                 }
                 const int m = meta[c];
                 const bool valid = (m >> 30) & 1;
+                const bool mine = ((unsigned)m >> 31) != 0u;  // the tile owns this patch row's unknown
                 const int lrow = m & 2047, rl = (m >> 11) & 2047;
                 T pr[PB];
                 T r = 0;
@@ -996,10 +983,15 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                 }
                 // same-class patches never read each other's unknowns, and the
                 // shuffles above order this patch's reads before its writes
-                if (valid && own[lrow]) xs[lrow] += d;
+                if (valid && mine) xs[lrow] += d;
                 __syncthreads();
             }
             // this tile's boundary rows: one Jacobi pass on the window
+            const unsigned char* gpack = t.bpack + (size_t)tile * pack_bytes<T>(TBC);  // k_stage_bpack's layout
+            const T* bval = reinterpret_cast<const T*>(gpack);
+            const T* bdiag = bval + HMEC_W * TBC;
+            const int16_t* boff = reinterpret_cast<const int16_t*>(bdiag + TBC);
+            const int16_t* blr = boff + HMEC_W * TBC;
             for (int k = threadIdx.x; k < nbt; k += blockDim.x) {
                 const int lr = blr[k];
                 T acc = bbv[k];
@@ -1013,9 +1005,10 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
             // publish the owned unknowns
             if (!solo || s == nsweeps - 1) {
                 for (int lw = threadIdx.x; lw < WIN_MAX; lw += blockDim.x) {
-                    if (!own[lw]) continue;
                     const int lc = lw / 6, v = lw - 6 * lc;
                     const int ci = wi0 + lc % WSTR, cj = wj0 + lc / WSTR;
+                    if (ci < 0 || ci > g.Ny || cj < 0 || cj > g.Nx || unknown_tile(g, t.ntile_i, ci, cj, v) != tile)
+                        continue;
                     dst[(cj * g.Ny1 + ci) * 6 + v] = xs[lw];
                 }
             }
@@ -1883,26 +1876,27 @@ static int alloc_level(hmec_inst* ctx, Level& L, bool mixed, bool coarse) {
         HMEC_CUDA(ctx, cudaMalloc(&L.tbnd_list, sizeof(int32_t) * bl.size()));
         HMEC_CUDA(ctx, cudaMemcpy(L.tbnd_start, bs.data(), sizeof(int32_t) * bs.size(), cudaMemcpyHostToDevice));
         HMEC_CUDA(ctx, cudaMemcpy(L.tbnd_list, bl.data(), sizeof(int32_t) * bl.size(), cudaMemcpyHostToDevice));
-        // per tile: window ownership flags and the per-lane colour table
-        std::vector<uint8_t> ownt((size_t)L.ntiles * OWN_STRIDE, 0);
+        // per tile: the per-lane colour table, with bit 31 set where the tile
+        // owns the unknown of the lane's patch row
         std::vector<int32_t> meta((size_t)L.ntiles * 9 * TILE_BS, 0);
         for (int tile = 0; tile < L.ntiles; tile++) {
             const int ti = tile % L.ntile_i, tj = tile / L.ntile_i;
             const int i0 = 1 + ti * TILE, j0 = 1 + tj * TILE;
             const int i1 = std::min(i0 + TILE, g.Ny), j1 = std::min(j0 + TILE, g.Nx);
-            for (int lw = 0; lw < WIN_MAX; lw++) {
-                const int lc = lw / 6, v = lw - 6 * lc;
-                const int ci = i0 - 2 + lc % WSTR, cj = j0 - 2 + lc / WSTR;
-                if (ci >= 0 && ci <= g.Ny && cj >= 0 && cj <= g.Nx)
-                    ownt[(size_t)tile * OWN_STRIDE + lw] = owner[(cj * g.Ny1 + ci) * 6 + v] == tile ? 1 : 0;
-            }
             for (int c = 0; c < 9; c++)
-                for (int tt = 0; tt < TILE_BS; tt++)
-                    meta[((size_t)tile * 9 + c) * TILE_BS + tt] = lane_meta(c, tt, i0, j0, i1, j1);
+                for (int tt = 0; tt < TILE_BS; tt++) {
+                    int m = lane_meta(c, tt, i0, j0, i1, j1);
+                    if ((m >> 30) & 1) {
+                        const int lw = m & 2047, lc = lw / 6, v = lw - 6 * lc;
+                        const int ci = i0 - 2 + lc % WSTR, cj = j0 - 2 + lc / WSTR;
+                        if (ci >= 0 && ci <= g.Ny && cj >= 0 && cj <= g.Nx &&
+                            owner[(cj * g.Ny1 + ci) * 6 + v] == tile)
+                            m = (int)((unsigned)m | 0x80000000u);
+                    }
+                    meta[((size_t)tile * 9 + c) * TILE_BS + tt] = m;
+                }
         }
-        HMEC_CUDA(ctx, cudaMalloc(&L.own_t, ownt.size()));
         HMEC_CUDA(ctx, cudaMalloc(&L.meta_t, sizeof(int32_t) * meta.size()));
-        HMEC_CUDA(ctx, cudaMemcpy(L.own_t, ownt.data(), ownt.size(), cudaMemcpyHostToDevice));
         HMEC_CUDA(ctx, cudaMemcpy(L.meta_t, meta.data(), sizeof(int32_t) * meta.size(), cudaMemcpyHostToDevice));
         // the smoother's padded matrix copy, the boundary packs, and their TMA maps
         const size_t st = mixed ? sizeof(float) : sizeof(double);
@@ -2101,7 +2095,6 @@ void solver_free(hmec_inst* ctx) {
         cudaFree(L.offs);
         cudaFree(L.std_off);
         cudaFree(L.std_t);
-        cudaFree(L.own_t);
         cudaFree(L.meta_t);
         cudaFree(L.bpack);
         cudaFree(L.pmx);
@@ -2275,6 +2268,7 @@ static int stage_config(hmec_inst* ctx, Level& L) {
     for (int w = 0; w < 2; w++) {
         const void* kern = w ? (const void*)k_smooth_stage<T, true> : (const void*)k_smooth_stage<T, false>;
         HMEC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+        HMEC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         smem[w] = stage_layout<T>(w, L.tb_cap).total;
         int per_sm = 0;
         if (smem[w] <= optin)
@@ -2347,7 +2341,6 @@ static StageArgs<T> stage_args(hmec_inst* ctx, size_t l, const T* b, T* x, int n
     t.x = x;
     t.xalt = x_alt<T>(L);
     t.tb_start = L.tbnd_start;
-    t.own_t = L.own_t;
     t.meta_t = L.meta_t;
     t.bpack = L.bpack;
     t.ntile_i = L.ntile_i;
@@ -2485,6 +2478,7 @@ static int vcycle_fused(hmec_inst* ctx, const T* b0, T* x0, bool* used) {
         // the kernel, and concurrent models (ensembles) launch it with
         // different layouts
         HMEC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+        HMEC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TILE_BS, (size_t)smem));
         if (grid < 1 || grid > per_sm * nsm) return HMEC_OK;
         // pre-smoothing down the levels, the coarsest level, post-smoothing up
