@@ -129,9 +129,11 @@ struct Level {
     int16_t* std_off = nullptr;
     uint8_t* std_t = nullptr;
     bool offs_ready = false;
-    // per tile: the per-lane colour table with the ownership of each lane's
-    // unknown (fixed by the geometry), and its boundary rows packed (rebuilt
-    // with each assembly; the smoothing pass reads them from global memory)
+    // per tile: its window's ownership bits and the per-lane colour table
+    // with the ownership of each lane's unknown (fixed by the geometry), and
+    // its boundary rows packed (rebuilt with each assembly; the smoothing
+    // pass reads them from global memory)
+    uint32_t* own_t = nullptr;
     int32_t* meta_t = nullptr;
     unsigned char* bpack = nullptr;
     int pack_bytes = 0;

@@ -290,20 +290,27 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
 // Corner sums: cs[(s * 4 + corner) * ncell + cj * (Ny-1) + ci], s = 0 the
 // weight, s = 1..NP the properties.
 // rec: the grid's marker records (RW floats each: dx, dy, NP properties).
-template <bool ROWP, bool COLP, int NP, int RW>
-__global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const float* __restrict__ rec,
-                            double* __restrict__ cs) {
+// One thread's share of cell (ci, cj): the weight sums when WT, and the
+// sums of properties [Q0, Q1).  Every sum sees the same operations in the
+// same order whichever thread holds it, so splitting a cell's properties
+// over threads changes no result.
+template <bool ROWP, bool COLP, int NP, int RW, int Q0, int Q1, bool WT>
+__device__ __forceinline__ void cell_sums_part(const Geo& g, const int32_t* __restrict__ start,
+                                               const float* __restrict__ rec, double* __restrict__ cs, int ci,
+                                               int cj) {
     static_assert(RW % 4 == 0 && RW >= 4 + 2 * NP, "record layout");
+    constexpr int NQ = Q1 - Q0;
+    // the record's float4s this share reads: the distances (0) and those
+    // holding properties Q0..Q1-1 (property q at floats 4 + 2q, 5 + 2q)
+    constexpr int F0 = 1 + Q0 / 2, F1 = 1 + (Q1 - 1) / 2;
     const int NCI = g.Ny - 1, NCJ = g.Nx - 1;
-    const int ci = blockIdx.x * blockDim.x + threadIdx.x, cj = blockIdx.y;
-    if (ci >= NCI) return;
     const int HR = 2 * (g.Ny - 1), HC = 2 * (g.Nx - 1);
     const int r0 = ROWP ? 2 * ci - 1 : 2 * ci, c0 = COLP ? 2 * cj - 1 : 2 * cj;
     const int rlo = r0 < 0 ? 0 : r0, rhi = r0 + 1 > HR - 1 ? HR - 1 : r0 + 1;
     // double-float accumulators: [c] weight, [q][c] weight * property
-    float Wh[4] = {0, 0, 0, 0}, Wl[4] = {0, 0, 0, 0}, Sh[NP][4], Sl[NP][4];
+    float Wh[4] = {0, 0, 0, 0}, Wl[4] = {0, 0, 0, 0}, Sh[NQ][4], Sl[NQ][4];
 #pragma unroll
-    for (int q = 0; q < NP; q++)
+    for (int q = 0; q < NQ; q++)
 #pragma unroll
         for (int c = 0; c < 4; c++) Sh[q][c] = Sl[q][c] = 0;
     // the low parts collect the high parts' rounding errors; folding them back
@@ -317,15 +324,22 @@ __global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const floa
                 since_norm = 0;
 #pragma unroll
                 for (int c = 0; c < 4; c++) {
-                    df_norm(Wh[c], Wl[c]);
+                    if (WT) df_norm(Wh[c], Wl[c]);
 #pragma unroll
-                    for (int q = 0; q < NP; q++) df_norm(Sh[q][c], Sl[q][c]);
+                    for (int q = 0; q < NQ; q++) df_norm(Sh[q][c], Sl[q][c]);
                 }
             }
             float r[RW];
             const float4* r4 = reinterpret_cast<const float4*>(rec + (size_t)k * RW);
+            {
+                const float4 x = __ldg(r4);
+                r[0] = x.x;
+                r[1] = x.y;
+                r[2] = x.z;
+                r[3] = x.w;
+            }
 #pragma unroll
-            for (int t = 0; t < RW / 4; t++) {
+            for (int t = F0; t <= F1; t++) {
                 const float4 x = __ldg(r4 + t);
                 r[4 * t] = x.x;
                 r[4 * t + 1] = x.y;
@@ -351,11 +365,11 @@ __global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const floa
 #pragma unroll
             for (int c = 0; c < 4; c++) {
                 df_norm(wh[c], wl[c]);
-                df_acc(Wh[c], Wl[c], wh[c], wl[c]);
+                if (WT) df_acc(Wh[c], Wl[c], wh[c], wl[c]);
             }
 #pragma unroll
-            for (int q = 0; q < NP; q++) {
-                const float ph = r[4 + 2 * q], pl = r[5 + 2 * q];
+            for (int q = 0; q < NQ; q++) {
+                const float ph = r[4 + 2 * (Q0 + q)], pl = r[5 + 2 * (Q0 + q)];
 #pragma unroll
                 for (int c = 0; c < 4; c++) {
                     float t, er;
@@ -366,13 +380,32 @@ __global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const floa
         }
     }
     const size_t ncell = (size_t)NCI * NCJ, cell = (size_t)cj * NCI + ci;
+    if (WT) {
 #pragma unroll
-    for (int c = 0; c < 4; c++) cs[(size_t)c * ncell + cell] = f2d_bits(Wh[c]) + f2d_bits(Wl[c]);
+        for (int c = 0; c < 4; c++) cs[(size_t)c * ncell + cell] = f2d_bits(Wh[c]) + f2d_bits(Wl[c]);
+    }
 #pragma unroll
-    for (int q = 0; q < NP; q++)
+    for (int q = 0; q < NQ; q++)
 #pragma unroll
         for (int c = 0; c < 4; c++)
-            cs[((size_t)(1 + q) * 4 + c) * ncell + cell] = f2d_bits(Sh[q][c]) + f2d_bits(Sl[q][c]);
+            cs[((size_t)(1 + Q0 + q) * 4 + c) * ncell + cell] = f2d_bits(Sh[q][c]) + f2d_bits(Sl[q][c]);
+}
+
+// SPLIT = 2: blockIdx.z = 0 sums the weights and the first half of the
+// properties, z = 1 the second half (the basic grid's ten properties in one
+// thread need 172 registers; halves keep twice the warps resident).
+template <bool ROWP, bool COLP, int NP, int RW, int SPLIT>
+__global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const float* __restrict__ rec,
+                            double* __restrict__ cs) {
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x, cj = blockIdx.y;
+    if (ci >= g.Ny - 1) return;
+    if (SPLIT == 1) {
+        cell_sums_part<ROWP, COLP, NP, RW, 0, NP, true>(g, start, rec, cs, ci, cj);
+    } else if (blockIdx.z == 0) {
+        cell_sums_part<ROWP, COLP, NP, RW, 0, NP / 2, true>(g, start, rec, cs, ci, cj);
+    } else {
+        cell_sums_part<ROWP, COLP, NP, RW, NP / 2, NP, false>(g, start, rec, cs, ci, cj);
+    }
 }
 
 // Node (i, j): cells (i-1, j-1), (i, j-1), (i-1, j), (i, j), of which it is
@@ -670,7 +703,7 @@ int p2g_run(hmec_inst* ctx) {
     const float* rec_x = rec_p + (size_t)n * REC_P;
     const float* rec_y = rec_x + (size_t)n * REC_X;
     const int bs = ctx->bs_st;
-    dim3 bb(bs), gc(nblocks(g.Ny - 1, bs), g.Nx - 1);
+    dim3 bb(bs), gc(nblocks(g.Ny - 1, bs), g.Nx - 1), gc2(nblocks(g.Ny - 1, bs), g.Nx - 1, 2);
     dim3 gb(nblocks(g.Ny, bs), g.Nx), gs(nblocks(g.Ny1, bs), g.Nx1);
     // the four grids' gathers are independent: each pair (cell sums, node
     // sums) on a stream of its own (streams of this section only: the
@@ -687,25 +720,25 @@ int p2g_run(hmec_inst* ctx) {
     };
     {
         StreamScope scope(ctx, on(0));
-        HMEC_LAUNCH(ctx, (k_cell_sums<false, false, 10, REC_B>), gc, bb, 0, g, ctx->hc_start, rec_b, cs_b);
+        HMEC_LAUNCH(ctx, (k_cell_sums<false, false, 10, REC_B, 2>), gc2, bb, 0, g, ctx->hc_start, rec_b, cs_b);
         HMEC_LAUNCH(ctx, k_node_basic, gb, bb, 0, g, cs_b, f[HMEC_F_RHO], f[HMEC_F_KKK], f[HMEC_F_TTT], f[HMEC_F_GGG],
                     f[HMEC_F_ETA0], f[HMEC_F_COHT], f[HMEC_F_FRIT], f[HMEC_F_COHC], f[HMEC_F_FRIC], f[HMEC_F_DILC]);
     }
     {
         StreamScope scope(ctx, on(1));
-        HMEC_LAUNCH(ctx, (k_cell_sums<true, true, 5, REC_P>), gc, bb, 0, g, ctx->hc_start, rec_p, cs_p);
+        HMEC_LAUNCH(ctx, (k_cell_sums<true, true, 5, REC_P, 2>), gc2, bb, 0, g, ctx->hc_start, rec_p, cs_p);
         HMEC_LAUNCH(ctx, k_node_p, gs, bb, 0, g, cs_p, f[HMEC_F_ETAP], f[HMEC_F_POR], f[HMEC_F_ETAB0],
                     f[HMEC_F_ETAP0], f[HMEC_F_GGGP]);
     }
     {
         StreamScope scope(ctx, on(2));
-        HMEC_LAUNCH(ctx, (k_cell_sums<true, false, 4, REC_X>), gc, bb, 0, g, ctx->hc_start, rec_x, cs_x);
+        HMEC_LAUNCH(ctx, (k_cell_sums<true, false, 4, REC_X, 1>), gc, bb, 0, g, ctx->hc_start, rec_x, cs_x);
         HMEC_LAUNCH(ctx, k_node_vx, gs, bb, 0, g, cs_x, f[HMEC_F_RHOX], f[HMEC_F_ETADX], f[HMEC_F_RHOFX],
                     f[HMEC_F_PORX]);
     }
     {
         StreamScope scope(ctx, on(3));
-        HMEC_LAUNCH(ctx, (k_cell_sums<false, true, 4, REC_Y>), gc, bb, 0, g, ctx->hc_start, rec_y, cs_y);
+        HMEC_LAUNCH(ctx, (k_cell_sums<false, true, 4, REC_Y, 1>), gc, bb, 0, g, ctx->hc_start, rec_y, cs_y);
         HMEC_LAUNCH(ctx, k_node_vy, gs, bb, 0, g, cs_y, f[HMEC_F_RHOY], f[HMEC_F_ETADY], f[HMEC_F_RHOFY],
                     f[HMEC_F_PORY]);
     }

@@ -454,6 +454,7 @@ constexpr int RSTR = ((TILE + 1) * 6 + 7) / 8 * 8;                // staged rows
 constexpr int ROWS_MAX = (TILE + 1) * RSTR;                       // staged rows of a tile
 constexpr int PV_MAX = ((TILE + 2) / 3) * ((TILE + 2) / 3);       // patches of one colour in a tile
 constexpr int TB_MAX = 320;                                       // boundary rows of a tile
+constexpr int OWN_BYTES = (WIN_MAX + 127) / 128 * 16;             // a tile's window ownership bits (16-byte multiple)
 static_assert(WIN_MAX == WSTR * WSTR * 6, "window size");
 static_assert(PV_MAX * 16 <= TILE_BS, "a colour's patches fit the block");
 static_assert((TILE * 6 * 4) % 16 == 0, "a tile's first staged row starts on 16 bytes in the padded layout");
@@ -639,6 +640,15 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
+// Prefetch of a 3-D box into L2 (no shared memory, no barrier): the next
+// tile's stage streams from DRAM while this tile computes.
+__device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap* map, int c0, int c1, int c2) {
+    asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];\n" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(c0), "r"(c1), "r"(c2)
+                 : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
     unsigned ok;
     asm volatile(
@@ -677,6 +687,7 @@ struct StageArgs {
     T* x;
     T* xalt;
     const int32_t* tb_start;
+    const uint32_t* own_t; // per tile: window ownership bits
     const int32_t* meta_t; // per tile: per-lane colour table
     const unsigned char* bpack;  // per tile: boundary-row pack
     int ntile_i, ntiles;
@@ -697,7 +708,7 @@ struct StageArgs {
 // inverses: about 143 KB, one block per SM; a level with more tiles than
 // blocks restages a tile every time a block takes it up).
 struct StageLayout {
-    int xs, val, b, pv, bb, bdel, bar, total;
+    int xs, val, b, pv, pack, own, bb, bdel, bar, total;
 };
 
 __host__ __device__ __forceinline__ int align_up(int x, int a) { return (x + a - 1) / a * a; }
@@ -715,6 +726,8 @@ __host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int t
     const int st = (int)sizeof(T);
     take(L.val, HMEC_W * ROWS_MAX * st, 128);
     take(L.pv, (pv_whole ? TILE * TILE : 2 * PV_MAX) * 100 * st, 128);
+    take(L.pack, pack_bytes<T>(tb_cap), 128);
+    take(L.own, OWN_BYTES, 16);
     take(L.xs, WIN_MAX * st, 16);
     take(L.b, ROWS_MAX * st, 16);
     take(L.bb, tb_cap * st, 16);
@@ -724,10 +737,12 @@ __host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int t
     return L;
 }
 
-// Bytes one tile's stage receives on its barrier.
+// Bytes one tile's stage receives on its barrier (the boundary pack only for
+// a tile that has boundary rows).
 template <typename T>
-__host__ __device__ __forceinline__ unsigned stage_tx_bytes(bool whole) {
-    return (unsigned)(HMEC_W * (TILE + 1) * RSTR * sizeof(T) + (whole ? TILE * TILE * 100 * sizeof(T) : 0));
+__host__ __device__ __forceinline__ unsigned stage_tx_bytes(bool whole, int tb_cap, bool pack) {
+    return (unsigned)(HMEC_W * (TILE + 1) * RSTR * sizeof(T) + (whole ? TILE * TILE * 100 * sizeof(T) : 0) +
+                      (pack ? pack_bytes<T>(tb_cap) : 0) + OWN_BYTES);
 }
 
 // bc = R (b - A x): each coarse row forms the residuals of its fine rows.
@@ -830,10 +845,16 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
     T* xs = reinterpret_cast<T*>(smem_raw + Lo.xs);
     T* sval = reinterpret_cast<T*>(smem_raw + Lo.val);
     T* sb = reinterpret_cast<T*>(smem_raw + Lo.b);
+    uint32_t* ownb = reinterpret_cast<uint32_t*>(smem_raw + Lo.own);
 
     unsigned long long* bar = sb_.bar;
     T* pv = reinterpret_cast<T*>(smem_raw + Lo.pv);
     const int TBC = t.tb_cap;
+    unsigned char* pack = smem_raw + Lo.pack;  // the pack layout of k_stage_bpack
+    const T* bval = reinterpret_cast<const T*>(pack);
+    const T* bdiag = bval + HMEC_W * TBC;
+    const int16_t* boff = reinterpret_cast<const int16_t*>(bdiag + TBC);
+    const int16_t* blr = boff + HMEC_W * TBC;
     T* bbv = reinterpret_cast<T*>(smem_raw + Lo.bb);
     T* bdel = reinterpret_cast<T*>(smem_raw + Lo.bdel);
     constexpr bool whole = WHOLE;
@@ -878,14 +899,26 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
             if (fresh) {
                 nbt = min(t.tb_start[tile + 1] - t.tb_start[tile], TBC);
                 tstd = t.std_t[tile];
-                // one thread: the tile's rows (values, one 3-D box) and its
-                // inverses (the edge tiles' boundary rows are read from
-                // their pack in global memory)
+                // one thread: the tile's rows (values, one 3-D box), its
+                // inverses, its window's ownership bits and, when it has
+                // boundary rows, its boundary pack
                 if (threadIdx.x == 0) {
                     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                    mbar_expect_tx(&bar[2], stage_tx_bytes<T>(whole));
+                    mbar_expect_tx(&bar[2], stage_tx_bytes<T>(whole, TBC, nbt > 0));
                     tma_load_3d(sval, &t.tm_val, (i0 - 1) * 6, j0 - 1, 0, &bar[2]);
                     if (whole) tma_load_3d(pv, &t.tm_pinv, 0, i0 - 1, j0 - 1, &bar[2]);
+                    bulk_g2s(ownb, t.own_t + (size_t)tile * (OWN_BYTES / 4), OWN_BYTES, &bar[2]);
+                    if (nbt > 0)
+                        bulk_g2s(pack, t.bpack + (size_t)tile * pack_bytes<T>(TBC), pack_bytes<T>(TBC), &bar[2]);
+                    // the tile this block stages next (this sweep's next, or
+                    // the next sweep's first when it is another tile): into L2
+                    int nx = tile + gridDim.x;
+                    if (nx >= t.ntiles) nx = s + 1 < nsweeps ? (int)blockIdx.x : -1;
+                    if (nx >= 0 && nx != tile) {
+                        const int ni0 = 1 + (nx % t.ntile_i) * TILE, nj0 = 1 + (nx / t.ntile_i) * TILE;
+                        tma_prefetch_3d(&t.tm_val, (ni0 - 1) * 6, nj0 - 1, 0);
+                        if (whole) tma_prefetch_3d(&t.tm_pinv, 0, ni0 - 1, nj0 - 1);
+                    }
                 }
                 // the rows' rhs: per staged column one run of RI*6 values
                 const int RI = i1 - i0 + 1, RJ = j1 - j0 + 1, nch = RI * 3;
@@ -987,11 +1020,6 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                 __syncthreads();
             }
             // this tile's boundary rows: one Jacobi pass on the window
-            const unsigned char* gpack = t.bpack + (size_t)tile * pack_bytes<T>(TBC);  // k_stage_bpack's layout
-            const T* bval = reinterpret_cast<const T*>(gpack);
-            const T* bdiag = bval + HMEC_W * TBC;
-            const int16_t* boff = reinterpret_cast<const int16_t*>(bdiag + TBC);
-            const int16_t* blr = boff + HMEC_W * TBC;
             for (int k = threadIdx.x; k < nbt; k += blockDim.x) {
                 const int lr = blr[k];
                 T acc = bbv[k];
@@ -1005,10 +1033,9 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
             // publish the owned unknowns
             if (!solo || s == nsweeps - 1) {
                 for (int lw = threadIdx.x; lw < WIN_MAX; lw += blockDim.x) {
+                    if (!((ownb[lw >> 5] >> (lw & 31)) & 1u)) continue;
                     const int lc = lw / 6, v = lw - 6 * lc;
                     const int ci = wi0 + lc % WSTR, cj = wj0 + lc / WSTR;
-                    if (ci < 0 || ci > g.Ny || cj < 0 || cj > g.Nx || unknown_tile(g, t.ntile_i, ci, cj, v) != tile)
-                        continue;
                     dst[(cj * g.Ny1 + ci) * 6 + v] = xs[lw];
                 }
             }
@@ -1876,13 +1903,21 @@ static int alloc_level(hmec_inst* ctx, Level& L, bool mixed, bool coarse) {
         HMEC_CUDA(ctx, cudaMalloc(&L.tbnd_list, sizeof(int32_t) * bl.size()));
         HMEC_CUDA(ctx, cudaMemcpy(L.tbnd_start, bs.data(), sizeof(int32_t) * bs.size(), cudaMemcpyHostToDevice));
         HMEC_CUDA(ctx, cudaMemcpy(L.tbnd_list, bl.data(), sizeof(int32_t) * bl.size(), cudaMemcpyHostToDevice));
-        // per tile: the per-lane colour table, with bit 31 set where the tile
-        // owns the unknown of the lane's patch row
+        // per tile: its window's ownership bits, and the per-lane colour
+        // table with bit 31 set where the tile owns the unknown of the lane's
+        // patch row
+        std::vector<uint32_t> ownt((size_t)L.ntiles * (OWN_BYTES / 4), 0u);
         std::vector<int32_t> meta((size_t)L.ntiles * 9 * TILE_BS, 0);
         for (int tile = 0; tile < L.ntiles; tile++) {
             const int ti = tile % L.ntile_i, tj = tile / L.ntile_i;
             const int i0 = 1 + ti * TILE, j0 = 1 + tj * TILE;
             const int i1 = std::min(i0 + TILE, g.Ny), j1 = std::min(j0 + TILE, g.Nx);
+            for (int lw = 0; lw < WIN_MAX; lw++) {
+                const int lc = lw / 6, v = lw - 6 * lc;
+                const int ci = i0 - 2 + lc % WSTR, cj = j0 - 2 + lc / WSTR;
+                if (ci >= 0 && ci <= g.Ny && cj >= 0 && cj <= g.Nx && owner[(cj * g.Ny1 + ci) * 6 + v] == tile)
+                    ownt[(size_t)tile * (OWN_BYTES / 4) + (lw >> 5)] |= 1u << (lw & 31);
+            }
             for (int c = 0; c < 9; c++)
                 for (int tt = 0; tt < TILE_BS; tt++) {
                     int m = lane_meta(c, tt, i0, j0, i1, j1);
@@ -1896,6 +1931,8 @@ static int alloc_level(hmec_inst* ctx, Level& L, bool mixed, bool coarse) {
                     meta[((size_t)tile * 9 + c) * TILE_BS + tt] = m;
                 }
         }
+        HMEC_CUDA(ctx, cudaMalloc(&L.own_t, sizeof(uint32_t) * ownt.size()));
+        HMEC_CUDA(ctx, cudaMemcpy(L.own_t, ownt.data(), sizeof(uint32_t) * ownt.size(), cudaMemcpyHostToDevice));
         HMEC_CUDA(ctx, cudaMalloc(&L.meta_t, sizeof(int32_t) * meta.size()));
         HMEC_CUDA(ctx, cudaMemcpy(L.meta_t, meta.data(), sizeof(int32_t) * meta.size(), cudaMemcpyHostToDevice));
         // the smoother's padded matrix copy, the boundary packs, and their TMA maps
@@ -2095,6 +2132,7 @@ void solver_free(hmec_inst* ctx) {
         cudaFree(L.offs);
         cudaFree(L.std_off);
         cudaFree(L.std_t);
+        cudaFree(L.own_t);
         cudaFree(L.meta_t);
         cudaFree(L.bpack);
         cudaFree(L.pmx);
@@ -2268,7 +2306,6 @@ static int stage_config(hmec_inst* ctx, Level& L) {
     for (int w = 0; w < 2; w++) {
         const void* kern = w ? (const void*)k_smooth_stage<T, true> : (const void*)k_smooth_stage<T, false>;
         HMEC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-        HMEC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         smem[w] = stage_layout<T>(w, L.tb_cap).total;
         int per_sm = 0;
         if (smem[w] <= optin)
@@ -2341,6 +2378,7 @@ static StageArgs<T> stage_args(hmec_inst* ctx, size_t l, const T* b, T* x, int n
     t.x = x;
     t.xalt = x_alt<T>(L);
     t.tb_start = L.tbnd_start;
+    t.own_t = L.own_t;
     t.meta_t = L.meta_t;
     t.bpack = L.bpack;
     t.ntile_i = L.ntile_i;
@@ -2478,7 +2516,6 @@ static int vcycle_fused(hmec_inst* ctx, const T* b0, T* x0, bool* used) {
         // the kernel, and concurrent models (ensembles) launch it with
         // different layouts
         HMEC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-        HMEC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         HMEC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TILE_BS, (size_t)smem));
         if (grid < 1 || grid > per_sm * nsm) return HMEC_OK;
         // pre-smoothing down the levels, the coarsest level, post-smoothing up
