@@ -703,6 +703,15 @@ struct StageArgs {
     const int* done;       // the solve's convergence flag: set, the pass does nothing
 };
 
+// Whether the stage holds an edge tile's boundary pack (FP32) or the pass
+// reads it from global memory (FP64: the smaller stage leaves more of the
+// SM's memory to L1, which the window loads, prolongation and restriction
+// use; 1001x401: 46 against 53 ms per step).
+template <typename T>
+__host__ __device__ constexpr bool stage_pack() {
+    return sizeof(T) == 4;
+}
+
 // Shared-memory layout of the staged pass, in bytes.  Its size depends on the
 // inverse mode and on the level's boundary-row capacity (FP32 with whole-tile
 // inverses: about 143 KB, one block per SM; a level with more tiles than
@@ -726,7 +735,7 @@ __host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int t
     const int st = (int)sizeof(T);
     take(L.val, HMEC_W * ROWS_MAX * st, 128);
     take(L.pv, (pv_whole ? TILE * TILE : 2 * PV_MAX) * 100 * st, 128);
-    take(L.pack, pack_bytes<T>(tb_cap), 128);
+    if (stage_pack<T>()) take(L.pack, pack_bytes<T>(tb_cap), 128);
     take(L.own, OWN_BYTES, 16);
     take(L.xs, WIN_MAX * st, 16);
     take(L.b, ROWS_MAX * st, 16);
@@ -738,7 +747,7 @@ __host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int t
 }
 
 // Bytes one tile's stage receives on its barrier (the boundary pack only for
-// a tile that has boundary rows).
+// a tile that has boundary rows, in the FP32 stage).
 template <typename T>
 __host__ __device__ __forceinline__ unsigned stage_tx_bytes(bool whole, int tb_cap, bool pack) {
     return (unsigned)(HMEC_W * (TILE + 1) * RSTR * sizeof(T) + (whole ? TILE * TILE * 100 * sizeof(T) : 0) +
@@ -850,11 +859,6 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
     unsigned long long* bar = sb_.bar;
     T* pv = reinterpret_cast<T*>(smem_raw + Lo.pv);
     const int TBC = t.tb_cap;
-    unsigned char* pack = smem_raw + Lo.pack;  // the pack layout of k_stage_bpack
-    const T* bval = reinterpret_cast<const T*>(pack);
-    const T* bdiag = bval + HMEC_W * TBC;
-    const int16_t* boff = reinterpret_cast<const int16_t*>(bdiag + TBC);
-    const int16_t* blr = boff + HMEC_W * TBC;
     T* bbv = reinterpret_cast<T*>(smem_raw + Lo.bb);
     T* bdel = reinterpret_cast<T*>(smem_raw + Lo.bdel);
     constexpr bool whole = WHOLE;
@@ -904,12 +908,13 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                 // boundary rows, its boundary pack
                 if (threadIdx.x == 0) {
                     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                    mbar_expect_tx(&bar[2], stage_tx_bytes<T>(whole, TBC, nbt > 0));
+                    mbar_expect_tx(&bar[2], stage_tx_bytes<T>(whole, TBC, stage_pack<T>() && nbt > 0));
                     tma_load_3d(sval, &t.tm_val, (i0 - 1) * 6, j0 - 1, 0, &bar[2]);
                     if (whole) tma_load_3d(pv, &t.tm_pinv, 0, i0 - 1, j0 - 1, &bar[2]);
                     bulk_g2s(ownb, t.own_t + (size_t)tile * (OWN_BYTES / 4), OWN_BYTES, &bar[2]);
-                    if (nbt > 0)
-                        bulk_g2s(pack, t.bpack + (size_t)tile * pack_bytes<T>(TBC), pack_bytes<T>(TBC), &bar[2]);
+                    if (stage_pack<T>() && nbt > 0)
+                        bulk_g2s(smem_raw + Lo.pack, t.bpack + (size_t)tile * pack_bytes<T>(TBC), pack_bytes<T>(TBC),
+                                 &bar[2]);
                     // the tile this block stages next (this sweep's next, or
                     // the next sweep's first when it is another tile): into L2
                     int nx = tile + gridDim.x;
@@ -1019,7 +1024,14 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                 if (valid && mine) xs[lrow] += d;
                 __syncthreads();
             }
-            // this tile's boundary rows: one Jacobi pass on the window
+            // this tile's boundary rows: one Jacobi pass on the window (the
+            // pack in k_stage_bpack's layout, staged or in global memory)
+            const unsigned char* pack =
+                stage_pack<T>() ? smem_raw + Lo.pack : t.bpack + (size_t)tile * pack_bytes<T>(TBC);
+            const T* bval = reinterpret_cast<const T*>(pack);
+            const T* bdiag = bval + HMEC_W * TBC;
+            const int16_t* boff = reinterpret_cast<const int16_t*>(bdiag + TBC);
+            const int16_t* blr = boff + HMEC_W * TBC;
             for (int k = threadIdx.x; k < nbt; k += blockDim.x) {
                 const int lr = blr[k];
                 T acc = bbv[k];
