@@ -182,6 +182,12 @@ int hmec_tune_apply(hmec_params* p) {
     get("krylov_blocks", &p->krylov_blocks, 0, 1 << 16);
     get("smooth_blocks", &p->smooth_blocks, 0, 1 << 16);
     get("smooth_inverses", &p->smooth_inverses, 0, 2);
+    {
+        // the tuned multigrid options (local sweeps); the others stay
+        int32_t f = -1;
+        get("mg_flags", &f, 0, 15);
+        if (f >= 0) p->mg_flags = (p->mg_flags & ~HMEC_MG_LOCAL_SWEEPS) | (f & HMEC_MG_LOCAL_SWEEPS);
+    }
     return 1;
 }
 

@@ -699,6 +699,7 @@ struct StageArgs {
     const T* rw;
     T* bc;
     int tb_cap;            // boundary rows one tile's stage holds
+    int local;             // HMEC_MG_LOCAL_SWEEPS: a tile's sweeps back to back on one stage
     int* status;
     const int* done;       // the solve's convergence flag: set, the pass does nothing
 };
@@ -893,7 +894,13 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
     // every unknown, so the sweeps stay in shared memory and only the last
     // one is published -- no grid barrier or window reload in between
     const bool solo = t.ntiles == 1 && gridDim.x == 1;
-    for (int s = 0; s < nsweeps; s++) {
+    // local sweeps (a solo tile, or on request for every level): a tile runs
+    // all the pass's sweeps on one stage, its neighbours' unknowns taken from
+    // the start of the pass -- one stage, one window load and one grid
+    // barrier per pass instead of per sweep
+    const bool local = solo || t.local;
+    const int outer = local ? 1 : nsweeps, inner = local ? nsweeps : 1;
+    for (int so = 0; so < outer; so++) {
         for (int tile = blockIdx.x; tile < t.ntiles; tile += gridDim.x) {
             const int ti = tile % t.ntile_i, tj = tile / t.ntile_i;
             const int i0 = 1 + ti * TILE, j0 = 1 + tj * TILE;
@@ -918,7 +925,7 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                     // the tile this block stages next (this sweep's next, or
                     // the next sweep's first when it is another tile): into L2
                     int nx = tile + gridDim.x;
-                    if (nx >= t.ntiles) nx = s + 1 < nsweeps ? (int)blockIdx.x : -1;
+                    if (nx >= t.ntiles) nx = so + 1 < outer ? (int)blockIdx.x : -1;
                     if (nx >= 0 && nx != tile) {
                         const int ni0 = 1 + (nx % t.ntile_i) * TILE, nj0 = 1 + (nx / t.ntile_i) * TILE;
                         tma_prefetch_3d(&t.tm_val, (ni0 - 1) * 6, nj0 - 1, 0);
@@ -940,10 +947,12 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                 for (int k = threadIdx.x; k < nbt; k += blockDim.x) bbv[k] = t.b[brow[k]];
                 staged = tile;
             }
+            for (int si = 0; si < inner; si++) {
+            const int s = local ? si : so;  // the sweep
             if (!whole && threadIdx.x == 0) issue_pinv(t, pv, bar, 0, 0, i0, j0, i1, j1);
             // the x window: zero, x + P xc, or the previous sweep's values
-            // (a solo tile keeps its window from the previous sweep)
-            if (!(solo && s > 0)) {
+            // (local sweeps keep the window from the previous sweep)
+            if (!(local && s > 0)) {
                 constexpr int WPT = (WIN_MAX + TILE_BS - 1) / TILE_BS;
                 T xv[WPT];
 #pragma unroll
@@ -965,7 +974,7 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
             }
             cp_async_wait_all();
             __syncthreads();
-            if (fresh) {
+            if (fresh && si == 0) {
                 mbar_wait(&bar[2], use2 & 1, t.status);
                 use2++;
             }
@@ -1043,7 +1052,7 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
             for (int k = threadIdx.x; k < nbt; k += blockDim.x) xs[blr[k]] += bdel[k];
             __syncthreads();
             // publish the owned unknowns
-            if (!solo || s == nsweeps - 1) {
+            if (!local || s == nsweeps - 1) {
                 for (int lw = threadIdx.x; lw < WIN_MAX; lw += blockDim.x) {
                     if (!((ownb[lw >> 5] >> (lw & 31)) & 1u)) continue;
                     const int lc = lw / 6, v = lw - 6 * lc;
@@ -1052,10 +1061,11 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                 }
             }
             __syncthreads();
+            }
         }
         // the last sweep needs the barrier only when this launch reads the
         // result back: the residual restriction, or a copy into x
-        const bool last_in_x = s == nsweeps - 1 && dst == t.x && !t.bc;
+        const bool last_in_x = so == outer - 1 && dst == t.x && !t.bc;
         if (!solo && !last_in_x) cg::this_grid().sync();
         src = dst;
         dst = (dst == t.xalt) ? t.x : t.xalt;
@@ -2404,6 +2414,7 @@ static StageArgs<T> stage_args(hmec_inst* ctx, size_t l, const T* b, T* x, int n
     t.rw = nullptr;
     t.bc = nullptr;
     t.tb_cap = L.tb_cap;
+    t.local = (ctx->p.mg_flags & HMEC_MG_LOCAL_SWEEPS) ? 1 : 0;
     t.status = &ctx->ds->status;
     t.done = sv.done;
     const double st = sizeof(T), N = L.g.N;

@@ -27,7 +27,7 @@ STATUS = {0: "HMEC_OK", -1: "HMEC_ERR_ARG", -2: "HMEC_ERR_CUDA", -3: "HMEC_ERR_B
           -9: "HMEC_ERR_TIMEOUT"}
 FORM_FP64, FORM_MIXED = 0, 1
 # hmec_params.mg_flags bits (include/hmec.h, enum hmec_mg_flags)
-MG_DARCY_HARMONIC, MG_UNTILED, MG_PASS_LAUNCHES = 1, 2, 4
+MG_DARCY_HARMONIC, MG_UNTILED, MG_PASS_LAUNCHES, MG_LOCAL_SWEEPS = 1, 2, 4, 8
 
 
 class HmecError(RuntimeError):

@@ -10,7 +10,9 @@ and keeps the fastest:
   - the blocks of the cooperative Arnoldi step;
   - the most blocks of one smoothing launch;
   - whether the smoothing pass stages a whole tile's Vanka inverses or one
-    colour's at a time.
+    colour's at a time;
+  - whether a tile runs a pass's sweeps back to back on one stage (local
+    sweeps, mg_flags bit 8).
 
 The search is coordinate-wise: the cycle shapes first, then each launch
 parameter in turn with the others at their best so far.  A candidate whose
@@ -39,10 +41,11 @@ TABLE = os.path.join(HERE, "tune_table.json")
 CYCLES = [(5, 2, 2, 8), (4, 2, 2, 8), (6, 2, 2, 4), (5, 1, 1, 8), (4, 1, 1, 8), (5, 1, 2, 8), (3, 2, 2, 8),
           (6, 1, 1, 4)]
 LAUNCH = [("bs_stencil", [64, 128, 256]), ("bs_sort", [128, 256, 512]),
-          ("krylov_blocks", [152, 304, 456, 608]), ("smooth_blocks", [0, 152]), ("smooth_inverses", [1, 2])]
+          ("krylov_blocks", [152, 304, 456, 608]), ("smooth_blocks", [0, 152]), ("smooth_inverses", [1, 2]),
+          ("mg_flags", [1 | 8])]
 SOLVER = dict(krylov_rtol=1e-15, krylov_restart=40, krylov_maxit=4000)
 DEFAULT = dict(mg_levels=5, mg_pre=2, mg_post=2, mg_coarse_sweeps=8, bs_stencil=64, bs_sort=256, krylov_blocks=0,
-               smooth_blocks=0, smooth_inverses=0)
+               smooth_blocks=0, smooth_inverses=0, mg_flags=1)
 
 
 def grid_case(name: str, seed_shift: int = 17):

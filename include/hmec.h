@@ -146,7 +146,13 @@ enum hmec_mg_flags {
      * fused V-cycle holds its fine level's grid through the small coarse
      * levels too), and at most a quarter of the SMs per pass, so that
      * several models' passes run side by side. */
-    HMEC_MG_PASS_LAUNCHES = 4
+    HMEC_MG_PASS_LAUNCHES = 4,
+    /* Local sweeps: a tile runs all the sweeps of a smoothing pass back to
+     * back on one stage, its neighbours' unknowns taken from the start of the
+     * pass (multiplicative inside a tile for every sweep, additive across
+     * tile borders for the pass): one stage, one window load and one grid
+     * barrier per pass instead of per sweep. */
+    HMEC_MG_LOCAL_SWEEPS = 8
 };
 
 /* ------------------------------------------------------------- node fields */

@@ -147,10 +147,22 @@ def test_timestep_replay(preset, nsteps, form, quirk):
     reference does (Q1, the zeroing at :377-381 acts on copies); the GPU
     restarts them every step, and the ratios agree to rounding.
     """
+    _replay(preset, nsteps, form, quirk)
+
+
+@pytest.mark.parametrize("form", [hmec.FORM_FP64, hmec.FORM_MIXED])
+def test_timestep_replay_local_sweeps(form):
+    """The preconditioner with local sweeps (HMEC_MG_LOCAL_SWEEPS: a tile's
+    sweeps back to back on one stage) gives the same steps within the same
+    bounds: the FP64 FGMRES reaches the same tolerance whatever the smoother."""
+    _replay("c0", 5, form, 0, mg_flags=hmec.MG_DARCY_HARMONIC | hmec.MG_LOCAL_SWEEPS, autotune=0)
+
+
+def _replay(preset, nsteps, form, quirk, **extra):
     o, mk, nodes = pairs.oracle_for(preset, quirk_accumulate_sums=quirk)
     o2, _, _ = pairs.oracle_for(preset, quirk_accumulate_sums=quirk)
     o2.ordering = "MMD_AT_PLUS_A"
-    m = pairs.model_for(preset, mk, nodes, form=form)
+    m = pairs.model_for(preset, mk, nodes, form=form, **extra)
     log = []
     for _ in range(nsteps):
         snap = o.snapshot()
