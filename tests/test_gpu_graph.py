@@ -46,7 +46,10 @@ def test_graph_steps_equal_host_driven_steps(preset, form):
     b.timestep()
     da, db = a.launches - la, b.launches - lb
     assert da > 0 and db > 0
-    assert abs(da - db) <= 0.2 * db, (da, db)  # host-driven steps also launch after convergence
+    # host-driven steps launch Arnoldi steps past convergence (the host looks
+    # at the flag only now and then); graph steps run the restart body's tail
+    # (least squares, update) in the converged cycle too
+    assert abs(da - db) <= 0.35 * db, (da, db)
     a.close()
     b.close()
 
