@@ -189,19 +189,39 @@ __global__ void k_rescale_guess(Geo g, const DevScalars* ds, double* S) {
 }
 
 // ------------------------------------------------------------- a9 assembly
+// A row under construction: at most 11 distinct columns (the ELL width), in
+// registers -- every index below is a compile-time constant after unrolling,
+// so nothing goes to local memory.
+constexpr int RB_CAP = 12;
 struct RowB {
     int n;
-    int c[16];
-    double v[16];
-    __device__ void add(int col, double val) {  // duplicates summed in insertion order (setFromTriplets)
-        for (int k = 0; k < n; k++)
-            if (c[k] == col) {
-                v[k] += val;
-                return;
-            }
-        c[n] = col;
-        v[n] = val;
-        n++;
+    int c[RB_CAP];
+    double v[RB_CAP];
+    __device__ __forceinline__ void reset() {
+        n = 0;
+#pragma unroll
+        for (int k = 0; k < RB_CAP; k++) {
+            c[k] = 0;
+            v[k] = 0.0;
+        }
+    }
+    // duplicates summed in insertion order (setFromTriplets); branch-free,
+    // so the arrays stay in registers
+    __device__ __forceinline__ void add(int col, double val) {
+        bool dup = false;
+#pragma unroll
+        for (int k = 0; k < RB_CAP; k++) {
+            const bool hit = k < n && c[k] == col;
+            v[k] = hit ? v[k] + val : v[k];
+            dup = dup || hit;
+        }
+#pragma unroll
+        for (int k = 0; k < RB_CAP; k++) {
+            const bool put = !dup && k == n;
+            c[k] = put ? col : c[k];
+            v[k] = put ? val : v[k];
+        }
+        n += dup ? 0 : 1;
     }
 };
 
@@ -210,27 +230,46 @@ struct RowB {
 // [0.5, 1), so scaling is exact.
 __device__ __forceinline__ void emit_row(RowB& rb, int row, int N, int32_t* col, double* val, double* dscale,
                                          double* rhs_scaled, double* rhs_raw, double rhs) {
-    double mx = 0;
-    for (int k = 0; k < rb.n; k++) mx = DMAX(mx, fabs(rb.v[k]));
+    // frexp's exponent of max|a| from the largest biased exponent (integer
+    // pipe); zeros, subnormals, infinities and NaN take the FP64 route
+    int emax = 0;
+#pragma unroll
+    for (int k = 0; k < RB_CAP; k++)
+        if (k < rb.n) emax = max(emax, (int)((__double_as_longlong(rb.v[k]) >> 52) & 0x7FF));
     double s = 1.0;
-    if (mx > 0 && isfinite(mx)) {
-        int e;
-        frexp(mx, &e);
-        s = ldexp(1.0, -e);
-    }
-    // sort by column (rows have at most 11 entries)
-    for (int a = 1; a < rb.n; a++) {
-        int cc = rb.c[a];
-        double vv = rb.v[a];
-        int q = a;
-        while (q > 0 && rb.c[q - 1] > cc) {
-            rb.c[q] = rb.c[q - 1];
-            rb.v[q] = rb.v[q - 1];
-            q--;
+    if (emax >= 1 && emax <= 2044) {
+        s = __longlong_as_double((long long)(2045 - emax) << 52);  // 2^-(emax - 1022)
+    } else {
+        double mx = 0;
+#pragma unroll
+        for (int k = 0; k < RB_CAP; k++)
+            if (k < rb.n) mx = DMAX(mx, fabs(rb.v[k]));
+        if (mx > 0 && isfinite(mx)) {
+            int e;
+            frexp(mx, &e);
+            s = ldexp(1.0, -e);
         }
-        rb.c[q] = cc;
-        rb.v[q] = vv;
     }
+    // sort by column: odd-even transposition over the fixed width, unused
+    // entries last (columns are distinct, so the order is the sorted one)
+#pragma unroll
+    for (int k = 0; k < RB_CAP; k++)
+        if (k >= rb.n) rb.c[k] = 0x7FFFFFFF;
+#pragma unroll
+    for (int pass = 0; pass < RB_CAP; pass++) {
+#pragma unroll
+        for (int k = pass & 1; k + 1 < RB_CAP; k += 2) {
+            if (rb.c[k] > rb.c[k + 1]) {
+                const int tc = rb.c[k];
+                rb.c[k] = rb.c[k + 1];
+                rb.c[k + 1] = tc;
+                const double tv = rb.v[k];
+                rb.v[k] = rb.v[k + 1];
+                rb.v[k + 1] = tv;
+            }
+        }
+    }
+#pragma unroll
     for (int k = 0; k < HMEC_W; k++) {
         const size_t o = (size_t)k * N + row;
         if (k < rb.n) {
@@ -272,7 +311,7 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
     double r;
     if (sec == 0) {
         // 5c) Pt  :842-862
-        rb.n = 0;
+        rb.reset();
         r = 0;
         if (i == 0 || j == 0 || i == Ny || j == Nx) {
             rb.add(kp, 1);
@@ -293,7 +332,7 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
     }
     if (sec == 1) {
         // 5a) vxs  :698-768
-        rb.n = 0;
+        rb.reset();
         r = 0;
         if (i == 0 || i == Ny || j == 0 || j >= Nx - 1) {
             if (j == Nx) rb.add(kx, 1);
@@ -350,7 +389,7 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
     }
     if (sec == 2) {
         // 5b) vys  :770-840
-        rb.n = 0;
+        rb.reset();
         r = 0;
         if (j == 0 || j == Nx || i == 0 || i >= Ny - 1) {
             if (i == Ny) rb.add(ky, 1);
@@ -399,7 +438,7 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
     }
     if (sec == 3) {
         // 5f) Pf  :951-980
-        rb.n = 0;
+        rb.reset();
         r = 0;
         if (j == 0 || j == Nx || i <= 1 || i >= Ny - 1) {
             if (i == 1 || i == Ny - 1) {
@@ -427,7 +466,7 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
     }
     if (sec == 4) {
         // 5d) vxD  :864-903
-        rb.n = 0;
+        rb.reset();
         r = 0;
         if (i == 0 || i == Ny || j == 0 || j >= Nx - 1) {
             if (j == Nx) rb.add(kxf, 1);
@@ -452,7 +491,7 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
     }
     if (sec == 5) {
         // 5e) vyD  :905-949
-        rb.n = 0;
+        rb.reset();
         r = 0;
         if (j == 0 || j == Nx || i == 0 || i >= Ny - 1) {
             if (i == Ny) rb.add(kyf, 1);

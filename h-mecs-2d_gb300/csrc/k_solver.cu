@@ -867,9 +867,8 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31, q = lane & 15, slot = threadIdx.x >> 4;
     const int warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    unsigned& use0 = sb_.use0;
-    unsigned& use1 = sb_.use1;
-    unsigned& use2 = sb_.use2;
+    // the barriers' phase counters in registers for the pass, written back at its end
+    unsigned use0 = sb_.use0, use1 = sb_.use1, use2 = sb_.use2;
     int staged = -1, nbt = 0, tstd = 0;
     int meta[9];  // lane_meta of this thread for the staged tile
 #pragma unroll
@@ -1074,6 +1073,9 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
     if (src != t.x)
         for (int r = tid; r < g.N; r += nth) t.x[r] = src[r];
     if (t.bc) restrict_resid(t.nc, t.ridx, t.rw, g.N, t.col, t.val, t.b, src, t.bc, tid, nth);
+    sb_.use0 = use0;
+    sb_.use1 = use1;
+    sb_.use2 = use2;
 }
 
 // One smoothing pass as its own cooperative launch.
