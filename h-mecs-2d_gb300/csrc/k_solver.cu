@@ -443,18 +443,19 @@ constexpr int WIN_MAX = (TILE + 3) * (TILE + 3) * 6;
 // The x window is reloaded every sweep.  It has a fixed stride (TILE+3 cells
 // per window column, starting two cells before the tile), so a column's
 // window offset depends only on its offset to the row and is precomputed
-// once per assembly (k_stage_prep).  The first sweep needs no grid barrier
-// before it: its window is zero (pre-smoothing) or x plus the prolonged
-// coarse correction computed on the fly (post-smoothing).  After the last
-// sweep the residual of the fine rows each coarse row needs is formed on the
-// fly and restricted (pre-smoothing), again without another barrier: one
-// grid barrier per sweep in all.
+// once per assembly (k_stage_prep).  The first sweep of a pre-smoothing pass
+// needs no grid barrier before it (its window is zero); a post-smoothing pass
+// first adds the prolonged coarse correction to x in one streaming pass over
+// the level and a grid barrier.  After the last sweep the residual of the
+// fine rows each coarse row needs is formed on the fly and restricted
+// (pre-smoothing), again without another barrier.
 constexpr int WSTR = TILE + 3;                                    // window cells per window column
 constexpr int RSTR = ((TILE + 1) * 6 + 7) / 8 * 8;                // staged rows per staged column (padded)
 constexpr int ROWS_MAX = (TILE + 1) * RSTR;                       // staged rows of a tile
 constexpr int PV_MAX = ((TILE + 2) / 3) * ((TILE + 2) / 3);       // patches of one colour in a tile
 constexpr int TB_MAX = 320;                                       // boundary rows of a tile
 constexpr int OWN_BYTES = (WIN_MAX + 127) / 128 * 16;             // a tile's window ownership bits (16-byte multiple)
+constexpr int META_BYTES = 9 * TILE_BS * 4;                       // a tile's per-lane colour table
 static_assert(WIN_MAX == WSTR * WSTR * 6, "window size");
 static_assert(PV_MAX * 16 <= TILE_BS, "a colour's patches fit the block");
 static_assert((TILE * 6 * 4) % 16 == 0, "a tile's first staged row starts on 16 bytes in the padded layout");
@@ -718,7 +719,7 @@ __host__ __device__ constexpr bool stage_pack() {
 // inverses: about 143 KB, one block per SM; a level with more tiles than
 // blocks restages a tile every time a block takes it up).
 struct StageLayout {
-    int xs, val, b, pv, pack, own, bb, bdel, bar, total;
+    int xs, val, b, pv, pack, own, meta, bb, bdel, bar, total;
 };
 
 __host__ __device__ __forceinline__ int align_up(int x, int a) { return (x + a - 1) / a * a; }
@@ -738,6 +739,7 @@ __host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int t
     take(L.pv, (pv_whole ? TILE * TILE : 2 * PV_MAX) * 100 * st, 128);
     if (stage_pack<T>()) take(L.pack, pack_bytes<T>(tb_cap), 128);
     take(L.own, OWN_BYTES, 16);
+    take(L.meta, META_BYTES, 16);
     take(L.xs, WIN_MAX * st, 16);
     take(L.b, ROWS_MAX * st, 16);
     take(L.bb, tb_cap * st, 16);
@@ -752,7 +754,7 @@ __host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int t
 template <typename T>
 __host__ __device__ __forceinline__ unsigned stage_tx_bytes(bool whole, int tb_cap, bool pack) {
     return (unsigned)(HMEC_W * (TILE + 1) * RSTR * sizeof(T) + (whole ? TILE * TILE * 100 * sizeof(T) : 0) +
-                      (pack ? pack_bytes<T>(tb_cap) : 0) + OWN_BYTES);
+                      (pack ? pack_bytes<T>(tb_cap) : 0) + OWN_BYTES + META_BYTES);
 }
 
 // bc = R (b - A x): each coarse row forms the residuals of its fine rows.
@@ -856,6 +858,7 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
     T* sval = reinterpret_cast<T*>(smem_raw + Lo.val);
     T* sb = reinterpret_cast<T*>(smem_raw + Lo.b);
     uint32_t* ownb = reinterpret_cast<uint32_t*>(smem_raw + Lo.own);
+    int32_t* smeta = reinterpret_cast<int32_t*>(smem_raw + Lo.meta);
 
     unsigned long long* bar = sb_.bar;
     T* pv = reinterpret_cast<T*>(smem_raw + Lo.pv);
@@ -870,9 +873,6 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
     // the barriers' phase counters in registers for the pass, written back at its end
     unsigned use0 = sb_.use0, use1 = sb_.use1, use2 = sb_.use2;
     int staged = -1, nbt = 0, tstd = 0;
-    int meta[9];  // lane_meta of this thread for the staged tile
-#pragma unroll
-    for (int c = 0; c < 9; c++) meta[c] = 0;
     // the standard window offsets of this lane's patch row (its unknown type
     // is fixed by the lane), two int16 per register
     constexpr int NSO = (HMEC_W + 1) / 2;
@@ -899,6 +899,13 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
     // barrier per pass instead of per sweep
     const bool local = solo || t.local;
     const int outer = local ? 1 : nsweeps, inner = local ? nsweeps : 1;
+    // post-smoothing: x += P xc as one streaming pass over the level, every
+    // block at once, then a grid barrier -- formed per tile inside the window
+    // loads the dependent table and coarse loads cost ~10 us per tile
+    if (mode == 1) {
+        prolong_add(g, t.gc, t.pmx, t.pmy, t.xc, t.x, tid, nth);
+        cg::this_grid().sync();
+    }
     for (int so = 0; so < outer; so++) {
         for (int tile = blockIdx.x; tile < t.ntiles; tile += gridDim.x) {
             const int ti = tile % t.ntile_i, tj = tile / t.ntile_i;
@@ -910,14 +917,15 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                 nbt = min(t.tb_start[tile + 1] - t.tb_start[tile], TBC);
                 tstd = t.std_t[tile];
                 // one thread: the tile's rows (values, one 3-D box), its
-                // inverses, its window's ownership bits and, when it has
-                // boundary rows, its boundary pack
+                // inverses, its window's ownership bits, its per-lane colour
+                // table and, when it has boundary rows, its boundary pack
                 if (threadIdx.x == 0) {
                     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
                     mbar_expect_tx(&bar[2], stage_tx_bytes<T>(whole, TBC, stage_pack<T>() && nbt > 0));
                     tma_load_3d(sval, &t.tm_val, (i0 - 1) * 6, j0 - 1, 0, &bar[2]);
                     if (whole) tma_load_3d(pv, &t.tm_pinv, 0, i0 - 1, j0 - 1, &bar[2]);
                     bulk_g2s(ownb, t.own_t + (size_t)tile * (OWN_BYTES / 4), OWN_BYTES, &bar[2]);
+                    bulk_g2s(smeta, t.meta_t + (size_t)tile * 9 * TILE_BS, META_BYTES, &bar[2]);
                     if (stage_pack<T>() && nbt > 0)
                         bulk_g2s(smem_raw + Lo.pack, t.bpack + (size_t)tile * pack_bytes<T>(TBC), pack_bytes<T>(TBC),
                                  &bar[2]);
@@ -938,8 +946,6 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                     const size_t g0 = ((size_t)(j0 - 1 + c) * g.Ny1 + (i0 - 1)) * 6;
                     for (int k = lane; k < nch; k += 32) cp_async<CH>(&sb[c * RSTR + 2 * k], t.b + g0 + 2 * k);
                 }
-#pragma unroll
-                for (int c = 0; c < 9; c++) meta[c] = t.meta_t[((size_t)tile * 9 + c) * TILE_BS + threadIdx.x];
                 // the boundary rows' rhs, gathered by their row numbers in the pack
                 const int32_t* brow = reinterpret_cast<const int32_t*>(
                     t.bpack + (size_t)tile * pack_bytes<T>(TBC) + (size_t)TBC * (HMEC_W * sizeof(T) + sizeof(T) + HMEC_W * 2 + 2));
@@ -962,7 +968,6 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                     xv[u] = (T)0;
                     if (lw < WIN_MAX && ci >= 0 && ci <= g.Ny && cj >= 0 && cj <= g.Nx && (s > 0 || mode == 1)) {
                         xv[u] = src[(cj * g.Ny1 + ci) * 6 + v];
-                        if (s == 0) xv[u] += prolong_one(g, t.gc, t.pmx, t.pmy, t.xc, ci, cj, v);
                     }
                 }
 #pragma unroll
@@ -991,7 +996,7 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                     // the other buffer's readers passed the previous colour's barrier
                     if (c < 8 && threadIdx.x == 0) issue_pinv(t, pv, bar, c + 1, bb ^ 1, i0, j0, i1, j1);
                 }
-                const int m = meta[c];
+                const int m = smeta[c * TILE_BS + threadIdx.x];
                 const bool valid = (m >> 30) & 1;
                 const bool mine = ((unsigned)m >> 31) != 0u;  // the tile owns this patch row's unknown
                 const int lrow = m & 2047, rl = (m >> 11) & 2047;
