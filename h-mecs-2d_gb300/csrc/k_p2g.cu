@@ -726,7 +726,7 @@ int p2g_run(hmec_inst* ctx) {
     }
     {
         StreamScope scope(ctx, on(1));
-        HMEC_LAUNCH(ctx, (k_cell_sums<true, true, 5, REC_P, 2>), gc2, bb, 0, g, ctx->hc_start, rec_p, cs_p);
+        HMEC_LAUNCH(ctx, (k_cell_sums<true, true, 5, REC_P, 1>), gc, bb, 0, g, ctx->hc_start, rec_p, cs_p);
         HMEC_LAUNCH(ctx, k_node_p, gs, bb, 0, g, cs_p, f[HMEC_F_ETAP], f[HMEC_F_POR], f[HMEC_F_ETAB0],
                     f[HMEC_F_ETAP0], f[HMEC_F_GGGP]);
     }
