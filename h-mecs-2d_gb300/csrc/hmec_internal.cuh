@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/hmec.h"
+#include "hmec_bits.cuh"
 
 #define HMEC_W 11  // ELL width: the longest assembled row (x/y-Stokes) has 11 entries
 
@@ -325,18 +326,6 @@ __device__ __forceinline__ int fix_quot(double x, double d, float rdf, bool half
 }
 __device__ __forceinline__ float rcp_f32(double d) { return __frcp_rn(__double2float_rn(d)); }
 
-// FP32 -> FP64 through the bit pattern, on the integer pipe (conversions run
-// at the FP64 rate on this GPU): exact for normal values, infinities and NaN;
-// FP32 subnormals (below 1.2e-38) give 0.
-__device__ __forceinline__ double f2d_bits(float f) {
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xFFu;
-    if (e == 0) return 0.0;
-    if (e == 0xFFu) return (double)f;
-    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                 ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
-    return __longlong_as_double((long long)b);
-}
 __device__ __forceinline__ double to_f64(float f) { return f2d_bits(f); }
 __device__ __forceinline__ double to_f64(double d) { return d; }
 
