@@ -43,11 +43,11 @@ TARGET_REL_ERR = 1e-8
 CONFIGS = {
     "c1": dict(workload="config 1: 201x201 nodes, 10x10 km, 5x5 markers/cell (1,000,000 markers), "
                         "seeded synthetic fault model",
-               vcycle_dram_bytes=94.97e6, dram_source="profiles/k_vcycle_stage_c1.md"),
+               vcycle_dram_bytes=84.04e6, dram_source="profiles/k_vcycle_stage_c1.md"),
     "c2": dict(workload="config 2: 1001x401 nodes, 40x16 km, 6x6 markers/cell (14,400,000 markers), "
                         "log-normal host viscosity (1e22 Pa s, sigma 1 decade), 1e19 Pa s fault band, "
                         "log-uniform permeability 1e-21..1e-14 m^2",
-               vcycle_dram_bytes=None, dram_source=None),
+               vcycle_dram_bytes=1.859e9, dram_source="profiles/k_vcycle_stage_c2.md"),
 }
 DOMINANT = "k_smooth"  # library profiling prefix: the smoothing passes (the fused V-cycle in the mixed form)
 FIELDS_ACC = ("vxs", "vys", "pt", "pf", "VSLIPB")
