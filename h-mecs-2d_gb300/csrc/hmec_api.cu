@@ -803,7 +803,13 @@ hmec_ctx* hmec_create(const hmec_params* p, int32_t n_instances, const hmec_grid
         // members of an ensemble share the GPU: one launch per smoothing
         // pass on a share of the SMs (HMEC_MG_PASS_LAUNCHES)
         if (n_instances > 1) q.mg_flags |= HMEC_MG_PASS_LAUNCHES;
-        if (q.autotune) hmec_tune_apply(&q);
+        if (q.autotune) {
+            // the table's smoothing grid is a single model's; ensemble members
+            // keep theirs (the quarter of the SMs per pass, or the caller's)
+            const int32_t sb = q.smooth_blocks;
+            hmec_tune_apply(&q);
+            if (n_instances > 1) q.smooth_blocks = sb;
+        }
         if (const char* why = params_problem(q)) {
             fprintf(stderr, "hmec_create: instance %d: %s\n", (int)k, why);
             delete E;
