@@ -364,6 +364,32 @@ static int32_t inst_upload_markers(hmec_inst* ctx, const double* const* fields, 
     return HMEC_OK;
 }
 
+// Registers (fields set) or drops (fields NULL) the host marker arrays that
+// every timestep copies in after its markers->nodes section.  They must be
+// page-locked, since the copies run asynchronously and inside the timestep's
+// graph (whose capture the registration invalidates).
+static int32_t inst_stream_markers(hmec_inst* ctx, const double* const* fields, int64_t n) {
+    if (!ctx) return HMEC_ERR_ARG;
+    if (fields) {
+        if (n != ctx->marknum) return fail(ctx, HMEC_ERR_ARG, "marker count differs from (Nx-1)*mx*(Ny-1)*my");
+        if (ctx->p.advect_markers)
+            return fail(ctx, HMEC_ERR_STATE, "marker streaming replaces the markers the advection moves");
+        for (int k = 0; k < HMEC_M_COUNT; k++) {
+            if (!fields[k]) return fail(ctx, HMEC_ERR_ARG, "null marker array");
+            cudaPointerAttributes at;
+            if (cudaPointerGetAttributes(&at, fields[k]) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+                cudaGetLastError();
+                return fail(ctx, HMEC_ERR_ARG, "streamed marker arrays must be page-locked (hmec_host_alloc)");
+            }
+        }
+        for (int k = 0; k < HMEC_M_COUNT; k++) ctx->src_mk[k] = fields[k];
+    }
+    HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->src_set = fields != nullptr;
+    graph_free(ctx);  // the captured copies name the arrays: capture again
+    return HMEC_OK;
+}
+
 static int32_t inst_download_markers(hmec_inst* ctx, double* const* fields, int64_t n) {
     if (!ctx || !fields) return fail(ctx, HMEC_ERR_ARG, "null argument");
     if (n != ctx->marknum) return fail(ctx, HMEC_ERR_ARG, "marker count differs from (Nx-1)*mx*(Ny-1)*my");
@@ -644,6 +670,8 @@ static int32_t inst_timestep(hmec_inst* ctx, hmec_step_report* rep) {
     if (rc) return rc;
     rc = inst_markers_to_nodes(ctx);
     if (rc) return rc;
+    rc = markers_stream_issue(ctx);
+    if (rc) return rc;
     rc = inst_timestep_begin(ctx);
     if (rc) return rc;
     int first_bad = HMEC_OK;
@@ -673,6 +701,11 @@ static int32_t inst_timestep(hmec_inst* ctx, hmec_step_report* rep) {
         if (rc) return rc;
         rc = pull_scalars(ctx);
         if (rc) return rc;
+    }
+    if (ctx->src_set) {
+        rc = markers_stream_join(ctx);
+        if (rc) return rc;
+        HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
     const int bits = ctx->hs->status;
     if (bits && !first_bad) first_bad = status_from_bits(bits);
@@ -887,6 +920,14 @@ int32_t hmec_download_field(hmec_ctx* E, int32_t i, int32_t f, double* a, int32_
 int32_t hmec_download_rows(hmec_ctx* E, int32_t i, int32_t row, int32_t nf, const int32_t* fields, double* out) {
     HMEC_INST(E, i);
     return relay(E, m_, inst_download_rows(m_, row, nf, fields, out));
+}
+int32_t hmec_stream_markers(hmec_ctx* E, int32_t i, const double* const* fields, int64_t n) {
+    HMEC_INST(E, i);
+    if (E->exec) {  // an ensemble graph holds the members' captures: build it again
+        ensemble_graph_free(E);
+        if (E->gstate > 0) E->gstate = 0;
+    }
+    return relay(E, m_, inst_stream_markers(m_, fields, n));
 }
 int32_t hmec_download_rows_async(hmec_ctx* E, int32_t i, int32_t row, int32_t nf, const int32_t* fields, double* out,
                                  int64_t* ticket) {

@@ -71,6 +71,13 @@ void abandon_capture(hmec_inst* ctx, cudaStream_t main) {
             cudaStreamEndCapture(a, &g);
         }
     }
+    if (ctx->up_stream) {
+        cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(ctx->up_stream, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(ctx->up_stream, &g);
+        }
+    }
     for (cudaStream_t a : ctx->sv.aux) {
         cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
         if (cudaStreamIsCapturing(a, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
@@ -99,7 +106,7 @@ int capture_step(hmec_inst* ctx) {
             rc = HMEC_ERR_CUDA;
             break;
         }
-        if ((rc = p2g_run(ctx)) || (rc = step_begin(ctx))) break;
+        if ((rc = p2g_run(ctx)) || (rc = markers_stream_issue(ctx)) || (rc = step_begin(ctx))) break;
         cudaGraphConditionalHandle hg = 0;
         if ((rc = graph_handle(ctx, main, &hg))) break;
         HMEC_LAUNCH(ctx, k_graph_begin, 1, 1, 0, gs.ctl, ctx->p.niterglobal + 1, hg);
@@ -118,6 +125,7 @@ int capture_step(hmec_inst* ctx) {
         // a16-a19 (and a18/a20 when advection is on)
         if ((rc = step_end(ctx))) break;
         if (ctx->p.advect_markers && (rc = advect_run(ctx))) break;
+        if ((rc = markers_stream_join(ctx))) break;
         if (cudaMemcpyAsync(ctx->hs, ctx->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, main) != cudaSuccess) {
             rc = HMEC_ERR_CUDA;
             break;

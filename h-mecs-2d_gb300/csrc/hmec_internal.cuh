@@ -241,6 +241,12 @@ struct hmec_inst {
     size_t stage_off = 0;    // floats of mprop before the marker transfers' staging
     cudaStream_t gs4[4] = {nullptr, nullptr, nullptr, nullptr};  // the four grids' gathers
     cudaEvent_t ev_g_fork = nullptr, ev_g_done[4] = {nullptr, nullptr, nullptr, nullptr};
+    // hmec_stream_markers: the page-locked host marker arrays every timestep
+    // copies in after its markers->nodes section, on a stream of its own
+    const double* src_mk[HMEC_M_COUNT] = {};
+    bool src_set = false;
+    cudaStream_t up_stream = nullptr;
+    cudaEvent_t ev_up_fork = nullptr, ev_up_done = nullptr;
     float* mprop;            // sorted per-marker gather records of the four grids (double-float)
     double* cellsum;         // per-cell corner sums of the four grids (k_cell_sums)
     int nhalf;               // number of half-cells
@@ -425,6 +431,12 @@ void p2g_free(hmec_inst* ctx);
 int p2g_run(hmec_inst* ctx);
 // Marker arrays in and out of the library's storage order (see k_p2g.cu).
 int p2g_store_markers(hmec_inst* ctx, const double* const* fields);
+// The marker stream of a timestep (hmec_stream_markers): issue forks the copy
+// of the registered host arrays (and their sort into half-cell order) from
+// the current stream after the markers->nodes section; join makes the
+// current stream wait for it.  Both do nothing without registered arrays.
+int markers_stream_issue(hmec_inst* ctx);
+int markers_stream_join(hmec_inst* ctx);
 int p2g_load_markers(hmec_inst* ctx, double* const* fields);
 int iter_prepare(hmec_inst* ctx);
 int iter_assemble(hmec_inst* ctx);

@@ -604,6 +604,12 @@ void p2g_free(hmec_inst* ctx) {
         if (ctx->ev_g_done[k]) cudaEventDestroy(ctx->ev_g_done[k]);
     }
     if (ctx->ev_g_fork) cudaEventDestroy(ctx->ev_g_fork);
+    if (ctx->up_stream) {
+        cudaStreamSynchronize(ctx->up_stream);
+        cudaStreamDestroy(ctx->up_stream);
+        cudaEventDestroy(ctx->ev_up_fork);
+        cudaEventDestroy(ctx->ev_up_done);
+    }
     cudaFree(ctx->mprop);
     cudaFree(ctx->cellsum);
 }
@@ -612,6 +618,34 @@ void p2g_free(hmec_inst* ctx) {
 // region past the part the radix sort uses as scratch.
 static double* stage_f64(hmec_inst* ctx, int k) {
     return reinterpret_cast<double*>(ctx->mprop + ctx->stage_off) + (size_t)k * (size_t)ctx->marknum;
+}
+
+int markers_stream_issue(hmec_inst* ctx) {
+    if (!ctx->src_set) return HMEC_OK;
+    if (!ctx->up_stream) {
+        HMEC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->up_stream, cudaStreamNonBlocking));
+        HMEC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_up_fork, cudaEventDisableTiming));
+        HMEC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_up_done, cudaEventDisableTiming));
+    }
+    // after the markers->nodes section nothing else in the step reads the
+    // marker arrays, their sort buffers or the record staging (advection,
+    // which would, is refused at registration)
+    HMEC_CUDA(ctx, cudaEventRecord(ctx->ev_up_fork, ctx->stream));
+    HMEC_CUDA(ctx, cudaStreamWaitEvent(ctx->up_stream, ctx->ev_up_fork, 0));
+    int rc;
+    {
+        StreamScope scope(ctx, ctx->up_stream);
+        rc = p2g_store_markers(ctx, ctx->src_mk);
+    }
+    if (rc) return rc;
+    HMEC_CUDA(ctx, cudaEventRecord(ctx->ev_up_done, ctx->up_stream));
+    return HMEC_OK;
+}
+
+int markers_stream_join(hmec_inst* ctx) {
+    if (!ctx->src_set) return HMEC_OK;
+    HMEC_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_up_done, 0));
+    return HMEC_OK;
 }
 
 int p2g_store_markers(hmec_inst* ctx, const double* const* fields) {

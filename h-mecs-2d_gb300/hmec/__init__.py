@@ -106,6 +106,7 @@ EXPORTS = ["hmec_abi_version", "hmec_params_default", "hmec_field_name", "hmec_f
            "hmec_scalar_name", "hmec_marknum", "hmec_create", "hmec_destroy", "hmec_instances", "hmec_last_error",
            "hmec_upload_markers", "hmec_download_markers", "hmec_upload_field", "hmec_download_field",
            "hmec_download_rows", "hmec_download_rows_async", "hmec_rows_wait", "hmec_host_alloc", "hmec_host_free",
+           "hmec_stream_markers",
            "hmec_set_scalar", "hmec_get_scalar", "hmec_markers_to_nodes", "hmec_timestep_begin",
            "hmec_global_iteration", "hmec_timestep_end", "hmec_advect_markers", "hmec_timestep",
            "hmec_assemble_csr", "hmec_solve_system", "hmec_kernel_launches", "hmec_synchronize", "hmec_stream",
@@ -161,6 +162,7 @@ def load(build_if_missing: bool = True):
     L.hmec_download_rows.argtypes = [vp, i32, i32, i32, P(i32), P(C.c_double)]
     L.hmec_download_rows_async.argtypes = [vp, i32, i32, i32, P(i32), P(C.c_double), P(C.c_int64)]
     L.hmec_rows_wait.argtypes = [vp, i32, C.c_int64]
+    L.hmec_stream_markers.argtypes = [vp, i32, P(P(C.c_double)), C.c_int64]
     L.hmec_host_alloc.argtypes = [C.c_size_t]
     L.hmec_host_alloc.restype = vp
     L.hmec_host_free.argtypes = [vp]
@@ -275,6 +277,23 @@ class Instance:
                 raise ValueError("marker arrays must have length %d" % self.marknum)
         ptrs = (C.POINTER(C.c_double) * len(bufs))(*[_dptr(b) for b in bufs])
         self._check(self.L.hmec_upload_markers(self.h, self.inst, ptrs, self.marknum), "upload_markers")
+
+    def stream_markers(self, arrays):
+        """hmec_stream_markers: every later timestep copies these page-locked
+        float64 arrays (dict by marker name, e.g. HostArray views) into the
+        device after its markers->nodes section; None stops it.  The arrays
+        are kept referenced while registered."""
+        if arrays is None:
+            self._check(self.L.hmec_stream_markers(self.h, self.inst, None, self.marknum), "stream_markers")
+            self._streamed = None
+            return
+        bufs = [arrays[k] for k in MARKERS]
+        for b in bufs:
+            if b.dtype != np.float64 or not b.flags.c_contiguous or b.shape != (self.marknum,):
+                raise ValueError("streamed marker arrays must be contiguous float64 of length %d" % self.marknum)
+        ptrs = (C.POINTER(C.c_double) * len(bufs))(*[_dptr(b) for b in bufs])
+        self._check(self.L.hmec_stream_markers(self.h, self.inst, ptrs, self.marknum), "stream_markers")
+        self._streamed = bufs
 
     def download_markers(self) -> dict:
         bufs = [np.empty(self.marknum) for _ in MARKERS]
