@@ -391,13 +391,17 @@ def run_gpu(args, cfg, world, device_index, peaks, with_fp64=True, with_e2e=True
         def ptr(flat):
             return flat.ctypes.data_as(C.POINTER(C.c_double))
 
+        up_ids = (C.c_int32 * len(host_state))(*[hmec.FIELDS.index(f) for f in host_state])
+        up_ptrs = (C.POINTER(C.c_double) * len(host_state))(*[ptr(v[0]) for v in host_state.values()])
+        down = list(host_out.items()) + list(host_state.items())
+        down_ids = (C.c_int32 * len(down))(*[hmec.FIELDS.index(f) for f, _ in down])
+        down_ptrs = (C.POINTER(C.c_double) * len(down))(*[ptr(v[0]) for _, v in down])
+
         def hook(phase):
             if phase == "upload":
-                for f, (flat, r, c) in host_state.items():
-                    m.L.hmec_upload_field(m.h, 0, hmec.FIELDS.index(f), ptr(flat), r, c)
+                m._check(m.L.hmec_upload_fields(m.h, 0, len(host_state), up_ids, up_ptrs), "upload_fields")
             elif phase == "download":
-                for f, (flat, r, c) in list(host_out.items()) + list(host_state.items()):
-                    m.L.hmec_download_field(m.h, 0, hmec.FIELDS.index(f), ptr(flat), r, c)
+                m._check(m.L.hmec_download_fields(m.h, 0, len(down), down_ids, down_ptrs), "download_fields")
 
         # the markers: every timestep copies the pinned host arrays in after
         # its markers->nodes section, overlapped with the rest of the step

@@ -413,6 +413,23 @@ static int32_t inst_upload_field(hmec_inst* ctx, int32_t f, const double* a, int
     return HMEC_OK;
 }
 
+// Several fields in one call: the copies queued back to back, one wait.
+static int32_t inst_move_fields(hmec_inst* ctx, int32_t nf, const int32_t* ids, double* const* ptrs, bool up) {
+    if (!ctx || (nf > 0 && (!ids || !ptrs))) return fail(ctx, HMEC_ERR_ARG, "null argument");
+    for (int k = 0; k < nf; k++)
+        if (ids[k] < 0 || ids[k] >= HMEC_F_COUNT || !ptrs[k]) return fail(ctx, HMEC_ERR_ARG, "unknown field or null array");
+    for (int k = 0; k < nf; k++) {
+        const int gr = hmec_field_grid(ids[k]);
+        const size_t bytes = sizeof(double) * (size_t)(ctx->g.Ny + gr) * (ctx->g.Nx + gr);
+        if (up)
+            HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->f[ids[k]], ptrs[k], bytes, cudaMemcpyHostToDevice, ctx->stream));
+        else
+            HMEC_CUDA(ctx, cudaMemcpyAsync(ptrs[k], ctx->f[ids[k]], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    HMEC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HMEC_OK;
+}
+
 static int32_t inst_download_field(hmec_inst* ctx, int32_t f, double* a, int32_t rows, int32_t cols) {
     if (!ctx || !a) return fail(ctx, HMEC_ERR_ARG, "null argument");
     if (!field_dims_ok(ctx, f, rows, cols)) return fail(ctx, HMEC_ERR_ARG, "unknown field or wrong dimensions");
@@ -920,6 +937,14 @@ int32_t hmec_download_field(hmec_ctx* E, int32_t i, int32_t f, double* a, int32_
 int32_t hmec_download_rows(hmec_ctx* E, int32_t i, int32_t row, int32_t nf, const int32_t* fields, double* out) {
     HMEC_INST(E, i);
     return relay(E, m_, inst_download_rows(m_, row, nf, fields, out));
+}
+int32_t hmec_upload_fields(hmec_ctx* E, int32_t i, int32_t nfields, const int32_t* ids, const double* const* arrays) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_move_fields(m_, nfields, ids, const_cast<double* const*>(arrays), true));
+}
+int32_t hmec_download_fields(hmec_ctx* E, int32_t i, int32_t nfields, const int32_t* ids, double* const* arrays) {
+    HMEC_INST(E, i);
+    return relay(E, m_, inst_move_fields(m_, nfields, ids, arrays, false));
 }
 int32_t hmec_stream_markers(hmec_ctx* E, int32_t i, const double* const* fields, int64_t n) {
     HMEC_INST(E, i);

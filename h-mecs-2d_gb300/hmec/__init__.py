@@ -106,7 +106,7 @@ EXPORTS = ["hmec_abi_version", "hmec_params_default", "hmec_field_name", "hmec_f
            "hmec_scalar_name", "hmec_marknum", "hmec_create", "hmec_destroy", "hmec_instances", "hmec_last_error",
            "hmec_upload_markers", "hmec_download_markers", "hmec_upload_field", "hmec_download_field",
            "hmec_download_rows", "hmec_download_rows_async", "hmec_rows_wait", "hmec_host_alloc", "hmec_host_free",
-           "hmec_stream_markers",
+           "hmec_stream_markers", "hmec_upload_fields", "hmec_download_fields",
            "hmec_set_scalar", "hmec_get_scalar", "hmec_markers_to_nodes", "hmec_timestep_begin",
            "hmec_global_iteration", "hmec_timestep_end", "hmec_advect_markers", "hmec_timestep",
            "hmec_assemble_csr", "hmec_solve_system", "hmec_kernel_launches", "hmec_synchronize", "hmec_stream",
@@ -163,6 +163,8 @@ def load(build_if_missing: bool = True):
     L.hmec_download_rows_async.argtypes = [vp, i32, i32, i32, P(i32), P(C.c_double), P(C.c_int64)]
     L.hmec_rows_wait.argtypes = [vp, i32, C.c_int64]
     L.hmec_stream_markers.argtypes = [vp, i32, P(P(C.c_double)), C.c_int64]
+    L.hmec_upload_fields.argtypes = [vp, i32, i32, P(i32), P(P(C.c_double))]
+    L.hmec_download_fields.argtypes = [vp, i32, i32, P(i32), P(P(C.c_double))]
     L.hmec_host_alloc.argtypes = [C.c_size_t]
     L.hmec_host_alloc.restype = vp
     L.hmec_host_free.argtypes = [vp]

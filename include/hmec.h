@@ -283,6 +283,14 @@ int32_t hmec_download_field(hmec_ctx* ctx, int32_t inst, int32_t field, double* 
  * replaces downloading the whole fields.                                    */
 int32_t hmec_download_rows(hmec_ctx* ctx, int32_t inst, int32_t row, int32_t nfields, const int32_t* fields,
                            double* out);
+/* Several whole fields in one call (arrays[k] of field ids[k], each of its
+ * field's shape as in hmec_upload_field): the copies are queued back to back
+ * and waited for once -- a host that moves its state every step (the
+ * reference's globals) saves a wait per field.                              */
+int32_t hmec_upload_fields(hmec_ctx* ctx, int32_t inst, int32_t nfields, const int32_t* ids,
+                           const double* const* arrays);
+int32_t hmec_download_fields(hmec_ctx* ctx, int32_t inst, int32_t nfields, const int32_t* ids,
+                             double* const* arrays);
 /* hmec_download_rows without waiting for the copy: the rows are gathered
  * after the work queued so far (the host waits for that gather only) and
  * copied to `out` on a stream of their own, overlapped with the next

@@ -93,3 +93,30 @@ def test_stream_markers_refusals():
         m2.close()
         for h in host.values():
             h.close()
+
+
+def test_batched_field_transfers_equal_single_ones():
+    import ctypes as C
+
+    p = hmec.default_params(**synth.PRESETS["tiny"])
+    mk, nodes = synth.make_state(p, "tiny")
+    m = _model(p, mk, nodes)
+    try:
+        m.timestep()
+        names = ["vxs", "pt", "SXY", "ETA", "VSLIPB", "OM0"]
+        ids = (C.c_int32 * len(names))(*[hmec.FIELDS.index(n) for n in names])
+        bufs = [np.zeros(m.shape(n), order="F") for n in names]
+        ptrs = (C.POINTER(C.c_double) * len(names))(*[b.ctypes.data_as(C.POINTER(C.c_double)) for b in bufs])
+        m._check(m.L.hmec_download_fields(m.h, 0, len(names), ids, ptrs), "download_fields")
+        for n, b in zip(names, bufs):
+            assert np.array_equal(b, m.field(n)), n
+        rng = np.random.default_rng(3)
+        for b in bufs:
+            b[...] = rng.standard_normal(b.shape)
+        m._check(m.L.hmec_upload_fields(m.h, 0, len(names), ids, ptrs), "upload_fields")
+        for n, b in zip(names, bufs):
+            assert np.array_equal(m.field(n), b), n
+        bad = (C.c_int32 * 1)(10_000)
+        assert m.L.hmec_download_fields(m.h, 0, 1, bad, ptrs) == -1  # HMEC_ERR_ARG
+    finally:
+        m.close()
