@@ -158,6 +158,12 @@ def test_timestep_replay_local_sweeps(form):
     _replay("c0", 5, form, 0, mg_flags=hmec.MG_DARCY_HARMONIC | hmec.MG_LOCAL_SWEEPS, autotune=0)
 
 
+def test_timestep_replay_per_colour_inverses():
+    """The FP32 smoother with per-colour inverses (smooth_inverses = 2, the
+    FP64 form's staging) gives the same steps within the same bounds."""
+    _replay("c0", 5, hmec.FORM_MIXED, 0, smooth_inverses=2, autotune=0)
+
+
 def _replay(preset, nsteps, form, quirk, **extra):
     o, mk, nodes = pairs.oracle_for(preset, quirk_accumulate_sums=quirk)
     o2, _, _ = pairs.oracle_for(preset, quirk_accumulate_sums=quirk)
