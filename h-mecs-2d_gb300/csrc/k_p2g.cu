@@ -628,16 +628,20 @@ int markers_stream_issue(hmec_inst* ctx) {
         HMEC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_up_done, cudaEventDisableTiming));
     }
     // after the markers->nodes section nothing else in the step reads the
-    // marker arrays, their sort buffers or the record staging (advection,
-    // which would, is refused at registration)
+    // marker arrays (advection, which would, is refused at registration).
+    // Streamed markers are stored in the caller's order: plain copies, no
+    // kernel competes with the solve for the SMs (the next step's sort orders
+    // them, as it does every step); the storage order becomes the identity.
     HMEC_CUDA(ctx, cudaEventRecord(ctx->ev_up_fork, ctx->stream));
     HMEC_CUDA(ctx, cudaStreamWaitEvent(ctx->up_stream, ctx->ev_up_fork, 0));
-    int rc;
+    const int64_t n = ctx->marknum;
+    for (int k = 0; k < HMEC_M_COUNT; k++)
+        HMEC_CUDA(ctx, cudaMemcpyAsync(ctx->mk[k], ctx->src_mk[k], sizeof(double) * (size_t)n, cudaMemcpyHostToDevice,
+                                       ctx->up_stream));
     {
         StreamScope scope(ctx, ctx->up_stream);
-        rc = p2g_store_markers(ctx, ctx->src_mk);
+        HMEC_LAUNCH(ctx, k_iota, nblocks(n, 256), 256, 0, ctx->mord, n);
     }
-    if (rc) return rc;
     HMEC_CUDA(ctx, cudaEventRecord(ctx->ev_up_done, ctx->up_stream));
     return HMEC_OK;
 }
