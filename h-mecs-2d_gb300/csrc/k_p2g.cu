@@ -404,17 +404,20 @@ __device__ __forceinline__ void cell_sums_part(const Geo& g, const int32_t* __re
             cs[((size_t)(1 + Q0 + q) * 4 + c) * ncell + cell] = f2d_bits(Sh[q][c]) + f2d_bits(Sl[q][c]);
 }
 
-// SPLIT = 2: blockIdx.z = 0 sums the weights and the first half of the
-// properties, z = 1 the second half (the basic grid's ten properties in one
-// thread need 172 registers; halves keep twice the warps resident).
+// Grid (SPLIT, cell-row blocks, cell columns).  SPLIT = 2: blockIdx.x = 0
+// sums the weights and the first half of the properties, 1 the second half
+// (the basic grid's ten properties in one thread need 172 registers; halves
+// keep twice the warps resident).  The half is the fastest grid index, so
+// both halves of a cell range run together and the second one reads the
+// records from L2, not DRAM again.
 template <bool ROWP, bool COLP, int NP, int RW, int SPLIT>
 __global__ void k_cell_sums(Geo g, const int32_t* __restrict__ start, const float* __restrict__ rec,
                             double* __restrict__ cs) {
-    const int ci = blockIdx.x * blockDim.x + threadIdx.x, cj = blockIdx.y;
+    const int ci = blockIdx.y * blockDim.x + threadIdx.x, cj = blockIdx.z;
     if (ci >= g.Ny - 1) return;
     if (SPLIT == 1) {
         cell_sums_part<ROWP, COLP, NP, RW, 0, NP, true>(g, start, rec, cs, ci, cj);
-    } else if (blockIdx.z == 0) {
+    } else if (blockIdx.x == 0) {
         cell_sums_part<ROWP, COLP, NP, RW, 0, NP / 2, true>(g, start, rec, cs, ci, cj);
     } else {
         cell_sums_part<ROWP, COLP, NP, RW, NP / 2, NP, false>(g, start, rec, cs, ci, cj);
@@ -754,7 +757,7 @@ int p2g_run(hmec_inst* ctx) {
     const float* rec_x = rec_p + (size_t)n * REC_P;
     const float* rec_y = rec_x + (size_t)n * REC_X;
     const int bs = ctx->bs_st;
-    dim3 bb(bs), gc(nblocks(g.Ny - 1, bs), g.Nx - 1), gc2(nblocks(g.Ny - 1, bs), g.Nx - 1, 2);
+    dim3 bb(bs), gc(1, nblocks(g.Ny - 1, bs), g.Nx - 1), gc2(2, nblocks(g.Ny - 1, bs), g.Nx - 1);
     dim3 gb(nblocks(g.Ny, bs), g.Nx), gs(nblocks(g.Ny1, bs), g.Nx1);
     // the four grids' gathers are independent: each pair (cell sums, node
     // sums) on a stream of its own (streams of this section only: the
