@@ -205,8 +205,21 @@ struct RowB {
             v[k] = 0.0;
         }
     }
-    // duplicates summed in insertion order (setFromTriplets); branch-free,
-    // so the arrays stay in registers
+    // an entry whose column the row does not hold yet (interior rows: their
+    // stencil columns are distinct), appended without a search -- no FP64
+    // operation, the arrays stay in registers
+    __device__ __forceinline__ void put(int col, double val) {
+#pragma unroll
+        for (int k = 0; k < RB_CAP; k++) {
+            const bool at = k == n;
+            c[k] = at ? col : c[k];
+            v[k] = at ? val : v[k];
+        }
+        n++;
+    }
+    // duplicates summed in insertion order (setFromTriplets; the boundary
+    // rows' branches can add a column twice); branch-free, so the arrays stay
+    // in registers
     __device__ __forceinline__ void add(int col, double val) {
         bool dup = false;
 #pragma unroll
@@ -323,12 +336,12 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
             const double BETADRAINED = (1. / IS(F.GGGB, i, j) + p.BETASOLID) / (1 - por);
             const double KBW = 1 - p.BETASOLID / BETADRAINED;
             const double ietab = 1. / IS(F.ETAB, i, j) / (1 - por);
-            rb.add(kx - RS, -idx);
-            rb.add(kx, idx);
-            rb.add(ky - NV, -idy);
-            rb.add(ky, idy);
-            rb.add(kp, ptscale * (ietab + BETADRAINED * idt));
-            rb.add(kpf, -pfscale * (ietab + BETADRAINED * KBW * idt));
+            rb.put(kx - RS, -idx);
+            rb.put(kx, idx);
+            rb.put(ky - NV, -idy);
+            rb.put(ky, idy);
+            rb.put(kp, ptscale * (ietab + BETADRAINED * idt));
+            rb.put(kpf, -pfscale * (ietab + BETADRAINED * KBW * idt));
             if (want_rhs) r = BETADRAINED * (IS(F.PT0, i, j) - KBW * IS(F.PF0, i, j)) / dt + IS(F.DILP, i, j);
         }
         emit_row(rb, kp, N, col, val, dscale, rhs_scaled, rhs_raw, r);
@@ -371,17 +384,17 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
             const double dRHOdx = (IS(F.RHOX, i, j + 1) - IS(F.RHOX, i, j - 1)) * g.i2dx;
             const double dRHOdy = (IB(F.RHO, i, j) - IB(F.RHO, i - 1, j)) * idy;
             const double temp = gx * dt * dRHOdy / 4.;
-            rb.add(kx, -(ETAXX1 + ETAXX2) * idx2 - (ETAXY1 + ETAXY2) * idy2 - gx * dt * dRHOdx - inertia * IS(F.RHOX, i, j) * idt);
-            rb.add(kx - RS, ETAXX1 * idx2);
-            rb.add(kx + RS, ETAXX2 * idx2);
-            rb.add(kx - NV, ETAXY1 * idy2);
-            rb.add(kx + NV, ETAXY2 * idy2);
-            rb.add(ky - NV, (ETAXY1 - ETAXX1) * idx_dy - temp);
-            rb.add(ky, (ETAXX1 - ETAXY2) * idx_dy - temp);
-            rb.add(ky - NV + RS, (ETAXX2 - ETAXY1) * idx_dy - temp);
-            rb.add(ky + RS, (ETAXY2 - ETAXX2) * idx_dy - temp);
-            rb.add(kp, ptscale * idx);
-            rb.add(kp + RS, -ptscale * idx);
+            rb.put(kx, -(ETAXX1 + ETAXX2) * idx2 - (ETAXY1 + ETAXY2) * idy2 - gx * dt * dRHOdx - inertia * IS(F.RHOX, i, j) * idt);
+            rb.put(kx - RS, ETAXX1 * idx2);
+            rb.put(kx + RS, ETAXX2 * idx2);
+            rb.put(kx - NV, ETAXY1 * idy2);
+            rb.put(kx + NV, ETAXY2 * idy2);
+            rb.put(ky - NV, (ETAXY1 - ETAXX1) * idx_dy - temp);
+            rb.put(ky, (ETAXX1 - ETAXY2) * idx_dy - temp);
+            rb.put(ky - NV + RS, (ETAXX2 - ETAXY1) * idx_dy - temp);
+            rb.put(ky + RS, (ETAXY2 - ETAXX2) * idx_dy - temp);
+            rb.put(kp, ptscale * idx);
+            rb.put(kp + RS, -ptscale * idx);
             if (want_rhs) {
                 const double SXY1 = IB(F.SXY0, i - 1, j) * (1 - KXY1), SXY2 = IB(F.SXY0, i, j) * (1 - KXY2);
                 const double SXX1 = IS(F.SXX0, i, j) * (1 - KXX1), SXX2 = IS(F.SXX0, i, j + 1) * (1 - KXX2);
@@ -420,17 +433,17 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
             const double dRHOdy = (IS(F.RHOY, i + 1, j) - IS(F.RHOY, i - 1, j)) * g.i2dy;
             const double dRHOdx = (IB(F.RHO, i, j) - IB(F.RHO, i, j - 1)) * idx;
             const double temp = gy * dt * dRHOdx / 4.;
-            rb.add(ky, -(ETAYY1 + ETAYY2) * idy2 - (ETAXY1 + ETAXY2) * idx2 - gy * dt * dRHOdy - inertia * IS(F.RHOY, i, j) * idt);
-            rb.add(ky - RS, ETAXY1 * idx2);
-            rb.add(ky + RS, ETAXY2 * idx2);
-            rb.add(ky - NV, ETAYY1 * idy2);
-            rb.add(ky + NV, ETAYY2 * idy2);
-            rb.add(kx - RS, (ETAXY1 - ETAYY1) * idx_dy - temp);
-            rb.add(kx + NV - RS, (ETAYY2 - ETAXY1) * idx_dy - temp);
-            rb.add(kx, (ETAYY1 - ETAXY2) * idx_dy - temp);
-            rb.add(kx + NV, (ETAXY2 - ETAYY2) * idx_dy - temp);
-            rb.add(kp, ptscale * idy);
-            rb.add(kp + NV, -ptscale * idy);
+            rb.put(ky, -(ETAYY1 + ETAYY2) * idy2 - (ETAXY1 + ETAXY2) * idx2 - gy * dt * dRHOdy - inertia * IS(F.RHOY, i, j) * idt);
+            rb.put(ky - RS, ETAXY1 * idx2);
+            rb.put(ky + RS, ETAXY2 * idx2);
+            rb.put(ky - NV, ETAYY1 * idy2);
+            rb.put(ky + NV, ETAYY2 * idy2);
+            rb.put(kx - RS, (ETAXY1 - ETAYY1) * idx_dy - temp);
+            rb.put(kx + NV - RS, (ETAYY2 - ETAXY1) * idx_dy - temp);
+            rb.put(kx, (ETAYY1 - ETAXY2) * idx_dy - temp);
+            rb.put(kx + NV, (ETAXY2 - ETAYY2) * idx_dy - temp);
+            rb.put(kp, ptscale * idy);
+            rb.put(kp + NV, -ptscale * idy);
             if (want_rhs) {
                 const double SXY1 = IB(F.SXY0, i, j - 1) * (1 - KXY1), SXY2 = IB(F.SXY0, i, j) * (1 - KXY2);
                 const double SYY1 = IS(F.SYY0, i, j) * (1 - KYY1), SYY2 = IS(F.SYY0, i + 1, j) * (1 - KYY2);
@@ -457,12 +470,12 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
             const double KBW = 1 - p.BETASOLID / BETADRAINED;
             const double KSK = (BETADRAINED - p.BETASOLID) / (BETADRAINED - p.BETASOLID + por * (p.BETAFLUID - p.BETASOLID));
             const double ietab = 1 / IS(F.ETAB, i, j) / (1 - por);
-            rb.add(kxf - RS, -idx);
-            rb.add(kxf, idx);
-            rb.add(kyf - NV, -idy);
-            rb.add(kyf, idy);
-            rb.add(kp, -ptscale * (ietab + BETADRAINED * KBW * idt));
-            rb.add(kpf, pfscale * (ietab + BETADRAINED * KBW / KSK * idt));
+            rb.put(kxf - RS, -idx);
+            rb.put(kxf, idx);
+            rb.put(kyf - NV, -idy);
+            rb.put(kyf, idy);
+            rb.put(kp, -ptscale * (ietab + BETADRAINED * KBW * idt));
+            rb.put(kpf, pfscale * (ietab + BETADRAINED * KBW / KSK * idt));
             if (want_rhs) r = -BETADRAINED * KBW * (IS(F.PT0, i, j) - 1. / KSK * IS(F.PF0, i, j)) / dt - IS(F.DILP, i, j);
         }
         emit_row(rb, kpf, N, col, val, dscale, rhs_scaled, rhs_raw, r);
@@ -484,10 +497,10 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
             if (j == 0) rb.add(kxf, 1);
             if (j == Nx - 1) rb.add(kxf, 1);
         } else {
-            rb.add(kxf, -IS(F.ETADX, i, j) - IS(F.RHOFX, i, j) / IS(F.PORX, i, j) * inertia * idt);
-            rb.add(kx, -IS(F.RHOFX, i, j) * inertia * idt);
-            rb.add(kpf, pfscale * idx);
-            rb.add(kpf + RS, -pfscale * idx);
+            rb.put(kxf, -IS(F.ETADX, i, j) - IS(F.RHOFX, i, j) / IS(F.PORX, i, j) * inertia * idt);
+            rb.put(kx, -IS(F.RHOFX, i, j) * inertia * idt);
+            rb.put(kpf, pfscale * idx);
+            rb.put(kpf + RS, -pfscale * idx);
             if (want_rhs) r = -IS(F.RHOFX, i, j) * (inertia * IS(F.VXF0, i, j) / dt + gx);
         }
         emit_row(rb, kxf, N, col, val, dscale, rhs_scaled, rhs_raw, r);
@@ -515,10 +528,10 @@ __global__ void k_assemble(Geo g, AsmFields F, const DevScalars* ds, hmec_params
                 r = p.bcvyflower;
             }
         } else {
-            rb.add(kyf, -IS(F.ETADY, i, j) - IS(F.RHOFY, i, j) / IS(F.PORY, i, j) * inertia * idt);
-            rb.add(ky, -IS(F.RHOFY, i, j) * inertia * idt);
-            rb.add(kpf, pfscale * idy);
-            rb.add(kpf + NV, -pfscale * idy);
+            rb.put(kyf, -IS(F.ETADY, i, j) - IS(F.RHOFY, i, j) / IS(F.PORY, i, j) * inertia * idt);
+            rb.put(ky, -IS(F.RHOFY, i, j) * inertia * idt);
+            rb.put(kpf, pfscale * idy);
+            rb.put(kpf + NV, -pfscale * idy);
             if (want_rhs) r = -IS(F.RHOFY, i, j) * (inertia * IS(F.VYF0, i, j) / dt + gy);
         }
         emit_row(rb, kyf, N, col, val, dscale, rhs_scaled, rhs_raw, r);
