@@ -705,10 +705,14 @@ struct StageArgs {
     const int* done;       // the solve's convergence flag: set, the pass does nothing
 };
 
-// Whether the stage holds an edge tile's boundary pack (FP32) or the pass
-// reads it from global memory (FP64: the smaller stage leaves more of the
-// SM's memory to L1, which the window loads, prolongation and restriction
-// use; 1001x401: 46 against 53 ms per step).
+// Whether the stage holds an edge tile's boundary pack, the per-lane colour
+// table and the boundary rows' corrections (FP32), or the pass reads the
+// pack from global memory and keeps the table and corrections in registers
+// (FP64: the smaller stage leaves more of the SM's memory to L1, which the
+// window loads, prolongation and restriction use; 1001x401: 53 -> 46 ms per
+// step without the pack, 53.5 -> 49.8 without the table and corrections).
+// The FP32 stage measured slower without them even with two blocks per SM
+// (1001x401: 19.2 against 18.4 ms; 201x201: 20.1 against 12.5).
 template <typename T>
 __host__ __device__ constexpr bool stage_pack() {
     return sizeof(T) == 4;
@@ -739,22 +743,23 @@ __host__ __device__ __forceinline__ StageLayout stage_layout(int pv_whole, int t
     take(L.pv, (pv_whole ? TILE * TILE : 2 * PV_MAX) * 100 * st, 128);
     if (stage_pack<T>()) take(L.pack, pack_bytes<T>(tb_cap), 128);
     take(L.own, OWN_BYTES, 16);
-    take(L.meta, META_BYTES, 16);
+    L.meta = L.bdel = 0;
+    if (stage_pack<T>()) take(L.meta, META_BYTES, 16);
     take(L.xs, WIN_MAX * st, 16);
     take(L.b, ROWS_MAX * st, 16);
     take(L.bb, tb_cap * st, 16);
-    take(L.bdel, tb_cap * st, 16);
+    if (stage_pack<T>()) take(L.bdel, tb_cap * st, 16);
     take(L.bar, 3 * 8, 16);
     L.total = align_up(o, 16);
     return L;
 }
 
-// Bytes one tile's stage receives on its barrier (the boundary pack only for
-// a tile that has boundary rows, in the FP32 stage).
+// Bytes one tile's stage receives on its barrier (the colour table in the
+// FP32 stage, the boundary pack only for a tile that has boundary rows).
 template <typename T>
 __host__ __device__ __forceinline__ unsigned stage_tx_bytes(bool whole, int tb_cap, bool pack) {
     return (unsigned)(HMEC_W * (TILE + 1) * RSTR * sizeof(T) + (whole ? TILE * TILE * 100 * sizeof(T) : 0) +
-                      (pack ? pack_bytes<T>(tb_cap) : 0) + OWN_BYTES + META_BYTES);
+                      (pack ? pack_bytes<T>(tb_cap) : 0) + OWN_BYTES + (stage_pack<T>() ? META_BYTES : 0));
 }
 
 // bc = R (b - A x): each coarse row forms the residuals of its fine rows.
@@ -873,6 +878,7 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
     // the barriers' phase counters in registers for the pass, written back at its end
     unsigned use0 = sb_.use0, use1 = sb_.use1, use2 = sb_.use2;
     int staged = -1, nbt = 0, tstd = 0;
+    int meta[9];  // FP64 stage: this lane's colour table for the staged tile
     // the standard window offsets of this lane's patch row (its unknown type
     // is fixed by the lane), two int16 per register
     constexpr int NSO = (HMEC_W + 1) / 2;
@@ -925,7 +931,7 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                     tma_load_3d(sval, &t.tm_val, (i0 - 1) * 6, j0 - 1, 0, &bar[2]);
                     if (whole) tma_load_3d(pv, &t.tm_pinv, 0, i0 - 1, j0 - 1, &bar[2]);
                     bulk_g2s(ownb, t.own_t + (size_t)tile * (OWN_BYTES / 4), OWN_BYTES, &bar[2]);
-                    bulk_g2s(smeta, t.meta_t + (size_t)tile * 9 * TILE_BS, META_BYTES, &bar[2]);
+                    if (stage_pack<T>()) bulk_g2s(smeta, t.meta_t + (size_t)tile * 9 * TILE_BS, META_BYTES, &bar[2]);
                     if (stage_pack<T>() && nbt > 0)
                         bulk_g2s(smem_raw + Lo.pack, t.bpack + (size_t)tile * pack_bytes<T>(TBC), pack_bytes<T>(TBC),
                                  &bar[2]);
@@ -950,6 +956,10 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                 const int32_t* brow = reinterpret_cast<const int32_t*>(
                     t.bpack + (size_t)tile * pack_bytes<T>(TBC) + (size_t)TBC * (HMEC_W * sizeof(T) + sizeof(T) + HMEC_W * 2 + 2));
                 for (int k = threadIdx.x; k < nbt; k += blockDim.x) bbv[k] = t.b[brow[k]];
+                if (!stage_pack<T>()) {
+#pragma unroll
+                    for (int c = 0; c < 9; c++) meta[c] = __ldg(t.meta_t + ((size_t)tile * 9 + c) * TILE_BS + threadIdx.x);
+                }
                 staged = tile;
             }
             for (int si = 0; si < inner; si++) {
@@ -996,7 +1006,7 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                     // the other buffer's readers passed the previous colour's barrier
                     if (c < 8 && threadIdx.x == 0) issue_pinv(t, pv, bar, c + 1, bb ^ 1, i0, j0, i1, j1);
                 }
-                const int m = smeta[c * TILE_BS + threadIdx.x];
+                const int m = stage_pack<T>() ? smeta[c * TILE_BS + threadIdx.x] : meta[c];
                 const bool valid = (m >> 30) & 1;
                 const bool mine = ((unsigned)m >> 31) != 0u;  // the tile owns this patch row's unknown
                 const int lrow = m & 2047, rl = (m >> 11) & 2047;
@@ -1045,15 +1055,38 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
             const T* bdiag = bval + HMEC_W * TBC;
             const int16_t* boff = reinterpret_cast<const int16_t*>(bdiag + TBC);
             const int16_t* blr = boff + HMEC_W * TBC;
-            for (int k = threadIdx.x; k < nbt; k += blockDim.x) {
-                const int lr = blr[k];
-                T acc = bbv[k];
+            if (stage_pack<T>()) {
+                for (int k = threadIdx.x; k < nbt; k += blockDim.x) {
+                    const int lr = blr[k];
+                    T acc = bbv[k];
 #pragma unroll
-                for (int sl = 0; sl < HMEC_W; sl++) acc -= bval[sl * TBC + k] * xs[lr + boff[sl * TBC + k]];
-                bdel[k] = bdiag[k] != (T)0 ? acc / bdiag[k] : (T)0;
+                    for (int sl = 0; sl < HMEC_W; sl++) acc -= bval[sl * TBC + k] * xs[lr + boff[sl * TBC + k]];
+                    bdel[k] = bdiag[k] != (T)0 ? acc / bdiag[k] : (T)0;
+                }
+                __syncthreads();
+                for (int k = threadIdx.x; k < nbt; k += blockDim.x) xs[blr[k]] += bdel[k];
+            } else {
+                constexpr int BDR = (TB_MAX + TILE_BS - 1) / TILE_BS;
+                T bd[BDR];
+#pragma unroll
+                for (int u = 0; u < BDR; u++) {
+                    const int k = threadIdx.x + u * TILE_BS;
+                    bd[u] = (T)0;
+                    if (k < nbt) {
+                        const int lr = blr[k];
+                        T acc = bbv[k];
+#pragma unroll
+                        for (int sl = 0; sl < HMEC_W; sl++) acc -= bval[sl * TBC + k] * xs[lr + boff[sl * TBC + k]];
+                        bd[u] = bdiag[k] != (T)0 ? acc / bdiag[k] : (T)0;
+                    }
+                }
+                __syncthreads();
+#pragma unroll
+                for (int u = 0; u < BDR; u++) {
+                    const int k = threadIdx.x + u * TILE_BS;
+                    if (k < nbt) xs[blr[k]] += bd[u];
+                }
             }
-            __syncthreads();
-            for (int k = threadIdx.x; k < nbt; k += blockDim.x) xs[blr[k]] += bdel[k];
             __syncthreads();
             // publish the owned unknowns
             if (!local || s == nsweeps - 1) {
