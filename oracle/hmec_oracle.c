@@ -35,6 +35,7 @@
 #include "hmec_oracle.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -75,6 +76,7 @@ struct hmo_state {
     int32_t last_ynpl;
     double last_dsylsq;
     int32_t rsf_noconv;
+    int nthreads; /* threads of the marker loop (1: the serial loop) */
 };
 
 /* ------------------------------------------------------------ constants */
@@ -245,6 +247,7 @@ hmo_state* hmo_create(const hmec_params* pin) {
     st->sc[HMEC_S_dt] = p->dtelastic0;
     st->sc[HMEC_S_yndtdecrease] = 1;
     st->sc[HMEC_S_timestep] = 1;
+    st->nthreads = 1;
     return st;
 }
 
@@ -307,21 +310,23 @@ static void weights(double dxm, double dym, double w[4]) {
     w[3] = dxm * dym;
 }
 
-void hmo_markers_to_nodes(hmo_state* st) {
+/* The marker sums of one pass: the node sums the loop adds into. */
+typedef struct {
+    double* sb[SB_N];
+    double* sp[SP_N];
+    double* sx[SV_N];
+    double* sy[SV_N];
+} hmo_sums;
+
+/* Markers m0 .. m1-1 added into the sums s (:385-529). */
+static void accumulate_markers(const hmo_state* st, int64_t m0, int64_t m1, const hmo_sums* s) {
     const hmec_params* p = &st->p;
-    const int Nx = st->Nx, Ny = st->Ny, Ny1 = st->Ny1, Nx1 = st->Nx1;
+    const int Nx = st->Nx, Ny = st->Ny, Ny1 = st->Ny1;
     const double dx = st->dx, dy = st->dy;
     const double *x = st->crd[0], *y = st->crd[1], *xvx = st->crd[2], *yvx = st->crd[3];
     const double *xvy = st->crd[4], *yvy = st->crd[5], *xp = st->crd[6], *yp = st->crd[7];
-    size_t nb = (size_t)Nx * Ny, ns = (size_t)Nx1 * Ny1;
-    if (!p->quirk_accumulate_sums) { /* :377-381 as intended */
-        for (int k = 0; k < SB_N; k++) memset(st->sb[k], 0, nb * sizeof(double));
-        for (int k = 0; k < SP_N; k++) memset(st->sp[k], 0, ns * sizeof(double));
-        for (int k = 0; k < SV_N; k++) memset(st->sx[k], 0, ns * sizeof(double));
-        for (int k = 0; k < SV_N; k++) memset(st->sy[k], 0, ns * sizeof(double));
-    }
     double* const* mk = st->mk;
-    for (int64_t m = 0; m < st->marknum; m++) { /* :385-529, serial order */
+    for (int64_t m = m0; m < m1; m++) { /* :385-529, in marker order */
         const double por = mk[HMEC_M_porm][m];
         double kkkmm = mk[HMEC_M_kkkm][m] * pow(por / p->POR0, 3);
         kkkmm = enforce_bounds(kkkmm, p->kkkmin, p->kkkmax);
@@ -357,46 +362,170 @@ void hmo_markers_to_nodes(hmo_state* st) {
         int j = check_bounds(fix_(xmm / dx), Nx);
         int i = check_bounds(fix_(ymm / dy), Ny);
         weights((xmm - x[j]) / dx, (ymm - y[i]) / dy, w);
-        add_block(st->sb[SB_RHO], Ny, i, j, rhomm, w);
-        add_block(st->sb[SB_KKK], Ny, i, j, kkkmm, w);
-        add_block(st->sb[SB_TTT], Ny, i, j, mk[HMEC_M_t_marker][m], w);
-        add_block(st->sb[SB_GGG], Ny, i, j, invg, w);
-        add_block(st->sb[SB_ETA0], Ny, i, j, etamm0, w);
-        add_block(st->sb[SB_COHT], Ny, i, j, cohestmm, w);
-        add_block(st->sb[SB_FRIT], Ny, i, j, fricttmm, w);
-        add_block(st->sb[SB_COHC], Ny, i, j, cohescmm, w);
-        add_block(st->sb[SB_FRIC], Ny, i, j, frictcmm, w);
-        add_block(st->sb[SB_DILC], Ny, i, j, dilatcmm, w);
-        add_wt(st->sb[SB_WT], Ny, i, j, w);
+        add_block(s->sb[SB_RHO], Ny, i, j, rhomm, w);
+        add_block(s->sb[SB_KKK], Ny, i, j, kkkmm, w);
+        add_block(s->sb[SB_TTT], Ny, i, j, mk[HMEC_M_t_marker][m], w);
+        add_block(s->sb[SB_GGG], Ny, i, j, invg, w);
+        add_block(s->sb[SB_ETA0], Ny, i, j, etamm0, w);
+        add_block(s->sb[SB_COHT], Ny, i, j, cohestmm, w);
+        add_block(s->sb[SB_FRIT], Ny, i, j, fricttmm, w);
+        add_block(s->sb[SB_COHC], Ny, i, j, cohescmm, w);
+        add_block(s->sb[SB_FRIC], Ny, i, j, frictcmm, w);
+        add_block(s->sb[SB_DILC], Ny, i, j, dilatcmm, w);
+        add_wt(s->sb[SB_WT], Ny, i, j, w);
         /* pressure nodes :468-484 */
         j = check_bounds(fix_((xmm + dx / 2.) / dx), Nx);
         i = check_bounds(fix_((ymm + dy / 2.) / dy), Ny);
         weights((xmm - xp[j]) / dx, (ymm - yp[i]) / dy, w);
-        add_block(st->sp[SP_ETAP], Ny1, i, j, etamm, w);
-        add_block(st->sp[SP_POR], Ny1, i, j, por, w);
-        add_block(st->sp[SP_GGGP], Ny1, i, j, invg, w);
-        add_block(st->sp[SP_ETAP0], Ny1, i, j, etamm0, w);
-        add_block(st->sp[SP_ETAB0], Ny1, i, j, etasmm0, w);
-        add_wt(st->sp[SP_WT], Ny1, i, j, w);
+        add_block(s->sp[SP_ETAP], Ny1, i, j, etamm, w);
+        add_block(s->sp[SP_POR], Ny1, i, j, por, w);
+        add_block(s->sp[SP_GGGP], Ny1, i, j, invg, w);
+        add_block(s->sp[SP_ETAP0], Ny1, i, j, etamm0, w);
+        add_block(s->sp[SP_ETAB0], Ny1, i, j, etasmm0, w);
+        add_wt(s->sp[SP_WT], Ny1, i, j, w);
         /* Vx nodes :493-506 */
         j = check_bounds(fix_(xmm / dx), Nx);
         i = check_bounds(fix_((ymm + dy / 2.) / dy), Ny);
         weights((xmm - xvx[j]) / dx, (ymm - yvx[i]) / dy, w);
-        add_block(st->sx[SV_RHO], Ny1, i, j, rhomm, w);
-        add_block(st->sx[SV_ETAD], Ny1, i, j, 1. / etadm, w);
-        add_block(st->sx[SV_RHOF], Ny1, i, j, mk[HMEC_M_rhofm][m], w);
-        add_block(st->sx[SV_POR], Ny1, i, j, por, w);
-        add_wt(st->sx[SV_WT], Ny1, i, j, w);
+        add_block(s->sx[SV_RHO], Ny1, i, j, rhomm, w);
+        add_block(s->sx[SV_ETAD], Ny1, i, j, 1. / etadm, w);
+        add_block(s->sx[SV_RHOF], Ny1, i, j, mk[HMEC_M_rhofm][m], w);
+        add_block(s->sx[SV_POR], Ny1, i, j, por, w);
+        add_wt(s->sx[SV_WT], Ny1, i, j, w);
         /* Vy nodes :515-528 */
         j = check_bounds(fix_((xmm + dx / 2.) / dx), Nx);
         i = check_bounds(fix_(ymm / dy), Ny);
         weights((xmm - xvy[j]) / dx, (ymm - yvy[i]) / dy, w);
-        add_block(st->sy[SV_RHO], Ny1, i, j, rhomm, w);
-        add_block(st->sy[SV_ETAD], Ny1, i, j, 1. / etadm, w);
-        add_block(st->sy[SV_RHOF], Ny1, i, j, mk[HMEC_M_rhofm][m], w);
-        add_block(st->sy[SV_POR], Ny1, i, j, por, w);
-        add_wt(st->sy[SV_WT], Ny1, i, j, w);
+        add_block(s->sy[SV_RHO], Ny1, i, j, rhomm, w);
+        add_block(s->sy[SV_ETAD], Ny1, i, j, 1. / etadm, w);
+        add_block(s->sy[SV_RHOF], Ny1, i, j, mk[HMEC_M_rhofm][m], w);
+        add_block(s->sy[SV_POR], Ny1, i, j, por, w);
+        add_wt(s->sy[SV_WT], Ny1, i, j, w);
     }
+}
+
+/* The marker loop on several threads (the reference runs it as an OpenMP
+ * parallel loop, :384, whose threads add into shared sums without
+ * synchronisation).  Here thread t takes the t-th contiguous share of the
+ * markers into sums of its own (thread 0 into the state's), and the shares
+ * are then added in thread order, each thread over its own slice of the
+ * nodes: deterministic for a given thread count, equal to the serial loop
+ * up to the order of the additions. */
+typedef struct {
+    const hmo_state* st;
+    int64_t m0, m1;
+    hmo_sums s;
+    int t, T;
+    hmo_sums* all;
+    size_t nb, ns;
+} hmo_job;
+
+static void* accumulate_job(void* arg) {
+    hmo_job* j = (hmo_job*)arg;
+    accumulate_markers(j->st, j->m0, j->m1, &j->s);
+    return NULL;
+}
+
+static void add_slice(double* dst, double* const* src, int T, size_t n, int t) {
+    const size_t a = n * (size_t)t / (size_t)T, b = n * (size_t)(t + 1) / (size_t)T;
+    for (size_t k = a; k < b; k++) {
+        double v = dst[k];
+        for (int u = 1; u < T; u++) v += src[u][k];
+        dst[k] = v;
+    }
+}
+
+static void* reduce_job(void* arg) {
+    hmo_job* j = (hmo_job*)arg;
+    double* src[256];
+    for (int k = 0; k < SB_N; k++) {
+        for (int u = 1; u < j->T; u++) src[u] = j->all[u].sb[k];
+        add_slice(j->all[0].sb[k], src, j->T, j->nb, j->t);
+    }
+    for (int k = 0; k < SP_N; k++) {
+        for (int u = 1; u < j->T; u++) src[u] = j->all[u].sp[k];
+        add_slice(j->all[0].sp[k], src, j->T, j->ns, j->t);
+    }
+    for (int k = 0; k < SV_N; k++) {
+        for (int u = 1; u < j->T; u++) src[u] = j->all[u].sx[k];
+        add_slice(j->all[0].sx[k], src, j->T, j->ns, j->t);
+        for (int u = 1; u < j->T; u++) src[u] = j->all[u].sy[k];
+        add_slice(j->all[0].sy[k], src, j->T, j->ns, j->t);
+    }
+    return NULL;
+}
+
+/* Returns 0, or -1 when a buffer or a thread could not be had (the sums are
+ * then formed by the serial loop). */
+static int accumulate_threaded(hmo_state* st, int T, size_t nb, size_t ns) {
+    hmo_sums all[256];
+    hmo_job job[256];
+    pthread_t th[256];
+    int ok = 1, started = 0;
+    memset(all, 0, sizeof(all));
+    for (int k = 0; k < SB_N; k++) all[0].sb[k] = st->sb[k];
+    for (int k = 0; k < SP_N; k++) all[0].sp[k] = st->sp[k];
+    for (int k = 0; k < SV_N; k++) all[0].sx[k] = st->sx[k];
+    for (int k = 0; k < SV_N; k++) all[0].sy[k] = st->sy[k];
+    for (int u = 1; u < T && ok; u++) {
+        for (int k = 0; k < SB_N; k++) ok = ok && (all[u].sb[k] = (double*)calloc(nb, sizeof(double)));
+        for (int k = 0; k < SP_N; k++) ok = ok && (all[u].sp[k] = (double*)calloc(ns, sizeof(double)));
+        for (int k = 0; k < SV_N; k++) ok = ok && (all[u].sx[k] = (double*)calloc(ns, sizeof(double)));
+        for (int k = 0; k < SV_N; k++) ok = ok && (all[u].sy[k] = (double*)calloc(ns, sizeof(double)));
+    }
+    if (ok) {
+        for (int t = 0; t < T; t++) {
+            job[t].st = st;
+            job[t].m0 = st->marknum * t / T;
+            job[t].m1 = st->marknum * (t + 1) / T;
+            job[t].s = all[t];
+            job[t].t = t;
+            job[t].T = T;
+            job[t].all = all;
+            job[t].nb = nb;
+            job[t].ns = ns;
+        }
+        for (; started < T; started++)
+            if (pthread_create(&th[started], NULL, accumulate_job, &job[started]) != 0) break;
+        for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+        if (started < T) {
+            /* the shares of the threads that never started, on this thread */
+            for (int t = started; t < T; t++) accumulate_markers(st, job[t].m0, job[t].m1, &job[t].s);
+        }
+        started = 0;
+        for (; started < T; started++)
+            if (pthread_create(&th[started], NULL, reduce_job, &job[started]) != 0) break;
+        for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+        for (int t = started; t < T; t++) reduce_job(&job[t]);
+    }
+    for (int u = 1; u < T; u++) {
+        for (int k = 0; k < SB_N; k++) free(all[u].sb[k]);
+        for (int k = 0; k < SP_N; k++) free(all[u].sp[k]);
+        for (int k = 0; k < SV_N; k++) free(all[u].sx[k]);
+        for (int k = 0; k < SV_N; k++) free(all[u].sy[k]);
+    }
+    return ok ? 0 : -1;
+}
+
+void hmo_set_threads(hmo_state* st, int32_t n) { st->nthreads = n < 1 ? 1 : (n > 256 ? 256 : n); }
+
+void hmo_markers_to_nodes(hmo_state* st) {
+    const hmec_params* p = &st->p;
+    const int Nx = st->Nx, Ny = st->Ny, Ny1 = st->Ny1, Nx1 = st->Nx1;
+    size_t nb = (size_t)Nx * Ny, ns = (size_t)Nx1 * Ny1;
+    if (!p->quirk_accumulate_sums) { /* :377-381 as intended */
+        for (int k = 0; k < SB_N; k++) memset(st->sb[k], 0, nb * sizeof(double));
+        for (int k = 0; k < SP_N; k++) memset(st->sp[k], 0, ns * sizeof(double));
+        for (int k = 0; k < SV_N; k++) memset(st->sx[k], 0, ns * sizeof(double));
+        for (int k = 0; k < SV_N; k++) memset(st->sy[k], 0, ns * sizeof(double));
+    }
+    hmo_sums own;
+    for (int k = 0; k < SB_N; k++) own.sb[k] = st->sb[k];
+    for (int k = 0; k < SP_N; k++) own.sp[k] = st->sp[k];
+    for (int k = 0; k < SV_N; k++) own.sx[k] = st->sx[k];
+    for (int k = 0; k < SV_N; k++) own.sy[k] = st->sy[k];
+    const int T = st->marknum >= 2 * (int64_t)st->nthreads ? st->nthreads : 1;
+    if (T < 2 || accumulate_threaded(st, T, nb, ns) != 0) accumulate_markers(st, 0, st->marknum, &own);
     /* normalisation :531-583 */
     for (int i = 0; i < Ny; i++) {
         for (int j = 0; j < Nx; j++) {

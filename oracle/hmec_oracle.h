@@ -51,6 +51,11 @@ const double* hmo_coords(const hmo_state* st, int32_t which);
 
 /* Sections, in the order main() runs them. */
 void hmo_markers_to_nodes(hmo_state* st);                       /* :376-583 */
+/* Threads of the marker loop of hmo_markers_to_nodes (default 1, the serial
+ * loop in marker order).  n > 1: contiguous marker shares summed per thread
+ * and added in thread order -- the reference's OpenMP loop (:384) without
+ * its unsynchronised additions; equal to the serial loop up to rounding. */
+void hmo_set_threads(hmo_state* st, int32_t n);
 void hmo_timestep_begin(hmo_state* st);                         /* :585-608 */
 void hmo_iter_prepare(hmo_state* st);                           /* :611-677 */
 /* :682-1049 -- builds R and the CSR of L; returns nnz. */

@@ -86,7 +86,7 @@ def build(force: bool = False) -> str:
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
     tmp = LIB_PATH + ".%d.tmp" % os.getpid()
     cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
-           "-D_DEFAULT_SOURCE", "-o", tmp, src, "-lm"]
+           "-D_DEFAULT_SOURCE", "-pthread", "-o", tmp, src, "-lm"]
     subprocess.check_call(cmd)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
@@ -123,6 +123,8 @@ def lib():
                    "hmo_advect_markers"):
             getattr(L, fn).argtypes = [C.c_void_p]
             getattr(L, fn).restype = None
+        L.hmo_set_threads.argtypes = [C.c_void_p, C.c_int32]
+        L.hmo_set_threads.restype = None
         L.hmo_assemble.argtypes = [C.c_void_p]
         L.hmo_assemble.restype = C.c_int64
         L.hmo_csr.argtypes = [C.c_void_p, P(P(C.c_int64)), P(P(C.c_int32)), P(P(C.c_double)), P(P(C.c_double))]
@@ -269,6 +271,10 @@ class Oracle:
                 self.set_scalar(s, snap["scalar_" + s])
 
     # --------------------------------------------------------- sections
+    def set_threads(self, n: int):
+        """Threads of the marker loop (1, the default: the serial loop)."""
+        self.L.hmo_set_threads(self.h, int(n))
+
     def markers_to_nodes(self):
         self.L.hmo_markers_to_nodes(self.h)
 

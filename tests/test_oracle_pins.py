@@ -303,3 +303,43 @@ def test_timestep_sequence_starts_like_the_reference_control_logic():
     assert o.scalar("timestep") == 2
     it2 = o.timestep()
     assert o.scalar("timestep") == 3 and it2 >= 1
+
+
+P2G_FIELDS = ("RHO", "KKK", "TTT", "GGG", "ETA0", "COHT", "FRIT", "COHC", "FRIC", "DILC", "ETAP", "POR", "ETAB0",
+              "ETAP0", "GGGP", "RHOX", "ETADX", "RHOFX", "PORX", "RHOY", "ETADY", "RHOFY", "PORY")
+
+
+@pytest.mark.parametrize("threads", [2, 3, 8])
+def test_threaded_marker_loop_matches_the_serial_one(threads):
+    # the CPU baseline's marker loop on several threads: per-thread sums
+    # added in thread order -- deterministic, and equal to the serial loop
+    # up to the order of the additions
+    o, _, _ = fresh("c1")
+    o.markers_to_nodes()
+    ref = {f: o.field(f).copy() for f in P2G_FIELDS}
+    o.set_threads(threads)
+    o.markers_to_nodes()
+    one = {f: o.field(f).copy() for f in P2G_FIELDS}
+    o.markers_to_nodes()
+    for f in P2G_FIELDS:
+        assert np.array_equal(one[f], o.field(f)), f  # same thread count, same bits
+        scale = np.max(np.abs(ref[f]))
+        assert np.max(np.abs(one[f] - ref[f])) <= 1e-13 * scale, f
+    o.set_threads(1)
+    o.markers_to_nodes()
+    for f in P2G_FIELDS:
+        assert np.array_equal(o.field(f), ref[f]), f  # back to the serial loop
+
+
+def test_threaded_marker_loop_keeps_accumulated_sums():
+    # quirk Q1 (sums kept across steps): the threads add to what the sums
+    # already hold, as the serial loop does
+    o1, _, _ = fresh("c0", quirk_accumulate_sums=1)
+    o2, _, _ = fresh("c0", quirk_accumulate_sums=1)
+    o2.set_threads(4)
+    for _ in range(2):
+        o1.markers_to_nodes()
+        o2.markers_to_nodes()
+    for f in P2G_FIELDS:
+        a, b = o1.field(f), o2.field(f)
+        assert np.max(np.abs(a - b)) <= 1e-13 * np.max(np.abs(a)), f
