@@ -409,7 +409,10 @@ def run_gpu(args, cfg, world, device_index, peaks, with_fp64=True, with_e2e=True
         # (hmec_stream_markers; the next step uses them), so each timed step
         # still moves every marker array host -> device
         m.stream_markers(pin)
-        m.timestep()  # the first step after registering captures the step graph again
+        # after registering, the first step runs host-driven and the second
+        # captures the step graph again: both before the timed steps
+        m.timestep()
+        m.timestep()
         m.load_state(snap)
         for f, (flat, r, c) in host_state.items():
             flat[...] = m.field(f).ravel(order="F")

@@ -304,16 +304,17 @@ int32_t hmec_download_rows_async(hmec_ctx* ctx, int32_t inst, int32_t row, int32
                                  const int32_t* fields, double* out, int64_t* ticket);
 int32_t hmec_rows_wait(hmec_ctx* ctx, int32_t inst, int64_t ticket);
 /* Marker streaming: registers the host's marker arrays (page-locked, e.g.
- * from hmec_host_alloc; fields[HMEC_M_COUNT] of n doubles, the layout of
- * hmec_upload_markers) that every later timestep copies into the device --
- * and sorts into the half-cell storage order -- right after its
- * markers->nodes section, on a stream of its own, overlapped with the rest
- * of the step.  So step k+1 uses what the arrays held while step k ran (the
- * reference's P2G reads its host marker arrays every step, :384-528).  The
- * arrays must stay valid and must not be written while a timestep runs.
- * fields = NULL stops the streaming.  Refused with advect_markers (the
- * device then moves the markers itself).  The first step after a change
- * runs host-driven (the step's graph is captured again).                    */
+ * from hmec_host_alloc; fields[HMEC_M_COUNT], each n doubles long inside
+ * its page-locked allocation, the layout of hmec_upload_markers) that every
+ * later timestep copies into the device, in the caller's order, right after
+ * its markers->nodes section, on a stream of its own, overlapped with the
+ * rest of the step (the next step's sort orders them, as every step does).
+ * So step k+1 uses what the arrays held while step k ran (the reference's
+ * P2G reads its host marker arrays every step, :384-528).  The arrays must
+ * stay valid and must not be written while a timestep runs.  fields = NULL
+ * stops the streaming.  Refused with advect_markers (the device then moves
+ * the markers itself).  The first step after a change runs host-driven and
+ * the second captures the step's graph again.                               */
 int32_t hmec_stream_markers(hmec_ctx* ctx, int32_t inst, const double* const* fields, int64_t n);
 /* Page-locked host memory for hmec_download_rows_async (NULL on failure). */
 void* hmec_host_alloc(size_t bytes);
