@@ -912,8 +912,15 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
         prolong_add(g, t.gc, t.pmx, t.pmy, t.xc, t.x, tid, nth);
         cg::this_grid().sync();
     }
+    // this block's tiles: blockIdx.x + k * gridDim.x.  Odd sweeps visit them
+    // in reverse, so the tile a sweep ends on starts the next one and stays
+    // staged; the order within a sweep changes nothing, as a sweep's tiles
+    // read only the previous sweep's values
+    const int ntb = (int)blockIdx.x < t.ntiles ? (t.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     for (int so = 0; so < outer; so++) {
-        for (int tile = blockIdx.x; tile < t.ntiles; tile += gridDim.x) {
+        const bool rev = (so & 1) != 0;
+        for (int kt = 0; kt < ntb; kt++) {
+            const int tile = (int)blockIdx.x + (rev ? ntb - 1 - kt : kt) * (int)gridDim.x;
             const int ti = tile % t.ntile_i, tj = tile / t.ntile_i;
             const int i0 = 1 + ti * TILE, j0 = 1 + tj * TILE;
             const int i1 = min(i0 + TILE, g.Ny), j1 = min(j0 + TILE, g.Nx);  // exclusive
@@ -935,11 +942,11 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                     if (stage_pack<T>() && nbt > 0)
                         bulk_g2s(smem_raw + Lo.pack, t.bpack + (size_t)tile * pack_bytes<T>(TBC), pack_bytes<T>(TBC),
                                  &bar[2]);
-                    // the tile this block stages next (this sweep's next, or
-                    // the next sweep's first when it is another tile): into L2
-                    int nx = tile + gridDim.x;
-                    if (nx >= t.ntiles) nx = so + 1 < outer ? (int)blockIdx.x : -1;
-                    if (nx >= 0 && nx != tile) {
+                    // the tile this block stages next in this sweep, into L2
+                    // (the next sweep starts on this one)
+                    const int nx =
+                        kt + 1 < ntb ? (int)blockIdx.x + (rev ? ntb - 2 - kt : kt + 1) * (int)gridDim.x : -1;
+                    if (nx >= 0) {
                         const int ni0 = 1 + (nx % t.ntile_i) * TILE, nj0 = 1 + (nx / t.ntile_i) * TILE;
                         tma_prefetch_3d(&t.tm_val, (ni0 - 1) * 6, nj0 - 1, 0);
                         if (whole) tma_prefetch_3d(&t.tm_pinv, 0, ni0 - 1, nj0 - 1);
