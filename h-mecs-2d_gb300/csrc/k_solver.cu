@@ -855,8 +855,9 @@ __device__ __forceinline__ void stage_bars_init(unsigned long long* bar) {
 // restriction), run by every block of the launch.  t lives in kernel
 // parameter space or in global memory (its tensor maps are read from where
 // it lives).  Lo: the launch's shared-memory layout, sized for at least this
-// level's boundary-row capacity.  WHOLE: the inverse mode.
-template <typename T, bool WHOLE>
+// level's boundary-row capacity.  WHOLE: the inverse mode.  REV: odd
+// sweeps visit the block's tiles in reverse (the fused V-cycle).
+template <typename T, bool WHOLE, bool REV>
 __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, int mode, unsigned char* smem_raw,
                                            const StageLayout& Lo, StageBars& sb_) {
     T* xs = reinterpret_cast<T*>(smem_raw + Lo.xs);
@@ -912,13 +913,13 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
         prolong_add(g, t.gc, t.pmx, t.pmy, t.xc, t.x, tid, nth);
         cg::this_grid().sync();
     }
-    // this block's tiles: blockIdx.x + k * gridDim.x.  Odd sweeps visit them
-    // in reverse, so the tile a sweep ends on starts the next one and stays
-    // staged; the order within a sweep changes nothing, as a sweep's tiles
-    // read only the previous sweep's values
+    // this block's tiles: blockIdx.x + k * gridDim.x.  With REV odd sweeps
+    // visit them in reverse, so the tile a sweep ends on starts the next one
+    // and stays staged; the order within a sweep changes nothing, as a
+    // sweep's tiles read only the previous sweep's values
     const int ntb = (int)blockIdx.x < t.ntiles ? (t.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     for (int so = 0; so < outer; so++) {
-        const bool rev = (so & 1) != 0;
+        const bool rev = REV && (so & 1) != 0;
         for (int kt = 0; kt < ntb; kt++) {
             const int tile = (int)blockIdx.x + (rev ? ntb - 1 - kt : kt) * (int)gridDim.x;
             const int ti = tile % t.ntile_i, tj = tile / t.ntile_i;
@@ -942,11 +943,16 @@ __device__ __forceinline__ void stage_pass(const StageArgs<T>& t, int nsweeps, i
                     if (stage_pack<T>() && nbt > 0)
                         bulk_g2s(smem_raw + Lo.pack, t.bpack + (size_t)tile * pack_bytes<T>(TBC), pack_bytes<T>(TBC),
                                  &bar[2]);
-                    // the tile this block stages next in this sweep, into L2
-                    // (the next sweep starts on this one)
-                    const int nx =
-                        kt + 1 < ntb ? (int)blockIdx.x + (rev ? ntb - 2 - kt : kt + 1) * (int)gridDim.x : -1;
-                    if (nx >= 0) {
+                    // the tile this block stages next into L2: this sweep's
+                    // next, or, in forward order, the next sweep's first when
+                    // it is another tile (in reverse the next sweep starts on
+                    // this one)
+                    int nx;
+                    if (REV)
+                        nx = kt + 1 < ntb ? (int)blockIdx.x + (rev ? ntb - 2 - kt : kt + 1) * (int)gridDim.x : -1;
+                    else
+                        nx = kt + 1 < ntb ? tile + (int)gridDim.x : (so + 1 < outer ? (int)blockIdx.x : -1);
+                    if (nx >= 0 && nx != tile) {
                         const int ni0 = 1 + (nx % t.ntile_i) * TILE, nj0 = 1 + (nx / t.ntile_i) * TILE;
                         tma_prefetch_3d(&t.tm_val, (ni0 - 1) * 6, nj0 - 1, 0);
                         if (whole) tma_prefetch_3d(&t.tm_pinv, 0, ni0 - 1, nj0 - 1);
@@ -1135,7 +1141,7 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_smooth_stage(const __grid_consta
     const StageLayout Lo = stage_layout<T>(WHOLE ? 1 : 0, t.tb_cap);
     StageBars sb{reinterpret_cast<unsigned long long*>(smem_raw + Lo.bar), 0, 0, 0};
     stage_bars_init(sb.bar);
-    stage_pass<T, WHOLE>(t, nsweeps, mode, smem_raw, Lo, sb);
+    stage_pass<T, WHOLE, false>(t, nsweeps, mode, smem_raw, Lo, sb);
 }
 
 // A whole V-cycle's smoothing passes in one cooperative launch: pass p of
@@ -1167,7 +1173,7 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_vcycle_stage(const __grid_consta
     stage_bars_init(sb.bar);
     for (int p = 0; p < v.npass; p++) {
         if (p > 0) cg::this_grid().sync();
-        stage_pass<T, WHOLE>(v.p[p].a, v.p[p].nsweeps, v.p[p].mode, smem_raw, Lo, sb);
+        stage_pass<T, WHOLE, true>(v.p[p].a, v.p[p].nsweeps, v.p[p].mode, smem_raw, Lo, sb);
     }
 }
 
