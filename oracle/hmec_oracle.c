@@ -458,11 +458,16 @@ static void* reduce_job(void* arg) {
 /* Returns 0, or -1 when a buffer or a thread could not be had (the sums are
  * then formed by the serial loop). */
 static int accumulate_threaded(hmo_state* st, int T, size_t nb, size_t ns) {
-    hmo_sums all[256];
-    hmo_job job[256];
-    pthread_t th[256];
-    int ok = 1, started = 0;
-    memset(all, 0, sizeof(all));
+    hmo_sums* all = (hmo_sums*)calloc((size_t)T, sizeof(hmo_sums));
+    hmo_job* job = (hmo_job*)calloc((size_t)T, sizeof(hmo_job));
+    pthread_t* th = (pthread_t*)calloc((size_t)T, sizeof(pthread_t));
+    int ok = all && job && th, started = 0;
+    if (!ok) {
+        free(all);
+        free(job);
+        free(th);
+        return -1;
+    }
     for (int k = 0; k < SB_N; k++) all[0].sb[k] = st->sb[k];
     for (int k = 0; k < SP_N; k++) all[0].sp[k] = st->sp[k];
     for (int k = 0; k < SV_N; k++) all[0].sx[k] = st->sx[k];
@@ -504,6 +509,9 @@ static int accumulate_threaded(hmo_state* st, int T, size_t nb, size_t ns) {
         for (int k = 0; k < SV_N; k++) free(all[u].sx[k]);
         for (int k = 0; k < SV_N; k++) free(all[u].sy[k]);
     }
+    free(all);
+    free(job);
+    free(th);
     return ok ? 0 : -1;
 }
 
