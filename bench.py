@@ -250,12 +250,12 @@ def rel_errors(got, ref):
     return out
 
 
-def judged(err):
-    """The errors the target is judged on: velocity as one vector field (vys
+def against_target(err):
+    """The errors the accuracy target is checked on: velocity as one vector field (vys
     alone is near zero in simple shear), pt, pf and the slip rate."""
     keys = ("velocity", "pt", "pf", "VSLIPB")
     worst = max(err[k] for k in keys if k in err)
-    return {"judged_on": list(keys), "max": worst, "target": TARGET_REL_ERR, "met": worst <= TARGET_REL_ERR}
+    return {"checked_on": list(keys), "max": worst, "target": TARGET_REL_ERR, "met": worst <= TARGET_REL_ERR}
 
 
 # -------------------------------------------------------------------- GPU arm
@@ -553,7 +553,7 @@ def member_oracle_error(over, mat, seed, fields_after_step1):
         o.set_field(k, v)
     gi = o.timestep()
     err = rel_errors(fields_after_step1, {k: o.field(k) for k in FIELDS_ACC})
-    return dict(err, **judged(err), Nx=over["Nx"], Ny=over["Ny"], prestress_pa=mat.get("prestress", 0.0),
+    return dict(err, **against_target(err), Nx=over["Nx"], Ny=over["Ny"], prestress_pa=mat.get("prestress", 0.0),
                 oracle_global_iters=gi, oracle_dt=o.scalar("dt"))
 
 
@@ -725,7 +725,7 @@ def model_block(args, cfg, world, res, peaks):
         blk["fp64_form"] = {"value": world * K / (f["ms"] / 1e3), "ms_per_step": f["ms"] / K,
                             "global_iters_per_step": f["gi"] / K, "krylov_iters_per_step": f["kr"] / K}
         if "err" in f:
-            blk["mixed_vs_fp64_form_rel_err"] = dict(f["err"], same_dt=f["same_dt"], **judged(f["err"]))
+            blk["mixed_vs_fp64_form_rel_err"] = dict(f["err"], same_dt=f["same_dt"], **against_target(f["err"]))
             blk["mixed_vs_fp64_form_rel_err"]["note"] = ("one timestep from the same state in both forms, "
                                                          "max |mixed - fp64| / max |fp64| per field; 'velocity' "
                                                          "over vxs and vys together")
@@ -780,7 +780,7 @@ def accuracy_vs_oracle(cfg, nsteps=3):
             m.timestep()
         free = rel_errors({k: m.field(k) for k in FIELDS_ACC}, ref)
         m.close()
-        out[label] = dict(err, **judged(err))
+        out[label] = dict(err, **against_target(err))
         out[label]["free_running"] = free
     # the oracle's own floor: the replayed step solved again with another
     # partial-pivoting threshold (the same system, other rounding)
@@ -790,7 +790,7 @@ def accuracy_vs_oracle(cfg, nsteps=3):
     o2.load_state(snap)
     o2.timestep()
     fl = rel_errors({k: o2.field(k) for k in FIELDS_ACC}, ref)
-    out["oracle_floor"] = dict(fl, **judged(fl))
+    out["oracle_floor"] = dict(fl, **against_target(fl))
     out["oracle_floor"]["note"] = ("the oracle against itself: step %d re-solved with partial-pivoting threshold "
                                    "0.1 instead of 1.0; near yield the plastic iterations amplify last-bit "
                                    "differences of the solve by up to ~1e7" % nsteps)

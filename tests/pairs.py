@@ -62,7 +62,7 @@ def field_errors(m, o, names):
 
 # Error groups: a vector field is compared as a whole (its components relative
 # to the largest component), so a component that is zero by symmetry (vys in
-# simple shear) is not judged against its own round-off.
+# simple shear) is not held against its own round-off.
 GROUPS = {
     "velocity": ["vxs", "vys"],
     "darcy": ["vxD", "vyD"],
