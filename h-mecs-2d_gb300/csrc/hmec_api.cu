@@ -376,10 +376,14 @@ static int32_t inst_stream_markers(hmec_inst* ctx, const double* const* fields, 
             return fail(ctx, HMEC_ERR_STATE, "marker streaming replaces the markers the advection moves");
         for (int k = 0; k < HMEC_M_COUNT; k++) {
             if (!fields[k]) return fail(ctx, HMEC_ERR_ARG, "null marker array");
-            cudaPointerAttributes at;
-            if (cudaPointerGetAttributes(&at, fields[k]) != cudaSuccess || at.type != cudaMemoryTypeHost) {
-                cudaGetLastError();
-                return fail(ctx, HMEC_ERR_ARG, "streamed marker arrays must be page-locked (hmec_host_alloc)");
+            // the first and the last element in page-locked memory (the
+            // copies run while the caller's thread goes on)
+            for (const double* q : {fields[k], fields[k] + (n - 1)}) {
+                cudaPointerAttributes at;
+                if (cudaPointerGetAttributes(&at, q) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+                    cudaGetLastError();
+                    return fail(ctx, HMEC_ERR_ARG, "streamed marker arrays must be page-locked (hmec_host_alloc)");
+                }
             }
         }
         for (int k = 0; k < HMEC_M_COUNT; k++) ctx->src_mk[k] = fields[k];
