@@ -23,6 +23,7 @@
 //     normalises in the epilogue (a4).  No float atomics.
 #include "hmec_dfexp.cuh"
 #include "hmec_internal.cuh"
+#include "hmec_mprop.cuh"
 #include "hmec_sort.cuh"
 
 namespace {
@@ -55,33 +56,6 @@ enum {
 // FP64<->FP32 conversions run at the FP64 rate, so FP64 values are split by
 // their bit patterns.  Relative error of a sum of same-sign terms ~1e-14.
 
-// x = h + l: h keeps the top 24 bits of the mantissa (truncated), l is the
-// remaining 29 bits rounded to FP32 (|x - h - l| < 2^-47 |x|).  Zeros and
-// FP64 subnormals give 0; |x| outside [2^-74, 2^127) (and inf/NaN) take the
-// FP64 conversions.
-__device__ __forceinline__ void split_df(double x, float& h, float& l) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
-    const int E = (int)((hi32 >> 20) & 0x7FF);
-    const unsigned sign = hi32 & 0x80000000u;
-    if (E >= 949 && E <= 1150) {
-        h = __uint_as_float(sign | ((unsigned)(E - 896) << 23) | ((hi32 & 0xFFFFFu) << 3) | (lo32 >> 29));
-        // the 29 remaining bits R as FP32: 2^23 + v has v in its mantissa for
-        // v < 2^23, so R = 64 (R >> 6) + (R & 63) converts exactly, one rounding
-        const unsigned R = lo32 & 0x1FFFFFFFu;
-        const float rh = __fsub_rn(__uint_as_float(0x4B000000u | (R >> 6)), 8388608.f);
-        const float rl = __fsub_rn(__uint_as_float(0x4B000000u | (R & 63u)), 8388608.f);
-        const float r = __fmul_rn(fmaf(rh, 64.f, rl), __uint_as_float((unsigned)(E - 948) << 23));
-        l = sign ? -r : r;
-    } else if (E == 0) {
-        h = 0.f;
-        l = 0.f;
-    } else {
-        h = __double2float_rn(x);
-        l = __double2float_rn(x - (double)h);
-    }
-}
-
 // (sh, sl) += t + e, with t + e already a double-float (|e| <= ulp(t)).
 __device__ __forceinline__ void df_acc(float& sh, float& sl, float t, float e) {
     const float s = __fadd_rn(sh, t);
@@ -89,21 +63,6 @@ __device__ __forceinline__ void df_acc(float& sh, float& sl, float t, float e) {
     const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(t, bb));
     sh = s;
     sl = __fadd_rn(sl, __fadd_rn(err, e));
-}
-
-// (ah + al)(bh + bl) as t + e (al * bl dropped, < 2^-48 relative).
-__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& t, float& e) {
-    t = __fmul_rn(ah, bh);
-    e = fmaf(ah, bh, -t);
-    e = fmaf(ah, bl, e);
-    e = fmaf(al, bh, e);
-}
-
-// normalised double-float a + b (|a| >= |b|)
-__device__ __forceinline__ void df_norm(float& a, float& b) {
-    const float s = __fadd_rn(a, b);
-    b = __fsub_rn(b, __fsub_rn(s, a));
-    a = s;
 }
 
 // h + l = 1 / a: the FP32 reciprocal refined by one Newton-Raphson step
@@ -124,15 +83,6 @@ __device__ __forceinline__ bool df_rcp(double a, float& h, float& l) {
     l = fmaf(ru, u, ru);  // r (u + u^2)
     df_norm(h, l);
     return true;
-}
-
-// v < lo ? lo : (v > hi ? hi : v).  Non-negative finite doubles order like
-// their bit patterns, so for those the compares run on the integer pipe.
-__device__ __forceinline__ double enforce_bounds(double v, double lo, double hi) {
-    const long long b = __double_as_longlong(v), bl = __double_as_longlong(lo), bh = __double_as_longlong(hi);
-    constexpr long long INF = 0x7FF0000000000000LL;
-    if (b >= 0 && b < INF && bl >= 0 && bl < INF && bh >= 0 && bh < INF) return b < bl ? lo : (b > bh ? hi : v);
-    return v < lo ? lo : (v > hi ? hi : v);
 }
 
 // a1 per marker (:389-423) in sorted order, plus interpolation distances.
@@ -156,47 +106,7 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int m = perm[k];
-    const double por = mk.porm[m];
-    const double pr = por * ipor0;  // por / POR0 to an ulp
-    double kkkmm = mk.kkkm[m] * (pr * pr * pr);
-    kkkmm = enforce_bounds(kkkmm, p.kkkmin, p.kkkmax);
-    double cohescmm, cohestmm, frictcmm, dilatcmm, fricttmm, etasmm0, etamm0, etamm, rhomm;
-    const double tm = mk.t_marker[m];
-    if ((__double_as_longlong(tm) << 1) != 0) {  // tm != 0 (either zero fails, NaN passes)
-        cohescmm = mk.cohescm[m] * (1 - por);
-        cohestmm = mk.cohestm[m] * (1 - por);
-        frictcmm = mk.frictcm[m];
-        dilatcmm = mk.dilatcm[m];
-        fricttmm = mk.fricttm[m];
-        etasmm0 = mk.etasm[m];
-        // etas exp(-alpha por): the exponential in double-float (two FP64
-        // operations of range reduction instead of the FP64 exp's ~20)
-        const double xe = -p.alpha * por;
-        float eh, el;
-        if (df_exp(xe, eh, el)) {
-            float sh, sl, t, e;
-            split_df(etasmm0, sh, sl);
-            df_mul(sh, sl, eh, el, t, e);
-            df_norm(t, e);
-            etamm0 = f2d_bits(t) + f2d_bits(e);
-        } else {
-            etamm0 = etasmm0 * exp(xe);
-        }
-        etamm = mk.etam[m];
-        rhomm = mk.rhom[m] * (1 - por) + mk.rhofm[m] * por;
-    } else {
-        cohescmm = mk.cohescm[m];
-        cohestmm = mk.cohestm[m];
-        frictcmm = mk.frictcm[m];
-        dilatcmm = 0;
-        fricttmm = mk.fricttm[m];
-        etasmm0 = mk.etasm[m];
-        etamm0 = mk.etasm[m];
-        etamm = mk.etam[m];
-        rhomm = mk.rhom[m];
-    }
-    etamm0 = enforce_bounds(etamm0, p.etamin, p.etamax);
-    etamm = enforce_bounds(etamm, p.etamin, p.etamax);
+    const MarkerProps q = marker_props(mk, m, p, ipor0);
     const double xmm = mk.xm[m], ymm = mk.ym[m];
     // half cell (hr, hc) = (2 ib + (iP - ib), 2 jb + (jP - jb)), key = hc * HR + hr
     const int HR = 2 * (g.Ny - 1), kk = key[m];
@@ -231,9 +141,9 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
     put_dist(MP_DYY, ymm - c.yvy[ib], iyh, iyl);
     put_dist(MP_DXP, xmm - c.xp[jP], ixh, ixl);
     put_dist(MP_DYP, ymm - c.yp[iP], iyh, iyl);
-    put(MP_RHO, rhomm);
-    put(MP_KKK, kkkmm);
-    put(MP_TTT, tm);
+    put(MP_RHO, q.rho);
+    put(MP_KKK, q.kkk);
+    put(MP_TTT, q.tm);
     {
         float h, l;
         if (df_rcp(mk.gm[m], h, l))
@@ -241,25 +151,25 @@ __global__ void k_mprop(MkPtrs mk, const int32_t* __restrict__ perm, const int32
         else
             put(MP_INVG, 1. / mk.gm[m]);
     }
-    put(MP_ETA0, etamm0);
-    put(MP_COHT, cohestmm);
-    put(MP_FRIT, fricttmm);
-    put(MP_COHC, cohescmm);
-    put(MP_FRIC, frictcmm);
-    put(MP_DILC, dilatcmm);
-    put(MP_ETAP, etamm);
-    put(MP_POR, por);
-    put(MP_ETAB0, etasmm0);
+    put(MP_ETA0, q.eta0);
+    put(MP_COHT, q.coht);
+    put(MP_FRIT, q.frit);
+    put(MP_COHC, q.cohc);
+    put(MP_FRIC, q.fric);
+    put(MP_DILC, q.dilc);
+    put(MP_ETAP, q.eta);
+    put(MP_POR, q.por);
+    put(MP_ETAB0, q.etas);
     {
         // k / etaf as k * (1 / etaf) in double-float
         float rh, rl, kh, kl, t, e;
         if (df_rcp(mk.etafm[m], rh, rl)) {
-            split_df(kkkmm, kh, kl);
+            split_df(q.kkk, kh, kl);
             df_mul(kh, kl, rh, rl, t, e);
             df_norm(t, e);
             put_df(MP_INVETAD, t, e);
         } else {
-            put(MP_INVETAD, kkkmm / mk.etafm[m]);
+            put(MP_INVETAD, q.kkk / mk.etafm[m]);
         }
     }
     put(MP_RHOF, mk.rhofm[m]);

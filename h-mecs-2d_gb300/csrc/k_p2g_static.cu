@@ -28,6 +28,7 @@
 #include <mutex>
 
 #include "hmec_internal.cuh"
+#include "hmec_mprop.cuh"
 #include "hmec_sort.cuh"
 
 #define HMEC_NOALLOC_MAX_MARKERS (1 << 20)
@@ -68,42 +69,29 @@ struct Mk {
         *porm, *kkkm, *gm, *rhofm, *etafm;
 };
 
-// Marker properties of :389-423.
+// Marker properties of :389-423 (the FP64 values of hmec_mprop.cuh, as the
+// context path forms them, plus the two reciprocals in FP64).
 struct Props {
     double rho, kkk, ttt, invg, eta0, coht, frit, cohc, fric, dilc, etap, por, etab0, invetad, rhof;
 };
 
-__device__ __forceinline__ double clampd(double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); }
-
-__device__ __forceinline__ Props props_of(const Mk& mk, int m, const hmec_params& p) {
+__device__ __forceinline__ Props props_of(const Mk& mk, int m, const hmec_params& p, double ipor0) {
+    const MarkerProps mp = marker_props(mk, m, p, ipor0);
     Props q;
-    const double por = mk.porm[m];
-    const double kkkmm = clampd(mk.kkkm[m] * pow(por / p.POR0, 3.0), p.kkkmin, p.kkkmax);
-    const double tm = mk.t_marker[m];
-    double etamm0;
-    if (tm != 0) {
-        q.cohc = mk.cohescm[m] * (1 - por);
-        q.coht = mk.cohestm[m] * (1 - por);
-        q.dilc = mk.dilatcm[m];
-        etamm0 = mk.etasm[m] * exp(-p.alpha * por);
-        q.rho = mk.rhom[m] * (1 - por) + mk.rhofm[m] * por;
-    } else {
-        q.cohc = mk.cohescm[m];
-        q.coht = mk.cohestm[m];
-        q.dilc = 0;
-        etamm0 = mk.etasm[m];
-        q.rho = mk.rhom[m];
-    }
-    q.fric = mk.frictcm[m];
-    q.frit = mk.fricttm[m];
-    q.eta0 = clampd(etamm0, p.etamin, p.etamax);
-    q.etap = clampd(mk.etam[m], p.etamin, p.etamax);
-    q.etab0 = mk.etasm[m];
-    q.kkk = kkkmm;
-    q.ttt = tm;
+    q.rho = mp.rho;
+    q.kkk = mp.kkk;
+    q.ttt = mp.tm;
     q.invg = 1. / mk.gm[m];
-    q.por = por;
-    q.invetad = 1. / (mk.etafm[m] / kkkmm);
+    q.eta0 = mp.eta0;
+    q.coht = mp.coht;
+    q.frit = mp.frit;
+    q.cohc = mp.cohc;
+    q.fric = mp.fric;
+    q.dilc = mp.dilc;
+    q.etap = mp.eta;
+    q.por = mp.por;
+    q.etab0 = mp.etas;
+    q.invetad = 1. / (mk.etafm[m] / mp.kkk);
     q.rhof = mk.rhofm[m];
     return q;
 }
@@ -128,6 +116,7 @@ __global__ void k_nz_gather(Mk mk, hmec_params p, Geo g, const int32_t* __restri
     const int ncol = (GRID == 0 || GRID == 2) ? g.Nx : g.Nx1;
     if (i >= nrow || j >= ncol) return;
     const int HR = 2 * (g.Ny - 1), HC = 2 * (g.Nx - 1);
+    const double ipor0 = 1.0 / p.POR0;
     const int r0 = ROWP ? 2 * i - 3 : 2 * i - 2, c0 = COLP ? 2 * j - 3 : 2 * j - 2;
     const int rlo = r0 < 0 ? 0 : r0, rhi = (r0 + 3) > HR - 1 ? HR - 1 : r0 + 3;
     double wt = 0, a[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -159,7 +148,7 @@ __global__ void k_nz_gather(Mk mk, hmec_params p, Geo g, const int32_t* __restri
                 const double fx = (cj == j) ? (1 - dxm) : dxm;
                 const double fy = (k >= bsplit) ? (1 - dym) : dym;
                 const double w = fx * fy;
-                const Props q = props_of(mk, m, p);
+                const Props q = props_of(mk, m, p, ipor0);
                 wt += w;
                 if (GRID == 0) {
                     a[0] += q.rho * w;

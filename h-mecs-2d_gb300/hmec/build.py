@@ -44,7 +44,8 @@ def _stale(target, deps):
 def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     headers = [os.path.join(SRC, "hmec_internal.cuh"), os.path.join(SRC, "hmec_sort.cuh"),
-               os.path.join(SRC, "hmec_bits.cuh"), os.path.join(SRC, "hmec_dfexp.cuh"), os.path.join(INC, "hmec.h")]
+               os.path.join(SRC, "hmec_bits.cuh"), os.path.join(SRC, "hmec_dfexp.cuh"),
+               os.path.join(SRC, "hmec_mprop.cuh"), os.path.join(INC, "hmec.h")]
     objs = []
     jobs = []
     for u in UNITS:
