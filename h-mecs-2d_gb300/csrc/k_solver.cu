@@ -65,7 +65,7 @@ __device__ __forceinline__ int patch_unknown(int i, int j, int Ny1, int q) {
 // pinv[p*100 + r*10 + c].  Half a warp per patch, lane r holding row r of
 // [A | I] in registers.  Pivoting is implicit: column c's pivot is the
 // largest |a| among the lanes not yet used as pivots, its normalised row is
-// broadcast by shuffles and eliminated from the other lanes; at the end the
+// broadcast through shared memory and eliminated from the other lanes; at the end the
 // pivot lane of column c holds row c of the inverse.
 constexpr int VS_BS = 128;
 template <typename T>
@@ -103,7 +103,11 @@ __global__ void __launch_bounds__(VS_BS) k_vanka_setup(Geo g, const int32_t* __r
     bool used = q >= PB;
     bool singular = false;
     int my_row = 0;
-    const int base = lane & 16;
+    // the pivot row of this half-warp's patch, written by the pivot lane and
+    // read by the others: a[c+1..PB-1] at [k], b at [PB + k] (vector loads
+    // instead of one shuffle per value)
+    __shared__ __align__(16) T srow[VS_BS / 16][2 * PB];
+    T* const prow = srow[threadIdx.x >> 4];
 #pragma unroll
     for (int c = 0; c < PB; c++) {
         T best = used ? (T)-1 : (T)fabs(a[c]);
@@ -126,20 +130,21 @@ __global__ void __launch_bounds__(VS_BS) k_vanka_setup(Geo g, const int32_t* __r
             for (int k = 0; k < PB; k++) b[k] *= inv;
             used = true;
             my_row = c;
+#pragma unroll
+            for (int k = c + 1; k < PB; k++) prow[k] = a[k];
+#pragma unroll
+            for (int k = 0; k < PB; k++) prow[PB + k] = b[k];
         }
-        T pa[PB], pb[PB];
-#pragma unroll
-        for (int k = c + 1; k < PB; k++) pa[k] = __shfl_sync(0xffffffffu, a[k], base | bl);
-#pragma unroll
-        for (int k = 0; k < PB; k++) pb[k] = __shfl_sync(0xffffffffu, b[k], base | bl);
+        __syncwarp();
         if (q != bl) {
             const T f = a[c];
 #pragma unroll
-            for (int k = c + 1; k < PB; k++) a[k] -= f * pa[k];
+            for (int k = c + 1; k < PB; k++) a[k] -= f * prow[k];
             a[c] = 0;
 #pragma unroll
-            for (int k = 0; k < PB; k++) b[k] -= f * pb[k];
+            for (int k = 0; k < PB; k++) b[k] -= f * prow[PB + k];
         }
+        __syncwarp();  // the row is read before the next pivot writes it
     }
     if (!live || q >= PB) return;
     if (singular) {
